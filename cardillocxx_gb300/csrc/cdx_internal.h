@@ -1,0 +1,189 @@
+// Internal definitions shared by the host engine and the kernels (not part of the C ABI).
+//
+// Device layout (HBM, structure of arrays):
+//   bodies   field-major FP64 arrays of length N (positions, quaternions, velocities, rotation
+//            matrix R[9], radius, mass, inertia, friction, restitution, 1/m, 1/I, M_ii),
+//   statics  field-major arrays of length S (halfspaces and drums),
+//   contacts field-major arrays of length `cap` in canonical order (entity id A, entity id B):
+//            direction rows n,t1,t2 (9), body-frame lever products r x d for side A and B (9+9),
+//            RW coefficients R_r * w (9+9+9), contact velocity bias (3), R-scaled bias (3),
+//            impulses (3), impulse increments (3), friction, restitution, flags,
+//   incidence body -> (contact, side) lists in solver row order (a sorted CSR of W^T), which turns
+//            the W^T scatter into a deterministic per-body gather.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace cdx {
+
+enum BodyField {
+    BF_PX, BF_PY, BF_PZ,
+    BF_QX, BF_QY, BF_QZ, BF_QW,
+    BF_VX, BF_VY, BF_VZ,
+    BF_WX, BF_WY, BF_WZ,
+    BF_R0, BF_R1, BF_R2, BF_R3, BF_R4, BF_R5, BF_R6, BF_R7, BF_R8,
+    BF_RAD, BF_MASS, BF_INERTIA, BF_MU, BF_RN, BF_RT,
+    BF_MINVL, BF_MINVA, BF_ML, BF_MA,
+    BF_COUNT
+};
+
+enum StaticField {
+    SF_PX, SF_PY, SF_PZ,
+    SF_QX, SF_QY, SF_QZ, SF_QW,
+    SF_VX, SF_VY, SF_VZ,
+    SF_WX, SF_WY, SF_WZ,
+    SF_DX, SF_DY, SF_DZ,
+    SF_D, SF_RAD, SF_MU, SF_RN, SF_RT,
+    SF_R0, SF_R1, SF_R2, SF_R3, SF_R4, SF_R5, SF_R6, SF_R7, SF_R8,
+    SF_COUNT
+};
+
+// contact flags
+enum : int32_t { CF_FRICTIONAL = 1 };
+
+struct Scene {
+    int N = 0;          // dynamic spheres
+    int S = 0;          // static shapes
+    int nscenes = 1;
+    int max_statics = 0;  // max statics of any scene
+    double* B = nullptr;  // BF_COUNT * N
+    int32_t* body_scene = nullptr;
+    double* St = nullptr;  // SF_COUNT * S
+    int32_t* static_kind = nullptr;
+    int32_t* static_scene = nullptr;
+    int32_t* scene_body_start = nullptr;    // nscenes + 1
+    int32_t* scene_static_start = nullptr;  // nscenes + 1
+    __host__ __device__ double* bf(int f) const { return B + (size_t)f * N; }
+    __host__ __device__ double* sf(int f) const { return St + (size_t)f * S; }
+};
+
+struct Grid {
+    double lo[3];
+    double cell;
+    int dim[3];
+    int64_t ncells;
+    int key_bits;
+};
+
+// Per-step contact storage (one generation). Keys, points and impulses are double-buffered
+// across steps for the warm start; everything else is rebuilt every step.
+struct Contacts {
+    int64_t cap = 0;
+    int32_t* a = nullptr;  // body index of side A (>= 0) or -(static index) - 1
+    int32_t* b = nullptr;  // body index of side B
+    int32_t* flags = nullptr;
+    int32_t* rank = nullptr;  // position in solver row order (frictionless first)
+    double* dir = nullptr;    // 9*cap: n, t1, t2 (world)
+    double* cA = nullptr;     // 9*cap
+    double* cB = nullptr;     // 9*cap
+    double* rd = nullptr;     // 9*cap: R_r * d_r
+    double* rcA = nullptr;    // 9*cap
+    double* rcB = nullptr;    // 9*cap
+    double* cb = nullptr;     // 3*cap
+    double* biasR = nullptr;  // 3*cap
+    double* dlam = nullptr;   // 3*cap
+    double* mu = nullptr;
+    double* eN = nullptr;
+    double* eT = nullptr;
+    // double-buffered generation data
+    unsigned long long* key[2] = {nullptr, nullptr};
+    double* point[2] = {nullptr, nullptr};  // 3*cap
+    double* lam[2] = {nullptr, nullptr};    // 3*cap
+};
+
+// FP32 contact record of the split form (matrix-free rows rebuilt from the normal and lever lengths)
+struct ContactsF {
+    int64_t cap = 0;
+    float* n = nullptr;      // 3*cap normal (A -> B)
+    float* lev = nullptr;    // 2*cap signed lever lengths along n (side A, side B)
+    float* R = nullptr;      // 2*cap: R_n, R_t
+    float* bias = nullptr;   // 3*cap R-scaled bias
+    float* lam = nullptr;    // 3*cap
+    float* mu = nullptr;
+    int32_t* a = nullptr;
+    int32_t* b = nullptr;
+};
+
+struct DevScalars {
+    int32_t n_static;        // static contacts this step
+    int32_t n_pair;          // pair contacts this step
+    int32_t overflow;        // per-sphere candidate buffer overflow
+    int32_t nonfinite;
+    unsigned long long maxd;  // bits of max ||dlambda_c|| (non-negative doubles order as integers)
+    unsigned long long maxl;  // bits of max |lambda_old|
+    double velres;            // sum of squared scaled velocity increments
+    int32_t done;
+    int32_t iters;
+    double res_last;
+    double res_final;
+    int32_t pad[4];
+};
+
+struct Incidence {
+    int64_t cap = 0;
+    uint32_t* key_in = nullptr;
+    uint32_t* val_in = nullptr;
+    uint32_t* key_out = nullptr;
+    uint32_t* val_out = nullptr;
+    int32_t* start = nullptr;  // N
+    int32_t* end = nullptr;    // N
+};
+
+// ---- launchers (k_common.cu) ----
+size_t scan_temp_bytes(int64_t n);
+size_t sort_temp_bytes(int64_t n);
+cudaError_t exclusive_scan(void* tmp, size_t tmp_bytes, const int32_t* in, int32_t* out, int64_t n, cudaStream_t s);
+cudaError_t sort_pairs(void* tmp, size_t tmp_bytes, const uint32_t* kin, uint32_t* kout, const uint32_t* vin,
+                       uint32_t* vout, int64_t n, int end_bit, cudaStream_t s);
+void launch_cell_keys(const Scene& sc, const Grid& g, uint32_t* keys, uint32_t* vals, cudaStream_t s);
+void launch_ranges(const uint32_t* sorted_keys, int64_t n, int32_t* start, int32_t* end, cudaStream_t s);
+
+// ---- FP64 plain method (k_fp64.cu) ----
+void launch_rhs64(const Scene& sc, double dt, const double* g, double* rhs, cudaStream_t s);
+void launch_drift64(const Scene& sc, double h, int compute_R, cudaStream_t s);
+void launch_static_flags64(const Scene& sc, double margin, int32_t* flags, cudaStream_t s);
+void launch_pair_count64(const Scene& sc, const Grid& g, const uint32_t* cell_body, const int32_t* cell_start,
+                         const int32_t* cell_end, double margin, int32_t* counts, DevScalars* ds, cudaStream_t s);
+void launch_static_write64(const Scene& sc, double margin, const int32_t* flags, const int32_t* pos,
+                           Contacts& C, int gen, int combine, int friction_enable, cudaStream_t s);
+void launch_pair_write64(const Scene& sc, const Grid& g, const uint32_t* cell_body, const int32_t* cell_start,
+                         const int32_t* cell_end, double margin, const int32_t* offsets, int32_t base,
+                         Contacts& C, int gen, int combine, int friction_enable, DevScalars* ds, cudaStream_t s);
+void launch_contact_setup64(const Scene& sc, Contacts& C, int gen, int nc, int prev_count, double alpha,
+                            double match2, int warmstart, cudaStream_t s);
+void launch_frictionless_flags(const Contacts& C, int nc, int32_t* isfl, cudaStream_t s);
+void launch_rank_and_incidence(const Scene& sc, Contacts& C, int nc, const int32_t* fl_scan, const int32_t* isfl,
+                               Incidence& inc, cudaStream_t s);
+void launch_xinit64(const Scene& sc, const Contacts& C, int gen, const Incidence& inc, const double* rhs, double* x,
+                    cudaStream_t s);
+void launch_sweep_contact64(const Scene& sc, Contacts& C, int gen, int nc, const double* x, DevScalars* ds, int dry,
+                            cudaStream_t s);
+void launch_sweep_body64(const Scene& sc, const Contacts& C, const Incidence& inc, double* x, double tol_abs,
+                         double tol_rel, int want_velres, DevScalars* ds, cudaStream_t s);
+void launch_check(DevScalars* ds, int iter, double residual_tol, int nv, int check_vel, cudaStream_t s);
+void launch_final_residual(DevScalars* ds, cudaStream_t s);
+void launch_writeback64(const Scene& sc, const double* x, cudaStream_t s);
+void launch_trace64(const Contacts& C, int gen, int nc, const int32_t* fl_scan, const int32_t* isfl, double* out,
+                    cudaStream_t s);
+
+}  // namespace cdx
+
+namespace cdx {
+// ---- solver-level drop-in on a general CSR Jacobian (k_csr.cu) ----
+void launch_csr_rhs(int nv, const double* mdiag, const double* v, const double* fext, const double* fgyro, double dt,
+                    double* rhs, cudaStream_t s);
+void launch_csr_rowidx(int nrows, const int32_t* ptr, int32_t* rowidx, uint32_t* colkey, uint32_t* nzid,
+                       const int32_t* col, cudaStream_t s);
+void launch_csr_setup(int nrows, const int32_t* ptr, const int32_t* col, const double* val, const double* cb,
+                      const double* e, const double* minv, const double* v, double alpha, double* RW, double* biasR,
+                      cudaStream_t s);
+void launch_csr_cols(int nv, const int32_t* cstart, const int32_t* cend, const uint32_t* nz_sorted,
+                     const int32_t* rowidx, const double* val, const double* y, const double* base,
+                     const double* mdiag, double* x, int mode, double tol_abs, double tol_rel, int want_velres,
+                     DevScalars* ds, cudaStream_t s);
+void launch_csr_rows(int nrows, int nfl, const int32_t* ptr, const int32_t* col, const double* RW,
+                     const double* biasR, const double* mu, const double* x, double* lam, double* dlam,
+                     DevScalars* ds, cudaStream_t s);
+}  // namespace cdx

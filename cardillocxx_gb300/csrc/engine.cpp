@@ -1,0 +1,644 @@
+// Host side of the engine: owns the device memory and the stream, and drives one Moreau midpoint
+// step as a sequence of kernel launches (MoreauIntegrator::step, src/physics/integration/moreau.cpp:6-13):
+//   refreshState -> drift (1-theta)h -> collision -> contact rows -> projected Jacobi -> write
+//   velocities -> drift theta h.
+// The C-ABI entry points (include/cdx.h) are implemented at the end of this file.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/cdx.h"
+#include "cdx_internal.h"
+#include "engine.h"
+
+using namespace cdx;
+
+namespace cdx {
+
+const char* status_name(int st) {
+    switch (st) {
+        case CDX_OK: return "ok";
+        case CDX_ERR_ARG: return "invalid argument";
+        case CDX_ERR_CUDA: return "CUDA error";
+        case CDX_ERR_OVERFLOW: return "overflow";
+        case CDX_ERR_NONFINITE: return "non-finite value";
+        case CDX_ERR_TIMEOUT: return "timeout";
+        case CDX_ERR_UNSUPPORTED: return "unsupported";
+        case CDX_ERR_STATE: return "bad state";
+    }
+    return "unknown";
+}
+
+}  // namespace cdx
+
+int Engine::fail(int st, const std::string& msg) {
+    err = std::string(status_name(st)) + ": " + msg;
+    return st;
+}
+
+int Engine::cuda_check(cudaError_t e, const char* where) {
+    if (e == cudaSuccess) return CDX_OK;
+    return fail(CDX_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+int Engine::dalloc(void** p, size_t bytes, const char* what) {
+    *p = nullptr;
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) return fail(CDX_ERR_CUDA, std::string("cudaMalloc ") + what + ": " + cudaGetErrorString(e));
+    owned.push_back(*p);
+    return CDX_OK;
+}
+
+void Engine::dfree(void* p) {
+    if (!p) return;
+    auto it = std::find(owned.begin(), owned.end(), p);
+    if (it != owned.end()) owned.erase(it);
+    cudaFree(p);
+}
+
+Engine::~Engine() {
+    if (stream) cudaStreamSynchronize(stream);
+    for (void* p : owned) cudaFree(p);
+    owned.clear();
+    if (hs) cudaFreeHost(hs);
+    for (auto& e : ev) if (e) cudaEventDestroy(e);
+    destroy_split();
+    if (stream) cudaStreamDestroy(stream);
+}
+
+int Engine::init(const cdx_config& c) {
+    cfg = c;
+    if (cfg.moreau_implicit_gyroscopy) return fail(CDX_ERR_UNSUPPORTED, "moreau.implicit_gyroscopy=on is not supported");
+    if (cfg.solver_type != 0) return fail(CDX_ERR_UNSUPPORTED, "only solver.type=projected_jacobi is on this path");
+    int st = cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    if (st) return st;
+    st = cuda_check(cudaMallocHost((void**)&hs, sizeof(DevScalars)), "cudaMallocHost");
+    if (st) return st;
+    std::memset(hs, 0, sizeof(DevScalars));
+    for (auto& e : ev) {
+        st = cuda_check(cudaEventCreate(&e), "cudaEventCreate");
+        if (st) return st;
+    }
+    return CDX_OK;
+}
+
+int Engine::load_scene(const cdx_scene& s) {
+    if (s.num_bodies < 0 || s.num_statics < 0) return fail(CDX_ERR_ARG, "negative sizes");
+    const int N = s.num_bodies, S = s.num_statics;
+    if (N > 0 && (!s.pos || !s.quat || !s.vel || !s.omega || !s.radius || !s.mass || !s.inertia || !s.mu ||
+                  !s.rest_n || !s.rest_t))
+        return fail(CDX_ERR_ARG, "missing body arrays");
+    if (S > 0 && (!s.static_kind || !s.static_pos || !s.static_quat || !s.static_vel || !s.static_omega ||
+                  !s.static_dir || !s.static_mu || !s.static_rest_n || !s.static_rest_t))
+        return fail(CDX_ERR_ARG, "missing static arrays");
+    if ((int64_t)N * 2 + 2 >= (int64_t)INT32_MAX / 2) return fail(CDX_ERR_ARG, "too many bodies");
+    const int nsc = std::max(1, s.num_scenes);
+    // scene ranges (bodies and statics must be grouped by scene)
+    std::vector<int32_t> bsc(N, 0), ssc(S, 0);
+    if (s.body_scene) std::copy(s.body_scene, s.body_scene + N, bsc.begin());
+    if (s.static_scene) std::copy(s.static_scene, s.static_scene + S, ssc.begin());
+    std::vector<int32_t> bstart(nsc + 1, 0), sstart(nsc + 1, 0);
+    for (int i = 0; i < N; ++i) {
+        if (bsc[i] < 0 || bsc[i] >= nsc || (i > 0 && bsc[i] < bsc[i - 1])) return fail(CDX_ERR_ARG, "body_scene must be nondecreasing in [0, num_scenes)");
+        bstart[bsc[i] + 1]++;
+    }
+    for (int i = 0; i < S; ++i) {
+        if (ssc[i] < 0 || ssc[i] >= nsc || (i > 0 && ssc[i] < ssc[i - 1])) return fail(CDX_ERR_ARG, "static_scene must be nondecreasing in [0, num_scenes)");
+        sstart[ssc[i] + 1]++;
+    }
+    int maxst = 0;
+    for (int k = 0; k < nsc; ++k) {
+        maxst = std::max(maxst, sstart[k + 1]);
+        bstart[k + 1] += bstart[k];
+        sstart[k + 1] += sstart[k];
+    }
+    for (int i = 0; i < N; ++i) {
+        if (!(s.radius[i] > 0) || !(s.mass[i] > 0) || !(s.inertia[i] > 0))
+            return fail(CDX_ERR_ARG, "bodies need positive radius, mass and inertia");
+    }
+    for (int i = 0; i < S; ++i)
+        if (s.static_kind[i] != CDX_STATIC_HALFSPACE && s.static_kind[i] != CDX_STATIC_DRUM)
+            return fail(CDX_ERR_ARG, "unknown static kind");
+
+    // host staging: body fields (field-major)
+    std::vector<double> B((size_t)BF_COUNT * N, 0.0);
+    auto bf = [&](int f, int i) -> double& { return B[(size_t)f * N + i]; };
+    rmax = 0;
+    for (int i = 0; i < N; ++i) {
+        for (int k = 0; k < 3; ++k) {
+            bf(BF_PX + k, i) = s.pos[3 * (size_t)i + k];
+            bf(BF_VX + k, i) = s.vel[3 * (size_t)i + k];
+            bf(BF_WX + k, i) = s.omega[3 * (size_t)i + k];
+        }
+        for (int k = 0; k < 4; ++k) bf(BF_QX + k, i) = s.quat[4 * (size_t)i + k];
+        bf(BF_RAD, i) = s.radius[i];
+        bf(BF_MASS, i) = s.mass[i];
+        bf(BF_INERTIA, i) = s.inertia[i];
+        bf(BF_MU, i) = s.mu[i];
+        bf(BF_RN, i) = s.rest_n[i];
+        bf(BF_RT, i) = s.rest_t[i];
+        // rebuildMass_ (dynamics_assembler.cpp:41-62): Minv = 1/m, M_ii = 1/Minv
+        const double il = 1.0 / s.mass[i], ia = 1.0 / s.inertia[i];
+        bf(BF_MINVL, i) = il;
+        bf(BF_MINVA, i) = ia;
+        bf(BF_ML, i) = il > 0.0 ? 1.0 / il : 0.0;
+        bf(BF_MA, i) = ia > 0.0 ? 1.0 / ia : 0.0;
+        rmax = std::max(rmax, s.radius[i]);
+    }
+    std::vector<double> St((size_t)SF_COUNT * S, 0.0);
+    auto sf = [&](int f, int i) -> double& { return St[(size_t)f * S + i]; };
+    for (int i = 0; i < S; ++i) {
+        for (int k = 0; k < 3; ++k) {
+            sf(SF_PX + k, i) = s.static_pos[3 * (size_t)i + k];
+            sf(SF_VX + k, i) = s.static_vel[3 * (size_t)i + k];
+            sf(SF_WX + k, i) = s.static_omega[3 * (size_t)i + k];
+        }
+        for (int k = 0; k < 4; ++k) sf(SF_QX + k, i) = s.static_quat[4 * (size_t)i + k];
+        // plane.normal.normalized(), d = n . x (collision_coal.cpp:292-297)
+        const double* u = &s.static_dir[3 * (size_t)i];
+        const double n2 = (u[0] * u[0] + u[1] * u[1]) + u[2] * u[2];
+        const double n = std::sqrt(n2);
+        double un[3];
+        for (int k = 0; k < 3; ++k) un[k] = n2 > 0 ? u[k] / n : u[k];
+        for (int k = 0; k < 3; ++k) sf(SF_DX + k, i) = un[k];
+        const double* p = &s.static_pos[3 * (size_t)i];
+        sf(SF_D, i) = (un[0] * p[0] + un[1] * p[1]) + un[2] * p[2];
+        sf(SF_RAD, i) = s.static_radius ? s.static_radius[i] : 0.0;
+        sf(SF_MU, i) = s.static_mu[i];
+        sf(SF_RN, i) = s.static_rest_n[i];
+        sf(SF_RT, i) = s.static_rest_t[i];
+    }
+
+    // grid over the initial bounding box plus statics' anchor points, padded
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int i = 0; i < N; ++i)
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = std::min(lo[k], s.pos[3 * (size_t)i + k]);
+            hi[k] = std::max(hi[k], s.pos[3 * (size_t)i + k]);
+        }
+    if (N == 0)
+        for (int k = 0; k < 3; ++k) { lo[k] = 0; hi[k] = 1; }
+    const double cell = 2.0 * rmax * 1.0001 + 1e-9;
+    for (int k = 0; k < 3; ++k) {
+        const double pad = 0.05 * (hi[k] - lo[k]) + 2 * cell;
+        lo[k] -= pad;
+        hi[k] += pad;
+    }
+    Grid g{};
+    int64_t ncells = 1;
+    for (int k = 0; k < 3; ++k) {
+        g.lo[k] = lo[k];
+        g.dim[k] = (int)std::min<double>(std::ceil((hi[k] - lo[k]) / cell) + 1, 1 << 20);
+        ncells *= g.dim[k];
+    }
+    // keep the dense cell table modest: coarsen cells if needed (still >= 2 rmax, so exact)
+    double cs = cell;
+    while (ncells > (int64_t)64 << 20) {
+        cs *= 1.25;
+        ncells = 1;
+        for (int k = 0; k < 3; ++k) {
+            g.dim[k] = (int)std::ceil((hi[k] - lo[k]) / cs) + 1;
+            ncells *= g.dim[k];
+        }
+    }
+    g.cell = cs;
+    g.ncells = ncells;
+    g.key_bits = 1;
+    while (((int64_t)1 << g.key_bits) < ncells) ++g.key_bits;
+    grid = g;
+
+    // free any previous scene
+    cudaStreamSynchronize(stream);
+    for (void* p : owned) cudaFree(p);
+    owned.clear();
+    sc = Scene{};
+    C = Contacts{};
+    inc = Incidence{};
+    destroy_split();
+    tmp = nullptr;
+    tmp_bytes = 0;
+    nc = 0;
+    prev_count = 0;
+    gen = 0;
+
+    int st;
+    sc.N = N;
+    sc.S = S;
+    sc.nscenes = nsc;
+    sc.max_statics = maxst;
+    if ((st = dalloc((void**)&sc.B, sizeof(double) * B.size(), "bodies"))) return st;
+    if ((st = dalloc((void**)&sc.body_scene, sizeof(int32_t) * std::max(1, N), "body_scene"))) return st;
+    if ((st = dalloc((void**)&sc.St, sizeof(double) * std::max<size_t>(1, St.size()), "statics"))) return st;
+    if ((st = dalloc((void**)&sc.static_kind, sizeof(int32_t) * std::max(1, S), "static_kind"))) return st;
+    if ((st = dalloc((void**)&sc.static_scene, sizeof(int32_t) * std::max(1, S), "static_scene"))) return st;
+    if ((st = dalloc((void**)&sc.scene_body_start, sizeof(int32_t) * (nsc + 1), "scene ranges"))) return st;
+    if ((st = dalloc((void**)&sc.scene_static_start, sizeof(int32_t) * (nsc + 1), "scene ranges"))) return st;
+    std::vector<int32_t> kind(s.static_kind, s.static_kind + S);
+    if ((st = cuda_check(cudaMemcpy(sc.B, B.data(), sizeof(double) * B.size(), cudaMemcpyHostToDevice), "upload"))) return st;
+    if (N && (st = cuda_check(cudaMemcpy(sc.body_scene, bsc.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice), "upload"))) return st;
+    if (S) {
+        if ((st = cuda_check(cudaMemcpy(sc.St, St.data(), sizeof(double) * St.size(), cudaMemcpyHostToDevice), "upload"))) return st;
+        if ((st = cuda_check(cudaMemcpy(sc.static_kind, kind.data(), sizeof(int32_t) * S, cudaMemcpyHostToDevice), "upload"))) return st;
+        if ((st = cuda_check(cudaMemcpy(sc.static_scene, ssc.data(), sizeof(int32_t) * S, cudaMemcpyHostToDevice), "upload"))) return st;
+    }
+    if ((st = cuda_check(cudaMemcpy(sc.scene_body_start, bstart.data(), sizeof(int32_t) * (nsc + 1), cudaMemcpyHostToDevice), "upload"))) return st;
+    if ((st = cuda_check(cudaMemcpy(sc.scene_static_start, sstart.data(), sizeof(int32_t) * (nsc + 1), cudaMemcpyHostToDevice), "upload"))) return st;
+    h_scene_body_start = bstart;
+    h_scene_static_start = sstart;
+
+    // per-body work arrays
+    if ((st = dalloc((void**)&rhs, sizeof(double) * 6 * std::max(1, N), "rhs"))) return st;
+    if ((st = dalloc((void**)&x, sizeof(double) * 6 * std::max(1, N), "x"))) return st;
+    if ((st = dalloc((void**)&cell_key_in, sizeof(uint32_t) * std::max(1, N), "grid"))) return st;
+    if ((st = dalloc((void**)&cell_val_in, sizeof(uint32_t) * std::max(1, N), "grid"))) return st;
+    if ((st = dalloc((void**)&cell_key_out, sizeof(uint32_t) * std::max(1, N), "grid"))) return st;
+    if ((st = dalloc((void**)&cell_val_out, sizeof(uint32_t) * std::max(1, N), "grid"))) return st;
+    if ((st = dalloc((void**)&cell_start, sizeof(int32_t) * ncells, "grid"))) return st;
+    if ((st = dalloc((void**)&cell_end, sizeof(int32_t) * ncells, "grid"))) return st;
+    const int64_t nflag = (int64_t)std::max(1, N) * std::max(1, maxst);
+    if ((st = dalloc((void**)&sflags, sizeof(int32_t) * nflag, "static flags"))) return st;
+    if ((st = dalloc((void**)&spos, sizeof(int32_t) * nflag, "static flags"))) return st;
+    if ((st = dalloc((void**)&pcount, sizeof(int32_t) * (N + 1), "pair counts"))) return st;
+    if ((st = dalloc((void**)&poff, sizeof(int32_t) * (N + 1), "pair offsets"))) return st;
+    if ((st = dalloc((void**)&ds, sizeof(DevScalars), "scalars"))) return st;
+    if ((st = dalloc((void**)&inc.start, sizeof(int32_t) * (N + 1), "incidence"))) return st;
+    if ((st = dalloc((void**)&inc.end, sizeof(int32_t) * (N + 1), "incidence"))) return st;
+    if ((st = cuda_check(cudaMemset(ds, 0, sizeof(DevScalars)), "memset"))) return st;
+    if ((st = cuda_check(cudaMemset(pcount, 0, sizeof(int32_t) * (N + 1)), "memset"))) return st;
+    const int64_t cap0 = std::max<int64_t>(1024, (int64_t)(cfg.gpu_contact_capacity_factor * std::max(1, N)));
+    if ((st = ensure_contacts(cap0))) return st;
+    if ((st = ensure_tmp(std::max<int64_t>(nflag, N + 1)))) return st;
+    loaded = true;
+    steps = 0;
+    return CDX_OK;
+}
+
+int Engine::ensure_tmp(int64_t n) {
+    const size_t need = std::max(scan_temp_bytes(n), sort_temp_bytes(n)) + 256;
+    if (need <= tmp_bytes) return CDX_OK;
+    if (tmp) dfree(tmp);
+    tmp = nullptr;
+    const size_t b = need + need / 4;
+    int st = dalloc(&tmp, b, "scratch");
+    if (st) return st;
+    tmp_bytes = b;
+    return CDX_OK;
+}
+
+// Contact arrays of capacity `cap`; the previous generation's keys/points/impulses survive growth.
+int Engine::ensure_contacts(int64_t need) {
+    if (need <= C.cap) return CDX_OK;
+    const int64_t cap = std::max<int64_t>(need + need / 4, 1024);
+    if (cap > (int64_t)INT32_MAX / 4) return fail(CDX_ERR_OVERFLOW, "contact count exceeds the 32-bit index range");
+    Contacts n;
+    n.cap = cap;
+    int st;
+    if ((st = dalloc((void**)&n.a, sizeof(int32_t) * cap, "contacts"))) return st;
+    if ((st = dalloc((void**)&n.b, sizeof(int32_t) * cap, "contacts"))) return st;
+    if ((st = dalloc((void**)&n.flags, sizeof(int32_t) * cap, "contacts"))) return st;
+    if ((st = dalloc((void**)&n.rank, sizeof(int32_t) * cap, "contacts"))) return st;
+    double** d9[] = {&n.dir, &n.cA, &n.cB, &n.rd, &n.rcA, &n.rcB};
+    for (auto p : d9)
+        if ((st = dalloc((void**)p, sizeof(double) * 9 * cap, "contacts"))) return st;
+    double** d3[] = {&n.cb, &n.biasR, &n.dlam};
+    for (auto p : d3)
+        if ((st = dalloc((void**)p, sizeof(double) * 3 * cap, "contacts"))) return st;
+    double** d1[] = {&n.mu, &n.eN, &n.eT};
+    for (auto p : d1)
+        if ((st = dalloc((void**)p, sizeof(double) * cap, "contacts"))) return st;
+    for (int gidx = 0; gidx < 2; ++gidx) {
+        if ((st = dalloc((void**)&n.key[gidx], sizeof(unsigned long long) * cap, "contacts"))) return st;
+        if ((st = dalloc((void**)&n.point[gidx], sizeof(double) * 3 * cap, "contacts"))) return st;
+        if ((st = dalloc((void**)&n.lam[gidx], sizeof(double) * 3 * cap, "contacts"))) return st;
+    }
+    // carry the previous generation (field-major with the old stride)
+    if (C.cap > 0 && prev_count > 0) {
+        const int pg = gen ^ 1;
+        st = cuda_check(cudaMemcpyAsync(n.key[pg], C.key[pg], sizeof(unsigned long long) * prev_count,
+                                        cudaMemcpyDeviceToDevice, stream), "copy prev");
+        if (st) return st;
+        for (int k = 0; k < 3; ++k) {
+            if ((st = cuda_check(cudaMemcpyAsync(n.point[pg] + k * cap, C.point[pg] + k * C.cap, sizeof(double) * prev_count,
+                                                 cudaMemcpyDeviceToDevice, stream), "copy prev"))) return st;
+            if ((st = cuda_check(cudaMemcpyAsync(n.lam[pg] + k * cap, C.lam[pg] + k * C.cap, sizeof(double) * prev_count,
+                                                 cudaMemcpyDeviceToDevice, stream), "copy prev"))) return st;
+        }
+        cudaStreamSynchronize(stream);
+    }
+    if (C.cap > 0) {
+        void* old[] = {C.a, C.b, C.flags, C.rank, C.dir, C.cA, C.cB, C.rd, C.rcA, C.rcB, C.cb, C.biasR, C.dlam,
+                       C.mu, C.eN, C.eT, C.key[0], C.key[1], C.point[0], C.point[1], C.lam[0], C.lam[1]};
+        for (void* p : old) dfree(p);
+        ++reallocations;
+    }
+    C = n;
+    // incidence (2 entries per contact) and frictionless scan
+    void* oldi[] = {inc.key_in, inc.val_in, inc.key_out, inc.val_out, isfl, flscan};
+    for (void* p : oldi) dfree(p);
+    inc.cap = 2 * cap;
+    if ((st = dalloc((void**)&inc.key_in, sizeof(uint32_t) * 2 * cap, "incidence"))) return st;
+    if ((st = dalloc((void**)&inc.val_in, sizeof(uint32_t) * 2 * cap, "incidence"))) return st;
+    if ((st = dalloc((void**)&inc.key_out, sizeof(uint32_t) * 2 * cap, "incidence"))) return st;
+    if ((st = dalloc((void**)&inc.val_out, sizeof(uint32_t) * 2 * cap, "incidence"))) return st;
+    if ((st = dalloc((void**)&isfl, sizeof(int32_t) * cap, "flags"))) return st;
+    if ((st = dalloc((void**)&flscan, sizeof(int32_t) * cap, "flags"))) return st;
+    return ensure_tmp(2 * cap);
+}
+
+int Engine::collide64() {
+    const int N = sc.N;
+    const double margin = cfg.collision_security_margin;
+    launch_cell_keys(sc, grid, cell_key_in, cell_val_in, stream);
+    ++launches;
+    int st = cuda_check(sort_pairs(tmp, tmp_bytes, cell_key_in, cell_key_out, cell_val_in, cell_val_out, N,
+                                   grid.key_bits, stream), "sort cells");
+    if (st) return st;
+    launches += 4;
+    cudaMemsetAsync(cell_start, 0, sizeof(int32_t) * grid.ncells, stream);
+    cudaMemsetAsync(cell_end, 0, sizeof(int32_t) * grid.ncells, stream);
+    launch_ranges(cell_key_out, N, cell_start, cell_end, stream);
+    ++launches;
+    // static contacts: flags in (static, sphere) order, then positions
+    const int64_t nflag = (int64_t)N * sc.max_statics;
+    if (nflag > 0) {
+        launch_static_flags64(sc, margin, sflags, stream);
+        ++launches;
+        if ((st = cuda_check(exclusive_scan(tmp, tmp_bytes, sflags, spos, nflag, stream), "scan"))) return st;
+        launches += 2;
+    }
+    launch_pair_count64(sc, grid, cell_val_out, cell_start, cell_end, margin, pcount, ds, stream);
+    ++launches;
+    if ((st = cuda_check(exclusive_scan(tmp, tmp_bytes, pcount, poff, N + 1, stream), "scan"))) return st;
+    launches += 2;
+    // totals to the host (one synchronisation per step: the contact count sizes everything after)
+    int32_t tot[4] = {0, 0, 0, 0};
+    if (nflag > 0) {
+        cudaMemcpyAsync(&tot[0], spos + nflag - 1, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+        cudaMemcpyAsync(&tot[1], sflags + nflag - 1, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+    }
+    cudaMemcpyAsync(&tot[2], poff + N, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(&tot[3], &ds->overflow, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+    if ((st = cuda_check(cudaStreamSynchronize(stream), "collision counts"))) return st;
+    if (tot[3]) return fail(CDX_ERR_OVERFLOW, "a sphere touches more than 64 higher-index spheres");
+    const int64_t n_static = (int64_t)tot[0] + tot[1];
+    const int64_t n_pair = tot[2];
+    if ((st = ensure_contacts(n_static + n_pair))) return st;
+    nc = (int)(n_static + n_pair);
+    if (nflag > 0 && n_static > 0) {
+        launch_static_write64(sc, margin, sflags, spos, C, gen, cfg.friction_combine, cfg.friction_enable, stream);
+        ++launches;
+    }
+    if (n_pair > 0) {
+        launch_pair_write64(sc, grid, cell_val_out, cell_start, cell_end, margin, poff, (int32_t)n_static, C, gen,
+                            cfg.friction_combine, cfg.friction_enable, ds, stream);
+        ++launches;
+    }
+    return CDX_OK;
+}
+
+int Engine::setup64() {
+    int st;
+    const double match2 = cfg.collision_match_max_dist * cfg.collision_match_max_dist;
+    launch_contact_setup64(sc, C, gen, nc, prev_count, cfg.pj_alpha, match2, cfg.pj_warmstart, stream);
+    launch_frictionless_flags(C, nc, isfl, stream);
+    launches += nc > 0 ? 2 : 0;
+    if (nc > 0) {
+        if ((st = cuda_check(exclusive_scan(tmp, tmp_bytes, isfl, flscan, nc, stream), "scan"))) return st;
+        launches += 2;
+    }
+    launch_rank_and_incidence(sc, C, nc, flscan, isfl, inc, stream);
+    int key_bits = 1;
+    while (((int64_t)1 << key_bits) <= sc.N) ++key_bits;
+    if (nc > 0) {
+        ++launches;
+        if ((st = cuda_check(sort_pairs(tmp, tmp_bytes, inc.key_in, inc.key_out, inc.val_in, inc.val_out, 2 * (int64_t)nc,
+                                        key_bits, stream), "sort incidence"))) return st;
+        launches += 4;
+    }
+    cudaMemsetAsync(inc.start, 0, sizeof(int32_t) * (sc.N + 1), stream);
+    cudaMemsetAsync(inc.end, 0, sizeof(int32_t) * (sc.N + 1), stream);
+    if (nc > 0) {
+        launch_ranges(inc.key_out, 2 * (int64_t)nc, inc.start, inc.end, stream);
+        ++launches;
+    }
+    return CDX_OK;
+}
+
+int Engine::solve64() {
+    const int N = sc.N;
+    int st;
+    launch_xinit64(sc, C, gen, inc, rhs, x, stream);
+    ++launches;
+    hs->done = 0;
+    last_iters = 0;
+    last_res = 0;
+    last_res_final = 0;
+    if (nc == 0) return CDX_OK;
+    cudaMemsetAsync(ds, 0, sizeof(DevScalars), stream);
+    const int maxit = std::max(1, cfg.pj_max_iterations);
+    const bool check_vel = !(cfg.pj_tol_abs == 0.0 && cfg.pj_tol_rel == 0.0);
+    const int every = std::max(1, cfg.gpu_check_every);
+    const int nrows = nfl_rows();
+    if (trace_next) {
+        trace_rows = nrows;
+        trace_buf.clear();
+        if (trace_dev) dfree(trace_dev);
+        trace_dev = nullptr;
+        if ((st = dalloc((void**)&trace_dev, sizeof(double) * (size_t)std::max(1, nrows), "trace"))) return st;
+    }
+    int it = 0;
+    for (; it < maxit; ++it) {
+        launch_sweep_contact64(sc, C, gen, nc, x, ds, 0, stream);
+        launch_sweep_body64(sc, C, inc, x, cfg.pj_tol_abs, cfg.pj_tol_rel, check_vel && (it % 10 == 0), ds, stream);
+        launch_check(ds, it, cfg.gpu_residual_tol, 6 * N, check_vel, stream);
+        launches += 3;
+        if (trace_next) {
+            launch_trace64(C, gen, nc, flscan, isfl, trace_dev, stream);
+            std::vector<double> h(nrows);
+            cudaMemcpyAsync(h.data(), trace_dev, sizeof(double) * nrows, cudaMemcpyDeviceToHost, stream);
+            cudaMemcpyAsync(&hs->done, &ds->done, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+            if ((st = cuda_check(cudaStreamSynchronize(stream), "trace"))) return st;
+            if (hs->done && !trace_done_seen) {
+                // the sweep that set the flag is kept; later ones are no-ops
+                trace_buf.insert(trace_buf.end(), h.begin(), h.end());
+                trace_done_seen = true;
+                break;
+            }
+            trace_buf.insert(trace_buf.end(), h.begin(), h.end());
+            continue;
+        }
+        if ((it + 1) % every == 0 && it + 1 < maxit) {
+            cudaMemcpyAsync(&hs->done, &ds->done, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+            if ((st = cuda_check(cudaStreamSynchronize(stream), "poll"))) return st;
+            if (hs->done) break;
+        }
+    }
+    trace_next = false;
+    trace_done_seen = false;
+    // final FP64 complementarity residual of the solved state
+    launch_sweep_contact64(sc, C, gen, nc, x, ds, 1, stream);
+    launch_final_residual(ds, stream);
+    launches += 2;
+    return CDX_OK;
+}
+
+int Engine::nfl_rows() {
+    // rows = frictionless contacts + 3 * frictional contacts
+    int32_t a = 0, b = 0;
+    if (nc == 0) return 0;
+    cudaMemcpyAsync(&a, flscan + nc - 1, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(&b, isfl + nc - 1, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+    cudaStreamSynchronize(stream);
+    const int nfl = a + b;
+    return nfl + 3 * (nc - nfl);
+}
+
+int Engine::step64() {
+    const double dt = cfg.sim_dt, th = cfg.moreau_theta;
+    int st;
+    if (timing) cudaEventRecord(ev[0], stream);
+    launch_rhs64(sc, dt, cfg.sim_gravity, rhs, stream);
+    launch_drift64(sc, (1.0 - th) * dt, 1, stream);
+    launches += 2;
+    if ((st = collide64())) return st;
+    if (timing) cudaEventRecord(ev[1], stream);
+    if ((st = setup64())) return st;
+    if (timing) cudaEventRecord(ev[2], stream);
+    if ((st = solve64())) return st;
+    if (timing) cudaEventRecord(ev[3], stream);
+    launch_writeback64(sc, x, stream);
+    launch_drift64(sc, th * dt, 0, stream);
+    launches += 2;
+    if (timing) cudaEventRecord(ev[4], stream);
+    cudaMemcpyAsync(hs, ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, stream);
+    if ((st = cuda_check(cudaStreamSynchronize(stream), "step"))) return st;
+    if ((st = cuda_check(cudaGetLastError(), "kernel launch"))) return st;
+    last_iters = nc > 0 ? hs->iters : 0;
+    last_res = nc > 0 ? hs->res_last : 0.0;
+    last_res_final = nc > 0 ? hs->res_final : 0.0;
+    last_rows = nc > 0 ? nfl_rows() : 0;
+    prev_count = nc;
+    gen ^= 1;
+    ++steps;
+    if (timing) {
+        float a = 0, b = 0, c2 = 0, d = 0;
+        cudaEventElapsedTime(&a, ev[0], ev[1]);
+        cudaEventElapsedTime(&b, ev[1], ev[2]);
+        cudaEventElapsedTime(&c2, ev[2], ev[3]);
+        cudaEventElapsedTime(&d, ev[3], ev[4]);
+        ms[0] = a; ms[1] = b; ms[2] = c2; ms[3] = d;
+    }
+    return CDX_OK;
+}
+
+int Engine::step(int nsteps) {
+    if (!loaded) return fail(CDX_ERR_STATE, "no scene loaded");
+    for (int k = 0; k < nsteps; ++k) {
+        int st = (cfg.gpu_precision == CDX_PRECISION_SPLIT) ? step_split() : step64();
+        if (st) return st;
+    }
+    return CDX_OK;
+}
+
+int Engine::get_state(double* pos, double* quat, double* vel, double* omega) {
+    if (!loaded) return fail(CDX_ERR_STATE, "no scene loaded");
+    int st;
+    if ((st = sync_state_to_fp64())) return st;
+    const int N = sc.N;
+    std::vector<double> B((size_t)BF_COUNT * N);
+    if ((st = cuda_check(cudaMemcpyAsync(B.data(), sc.B, sizeof(double) * B.size(), cudaMemcpyDeviceToHost, stream), "download"))) return st;
+    if ((st = cuda_check(cudaStreamSynchronize(stream), "download"))) return st;
+    auto bf = [&](int f, int i) { return B[(size_t)f * N + i]; };
+    for (int i = 0; i < N; ++i) {
+        for (int k = 0; k < 3; ++k) {
+            if (pos) pos[3 * (size_t)i + k] = bf(BF_PX + k, i);
+            if (vel) vel[3 * (size_t)i + k] = bf(BF_VX + k, i);
+            if (omega) omega[3 * (size_t)i + k] = bf(BF_WX + k, i);
+        }
+        for (int k = 0; k < 4; ++k)
+            if (quat) quat[4 * (size_t)i + k] = bf(BF_QX + k, i);
+    }
+    return CDX_OK;
+}
+
+int Engine::set_state(const double* pos, const double* quat, const double* vel, const double* omega) {
+    if (!loaded) return fail(CDX_ERR_STATE, "no scene loaded");
+    int st;
+    if ((st = sync_state_to_fp64())) return st;
+    const int N = sc.N;
+    std::vector<double> B((size_t)BF_COUNT * N);
+    if ((st = cuda_check(cudaMemcpy(B.data(), sc.B, sizeof(double) * B.size(), cudaMemcpyDeviceToHost), "download"))) return st;
+    auto bf = [&](int f, int i) -> double& { return B[(size_t)f * N + i]; };
+    for (int i = 0; i < N; ++i) {
+        for (int k = 0; k < 3; ++k) {
+            if (pos) bf(BF_PX + k, i) = pos[3 * (size_t)i + k];
+            if (vel) bf(BF_VX + k, i) = vel[3 * (size_t)i + k];
+            if (omega) bf(BF_WX + k, i) = omega[3 * (size_t)i + k];
+        }
+        for (int k = 0; k < 4; ++k)
+            if (quat) bf(BF_QX + k, i) = quat[4 * (size_t)i + k];
+    }
+    if ((st = cuda_check(cudaMemcpy(sc.B, B.data(), sizeof(double) * B.size(), cudaMemcpyHostToDevice), "upload"))) return st;
+    return mark_state_changed();
+}
+
+int Engine::get_contacts(int32_t* ia, int32_t* ib, double* point, double* lambda, double* normal, int32_t* count) {
+    if (!loaded) return fail(CDX_ERR_STATE, "no scene loaded");
+    if (cfg.gpu_precision == CDX_PRECISION_SPLIT) return get_contacts_split(ia, ib, point, lambda, normal, count);
+    const int n = prev_count;  // contacts of the last completed step
+    if (count) *count = n;
+    if (n == 0 || (!ia && !ib && !point && !lambda && !normal)) return CDX_OK;
+    const int g = gen ^ 1;
+    std::vector<unsigned long long> keys(n);
+    std::vector<double> p(3 * (size_t)n), l(3 * (size_t)n), nn(3 * (size_t)n);
+    int st;
+    if ((st = cuda_check(cudaMemcpy(keys.data(), C.key[g], sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost), "download"))) return st;
+    for (int k = 0; k < 3; ++k) {
+        if ((st = cuda_check(cudaMemcpy(p.data() + (size_t)k * n, C.point[g] + k * C.cap, sizeof(double) * n, cudaMemcpyDeviceToHost), "download"))) return st;
+        if ((st = cuda_check(cudaMemcpy(l.data() + (size_t)k * n, C.lam[g] + k * C.cap, sizeof(double) * n, cudaMemcpyDeviceToHost), "download"))) return st;
+        if ((st = cuda_check(cudaMemcpy(nn.data() + (size_t)k * n, C.dir + k * C.cap, sizeof(double) * n, cudaMemcpyDeviceToHost), "download"))) return st;
+    }
+    for (int c = 0; c < n; ++c) {
+        if (ia) ia[c] = (int32_t)(keys[c] >> 32);
+        if (ib) ib[c] = (int32_t)(keys[c] & 0xffffffffu);
+        for (int k = 0; k < 3; ++k) {
+            if (point) point[3 * (size_t)c + k] = p[(size_t)k * n + c];
+            if (lambda) lambda[3 * (size_t)c + k] = l[(size_t)k * n + c];
+            if (normal) normal[3 * (size_t)c + k] = nn[(size_t)k * n + c];
+        }
+    }
+    return CDX_OK;
+}
+
+void Engine::fill_stats(cdx_stats* s) {
+    std::memset(s, 0, sizeof(*s));
+    s->steps = steps;
+    s->num_contacts = prev_count;
+    s->num_rows = last_rows;
+    s->iterations = last_iters;
+    s->reallocations = reallocations;
+    s->residual = last_res_final;
+    s->residual_last = last_res;
+    s->ms_collision = ms[0];
+    s->ms_setup = ms[1];
+    s->ms_solve = ms[2];
+    s->ms_integrate = ms[3];
+    s->solve_bytes_per_iter = solve_bytes_per_iter();
+    s->kernel_launches = launches;
+}
+
+double Engine::solve_bytes_per_iter() const {
+    // algorithmic bytes of one sweep: per contact the rows' RW coefficients (27 words), the bias (3),
+    // mu (1), lambda read+write (6), the directions and lever products read by the W^T gather
+    // (9 + 9 per side counted once: 27) and the increments written and read (6), two indices;
+    // per body x read+write (12) and 1/M (2)
+    if (cfg.gpu_precision == CDX_PRECISION_SPLIT) return split_bytes_per_iter();
+    const double w = 8.0;
+    return (double)prev_count * ((27 + 3 + 1 + 6 + 27 + 6) * w + 8.0) + (double)sc.N * (14 * w);
+}

@@ -1,0 +1,88 @@
+// Host engine state (one per cdx_ctx).
+#pragma once
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/cdx.h"
+#include "cdx_internal.h"
+
+namespace cdx {
+const char* status_name(int st);
+struct SplitState;
+}  // namespace cdx
+
+struct Engine {
+    cdx_config cfg{};
+    std::string err;
+    cudaStream_t stream = nullptr;
+    bool loaded = false;
+    bool timing = false;
+    cdx::Scene sc;
+    cdx::Grid grid{};
+    double rmax = 0;
+    std::vector<int32_t> h_scene_body_start, h_scene_static_start;
+    std::vector<void*> owned;
+
+    double* rhs = nullptr;
+    double* x = nullptr;
+    uint32_t *cell_key_in = nullptr, *cell_val_in = nullptr, *cell_key_out = nullptr, *cell_val_out = nullptr;
+    int32_t *cell_start = nullptr, *cell_end = nullptr;
+    int32_t *sflags = nullptr, *spos = nullptr, *pcount = nullptr, *poff = nullptr;
+    int32_t *isfl = nullptr, *flscan = nullptr;
+    cdx::Contacts C;
+    cdx::Incidence inc;
+    cdx::DevScalars* ds = nullptr;
+    cdx::DevScalars* hs = nullptr;  // pinned mirror
+    void* tmp = nullptr;
+    size_t tmp_bytes = 0;
+    int nc = 0, prev_count = 0, gen = 0;
+    int last_iters = 0, last_rows = 0;
+    double last_res = 0, last_res_final = 0;
+    int64_t steps = 0;
+    int64_t launches = 0;
+    int reallocations = 0;
+    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    double ms[4] = {0, 0, 0, 0};
+
+    bool trace_next = false, trace_done_seen = false;
+    int trace_rows = 0;
+    double* trace_dev = nullptr;
+    std::vector<double> trace_buf;
+
+    cdx::SplitState* split = nullptr;
+
+    ~Engine();
+    int fail(int st, const std::string& msg);
+    int cuda_check(cudaError_t e, const char* where);
+    int dalloc(void** p, size_t bytes, const char* what);
+    void dfree(void* p);
+    int init(const cdx_config& c);
+    int load_scene(const cdx_scene& s);
+    int ensure_tmp(int64_t n);
+    int ensure_contacts(int64_t need);
+    int collide64();
+    int setup64();
+    int solve64();
+    int step64();
+    int nfl_rows();
+    int step(int nsteps);
+    int get_state(double* pos, double* quat, double* vel, double* omega);
+    int set_state(const double* pos, const double* quat, const double* vel, const double* omega);
+    int get_contacts(int32_t* ia, int32_t* ib, double* point, double* lambda, double* normal, int32_t* count);
+    void fill_stats(cdx_stats* s);
+    double solve_bytes_per_iter() const;
+
+    // split-precision form (engine_split.cpp)
+    int step_split();
+    void destroy_split();
+    int sync_state_to_fp64();
+    int mark_state_changed();
+    int get_contacts_split(int32_t* ia, int32_t* ib, double* point, double* lambda, double* normal, int32_t* count);
+    double split_bytes_per_iter() const;
+};
+
+struct cdx_ctx {
+    Engine eng;
+};

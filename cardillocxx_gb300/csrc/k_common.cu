@@ -1,0 +1,75 @@
+// Shared device building blocks: uniform-grid cell keys and cell ranges (the broad phase that
+// replaces coal's dynamic AABB tree, collision_coal.cpp:247-270,423-431), and the radix sort /
+// exclusive scan used for the grid, the contact offsets and the W^T incidence lists.
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
+
+#include "cdx_internal.h"
+
+namespace cdx {
+
+namespace {
+constexpr int NT = 256;
+inline int nblk(int64_t n, int nt = NT) { return (int)((n + nt - 1) / nt); }
+
+__global__ void k_cell_keys(Scene sc, Grid g, uint32_t* keys, uint32_t* vals) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sc.N) return;
+    const double p[3] = {sc.bf(BF_PX)[i], sc.bf(BF_PY)[i], sc.bf(BF_PZ)[i]};
+    int ci[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        double f = floor((p[k] - g.lo[k]) / g.cell);
+        if (!(f >= 0.0)) f = 0.0;
+        if (f > (double)(g.dim[k] - 1)) f = (double)(g.dim[k] - 1);
+        ci[k] = (int)f;
+    }
+    keys[i] = (uint32_t)(((int64_t)ci[2] * g.dim[1] + ci[1]) * g.dim[0] + ci[0]);
+    vals[i] = (uint32_t)i;
+}
+
+// start[k]/end[k] of each key present in a sorted key array (absent keys keep their cleared value)
+__global__ void k_ranges(const uint32_t* keys, int64_t n, int32_t* start, int32_t* end) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const uint32_t k = keys[p];
+    if (p == 0 || keys[p - 1] != k) start[k] = (int32_t)p;
+    if (p == n - 1 || keys[p + 1] != k) end[k] = (int32_t)(p + 1);
+}
+}  // namespace
+
+size_t scan_temp_bytes(int64_t n) {
+    size_t b = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, b, (const int32_t*)nullptr, (int32_t*)nullptr, (int)n);
+    return b;
+}
+
+size_t sort_temp_bytes(int64_t n) {
+    size_t b = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, b, (const uint32_t*)nullptr, (uint32_t*)nullptr,
+                                    (const uint32_t*)nullptr, (uint32_t*)nullptr, (int)n, 0, 32);
+    return b;
+}
+
+cudaError_t exclusive_scan(void* tmp, size_t tmp_bytes, const int32_t* in, int32_t* out, int64_t n, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    return cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, in, out, (int)n, s);
+}
+
+cudaError_t sort_pairs(void* tmp, size_t tmp_bytes, const uint32_t* kin, uint32_t* kout, const uint32_t* vin,
+                       uint32_t* vout, int64_t n, int end_bit, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    return cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, kin, kout, vin, vout, (int)n, 0, end_bit, s);
+}
+
+void launch_cell_keys(const Scene& sc, const Grid& g, uint32_t* keys, uint32_t* vals, cudaStream_t s) {
+    if (sc.N == 0) return;
+    k_cell_keys<<<nblk(sc.N), NT, 0, s>>>(sc, g, keys, vals);
+}
+
+void launch_ranges(const uint32_t* sorted_keys, int64_t n, int32_t* start, int32_t* end, cudaStream_t s) {
+    if (n <= 0) return;
+    k_ranges<<<nblk(n), NT, 0, s>>>(sorted_keys, n, start, end);
+}
+
+}  // namespace cdx

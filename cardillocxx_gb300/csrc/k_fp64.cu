@@ -1,0 +1,801 @@
+// Plain FP64 method: collision, contact setup, projected Jacobi and Moreau drift on the GPU.
+//
+// Compiled with --fmad=false. Every kernel restates one stage of the reference's step with the
+// same operation order as the CPU oracle, so the plain method is bit-identical to it:
+//   k_rhs64           PjAssembler::rhs (pj_assembler.cpp:127-170), World forces (world.cpp:113-173)
+//   k_drift64         IntegrationBase::explicitPositionUpdate (integration_base.cpp:6-30)
+//   k_*_flags/count/write64  coal narrow phase + makeContact (collision_coal.cpp:112-163,405-548)
+//   k_contact_setup64 rebuildW_ (dynamics_assembler.cpp:211-332), build_workspace + rdiag_sparse
+//                     (projected_jacobi.cpp:316-369,57-69), warm start (contact_tracker.cpp:43-72)
+//   k_xinit64         x0 = S^-1 (rhs + W^T p) (projected_jacobi.cpp:361-363)
+//   k_sweep_contact64 pj_sweep's RW x + bias, project (projected_jacobi.cpp:100-131)
+//   k_sweep_body64    pj_sweep's x += S^-1 W^T dlambda (projected_jacobi.cpp:134-137)
+// W is never formed: each contact keeps its three directions and body-frame lever products, W^T
+// is applied as a per-body gather over the body's incidence list in solver row order.
+#include <cstdio>
+
+#include "cdx_internal.h"
+#include "fp64_math.cuh"
+
+namespace cdx {
+using namespace f64;
+
+namespace {
+
+constexpr int NT = 256;
+constexpr int MAX_PAIR = 64;  // touching neighbours j > i per sphere
+inline int nblk(int64_t n, int nt = NT) { return (int)((n + nt - 1) / nt); }
+
+__device__ __forceinline__ void cell_of(const Grid& g, double x, double y, double z, int* ci) {
+    const double p[3] = {x, y, z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        double f = floor((p[k] - g.lo[k]) / g.cell);
+        if (!(f >= 0.0)) f = 0.0;  // also maps NaN to 0
+        if (f > (double)(g.dim[k] - 1)) f = (double)(g.dim[k] - 1);
+        ci[k] = (int)f;
+    }
+}
+
+struct Geom {
+    double p1[3], p2[3], nraw[3], xa[3];
+};
+
+// coal::Halfspace {x : n.x <= d} (shape 1) against a sphere (shape 2), or the inner wall of a drum.
+__device__ __forceinline__ bool static_geom(const Scene& sc, int s, const double* xb, double rb, double margin,
+                                            Geom& g) {
+    const double u[3] = {sc.sf(SF_DX)[s], sc.sf(SF_DY)[s], sc.sf(SF_DZ)[s]};
+    g.xa[0] = sc.sf(SF_PX)[s];
+    g.xa[1] = sc.sf(SF_PY)[s];
+    g.xa[2] = sc.sf(SF_PZ)[s];
+    if (sc.static_kind[s] == 0) {
+        const double sdist = dot3(u, xb) - sc.sf(SF_D)[s];
+        const double dist = sdist - rb;
+        if (!(dist <= margin)) return false;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            g.p1[k] = xb[k] - sdist * u[k];
+            g.p2[k] = xb[k] - rb * u[k];
+            g.nraw[k] = u[k];
+        }
+        return true;
+    }
+    const double R = sc.sf(SF_RAD)[s];
+    double rel[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) rel[k] = xb[k] - g.xa[k];
+    const double ax = dot3(rel, u);
+    double perp[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) perp[k] = rel[k] - ax * u[k];
+    const double rho = norm3(perp);
+    const double dist = (R - rho) - rb;
+    if (!(dist <= margin)) return false;
+    double e[3] = {0, 0, 0};
+    if (rho > 0.0) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) e[k] = perp[k] / rho;
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        g.p1[k] = (g.xa[k] + ax * u[k]) + R * e[k];
+        g.p2[k] = xb[k] + rb * e[k];
+        g.nraw[k] = -e[k];
+    }
+    return true;
+}
+
+// sphere (A, lower index) against sphere (B)
+__device__ __forceinline__ bool pair_geom(const double* xA, double ra, const double* xb, double rb, double margin,
+                                          Geom& g) {
+    double d[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) d[k] = xb[k] - xA[k];
+    const double dl = norm3(d);
+    const double dist = (dl - ra) - rb;
+    if (!(dist <= margin)) return false;
+    double nn[3] = {0, 0, 0};
+    if (dl > 0.0) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) nn[k] = d[k] / dl;
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        g.p1[k] = xA[k] + ra * nn[k];
+        g.p2[k] = xb[k] - rb * nn[k];
+        g.nraw[k] = nn[k];
+        g.xa[k] = xA[k];
+    }
+    return true;
+}
+
+__device__ __forceinline__ bool pair_touch(const double* xA, double ra, const double* xb, double rb, double margin) {
+    // cheap exact-safe reject: far pairs cannot pass the exact test below
+    const double dx = xb[0] - xA[0], dy = xb[1] - xA[1], dz = xb[2] - xA[2];
+    const double lim = (ra + rb) * 1.000001 + fabs(margin) + 1e-300;
+    if (dx * dx + dy * dy + dz * dz > lim * lim) return false;
+    Geom g;
+    return pair_geom(xA, ra, xb, rb, margin, g);
+}
+
+// makeContact: sanitise points, normal with fallbacks, Frisvad frame, midpoint.
+__device__ __forceinline__ void finish_contact(Geom& g, const double* xb, double* n, double* t1, double* t2,
+                                               double* point) {
+    if (!finite3(g.p1)) {
+        if (finite3(g.p2)) { for (int k = 0; k < 3; ++k) g.p1[k] = g.p2[k]; }
+        else { for (int k = 0; k < 3; ++k) g.p1[k] = g.xa[k]; }
+    }
+    if (!finite3(g.p2)) {
+        if (finite3(g.p1)) { for (int k = 0; k < 3; ++k) g.p2[k] = g.p1[k]; }
+        else { for (int k = 0; k < 3; ++k) g.p2[k] = xb[k]; }
+    }
+    const double nlen = norm3(g.nraw);
+    if (nlen > 0.0 && isfinite(nlen)) {
+        for (int k = 0; k < 3; ++k) n[k] = g.nraw[k] / nlen;
+    } else {
+        double f[3];
+        for (int k = 0; k < 3; ++k) f[k] = g.p2[k] - g.p1[k];
+        double fl = norm3(f);
+        if (!(fl > 0.0) || !isfinite(fl)) {
+            for (int k = 0; k < 3; ++k) f[k] = xb[k] - g.xa[k];
+            fl = norm3(f);
+        }
+        if (fl > 0.0 && isfinite(fl)) { for (int k = 0; k < 3; ++k) n[k] = f[k] / fl; }
+        else { n[0] = 0; n[1] = 0; n[2] = 1; }
+    }
+    tangent_frame(n, t1, t2);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) point[k] = (g.p1[k] + g.p2[k]) * 0.5;
+}
+
+__device__ __forceinline__ void write_contact(const Scene& sc, Contacts& C, int gen, int64_t c, int a_code, int b,
+                                              Geom& g, const double* xb, int combine, int friction_enable) {
+    double n[3], t1[3], t2[3], p[3];
+    finish_contact(g, xb, n, t1, t2, p);
+    const int64_t cap = C.cap;
+    C.a[c] = a_code;
+    C.b[c] = b;
+    const uint32_t ida = a_code >= 0 ? (uint32_t)(sc.S + a_code) : (uint32_t)(-a_code - 1);
+    const uint32_t idb = (uint32_t)(sc.S + b);
+    C.key[gen][c] = ((unsigned long long)ida << 32) | idb;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        C.point[gen][k * cap + c] = p[k];
+        C.dir[(0 + k) * cap + c] = n[k];
+        C.dir[(3 + k) * cap + c] = t1[k];
+        C.dir[(6 + k) * cap + c] = t2[k];
+    }
+    double muA, rnA, rtA;
+    if (a_code >= 0) {
+        muA = sc.bf(BF_MU)[a_code];
+        rnA = sc.bf(BF_RN)[a_code];
+        rtA = sc.bf(BF_RT)[a_code];
+    } else {
+        const int s = -a_code - 1;
+        muA = sc.sf(SF_MU)[s];
+        rnA = sc.sf(SF_RN)[s];
+        rtA = sc.sf(SF_RT)[s];
+    }
+    const double mu = combine_mu(combine, muA, sc.bf(BF_MU)[b]);
+    C.mu[c] = mu;
+    C.eN[c] = smin(smax(0.0, rnA), smax(0.0, sc.bf(BF_RN)[b]));
+    C.eT[c] = smin(smax(0.0, rtA), smax(0.0, sc.bf(BF_RT)[b]));
+    C.flags[c] = (friction_enable && mu > 0.0) ? CF_FRICTIONAL : 0;
+}
+
+__global__ void k_rhs64(Scene sc, double dt, double g0, double g1, double g2, double* rhs) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sc.N) return;
+    const int N = sc.N;
+    const double w[3] = {sc.bf(BF_WX)[i], sc.bf(BF_WY)[i], sc.bf(BF_WZ)[i]};
+    const double v[3] = {sc.bf(BF_VX)[i], sc.bf(BF_VY)[i], sc.bf(BF_VZ)[i]};
+    const double I = sc.bf(BF_INERTIA)[i], m = sc.bf(BF_MASS)[i];
+    const double Ml = sc.bf(BF_ML)[i], Ma = sc.bf(BF_MA)[i];
+    const double g[3] = {g0, g1, g2};
+    const double Iw[3] = {I * w[0], I * w[1], I * w[2]};
+    double c[3];
+    cross3(w, Iw, c);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const double fext = m * g[k];
+        rhs[(size_t)k * N + i] = (Ml * v[k] + dt * fext) + dt * 0.0;
+        rhs[(size_t)(3 + k) * N + i] = (Ma * w[k] + dt * 0.0) + dt * (-c[k]);
+    }
+}
+
+__global__ void k_drift64(Scene sc, double h, int compute_R) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < sc.N) {
+        double x[3] = {sc.bf(BF_PX)[i], sc.bf(BF_PY)[i], sc.bf(BF_PZ)[i]};
+        double q[4] = {sc.bf(BF_QX)[i], sc.bf(BF_QY)[i], sc.bf(BF_QZ)[i], sc.bf(BF_QW)[i]};
+        const double v[3] = {sc.bf(BF_VX)[i], sc.bf(BF_VY)[i], sc.bf(BF_VZ)[i]};
+        const double w[3] = {sc.bf(BF_WX)[i], sc.bf(BF_WY)[i], sc.bf(BF_WZ)[i]};
+        drift(x, q, v, w, h);
+        sc.bf(BF_PX)[i] = x[0]; sc.bf(BF_PY)[i] = x[1]; sc.bf(BF_PZ)[i] = x[2];
+        sc.bf(BF_QX)[i] = q[0]; sc.bf(BF_QY)[i] = q[1]; sc.bf(BF_QZ)[i] = q[2]; sc.bf(BF_QW)[i] = q[3];
+        if (compute_R) {
+            double R[9];
+            rotmat(q, R);
+#pragma unroll
+            for (int k = 0; k < 9; ++k) sc.bf(BF_R0 + k)[i] = R[k];
+        }
+    } else if (i < sc.N + sc.S) {
+        const int s = i - sc.N;
+        double x[3] = {sc.sf(SF_PX)[s], sc.sf(SF_PY)[s], sc.sf(SF_PZ)[s]};
+        double q[4] = {sc.sf(SF_QX)[s], sc.sf(SF_QY)[s], sc.sf(SF_QZ)[s], sc.sf(SF_QW)[s]};
+        const double v[3] = {sc.sf(SF_VX)[s], sc.sf(SF_VY)[s], sc.sf(SF_VZ)[s]};
+        const double w[3] = {sc.sf(SF_WX)[s], sc.sf(SF_WY)[s], sc.sf(SF_WZ)[s]};
+        drift(x, q, v, w, h);
+        sc.sf(SF_PX)[s] = x[0]; sc.sf(SF_PY)[s] = x[1]; sc.sf(SF_PZ)[s] = x[2];
+        sc.sf(SF_QX)[s] = q[0]; sc.sf(SF_QY)[s] = q[1]; sc.sf(SF_QZ)[s] = q[2]; sc.sf(SF_QW)[s] = q[3];
+        if (compute_R) {
+            double R[9];
+            rotmat(q, R);
+#pragma unroll
+            for (int k = 0; k < 9; ++k) sc.sf(SF_R0 + k)[s] = R[k];
+        }
+    }
+}
+
+// flags laid out per scene as [static slot l][sphere within scene], so an exclusive scan yields
+// positions in (static id, sphere id) order
+__global__ void k_static_flags64(Scene sc, double margin, int32_t* flags) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sc.N) return;
+    const int s = sc.body_scene[i];
+    const int b0 = sc.scene_body_start[s], ns_b = sc.scene_body_start[s + 1] - b0;
+    const int st0 = sc.scene_static_start[s], nst = sc.scene_static_start[s + 1] - st0;
+    const double xb[3] = {sc.bf(BF_PX)[i], sc.bf(BF_PY)[i], sc.bf(BF_PZ)[i]};
+    const double rb = sc.bf(BF_RAD)[i];
+    const int L = sc.max_statics;
+    for (int l = 0; l < L; ++l) {
+        int f = 0;
+        if (l < nst) {
+            Geom g;
+            f = static_geom(sc, st0 + l, xb, rb, margin, g) ? 1 : 0;
+        }
+        flags[(size_t)b0 * L + (size_t)l * ns_b + (i - b0)] = f;
+    }
+}
+
+__global__ void k_static_write64(Scene sc, double margin, const int32_t* flags, const int32_t* pos, Contacts C,
+                                 int gen, int combine, int friction_enable) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sc.N) return;
+    const int s = sc.body_scene[i];
+    const int b0 = sc.scene_body_start[s], ns_b = sc.scene_body_start[s + 1] - b0;
+    const int st0 = sc.scene_static_start[s], nst = sc.scene_static_start[s + 1] - st0;
+    const double xb[3] = {sc.bf(BF_PX)[i], sc.bf(BF_PY)[i], sc.bf(BF_PZ)[i]};
+    const double rb = sc.bf(BF_RAD)[i];
+    const int L = sc.max_statics;
+    for (int l = 0; l < nst && l < L; ++l) {
+        const size_t slot = (size_t)b0 * L + (size_t)l * ns_b + (i - b0);
+        if (!flags[slot]) continue;
+        Geom g;
+        static_geom(sc, st0 + l, xb, rb, margin, g);
+        write_contact(sc, C, gen, pos[slot], -(st0 + l) - 1, i, g, xb, combine, friction_enable);
+    }
+}
+
+template <bool WRITE>
+__global__ void k_pairs64(Scene sc, Grid gr, const uint32_t* cell_body, const int32_t* cell_start,
+                          const int32_t* cell_end, double margin, int32_t* counts, const int32_t* offsets,
+                          int32_t base, Contacts C, int gen, int combine, int friction_enable, DevScalars* ds) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sc.N) return;
+    const double xi[3] = {sc.bf(BF_PX)[i], sc.bf(BF_PY)[i], sc.bf(BF_PZ)[i]};
+    const double ri = sc.bf(BF_RAD)[i];
+    const int si = sc.body_scene[i];
+    int ci[3];
+    cell_of(gr, xi[0], xi[1], xi[2], ci);
+    int list[MAX_PAIR];
+    int cnt = 0;
+    for (int dz = -1; dz <= 1; ++dz) {
+        const int z = ci[2] + dz;
+        if (z < 0 || z >= gr.dim[2]) continue;
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int y = ci[1] + dy;
+            if (y < 0 || y >= gr.dim[1]) continue;
+            for (int dx = -1; dx <= 1; ++dx) {
+                const int x = ci[0] + dx;
+                if (x < 0 || x >= gr.dim[0]) continue;
+                const int64_t cell = ((int64_t)z * gr.dim[1] + y) * gr.dim[0] + x;
+                const int e = cell_end[cell];
+                for (int p = cell_start[cell]; p < e; ++p) {
+                    const int j = (int)cell_body[p];
+                    if (j <= i || sc.body_scene[j] != si) continue;
+                    const double xj[3] = {sc.bf(BF_PX)[j], sc.bf(BF_PY)[j], sc.bf(BF_PZ)[j]};
+                    if (!pair_touch(xi, ri, xj, sc.bf(BF_RAD)[j], margin)) continue;
+                    if (WRITE) {
+                        if (cnt < MAX_PAIR) list[cnt] = j;
+                    }
+                    ++cnt;
+                }
+            }
+        }
+    }
+    if (!WRITE) {
+        counts[i] = cnt;
+        if (cnt > MAX_PAIR) atomicExch(&ds->overflow, 1);
+        return;
+    }
+    if (cnt > MAX_PAIR) cnt = MAX_PAIR;
+    // canonical order: increasing partner index
+    for (int a = 1; a < cnt; ++a) {
+        const int v = list[a];
+        int b = a - 1;
+        while (b >= 0 && list[b] > v) {
+            list[b + 1] = list[b];
+            --b;
+        }
+        list[b + 1] = v;
+    }
+    const int64_t o = (int64_t)base + offsets[i];
+    for (int k = 0; k < cnt; ++k) {
+        const int j = list[k];
+        const double xj[3] = {sc.bf(BF_PX)[j], sc.bf(BF_PY)[j], sc.bf(BF_PZ)[j]};
+        Geom g;
+        pair_geom(xi, ri, xj, sc.bf(BF_RAD)[j], margin, g);
+        write_contact(sc, C, gen, o + k, i, j, g, xj, combine, friction_enable);
+    }
+}
+
+__device__ __forceinline__ void body_frame(const Scene& sc, int a_code, double* R, double* x) {
+    if (a_code >= 0) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) R[k] = sc.bf(BF_R0 + k)[a_code];
+        x[0] = sc.bf(BF_PX)[a_code]; x[1] = sc.bf(BF_PY)[a_code]; x[2] = sc.bf(BF_PZ)[a_code];
+    } else {
+        const int s = -a_code - 1;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) R[k] = sc.sf(SF_R0 + k)[s];
+        x[0] = sc.sf(SF_PX)[s]; x[1] = sc.sf(SF_PY)[s]; x[2] = sc.sf(SF_PZ)[s];
+    }
+}
+
+__global__ void k_contact_setup64(Scene sc, Contacts C, int gen, int nc, int prev_count, double alpha,
+                                  double match2, int warmstart) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    const int64_t cap = C.cap;
+    const int a = C.a[c], b = C.b[c];
+    const bool fr = (C.flags[c] & CF_FRICTIONAL) != 0;
+    double d[9], pt[3];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) d[k] = C.dir[k * cap + c];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) pt[k] = C.point[gen][k * cap + c];
+    // body-frame lever products (transform::point / transform::direction + buildContactRowByDof)
+    double cA[9], cB[9];
+    for (int side = 0; side < 2; ++side) {
+        double R[9], x[3];
+        body_frame(sc, side == 0 ? a : b, R, x);
+        double rel[3], rb[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) rel[k] = pt[k] - x[k];
+        matTvec(R, rel, rb);
+        double* cc = side == 0 ? cA : cB;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            double db[3];
+            matTvec(R, &d[3 * r], db);
+            cross3(rb, db, &cc[3 * r]);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        C.cA[k * cap + c] = cA[k];
+        C.cB[k * cap + c] = cB[k];
+    }
+    // static side velocity: contact_v_vec[row] += row . [v_world, omega_body]  (sign -1 on side A)
+    double cbv[3] = {0.0, 0.0, 0.0};
+    if (a < 0) {
+        const int s = -a - 1;
+        const double vs[3] = {sc.sf(SF_VX)[s], sc.sf(SF_VY)[s], sc.sf(SF_VZ)[s]};
+        const double ws[3] = {sc.sf(SF_WX)[s], sc.sf(SF_WY)[s], sc.sf(SF_WZ)[s]};
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            double acc = (-d[3 * r]) * vs[0];
+            acc = acc + (-d[3 * r + 1]) * vs[1];
+            acc = acc + (-d[3 * r + 2]) * vs[2];
+            acc = acc + (-cA[3 * r]) * ws[0];
+            acc = acc + (-cA[3 * r + 1]) * ws[1];
+            acc = acc + (-cA[3 * r + 2]) * ws[2];
+            cbv[r] = 0.0 + acc;
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < 3; ++r) C.cb[r * cap + c] = cbv[r];
+    // warm start: same pair in the previous step within collision.match_max_dist
+    double lam0[3] = {0.0, 0.0, 0.0};
+    if (warmstart && prev_count > 0) {
+        const unsigned long long key = C.key[gen][c];
+        const unsigned long long* pk = C.key[gen ^ 1];
+        int lo = 0, hi = prev_count;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (pk[mid] < key) lo = mid + 1;
+            else hi = mid;
+        }
+        if (lo < prev_count && pk[lo] == key) {
+            double dd[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) dd[k] = pt[k] - C.point[gen ^ 1][k * cap + lo];
+            if (dot3(dd, dd) <= match2) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) lam0[k] = C.lam[gen ^ 1][k * cap + lo];
+            }
+        }
+    }
+    if (!fr) { lam0[1] = 0.0; lam0[2] = 0.0; }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) C.lam[gen][k * cap + c] = lam0[k];
+    // rows: contact velocity, Delassus diagonal, R = alpha / D, RW and R-scaled bias
+    double vA[6] = {0, 0, 0, 0, 0, 0}, vB[6], mA[6] = {0, 0, 0, 0, 0, 0}, mB[6];
+    if (a >= 0) {
+        vA[0] = sc.bf(BF_VX)[a]; vA[1] = sc.bf(BF_VY)[a]; vA[2] = sc.bf(BF_VZ)[a];
+        vA[3] = sc.bf(BF_WX)[a]; vA[4] = sc.bf(BF_WY)[a]; vA[5] = sc.bf(BF_WZ)[a];
+        const double ml = sc.bf(BF_MINVL)[a], ma = sc.bf(BF_MINVA)[a];
+        mA[0] = ml; mA[1] = ml; mA[2] = ml; mA[3] = ma; mA[4] = ma; mA[5] = ma;
+    }
+    vB[0] = sc.bf(BF_VX)[b]; vB[1] = sc.bf(BF_VY)[b]; vB[2] = sc.bf(BF_VZ)[b];
+    vB[3] = sc.bf(BF_WX)[b]; vB[4] = sc.bf(BF_WY)[b]; vB[5] = sc.bf(BF_WZ)[b];
+    {
+        const double ml = sc.bf(BF_MINVL)[b], ma = sc.bf(BF_MINVA)[b];
+        mB[0] = ml; mB[1] = ml; mB[2] = ml; mB[3] = ma; mB[4] = ma; mB[5] = ma;
+    }
+    const int nr = fr ? 3 : 1;
+    for (int r = 0; r < 3; ++r) {
+        if (r >= nr) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                C.rd[(3 * r + k) * cap + c] = 0.0;
+                C.rcA[(3 * r + k) * cap + c] = 0.0;
+                C.rcB[(3 * r + k) * cap + c] = 0.0;
+            }
+            C.biasR[r * cap + c] = 0.0;
+            continue;
+        }
+        int ne = 0;
+        double val[12], vel[12], mi[12];
+        if (a >= 0) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) { val[ne] = -d[3 * r + k]; vel[ne] = vA[k]; mi[ne] = mA[k]; ++ne; }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) { val[ne] = -cA[3 * r + k]; vel[ne] = vA[3 + k]; mi[ne] = mA[3 + k]; ++ne; }
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) { val[ne] = d[3 * r + k]; vel[ne] = vB[k]; mi[ne] = mB[k]; ++ne; }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) { val[ne] = cB[3 * r + k]; vel[ne] = vB[3 + k]; mi[ne] = mB[3 + k]; ++ne; }
+        double vp = 0.0, D = 0.0;
+        for (int k = 0; k < ne; ++k) vp = vp + val[k] * vel[k];
+        vp = vp + cbv[r];
+        const double e = r == 0 ? C.eN[c] : C.eT[c];
+        const double bias = cbv[r] + e * vp;
+        for (int k = 0; k < ne; ++k) D = D + (val[k] * val[k]) * mi[k];
+        const double Rr = (D > 0.0) ? (alpha / D) : 0.0;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            C.rd[(3 * r + k) * cap + c] = Rr * d[3 * r + k];
+            C.rcA[(3 * r + k) * cap + c] = Rr * cA[3 * r + k];
+            C.rcB[(3 * r + k) * cap + c] = Rr * cB[3 * r + k];
+        }
+        C.biasR[r * cap + c] = Rr * bias;
+    }
+}
+
+__global__ void k_frictionless_flags(Contacts C, int nc, int32_t* isfl) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    isfl[c] = (C.flags[c] & CF_FRICTIONAL) ? 0 : 1;
+}
+
+// solver row order: frictionless contacts first, then frictional ones, each in canonical order
+// (rebuildW_'s two passes, dynamics_assembler.cpp:236-324); incidence list input in that order
+__global__ void k_rank_incidence(int N, Contacts C, int nc, const int32_t* fl_scan, const int32_t* isfl,
+                                 Incidence inc) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    const int nfl = fl_scan[nc - 1] + isfl[nc - 1];
+    const int rank = isfl[c] ? fl_scan[c] : nfl + (c - fl_scan[c]);
+    C.rank[c] = rank;
+    const int a = C.a[c];
+    inc.key_in[2 * (size_t)rank] = a >= 0 ? (uint32_t)a : (uint32_t)N;
+    inc.val_in[2 * (size_t)rank] = (uint32_t)(2 * c);
+    inc.key_in[2 * (size_t)rank + 1] = (uint32_t)C.b[c];
+    inc.val_in[2 * (size_t)rank + 1] = (uint32_t)(2 * c + 1);
+}
+
+// body gather of W^T y over the incidence list (rows in solver order); acc is accumulated in place
+template <int LAMGEN>
+__device__ __forceinline__ void gather_wt(const Contacts& C, const double* y, const Incidence& inc, int i,
+                                          double* acc) {
+    const int64_t cap = C.cap;
+    const int e = inc.end[i];
+    for (int p = inc.start[i]; p < e; ++p) {
+        const uint32_t code = inc.val_out[p];
+        const int c = (int)(code >> 1);
+        const bool sideB = code & 1u;
+        const double s = sideB ? 1.0 : -1.0;
+        const double* cx = sideB ? C.cB : C.cA;
+        const int nr = (C.flags[c] & CF_FRICTIONAL) ? 3 : 1;
+        for (int r = 0; r < nr; ++r) {
+            const double yr = y[r * cap + c];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) acc[k] = acc[k] + (s * C.dir[(3 * r + k) * cap + c]) * yr;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) acc[3 + k] = acc[3 + k] + (s * cx[(3 * r + k) * cap + c]) * yr;
+        }
+    }
+}
+
+__global__ void k_xinit64(Scene sc, Contacts C, int gen, Incidence inc, const double* rhs, double* x) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sc.N) return;
+    const int N = sc.N;
+    double acc[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) acc[k] = rhs[(size_t)k * N + i];
+    gather_wt<0>(C, C.lam[gen], inc, i, acc);
+    const double Ml = sc.bf(BF_ML)[i], Ma = sc.bf(BF_MA)[i];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) x[(size_t)k * N + i] = acc[k] / (k < 3 ? Ml : Ma);
+}
+
+__device__ __forceinline__ void atomic_max_nonneg(unsigned long long* addr, double v) {
+    atomicMax(addr, (unsigned long long)__double_as_longlong(v));
+}
+
+__device__ __forceinline__ double block_max(double v) {
+    __shared__ double sh[32];
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    v = (threadIdx.x < (blockDim.x >> 5)) ? sh[lane] : 0.0;
+    if (wid == 0)
+        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+__device__ __forceinline__ double block_sum(double v) {
+    __shared__ double sh[32];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    v = (threadIdx.x < (blockDim.x >> 5)) ? sh[lane] : 0.0;
+    if (wid == 0)
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__global__ void k_sweep_contact64(Scene sc, Contacts C, int gen, int nc, const double* x, DevScalars* ds,
+                                  int dry) {
+    if (!dry && *(volatile int32_t*)&ds->done) return;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    double maxd = 0.0, maxl = 0.0;
+    if (c < nc) {
+        const int64_t cap = C.cap;
+        const int N = sc.N;
+        const int a = C.a[c], b = C.b[c];
+        const bool fr = (C.flags[c] & CF_FRICTIONAL) != 0;
+        const int nr = fr ? 3 : 1;
+        double xA[6], xB[6];
+        if (a >= 0) {
+#pragma unroll
+            for (int k = 0; k < 6; ++k) xA[k] = x[(size_t)k * N + a];
+        }
+#pragma unroll
+        for (int k = 0; k < 6; ++k) xB[k] = x[(size_t)k * N + b];
+        double* lamp = C.lam[gen];
+        double lold[3], lnew[3];
+        for (int r = 0; r < nr; ++r) {
+            double t = 0.0;
+            if (a >= 0) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) t = t + (-C.rd[(3 * r + k) * cap + c]) * xA[k];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) t = t + (-C.rcA[(3 * r + k) * cap + c]) * xA[3 + k];
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) t = t + C.rd[(3 * r + k) * cap + c] * xB[k];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) t = t + C.rcB[(3 * r + k) * cap + c] * xB[3 + k];
+            const double g = t + C.biasR[r * cap + c];
+            lold[r] = lamp[r * cap + c];
+            lnew[r] = lold[r] - g;
+        }
+        // project (projected_jacobi.cpp:100-119)
+        lnew[0] = smax(lnew[0], 0.0);
+        if (fr) {
+            const double t1 = lnew[1], t2 = lnew[2];
+            const double tn2 = t1 * t1 + t2 * t2;
+            if (tn2 > 0) {
+                const double s = smin(1.0, (C.mu[c] * lnew[0]) / sqrt(tn2));
+                lnew[1] = s * t1;
+                lnew[2] = s * t2;
+            }
+        }
+        double s2 = 0.0;
+        for (int r = 0; r < nr; ++r) {
+            const double dl = lnew[r] - lold[r];
+            s2 = s2 + dl * dl;
+            maxl = smax(maxl, fabs(lold[r]));
+            if (!dry) {
+                lamp[r * cap + c] = lnew[r];
+                C.dlam[r * cap + c] = dl;
+            }
+        }
+        maxd = sqrt(s2);
+    }
+    maxd = block_max(maxd);
+    maxl = block_max(maxl);
+    if (threadIdx.x == 0) {
+        atomic_max_nonneg(&ds->maxd, maxd);
+        atomic_max_nonneg(&ds->maxl, maxl);
+    }
+}
+
+__global__ void k_sweep_body64(Scene sc, Contacts C, Incidence inc, double* x, double tol_abs, double tol_rel,
+                               int want_velres, DevScalars* ds) {
+    if (*(volatile int32_t*)&ds->done) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double part = 0.0;
+    if (i < sc.N) {
+        const int N = sc.N;
+        double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        gather_wt<1>(C, C.dlam, inc, i, acc);
+        const double Ml = sc.bf(BF_ML)[i], Ma = sc.bf(BF_MA)[i];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const double xo = x[(size_t)k * N + i];
+            const double xn = xo + acc[k] / (k < 3 ? Ml : Ma);
+            x[(size_t)k * N + i] = xn;
+            if (want_velres) {
+                const double q = smax(fabs(xn), fabs(xo)) * tol_rel + tol_abs;
+                const double dd = (xn - xo) / q;
+                part = part + dd * dd;
+            }
+        }
+    }
+    if (want_velres) {
+        part = block_sum(part);
+        if (threadIdx.x == 0) atomicAdd(&ds->velres, part);
+    }
+}
+
+__global__ void k_check(DevScalars* ds, int iter, double residual_tol, int nv, int check_vel) {
+    const double maxd = __longlong_as_double((long long)ds->maxd);
+    const double maxl = __longlong_as_double((long long)ds->maxl);
+    const double r = maxd / smax(maxl, 1e-30);
+    if (!ds->done) {
+        ds->res_last = r;
+        ds->iters = iter + 1;
+        bool stop = false;
+        if (check_vel && iter % 10 == 0) {
+            const double vr = 1.0 / sqrt((double)nv) * sqrt(ds->velres);
+            if (vr <= 1) stop = true;
+        }
+        if (residual_tol > 0 && r <= residual_tol) stop = true;
+        if (stop) ds->done = 1;
+    }
+    ds->maxd = 0ull;
+    ds->maxl = 0ull;
+    ds->velres = 0.0;
+}
+
+__global__ void k_final_residual(DevScalars* ds) {
+    const double maxd = __longlong_as_double((long long)ds->maxd);
+    const double maxl = __longlong_as_double((long long)ds->maxl);
+    ds->res_final = maxd / smax(maxl, 1e-30);
+    ds->maxd = 0ull;
+    ds->maxl = 0ull;
+}
+
+__global__ void k_writeback64(Scene sc, const double* x) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sc.N) return;
+    const int N = sc.N;
+    sc.bf(BF_VX)[i] = x[0 * (size_t)N + i];
+    sc.bf(BF_VY)[i] = x[1 * (size_t)N + i];
+    sc.bf(BF_VZ)[i] = x[2 * (size_t)N + i];
+    sc.bf(BF_WX)[i] = x[3 * (size_t)N + i];
+    sc.bf(BF_WY)[i] = x[4 * (size_t)N + i];
+    sc.bf(BF_WZ)[i] = x[5 * (size_t)N + i];
+}
+
+__global__ void k_trace64(Contacts C, int gen, int nc, const int32_t* fl_scan, const int32_t* isfl, double* out) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    const int nfl = fl_scan[nc - 1] + isfl[nc - 1];
+    const int rank = C.rank[c];
+    const int64_t cap = C.cap;
+    if (rank < nfl) {
+        out[rank] = C.lam[gen][c];
+    } else {
+        const int row = nfl + 3 * (rank - nfl);
+        for (int r = 0; r < 3; ++r) out[row + r] = C.lam[gen][r * cap + c];
+    }
+}
+
+}  // namespace
+
+void launch_rhs64(const Scene& sc, double dt, const double* g, double* rhs, cudaStream_t s) {
+    if (sc.N == 0) return;
+    k_rhs64<<<nblk(sc.N), NT, 0, s>>>(sc, dt, g[0], g[1], g[2], rhs);
+}
+void launch_drift64(const Scene& sc, double h, int compute_R, cudaStream_t s) {
+    if (sc.N + sc.S == 0) return;
+    k_drift64<<<nblk(sc.N + sc.S), NT, 0, s>>>(sc, h, compute_R);
+}
+void launch_static_flags64(const Scene& sc, double margin, int32_t* flags, cudaStream_t s) {
+    if (sc.N == 0) return;
+    k_static_flags64<<<nblk(sc.N), NT, 0, s>>>(sc, margin, flags);
+}
+void launch_pair_count64(const Scene& sc, const Grid& g, const uint32_t* cell_body, const int32_t* cell_start,
+                         const int32_t* cell_end, double margin, int32_t* counts, DevScalars* ds, cudaStream_t s) {
+    if (sc.N == 0) return;
+    Contacts dummy;
+    k_pairs64<false><<<nblk(sc.N), NT, 0, s>>>(sc, g, cell_body, cell_start, cell_end, margin, counts, nullptr, 0,
+                                                dummy, 0, 0, 0, ds);
+}
+void launch_static_write64(const Scene& sc, double margin, const int32_t* flags, const int32_t* pos,
+                           Contacts& C, int gen, int combine, int friction_enable, cudaStream_t s) {
+    if (sc.N == 0) return;
+    k_static_write64<<<nblk(sc.N), NT, 0, s>>>(sc, margin, flags, pos, C, gen, combine, friction_enable);
+}
+void launch_pair_write64(const Scene& sc, const Grid& g, const uint32_t* cell_body, const int32_t* cell_start,
+                         const int32_t* cell_end, double margin, const int32_t* offsets, int32_t base,
+                         Contacts& C, int gen, int combine, int friction_enable, DevScalars* ds, cudaStream_t s) {
+    if (sc.N == 0) return;
+    k_pairs64<true><<<nblk(sc.N), NT, 0, s>>>(sc, g, cell_body, cell_start, cell_end, margin, nullptr, offsets, base,
+                                               C, gen, combine, friction_enable, ds);
+}
+void launch_contact_setup64(const Scene& sc, Contacts& C, int gen, int nc, int prev_count, double alpha,
+                            double match2, int warmstart, cudaStream_t s) {
+    if (nc == 0) return;
+    k_contact_setup64<<<nblk(nc), NT, 0, s>>>(sc, C, gen, nc, prev_count, alpha, match2, warmstart);
+}
+void launch_frictionless_flags(const Contacts& C, int nc, int32_t* isfl, cudaStream_t s) {
+    if (nc == 0) return;
+    k_frictionless_flags<<<nblk(nc), NT, 0, s>>>(C, nc, isfl);
+}
+void launch_rank_and_incidence(const Scene& sc, Contacts& C, int nc, const int32_t* fl_scan, const int32_t* isfl,
+                               Incidence& inc, cudaStream_t s) {
+    if (nc == 0) return;
+    k_rank_incidence<<<nblk(nc), NT, 0, s>>>(sc.N, C, nc, fl_scan, isfl, inc);
+}
+void launch_xinit64(const Scene& sc, const Contacts& C, int gen, const Incidence& inc, const double* rhs, double* x,
+                    cudaStream_t s) {
+    if (sc.N == 0) return;
+    k_xinit64<<<nblk(sc.N), NT, 0, s>>>(sc, C, gen, inc, rhs, x);
+}
+void launch_sweep_contact64(const Scene& sc, Contacts& C, int gen, int nc, const double* x, DevScalars* ds, int dry,
+                            cudaStream_t s) {
+    if (nc == 0) return;
+    k_sweep_contact64<<<nblk(nc), NT, 0, s>>>(sc, C, gen, nc, x, ds, dry);
+}
+void launch_sweep_body64(const Scene& sc, const Contacts& C, const Incidence& inc, double* x, double tol_abs,
+                         double tol_rel, int want_velres, DevScalars* ds, cudaStream_t s) {
+    if (sc.N == 0) return;
+    k_sweep_body64<<<nblk(sc.N), NT, 0, s>>>(sc, C, inc, x, tol_abs, tol_rel, want_velres, ds);
+}
+void launch_check(DevScalars* ds, int iter, double residual_tol, int nv, int check_vel, cudaStream_t s) {
+    k_check<<<1, 1, 0, s>>>(ds, iter, residual_tol, nv, check_vel);
+}
+void launch_final_residual(DevScalars* ds, cudaStream_t s) { k_final_residual<<<1, 1, 0, s>>>(ds); }
+void launch_writeback64(const Scene& sc, const double* x, cudaStream_t s) {
+    if (sc.N == 0) return;
+    k_writeback64<<<nblk(sc.N), NT, 0, s>>>(sc, x);
+}
+void launch_trace64(const Contacts& C, int gen, int nc, const int32_t* fl_scan, const int32_t* isfl, double* out,
+                    cudaStream_t s) {
+    if (nc == 0) return;
+    k_trace64<<<nblk(nc), NT, 0, s>>>(C, gen, nc, fl_scan, isfl, out);
+}
+
+}  // namespace cdx

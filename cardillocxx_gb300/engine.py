@@ -1,0 +1,188 @@
+"""Host-side mirror of the reference's engine interface for the contact path.
+
+`Config` keeps the reference's key=value keys (ConfigReader::fromFile, src/config/config.cpp:22-420);
+parsing happens in C++ (cdx_config_set) so the semantics are the library's. `PhysicsEngine`
+wraps one cdx context: load a scene, `step()` (MoreauIntegrator::step, moreau.cpp:6-13), read
+the state back. `pj_solve_csr` is the solver-level drop-in (ProjectedJacobiSolver::solve,
+projected_jacobi.cpp:451-500). Every call goes to the CUDA library; nothing here computes physics.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import CdxConfig, CdxError, CdxScene, CdxStats, dp, ip
+
+
+class Config:
+    """Reference-compatible configuration (pj.*, moreau.*, friction.*, collision.*, sim.*, gpu.*)."""
+
+    def __init__(self, values: dict | None = None):
+        self._c = CdxConfig()
+        _lib.lib().cdx_config_default(C.byref(self._c))
+        for k, v in (values or {}).items():
+            self.set(k, v)
+
+    @classmethod
+    def from_file(cls, path: str) -> "Config":
+        cfg = cls()
+        st = _lib.lib().cdx_config_from_file(path.encode(), C.byref(cfg._c))
+        if st:
+            raise CdxError(st, f"config file {path}")
+        return cfg
+
+    def set(self, key: str, value) -> "Config":
+        if isinstance(value, bool):
+            value = "true" if value else "false"
+        elif isinstance(value, (list, tuple)):
+            value = " ".join(repr(float(v)) for v in value)
+        elif isinstance(value, float):
+            value = repr(value)
+        st = _lib.lib().cdx_config_set(C.byref(self._c), str(key).encode(), str(value).encode())
+        if st:
+            raise CdxError(st, f"config key {key}={value}")
+        return self
+
+    @property
+    def struct(self) -> CdxConfig:
+        return self._c
+
+    def get(self, field: str):
+        v = getattr(self._c, field)
+        return list(v) if field == "sim_gravity" else v
+
+    def to_keys(self) -> dict:
+        """Typed dict of the reference keys (used to configure the CPU oracle identically)."""
+        c = self._c
+        return {
+            "sim.dt": c.sim_dt, "sim.gravity": tuple(c.sim_gravity), "moreau.theta": c.moreau_theta,
+            "friction.enable": bool(c.friction_enable),
+            "friction.combine": {0: "min", 1: "arith", 2: "geom"}[c.friction_combine],
+            "pj.max_iterations": c.pj_max_iterations, "pj.warmstart": bool(c.pj_warmstart),
+            "pj.tol_abs": c.pj_tol_abs, "pj.tol_rel": c.pj_tol_rel, "pj.alpha": c.pj_alpha,
+            "collision.security_margin": c.collision_security_margin,
+            "collision.match_max_dist": c.collision_match_max_dist, "gpu.residual_tol": c.gpu_residual_tol,
+        }
+
+
+def scene_struct(scene: dict) -> tuple[CdxScene, dict]:
+    keep = {k: (np.ascontiguousarray(v) if isinstance(v, np.ndarray) else v) for k, v in scene.items()}
+    s = CdxScene()
+    s.num_bodies = int(keep["pos"].shape[0])
+    for name in ("pos", "quat", "vel", "omega", "radius", "mass", "inertia", "mu", "rest_n", "rest_t"):
+        arr = keep[name]
+        assert arr.dtype == np.float64, name
+        setattr(s, name, dp(arr))
+    s.body_scene = ip(keep.get("body_scene"))
+    s.num_statics = int(keep["static_kind"].shape[0])
+    s.static_kind = ip(keep["static_kind"])
+    for name in ("static_pos", "static_quat", "static_vel", "static_omega", "static_dir", "static_radius",
+                 "static_mu", "static_rest_n", "static_rest_t"):
+        setattr(s, name, dp(keep[name]))
+    s.static_scene = ip(keep.get("static_scene"))
+    s.num_scenes = int(keep.get("num_scenes", 1))
+    return s, keep
+
+
+class PhysicsEngine:
+    """One cdx context on the current CUDA device: the GPU Moreau midpoint step."""
+
+    def __init__(self, cfg: Config | dict | None = None):
+        if not isinstance(cfg, Config):
+            cfg = Config(cfg or {})
+        self.cfg = cfg
+        self.L = _lib.lib()
+        h = C.c_void_p()
+        st = self.L.cdx_create(C.byref(cfg.struct), C.byref(h))
+        self.h = h
+        if st:
+            msg = self.L.cdx_last_error(h).decode() if h else ""
+            self.close()
+            raise CdxError(st, msg)
+        self.N = 0
+
+    def _check(self, st: int):
+        if st:
+            raise CdxError(st, self.L.cdx_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.cdx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def load_scene(self, scene: dict):
+        s, keep = scene_struct(scene)
+        self._check(self.L.cdx_load_scene(self.h, C.byref(s)))
+        self.N = s.num_bodies
+        return self
+
+    def step(self, n: int = 1):
+        self._check(self.L.cdx_step(self.h, int(n)))
+
+    def synchronize(self):
+        self._check(self.L.cdx_synchronize(self.h))
+
+    def set_timing(self, on: bool = True):
+        self._check(self.L.cdx_set_timing(self.h, int(on)))
+
+    def state(self) -> dict:
+        N = self.N
+        pos = np.empty((N, 3)); quat = np.empty((N, 4)); vel = np.empty((N, 3)); om = np.empty((N, 3))
+        self._check(self.L.cdx_get_state(self.h, dp(pos), dp(quat), dp(vel), dp(om)))
+        return {"pos": pos, "quat": quat, "vel": vel, "omega": om}
+
+    def set_state(self, pos=None, quat=None, vel=None, omega=None):
+        conv = [None if a is None else np.ascontiguousarray(a, np.float64) for a in (pos, quat, vel, omega)]
+        self._check(self.L.cdx_set_state(self.h, *[dp(a) for a in conv]))
+
+    def stats(self) -> dict:
+        st = CdxStats()
+        self._check(self.L.cdx_get_stats(self.h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in CdxStats._fields_}
+
+    def contacts(self) -> dict:
+        n = C.c_int32(0)
+        self._check(self.L.cdx_get_contacts(self.h, None, None, None, None, None, C.byref(n)))
+        m = n.value
+        ia = np.empty(m, np.int32); ib = np.empty(m, np.int32)
+        pt = np.empty((m, 3)); lam = np.empty((m, 3)); nrm = np.empty((m, 3))
+        self._check(self.L.cdx_get_contacts(self.h, ip(ia), ip(ib), dp(pt), dp(lam), dp(nrm), C.byref(n)))
+        return {"id_a": ia, "id_b": ib, "point": pt, "lambda": lam, "normal": nrm}
+
+    def set_trace(self, on: bool = True):
+        self._check(self.L.cdx_set_trace(self.h, int(on)))
+
+    def trace(self, nrows: int):
+        n = C.c_int64(0)
+        self._check(self.L.cdx_get_trace(self.h, None, 0, C.byref(n)))
+        out = np.empty(n.value)
+        self._check(self.L.cdx_get_trace(self.h, dp(out), n.value, C.byref(n)))
+        return out.reshape(-1, nrows) if nrows else out
+
+    def stream(self) -> int:
+        return int(self.L.cdx_stream(self.h) or 0)
+
+    def pj_solve_csr(self, row_ptr, col, val, contact_bias, mu, restitution, minv, mdiag, v, f_ext, f_gyro, dt,
+                     alpha, max_iter, tol_abs, tol_rel, lam0, nfl=0):
+        """Solver-level drop-in: ProjectedJacobiSolver::solve with S = diag(M) on host arrays."""
+        row_ptr = np.ascontiguousarray(row_ptr, np.int32)
+        col = np.ascontiguousarray(col, np.int32)
+        arrs = [np.ascontiguousarray(a, np.float64) for a in (val, contact_bias, mu, restitution, minv, mdiag, v,
+                                                              f_ext, f_gyro)]
+        nrows = row_ptr.shape[0] - 1
+        nv = arrs[4].shape[0]
+        lam = np.array(lam0, np.float64, copy=True)
+        x = np.empty(nv)
+        it = C.c_int32(0)
+        self._check(self.L.cdx_pj_solve_csr(self.h, nrows, nv, int(nfl), ip(row_ptr), ip(col),
+                                            *[dp(a) for a in arrs], float(dt), float(alpha), int(max_iter),
+                                            float(tol_abs), float(tol_rel), dp(lam), dp(x), C.byref(it)))
+        return x, lam, it.value

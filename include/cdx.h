@@ -1,0 +1,188 @@
+/*
+ * cdx -- GB300-native contact hot path of CardilloCxx behind a thin C ABI.
+ *
+ * The path is the Moreau midpoint step for sphere scenes: uniform-grid broad phase,
+ * sphere-sphere / sphere-halfspace / sphere-drum narrow phase, projected Jacobi over disk-shaped
+ * Coulomb cones applied matrix-free as G M^-1 G^T, then the velocity and quaternion update.
+ * Kernels are hand-written CUDA for sm_103a; the host side is C++.
+ *
+ * Conventions
+ *   - All functions return an int status (CDX_OK = 0). cdx_last_error(ctx) holds the message.
+ *   - Plain pointers and sizes only. Host arrays passed in are borrowed for the call.
+ *   - Interleaved host layouts: positions/velocities [3*N] (x,y,z per body), quaternions [4*N]
+ *     (x,y,z,w), angular velocities in the body frame (as the reference's C_AngularVelocity3).
+ *   - Entity ids (contacts, warm start): static shapes 0..S-1, then sphere i has id S+i.
+ *   - One context per host thread; each context owns its device memory and one CUDA stream.
+ *   - No call allocates device memory on the per-step path except when the contact buffers
+ *     must grow (reported in cdx_stats.reallocations).
+ */
+#ifndef CDX_H
+#define CDX_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CDX_OK 0
+#define CDX_ERR_ARG 1
+#define CDX_ERR_CUDA 2
+#define CDX_ERR_OVERFLOW 3
+#define CDX_ERR_NONFINITE 4
+#define CDX_ERR_TIMEOUT 5
+#define CDX_ERR_UNSUPPORTED 6
+#define CDX_ERR_STATE 7
+
+#define CDX_PRECISION_FP64 0  /* plain method: FP64 everywhere, bit-reproducible vs the oracle */
+#define CDX_PRECISION_SPLIT 1 /* FP32 contact/Delassus/projection, FP64 state and residual check */
+
+#define CDX_STATIC_HALFSPACE 0
+#define CDX_STATIC_DRUM 1 /* hollow cylinder: spheres touch its inner wall */
+
+/* Engine configuration. Field names follow the reference's config keys
+ * (src/config/config.hpp:12-237, parsed by ConfigReader::fromFile, src/config/config.cpp:22-420).
+ * Keys after the gpu_ prefix are new. */
+typedef struct cdx_config {
+    double sim_dt;                    /* sim.dt */
+    double sim_T;                     /* sim.T */
+    double sim_gravity[3];            /* sim.gravity */
+    double moreau_theta;              /* moreau.theta (0.5 = midpoint) */
+    int32_t moreau_implicit_gyroscopy;/* moreau.implicit_gyroscopy (only 0 is supported) */
+    int32_t friction_enable;          /* friction.enable */
+    int32_t friction_combine;         /* friction.combine: 0 min, 1 arith, 2 geom */
+    double friction_default_mu;       /* friction.default_mu (scene generators) */
+    double restitution_default_normal;     /* restitution.default_normal */
+    double restitution_default_tangential; /* restitution.default_tangential */
+    int32_t pj_max_iterations;        /* pj.max_iterations */
+    int32_t pj_warmstart;             /* pj.warmstart */
+    double pj_tol_abs;                /* pj.tol_abs */
+    double pj_tol_rel;                /* pj.tol_rel */
+    double pj_alpha;                  /* pj.alpha */
+    double pj_relaxation;             /* pj.relaxation (accepted, unused by PJ as in the reference) */
+    int32_t solver_type;              /* solver.type: 0 projected_jacobi (the only one here) */
+    double collision_security_margin; /* collision.security_margin */
+    double collision_match_max_dist;  /* collision.match_max_dist */
+    int32_t collision_broadphase;     /* collision.broadphase: 0 uniform_grid (any reference value maps here) */
+    int32_t gpu_precision;            /* gpu.precision: CDX_PRECISION_FP64 | CDX_PRECISION_SPLIT */
+    double gpu_residual_tol;          /* gpu.residual_tol: stop when the complementarity residual <= tol (0 off) */
+    int32_t gpu_check_every;          /* gpu.check_every: host polls the stop flag every k sweeps */
+    int32_t gpu_block;                /* gpu.block: threads per block for contact kernels (0 = auto) */
+    double gpu_contact_capacity_factor; /* gpu.contact_capacity: initial contact slots per body */
+    int32_t gpu_use_graph;            /* gpu.graph: capture the solver loop in a CUDA graph (split form) */
+} cdx_config;
+
+/* Scene: dynamic spheres plus static shapes (halfspaces, drums). Bodies of one scene are
+ * contiguous; body_scene/static_scene may be NULL for a single scene. */
+typedef struct cdx_scene {
+    int32_t num_bodies;
+    const double* pos;     /* [3N] */
+    const double* quat;    /* [4N] x,y,z,w */
+    const double* vel;     /* [3N] world frame */
+    const double* omega;   /* [3N] body frame */
+    const double* radius;  /* [N] */
+    const double* mass;    /* [N] */
+    const double* inertia; /* [N] isotropic inertia diagonal */
+    const double* mu;      /* [N] friction coefficient (C_Friction) */
+    const double* rest_n;  /* [N] normal restitution */
+    const double* rest_t;  /* [N] tangential restitution */
+    const int32_t* body_scene; /* [N] nondecreasing, or NULL */
+    int32_t num_statics;
+    const int32_t* static_kind; /* CDX_STATIC_* */
+    const double* static_pos;   /* [3S] halfspace point / drum axis point */
+    const double* static_quat;  /* [4S] */
+    const double* static_vel;   /* [3S] world-frame velocity (enters the contact bias) */
+    const double* static_omega; /* [3S] body-frame angular velocity (moving walls) */
+    const double* static_dir;   /* [3S] halfspace normal / drum axis, world frame */
+    const double* static_radius;/* [S] drum radius (ignored for halfspaces) */
+    const double* static_mu;
+    const double* static_rest_n;
+    const double* static_rest_t;
+    const int32_t* static_scene; /* [S] nondecreasing, or NULL */
+    int32_t num_scenes;
+} cdx_scene;
+
+typedef struct cdx_stats {
+    int64_t steps;
+    int32_t num_contacts;      /* last step */
+    int32_t num_rows;          /* contact rows (3 per frictional contact, 1 otherwise) */
+    int32_t iterations;        /* PJ sweeps of the last step */
+    int32_t reallocations;     /* contact-buffer growths so far */
+    double residual;           /* FP64 complementarity residual of the final state, last step */
+    double residual_last;      /* residual measured inside the last sweep */
+    double ms_collision;       /* device time of the last step by phase (CUDA events; 0 if timing off) */
+    double ms_setup;
+    double ms_solve;
+    double ms_integrate;
+    double solve_bytes_per_iter; /* algorithmic bytes of one sweep (per-contact and per-body words) */
+    int64_t kernel_launches;   /* cdx kernels launched so far */
+} cdx_stats;
+
+typedef struct cdx_ctx cdx_ctx;
+
+/* ---- configuration (ConfigReader::fromFile semantics: unknown keys ignored, bad values keep the
+ * default, pj./solver. prefixes accepted) ---- */
+int cdx_config_default(cdx_config* cfg);
+int cdx_config_set(cdx_config* cfg, const char* key, const char* value); /* config.cpp:41-415 */
+int cdx_config_from_file(const char* path, cdx_config* cfg);              /* config.cpp:22-40 */
+
+/* ---- engine (the integrator-level drop-in: MoreauIntegrator::step, moreau.cpp:6-13, behind
+ * IntegrationBase::step, integration_base.hpp:19) ---- */
+int cdx_create(const cdx_config* cfg, cdx_ctx** out);
+void cdx_destroy(cdx_ctx* ctx);
+const char* cdx_last_error(const cdx_ctx* ctx);
+int cdx_load_scene(cdx_ctx* ctx, const cdx_scene* scene);
+int cdx_step(cdx_ctx* ctx, int32_t nsteps);
+int cdx_synchronize(cdx_ctx* ctx);
+int cdx_get_state(cdx_ctx* ctx, double* pos, double* quat, double* vel, double* omega);
+int cdx_set_state(cdx_ctx* ctx, const double* pos, const double* quat, const double* vel, const double* omega);
+int cdx_get_stats(cdx_ctx* ctx, cdx_stats* out);
+/* contacts of the last step in canonical order (entity ids, points, impulses n/t1/t2, normals);
+ * pass NULL arrays to query the count */
+int cdx_get_contacts(cdx_ctx* ctx, int32_t* id_a, int32_t* id_b, double* point, double* lambda, double* normal,
+                     int32_t* count);
+/* per-sweep impulse trace of the next step (rows in solver order), for parity checks */
+int cdx_set_trace(cdx_ctx* ctx, int32_t on);
+int cdx_get_trace(cdx_ctx* ctx, double* out, int64_t max_values, int64_t* num_values);
+int cdx_set_timing(cdx_ctx* ctx, int32_t on);
+/* the stream the engine launches on (cudaStream_t as void*) */
+void* cdx_stream(cdx_ctx* ctx);
+
+/* ---- solver-level drop-in: ProjectedJacobiSolver::solve(dt, theta)
+ * (src/physics/solver/projected_jacobi.cpp:451-500) with S = diag(M) (pj_assembler.cpp:127-182).
+ * Inputs are what the solver pulls from DynamicsAssembler (dynamics_assembler.hpp:23-94):
+ * W as CSR (nrows x nv; the first nfl rows are frictionless contacts, the rest 3-row frictional
+ * blocks), contactVVec, muVec, restitutionVec, MinvDiag, MDiag, vVec, fVecExternal,
+ * fVecGyroscopic. lambda_inout carries the warm start in and the impulses out; x_out receives
+ * the stacked velocities. Host arrays; FP64; bit-reproducible vs the oracle. ---- */
+int cdx_pj_solve_csr(cdx_ctx* ctx, int32_t nrows, int32_t nv, int32_t nfl, const int32_t* row_ptr,
+                     const int32_t* col, const double* val, const double* contact_bias, const double* mu,
+                     const double* restitution, const double* minv, const double* mdiag, const double* v,
+                     const double* f_ext, const double* f_gyro, double dt, double alpha, int32_t max_iter,
+                     double tol_abs, double tol_rel, double* lambda_inout, double* x_out, int32_t* iterations);
+
+/* ---- seeded scene generators for the benchmark scenes (host only) ---- */
+typedef struct cdx_gen_params {
+    int32_t kind;          /* 0 box pile(s), 1 rotating drum */
+    int32_t num_scenes;    /* box piles: independent scenes laid out side by side */
+    int32_t num_bodies;    /* bodies per scene (ignored when nb_lo > 0) */
+    int32_t nb_lo, nb_hi;  /* per-scene body count log-uniform in [nb_lo, nb_hi] (0 = off) */
+    double r_lo, r_hi;     /* radius uniform in [r_lo, r_hi] */
+    double density;
+    double box[3];         /* box extents (x, y, z) per scene */
+    double mu, mu_lo, mu_hi; /* friction; per-scene uniform in [mu_lo, mu_hi] when mu_hi > mu_lo */
+    double v_sigma;        /* initial velocity N(0, v_sigma^2) per component */
+    double drum_radius, drum_length, drum_omega;
+    uint64_t seed;
+    int32_t max_attempts;  /* rejection-sampling attempts per body */
+} cdx_gen_params;
+
+typedef struct cdx_gen_scene cdx_gen_scene;
+int cdx_gen_create(const cdx_gen_params* p, cdx_gen_scene** out);
+/* fills a cdx_scene view whose arrays live in the generated object */
+int cdx_gen_view(const cdx_gen_scene* g, cdx_scene* view);
+void cdx_gen_destroy(cdx_gen_scene* g);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CDX_H */

@@ -1,0 +1,828 @@
+// Oracle: CPU FP64 restatement of CardilloCxx's Moreau midpoint step for sphere scenes.
+//
+// TEST INFRASTRUCTURE ONLY (the checker and the timed CPU baseline). Nothing in the product
+// package loads this file. Parity status: UNPINNED -- the reference needs Eigen 5.0.1, EnTT 3.13.2
+// and coal 3.0.4, none of which exist here, and it has no tests or golden vectors for this path.
+//
+// Every function cites the reference lines it restates (paths relative to the reference repo).
+// Floating-point rules: plain IEEE double, no FMA contraction (built with -ffp-contract=off),
+// every expression evaluated left to right as written in the reference's Eigen code. Where the
+// reference's result depends on Eigen's internal reduction order (vectorised dot products and
+// norms), this file fixes the sequential order ((a0*b0 + a1*b1) + a2*b2); identity-matrix
+// products that Eigen evaluates literally (transform::point from the inertial frame) are elided,
+// which can only change the sign of an exact zero.
+#include "cdx_oracle.h"
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+inline double dot3(const double* a, const double* b) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
+inline double norm3(const double* a) { return std::sqrt(dot3(a, a)); }
+inline void cross3(const double* a, const double* b, double* o) {
+    o[0] = a[1] * b[2] - a[2] * b[1];
+    o[1] = a[2] * b[0] - a[0] * b[2];
+    o[2] = a[0] * b[1] - a[1] * b[0];
+}
+inline bool finite3(const double* a) { return std::isfinite(a[0]) && std::isfinite(a[1]) && std::isfinite(a[2]); }
+inline double std_min(double a, double b) { return (b < a) ? b : a; }  // std::min semantics
+inline double std_max(double a, double b) { return (a < b) ? b : a; }  // std::max semantics
+
+// Quaternion (x,y,z,w) -> row-major rotation matrix, Eigen's QuaternionBase::toRotationMatrix
+// (C_Orientation::setValue, src/physics/ecs_types.hpp:37-41).
+inline void rotmat(const double* q, double* R) {
+    const double x = q[0], y = q[1], z = q[2], w = q[3];
+    const double tx = 2.0 * x, ty = 2.0 * y, tz = 2.0 * z;
+    const double twx = tx * w, twy = ty * w, twz = tz * w;
+    const double txx = tx * x, txy = ty * x, txz = tz * x;
+    const double tyy = ty * y, tyz = tz * y, tzz = tz * z;
+    R[0] = 1.0 - (tyy + tzz); R[1] = txy - twz;         R[2] = txz + twy;
+    R[3] = txy + twz;         R[4] = 1.0 - (txx + tzz); R[5] = tyz - twx;
+    R[6] = txz - twy;         R[7] = tyz + twx;         R[8] = 1.0 - (txx + tyy);
+}
+// R^T v (transformations.hpp:34-43: inertialToBodyPoint / inertialToBodyVector)
+inline void matTvec(const double* R, const double* v, double* o) {
+    for (int i = 0; i < 3; ++i) o[i] = (R[0 + i] * v[0] + R[3 + i] * v[1]) + R[6 + i] * v[2];
+}
+
+// src/misc/math_helper.hpp:11-17 (alignQuaternionTo) with Eigen's normalize()
+inline void align_quat(double* q, const double* qref) {
+    if (!(std::isfinite(q[0]) && std::isfinite(q[1]) && std::isfinite(q[2]) && std::isfinite(q[3]))) {
+        for (int k = 0; k < 4; ++k) q[k] = qref[k];
+        return;
+    }
+    const double n2 = ((q[0] * q[0] + q[1] * q[1]) + q[2] * q[2]) + q[3] * q[3];
+    if (n2 > 0.0) {
+        const double n = std::sqrt(n2);
+        for (int k = 0; k < 4; ++k) q[k] = q[k] / n;
+    }
+    const double d = ((qref[0] * q[0] + qref[1] * q[1]) + qref[2] * q[2]) + qref[3] * q[3];
+    if (d < 0.0)
+        for (int k = 0; k < 4; ++k) q[k] = -q[k];
+}
+
+// src/physics/integration/integration_base.cpp:6-30 (explicitPositionUpdate) for one entity.
+inline void drift(double* x, double* q, const double* v, const double* w, double h) {
+    for (int k = 0; k < 3; ++k) x[k] = x[k] + h * v[k];
+    const double qprev[4] = {q[0], q[1], q[2], q[3]};
+    const double hh = h * 0.5;
+    const double qw = q[3];
+    q[3] = q[3] - hh * dot3(q, w);
+    double c[3];
+    cross3(qprev, w, c);
+    for (int k = 0; k < 3; ++k) q[k] = qprev[k] + hh * (qw * w[k] + c[k]);
+    align_quat(q, qprev);
+}
+
+// src/collision/tangent_frame.hpp:23-50 (tangentFrameFromNormal)
+inline void tangent_frame(const double* n_in, double* t1, double* t2) {
+    const double len = norm3(n_in);
+    if (len <= DBL_EPSILON) {
+        t1[0] = 1; t1[1] = 0; t1[2] = 0;
+        t2[0] = 0; t2[1] = 1; t2[2] = 0;
+        return;
+    }
+    const double n[3] = {n_in[0] / len, n_in[1] / len, n_in[2] / len};
+    if (n[2] < -0.9999999) {
+        t1[0] = 0; t1[1] = -1; t1[2] = 0;
+        const double d = dot3(n, t1);
+        for (int k = 0; k < 3; ++k) t1[k] = t1[k] - n[k] * d;
+    } else {
+        const double a = 1.0 / (1.0 + n[2]);
+        const double b = (-n[0] * n[1]) * a;
+        t1[0] = 1.0 - (n[0] * n[0]) * a;
+        t1[1] = b;
+        t1[2] = -n[0];
+    }
+    const double t2n = dot3(t1, t1);
+    if (t2n > 0.0) {
+        const double s = std::sqrt(t2n);
+        for (int k = 0; k < 3; ++k) t1[k] = t1[k] / s;
+    }
+    cross3(n, t1, t2);
+}
+
+struct Contact {
+    int32_t a = -1, b = -1;    // entity ids: statics 0..S-1, spheres S..S+N-1
+    int32_t sa = -1, sb = -1;  // static index of side A (or -1); body index of side A/B (or -1)
+    int32_t ba = -1, bb = -1;
+    double point[3], n[3], t1[3], t2[3];
+    double cA[9], cB[9];  // r_X^body x d_k^body for k = n, t1, t2 (unsigned)
+    double cb[3];          // static-side contact velocity per row
+    double mu = 0, eN = 0, eT = 0;
+    bool frictional = false;
+    double lam0[3] = {0, 0, 0};
+    uint64_t key() const { return ((uint64_t)(uint32_t)a << 32) | (uint32_t)b; }
+};
+
+struct Engine {
+    or_config cfg{};
+    int N = 0, S = 0;
+    std::vector<double> pos, q, v, w, R, rad, mass, inertia, mu, rn, rt;
+    std::vector<int32_t> scene;
+    std::vector<double> minv, Mdiag;  // per DOF (6 per body)
+    std::vector<int32_t> skind, sscene;
+    std::vector<double> spos, sq, sv, sw, sdir, srad, sd, smu, srn, srt, sR;
+    // warm-start memory of the previous step (canonical order, sorted by key)
+    std::vector<uint64_t> prev_keys;
+    std::vector<double> prev_point, prev_lambda;
+    // last step's contacts for inspection
+    std::vector<Contact> last;
+    std::vector<double> last_lambda;
+    bool trace_on = false;
+    std::vector<double> trace;
+    or_stats stats{};
+    double rmax = 0;
+};
+
+// Sphere mass matrix, src/physics/assembly/dynamics_assembler.cpp:41-62 (rebuildMass_) with
+// src/physics/world.cpp:49-72: Minv = 1/[m,m,m,I,I,I], M_ii = 1/Minv_ii.
+void build_mass(Engine& E) {
+    E.minv.assign(6 * (size_t)E.N, 0.0);
+    E.Mdiag.assign(6 * (size_t)E.N, 0.0);
+    for (int i = 0; i < E.N; ++i) {
+        for (int k = 0; k < 6; ++k) {
+            const double md = (k < 3) ? E.mass[i] : E.inertia[i];
+            const double inv = 1.0 / md;
+            E.minv[6 * i + k] = inv;
+            E.Mdiag[6 * i + k] = (inv > 0.0) ? 1.0 / inv : 0.0;
+        }
+    }
+}
+
+// Narrow phase for one (static, sphere) or (sphere, sphere) pair plus makeContact
+// (src/collision/collision_coal.cpp:112-163). Returns false when the shapes are apart
+// (distance > collision.security_margin, coal's ShapeShapeCollider rule).
+bool make_contact(const Engine& E, int a_static, int a_body, int b_body, Contact& c) {
+    const double* xb = &E.pos[3 * (size_t)b_body];
+    const double rb = E.rad[b_body];
+    double p1[3], p2[3], nraw[3], xa[3];
+    const double margin = E.cfg.collision_security_margin;
+    if (a_static >= 0) {
+        const int s = a_static;
+        for (int k = 0; k < 3; ++k) xa[k] = E.spos[3 * s + k];
+        const double* u = &E.sdir[3 * s];
+        if (E.skind[s] == 0) {
+            // coal::Halfspace {x : n.x <= d}; shape 1 = halfspace, shape 2 = sphere
+            const double sdist = dot3(u, xb) - E.sd[s];
+            const double dist = sdist - rb;
+            if (!(dist <= margin)) return false;
+            for (int k = 0; k < 3; ++k) {
+                p1[k] = xb[k] - sdist * u[k];
+                p2[k] = xb[k] - rb * u[k];
+                nraw[k] = u[k];
+            }
+        } else {
+            // hollow drum wall (new primitive; the reference has no counterpart)
+            double rel[3];
+            for (int k = 0; k < 3; ++k) rel[k] = xb[k] - xa[k];
+            const double ax = dot3(rel, u);
+            double perp[3];
+            for (int k = 0; k < 3; ++k) perp[k] = rel[k] - ax * u[k];
+            const double rho = norm3(perp);
+            const double dist = (E.srad[s] - rho) - rb;
+            if (!(dist <= margin)) return false;
+            double e[3] = {0, 0, 0};
+            if (rho > 0.0)
+                for (int k = 0; k < 3; ++k) e[k] = perp[k] / rho;
+            for (int k = 0; k < 3; ++k) {
+                p1[k] = (xa[k] + ax * u[k]) + E.srad[s] * e[k];
+                p2[k] = xb[k] + rb * e[k];
+                nraw[k] = -e[k];
+            }
+        }
+        c.a = s;
+        c.sa = s;
+        c.ba = -1;
+    } else {
+        const double* xA = &E.pos[3 * (size_t)a_body];
+        const double ra = E.rad[a_body];
+        double d[3];
+        for (int k = 0; k < 3; ++k) d[k] = xb[k] - xA[k];
+        const double dl = norm3(d);
+        const double dist = (dl - ra) - rb;
+        if (!(dist <= margin)) return false;
+        double nn[3] = {0, 0, 0};
+        if (dl > 0.0)
+            for (int k = 0; k < 3; ++k) nn[k] = d[k] / dl;
+        for (int k = 0; k < 3; ++k) {
+            p1[k] = xA[k] + ra * nn[k];
+            p2[k] = xb[k] - rb * nn[k];
+            nraw[k] = nn[k];
+            xa[k] = xA[k];
+        }
+        c.a = E.S + a_body;
+        c.sa = -1;
+        c.ba = a_body;
+    }
+    c.b = E.S + b_body;
+    c.bb = b_body;
+
+    // makeContact: sanitise points, normalise the normal with fallbacks
+    if (!finite3(p1)) {
+        if (finite3(p2)) { for (int k = 0; k < 3; ++k) p1[k] = p2[k]; }
+        else { for (int k = 0; k < 3; ++k) p1[k] = xa[k]; }
+    }
+    if (!finite3(p2)) {
+        if (finite3(p1)) { for (int k = 0; k < 3; ++k) p2[k] = p1[k]; }
+        else { for (int k = 0; k < 3; ++k) p2[k] = xb[k]; }
+    }
+    double n[3];
+    const double nlen = norm3(nraw);
+    if (nlen > 0.0 && std::isfinite(nlen)) {
+        for (int k = 0; k < 3; ++k) n[k] = nraw[k] / nlen;
+    } else {
+        double f[3];
+        for (int k = 0; k < 3; ++k) f[k] = p2[k] - p1[k];
+        double fl = norm3(f);
+        if (!(fl > 0.0) || !std::isfinite(fl)) {
+            for (int k = 0; k < 3; ++k) f[k] = xb[k] - xa[k];
+            fl = norm3(f);
+        }
+        if (fl > 0.0 && std::isfinite(fl)) { for (int k = 0; k < 3; ++k) n[k] = f[k] / fl; }
+        else { n[0] = 0; n[1] = 0; n[2] = 1; }
+    }
+    for (int k = 0; k < 3; ++k) c.n[k] = n[k];
+    tangent_frame(n, c.t1, c.t2);
+    for (int k = 0; k < 3; ++k) c.point[k] = (p1[k] + p2[k]) * 0.5;
+    return true;
+}
+
+// Body-frame lever arms and static-side contact velocities: makeContact's transform::point /
+// transform::direction (collision_coal.cpp:151-160) and rebuildW_'s accumulateDirForSide
+// (dynamics_assembler.cpp:262-286) with buildContactRowByDof (contact_jacobian.hpp:17-23).
+void contact_rows(const Engine& E, Contact& c) {
+    const double* dirs[3] = {c.n, c.t1, c.t2};
+    for (int side = 0; side < 2; ++side) {
+        const double* R;
+        const double* x;
+        if (side == 0) {
+            if (c.sa >= 0) { R = &E.sR[9 * c.sa]; x = &E.spos[3 * c.sa]; }
+            else { R = &E.R[9 * (size_t)c.ba]; x = &E.pos[3 * (size_t)c.ba]; }
+        } else {
+            R = &E.R[9 * (size_t)c.bb];
+            x = &E.pos[3 * (size_t)c.bb];
+        }
+        double rel[3], rbody[3];
+        for (int k = 0; k < 3; ++k) rel[k] = c.point[k] - x[k];
+        matTvec(R, rel, rbody);
+        double* cc = side == 0 ? c.cA : c.cB;
+        for (int r = 0; r < 3; ++r) {
+            double db[3];
+            matTvec(R, dirs[r], db);
+            cross3(rbody, db, &cc[3 * r]);
+        }
+    }
+    // static side A: contact_v_vec[row] = 0 + row . [v_world, omega_body] with sign -1
+    for (int r = 0; r < 3; ++r) c.cb[r] = 0.0;
+    if (c.sa >= 0) {
+        const double* vs = &E.sv[3 * c.sa];
+        const double* ws = &E.sw[3 * c.sa];
+        for (int r = 0; r < 3; ++r) {
+            const double* d = dirs[r];
+            const double row[6] = {-d[0], -d[1], -d[2], -c.cA[3 * r], -c.cA[3 * r + 1], -c.cA[3 * r + 2]};
+            double acc = row[0] * vs[0];
+            acc = acc + row[1] * vs[1];
+            acc = acc + row[2] * vs[2];
+            acc = acc + row[3] * ws[0];
+            acc = acc + row[4] * ws[1];
+            acc = acc + row[5] * ws[2];
+            c.cb[r] = 0.0 + acc;
+        }
+    }
+}
+
+double combine_mu(int mode, double a, double b) {  // collision_coal.cpp:94-106
+    a = std_max(0.0, a);
+    b = std_max(0.0, b);
+    if (mode == 1) return (a + b) * 0.5;
+    if (mode == 2) return std::sqrt(std_max(0.0, a * b));
+    return std_min(a, b);
+}
+
+// Collision: canonical order by (entity id A, entity id B), statics first.
+// Replaces collision_coal.cpp:405-548 (coal broad phase + hash-map flatten order).
+void detect(Engine& E, std::vector<Contact>& out) {
+    out.clear();
+    const int N = E.N, S = E.S;
+    // static contacts, ordered by (static, sphere)
+    for (int s = 0; s < S; ++s) {
+        for (int i = 0; i < N; ++i) {
+            if (E.scene[i] != E.sscene[s]) continue;
+            Contact c;
+            if (make_contact(E, s, -1, i, c)) out.push_back(c);
+        }
+    }
+    // sphere pairs via a uniform grid (any exact candidate method yields the same set)
+    if (N == 0) return;
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int i = 0; i < N; ++i)
+        for (int k = 0; k < 3; ++k) {
+            const double p = E.pos[3 * (size_t)i + k];
+            if (std::isfinite(p)) { lo[k] = std::min(lo[k], p); hi[k] = std::max(hi[k], p); }
+        }
+    const double cell = 2.0 * E.rmax * 1.0001 + 1e-12;
+    int64_t dim[3];
+    for (int k = 0; k < 3; ++k) {
+        if (!(hi[k] >= lo[k])) { lo[k] = 0; hi[k] = 0; }
+        dim[k] = std::min<int64_t>((int64_t)((hi[k] - lo[k]) / cell) + 1, 1 << 20);
+    }
+    auto cell_of = [&](const double* p, int64_t* ci) {
+        for (int k = 0; k < 3; ++k) {
+            double f = std::isfinite(p[k]) ? std::floor((p[k] - lo[k]) / cell) : 0.0;
+            int64_t c = (int64_t)std::max(0.0, std::min((double)(dim[k] - 1), f));
+            ci[k] = c;
+        }
+    };
+    std::vector<std::pair<uint64_t, int>> keyed(N);
+    for (int i = 0; i < N; ++i) {
+        int64_t ci[3];
+        cell_of(&E.pos[3 * (size_t)i], ci);
+        keyed[i] = {(uint64_t)((ci[2] * dim[1] + ci[1]) * dim[0] + ci[0]), i};
+    }
+    std::sort(keyed.begin(), keyed.end());
+    std::vector<std::vector<Contact>> per(N);
+#pragma omp parallel for schedule(dynamic, 256) if (E.cfg.omp_mode == 1)
+    for (int i = 0; i < N; ++i) {
+        int64_t ci[3];
+        cell_of(&E.pos[3 * (size_t)i], ci);
+        std::vector<int> cand;
+        for (int dz = -1; dz <= 1; ++dz)
+            for (int dy = -1; dy <= 1; ++dy)
+                for (int dx = -1; dx <= 1; ++dx) {
+                    const int64_t x = ci[0] + dx, y = ci[1] + dy, z = ci[2] + dz;
+                    if (x < 0 || y < 0 || z < 0 || x >= dim[0] || y >= dim[1] || z >= dim[2]) continue;
+                    const uint64_t key = (uint64_t)((z * dim[1] + y) * dim[0] + x);
+                    auto it = std::lower_bound(keyed.begin(), keyed.end(), std::make_pair(key, -1));
+                    for (; it != keyed.end() && it->first == key; ++it) {
+                        const int j = it->second;
+                        if (j > i && E.scene[j] == E.scene[i]) cand.push_back(j);
+                    }
+                }
+        std::sort(cand.begin(), cand.end());
+        for (int j : cand) {
+            Contact c;
+            if (make_contact(E, -1, i, j, c)) per[i].push_back(c);
+        }
+    }
+    for (int i = 0; i < N; ++i)
+        for (auto& c : per[i]) out.push_back(c);
+}
+
+// Contact attributes: mu, restitution (dynamics_assembler.cpp:249-258, collision_coal.cpp:188)
+void contact_props(const Engine& E, Contact& c) {
+    const double muA = c.sa >= 0 ? E.smu[c.sa] : E.mu[c.ba];
+    const double muB = E.mu[c.bb];
+    c.mu = combine_mu(E.cfg.friction_combine, muA, muB);
+    const double rnA = std_max(0.0, c.sa >= 0 ? E.srn[c.sa] : E.rn[c.ba]);
+    const double rtA = std_max(0.0, c.sa >= 0 ? E.srt[c.sa] : E.rt[c.ba]);
+    c.eN = std_min(rnA, std_max(0.0, E.rn[c.bb]));
+    c.eT = std_min(rtA, std_max(0.0, E.rt[c.bb]));
+    c.frictional = E.cfg.friction_enable && c.mu > 0.0;
+}
+
+// Sparse contact Jacobian row (CSR, column order), as assembled by rebuildW_
+// (dynamics_assembler.cpp:211-332) and converted by TripletMatrix::asSparseRowMajor.
+struct Rows {
+    int nrows = 0, nfl = 0;
+    std::vector<int32_t> ptr, col;
+    std::vector<double> val;
+    std::vector<double> cb, mu, e;  // contact_v_vec, mu (normal row), restitution per row
+    std::vector<int32_t> row_contact;  // contact index per row, row kind in contact
+    std::vector<int32_t> row_base;     // per contact: first row
+};
+
+void build_rows(const Engine& E, const std::vector<Contact>& C, Rows& W) {
+    W = Rows{};
+    std::vector<int> order;
+    for (int pass = 0; pass < 2; ++pass)
+        for (int i = 0; i < (int)C.size(); ++i)
+            if ((pass == 1) == C[i].frictional) order.push_back(i);
+    W.row_base.assign(C.size(), -1);
+    W.ptr.push_back(0);
+    for (int ci : order) {
+        const Contact& c = C[ci];
+        const int nr = c.frictional ? 3 : 1;
+        if (!c.frictional) W.nfl++;
+        W.row_base[ci] = W.nrows;
+        const double* dirs[3] = {c.n, c.t1, c.t2};
+        for (int r = 0; r < nr; ++r) {
+            // sides in column order (lower body index first)
+            struct Side { int body; double s; const double* cc; };
+            Side sides[2];
+            int ns = 0;
+            if (c.ba >= 0) sides[ns++] = {c.ba, -1.0, &c.cA[3 * r]};
+            sides[ns++] = {c.bb, 1.0, &c.cB[3 * r]};
+            if (ns == 2 && sides[1].body < sides[0].body) std::swap(sides[0], sides[1]);
+            for (int k = 0; k < ns; ++k) {
+                const Side& sd = sides[k];
+                for (int j = 0; j < 3; ++j) { W.col.push_back(6 * sd.body + j); W.val.push_back(sd.s * dirs[r][j]); }
+                for (int j = 0; j < 3; ++j) { W.col.push_back(6 * sd.body + 3 + j); W.val.push_back(sd.s * sd.cc[j]); }
+            }
+            W.ptr.push_back((int32_t)W.col.size());
+            W.cb.push_back(c.cb[r]);
+            W.mu.push_back(c.frictional ? c.mu : 0.0);
+            W.e.push_back(r == 0 ? c.eN : c.eT);
+            W.row_contact.push_back(ci);
+            W.nrows++;
+        }
+    }
+}
+
+// ---- projected Jacobi, src/physics/solver/projected_jacobi.cpp ----
+struct PJ {
+    int nrows = 0, nv = 0, nfl = 0;
+    const int32_t* ptr = nullptr;
+    const int32_t* col = nullptr;
+    const double* val = nullptr;
+    std::vector<double> RW, biasR, mu;
+    // column-major copy of W (for the all-OpenMP W^T gather; same per-column row order)
+    std::vector<int32_t> cptr, crow;
+    std::vector<double> cval;
+};
+
+// projected_jacobi.cpp:100-119 (project) applied to one contact's rows
+inline void project_rows(double* lam, int r, bool frictional, double mu) {
+    if (!frictional) { lam[r] = std_max(lam[r], 0.0); return; }
+    lam[r] = std_max(lam[r], 0.0);
+    const double t1 = lam[r + 1], t2 = lam[r + 2];
+    const double tn2 = t1 * t1 + t2 * t2;
+    if (tn2 <= 0) return;
+    const double s = std_min(1.0, (mu * lam[r]) / std::sqrt(tn2));
+    lam[r + 1] = s * t1;
+    lam[r + 2] = s * t2;
+}
+
+// build_workspace (projected_jacobi.cpp:316-369) + rdiag_sparse (:57-69)
+void pj_setup(PJ& P, const double* cb, const double* e, const double* mu, const double* minv, const double* vn,
+              double alpha, int omp_all) {
+    P.RW.assign(P.ptr[P.nrows], 0.0);
+    P.biasR.assign(P.nrows, 0.0);
+    P.mu.assign(mu, mu + P.nrows);
+#pragma omp parallel for schedule(static) if (omp_all)
+    for (int r = 0; r < P.nrows; ++r) {
+        double vp = 0.0, D = 0.0;
+        for (int k = P.ptr[r]; k < P.ptr[r + 1]; ++k) vp = vp + P.val[k] * vn[P.col[k]];
+        vp = vp + cb[r];
+        const double bias = cb[r] + e[r] * vp;
+        for (int k = P.ptr[r]; k < P.ptr[r + 1]; ++k) D = D + (P.val[k] * P.val[k]) * minv[P.col[k]];
+        const double R = (D > 0.0) ? (alpha / D) : 0.0;
+        for (int k = P.ptr[r]; k < P.ptr[r + 1]; ++k) P.RW[k] = R * P.val[k];
+        P.biasR[r] = R * bias;
+    }
+    if (omp_all) {
+        std::vector<int32_t> cnt(P.nv + 1, 0);
+        for (int k = 0; k < P.ptr[P.nrows]; ++k) cnt[P.col[k] + 1]++;
+        for (int j = 0; j < P.nv; ++j) cnt[j + 1] += cnt[j];
+        P.cptr = cnt;
+        P.crow.assign(P.ptr[P.nrows], 0);
+        P.cval.assign(P.ptr[P.nrows], 0.0);
+        std::vector<int32_t> fill(cnt.begin(), cnt.end() - 1);
+        for (int r = 0; r < P.nrows; ++r)
+            for (int k = P.ptr[r]; k < P.ptr[r + 1]; ++k) {
+                const int j = P.col[k];
+                P.crow[fill[j]] = r;
+                P.cval[fill[j]] = P.val[k];
+                fill[j]++;
+            }
+    }
+}
+
+// dst_j += sum_r W_rj * y_r in row order (Eigen's column-major sparse * dense kernel)
+void wt_accumulate(const PJ& P, const double* y, double* dst, int omp_all) {
+    if (omp_all) {
+#pragma omp parallel for schedule(static)
+        for (int j = 0; j < P.nv; ++j) {
+            double a = dst[j];
+            for (int k = P.cptr[j]; k < P.cptr[j + 1]; ++k) a = a + P.cval[k] * y[P.crow[k]];
+            dst[j] = a;
+        }
+    } else {
+        for (int r = 0; r < P.nrows; ++r) {
+            const double yr = y[r];
+            for (int k = P.ptr[r]; k < P.ptr[r + 1]; ++k) dst[P.col[k]] = dst[P.col[k]] + P.val[k] * yr;
+        }
+    }
+}
+
+// frictional-row mask: rows >= nfl come in 3-row blocks
+struct SweepOut { double maxd = 0, maxl = 0; };
+
+// pj_sweep (projected_jacobi.cpp:121-138). Returns the max contact update and max |lambda_old|
+// (the complementarity residual of the iterate entering the sweep).
+SweepOut pj_sweep(PJ& P, double* x, double* lam, double* dlam, double* acc, const double* Mdiag, int omp_all,
+                  bool apply = true) {
+    const int nr = P.nrows;
+    std::vector<double> lnew(nr);
+#pragma omp parallel for schedule(static) if (omp_all)
+    for (int r = 0; r < nr; ++r) {
+        double t = 0.0;
+        for (int k = P.ptr[r]; k < P.ptr[r + 1]; ++k) t = t + P.RW[k] * x[P.col[k]];
+        const double g = t + P.biasR[r];
+        lnew[r] = lam[r] - g;
+    }
+    // project(): frictionless rows, then frictional blocks (OpenMP, as the reference)
+    for (int r = 0; r < P.nfl; ++r) project_rows(lnew.data(), r, false, 0.0);
+    const int nb = (nr - P.nfl) / 3;
+#pragma omp parallel for schedule(static)
+    for (int b = 0; b < nb; ++b) {
+        const int r = P.nfl + 3 * b;
+        project_rows(lnew.data(), r, true, P.mu[r]);
+    }
+    SweepOut so;
+    auto upd = [&](int r0, int n) {
+        double s = 0.0, ml = 0.0;
+        for (int q = 0; q < n; ++q) {
+            const double d = lnew[r0 + q] - lam[r0 + q];
+            dlam[r0 + q] = d;
+            s = s + d * d;
+            ml = std::max(ml, std::fabs(lam[r0 + q]));
+        }
+        so.maxd = std::max(so.maxd, std::sqrt(s));
+        so.maxl = std::max(so.maxl, ml);
+    };
+    for (int r = 0; r < P.nfl; ++r) upd(r, 1);
+    for (int b = 0; b < nb; ++b) upd(P.nfl + 3 * b, 3);
+    if (!apply) return so;
+    for (int r = 0; r < nr; ++r) lam[r] = lnew[r];
+    std::fill(acc, acc + P.nv, 0.0);
+    wt_accumulate(P, dlam, acc, omp_all);
+    for (int j = 0; j < P.nv; ++j) x[j] = x[j] + acc[j] / Mdiag[j];
+    return so;
+}
+
+inline double rel_residual(const SweepOut& s) { return s.maxd / std::max(s.maxl, 1e-30); }
+
+// projected_jacobi.cpp:140-144 (residual)
+double vel_residual(const double* x, const double* xp, int nv, double tol_rel, double tol_abs) {
+    double s = 0.0;
+    for (int j = 0; j < nv; ++j) {
+        const double q = std::max(std::fabs(x[j]), std::fabs(xp[j])) * tol_rel + tol_abs;
+        const double d = (x[j] - xp[j]) / q;
+        s = s + d * d;
+    }
+    return 1.0 / std::sqrt((double)nv) * std::sqrt(s);
+}
+
+struct SolveResult { int iters = 0; double res_last = 0, res_final = 0; };
+
+// ProjectedJacobiSolver::solve with standard_loop (projected_jacobi.cpp:371-377, 451-500).
+// rhs is consumed (becomes rhs + W^T p), x receives the velocities, lam in/out.
+SolveResult pj_solve(PJ& P, double* rhs, const double* Mdiag, double* lam, double* x, int max_iter,
+                     double tol_abs, double tol_rel, double residual_tol, int omp_all, std::vector<double>* trace) {
+    SolveResult res;
+    wt_accumulate(P, lam, rhs, omp_all);  // rhs_init += W^T p
+    for (int j = 0; j < P.nv; ++j) x[j] = rhs[j] / Mdiag[j];
+    if (P.nrows == 0) return res;
+    std::vector<double> dlam(P.nrows), acc(P.nv), xprev(P.nv);
+    const int maxit = std::max(1, max_iter);
+    for (int it = 0; it < maxit; ++it) {
+        std::copy(x, x + P.nv, xprev.begin());
+        SweepOut so = pj_sweep(P, x, lam, dlam.data(), acc.data(), Mdiag, omp_all);
+        res.iters = it + 1;
+        res.res_last = rel_residual(so);
+        if (trace) trace->insert(trace->end(), lam, lam + P.nrows);
+        if (it % 10 == 0 && vel_residual(x, xprev.data(), P.nv, tol_rel, tol_abs) <= 1) break;
+        if (residual_tol > 0 && res.res_last <= residual_tol) break;
+    }
+    SweepOut fin = pj_sweep(P, x, lam, dlam.data(), acc.data(), Mdiag, omp_all, false);
+    res.res_final = rel_residual(fin);
+    return res;
+}
+
+// MoreauIntegrator::step (src/physics/integration/moreau.cpp:6-13)
+void step_once(Engine& E) {
+    const int N = E.N, S = E.S, nv = 6 * N;
+    const double dt = E.cfg.sim_dt, th = E.cfg.moreau_theta;
+    const int omp_all = E.cfg.omp_mode == 1;
+    // refreshState: f_ext = m g, f_gyro = -w x (I w)  (world.cpp:113-173); rhs (pj_assembler.cpp:152-153)
+    std::vector<double> rhs(nv), vn(nv);
+    for (int i = 0; i < N; ++i) {
+        const double* w = &E.w[3 * (size_t)i];
+        const double Iw[3] = {E.inertia[i] * w[0], E.inertia[i] * w[1], E.inertia[i] * w[2]};
+        double c[3];
+        cross3(w, Iw, c);
+        for (int k = 0; k < 3; ++k) {
+            const double fext = E.mass[i] * E.cfg.sim_gravity[k];
+            const double Ml = E.Mdiag[6 * i + k];
+            rhs[6 * i + k] = (Ml * E.v[3 * (size_t)i + k] + dt * fext) + dt * 0.0;
+            const double Ma = E.Mdiag[6 * i + 3 + k];
+            rhs[6 * i + 3 + k] = (Ma * w[k] + dt * 0.0) + dt * (-c[k]);
+            vn[6 * i + k] = E.v[3 * (size_t)i + k];
+            vn[6 * i + 3 + k] = w[k];
+        }
+    }
+    // drift 1: (1 - theta) h, every entity with a velocity (statics included)
+    const double h1 = (1.0 - th) * dt;
+    for (int i = 0; i < N; ++i) drift(&E.pos[3 * (size_t)i], &E.q[4 * (size_t)i], &E.v[3 * (size_t)i], &E.w[3 * (size_t)i], h1);
+    for (int s = 0; s < S; ++s) drift(&E.spos[3 * s], &E.sq[4 * s], &E.sv[3 * s], &E.sw[3 * s], h1);
+    for (int i = 0; i < N; ++i) rotmat(&E.q[4 * (size_t)i], &E.R[9 * (size_t)i]);
+    for (int s = 0; s < S; ++s) rotmat(&E.sq[4 * s], &E.sR[9 * s]);
+
+    // updateStateDependentTerms: collision + W
+    std::vector<Contact> C;
+    detect(E, C);
+#pragma omp parallel for schedule(static) if (omp_all)
+    for (int i = 0; i < (int)C.size(); ++i) {
+        contact_rows(E, C[i]);
+        contact_props(E, C[i]);
+    }
+    // warm start: nearest previous contact of the same pair within collision.match_max_dist
+    // (contact_tracker.cpp:43-72, :11-20; warmstart.hpp:26-39)
+    const double max2 = E.cfg.collision_match_max_dist * E.cfg.collision_match_max_dist;
+    if (E.cfg.pj_warmstart) {
+        for (auto& c : C) {
+            auto it = std::lower_bound(E.prev_keys.begin(), E.prev_keys.end(), c.key());
+            if (it == E.prev_keys.end() || *it != c.key()) continue;
+            const size_t j = (size_t)(it - E.prev_keys.begin());
+            double d[3];
+            for (int k = 0; k < 3; ++k) d[k] = c.point[k] - E.prev_point[3 * j + k];
+            if (dot3(d, d) <= max2)
+                for (int k = 0; k < 3; ++k) c.lam0[k] = E.prev_lambda[3 * j + k];
+        }
+    }
+    Rows W;
+    build_rows(E, C, W);
+    PJ P;
+    P.nrows = W.nrows;
+    P.nv = nv;
+    P.nfl = W.nfl;
+    P.ptr = W.ptr.data();
+    P.col = W.col.data();
+    P.val = W.val.data();
+    pj_setup(P, W.cb.data(), W.e.data(), W.mu.data(), E.minv.data(), vn.data(), E.cfg.pj_alpha, omp_all);
+    std::vector<double> lam(W.nrows, 0.0), x(nv);
+    for (size_t ci = 0; ci < C.size(); ++ci) {
+        const int r0 = W.row_base[ci];
+        const int nr = C[ci].frictional ? 3 : 1;
+        for (int k = 0; k < nr; ++k) lam[r0 + k] = C[ci].lam0[k];
+    }
+    E.trace.clear();
+    SolveResult sr;
+    if (C.empty()) {
+        for (int j = 0; j < nv; ++j) x[j] = rhs[j] / E.Mdiag[j];
+    } else {
+        sr = pj_solve(P, rhs.data(), E.Mdiag.data(), lam.data(), x.data(), E.cfg.pj_max_iterations,
+                      E.cfg.pj_tol_abs, E.cfg.pj_tol_rel, E.cfg.residual_tol, omp_all,
+                      E.trace_on ? &E.trace : nullptr);
+    }
+    E.trace_on = false;
+    // storeImpulse (warmstart.hpp:41-56) and the tracker's memory for the next step
+    E.prev_keys.resize(C.size());
+    E.prev_point.resize(3 * C.size());
+    E.prev_lambda.assign(3 * C.size(), 0.0);
+    for (size_t ci = 0; ci < C.size(); ++ci) {
+        E.prev_keys[ci] = C[ci].key();
+        for (int k = 0; k < 3; ++k) E.prev_point[3 * ci + k] = C[ci].point[k];
+        const int r0 = W.row_base[ci];
+        const int nr = C[ci].frictional ? 3 : 1;
+        for (int k = 0; k < nr; ++k) E.prev_lambda[3 * ci + k] = lam[r0 + k];
+    }
+    E.last = C;
+    E.last_lambda = E.prev_lambda;
+    // writeVelocityToSystem (dynamics_assembler.cpp:145-188)
+    for (int i = 0; i < N; ++i)
+        for (int k = 0; k < 3; ++k) {
+            E.v[3 * (size_t)i + k] = x[6 * i + k];
+            E.w[3 * (size_t)i + k] = x[6 * i + 3 + k];
+        }
+    // drift 2: theta h
+    const double h2 = th * dt;
+    for (int i = 0; i < N; ++i) drift(&E.pos[3 * (size_t)i], &E.q[4 * (size_t)i], &E.v[3 * (size_t)i], &E.w[3 * (size_t)i], h2);
+    for (int s = 0; s < S; ++s) drift(&E.spos[3 * s], &E.sq[4 * s], &E.sv[3 * s], &E.sw[3 * s], h2);
+    E.stats.num_contacts = (int32_t)C.size();
+    E.stats.num_rows = W.nrows;
+    E.stats.iterations = sr.iters;
+    E.stats.residual = sr.res_final;
+    E.stats.residual_last = sr.res_last;
+}
+
+}  // namespace
+
+extern "C" {
+
+void* or_create(const or_config* cfg, const or_scene* sc) {
+    Engine* E = new Engine();
+    E->cfg = *cfg;
+    E->N = sc->num_bodies;
+    E->S = sc->num_statics;
+    const size_t N = (size_t)E->N, S = (size_t)E->S;
+    E->pos.assign(sc->pos, sc->pos + 3 * N);
+    E->q.assign(sc->quat, sc->quat + 4 * N);
+    E->v.assign(sc->vel, sc->vel + 3 * N);
+    E->w.assign(sc->omega, sc->omega + 3 * N);
+    E->rad.assign(sc->radius, sc->radius + N);
+    E->mass.assign(sc->mass, sc->mass + N);
+    E->inertia.assign(sc->inertia, sc->inertia + N);
+    E->mu.assign(sc->mu, sc->mu + N);
+    E->rn.assign(sc->rest_n, sc->rest_n + N);
+    E->rt.assign(sc->rest_t, sc->rest_t + N);
+    E->scene.assign(N, 0);
+    if (sc->body_scene) E->scene.assign(sc->body_scene, sc->body_scene + N);
+    E->R.assign(9 * N, 0.0);
+    for (size_t i = 0; i < N; ++i) E->rmax = std::max(E->rmax, E->rad[i]);
+    E->skind.assign(sc->static_kind, sc->static_kind + S);
+    E->spos.assign(sc->static_pos, sc->static_pos + 3 * S);
+    E->sq.assign(sc->static_quat, sc->static_quat + 4 * S);
+    E->sv.assign(sc->static_vel, sc->static_vel + 3 * S);
+    E->sw.assign(sc->static_omega, sc->static_omega + 3 * S);
+    E->sdir.assign(3 * S, 0.0);
+    E->sd.assign(S, 0.0);
+    for (size_t s = 0; s < S; ++s) {
+        // plane.normal.normalized() and d = n . x (collision_coal.cpp:292-297)
+        const double* u = &sc->static_dir[3 * s];
+        const double n2 = dot3(u, u);
+        const double n = std::sqrt(n2);
+        for (int k = 0; k < 3; ++k) E->sdir[3 * s + k] = n2 > 0 ? u[k] / n : u[k];
+        E->sd[s] = dot3(&E->sdir[3 * s], &E->spos[3 * s]);
+    }
+    E->srad.assign(S, 0.0);
+    if (sc->static_radius) E->srad.assign(sc->static_radius, sc->static_radius + S);
+    E->smu.assign(sc->static_mu, sc->static_mu + S);
+    E->srn.assign(sc->static_rest_n, sc->static_rest_n + S);
+    E->srt.assign(sc->static_rest_t, sc->static_rest_t + S);
+    E->sscene.assign(S, 0);
+    if (sc->static_scene) E->sscene.assign(sc->static_scene, sc->static_scene + S);
+    E->sR.assign(9 * S, 0.0);
+    build_mass(*E);
+#ifdef _OPENMP
+    if (cfg->num_threads > 0) omp_set_num_threads(cfg->num_threads);
+#endif
+    return E;
+}
+
+void or_destroy(void* h) { delete (Engine*)h; }
+
+int or_step(void* h, int32_t nsteps) {
+    Engine* E = (Engine*)h;
+    for (int s = 0; s < nsteps; ++s) step_once(*E);
+    return 0;
+}
+
+void or_get_state(void* h, double* pos, double* quat, double* vel, double* omega) {
+    Engine* E = (Engine*)h;
+    if (pos) std::copy(E->pos.begin(), E->pos.end(), pos);
+    if (quat) std::copy(E->q.begin(), E->q.end(), quat);
+    if (vel) std::copy(E->v.begin(), E->v.end(), vel);
+    if (omega) std::copy(E->w.begin(), E->w.end(), omega);
+}
+
+void or_get_stats(void* h, or_stats* out) { *out = ((Engine*)h)->stats; }
+
+int32_t or_get_contacts(void* h, int32_t* id_a, int32_t* id_b, double* point, double* lambda, double* normal) {
+    Engine* E = (Engine*)h;
+    const size_t C = E->last.size();
+    for (size_t i = 0; i < C; ++i) {
+        if (id_a) id_a[i] = E->last[i].a;
+        if (id_b) id_b[i] = E->last[i].b;
+        for (int k = 0; k < 3; ++k) {
+            if (point) point[3 * i + k] = E->last[i].point[k];
+            if (normal) normal[3 * i + k] = E->last[i].n[k];
+            if (lambda) lambda[3 * i + k] = E->last_lambda[3 * i + k];
+        }
+    }
+    return (int32_t)C;
+}
+
+void or_set_trace(void* h, int32_t on) { ((Engine*)h)->trace_on = on != 0; }
+
+int32_t or_get_trace(void* h, double* out, int64_t max_values) {
+    Engine* E = (Engine*)h;
+    const int64_t n = std::min<int64_t>(max_values, (int64_t)E->trace.size());
+    if (out) std::copy(E->trace.begin(), E->trace.begin() + n, out);
+    return (int32_t)E->trace.size();
+}
+
+int32_t or_pj_solve_csr(int32_t nrows, int32_t nv, int32_t nfl, const int32_t* row_ptr, const int32_t* col,
+                        const double* val, const double* contact_bias, const double* mu, const double* restitution,
+                        const double* minv, const double* mdiag, const double* v, const double* f_ext,
+                        const double* f_gyro, double dt, double alpha, int32_t max_iter, double tol_abs,
+                        double tol_rel, double* lambda_inout, double* x_out) {
+    PJ P;
+    P.nrows = nrows;
+    P.nv = nv;
+    P.nfl = nfl;
+    P.ptr = row_ptr;
+    P.col = col;
+    P.val = val;
+    // PjAssembler::rhs (pj_assembler.cpp:152-153): M v + dt f_ext + dt f_gyro
+    std::vector<double> rhs(nv);
+    for (int j = 0; j < nv; ++j) rhs[j] = (mdiag[j] * v[j] + dt * f_ext[j]) + dt * f_gyro[j];
+    if (nrows == 0) {
+        for (int j = 0; j < nv; ++j) x_out[j] = rhs[j] / mdiag[j];
+        return 0;
+    }
+    pj_setup(P, contact_bias, restitution, mu, minv, v, alpha, 0);
+    SolveResult r = pj_solve(P, rhs.data(), mdiag, lambda_inout, x_out, max_iter, tol_abs, tol_rel, 0.0, 0, nullptr);
+    return r.iters;
+}
+
+}  // extern "C"

@@ -1,0 +1,220 @@
+"""ctypes binding for the CPU oracle (test infrastructure only).
+
+The oracle is a plain C++ FP64 restatement of CardilloCxx's Moreau midpoint step for sphere
+scenes (see cdx_oracle.cpp for the file:line citations). Only tests/, __graft_entry__.smoke()
+and bench.py's CPU-baseline leg import this module; the product package never does.
+
+Parity status: unpinned (the reference cannot be built here and ships no golden vectors).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "liboracle.so")
+_lock = threading.Lock()
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with g++ (no FMA contraction, OpenMP)."""
+    src = os.path.join(HERE, "cdx_oracle.cpp")
+    hdr = os.path.join(HERE, "cdx_oracle.h")
+    if (not force and os.path.exists(LIB)
+            and os.path.getmtime(LIB) >= max(os.path.getmtime(src), os.path.getmtime(hdr))):
+        return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    tmp = LIB + f".{os.getpid()}.tmp"
+    cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+           "-fno-fast-math", src, "-o", tmp]
+    subprocess.check_call(cmd)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+class OrConfig(C.Structure):
+    _fields_ = [
+        ("sim_dt", C.c_double),
+        ("sim_gravity", C.c_double * 3),
+        ("moreau_theta", C.c_double),
+        ("friction_enable", C.c_int32),
+        ("friction_combine", C.c_int32),
+        ("pj_max_iterations", C.c_int32),
+        ("pj_warmstart", C.c_int32),
+        ("pj_tol_abs", C.c_double),
+        ("pj_tol_rel", C.c_double),
+        ("pj_alpha", C.c_double),
+        ("collision_security_margin", C.c_double),
+        ("collision_match_max_dist", C.c_double),
+        ("residual_tol", C.c_double),
+        ("omp_mode", C.c_int32),
+        ("num_threads", C.c_int32),
+    ]
+
+
+_P = C.POINTER(C.c_double)
+_PI = C.POINTER(C.c_int32)
+
+
+class OrScene(C.Structure):
+    _fields_ = [
+        ("num_bodies", C.c_int32),
+        ("pos", _P), ("quat", _P), ("vel", _P), ("omega", _P),
+        ("radius", _P), ("mass", _P), ("inertia", _P), ("mu", _P), ("rest_n", _P), ("rest_t", _P),
+        ("body_scene", _PI),
+        ("num_statics", C.c_int32),
+        ("static_kind", _PI),
+        ("static_pos", _P), ("static_quat", _P), ("static_vel", _P), ("static_omega", _P),
+        ("static_dir", _P), ("static_radius", _P),
+        ("static_mu", _P), ("static_rest_n", _P), ("static_rest_t", _P),
+        ("static_scene", _PI),
+        ("num_scenes", C.c_int32),
+    ]
+
+
+class OrStats(C.Structure):
+    _fields_ = [
+        ("num_contacts", C.c_int32),
+        ("num_rows", C.c_int32),
+        ("iterations", C.c_int32),
+        ("residual", C.c_double),
+        ("residual_last", C.c_double),
+    ]
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            L = C.CDLL(build())
+            L.or_create.restype = C.c_void_p
+            L.or_create.argtypes = [C.POINTER(OrConfig), C.POINTER(OrScene)]
+            L.or_destroy.argtypes = [C.c_void_p]
+            L.or_step.argtypes = [C.c_void_p, C.c_int32]
+            L.or_get_state.argtypes = [C.c_void_p, _P, _P, _P, _P]
+            L.or_get_stats.argtypes = [C.c_void_p, C.POINTER(OrStats)]
+            L.or_get_contacts.restype = C.c_int32
+            L.or_get_contacts.argtypes = [C.c_void_p, _PI, _PI, _P, _P, _P]
+            L.or_set_trace.argtypes = [C.c_void_p, C.c_int32]
+            L.or_get_trace.restype = C.c_int32
+            L.or_get_trace.argtypes = [C.c_void_p, _P, C.c_int64]
+            L.or_pj_solve_csr.restype = C.c_int32
+            L.or_pj_solve_csr.argtypes = [C.c_int32, C.c_int32, C.c_int32, _PI, _PI, _P, _P, _P, _P, _P, _P,
+                                          _P, _P, _P, C.c_double, C.c_double, C.c_int32, C.c_double,
+                                          C.c_double, _P, _P]
+            _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(_P) if a is not None else None
+
+
+def _ip(a):
+    return a.ctypes.data_as(_PI) if a is not None else None
+
+
+def config_from(cfg: dict, omp_mode: int = 0, num_threads: int = 0) -> OrConfig:
+    """Build the oracle config from the same dict of reference keys the product uses."""
+    c = OrConfig()
+    c.sim_dt = float(cfg.get("sim.dt", 1e-3))
+    g = cfg.get("sim.gravity", (0.0, 0.0, -9.81))
+    for k in range(3):
+        c.sim_gravity[k] = float(g[k])
+    c.moreau_theta = float(cfg.get("moreau.theta", 1.0))
+    c.friction_enable = int(bool(cfg.get("friction.enable", False)))
+    c.friction_combine = {"min": 0, "arith": 1, "geom": 2}[cfg.get("friction.combine", "min")]
+    c.pj_max_iterations = int(cfg.get("pj.max_iterations", 200000))
+    c.pj_warmstart = int(bool(cfg.get("pj.warmstart", True)))
+    c.pj_tol_abs = float(cfg.get("pj.tol_abs", 1e-5))
+    c.pj_tol_rel = float(cfg.get("pj.tol_rel", 1e-5))
+    c.pj_alpha = float(cfg.get("pj.alpha", 0.3))
+    c.collision_security_margin = float(cfg.get("collision.security_margin", 0.0))
+    c.collision_match_max_dist = float(cfg.get("collision.match_max_dist", 0.02))
+    c.residual_tol = float(cfg.get("gpu.residual_tol", 0.0))
+    c.omp_mode = omp_mode
+    c.num_threads = num_threads
+    return c
+
+
+class Oracle:
+    """CPU FP64 engine over a scene dict (numpy arrays, see cardillocxx_gb300.scenes)."""
+
+    def __init__(self, scene: dict, cfg: dict, omp_mode: int = 0, num_threads: int = 0):
+        self.L = lib()
+        self._keep = {k: (np.ascontiguousarray(v) if isinstance(v, np.ndarray) else v) for k, v in scene.items()}
+        s = self._keep
+        sc = OrScene()
+        sc.num_bodies = int(s["pos"].shape[0])
+        for name in ("pos", "quat", "vel", "omega", "radius", "mass", "inertia", "mu", "rest_n", "rest_t"):
+            setattr(sc, name, _dp(s[name]))
+        sc.body_scene = _ip(s.get("body_scene"))
+        sc.num_statics = int(s["static_kind"].shape[0])
+        sc.static_kind = _ip(s["static_kind"])
+        for name in ("static_pos", "static_quat", "static_vel", "static_omega", "static_dir", "static_radius",
+                     "static_mu", "static_rest_n", "static_rest_t"):
+            setattr(sc, name, _dp(s[name]))
+        sc.static_scene = _ip(s.get("static_scene"))
+        sc.num_scenes = int(s.get("num_scenes", 1))
+        self.cfg = config_from(cfg, omp_mode, num_threads)
+        self.h = self.L.or_create(C.byref(self.cfg), C.byref(sc))
+        self.N = sc.num_bodies
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            self.L.or_destroy(h)
+            self.h = None
+
+    def step(self, n: int = 1):
+        self.L.or_step(self.h, int(n))
+
+    def state(self):
+        N = self.N
+        pos = np.empty((N, 3)); quat = np.empty((N, 4)); vel = np.empty((N, 3)); om = np.empty((N, 3))
+        self.L.or_get_state(self.h, _dp(pos), _dp(quat), _dp(vel), _dp(om))
+        return {"pos": pos, "quat": quat, "vel": vel, "omega": om}
+
+    def stats(self) -> dict:
+        st = OrStats()
+        self.L.or_get_stats(self.h, C.byref(st))
+        return {k: getattr(st, k) for k, _ in OrStats._fields_}
+
+    def contacts(self):
+        n = self.L.or_get_contacts(self.h, None, None, None, None, None)
+        ia = np.empty(n, np.int32); ib = np.empty(n, np.int32)
+        pt = np.empty((n, 3)); lam = np.empty((n, 3)); nrm = np.empty((n, 3))
+        self.L.or_get_contacts(self.h, _ip(ia), _ip(ib), _dp(pt), _dp(lam), _dp(nrm))
+        return {"id_a": ia, "id_b": ib, "point": pt, "lambda": lam, "normal": nrm}
+
+    def set_trace(self, on: bool = True):
+        self.L.or_set_trace(self.h, int(on))
+
+    def trace(self, nrows: int):
+        n = self.L.or_get_trace(self.h, None, 0)
+        out = np.empty(n)
+        self.L.or_get_trace(self.h, _dp(out), n)
+        return out.reshape(-1, nrows) if nrows else out
+
+
+def pj_solve_csr(row_ptr, col, val, contact_bias, mu, restitution, minv, mdiag, v, f_ext, f_gyro, dt, alpha,
+                 max_iter, tol_abs, tol_rel, lam0, nfl=0):
+    """Oracle for the solver-level drop-in (ProjectedJacobiSolver::solve, S = diag(M))."""
+    L = lib()
+    row_ptr = np.ascontiguousarray(row_ptr, np.int32)
+    col = np.ascontiguousarray(col, np.int32)
+    arrs = [np.ascontiguousarray(a, np.float64) for a in (val, contact_bias, mu, restitution, minv, mdiag, v,
+                                                          f_ext, f_gyro)]
+    nrows = row_ptr.shape[0] - 1
+    nv = arrs[4].shape[0]
+    lam = np.array(lam0, np.float64, copy=True)
+    x = np.empty(nv)
+    it = L.or_pj_solve_csr(nrows, nv, int(nfl), _ip(row_ptr), _ip(col), *[_dp(a) for a in arrs], float(dt),
+                           float(alpha), int(max_iter), float(tol_abs), float(tol_rel), _dp(lam), _dp(x))
+    return x, lam, it

@@ -1,0 +1,181 @@
+"""Known-answer tests that pin the CPU oracle (CPU only).
+
+The reference ships no tests or golden vectors for this path, so the oracle is pinned by physics
+with closed-form answers (Moreau midpoint free fall, resting load m*g*h, Coulomb sliding,
+drum wall drag) and by the projection branches of projected_jacobi.cpp:100-119.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from cardillocxx_gb300.scenes import make_scene
+
+G = 9.81
+H = 1e-3
+
+
+def cfg(**kw):
+    c = {"sim.dt": H, "moreau.theta": 0.5, "friction.enable": True, "friction.combine": "min",
+         "pj.max_iterations": 50, "pj.alpha": 0.5, "pj.tol_abs": 0.0, "pj.tol_rel": 0.0, "pj.warmstart": True,
+         "collision.match_max_dist": 0.02}
+    c.update(kw)
+    return c
+
+
+GROUND = {"kind": "halfspace", "pos": (0, 0, 0), "dir": (0, 0, 1), "mu": 0.3}
+
+
+def test_free_fall_midpoint_exact(oracle_mod):
+    s = make_scene([{"pos": (0.2, 0.3, 5.0), "radius": 0.05, "vel": (0.3, -0.2, 1.0)}], [GROUND])
+    o = oracle_mod.Oracle(s, cfg())
+    n = 200
+    o.step(n)
+    t = n * H
+    st = o.state()
+    exp = np.array([0.2 + 0.3 * t, 0.3 - 0.2 * t, 5.0 + 1.0 * t - 0.5 * G * t * t])
+    np.testing.assert_allclose(st["pos"][0], exp, rtol=0, atol=1e-12)
+    np.testing.assert_allclose(st["vel"][0], [0.3, -0.2, 1.0 - G * t], rtol=0, atol=1e-12)
+    assert o.stats()["num_contacts"] == 0
+
+
+def test_resting_contact_carries_weight(oracle_mod):
+    r = 0.05
+    s = make_scene([{"pos": (0.0, 0.0, r), "radius": r}], [GROUND])
+    m = s["mass"][0]
+    o = oracle_mod.Oracle(s, cfg())
+    o.step(1)
+    c = o.contacts()
+    assert c["id_a"].tolist() == [0] and c["id_b"].tolist() == [1]
+    np.testing.assert_allclose(c["lambda"][0, 0], m * G * H, rtol=1e-12)
+    assert abs(c["lambda"][0, 1]) < 1e-15 and abs(c["lambda"][0, 2]) < 1e-15
+    assert abs(o.state()["vel"][0, 2]) < 1e-13
+    np.testing.assert_allclose(c["normal"][0], [0, 0, 1])
+
+
+def test_sliding_friction_decelerates_mu_g(oracle_mod):
+    r, mu, v0 = 0.05, 0.3, 1.0
+    s = make_scene([{"pos": (0.0, 0.0, r), "radius": r, "vel": (v0, 0, 0), "mu": mu}], [dict(GROUND, mu=mu)])
+    o = oracle_mod.Oracle(s, cfg())
+    n = 10
+    o.step(n)
+    st = o.state()
+    np.testing.assert_allclose(st["vel"][0, 0], v0 - n * mu * G * H, rtol=1e-10)
+    # friction torque r mu m g about +y, I = 2/5 m r^2
+    np.testing.assert_allclose(st["omega"][0, 1], n * H * 5 * mu * G / (2 * r), rtol=1e-9)
+    lam = o.contacts()["lambda"][0]
+    m = s["mass"][0]
+    np.testing.assert_allclose(math.hypot(lam[1], lam[2]), mu * lam[0], rtol=1e-12)
+    np.testing.assert_allclose(lam[0], m * G * H, rtol=1e-10)
+
+
+def test_rotating_drum_drags_sphere(oracle_mod):
+    r, mu, w = 0.1, 0.4, 2.0
+    drum = {"kind": "drum", "pos": (0, 0, 0), "dir": (1, 0, 0), "radius": 1.0, "omega": (w, 0, 0), "mu": mu}
+    s = make_scene([{"pos": (0.5, 0.0, -0.9), "radius": r, "mu": mu}], [drum])
+    o = oracle_mod.Oracle(s, cfg())
+    o.step(1)
+    c = o.contacts()
+    m = s["mass"][0]
+    np.testing.assert_allclose(c["normal"][0], [0, 0, 1], atol=1e-15)
+    np.testing.assert_allclose(c["lambda"][0, 0], m * G * H, rtol=1e-10)
+    v = o.state()["vel"][0]
+    # wall point at the bottom moves along +y (omega x r_wall); sliding friction mu g h
+    np.testing.assert_allclose(v[1], mu * G * H, rtol=1e-9)
+    assert abs(v[2]) < 1e-12
+
+
+def test_static_drum_holds_sphere(oracle_mod):
+    r = 0.1
+    drum = {"kind": "drum", "pos": (0, 0, 0), "dir": (1, 0, 0), "radius": 1.0, "mu": 0.3}
+    s = make_scene([{"pos": (0.5, 0.0, -0.9), "radius": r}], [drum])
+    o = oracle_mod.Oracle(s, cfg())
+    o.step(5)
+    v = o.state()["vel"][0]
+    assert np.abs(v).max() < 1e-12
+
+
+def test_ceiling_contact_uses_south_pole_frame(oracle_mod):
+    # a sphere pressed up against a ceiling: normal (0,0,-1) takes the south-pole branch of
+    # tangentFrameFromNormal (tangent_frame.hpp:34-41)
+    r = 0.05
+    ceiling = {"kind": "halfspace", "pos": (0, 0, 1.0), "dir": (0, 0, -1), "mu": 0.3}
+    s = make_scene([{"pos": (0.0, 0.0, 1.0 - r), "radius": r, "vel": (0, 0, 0.5)}], [ceiling])
+    o = oracle_mod.Oracle(s, cfg(**{"sim.gravity": (0.0, 0.0, 0.0)}))
+    o.step(1)
+    c = o.contacts()
+    np.testing.assert_allclose(c["normal"][0], [0, 0, -1])
+    assert o.state()["vel"][0, 2] == pytest.approx(0.0, abs=1e-13)
+
+
+def _one_contact_problem(v, mu=0.3):
+    # one body with unit mass, one frictional contact with rows n = e_z, t1 = e_x, t2 = e_y
+    row_ptr = np.array([0, 1, 2, 3], np.int32)
+    col = np.array([2, 0, 1], np.int32)
+    val = np.ones(3)
+    ones6 = np.ones(6)
+    return dict(row_ptr=row_ptr, col=col, val=val, contact_bias=np.zeros(3), mu=np.full(3, mu),
+                restitution=np.zeros(3), minv=ones6, mdiag=ones6, v=np.asarray(v, float), f_ext=np.zeros(6),
+                f_gyro=np.zeros(6), dt=H, alpha=1.0, max_iter=50, tol_abs=0.0, tol_rel=0.0, lam0=np.zeros(3))
+
+
+@pytest.mark.parametrize("v,lam_exp,x_exp", [
+    ((0, 0, 1, 0, 0, 0), (0, 0, 0), (0, 0, 1)),           # separating: normal clamp to 0
+    ((0.1, 0, -1, 0, 0, 0), (1, -0.1, 0), (0, 0, 0)),      # sticking: inside the disk
+    ((1.0, 0, -1, 0, 0, 0), (1, -0.3, 0), (0.7, 0, 0)),    # sliding: scaled onto the disk
+    ((0, 0, -1, 0, 0, 0), (1, 0, 0), (0, 0, 0)),           # ||lambda_t|| = 0 branch
+])
+def test_projection_branches(oracle_mod, v, lam_exp, x_exp):
+    x, lam, it = oracle_mod.pj_solve_csr(**_one_contact_problem(v))
+    np.testing.assert_allclose(lam, lam_exp, atol=1e-14)
+    np.testing.assert_allclose(x[:3], x_exp, atol=1e-14)
+    assert it == 50
+
+
+def test_velocity_residual_early_exit(oracle_mod):
+    # the reference's own stop test (every 10th sweep, projected_jacobi.cpp:371-377)
+    p = _one_contact_problem((0.1, 0, -1, 0, 0, 0))
+    p.update(tol_abs=1e-6, tol_rel=1e-6, max_iter=1000)
+    x, lam, it = oracle_mod.pj_solve_csr(**p)
+    assert it in (1, 11, 21)
+    np.testing.assert_allclose(lam, (1, -0.1, 0), atol=1e-12)
+
+
+def test_warm_start_carries_impulse(oracle_mod):
+    r = 0.05
+    s = make_scene([{"pos": (0.0, 0.0, r), "radius": r}], [GROUND])
+    o = oracle_mod.Oracle(s, cfg(**{"pj.max_iterations": 1}))
+    m = s["mass"][0]
+    o.step(1)
+    l1 = o.contacts()["lambda"][0, 0]
+    o.step(1)
+    l2 = o.contacts()["lambda"][0, 0]
+    # one sweep per step at alpha 0.5: the warm start lets the impulse keep converging to m g h
+    assert l1 == pytest.approx(0.5 * m * G * H, rel=1e-12)
+    assert l2 > l1
+    o2 = oracle_mod.Oracle(s, cfg(**{"pj.max_iterations": 1, "pj.warmstart": False}))
+    o2.step(2)
+    assert o2.contacts()["lambda"][0, 0] < l2
+
+
+def test_pile_settles_without_nan(oracle_mod):
+    from cardillocxx_gb300 import scenes
+    s = scenes.generate("pile_1k", scale=0.1)
+    o = oracle_mod.Oracle(s, scenes.config_for("pile_1k"))
+    o.step(150)
+    st = o.state()
+    assert np.isfinite(st["pos"]).all() and np.isfinite(st["quat"]).all()
+    np.testing.assert_allclose(np.linalg.norm(st["quat"], axis=1), 1.0, atol=1e-14)
+    assert o.stats()["num_contacts"] > 0
+
+
+def test_omp_modes_bit_identical(oracle_mod):
+    from cardillocxx_gb300 import scenes
+    s = scenes.generate("pile_1k", scale=0.2)
+    c = scenes.config_for("pile_1k")
+    a = oracle_mod.Oracle(s, c, omp_mode=0)
+    b = oracle_mod.Oracle(s, c, omp_mode=1, num_threads=4)
+    a.step(120)
+    b.step(120)
+    for k in ("pos", "quat", "vel", "omega"):
+        assert np.array_equal(a.state()[k], b.state()[k]), k

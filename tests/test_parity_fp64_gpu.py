@@ -1,0 +1,181 @@
+"""Parity of the plain FP64 GPU method against the CPU oracle (GPU tests).
+
+The bar set by the path's definition is impulses within 1e-10 relative per iteration and
+trajectories within 1e-9 over the run; the plain method is built to be bit-identical (same
+operation order, no FMA contraction, deterministic gathers), so these tests assert exact equality
+and report the largest difference when it fails.
+"""
+import numpy as np
+import pytest
+
+from cardillocxx_gb300 import PhysicsEngine, scenes
+from cardillocxx_gb300.scenes import make_scene
+
+pytestmark = pytest.mark.gpu
+
+IT_RTOL = 1e-10   # per-iteration impulse tolerance (relative)
+TRAJ_TOL = 1e-9   # trajectory tolerance over the run
+
+
+def _max_rel(a, b):
+    a = np.asarray(a, float)
+    b = np.asarray(b, float)
+    if a.size == 0:
+        return 0.0
+    den = np.maximum(np.abs(b), 1e-300)
+    return float(np.max(np.abs(a - b) / np.maximum(den, np.max(np.abs(b)) * 1e-300 + 1e-300)))
+
+
+def assert_same(a, b, what, atol=0.0):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    assert a.shape == b.shape, (what, a.shape, b.shape)
+    if atol == 0.0:
+        if not np.array_equal(a, b):
+            d = np.abs(a.astype(float) - b.astype(float))
+            raise AssertionError(f"{what}: not bit-identical, max |diff| {np.nanmax(d):.3e}")
+    else:
+        np.testing.assert_allclose(a, b, rtol=0, atol=atol, err_msg=what)
+
+
+def run_pair(oracle_mod, scene, cfg, nsteps, check_every=None):
+    eng = PhysicsEngine(cfg).load_scene(scene)
+    orc = oracle_mod.Oracle(scene, cfg)
+    check_every = check_every or nsteps
+    done = 0
+    while done < nsteps:
+        k = min(check_every, nsteps - done)
+        eng.step(k)
+        orc.step(k)
+        done += k
+        g, o = eng.state(), orc.state()
+        for key in ("pos", "quat", "vel", "omega"):
+            assert_same(g[key], o[key], f"{key} after {done} steps")
+        gc, oc = eng.contacts(), orc.contacts()
+        for key in ("id_a", "id_b", "point", "lambda", "normal"):
+            assert_same(gc[key], oc[key], f"contact {key} after {done} steps")
+        gs, os_ = eng.stats(), orc.stats()
+        assert gs["iterations"] == os_["iterations"]
+        assert gs["num_contacts"] == os_["num_contacts"]
+        assert gs["num_rows"] == os_["num_rows"]
+        assert gs["residual"] == os_["residual"]
+    return eng, orc
+
+
+def test_known_answer_scenes(gpu, oracle_mod):
+    ground = {"kind": "halfspace", "pos": (0, 0, 0), "dir": (0, 0, 1), "mu": 0.3}
+    drum = {"kind": "drum", "pos": (0, 0, 0), "dir": (1, 0, 0), "radius": 1.0, "omega": (2.0, 0, 0), "mu": 0.4}
+    cfg = scenes.config_for("pile_1k")
+    cases = [
+        make_scene([{"pos": (0.0, 0.0, 0.05), "radius": 0.05, "vel": (1.0, 0, 0)}], [ground]),
+        make_scene([{"pos": (0.5, 0.0, -0.9), "radius": 0.1, "mu": 0.4}], [drum]),
+        make_scene([{"pos": (0.2, 0.3, 5.0), "radius": 0.05, "vel": (0.3, -0.2, 1.0)}], [ground]),
+        make_scene([{"pos": (0.0, 0.0, 0.05), "radius": 0.05}, {"pos": (0.0, 0.0, 0.15), "radius": 0.05}], [ground]),
+    ]
+    for s in cases:
+        run_pair(oracle_mod, s, cfg, 20, 5)
+
+
+def test_pile_small_bit_identical(gpu, oracle_mod):
+    s = scenes.generate("pile_1k", scale=0.2)
+    run_pair(oracle_mod, s, scenes.config_for("pile_1k"), 240, 40)
+
+
+def test_per_iteration_impulses(gpu, oracle_mod):
+    s = scenes.generate("pile_1k", scale=0.3)
+    cfg = scenes.config_for("pile_1k")
+    eng, orc = run_pair(oracle_mod, s, cfg, 200, 200)
+    eng.set_trace(True)
+    orc.set_trace(True)
+    eng.step(1)
+    orc.step(1)
+    nrows = orc.stats()["num_rows"]
+    assert nrows > 0
+    tg, to = eng.trace(nrows), orc.trace(nrows)
+    assert tg.shape == to.shape and tg.shape[0] == 50
+    scale = np.maximum(np.abs(to).max(axis=1, keepdims=True), 1e-300)
+    rel = np.abs(tg - to) / scale
+    assert rel.max() <= IT_RTOL, f"per-iteration impulse rel diff {rel.max():.3e}"
+    assert_same(tg, to, "trace")
+
+
+def test_pile_1k_full_run_trajectory(gpu, oracle_mod):
+    # the 1,000-sphere pile over its full 500 steps (the plain method's CPU-runnable case)
+    s = scenes.generate("pile_1k")
+    cfg = scenes.config_for("pile_1k")
+    eng = PhysicsEngine(cfg).load_scene(s)
+    orc = oracle_mod.Oracle(s, cfg, omp_mode=1)
+    eng.step(500)
+    orc.step(500)
+    g, o = eng.state(), orc.state()
+    for key in ("pos", "quat", "vel", "omega"):
+        d = np.abs(g[key] - o[key]).max()
+        assert d <= TRAJ_TOL, f"{key} trajectory diff {d:.3e}"
+        assert_same(g[key], o[key], key)
+
+
+def test_batched_scenes_parity(gpu, oracle_mod):
+    s = scenes.generate("batch_4096", scale=0.005)
+    assert s["num_scenes"] > 10
+    run_pair(oracle_mod, s, scenes.config_for("batch_4096"), 60, 30)
+
+
+def test_drum_parity(gpu, oracle_mod):
+    s = scenes.generate("drum_1m", scale=0.0004)
+    run_pair(oracle_mod, s, scenes.config_for("drum_1m"), 60, 20)
+
+
+def test_frictionless_mixture_and_options(gpu, oracle_mod):
+    s = scenes.generate("pile_1k", scale=0.15)
+    s["mu"][::3] = 0.0  # a third of the spheres frictionless: rows partitioned frictionless-first
+    cfg = scenes.config_for("pile_1k", **{"pj.warmstart": True, "friction.combine": "arith"})
+    run_pair(oracle_mod, s, cfg, 120, 60)
+    cfg2 = scenes.config_for("pile_1k", **{"friction.enable": False, "pj.warmstart": False})
+    run_pair(oracle_mod, s, cfg2, 80, 40)
+
+
+def test_stop_rules_match(gpu, oracle_mod):
+    s = scenes.generate("pile_1k", scale=0.15)
+    # the reference's velocity-increment test (every 10th sweep) and the residual test
+    cfg = scenes.config_for("pile_1k", **{"pj.tol_abs": 1e-6, "pj.tol_rel": 1e-4, "pj.max_iterations": 200})
+    run_pair(oracle_mod, s, cfg, 100, 50)
+    cfg2 = scenes.config_for("pile_1k", **{"gpu.residual_tol": 1e-3, "pj.max_iterations": 200})
+    run_pair(oracle_mod, s, cfg2, 100, 50)
+
+
+def test_csr_solver_dropin(gpu, oracle_mod):
+    rng = np.random.default_rng(7)
+    nb = 40
+    nv = 6 * nb
+    nfl = 6
+    nfr = 30
+    rows, cols, vals = [], [], []
+    ptr = [0]
+    for r in range(nfl + 3 * nfr):
+        a, b = sorted(rng.choice(nb, 2, replace=False))
+        for body in (a, b):
+            for k in range(6):
+                cols.append(6 * body + k)
+                vals.append(rng.normal())
+        ptr.append(len(cols))
+    ptr = np.array(ptr, np.int32)
+    col = np.array(cols, np.int32)
+    val = np.array(vals)
+    nrows = nfl + 3 * nfr
+    m = rng.uniform(0.5, 2.0, nv)
+    args = dict(row_ptr=ptr, col=col, val=val, contact_bias=rng.normal(size=nrows) * 0.1,
+                mu=rng.uniform(0.1, 0.6, nrows), restitution=rng.uniform(0, 0.2, nrows), minv=1.0 / m,
+                mdiag=1.0 / (1.0 / m), v=rng.normal(size=nv), f_ext=rng.normal(size=nv), f_gyro=rng.normal(size=nv) * 1e-3,
+                dt=1e-3, alpha=0.3, max_iter=40, tol_abs=0.0, tol_rel=0.0, lam0=np.abs(rng.normal(size=nrows)) * 0.01,
+                nfl=nfl)
+    xo, lo, ito = oracle_mod.pj_solve_csr(**args)
+    eng = PhysicsEngine(scenes.config_for("pile_1k"))
+    xg, lg, itg = eng.pj_solve_csr(**args)
+    assert ito == itg == 40
+    assert_same(xg, xo, "csr x")
+    assert_same(lg, lo, "csr lambda")
+    args.update(tol_abs=1e-7, tol_rel=1e-5, max_iter=2000)
+    xo, lo, ito = oracle_mod.pj_solve_csr(**args)
+    xg, lg, itg = eng.pj_solve_csr(**args)
+    assert ito == itg
+    assert_same(xg, xo, "csr x (early exit)")
