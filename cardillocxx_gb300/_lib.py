@@ -135,6 +135,7 @@ SIGNATURES = [
     ("cdx_get_trace", C.c_int, [C.c_void_p, _P, C.c_int64, C.POINTER(C.c_int64)]),
     ("cdx_set_timing", C.c_int, [C.c_void_p, C.c_int32]),
     ("cdx_stream", C.c_void_p, [C.c_void_p]),
+    ("cdx_time_sweeps", C.c_int, [C.c_void_p, C.c_int32, _P, _P, _P, _P]),
     ("cdx_pj_solve_csr", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, _PI, _PI, _P, _P, _P, _P, _P, _P,
                                    _P, _P, _P, C.c_double, C.c_double, C.c_int32, C.c_double, C.c_double, _P, _P,
                                    _PI]),

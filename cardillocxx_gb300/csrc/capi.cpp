@@ -95,4 +95,10 @@ int cdx_set_timing(cdx_ctx* ctx, int32_t on) {
 
 void* cdx_stream(cdx_ctx* ctx) { return ctx ? (void*)ctx->eng.stream : nullptr; }
 
+int cdx_time_sweeps(cdx_ctx* ctx, int32_t n, double* ms_contact, double* ms_body, double* bytes_contact,
+                    double* bytes_body) {
+    if (!ctx) return CDX_ERR_ARG;
+    return ctx->eng.time_sweeps(n, ms_contact, ms_body, bytes_contact, bytes_body);
+}
+
 }  // extern "C"

@@ -139,6 +139,9 @@ cudaError_t sort_pairs(void* tmp, size_t tmp_bytes, const uint32_t* kin, uint32_
                        uint32_t* vout, int64_t n, int end_bit, cudaStream_t s);
 void launch_cell_keys(const Scene& sc, const Grid& g, uint32_t* keys, uint32_t* vals, cudaStream_t s);
 void launch_ranges(const uint32_t* sorted_keys, int64_t n, int32_t* start, int32_t* end, cudaStream_t s);
+// state staging: 13 doubles per body, interleaved as the C ABI's host arrays
+void launch_pack_state(const Scene& sc, double* out, cudaStream_t s);
+void launch_unpack_state(const Scene& sc, const double* in, int mask, cudaStream_t s);
 
 // ---- FP64 plain method (k_fp64.cu) ----
 void launch_rhs64(const Scene& sc, double dt, const double* g, double* rhs, cudaStream_t s);

@@ -64,11 +64,11 @@ void Engine::dfree(void* p) {
 
 Engine::~Engine() {
     if (stream) cudaStreamSynchronize(stream);
+    destroy_split();
     for (void* p : owned) cudaFree(p);
     owned.clear();
     if (hs) cudaFreeHost(hs);
     for (auto& e : ev) if (e) cudaEventDestroy(e);
-    destroy_split();
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -215,12 +215,13 @@ int Engine::load_scene(const cdx_scene& s) {
 
     // free any previous scene
     cudaStreamSynchronize(stream);
+    destroy_split();
     for (void* p : owned) cudaFree(p);
     owned.clear();
     sc = Scene{};
     C = Contacts{};
     inc = Incidence{};
-    destroy_split();
+    trace_dev = nullptr;
     tmp = nullptr;
     tmp_bytes = 0;
     nc = 0;
@@ -255,6 +256,7 @@ int Engine::load_scene(const cdx_scene& s) {
     // per-body work arrays
     if ((st = dalloc((void**)&rhs, sizeof(double) * 6 * std::max(1, N), "rhs"))) return st;
     if ((st = dalloc((void**)&x, sizeof(double) * 6 * std::max(1, N), "x"))) return st;
+    if ((st = dalloc((void**)&stage, sizeof(double) * 13 * std::max(1, N), "state staging"))) return st;
     if ((st = dalloc((void**)&cell_key_in, sizeof(uint32_t) * std::max(1, N), "grid"))) return st;
     if ((st = dalloc((void**)&cell_val_in, sizeof(uint32_t) * std::max(1, N), "grid"))) return st;
     if ((st = dalloc((void**)&cell_key_out, sizeof(uint32_t) * std::max(1, N), "grid"))) return st;
@@ -548,44 +550,35 @@ int Engine::step(int nsteps) {
 
 int Engine::get_state(double* pos, double* quat, double* vel, double* omega) {
     if (!loaded) return fail(CDX_ERR_STATE, "no scene loaded");
+    const size_t N = (size_t)sc.N;
+    if (N == 0) return CDX_OK;
     int st;
-    if ((st = sync_state_to_fp64())) return st;
-    const int N = sc.N;
-    std::vector<double> B((size_t)BF_COUNT * N);
-    if ((st = cuda_check(cudaMemcpyAsync(B.data(), sc.B, sizeof(double) * B.size(), cudaMemcpyDeviceToHost, stream), "download"))) return st;
-    if ((st = cuda_check(cudaStreamSynchronize(stream), "download"))) return st;
-    auto bf = [&](int f, int i) { return B[(size_t)f * N + i]; };
-    for (int i = 0; i < N; ++i) {
-        for (int k = 0; k < 3; ++k) {
-            if (pos) pos[3 * (size_t)i + k] = bf(BF_PX + k, i);
-            if (vel) vel[3 * (size_t)i + k] = bf(BF_VX + k, i);
-            if (omega) omega[3 * (size_t)i + k] = bf(BF_WX + k, i);
-        }
-        for (int k = 0; k < 4; ++k)
-            if (quat) quat[4 * (size_t)i + k] = bf(BF_QX + k, i);
-    }
-    return CDX_OK;
+    launch_pack_state(sc, stage, stream);
+    ++launches;
+    // one copy per requested array straight into the caller's buffers
+    if (pos && (st = cuda_check(cudaMemcpyAsync(pos, stage, 8 * 3 * N, cudaMemcpyDeviceToHost, stream), "download"))) return st;
+    if (quat && (st = cuda_check(cudaMemcpyAsync(quat, stage + 3 * N, 8 * 4 * N, cudaMemcpyDeviceToHost, stream), "download"))) return st;
+    if (vel && (st = cuda_check(cudaMemcpyAsync(vel, stage + 7 * N, 8 * 3 * N, cudaMemcpyDeviceToHost, stream), "download"))) return st;
+    if (omega && (st = cuda_check(cudaMemcpyAsync(omega, stage + 10 * N, 8 * 3 * N, cudaMemcpyDeviceToHost, stream), "download"))) return st;
+    return cuda_check(cudaStreamSynchronize(stream), "download");
 }
 
 int Engine::set_state(const double* pos, const double* quat, const double* vel, const double* omega) {
     if (!loaded) return fail(CDX_ERR_STATE, "no scene loaded");
+    const size_t N = (size_t)sc.N;
+    if (N == 0) return CDX_OK;
     int st;
-    if ((st = sync_state_to_fp64())) return st;
-    const int N = sc.N;
-    std::vector<double> B((size_t)BF_COUNT * N);
-    if ((st = cuda_check(cudaMemcpy(B.data(), sc.B, sizeof(double) * B.size(), cudaMemcpyDeviceToHost), "download"))) return st;
-    auto bf = [&](int f, int i) -> double& { return B[(size_t)f * N + i]; };
-    for (int i = 0; i < N; ++i) {
-        for (int k = 0; k < 3; ++k) {
-            if (pos) bf(BF_PX + k, i) = pos[3 * (size_t)i + k];
-            if (vel) bf(BF_VX + k, i) = vel[3 * (size_t)i + k];
-            if (omega) bf(BF_WX + k, i) = omega[3 * (size_t)i + k];
-        }
-        for (int k = 0; k < 4; ++k)
-            if (quat) bf(BF_QX + k, i) = quat[4 * (size_t)i + k];
-    }
-    if ((st = cuda_check(cudaMemcpy(sc.B, B.data(), sizeof(double) * B.size(), cudaMemcpyHostToDevice), "upload"))) return st;
-    return mark_state_changed();
+    int mask = 0;
+    if (pos && (st = cuda_check(cudaMemcpyAsync(stage, pos, 8 * 3 * N, cudaMemcpyHostToDevice, stream), "upload"))) return st;
+    if (quat && (st = cuda_check(cudaMemcpyAsync(stage + 3 * N, quat, 8 * 4 * N, cudaMemcpyHostToDevice, stream), "upload"))) return st;
+    if (vel && (st = cuda_check(cudaMemcpyAsync(stage + 7 * N, vel, 8 * 3 * N, cudaMemcpyHostToDevice, stream), "upload"))) return st;
+    if (omega && (st = cuda_check(cudaMemcpyAsync(stage + 10 * N, omega, 8 * 3 * N, cudaMemcpyHostToDevice, stream), "upload"))) return st;
+    mask = (pos ? 1 : 0) | (quat ? 2 : 0) | (vel ? 4 : 0) | (omega ? 8 : 0);
+    launch_unpack_state(sc, stage, mask, stream);
+    ++launches;
+    // the warm-start memory (pair keys, points, impulses) is kept, as the reference's tracker
+    // keeps it across user edits of the state; matching is by pair and contact-point distance
+    return CDX_OK;
 }
 
 int Engine::get_contacts(int32_t* ia, int32_t* ib, double* point, double* lambda, double* normal, int32_t* count) {

@@ -27,6 +27,7 @@ struct Engine {
 
     double* rhs = nullptr;
     double* x = nullptr;
+    double* stage = nullptr;  // 13 N doubles: state staging for get/set_state
     uint32_t *cell_key_in = nullptr, *cell_val_in = nullptr, *cell_key_out = nullptr, *cell_val_out = nullptr;
     int32_t *cell_start = nullptr, *cell_end = nullptr;
     int32_t *sflags = nullptr, *spos = nullptr, *pcount = nullptr, *poff = nullptr;
@@ -77,10 +78,9 @@ struct Engine {
     // split-precision form (engine_split.cpp)
     int step_split();
     void destroy_split();
-    int sync_state_to_fp64();
-    int mark_state_changed();
     int get_contacts_split(int32_t* ia, int32_t* ib, double* point, double* lambda, double* normal, int32_t* count);
     double split_bytes_per_iter() const;
+    int time_sweeps(int n, double* msc, double* msb, double* bc, double* bb);
 };
 
 struct cdx_ctx {

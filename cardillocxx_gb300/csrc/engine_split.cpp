@@ -1,11 +1,409 @@
-// Split-precision form (FP32 contact/Delassus/projection, FP64 state): host side.
-#include "engine.h"
+// Host side of the split-precision form: FP32 collision and projected Jacobi, FP64 state, final
+// velocities and residual. The sweep loop runs as a CUDA graph with a device-side while node:
+// the check kernel ends the loop at the iteration cap or when the complementarity residual
+// reaches gpu.residual_tol, so a step needs no host round trip per sweep.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
 
-int Engine::step_split() { return fail(CDX_ERR_UNSUPPORTED, "split precision not built yet"); }
-void Engine::destroy_split() {}
-int Engine::sync_state_to_fp64() { return CDX_OK; }
-int Engine::mark_state_changed() { return CDX_OK; }
-int Engine::get_contacts_split(int32_t*, int32_t*, double*, double*, double*, int32_t*) {
-    return fail(CDX_ERR_UNSUPPORTED, "split precision not built yet");
+#include "engine.h"
+#include "split.h"
+
+using namespace cdx;
+
+namespace cdx {
+struct SplitState {
+    SplitBuf sb;
+    int gen = 0;
+    int prev_count = 0;
+    int nc = 0;
+    int sms = 148;
+    int32_t* h_nc = nullptr;  // pinned
+    SplitScalars* h_ss = nullptr;
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};
+    cudaGraph_t graph[2] = {nullptr, nullptr};
+    int graph_blocks = 0;
+    int graph_body_blocks = 0;
+    int graph_maxit = -1;
+    float graph_tol = -1.f;
+    int64_t graph_cap = -1;
+    std::vector<void*> bufs;
+    int last_iters = 0;
+    double res_last = 0, res_final = 0;
+};
+}  // namespace cdx
+
+static int salloc(Engine& E, void** p, size_t bytes, const char* what) {
+    int st = E.dalloc(p, bytes, what);
+    if (!st) E.split->bufs.push_back(*p);
+    return st;
 }
-double Engine::split_bytes_per_iter() const { return 0.0; }
+
+static void destroy_graphs(SplitState* S) {
+    for (int g = 0; g < 2; ++g) {
+        if (S->exec[g]) cudaGraphExecDestroy(S->exec[g]);
+        if (S->graph[g]) cudaGraphDestroy(S->graph[g]);
+        S->exec[g] = nullptr;
+        S->graph[g] = nullptr;
+    }
+    S->graph_cap = -1;
+}
+
+void Engine::destroy_split() {
+    if (!split) return;
+    destroy_graphs(split);
+    for (void* p : split->bufs) dfree(p);
+    if (split->h_nc) cudaFreeHost(split->h_nc);
+    if (split->h_ss) cudaFreeHost(split->h_ss);
+    delete split;
+    split = nullptr;
+}
+
+static int split_contacts(Engine& E, int64_t need) {
+    SplitState* S = E.split;
+    SplitBuf& b = S->sb;
+    if (need <= b.cap) return CDX_OK;
+    const int64_t cap = std::max<int64_t>(need + need / 4, 1024);
+    SplitBuf n = b;
+    n.cap = cap;
+    int st;
+    if ((st = salloc(E, (void**)&n.ab, sizeof(int2) * cap, "split contacts"))) return st;
+    float4** f4[] = {&n.nmu, &n.levR, &n.bias, &n.lam[0], &n.lam[1], &n.pt[0], &n.pt[1]};
+    for (auto p : f4)
+        if ((st = salloc(E, (void**)p, sizeof(float4) * cap, "split contacts"))) return st;
+    if ((st = salloc(E, (void**)&n.key[0], sizeof(unsigned long long) * cap, "split contacts"))) return st;
+    if ((st = salloc(E, (void**)&n.key[1], sizeof(unsigned long long) * cap, "split contacts"))) return st;
+    if ((st = salloc(E, (void**)&n.g64, sizeof(double) * 5 * cap, "split contacts"))) return st;
+    if (b.cap > 0 && S->prev_count > 0) {
+        const int pg = S->gen ^ 1;
+        cudaMemcpyAsync(n.key[pg], b.key[pg], sizeof(unsigned long long) * S->prev_count, cudaMemcpyDeviceToDevice, E.stream);
+        cudaMemcpyAsync(n.lam[pg], b.lam[pg], sizeof(float4) * S->prev_count, cudaMemcpyDeviceToDevice, E.stream);
+        cudaMemcpyAsync(n.pt[pg], b.pt[pg], sizeof(float4) * S->prev_count, cudaMemcpyDeviceToDevice, E.stream);
+        if ((st = E.cuda_check(cudaStreamSynchronize(E.stream), "split grow"))) return st;
+    }
+    if (b.cap > 0) {
+        void* old[] = {b.ab, b.nmu, b.levR, b.bias, b.lam[0], b.lam[1], b.pt[0], b.pt[1], b.key[0], b.key[1], b.g64};
+        for (void* p : old) {
+            auto& v = S->bufs;
+            v.erase(std::remove(v.begin(), v.end(), p), v.end());
+            E.dfree(p);
+        }
+        ++E.reallocations;
+    }
+    b = n;
+    destroy_graphs(S);
+    return E.ensure_tmp(cap);
+}
+
+static int init_split(Engine& E) {
+    E.split = new SplitState();
+    SplitState* S = E.split;
+    SplitBuf& b = S->sb;
+    const int N = E.sc.N, Ss = E.sc.S, nsc = E.sc.nscenes;
+    b.N = N;
+    int st;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&S->sms, cudaDevAttrMultiProcessorCount, dev);
+    const size_t n1 = std::max(1, N);
+    if ((st = salloc(E, (void**)&b.pos4, sizeof(float4) * n1, "split bodies"))) return st;
+    if ((st = salloc(E, (void**)&b.vel4, sizeof(float4) * 2 * n1, "split bodies"))) return st;
+    if ((st = salloc(E, (void**)&b.acc4, sizeof(float4) * 2 * n1, "split bodies"))) return st;
+    if ((st = salloc(E, (void**)&b.vn4, sizeof(float4) * 2 * n1, "split bodies"))) return st;
+    if ((st = salloc(E, (void**)&b.vfree, sizeof(double) * 6 * n1, "split bodies"))) return st;
+    if ((st = salloc(E, (void**)&b.acc64, sizeof(double) * 6 * n1, "split bodies"))) return st;
+    if ((st = salloc(E, (void**)&b.origin, sizeof(double) * 3 * nsc, "split scenes"))) return st;
+    const size_t s1 = std::max(1, Ss);
+    float4** f4[] = {&b.st_dir, &b.st_pt, &b.st_v, &b.st_w};
+    for (auto p : f4)
+        if ((st = salloc(E, (void**)p, sizeof(float4) * s1, "split statics"))) return st;
+    if ((st = salloc(E, (void**)&b.nc_dev, sizeof(int32_t), "split"))) return st;
+    if ((st = salloc(E, (void**)&b.ss, sizeof(SplitScalars), "split"))) return st;
+    if ((st = E.cuda_check(cudaMallocHost((void**)&S->h_nc, sizeof(int32_t)), "pinned"))) return st;
+    if ((st = E.cuda_check(cudaMallocHost((void**)&S->h_ss, sizeof(SplitScalars)), "pinned"))) return st;
+    cudaMemsetAsync(b.ss, 0, sizeof(SplitScalars), E.stream);
+    cudaMemsetAsync(b.nc_dev, 0, sizeof(int32_t), E.stream);
+    // scene origins: centroid of each scene's bodies (FP32 coordinates stay small)
+    std::vector<double> B((size_t)BF_COUNT * N), org(3 * (size_t)nsc, 0.0);
+    if (N) {
+        if ((st = E.cuda_check(cudaMemcpy(B.data(), E.sc.B, sizeof(double) * B.size(), cudaMemcpyDeviceToHost), "origins"))) return st;
+    }
+    for (int s = 0; s < nsc; ++s) {
+        const int b0 = E.h_scene_body_start[s], b1 = E.h_scene_body_start[s + 1];
+        for (int k = 0; k < 3; ++k) {
+            double acc = 0;
+            for (int i = b0; i < b1; ++i) acc += B[(size_t)(BF_PX + k) * N + i];
+            org[3 * s + k] = b1 > b0 ? std::round(acc / (b1 - b0) * 64.0) / 64.0 : 0.0;
+        }
+    }
+    if ((st = E.cuda_check(cudaMemcpy(b.origin, org.data(), sizeof(double) * org.size(), cudaMemcpyHostToDevice), "origins"))) return st;
+    const int64_t cap0 = std::max<int64_t>(1024, (int64_t)(E.cfg.gpu_contact_capacity_factor * std::max(1, N)));
+    return split_contacts(E, cap0);
+}
+
+static int build_graph(Engine& E, int g) {
+    SplitState* S = E.split;
+    const int maxit = std::max(1, E.cfg.pj_max_iterations);
+    const float tol = (float)E.cfg.gpu_residual_tol;
+    cudaGraph_t graph;
+    int st;
+    if ((st = E.cuda_check(cudaGraphCreate(&graph, 0), "graph create"))) return st;
+    cudaGraphConditionalHandle h;
+    if ((st = E.cuda_check(cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault), "cond handle"))) return st;
+    alignas(cudaGraphNodeParams) unsigned char pbuf[sizeof(cudaGraphNodeParams)];
+    std::memset(pbuf, 0, sizeof(pbuf));
+    cudaGraphNodeParams& p = *reinterpret_cast<cudaGraphNodeParams*>(pbuf);
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = cudaGraphCondTypeWhile;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    if ((st = E.cuda_check(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &p), "cond node"))) return st;
+    cudaGraph_t body = p.conditional.phGraph_out[0];
+    if ((st = E.cuda_check(cudaStreamBeginCaptureToGraph(E.stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed),
+                           "capture"))) return st;
+    launch_s_contact(S->sb, g, S->graph_blocks, E.stream);
+    launch_s_body(S->sb, E.sc.N, S->graph_body_blocks, 0, E.stream);
+    launch_s_check(S->sb, maxit, tol, h, 1, E.stream);
+    cudaGraph_t captured = nullptr;
+    if ((st = E.cuda_check(cudaStreamEndCapture(E.stream, &captured), "end capture"))) return st;
+    if ((st = E.cuda_check(cudaGraphInstantiate(&S->exec[g], graph, 0), "graph instantiate"))) return st;
+    S->graph[g] = graph;
+    return CDX_OK;
+}
+
+int Engine::step_split() {
+    int st;
+    if (!split && (st = init_split(*this))) return st;
+    SplitState* S = split;
+    SplitBuf& sb = S->sb;
+    const int N = sc.N;
+    const double dt = cfg.sim_dt, th = cfg.moreau_theta;
+    SplitParams P;
+    P.alpha = (float)cfg.pj_alpha;
+    P.margin = (float)cfg.collision_security_margin;
+    P.match2 = (float)(cfg.collision_match_max_dist * cfg.collision_match_max_dist);
+    P.combine = cfg.friction_combine;
+    P.friction_enable = cfg.friction_enable;
+    P.prev_count = cfg.pj_warmstart ? S->prev_count : 0;
+    const int gen = S->gen;
+
+    if (timing) cudaEventRecord(ev[0], stream);
+    launch_s_prep(sc, sb, dt, cfg.sim_gravity, (1.0 - th) * dt, stream);
+    launch_cell_keys(sc, grid, cell_key_in, cell_val_in, stream);
+    if ((st = cuda_check(sort_pairs(tmp, tmp_bytes, cell_key_in, cell_key_out, cell_val_in, cell_val_out, N,
+                                    grid.key_bits, stream), "sort cells"))) return st;
+    cudaMemsetAsync(cell_start, 0, sizeof(int32_t) * grid.ncells, stream);
+    cudaMemsetAsync(cell_end, 0, sizeof(int32_t) * grid.ncells, stream);
+    launch_ranges(cell_key_out, N, cell_start, cell_end, stream);
+    launches += 8;
+    const int64_t nflag = (int64_t)N * sc.max_statics;
+    if (nflag > 0) {
+        launch_s_static_flags(sc, sb, P.margin, sflags, stream);
+        if ((st = cuda_check(exclusive_scan(tmp, tmp_bytes, sflags, spos, nflag, stream), "scan"))) return st;
+        launches += 3;
+    }
+    launch_s_pair_count(sc, grid, sb, cell_val_out, cell_start, cell_end, pcount, P, ds, stream);
+    if ((st = cuda_check(exclusive_scan(tmp, tmp_bytes, pcount, poff, N + 1, stream), "scan"))) return st;
+    launches += 3;
+    int32_t tot[4] = {0, 0, 0, 0};
+    if (nflag > 0) {
+        cudaMemcpyAsync(&tot[0], spos + nflag - 1, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+        cudaMemcpyAsync(&tot[1], sflags + nflag - 1, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+    }
+    cudaMemcpyAsync(&tot[2], poff + N, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(&tot[3], &ds->overflow, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+    if ((st = cuda_check(cudaStreamSynchronize(stream), "collision counts"))) return st;
+    if (tot[3]) return fail(CDX_ERR_OVERFLOW, "a sphere touches more than 64 higher-index spheres");
+    const int64_t n_static = (int64_t)tot[0] + tot[1];
+    const int64_t n_pair = tot[2];
+    if ((st = split_contacts(*this, n_static + n_pair))) return st;
+    S->nc = (int)(n_static + n_pair);
+    *S->h_nc = S->nc;
+    cudaMemcpyAsync(sb.nc_dev, S->h_nc, sizeof(int32_t), cudaMemcpyHostToDevice, stream);
+    if (nflag > 0 && n_static > 0) {
+        launch_s_static_write(sc, sb, sflags, spos, gen, P, stream);
+        ++launches;
+    }
+    if (n_pair > 0) {
+        launch_s_pair_write(sc, grid, sb, cell_val_out, cell_start, cell_end, poff, (int32_t)n_static, gen, P, ds, stream);
+        ++launches;
+    }
+    if (timing) cudaEventRecord(ev[1], stream);
+    // x0 = v_free + M^-1 W^T lambda_warm
+    const int cblocks = split_grid_blocks(std::max(S->nc, 1), S->sms);
+    const int bblocks = split_grid_blocks(std::max(N, 1), S->sms);
+    launch_s_reset(sb, stream);
+    launch_s_apply_warm(sb, gen, cblocks, stream);
+    launch_s_body(sb, N, bblocks, 1, stream);
+    launches += 3;
+    if (timing) cudaEventRecord(ev[2], stream);
+    const int maxit = std::max(1, cfg.pj_max_iterations);
+    if (S->nc > 0) {
+        if (cfg.gpu_use_graph) {
+            // grid sized for the capacity so a graph serves every step until the buffers grow
+            const int gblocks = split_grid_blocks(sb.cap, S->sms);
+            const float tol = (float)cfg.gpu_residual_tol;
+            if (S->graph_cap != sb.cap || S->graph_maxit != maxit || S->graph_tol != tol) {
+                destroy_graphs(S);
+                S->graph_blocks = gblocks;
+                S->graph_body_blocks = bblocks;
+                if ((st = build_graph(*this, 0)) || (st = build_graph(*this, 1))) return st;
+                S->graph_cap = sb.cap;
+                S->graph_maxit = maxit;
+                S->graph_tol = tol;
+            }
+            if ((st = cuda_check(cudaGraphLaunch(S->exec[gen], stream), "graph launch"))) return st;
+        } else {
+            const int every = std::max(1, cfg.gpu_check_every);
+            cudaGraphConditionalHandle none = 0;
+            for (int it = 0; it < maxit; ++it) {
+                launch_s_contact(sb, gen, cblocks, stream);
+                launch_s_body(sb, N, bblocks, 0, stream);
+                launch_s_check(sb, maxit, (float)cfg.gpu_residual_tol, none, 0, stream);
+                if ((it + 1) % every == 0 && it + 1 < maxit) {
+                    cudaMemcpyAsync(&S->h_ss->done, &sb.ss->done, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+                    if ((st = cuda_check(cudaStreamSynchronize(stream), "poll"))) return st;
+                    if (S->h_ss->done) break;
+                }
+            }
+        }
+    }
+    if (timing) cudaEventRecord(ev[3], stream);
+    // FP64: final velocities, residual, write back, drift theta h
+    launch_s_final(sc, sb, gen, cfg.pj_alpha, cfg.friction_enable, cfg.friction_combine, cblocks, stream);
+    launch_drift64(sc, th * dt, 0, stream);
+    launches += 7;
+    if (timing) cudaEventRecord(ev[4], stream);
+    cudaMemcpyAsync(S->h_ss, sb.ss, sizeof(SplitScalars), cudaMemcpyDeviceToHost, stream);
+    if ((st = cuda_check(cudaStreamSynchronize(stream), "split step"))) return st;
+    if ((st = cuda_check(cudaGetLastError(), "split launch"))) return st;
+    S->last_iters = S->nc > 0 ? S->h_ss->iters : 0;
+    launches += 3 * (int64_t)S->last_iters;
+    S->res_last = S->h_ss->res_last;
+    S->res_final = S->nc > 0 ? S->h_ss->res_final : 0.0;
+    S->prev_count = S->nc;
+    S->gen ^= 1;
+    // mirror into the common stats fields
+    prev_count = S->nc;
+    last_iters = S->last_iters;
+    last_rows = 3 * S->nc;
+    last_res = S->res_last;
+    last_res_final = S->res_final;
+    ++steps;
+    if (timing) {
+        float a = 0, b = 0, c2 = 0, d = 0;
+        cudaEventElapsedTime(&a, ev[0], ev[1]);
+        cudaEventElapsedTime(&b, ev[1], ev[2]);
+        cudaEventElapsedTime(&c2, ev[2], ev[3]);
+        cudaEventElapsedTime(&d, ev[3], ev[4]);
+        ms[0] = a; ms[1] = b; ms[2] = c2; ms[3] = d;
+    }
+    return CDX_OK;
+}
+
+int Engine::get_contacts_split(int32_t* ia, int32_t* ib, double* point, double* lambda, double* normal,
+                               int32_t* count) {
+    const int n = split ? split->prev_count : 0;
+    if (count) *count = n;
+    if (n == 0 || (!ia && !ib && !point && !lambda && !normal)) return CDX_OK;
+    SplitBuf& sb = split->sb;
+    const int g = split->gen ^ 1;
+    std::vector<unsigned long long> keys(n);
+    std::vector<float4> pt(n), lam(n), nm(n);
+    int st;
+    if ((st = cuda_check(cudaMemcpy(keys.data(), sb.key[g], 8 * (size_t)n, cudaMemcpyDeviceToHost), "download"))) return st;
+    if ((st = cuda_check(cudaMemcpy(pt.data(), sb.pt[g], 16 * (size_t)n, cudaMemcpyDeviceToHost), "download"))) return st;
+    if ((st = cuda_check(cudaMemcpy(lam.data(), sb.lam[g], 16 * (size_t)n, cudaMemcpyDeviceToHost), "download"))) return st;
+    if ((st = cuda_check(cudaMemcpy(nm.data(), sb.nmu, 16 * (size_t)n, cudaMemcpyDeviceToHost), "download"))) return st;
+    std::vector<double> org(3 * (size_t)sc.nscenes);
+    if ((st = cuda_check(cudaMemcpy(org.data(), sb.origin, 8 * org.size(), cudaMemcpyDeviceToHost), "download"))) return st;
+    std::vector<int32_t> bscene(sc.N);
+    if (sc.N && (st = cuda_check(cudaMemcpy(bscene.data(), sc.body_scene, 4 * (size_t)sc.N, cudaMemcpyDeviceToHost), "download"))) return st;
+    for (int c = 0; c < n; ++c) {
+        const int32_t a = (int32_t)(keys[c] >> 32), b = (int32_t)(keys[c] & 0xffffffffu);
+        if (ia) ia[c] = a;
+        if (ib) ib[c] = b;
+        const int scn = bscene[b - sc.S];
+        const float p[3] = {pt[c].x, pt[c].y, pt[c].z}, l[3] = {lam[c].x, lam[c].y, lam[c].z},
+                    nn[3] = {nm[c].x, nm[c].y, nm[c].z};
+        for (int k = 0; k < 3; ++k) {
+            if (point) point[3 * (size_t)c + k] = (double)p[k] + org[3 * scn + k];
+            if (lambda) lambda[3 * (size_t)c + k] = l[k];
+            if (normal) normal[3 * (size_t)c + k] = nn[k];
+        }
+    }
+    return CDX_OK;
+}
+
+double Engine::split_bytes_per_iter() const {
+    // per contact: ab (8) + nmu (16) + levR (16) + bias (16) + lambda read+write (32); per body:
+    // vel4 read+write (64) + acc4 read+write (64)
+    const int n = split ? split->prev_count : 0;
+    return (double)n * (8 + 16 + 16 + 16 + 32) + (double)sc.N * 128.0;
+}
+
+// Kernel-level timing of the sweep (CUDA events around each launch, engine stream).
+int Engine::time_sweeps(int n, double* msc, double* msb, double* bc, double* bb) {
+    if (!loaded) return fail(CDX_ERR_STATE, "no scene loaded");
+    if (n <= 0) return fail(CDX_ERR_ARG, "n must be positive");
+    cudaEvent_t e[4];
+    for (auto& x : e) cudaEventCreate(&x);
+    double tc = 0, tb = 0;
+    int st = CDX_OK;
+    const bool sp = cfg.gpu_precision == CDX_PRECISION_SPLIT;
+    if (sp && split && split->prev_count > 0) {
+        SplitState* S = split;
+        const int g = S->gen ^ 1;
+        const int cblocks = split_grid_blocks(S->prev_count, S->sms);
+        const int bblocks = split_grid_blocks(std::max(sc.N, 1), S->sms);
+        *S->h_nc = S->prev_count;
+        cudaMemcpyAsync(S->sb.nc_dev, S->h_nc, sizeof(int32_t), cudaMemcpyHostToDevice, stream);
+        cudaMemsetAsync(S->sb.ss, 0, sizeof(SplitScalars), stream);
+        for (int k = 0; k < n; ++k) {
+            cudaEventRecord(e[0], stream);
+            launch_s_contact(S->sb, g, cblocks, stream);
+            cudaEventRecord(e[1], stream);
+            launch_s_body(S->sb, sc.N, bblocks, 0, stream);
+            cudaEventRecord(e[2], stream);
+            if ((st = cuda_check(cudaEventSynchronize(e[2]), "time sweeps"))) break;
+            float a = 0, b = 0;
+            cudaEventElapsedTime(&a, e[0], e[1]);
+            cudaEventElapsedTime(&b, e[1], e[2]);
+            tc += a;
+            tb += b;
+        }
+        launches += 2 * (int64_t)n;
+        if (bc) *bc = (double)S->prev_count * 76.0;
+        if (bb) *bb = (double)sc.N * 96.0;
+    } else if (!sp && prev_count > 0) {
+        const int g = gen ^ 1;
+        cudaMemsetAsync(ds, 0, sizeof(DevScalars), stream);
+        for (int k = 0; k < n; ++k) {
+            cudaEventRecord(e[0], stream);
+            launch_sweep_contact64(sc, C, g, prev_count, x, ds, 0, stream);
+            cudaEventRecord(e[1], stream);
+            launch_sweep_body64(sc, C, inc, x, 0.0, 0.0, 0, ds, stream);
+            cudaEventRecord(e[2], stream);
+            if ((st = cuda_check(cudaEventSynchronize(e[2]), "time sweeps"))) break;
+            float a = 0, b = 0;
+            cudaEventElapsedTime(&a, e[0], e[1]);
+            cudaEventElapsedTime(&b, e[1], e[2]);
+            tc += a;
+            tb += b;
+        }
+        launches += 2 * (int64_t)n;
+        // contact kernel: ids, flags, RW (27 words), bias (3), mu, lambda read+write, dlambda write
+        if (bc) *bc = (double)prev_count * (8 + 4 + 27 * 8 + 3 * 8 + 8 + 6 * 8 + 3 * 8);
+        // body kernel: incidence ranges, x read+write, M, and the gathered rows (dir, lever, dlambda)
+        if (bb) *bb = (double)sc.N * (8 + 12 * 8 + 2 * 8) + (double)prev_count * (9 + 9 + 9 + 3) * 8;
+    } else {
+        st = fail(CDX_ERR_STATE, "no contacts from a previous step");
+    }
+    for (auto& x : e) cudaEventDestroy(x);
+    if (st) return st;
+    if (msc) *msc = tc / n;
+    if (msb) *msb = tb / n;
+    return CDX_OK;
+}

@@ -73,3 +73,38 @@ void launch_ranges(const uint32_t* sorted_keys, int64_t n, int32_t* start, int32
 }
 
 }  // namespace cdx
+
+namespace cdx {
+namespace {
+// interleaved host layout <-> field-major device state: pos[3N], quat[4N], vel[3N], omega[3N]
+__global__ void k_pack_state(Scene sc, double* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sc.N) return;
+    const size_t N = sc.N;
+    for (int k = 0; k < 3; ++k) {
+        out[3 * (size_t)i + k] = sc.bf(BF_PX + k)[i];
+        out[7 * N + 3 * (size_t)i + k] = sc.bf(BF_VX + k)[i];
+        out[10 * N + 3 * (size_t)i + k] = sc.bf(BF_WX + k)[i];
+    }
+    for (int k = 0; k < 4; ++k) out[3 * N + 4 * (size_t)i + k] = sc.bf(BF_QX + k)[i];
+}
+__global__ void k_unpack_state(Scene sc, const double* in, int mask) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sc.N) return;
+    const size_t N = sc.N;
+    for (int k = 0; k < 3; ++k) {
+        if (mask & 1) sc.bf(BF_PX + k)[i] = in[3 * (size_t)i + k];
+        if (mask & 4) sc.bf(BF_VX + k)[i] = in[7 * N + 3 * (size_t)i + k];
+        if (mask & 8) sc.bf(BF_WX + k)[i] = in[10 * N + 3 * (size_t)i + k];
+    }
+    if (mask & 2)
+        for (int k = 0; k < 4; ++k) sc.bf(BF_QX + k)[i] = in[3 * N + 4 * (size_t)i + k];
+}
+}  // namespace
+void launch_pack_state(const Scene& sc, double* out, cudaStream_t s) {
+    if (sc.N) k_pack_state<<<nblk(sc.N), NT, 0, s>>>(sc, out);
+}
+void launch_unpack_state(const Scene& sc, const double* in, int mask, cudaStream_t s) {
+    if (sc.N) k_unpack_state<<<nblk(sc.N), NT, 0, s>>>(sc, in, mask);
+}
+}  // namespace cdx

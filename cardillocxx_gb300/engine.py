@@ -139,6 +139,12 @@ class PhysicsEngine:
         self._check(self.L.cdx_get_state(self.h, dp(pos), dp(quat), dp(vel), dp(om)))
         return {"pos": pos, "quat": quat, "vel": vel, "omega": om}
 
+    def state_into(self, pos, quat, vel, omega):
+        """Copy the state into caller-owned host arrays (e.g. pinned buffers); one D2H copy each."""
+        for a in (pos, quat, vel, omega):
+            assert a is None or (a.dtype == np.float64 and a.flags["C_CONTIGUOUS"])
+        self._check(self.L.cdx_get_state(self.h, dp(pos), dp(quat), dp(vel), dp(omega)))
+
     def set_state(self, pos=None, quat=None, vel=None, omega=None):
         conv = [None if a is None else np.ascontiguousarray(a, np.float64) for a in (pos, quat, vel, omega)]
         self._check(self.L.cdx_set_state(self.h, *[dp(a) for a in conv]))
@@ -166,6 +172,13 @@ class PhysicsEngine:
         out = np.empty(n.value)
         self._check(self.L.cdx_get_trace(self.h, dp(out), n.value, C.byref(n)))
         return out.reshape(-1, nrows) if nrows else out
+
+    def time_sweeps(self, n: int = 20) -> dict:
+        """Average per-launch time and algorithmic bytes of the sweep kernels (CUDA events)."""
+        vals = [C.c_double(0) for _ in range(4)]
+        self._check(self.L.cdx_time_sweeps(self.h, int(n), *[C.byref(v) for v in vals]))
+        return {"ms_contact": vals[0].value, "ms_body": vals[1].value, "bytes_contact": vals[2].value,
+                "bytes_body": vals[3].value}
 
     def stream(self) -> int:
         return int(self.L.cdx_stream(self.h) or 0)

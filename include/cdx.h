@@ -146,6 +146,12 @@ int cdx_get_trace(cdx_ctx* ctx, double* out, int64_t max_values, int64_t* num_va
 int cdx_set_timing(cdx_ctx* ctx, int32_t on);
 /* the stream the engine launches on (cudaStream_t as void*) */
 void* cdx_stream(cdx_ctx* ctx);
+/* Re-run `n` projected-Jacobi sweeps on the last step's contacts, timing every launch of the
+ * contact kernel and of the body kernel with CUDA events on the engine's stream. Returns the
+ * average milliseconds per launch and the algorithmic bytes one launch moves. Leaves the solver
+ * temporaries (not the body state) modified: call it after the steps being measured. */
+int cdx_time_sweeps(cdx_ctx* ctx, int32_t n, double* ms_contact, double* ms_body, double* bytes_contact,
+                    double* bytes_body);
 
 /* ---- solver-level drop-in: ProjectedJacobiSolver::solve(dt, theta)
  * (src/physics/solver/projected_jacobi.cpp:451-500) with S = diag(M) (pj_assembler.cpp:127-182).

@@ -1,0 +1,139 @@
+"""Split-precision form (FP32 contacts/Delassus/projection, FP64 state and residual) -- GPU tests.
+
+Known answers hold to FP32 accuracy; against the plain FP64 method the split form agrees to the
+FP32 rounding level on one step from the same state, and statistically over a run.
+"""
+import numpy as np
+import pytest
+
+from cardillocxx_gb300 import PhysicsEngine, scenes
+from cardillocxx_gb300.scenes import make_scene
+
+pytestmark = pytest.mark.gpu
+
+G = 9.81
+H = 1e-3
+F32_RTOL = 2e-5  # FP32 contact arithmetic: relative tolerance on impulses and velocities
+
+
+def cfg(**kw):
+    c = {"sim.dt": H, "moreau.theta": 0.5, "friction.enable": True, "friction.combine": "min",
+         "pj.max_iterations": 50, "pj.alpha": 0.5, "pj.tol_abs": 0.0, "pj.tol_rel": 0.0, "pj.warmstart": True,
+         "gpu.precision": "split"}
+    c.update(kw)
+    return c
+
+
+GROUND = {"kind": "halfspace", "pos": (0, 0, 0), "dir": (0, 0, 1), "mu": 0.3}
+
+
+def test_split_resting_and_sliding(gpu):
+    r, mu = 0.05, 0.3
+    s = make_scene([{"pos": (0.0, 0.0, r - 1e-5), "radius": r, "vel": (1.0, 0, 0), "mu": mu}], [GROUND])
+    e = PhysicsEngine(cfg()).load_scene(s)
+    n = 10
+    e.step(n)
+    st = e.state()
+    m = s["mass"][0]
+    np.testing.assert_allclose(st["vel"][0, 0], 1.0 - n * mu * G * H, rtol=F32_RTOL)
+    np.testing.assert_allclose(st["omega"][0, 1], n * H * 5 * mu * G / (2 * r), rtol=1e-4)
+    lam = e.contacts()["lambda"][0]
+    np.testing.assert_allclose(lam[0], m * G * H, rtol=F32_RTOL)
+    assert e.stats()["residual"] < 1e-5
+
+
+def test_split_free_fall_is_fp64_exact(gpu):
+    s = make_scene([{"pos": (0.2, 0.3, 5.0), "radius": 0.05, "vel": (0.3, -0.2, 1.0)}], [GROUND])
+    e = PhysicsEngine(cfg()).load_scene(s)
+    e.step(200)
+    t = 200 * H
+    np.testing.assert_allclose(e.state()["pos"][0], [0.2 + 0.3 * t, 0.3 - 0.2 * t, 5.0 + t - 0.5 * G * t * t],
+                               rtol=0, atol=1e-12)
+
+
+def test_split_drum_drag(gpu):
+    r, mu, w = 0.1, 0.4, 2.0
+    drum = {"kind": "drum", "pos": (0, 0, 0), "dir": (1, 0, 0), "radius": 1.0, "omega": (w, 0, 0), "mu": mu}
+    # 10 micrometres of overlap: an exactly touching pair can round to a positive FP32 gap
+    s = make_scene([{"pos": (0.5, 0.0, -0.90001), "radius": r, "mu": mu}], [drum])
+    e = PhysicsEngine(cfg()).load_scene(s)
+    e.step(1)
+    v = e.state()["vel"][0]
+    np.testing.assert_allclose(v[1], mu * G * H, rtol=1e-4)
+    assert abs(v[2]) < 1e-6
+
+
+def test_split_one_step_matches_fp64(gpu):
+    s = scenes.generate("pile_1k", scale=0.3)
+    base = scenes.config_for("pile_1k")
+    ref = PhysicsEngine(base).load_scene(s)
+    ref.step(250)
+    st = ref.state()
+    # one step from the same state, no warm start, iterated far enough that both forms converge
+    c = dict(base, **{"pj.warmstart": False, "pj.max_iterations": 3000})
+    e64 = PhysicsEngine(c).load_scene(s)
+    e32 = PhysicsEngine(dict(c, **{"gpu.precision": "split"})).load_scene(s)
+    for e in (e64, e32):
+        e.set_state(st["pos"], st["quat"], st["vel"], st["omega"])
+        e.step(1)
+    c64, c32 = e64.contacts(), e32.contacts()
+    assert np.array_equal(c64["id_a"], c32["id_a"]) and np.array_equal(c64["id_b"], c32["id_b"])
+    lmax = np.abs(c64["lambda"]).max()
+    assert np.abs(c64["lambda"][:, 0] - c32["lambda"][:, 0]).max() <= 5e-3 * lmax
+    v64, v32 = e64.state()["vel"], e32.state()["vel"]
+    vscale = np.abs(st["vel"]).max() + G * H
+    assert np.abs(v64 - v32).max() <= 5e-3 * vscale
+    np.testing.assert_allclose(e64.state()["pos"], e32.state()["pos"], rtol=0, atol=1e-7)
+
+
+def test_split_residual_is_fp64_and_decreases(gpu):
+    s = scenes.generate("pile_1k", scale=0.3)
+    base = scenes.config_for("pile_1k", **{"gpu.precision": "split"})
+    e = PhysicsEngine(base).load_scene(s)
+    e.step(250)
+    res = {}
+    for it in (10, 100, 1000):
+        ee = PhysicsEngine(dict(base, **{"pj.max_iterations": it, "pj.warmstart": False})).load_scene(s)
+        st = e.state()
+        ee.set_state(st["pos"], st["quat"], st["vel"], st["omega"])
+        ee.step(1)
+        res[it] = ee.stats()["residual"]
+    assert res[1000] < res[100] < res[10]
+    assert res[1000] < 1e-4
+
+
+def test_split_residual_stop_rule(gpu):
+    s = scenes.generate("pile_1k", scale=0.3)
+    c = scenes.config_for("pile_1k", **{"gpu.precision": "split", "pj.max_iterations": 400,
+                                        "gpu.residual_tol": 1e-3})
+    e = PhysicsEngine(c).load_scene(s)
+    e.step(200)
+    st = e.stats()
+    assert st["iterations"] < 400
+    assert st["residual_last"] <= 1e-3
+
+
+def test_split_pile_statistics_match_fp64(gpu):
+    s = scenes.generate("pile_1k", scale=0.5)
+    base = scenes.config_for("pile_1k")
+    e64 = PhysicsEngine(base).load_scene(s)
+    e32 = PhysicsEngine(dict(base, **{"gpu.precision": "split"})).load_scene(s)
+    e64.step(400)
+    e32.step(400)
+    z64, z32 = e64.state()["pos"][:, 2], e32.state()["pos"][:, 2]
+    assert abs(z64.mean() - z32.mean()) < 2e-3
+    assert abs(e64.stats()["num_contacts"] - e32.stats()["num_contacts"]) <= 0.05 * e64.stats()["num_contacts"] + 5
+    assert np.isfinite(e32.state()["vel"]).all()
+
+
+def test_split_batched_and_graph_off(gpu):
+    s = scenes.generate("batch_4096", scale=0.01)
+    c = scenes.config_for("batch_4096", **{"gpu.precision": "split"})
+    a = PhysicsEngine(c).load_scene(s)
+    b = PhysicsEngine(dict(c, **{"gpu.graph": False})).load_scene(s)
+    a.step(150)
+    b.step(150)
+    za, zb = a.state()["pos"][:, 2], b.state()["pos"][:, 2]
+    assert np.isfinite(za).all() and np.isfinite(zb).all()
+    assert abs(za.mean() - zb.mean()) < 1e-3
+    assert a.stats()["iterations"] == b.stats()["iterations"] == 50
