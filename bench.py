@@ -53,6 +53,7 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=20.0)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-graph", action="store_true", help="launch the sweep kernels one by one (profiling)")
     p.add_argument("--save-state", default=None, help="write the settled state (npz) and continue")
     p.add_argument("--load-state", default=None, help="start from a settled state written by --save-state")
     return p.parse_args()
@@ -205,12 +206,13 @@ def run_cdx(a, log):
     state = load_or_settle(a, scene, cfg, log)
     sscene = with_state(scene, state)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-    run_cfg = dict(cfg, **{"gpu.precision": a.precision})
+    run_cfg = dict(cfg, **{"gpu.precision": a.precision, "gpu.graph": not a.no_graph})
     if world > 1:
         torch.distributed.barrier()
     clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
     clocks.start()
     eng, ms, iters, contacts, res, launches = time_engine(sscene, run_cfg, a.steps, a.warmup, log, flush)
+    est = eng.stats()
     clk = clocks.stop()
     total_ms = sum(ms)
     if world > 1:
@@ -287,6 +289,7 @@ def run_cdx(a, log):
                       "residual": res[-1], "residual_tol": cfg.get("gpu.residual_tol"),
                       "max_iterations": cfg["pj.max_iterations"], "dt": cfg["sim.dt"], "precision": a.precision,
                       "l2": "flushed between timed steps (256 MiB write outside the timed events)",
+                      "contact_variant": est.get("contact_variant"), "autotune_runs": est.get("autotune_runs"),
                       "parallelism": "replicas" if world > 1 else "single"},
            "contact_iters_per_s": cit * (world if world > 1 else 1), "roofline": roofline,
            "plain_fp64": plain, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk}

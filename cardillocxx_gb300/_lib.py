@@ -56,6 +56,7 @@ class CdxConfig(C.Structure):
         ("gpu_block", C.c_int32),
         ("gpu_contact_capacity_factor", C.c_double),
         ("gpu_use_graph", C.c_int32),
+        ("gpu_autotune", C.c_int32),
     ]
 
 
@@ -90,6 +91,8 @@ class CdxStats(C.Structure):
         ("ms_integrate", C.c_double),
         ("solve_bytes_per_iter", C.c_double),
         ("kernel_launches", C.c_int64),
+        ("contact_variant", C.c_int32),
+        ("autotune_runs", C.c_int32),
     ]
 
 
@@ -136,6 +139,7 @@ SIGNATURES = [
     ("cdx_set_timing", C.c_int, [C.c_void_p, C.c_int32]),
     ("cdx_stream", C.c_void_p, [C.c_void_p]),
     ("cdx_time_sweeps", C.c_int, [C.c_void_p, C.c_int32, _P, _P, _P, _P]),
+    ("cdx_selftest_nr64", C.c_int, [C.c_void_p, C.c_int32, _P, _P, _P]),
     ("cdx_pj_solve_csr", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, _PI, _PI, _P, _P, _P, _P, _P, _P,
                                    _P, _P, _P, C.c_double, C.c_double, C.c_int32, C.c_double, C.c_double, _P, _P,
                                    _PI]),

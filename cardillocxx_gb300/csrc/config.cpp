@@ -90,6 +90,7 @@ int cdx_config_default(cdx_config* c) {
     c->gpu_block = 0;
     c->gpu_contact_capacity_factor = 8.0;
     c->gpu_use_graph = 1;
+    c->gpu_autotune = 1;
     return CDX_OK;
 }
 
@@ -165,6 +166,8 @@ int cdx_config_set(cdx_config* c, const char* key_c, const char* val_c) {
         if (as_double(val, &d) && d > 0) c->gpu_contact_capacity_factor = d;
     } else if (key == "gpu.graph") {
         c->gpu_use_graph = as_bool(val);
+    } else if (key == "gpu.autotune") {
+        c->gpu_autotune = as_bool(val);
     }
     return CDX_OK;  // unknown keys are ignored, as in the reference
 }

@@ -266,6 +266,9 @@ int Engine::load_scene(const cdx_scene& s) {
     const int64_t nflag = (int64_t)std::max(1, N) * std::max(1, maxst);
     if ((st = dalloc((void**)&sflags, sizeof(int32_t) * nflag, "static flags"))) return st;
     if ((st = dalloc((void**)&spos, sizeof(int32_t) * nflag, "static flags"))) return st;
+    if ((st = dalloc((void**)&sflags_prev, sizeof(int32_t) * nflag, "static flags"))) return st;
+    if ((st = dalloc((void**)&spos_prev, sizeof(int32_t) * nflag, "static flags"))) return st;
+    if ((st = dalloc((void**)&poff_prev, sizeof(int32_t) * (N + 1), "pair offsets"))) return st;
     if ((st = dalloc((void**)&pcount, sizeof(int32_t) * (N + 1), "pair counts"))) return st;
     if ((st = dalloc((void**)&poff, sizeof(int32_t) * (N + 1), "pair offsets"))) return st;
     if ((st = dalloc((void**)&ds, sizeof(DevScalars), "scalars"))) return st;
@@ -624,6 +627,8 @@ void Engine::fill_stats(cdx_stats* s) {
     s->ms_integrate = ms[3];
     s->solve_bytes_per_iter = solve_bytes_per_iter();
     s->kernel_launches = launches;
+    s->contact_variant = split_variant();
+    s->autotune_runs = split_tune_runs();
 }
 
 double Engine::solve_bytes_per_iter() const {

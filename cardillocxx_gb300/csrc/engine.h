@@ -31,6 +31,7 @@ struct Engine {
     uint32_t *cell_key_in = nullptr, *cell_val_in = nullptr, *cell_key_out = nullptr, *cell_val_out = nullptr;
     int32_t *cell_start = nullptr, *cell_end = nullptr;
     int32_t *sflags = nullptr, *spos = nullptr, *pcount = nullptr, *poff = nullptr;
+    int32_t *sflags_prev = nullptr, *spos_prev = nullptr, *poff_prev = nullptr;  // split form warm start
     int32_t *isfl = nullptr, *flscan = nullptr;
     cdx::Contacts C;
     cdx::Incidence inc;
@@ -80,6 +81,8 @@ struct Engine {
     void destroy_split();
     int get_contacts_split(int32_t* ia, int32_t* ib, double* point, double* lambda, double* normal, int32_t* count);
     double split_bytes_per_iter() const;
+    int split_variant() const;
+    int split_tune_runs() const;
     int time_sweeps(int n, double* msc, double* msb, double* bc, double* bb);
 };
 

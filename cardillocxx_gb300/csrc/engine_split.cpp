@@ -17,6 +17,7 @@ struct SplitState {
     SplitBuf sb;
     int gen = 0;
     int prev_count = 0;
+    int prev_n_static = 0;
     int nc = 0;
     int sms = 148;
     int32_t* h_nc = nullptr;  // pinned
@@ -31,6 +32,11 @@ struct SplitState {
     std::vector<void*> bufs;
     int last_iters = 0;
     double res_last = 0, res_final = 0;
+    int variant = 0;         // contact-sweep launch shape (autotuned)
+    int graph_variant = -1;
+    int64_t tuned_at = 0;    // contact count at the last tuning
+    int tune_runs = 0;
+    cudaEvent_t tev[2] = {nullptr, nullptr};
 };
 }  // namespace cdx
 
@@ -53,6 +59,8 @@ static void destroy_graphs(SplitState* S) {
 void Engine::destroy_split() {
     if (!split) return;
     destroy_graphs(split);
+    for (auto& e : split->tev)
+        if (e) cudaEventDestroy(e);
     for (void* p : split->bufs) dfree(p);
     if (split->h_nc) cudaFreeHost(split->h_nc);
     if (split->h_ss) cudaFreeHost(split->h_ss);
@@ -68,13 +76,11 @@ static int split_contacts(Engine& E, int64_t need) {
     SplitBuf n = b;
     n.cap = cap;
     int st;
-    if ((st = salloc(E, (void**)&n.ab, sizeof(int2) * cap, "split contacts"))) return st;
-    float4** f4[] = {&n.nmu, &n.levR, &n.bias, &n.lam[0], &n.lam[1], &n.pt[0], &n.pt[1]};
+    float4** f4[] = {&n.rec0, &n.rec1, &n.bias, &n.lam[0], &n.lam[1], &n.pt[0], &n.pt[1]};
     for (auto p : f4)
         if ((st = salloc(E, (void**)p, sizeof(float4) * cap, "split contacts"))) return st;
     if ((st = salloc(E, (void**)&n.key[0], sizeof(unsigned long long) * cap, "split contacts"))) return st;
     if ((st = salloc(E, (void**)&n.key[1], sizeof(unsigned long long) * cap, "split contacts"))) return st;
-    if ((st = salloc(E, (void**)&n.g64, sizeof(double) * 5 * cap, "split contacts"))) return st;
     if (b.cap > 0 && S->prev_count > 0) {
         const int pg = S->gen ^ 1;
         cudaMemcpyAsync(n.key[pg], b.key[pg], sizeof(unsigned long long) * S->prev_count, cudaMemcpyDeviceToDevice, E.stream);
@@ -83,7 +89,7 @@ static int split_contacts(Engine& E, int64_t need) {
         if ((st = E.cuda_check(cudaStreamSynchronize(E.stream), "split grow"))) return st;
     }
     if (b.cap > 0) {
-        void* old[] = {b.ab, b.nmu, b.levR, b.bias, b.lam[0], b.lam[1], b.pt[0], b.pt[1], b.key[0], b.key[1], b.g64};
+        void* old[] = {b.rec0, b.rec1, b.bias, b.lam[0], b.lam[1], b.pt[0], b.pt[1], b.key[0], b.key[1]};
         for (void* p : old) {
             auto& v = S->bufs;
             v.erase(std::remove(v.begin(), v.end(), p), v.end());
@@ -120,6 +126,7 @@ static int init_split(Engine& E) {
         if ((st = salloc(E, (void**)p, sizeof(float4) * s1, "split statics"))) return st;
     if ((st = salloc(E, (void**)&b.nc_dev, sizeof(int32_t), "split"))) return st;
     if ((st = salloc(E, (void**)&b.ss, sizeof(SplitScalars), "split"))) return st;
+    if ((st = salloc(E, (void**)&b.part, sizeof(float2) * SPLIT_MAX_PARTS, "split"))) return st;
     if ((st = E.cuda_check(cudaMallocHost((void**)&S->h_nc, sizeof(int32_t)), "pinned"))) return st;
     if ((st = E.cuda_check(cudaMallocHost((void**)&S->h_ss, sizeof(SplitScalars)), "pinned"))) return st;
     cudaMemsetAsync(b.ss, 0, sizeof(SplitScalars), E.stream);
@@ -128,6 +135,14 @@ static int init_split(Engine& E) {
     std::vector<double> B((size_t)BF_COUNT * N), org(3 * (size_t)nsc, 0.0);
     if (N) {
         if ((st = E.cuda_check(cudaMemcpy(B.data(), E.sc.B, sizeof(double) * B.size(), cudaMemcpyDeviceToHost), "origins"))) return st;
+    }
+    for (int i = 0; i < N && !b.has_restitution; ++i)
+        if (B[(size_t)BF_RN * N + i] > 0 || B[(size_t)BF_RT * N + i] > 0) b.has_restitution = 1;
+    if (Ss > 0) {
+        std::vector<double> St((size_t)SF_COUNT * Ss);
+        if ((st = E.cuda_check(cudaMemcpy(St.data(), E.sc.St, sizeof(double) * St.size(), cudaMemcpyDeviceToHost), "statics"))) return st;
+        for (int i = 0; i < Ss && !b.has_restitution; ++i)
+            if (St[(size_t)SF_RN * Ss + i] > 0 || St[(size_t)SF_RT * Ss + i] > 0) b.has_restitution = 1;
     }
     for (int s = 0; s < nsc; ++s) {
         const int b0 = E.h_scene_body_start[s], b1 = E.h_scene_body_start[s + 1];
@@ -163,9 +178,8 @@ static int build_graph(Engine& E, int g) {
     cudaGraph_t body = p.conditional.phGraph_out[0];
     if ((st = E.cuda_check(cudaStreamBeginCaptureToGraph(E.stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed),
                            "capture"))) return st;
-    launch_s_contact(S->sb, g, S->graph_blocks, E.stream);
-    launch_s_body(S->sb, E.sc.N, S->graph_body_blocks, 0, E.stream);
-    launch_s_check(S->sb, maxit, tol, h, 1, E.stream);
+    launch_s_contact(S->sb, g, (float)E.cfg.pj_alpha, S->variant, S->graph_blocks, E.stream);
+    launch_s_body(S->sb, E.sc.N, S->graph_body_blocks, 0, maxit, tol, S->graph_blocks, h, 1, E.stream);
     cudaGraph_t captured = nullptr;
     if ((st = E.cuda_check(cudaStreamEndCapture(E.stream, &captured), "end capture"))) return st;
     if ((st = E.cuda_check(cudaGraphInstantiate(&S->exec[g], graph, 0), "graph instantiate"))) return st;
@@ -187,6 +201,10 @@ int Engine::step_split() {
     P.combine = cfg.friction_combine;
     P.friction_enable = cfg.friction_enable;
     P.prev_count = cfg.pj_warmstart ? S->prev_count : 0;
+    P.prev_sflags = sflags_prev;
+    P.prev_spos = spos_prev;
+    P.prev_poff = poff_prev;
+    P.prev_n_static = S->prev_n_static;
     const int gen = S->gen;
 
     if (timing) cudaEventRecord(ev[0], stream);
@@ -233,20 +251,62 @@ int Engine::step_split() {
     if (timing) cudaEventRecord(ev[1], stream);
     // x0 = v_free + M^-1 W^T lambda_warm
     const int cblocks = split_grid_blocks(std::max(S->nc, 1), S->sms);
-    const int bblocks = split_grid_blocks(std::max(N, 1), S->sms);
+    const int sblocks = split_contact_blocks(S->variant, std::max(S->nc, 1), S->sms);
+    const int bblocks = split_body_blocks(std::max(N, 1), S->sms);
     launch_s_reset(sb, stream);
     launch_s_apply_warm(sb, gen, cblocks, stream);
-    launch_s_body(sb, N, bblocks, 1, stream);
+    launch_s_body(sb, N, bblocks, 1, 0, 0.f, 0, 0, 0, stream);
     launches += 3;
     if (timing) cudaEventRecord(ev[2], stream);
     const int maxit = std::max(1, cfg.pj_max_iterations);
-    if (S->nc > 0) {
+    bool solved = false;
+    if (S->nc > 0 && cfg.gpu_autotune && S->nc >= 4096 && (double)S->nc >= 1.5 * (double)S->tuned_at &&
+        maxit > 2 * split_num_variants()) {
+        // autotune: the first sweeps of this step run once with every launch shape; each is a full
+        // sweep of the same math, so the step's result does not depend on which shape ran them
+        if (!S->tev[0]) {
+            cudaEventCreate(&S->tev[0]);
+            cudaEventCreate(&S->tev[1]);
+        }
+        const int nv = split_num_variants();
+        double best_t = 1e300;
+        int best = S->variant;
+        cudaGraphConditionalHandle none = 0;
+        for (int v = 0; v < nv; ++v) {
+            double t = 0;
+            for (int r = 0; r < 2; ++r) {
+                const int vb = split_contact_blocks(v, S->nc, S->sms);
+                cudaEventRecord(S->tev[0], stream);
+                launch_s_contact(sb, gen, (float)cfg.pj_alpha, v, vb, stream);
+                cudaEventRecord(S->tev[1], stream);
+                launch_s_body(sb, N, bblocks, 0, maxit, (float)cfg.gpu_residual_tol, vb, none, 0, stream);
+                if ((st = cuda_check(cudaEventSynchronize(S->tev[1]), "autotune"))) return st;
+                float ms1 = 0;
+                cudaEventElapsedTime(&ms1, S->tev[0], S->tev[1]);
+                t += ms1;
+            }
+            launches += 4;
+            if (t < best_t) {
+                best_t = t;
+                best = v;
+            }
+        }
+        S->variant = best;
+        S->tuned_at = S->nc;
+        ++S->tune_runs;
+        cudaMemcpyAsync(&S->h_ss->done, &sb.ss->done, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+        if ((st = cuda_check(cudaStreamSynchronize(stream), "autotune"))) return st;
+        solved = S->h_ss->done != 0;
+    }
+    if (S->nc > 0 && !solved) {
         if (cfg.gpu_use_graph) {
             // grid sized for the capacity so a graph serves every step until the buffers grow
-            const int gblocks = split_grid_blocks(sb.cap, S->sms);
+            const int gblocks = split_contact_blocks(S->variant, sb.cap, S->sms);
             const float tol = (float)cfg.gpu_residual_tol;
-            if (S->graph_cap != sb.cap || S->graph_maxit != maxit || S->graph_tol != tol) {
+            if (S->graph_cap != sb.cap || S->graph_maxit != maxit || S->graph_tol != tol ||
+                S->graph_variant != S->variant) {
                 destroy_graphs(S);
+                S->graph_variant = S->variant;
                 S->graph_blocks = gblocks;
                 S->graph_body_blocks = bblocks;
                 if ((st = build_graph(*this, 0)) || (st = build_graph(*this, 1))) return st;
@@ -259,32 +319,35 @@ int Engine::step_split() {
             const int every = std::max(1, cfg.gpu_check_every);
             cudaGraphConditionalHandle none = 0;
             for (int it = 0; it < maxit; ++it) {
-                launch_s_contact(sb, gen, cblocks, stream);
-                launch_s_body(sb, N, bblocks, 0, stream);
-                launch_s_check(sb, maxit, (float)cfg.gpu_residual_tol, none, 0, stream);
-                if ((it + 1) % every == 0 && it + 1 < maxit) {
+                if (it > 0 && it % every == 0) {
                     cudaMemcpyAsync(&S->h_ss->done, &sb.ss->done, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
                     if ((st = cuda_check(cudaStreamSynchronize(stream), "poll"))) return st;
                     if (S->h_ss->done) break;
                 }
+                launch_s_contact(sb, gen, (float)cfg.pj_alpha, S->variant, sblocks, stream);
+                launch_s_body(sb, N, bblocks, 0, maxit, (float)cfg.gpu_residual_tol, sblocks, none, 0, stream);
             }
         }
     }
     if (timing) cudaEventRecord(ev[3], stream);
     // FP64: final velocities, residual, write back, drift theta h
     launch_s_final(sc, sb, gen, cfg.pj_alpha, cfg.friction_enable, cfg.friction_combine, cblocks, stream);
-    launch_drift64(sc, th * dt, 0, stream);
-    launches += 7;
+    launch_s_drift(sc, th * dt, stream);
+    launches += 5;
     if (timing) cudaEventRecord(ev[4], stream);
     cudaMemcpyAsync(S->h_ss, sb.ss, sizeof(SplitScalars), cudaMemcpyDeviceToHost, stream);
     if ((st = cuda_check(cudaStreamSynchronize(stream), "split step"))) return st;
     if ((st = cuda_check(cudaGetLastError(), "split launch"))) return st;
     S->last_iters = S->nc > 0 ? S->h_ss->iters : 0;
-    launches += 3 * (int64_t)S->last_iters;
+    launches += 2 * (int64_t)S->last_iters;
     S->res_last = S->h_ss->res_last;
     S->res_final = S->nc > 0 ? S->h_ss->res_final : 0.0;
     S->prev_count = S->nc;
+    S->prev_n_static = (int)n_static;
     S->gen ^= 1;
+    std::swap(sflags, sflags_prev);
+    std::swap(spos, spos_prev);
+    std::swap(poff, poff_prev);
     // mirror into the common stats fields
     prev_count = S->nc;
     last_iters = S->last_iters;
@@ -316,7 +379,7 @@ int Engine::get_contacts_split(int32_t* ia, int32_t* ib, double* point, double* 
     if ((st = cuda_check(cudaMemcpy(keys.data(), sb.key[g], 8 * (size_t)n, cudaMemcpyDeviceToHost), "download"))) return st;
     if ((st = cuda_check(cudaMemcpy(pt.data(), sb.pt[g], 16 * (size_t)n, cudaMemcpyDeviceToHost), "download"))) return st;
     if ((st = cuda_check(cudaMemcpy(lam.data(), sb.lam[g], 16 * (size_t)n, cudaMemcpyDeviceToHost), "download"))) return st;
-    if ((st = cuda_check(cudaMemcpy(nm.data(), sb.nmu, 16 * (size_t)n, cudaMemcpyDeviceToHost), "download"))) return st;
+    if ((st = cuda_check(cudaMemcpy(nm.data(), sb.rec0, 16 * (size_t)n, cudaMemcpyDeviceToHost), "download"))) return st;
     std::vector<double> org(3 * (size_t)sc.nscenes);
     if ((st = cuda_check(cudaMemcpy(org.data(), sb.origin, 8 * org.size(), cudaMemcpyDeviceToHost), "download"))) return st;
     std::vector<int32_t> bscene(sc.N);
@@ -338,10 +401,10 @@ int Engine::get_contacts_split(int32_t* ia, int32_t* ib, double* point, double* 
 }
 
 double Engine::split_bytes_per_iter() const {
-    // per contact: ab (8) + nmu (16) + levR (16) + bias (16) + lambda read+write (32); per body:
-    // vel4 read+write (64) + acc4 read+write (64)
+    // per contact: n and mu (16), lever lengths and body indices (16), lambda read + write (24, its
+    // three words); per body: velocities read + write (48) and accumulators read + zeroed (48)
     const int n = split ? split->prev_count : 0;
-    return (double)n * (8 + 16 + 16 + 16 + 32) + (double)sc.N * 128.0;
+    return (double)n * (16 + 16 + 24) + (double)sc.N * 96.0;
 }
 
 // Kernel-level timing of the sweep (CUDA events around each launch, engine stream).
@@ -356,16 +419,16 @@ int Engine::time_sweeps(int n, double* msc, double* msb, double* bc, double* bb)
     if (sp && split && split->prev_count > 0) {
         SplitState* S = split;
         const int g = S->gen ^ 1;
-        const int cblocks = split_grid_blocks(S->prev_count, S->sms);
-        const int bblocks = split_grid_blocks(std::max(sc.N, 1), S->sms);
+        const int cblocks = split_contact_blocks(S->variant, S->prev_count, S->sms);
+        const int bblocks = split_body_blocks(std::max(sc.N, 1), S->sms);
         *S->h_nc = S->prev_count;
         cudaMemcpyAsync(S->sb.nc_dev, S->h_nc, sizeof(int32_t), cudaMemcpyHostToDevice, stream);
         cudaMemsetAsync(S->sb.ss, 0, sizeof(SplitScalars), stream);
         for (int k = 0; k < n; ++k) {
             cudaEventRecord(e[0], stream);
-            launch_s_contact(S->sb, g, cblocks, stream);
+            launch_s_contact(S->sb, g, (float)cfg.pj_alpha, S->variant, cblocks, stream);
             cudaEventRecord(e[1], stream);
-            launch_s_body(S->sb, sc.N, bblocks, 0, stream);
+            launch_s_body(S->sb, sc.N, bblocks, 0, 1 << 30, 0.f, cblocks, 0, 0, stream);
             cudaEventRecord(e[2], stream);
             if ((st = cuda_check(cudaEventSynchronize(e[2]), "time sweeps"))) break;
             float a = 0, b = 0;
@@ -375,7 +438,7 @@ int Engine::time_sweeps(int n, double* msc, double* msb, double* bc, double* bb)
             tb += b;
         }
         launches += 2 * (int64_t)n;
-        if (bc) *bc = (double)S->prev_count * 76.0;
+        if (bc) *bc = (double)S->prev_count * (16 + 16 + 24);
         if (bb) *bb = (double)sc.N * 96.0;
     } else if (!sp && prev_count > 0) {
         const int g = gen ^ 1;
@@ -406,4 +469,23 @@ int Engine::time_sweeps(int n, double* msc, double* msb, double* bc, double* bb)
     if (msc) *msc = tc / n;
     if (msb) *msb = tb / n;
     return CDX_OK;
+}
+
+int Engine::split_variant() const { return split ? split->variant : -1; }
+int Engine::split_tune_runs() const { return split ? split->tune_runs : 0; }
+
+extern "C" int cdx_selftest_nr64(cdx_ctx* ctx, int32_t n, const double* x, double* rcp, double* rsq) {
+    if (!ctx || n < 0 || (n > 0 && (!x || !rcp || !rsq))) return CDX_ERR_ARG;
+    Engine& E = ctx->eng;
+    if (n == 0) return CDX_OK;
+    double* d = nullptr;
+    int st = E.dalloc((void**)&d, sizeof(double) * 3 * (size_t)n, "selftest");
+    if (st) return st;
+    cudaMemcpyAsync(d, x, sizeof(double) * n, cudaMemcpyHostToDevice, E.stream);
+    launch_nr64_selftest(n, d, d + n, d + 2 * (size_t)n, E.stream);
+    cudaMemcpyAsync(rcp, d + n, sizeof(double) * n, cudaMemcpyDeviceToHost, E.stream);
+    cudaMemcpyAsync(rsq, d + 2 * (size_t)n, sizeof(double) * n, cudaMemcpyDeviceToHost, E.stream);
+    st = E.cuda_check(cudaStreamSynchronize(E.stream), "selftest");
+    E.dfree(d);
+    return st;
 }

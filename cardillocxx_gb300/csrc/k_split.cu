@@ -16,6 +16,7 @@
 #include "cdx_internal.h"
 #include "fp64_math.cuh"
 #include "split.h"
+#include "nr64.cuh"
 
 namespace cdx {
 
@@ -57,7 +58,55 @@ __device__ __forceinline__ float combine_mu32(int mode, float a, float b) {
     return fminf(a, b);
 }
 
-__device__ __forceinline__ void atomic_max_f(unsigned int* addr, float v) { atomicMax(addr, __float_as_uint(v)); }
+// the sign bit of the mu field flags a contact that carries a velocity bias
+__device__ __forceinline__ bool split_has_bias(float mu_field) { return signbit(mu_field); }
+
+
+// Max of (a, b) over the block, then one atomic per block: per-warp atomics on one address
+// serialise at a single L2 slice and dominated the sweep.
+template <typename T>
+__device__ __forceinline__ void block_max2(T& a, T& b) {
+    __shared__ T sh[2][32];
+    for (int o = 16; o > 0; o >>= 1) {
+        a = max(a, __shfl_xor_sync(0xffffffffu, a, o));
+        b = max(b, __shfl_xor_sync(0xffffffffu, b, o));
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) {
+        sh[0][wid] = a;
+        sh[1][wid] = b;
+    }
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+        a = lane < nw ? sh[0][lane] : T(0);
+        b = lane < nw ? sh[1][lane] : T(0);
+        for (int o = 16; o > 0; o >>= 1) {
+            a = max(a, __shfl_xor_sync(0xffffffffu, a, o));
+            b = max(b, __shfl_xor_sync(0xffffffffu, b, o));
+        }
+    }
+}
+
+// explicitPositionUpdate in FP64 for the split form: the same update as the plain method, with the
+// quaternion normalised by one reciprocal square root instead of four divisions
+__device__ __forceinline__ void drift_fast(double* x, double* q, const double* v, const double* w, double h) {
+    for (int k = 0; k < 3; ++k) x[k] = x[k] + h * v[k];
+    const double qp[4] = {q[0], q[1], q[2], q[3]};
+    const double hh = h * 0.5;
+    q[3] = qp[3] - hh * (qp[0] * w[0] + qp[1] * w[1] + qp[2] * w[2]);
+    q[0] = qp[0] + hh * (qp[3] * w[0] + (qp[1] * w[2] - qp[2] * w[1]));
+    q[1] = qp[1] + hh * (qp[3] * w[1] + (qp[2] * w[0] - qp[0] * w[2]));
+    q[2] = qp[2] + hh * (qp[3] * w[2] + (qp[0] * w[1] - qp[1] * w[0]));
+    const double n2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
+    if (!(n2 > 0.0) || !isfinite(n2)) {
+        for (int k = 0; k < 4; ++k) q[k] = qp[k];
+        return;
+    }
+    double inv = rsqrt_nr(n2);
+    if (qp[0] * q[0] + qp[1] * q[1] + qp[2] * q[2] + qp[3] * q[3] < 0.0) inv = -inv;
+    for (int k = 0; k < 4; ++k) q[k] *= inv;
+}
 
 // ------------------------------------------------------------------ per-body preparation (FP64)
 __global__ void k_s_prep(Scene sc, SplitBuf sb, double dt, double g0, double g1, double g2, double h1) {
@@ -80,26 +129,27 @@ __global__ void k_s_prep(Scene sc, SplitBuf sb, double dt, double g0, double g1,
             vf[k] = v[k] + dt * g[k];
             wf[k] = w[k] + dt * ia * (-c[k]);
         }
-        f64::drift(x, q, v, w, h1);
+        drift_fast(x, q, v, w, h1);
         sc.bf(BF_PX)[i] = x[0]; sc.bf(BF_PY)[i] = x[1]; sc.bf(BF_PZ)[i] = x[2];
         sc.bf(BF_QX)[i] = q[0]; sc.bf(BF_QY)[i] = q[1]; sc.bf(BF_QZ)[i] = q[2]; sc.bf(BF_QW)[i] = q[3];
         double R[9];
         f64::rotmat(q, R);
         for (int k = 0; k < 9; ++k) sc.bf(BF_R0 + k)[i] = R[k];
         // world-frame angular velocities: R w
-        double ww[3], wfw[3];
-        for (int k = 0; k < 3; ++k) {
-            ww[k] = R[3 * k] * w[0] + R[3 * k + 1] * w[1] + R[3 * k + 2] * w[2];
-            wfw[k] = R[3 * k] * wf[0] + R[3 * k + 1] * wf[1] + R[3 * k + 2] * wf[2];
-        }
+        double wfw[3];
+        for (int k = 0; k < 3; ++k) wfw[k] = R[3 * k] * wf[0] + R[3 * k + 1] * wf[1] + R[3 * k + 2] * wf[2];
         for (int k = 0; k < 3; ++k) {
             sb.vfree[(size_t)k * N + i] = vf[k];
             sb.vfree[(size_t)(3 + k) * N + i] = wfw[k];
         }
         sb.vel4[2 * i] = make_float4((float)vf[0], (float)vf[1], (float)vf[2], (float)il);
         sb.vel4[2 * i + 1] = make_float4((float)wfw[0], (float)wfw[1], (float)wfw[2], (float)ia);
-        sb.vn4[2 * i] = make_float4((float)v[0], (float)v[1], (float)v[2], 0.f);
-        sb.vn4[2 * i + 1] = make_float4((float)ww[0], (float)ww[1], (float)ww[2], 0.f);
+        if (sb.has_restitution) {
+            double ww[3];
+            for (int k = 0; k < 3; ++k) ww[k] = R[3 * k] * w[0] + R[3 * k + 1] * w[1] + R[3 * k + 2] * w[2];
+            sb.vn4[2 * i] = make_float4((float)v[0], (float)v[1], (float)v[2], 0.f);
+            sb.vn4[2 * i + 1] = make_float4((float)ww[0], (float)ww[1], (float)ww[2], 0.f);
+        }
         sb.acc4[2 * i] = make_float4(0.f, 0.f, 0.f, 0.f);
         sb.acc4[2 * i + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
         const int s = sc.body_scene[i];
@@ -112,7 +162,7 @@ __global__ void k_s_prep(Scene sc, SplitBuf sb, double dt, double g0, double g1,
         double q[4] = {sc.sf(SF_QX)[s], sc.sf(SF_QY)[s], sc.sf(SF_QZ)[s], sc.sf(SF_QW)[s]};
         const double v[3] = {sc.sf(SF_VX)[s], sc.sf(SF_VY)[s], sc.sf(SF_VZ)[s]};
         const double w[3] = {sc.sf(SF_WX)[s], sc.sf(SF_WY)[s], sc.sf(SF_WZ)[s]};
-        f64::drift(x, q, v, w, h1);
+        drift_fast(x, q, v, w, h1);
         sc.sf(SF_PX)[s] = x[0]; sc.sf(SF_PY)[s] = x[1]; sc.sf(SF_PZ)[s] = x[2];
         sc.sf(SF_QX)[s] = q[0]; sc.sf(SF_QY)[s] = q[1]; sc.sf(SF_QZ)[s] = q[2]; sc.sf(SF_QW)[s] = q[3];
         double R[9];
@@ -181,20 +231,20 @@ __global__ void k_s_static_flags(Scene sc, SplitBuf sb, float margin, int32_t* f
     }
 }
 
-__device__ __forceinline__ void warm_start(const SplitBuf& sb, int gen, int prev_count, unsigned long long key,
+// warm start: the same pair among the previous step's contacts [lo, hi) (at most a few), within
+// collision.match_max_dist of its old contact point (contact_tracker.cpp:43-72)
+__device__ __forceinline__ void warm_start(const SplitBuf& sb, int gen, int lo, int hi, unsigned long long key,
                                            float3 pt, float match2, float4& lam0) {
     lam0 = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (prev_count <= 0) return;
     const unsigned long long* pk = sb.key[gen ^ 1];
-    int lo = 0, hi = prev_count;
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (pk[mid] < key) lo = mid + 1;
-        else hi = mid;
-    }
-    if (lo < prev_count && pk[lo] == key) {
-        const float3 d = pt - f3(sb.pt[gen ^ 1][lo]);
-        if (dot(d, d) <= match2) lam0 = sb.lam[gen ^ 1][lo];
+    for (int p = lo; p < hi; ++p) {
+        const unsigned long long k = pk[p];
+        if (k < key) continue;
+        if (k == key) {
+            const float3 d = pt - f3(sb.pt[gen ^ 1][p]);
+            if (dot(d, d) <= match2) lam0 = sb.lam[gen ^ 1][p];
+        }
+        break;
     }
 }
 
@@ -202,20 +252,12 @@ __device__ __forceinline__ void warm_start(const SplitBuf& sb, int gen, int prev
 __device__ __forceinline__ void finish_contact32(const Scene& sc, SplitBuf& sb, int gen, int c, int a, int b,
                                                  float3 n, float rhoA, float rhoB, float3 pt, float mu_a,
                                                  float rn_a, float rt_a, const float3* wall_v, const float3* wall_w,
-                                                 const float3* wall_p, const SplitParams& P) {
-    const float4 vb = sb.vel4[2 * b], wb = sb.vel4[2 * b + 1];
-    float ima = 0.f, iia = 0.f;
+                                                 const float3* wall_p, const SplitParams& P, int prev_lo, int prev_hi) {
     float3 vna = make_float3(0.f, 0.f, 0.f), wna = vna;
-    if (a >= 0) {
-        ima = sb.vel4[2 * a].w;
-        iia = sb.vel4[2 * a + 1].w;
+    if (a >= 0 && sb.has_restitution) {
         vna = f3(sb.vn4[2 * a]);
         wna = f3(sb.vn4[2 * a + 1]);
     }
-    const float Dn = ima + vb.w;
-    const float Dt = Dn + rhoA * rhoA * iia + rhoB * rhoB * wb.w;
-    const float Rn = Dn > 0.f ? P.alpha / Dn : 0.f;
-    const float Rt = Dt > 0.f ? P.alpha / Dt : 0.f;
     float mu = combine_mu32(P.combine, mu_a, (float)sc.bf(BF_MU)[b]);
     if (!P.friction_enable || !(mu > 0.f)) mu = 0.f;
     float3 t1, t2;
@@ -231,25 +273,25 @@ __device__ __forceinline__ void finish_contact32(const Scene& sc, SplitBuf& sb, 
     }
     const float eN = fminf(fmaxf(0.f, rn_a), fmaxf(0.f, (float)sc.bf(BF_RN)[b]));
     const float eT = fminf(fmaxf(0.f, rt_a), fmaxf(0.f, (float)sc.bf(BF_RT)[b]));
-    float4 bias = make_float4(Rn * cb[0], Rt * cb[1], Rt * cb[2], 0.f);
+    float4 bias = make_float4(cb[0], cb[1], cb[2], 0.f);
     if (eN > 0.f || eT > 0.f) {
         const float3 dv = f3(sb.vn4[2 * b]) - vna;
         const float3 Om = rhoB * f3(sb.vn4[2 * b + 1]) - rhoA * wna;
         const float vp0 = dot(n, dv) + cb[0];
         const float vp1 = dot(t1, dv) + dot(t2, Om) + cb[1];
         const float vp2 = dot(t2, dv) - dot(t1, Om) + cb[2];
-        bias = make_float4(Rn * (cb[0] + eN * vp0), Rt * (cb[1] + eT * vp1), Rt * (cb[2] + eT * vp2), 0.f);
+        bias = make_float4(cb[0] + eN * vp0, cb[1] + eT * vp1, cb[2] + eT * vp2, 0.f);
     }
     const uint32_t ida = a >= 0 ? (uint32_t)(sc.S + a) : (uint32_t)(-a - 1);
     const uint32_t idb = (uint32_t)(sc.S + b);
     const unsigned long long key = ((unsigned long long)ida << 32) | idb;
-    float4 lam0;
-    warm_start(sb, gen, P.prev_count, key, pt, P.match2, lam0);
+    float4 lam0 = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (P.prev_count > 0) warm_start(sb, gen, prev_lo, prev_hi, key, pt, P.match2, lam0);
     if (mu == 0.f) { lam0.y = 0.f; lam0.z = 0.f; }
-    sb.ab[c] = make_int2(a, b);
-    sb.nmu[c] = make_float4(n.x, n.y, n.z, mu);
-    sb.levR[c] = make_float4(rhoA, rhoB, Rn, Rt);
-    sb.bias[c] = bias;
+    const bool has_bias = bias.x != 0.f || bias.y != 0.f || bias.z != 0.f;
+    sb.rec0[c] = make_float4(n.x, n.y, n.z, has_bias ? -mu - 0.f : mu);
+    sb.rec1[c] = make_float4(rhoA, rhoB, __int_as_float(a), __int_as_float(b));
+    if (has_bias) sb.bias[c] = bias;
     sb.lam[gen][c] = lam0;
     sb.key[gen][c] = key;
     sb.pt[gen][c] = make_float4(pt.x, pt.y, pt.z, 0.f);
@@ -273,8 +315,14 @@ __global__ void k_s_static_write(Scene sc, SplitBuf sb, const int32_t* flags, co
         const float3 pt = f3(p) + g.rhoB * g.n;
         const float3 wv = f3(sb.st_v[st]), ww = f3(sb.st_w[st]), wp = f3(sb.st_pt[st]);
         const bool moving = (wv.x != 0.f || wv.y != 0.f || wv.z != 0.f || ww.x != 0.f || ww.y != 0.f || ww.z != 0.f);
+        int plo = 0, phi = 0;
+        if (P.prev_count > 0 && P.prev_sflags[slot]) {
+            plo = P.prev_spos[slot];
+            phi = plo + 1;
+        }
         finish_contact32(sc, sb, gen, pos[slot], -st - 1, i, g.n, 0.f, g.rhoB, pt, sb.st_w[st].w,
-                         (float)sc.sf(SF_RN)[st], (float)sc.sf(SF_RT)[st], moving ? &wv : nullptr, &ww, &wp, P);
+                         (float)sc.sf(SF_RN)[st], (float)sc.sf(SF_RT)[st], moving ? &wv : nullptr, &ww, &wp, P, plo,
+                         phi);
     }
 }
 
@@ -350,6 +398,11 @@ __global__ void k_s_pairs(Scene sc, Grid gr, SplitBuf sb, const uint32_t* cell_b
         list[b + 1] = v;
     }
     const int c0 = base + offsets[i];
+    int plo = 0, phi = 0;
+    if (P.prev_count > 0) {
+        plo = P.prev_n_static + P.prev_poff[i];
+        phi = P.prev_n_static + P.prev_poff[i + 1];
+    }
     const float mu_a = (float)sc.bf(BF_MU)[i];
     const float rn_a = (float)sc.bf(BF_RN)[i], rt_a = (float)sc.bf(BF_RT)[i];
     for (int k = 0; k < cnt; ++k) {
@@ -361,7 +414,8 @@ __global__ void k_s_pairs(Scene sc, Grid gr, SplitBuf sb, const uint32_t* cell_b
         const float rhoA = 0.5f * (dl + pi.w - pj.w);
         const float rhoB = 0.5f * (pi.w - pj.w - dl);
         const float3 pt = f3(pi) + rhoA * n;
-        finish_contact32(sc, sb, gen, c0 + k, i, j, n, rhoA, rhoB, pt, mu_a, rn_a, rt_a, nullptr, nullptr, nullptr, P);
+        finish_contact32(sc, sb, gen, c0 + k, i, j, n, rhoA, rhoB, pt, mu_a, rn_a, rt_a, nullptr, nullptr, nullptr, P,
+                         plo, phi);
     }
 }
 
@@ -389,106 +443,186 @@ __global__ void k_s_apply_warm(SplitBuf sb, int gen) {
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
         const float4 l = sb.lam[gen][c];
         if (l.x == 0.f && l.y == 0.f && l.z == 0.f) continue;
-        const int2 ab = sb.ab[c];
-        const float4 nm = sb.nmu[c], lr = sb.levR[c];
-        const float3 n = f3(nm);
+        const float4 r0 = sb.rec0[c], r1 = sb.rec1[c];
+        const int a = __float_as_int(r1.z), b = __float_as_int(r1.w);
+        const float3 n = f3(r0);
         float3 t1, t2;
         frame32(n, t1, t2);
-        const float imb = sb.vel4[2 * ab.y].w, iib = sb.vel4[2 * ab.y + 1].w;
+        const float imb = sb.vel4[2 * b].w, iib = sb.vel4[2 * b + 1].w;
         float ima = 0.f, iia = 0.f;
-        if (ab.x >= 0) {
-            ima = sb.vel4[2 * ab.x].w;
-            iia = sb.vel4[2 * ab.x + 1].w;
+        if (a >= 0) {
+            ima = sb.vel4[2 * a].w;
+            iia = sb.vel4[2 * a + 1].w;
         }
-        scatter(sb, ab.x, ab.y, n, t1, t2, lr.x, lr.y, l.x, l.y, l.z, imb, iib, ima, iia);
+        scatter(sb, a, b, n, t1, t2, r1.x, r1.y, l.x, l.y, l.z, imb, iib, ima, iia);
     }
 }
 
-__global__ void __launch_bounds__(NT) k_s_contact(SplitBuf sb, int gen) {
+// One sweep over the contacts. The sweep is latency-bound (a dependent chain: contact record ->
+// body gathers -> atomics), so every thread takes UNROLL contacts and issues all their record
+// loads, then all their body gathers, before computing; read-only data goes through the
+// non-coherent path. The grid is sized to the resident capacity and strides over the contacts.
+__device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
+
+template <int UNROLL, int NTH, int MINB>
+__global__ void __launch_bounds__(NTH, MINB) k_s_contact_t(SplitBuf sb, int gen, float alpha) {
     if (*(volatile int32_t*)&sb.ss->done) return;
     const int nc = *sb.nc_dev;
     float maxd = 0.f, maxl = 0.f;
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
-        const int2 ab = sb.ab[c];
-        const float4 nm = sb.nmu[c];
-        const float4 lr = sb.levR[c];
-        const float4 bs = sb.bias[c];
-        const float4 l = sb.lam[gen][c];
-        const float3 n = f3(nm);
-        float3 t1, t2;
-        frame32(n, t1, t2);
-        const float4 vb = sb.vel4[2 * ab.y], wb = sb.vel4[2 * ab.y + 1];
-        float3 dv = f3(vb);
-        float3 Om = lr.y * f3(wb);
-        float ima = 0.f, iia = 0.f;
-        if (ab.x >= 0) {
-            const float4 va = sb.vel4[2 * ab.x], wa = sb.vel4[2 * ab.x + 1];
-            dv = dv - f3(va);
-            Om = Om - lr.x * f3(wa);
-            ima = va.w;
-            iia = wa.w;
+    const int T = gridDim.x * blockDim.x;
+    float4* __restrict__ lamp = sb.lam[gen];
+    for (int c0 = blockIdx.x * blockDim.x + threadIdx.x; c0 < nc; c0 += T * UNROLL) {
+        float4 r0[UNROLL], r1[UNROLL], l[UNROLL];
+        bool ok[UNROLL];
+#pragma unroll
+        for (int u = 0; u < UNROLL; ++u) {
+            const int c = c0 + u * T;
+            ok[u] = c < nc;
+            if (ok[u]) {
+                r0[u] = ldg4(&sb.rec0[c]);
+                r1[u] = ldg4(&sb.rec1[c]);
+                l[u] = lamp[c];
+            }
         }
-        const float gn = dot(n, dv) + bs.x;
-        const float gt1 = dot(t1, dv) + dot(t2, Om) + bs.y;
-        const float gt2 = dot(t2, dv) - dot(t1, Om) + bs.z;
-        float ln = fmaxf(l.x - lr.z * gn, 0.f);
-        float lt1 = l.y - lr.w * gt1;
-        float lt2 = l.z - lr.w * gt2;
-        const float tn2 = lt1 * lt1 + lt2 * lt2;
-        if (tn2 > 0.f) {
-            const float s = fminf(1.f, nm.w * ln * rsqrtf(tn2));
-            lt1 *= s;
-            lt2 *= s;
+        float4 vb[UNROLL], wb[UNROLL], va[UNROLL], wa[UNROLL];
+#pragma unroll
+        for (int u = 0; u < UNROLL; ++u) {
+            if (!ok[u]) continue;
+            const int a = __float_as_int(r1[u].z), b = __float_as_int(r1[u].w);
+            vb[u] = ldg4(&sb.vel4[2 * b]);
+            wb[u] = ldg4(&sb.vel4[2 * b + 1]);
+            if (a >= 0) {
+                va[u] = ldg4(&sb.vel4[2 * a]);
+                wa[u] = ldg4(&sb.vel4[2 * a + 1]);
+            } else {
+                va[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+                wa[u] = va[u];
+            }
         }
-        const float dln = ln - l.x, dlt1 = lt1 - l.y, dlt2 = lt2 - l.z;
-        sb.lam[gen][c] = make_float4(ln, lt1, lt2, 0.f);
-        maxd = fmaxf(maxd, sqrtf(dln * dln + dlt1 * dlt1 + dlt2 * dlt2));
-        maxl = fmaxf(maxl, fmaxf(fabsf(l.x), fmaxf(fabsf(l.y), fabsf(l.z))));
-        if (dln != 0.f || dlt1 != 0.f || dlt2 != 0.f)
-            scatter(sb, ab.x, ab.y, n, t1, t2, lr.x, lr.y, dln, dlt1, dlt2, vb.w, wb.w, ima, iia);
+#pragma unroll
+        for (int u = 0; u < UNROLL; ++u) {
+            if (!ok[u]) continue;
+            const int c = c0 + u * T;
+            const float3 n = f3(r0[u]);
+            float3 t1, t2;
+            frame32(n, t1, t2);
+            const float rA = r1[u].x, rB = r1[u].y;
+            const float3 dv = f3(vb[u]) - f3(va[u]);
+            const float3 Om = rB * f3(wb[u]) - rA * f3(wa[u]);
+            float gn = dot(n, dv);
+            float gt1 = dot(t1, dv) + dot(t2, Om);
+            float gt2 = dot(t2, dv) - dot(t1, Om);
+            if (split_has_bias(r0[u].w)) {
+                const float4 bs = ldg4(&sb.bias[c]);
+                gn += bs.x;
+                gt1 += bs.y;
+                gt2 += bs.z;
+            }
+            // R = alpha / Delassus diagonal, from the inverse masses carried in the .w lanes
+            const float Dn = va[u].w + vb[u].w;
+            const float Dt = Dn + rA * rA * wa[u].w + rB * rB * wb[u].w;
+            const float Rn = alpha * __frcp_rn(Dn), Rt = alpha * __frcp_rn(Dt);
+            const float mu = fabsf(r0[u].w);
+            float ln = fmaxf(l[u].x - Rn * gn, 0.f);
+            float lt1 = l[u].y - Rt * gt1;
+            float lt2 = l[u].z - Rt * gt2;
+            const float tn2 = lt1 * lt1 + lt2 * lt2;
+            if (tn2 > 0.f) {
+                const float sc = fminf(1.f, mu * ln * rsqrtf(tn2));
+                lt1 *= sc;
+                lt2 *= sc;
+            }
+            const float dln = ln - l[u].x, dlt1 = lt1 - l[u].y, dlt2 = lt2 - l[u].z;
+            lamp[c] = make_float4(ln, lt1, lt2, 0.f);
+            maxd = fmaxf(maxd, sqrtf(dln * dln + dlt1 * dlt1 + dlt2 * dlt2));
+            maxl = fmaxf(maxl, fmaxf(fabsf(l[u].x), fmaxf(fabsf(l[u].y), fabsf(l[u].z))));
+            if (dln != 0.f || dlt1 != 0.f || dlt2 != 0.f)
+                scatter(sb, __float_as_int(r1[u].z), __float_as_int(r1[u].w), n, t1, t2, rA, rB, dln, dlt1, dlt2,
+                        vb[u].w, wb[u].w, va[u].w, wa[u].w);
+        }
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        maxd = fmaxf(maxd, __shfl_xor_sync(0xffffffffu, maxd, o));
-        maxl = fmaxf(maxl, __shfl_xor_sync(0xffffffffu, maxl, o));
-    }
-    if ((threadIdx.x & 31) == 0) {
-        atomic_max_f(&sb.ss->maxd, maxd);
-        atomic_max_f(&sb.ss->maxl, maxl);
-    }
+    block_max2(maxd, maxl);
+    if (threadIdx.x == 0) sb.part[blockIdx.x] = make_float2(maxd, maxl);
 }
 
-__global__ void k_s_body(SplitBuf sb, int N, int apply_only) {
-    if (!apply_only && *(volatile int32_t*)&sb.ss->done) return;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
-        const float4 a0 = sb.acc4[2 * i], a1 = sb.acc4[2 * i + 1];
-        float4 v = sb.vel4[2 * i], w = sb.vel4[2 * i + 1];
-        v.x += a0.x; v.y += a0.y; v.z += a0.z;
-        w.x += a0.w; w.y += a1.x; w.z += a1.y;
-        sb.vel4[2 * i] = v;
-        sb.vel4[2 * i + 1] = w;
-        sb.acc4[2 * i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        sb.acc4[2 * i + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-}
-
-__global__ void k_s_check(SplitBuf sb, int max_iter, float tol, cudaGraphConditionalHandle handle, int use_handle) {
-    SplitScalars* ss = sb.ss;
+// stop rule after a sweep: iteration cap, complementarity residual of the iterate entering the
+// sweep (max_c ||dlambda_c|| / max |lambda|), or a non-finite value
+__device__ __forceinline__ void sweep_check(SplitScalars* ss, float maxd, float maxl, int max_iter, float tol,
+                                            cudaGraphConditionalHandle handle, int use_handle) {
     if (!ss->done) {
-        const float maxd = __uint_as_float(ss->maxd), maxl = __uint_as_float(ss->maxl);
         const float r = maxd / fmaxf(maxl, 1e-30f);
         ss->res_last = r;
         ss->iters += 1;
         if (ss->iters >= max_iter || (tol > 0.f && r <= tol) || !(r == r)) ss->done = 1;
     }
-    ss->maxd = 0u;
-    ss->maxl = 0u;
     if (use_handle) cudaGraphSetConditional(handle, ss->done ? 0u : 1u);
+}
+
+// v += M^-1 W^T dlambda for every body; the last block to finish reduces the contact sweep's
+// per-block maxima and runs the stop rule (a completion counter, no waiting), so a sweep is two
+// kernels. Two bodies per thread keep four 16-byte loads in flight per body pair.
+__global__ void __launch_bounds__(256) k_s_body(SplitBuf sb, int N, int apply_only, int max_iter, float tol,
+                                                int nparts, cudaGraphConditionalHandle handle, int use_handle) {
+    if (!apply_only && *(volatile int32_t*)&sb.ss->done) {
+        // the loop is over: make sure the while node sees it even if no check runs this time
+        if (use_handle && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(handle, 0u);
+        return;
+    }
+    const int T = gridDim.x * blockDim.x;
+    for (int i0 = blockIdx.x * blockDim.x + threadIdx.x; i0 < N; i0 += 2 * T) {
+        const int i1 = i0 + T;
+        float4 a0 = sb.acc4[2 * i0], a1 = sb.acc4[2 * i0 + 1];
+        float4 v = sb.vel4[2 * i0], w = sb.vel4[2 * i0 + 1];
+        float4 b0, b1, u, z;
+        const bool two = i1 < N;
+        if (two) {
+            b0 = sb.acc4[2 * i1];
+            b1 = sb.acc4[2 * i1 + 1];
+            u = sb.vel4[2 * i1];
+            z = sb.vel4[2 * i1 + 1];
+        }
+        v.x += a0.x; v.y += a0.y; v.z += a0.z;
+        w.x += a0.w; w.y += a1.x; w.z += a1.y;
+        sb.vel4[2 * i0] = v;
+        sb.vel4[2 * i0 + 1] = w;
+        sb.acc4[2 * i0] = make_float4(0.f, 0.f, 0.f, 0.f);
+        sb.acc4[2 * i0 + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (two) {
+            u.x += b0.x; u.y += b0.y; u.z += b0.z;
+            z.x += b0.w; z.y += b1.x; z.z += b1.y;
+            sb.vel4[2 * i1] = u;
+            sb.vel4[2 * i1 + 1] = z;
+            sb.acc4[2 * i1] = make_float4(0.f, 0.f, 0.f, 0.f);
+            sb.acc4[2 * i1 + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    }
+    if (apply_only) return;
+    __shared__ bool last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(&sb.ss->blocks_done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    float md = 0.f, ml = 0.f;
+    for (int p = threadIdx.x; p < nparts; p += blockDim.x) {
+        const float2 q = sb.part[p];
+        md = fmaxf(md, q.x);
+        ml = fmaxf(ml, q.y);
+    }
+    block_max2(md, ml);
+    if (threadIdx.x == 0) {
+        sb.ss->blocks_done = 0u;
+        sweep_check(sb.ss, md, ml, max_iter, tol, handle, use_handle);
+    }
 }
 
 __global__ void k_s_reset(SplitBuf sb) {
     SplitScalars* ss = sb.ss;
     ss->done = (*sb.nc_dev == 0) ? 1 : 0;
     ss->iters = 0;
+    ss->blocks_done = 0u;
     ss->maxd = 0u;
     ss->maxl = 0u;
     ss->res_last = 0.f;
@@ -505,9 +639,13 @@ __device__ __forceinline__ void geom64(const Scene& sc, int a, int b, double* n,
         const double xa[3] = {sc.bf(BF_PX)[a], sc.bf(BF_PY)[a], sc.bf(BF_PZ)[a]};
         const double ra = sc.bf(BF_RAD)[a];
         double d[3] = {xb[0] - xa[0], xb[1] - xa[1], xb[2] - xa[2]};
-        const double dl = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-        if (dl > 0.0) { n[0] = d[0] / dl; n[1] = d[1] / dl; n[2] = d[2] / dl; }
-        else { n[0] = 0; n[1] = 0; n[2] = 1; }
+        const double dl2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        double dl = 0.0;
+        if (dl2 > 0.0) {
+            const double inv = rsqrt_nr(dl2);
+            dl = dl2 * inv;
+            n[0] = d[0] * inv; n[1] = d[1] * inv; n[2] = d[2] * inv;
+        } else { n[0] = 0; n[1] = 0; n[2] = 1; }
         rhoA = 0.5 * (dl + ra - rb);
         rhoB = 0.5 * (ra - rb - dl);
         return;
@@ -525,72 +663,49 @@ __device__ __forceinline__ void geom64(const Scene& sc, int a, int b, double* n,
     const double rel[3] = {xb[0] - p[0], xb[1] - p[1], xb[2] - p[2]};
     const double ax = rel[0] * u[0] + rel[1] * u[1] + rel[2] * u[2];
     const double perp[3] = {rel[0] - ax * u[0], rel[1] - ax * u[1], rel[2] - ax * u[2]};
-    const double rho = sqrt(perp[0] * perp[0] + perp[1] * perp[1] + perp[2] * perp[2]);
-    if (rho > 0.0) { n[0] = -perp[0] / rho; n[1] = -perp[1] / rho; n[2] = -perp[2] / rho; }
-    else { n[0] = 0; n[1] = 0; n[2] = 1; }
+    const double rho2 = perp[0] * perp[0] + perp[1] * perp[1] + perp[2] * perp[2];
+    double rho = 0.0;
+    if (rho2 > 0.0) {
+        const double inv = rsqrt_nr(rho2);
+        rho = rho2 * inv;
+        n[0] = -perp[0] * inv; n[1] = -perp[1] * inv; n[2] = -perp[2] * inv;
+    } else { n[0] = 0; n[1] = 0; n[2] = 1; }
     rhoB = -0.5 * ((sc.sf(SF_RAD)[s] - rho) + rb);
 }
 
+// Frisvad frame of a unit FP64 normal. The construction is orthonormal in exact arithmetic and the
+// normal is unit to ~1e-16, so the tangent is not renormalised (the residual tolerance is 1e-6).
 __device__ __forceinline__ void frame64(const double* n, double* t1, double* t2) {
     if (n[2] < -0.9999999) {
         t1[0] = 0; t1[1] = -1; t1[2] = 0;
         const double d = n[0] * t1[0] + n[1] * t1[1] + n[2] * t1[2];
         for (int k = 0; k < 3; ++k) t1[k] -= n[k] * d;
     } else {
-        const double a = 1.0 / (1.0 + n[2]);
+        const double a = rcp_nr(1.0 + n[2]);
         const double b = (-n[0] * n[1]) * a;
         t1[0] = 1.0 - (n[0] * n[0]) * a;
         t1[1] = b;
         t1[2] = -n[0];
     }
-    const double s = 1.0 / sqrt(t1[0] * t1[0] + t1[1] * t1[1] + t1[2] * t1[2]);
-    for (int k = 0; k < 3; ++k) t1[k] *= s;
+    if (n[2] < -0.9999999) {
+        const double s = rsqrt_nr(t1[0] * t1[0] + t1[1] * t1[1] + t1[2] * t1[2]);
+        for (int k = 0; k < 3; ++k) t1[k] *= s;
+    }
     f64::cross3(n, t1, t2);
 }
 
-__global__ void k_s_final_w(Scene sc, SplitBuf sb, int gen) {
-    const int nc = *sb.nc_dev;
-    const int N = sc.N;
-    const int64_t cap = sb.cap;
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
-        const int2 ab = sb.ab[c];
-        double n[3], rA, rB;
-        geom64(sc, ab.x, ab.y, n, rA, rB);
-        for (int k = 0; k < 3; ++k) sb.g64[k * cap + c] = n[k];
-        sb.g64[3 * cap + c] = rA;
-        sb.g64[4 * cap + c] = rB;
-        const float4 l = sb.lam[gen][c];
-        if (l.x == 0.f && l.y == 0.f && l.z == 0.f) continue;
-        double t1[3], t2[3];
-        frame64(n, t1, t2);
-        double P[3], tau[3];
-        for (int k = 0; k < 3; ++k) {
-            P[k] = (double)l.x * n[k] + (double)l.y * t1[k] + (double)l.z * t2[k];
-            tau[k] = (double)l.y * t2[k] - (double)l.z * t1[k];
-        }
-        for (int k = 0; k < 3; ++k) {
-            atomicAdd(&sb.acc64[(size_t)k * N + ab.y], P[k]);
-            atomicAdd(&sb.acc64[(size_t)(3 + k) * N + ab.y], rB * tau[k]);
-        }
-        if (ab.x >= 0) {
-            for (int k = 0; k < 3; ++k) {
-                atomicAdd(&sb.acc64[(size_t)k * N + ab.x], -P[k]);
-                atomicAdd(&sb.acc64[(size_t)(3 + k) * N + ab.x], -rA * tau[k]);
-            }
-        }
-    }
-}
-
-// v = v_free + M^-1 W^T lambda (world frame), in place of the accumulators
+// Final FP64 velocities (world frame): the FP64 free velocity plus the velocity increment the FP32
+// sweeps accumulated, v = v_free + (v32 - (float)v_free); the FP32 part only carries M^-1 W^T lambda.
 __global__ void k_s_final_body(Scene sc, SplitBuf sb) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= sc.N) return;
     const int N = sc.N;
-    const double il = sc.bf(BF_MINVL)[i], ia = sc.bf(BF_MINVA)[i];
-    for (int k = 0; k < 3; ++k) {
-        const size_t jl = (size_t)k * N + i, ja = (size_t)(3 + k) * N + i;
-        sb.acc64[jl] = sb.vfree[jl] + il * sb.acc64[jl];
-        sb.acc64[ja] = sb.vfree[ja] + ia * sb.acc64[ja];
+    const float4 v = sb.vel4[2 * i], w = sb.vel4[2 * i + 1];
+    const float vf[6] = {v.x, v.y, v.z, w.x, w.y, w.z};
+    for (int k = 0; k < 6; ++k) {
+        const size_t j = (size_t)k * N + i;
+        const double base = sb.vfree[j];
+        sb.acc64[j] = base + (double)(vf[k] - (float)base);
     }
 }
 
@@ -598,12 +713,12 @@ __global__ void k_s_final_body(Scene sc, SplitBuf sb) {
 __global__ void k_s_residual(Scene sc, SplitBuf sb, int gen, double alpha, int friction_enable, int combine) {
     const int nc = *sb.nc_dev;
     const int N = sc.N;
-    const int64_t cap = sb.cap;
     double maxd = 0.0, maxl = 0.0;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
-        const int2 ab = sb.ab[c];
-        const double n[3] = {sb.g64[c], sb.g64[cap + c], sb.g64[2 * cap + c]};
-        const double rA = sb.g64[3 * cap + c], rB = sb.g64[4 * cap + c];
+        const float4 r0 = sb.rec0[c], r1 = sb.rec1[c];
+        const int2 ab = make_int2(__float_as_int(r1.z), __float_as_int(r1.w));
+        double n[3], rA, rB;
+        geom64(sc, ab.x, ab.y, n, rA, rB);
         double t1[3], t2[3];
         frame64(n, t1, t2);
         double dv[3], Om[3];
@@ -622,7 +737,7 @@ __global__ void k_s_residual(Scene sc, SplitBuf sb, int gen, double alpha, int f
         }
         const double imb = sc.bf(BF_MINVL)[ab.y], iib = sc.bf(BF_MINVA)[ab.y];
         const double Dn = ima + imb, Dt = Dn + rA * rA * iia + rB * rB * iib;
-        const double Rn = Dn > 0 ? alpha / Dn : 0.0, Rt = Dt > 0 ? alpha / Dt : 0.0;
+        const double Rn = Dn > 0 ? alpha * rcp_nr(Dn) : 0.0, Rt = Dt > 0 ? alpha * rcp_nr(Dt) : 0.0;
         double g[3];
         g[0] = n[0] * dv[0] + n[1] * dv[1] + n[2] * dv[2];
         g[1] = (t1[0] * dv[0] + t1[1] * dv[1] + t1[2] * dv[2]) + (t2[0] * Om[0] + t2[1] * Om[1] + t2[2] * Om[2]);
@@ -690,30 +805,49 @@ __global__ void k_s_residual(Scene sc, SplitBuf sb, int gen, double alpha, int f
         }
         const float4 l = sb.lam[gen][c];
         const double lo[3] = {l.x, l.y, l.z};
-        const double mu = sb.nmu[c].w;
+        const double mu = fabsf(r0.w);
         double ln = lo[0] - Rn * (g[0] + bias[0]);
         double lt1 = lo[1] - Rt * (g[1] + bias[1]);
         double lt2 = lo[2] - Rt * (g[2] + bias[2]);
         ln = ln < 0.0 ? 0.0 : ln;
         const double tn2 = lt1 * lt1 + lt2 * lt2;
         if (tn2 > 0.0) {
-            const double s = fmin(1.0, (mu * ln) / sqrt(tn2));
+            const double s = fmin(1.0, (mu * ln) * rsqrt_nr(tn2));
             lt1 *= s;
             lt2 *= s;
         }
         const double d0 = ln - lo[0], d1 = lt1 - lo[1], d2 = lt2 - lo[2];
-        maxd = fmax(maxd, sqrt(d0 * d0 + d1 * d1 + d2 * d2));
+        maxd = fmax(maxd, d0 * d0 + d1 * d1 + d2 * d2);  // squared; the root is taken once at the end
         maxl = fmax(maxl, fmax(fabs(lo[0]), fmax(fabs(lo[1]), fabs(lo[2]))));
     }
     (void)friction_enable;
     (void)combine;
-    for (int o = 16; o > 0; o >>= 1) {
-        maxd = fmax(maxd, __shfl_xor_sync(0xffffffffu, maxd, o));
-        maxl = fmax(maxl, __shfl_xor_sync(0xffffffffu, maxl, o));
-    }
-    if ((threadIdx.x & 31) == 0) {
+    block_max2(maxd, maxl);
+    if (threadIdx.x == 0) {
         atomicMax(&sb.ss->maxd64, (unsigned long long)__double_as_longlong(maxd));
         atomicMax(&sb.ss->maxl64, (unsigned long long)__double_as_longlong(maxl));
+    }
+}
+
+__global__ void k_s_drift(Scene sc, double h) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < sc.N) {
+        double x[3] = {sc.bf(BF_PX)[i], sc.bf(BF_PY)[i], sc.bf(BF_PZ)[i]};
+        double q[4] = {sc.bf(BF_QX)[i], sc.bf(BF_QY)[i], sc.bf(BF_QZ)[i], sc.bf(BF_QW)[i]};
+        const double v[3] = {sc.bf(BF_VX)[i], sc.bf(BF_VY)[i], sc.bf(BF_VZ)[i]};
+        const double w[3] = {sc.bf(BF_WX)[i], sc.bf(BF_WY)[i], sc.bf(BF_WZ)[i]};
+        drift_fast(x, q, v, w, h);
+        sc.bf(BF_PX)[i] = x[0]; sc.bf(BF_PY)[i] = x[1]; sc.bf(BF_PZ)[i] = x[2];
+        sc.bf(BF_QX)[i] = q[0]; sc.bf(BF_QY)[i] = q[1]; sc.bf(BF_QZ)[i] = q[2]; sc.bf(BF_QW)[i] = q[3];
+    } else if (i < sc.N + sc.S) {
+        const int s = i - sc.N;
+        double x[3] = {sc.sf(SF_PX)[s], sc.sf(SF_PY)[s], sc.sf(SF_PZ)[s]};
+        double q[4] = {sc.sf(SF_QX)[s], sc.sf(SF_QY)[s], sc.sf(SF_QZ)[s], sc.sf(SF_QW)[s]};
+        const double v[3] = {sc.sf(SF_VX)[s], sc.sf(SF_VY)[s], sc.sf(SF_VZ)[s]};
+        const double w[3] = {sc.sf(SF_WX)[s], sc.sf(SF_WY)[s], sc.sf(SF_WZ)[s]};
+        drift_fast(x, q, v, w, h);
+        sc.sf(SF_PX)[s] = x[0]; sc.sf(SF_PY)[s] = x[1]; sc.sf(SF_PZ)[s] = x[2];
+        sc.sf(SF_QX)[s] = q[0]; sc.sf(SF_QY)[s] = q[1]; sc.sf(SF_QZ)[s] = q[2]; sc.sf(SF_QW)[s] = q[3];
     }
 }
 
@@ -739,14 +873,69 @@ __global__ void k_s_final_scalar(SplitBuf sb) {
     SplitScalars* ss = sb.ss;
     const double maxd = __longlong_as_double((long long)ss->maxd64);
     const double maxl = __longlong_as_double((long long)ss->maxl64);
-    ss->res_final = maxd / fmax(maxl, 1e-30);
+    ss->res_final = sqrt(maxd) / fmax(maxl, 1e-30);
+}
+
+__global__ void k_nr64_selftest(int n, const double* x, double* rcp, double* rsq) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    rcp[i] = rcp_nr(x[i]);
+    rsq[i] = rsqrt_nr(x[i]);
 }
 
 }  // namespace
 
+int launch_nr64_selftest(int n, const double* x, double* rcp, double* rsq, cudaStream_t s) {
+    if (n > 0) k_nr64_selftest<<<nblk(n), NT, 0, s>>>(n, x, rcp, rsq);
+    return 0;
+}
+
 int split_grid_blocks(int64_t n, int sms) {
     const int64_t want = (n + NT - 1) / NT;
     const int64_t cap = (int64_t)sms * 8;
+    return (int)(want < 1 ? 1 : (want < cap ? want : cap));
+}
+
+// Launch shapes of the contact sweep the autotuner chooses between: contacts per thread, threads
+// per block and the register budget (minimum resident blocks per SM).
+struct ContactVariant {
+    void (*kernel)(SplitBuf, int, float);
+    int unroll, nth, minb;
+    int per_sm;
+};
+static ContactVariant g_variants[] = {
+    {k_s_contact_t<1, 256, 4>, 1, 256, 4, 0},
+    {k_s_contact_t<1, 256, 5>, 1, 256, 5, 0},
+    {k_s_contact_t<2, 256, 2>, 2, 256, 2, 0},
+    {k_s_contact_t<1, 128, 8>, 1, 128, 8, 0},
+    {k_s_contact_t<2, 128, 4>, 2, 128, 4, 0},
+};
+constexpr int N_VARIANTS = sizeof(g_variants) / sizeof(g_variants[0]);
+
+// a variant is a kernel shape and a grid of 1 or 2 resident waves (index = 2 * shape + waves - 1)
+int split_num_variants() { return 2 * N_VARIANTS; }
+
+const char* split_variant_name(int v) {
+    static const char* names[] = {"u1-t256-b4-w1", "u1-t256-b4-w2", "u1-t256-b5-w1", "u1-t256-b5-w2",
+                                  "u2-t256-b2-w1", "u2-t256-b2-w2", "u1-t128-b8-w1", "u1-t128-b8-w2",
+                                  "u2-t128-b4-w1", "u2-t128-b4-w2"};
+    return (v >= 0 && v < 2 * N_VARIANTS) ? names[v] : "?";
+}
+
+// grid of a variant: the resident capacity of the GPU (no partial tail wave), or fewer blocks when
+// there is less work than one pass
+int split_contact_blocks(int vi, int64_t n, int sms) {
+    ContactVariant& cv = g_variants[vi / 2];
+    const int waves = 1 + (vi & 1);
+    if (cv.per_sm == 0) {
+        int b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, cv.kernel, cv.nth, 0);
+        cv.per_sm = b > 0 ? b : 1;
+    }
+    const int64_t per_block = (int64_t)cv.nth * cv.unroll;
+    const int64_t want = (n + per_block - 1) / per_block;
+    int64_t cap = (int64_t)sms * cv.per_sm * waves;
+    if (cap > SPLIT_MAX_PARTS) cap = SPLIT_MAX_PARTS;
     return (int)(want < 1 ? 1 : (want < cap ? want : cap));
 }
 
@@ -780,20 +969,26 @@ void launch_s_reset(const SplitBuf& sb, cudaStream_t s) { k_s_reset<<<1, 1, 0, s
 void launch_s_apply_warm(const SplitBuf& sb, int gen, int blocks, cudaStream_t s) {
     k_s_apply_warm<<<blocks, NT, 0, s>>>(sb, gen);
 }
-void launch_s_contact(const SplitBuf& sb, int gen, int blocks, cudaStream_t s) {
-    k_s_contact<<<blocks, NT, 0, s>>>(sb, gen);
+void launch_s_contact(const SplitBuf& sb, int gen, float alpha, int variant, int blocks, cudaStream_t s) {
+    const ContactVariant& cv = g_variants[variant / 2];
+    cv.kernel<<<blocks, cv.nth, 0, s>>>(sb, gen, alpha);
 }
-void launch_s_body(const SplitBuf& sb, int N, int blocks, int apply_only, cudaStream_t s) {
-    k_s_body<<<blocks, NT, 0, s>>>(sb, N, apply_only);
+void launch_s_body(const SplitBuf& sb, int N, int blocks, int apply_only, int max_iter, float tol, int nparts,
+                   cudaGraphConditionalHandle h, int use_handle, cudaStream_t s) {
+    k_s_body<<<blocks, NT, 0, s>>>(sb, N, apply_only, max_iter, tol, nparts, h, use_handle);
 }
-void launch_s_check(const SplitBuf& sb, int max_iter, float tol, cudaGraphConditionalHandle h, int use_handle,
-                    cudaStream_t s) {
-    k_s_check<<<1, 1, 0, s>>>(sb, max_iter, tol, h, use_handle);
+
+// body-pass grid: two resident waves' worth of blocks at most (each thread takes two bodies)
+int split_body_blocks(int64_t n, int sms) {
+    const int64_t want = (n + 2 * (int64_t)NT - 1) / (2 * (int64_t)NT);
+    const int64_t cap = (int64_t)sms * 4;
+    return (int)(want < 1 ? 1 : (want < cap ? want : cap));
+}
+void launch_s_drift(const Scene& sc, double h, cudaStream_t s) {
+    if (sc.N + sc.S > 0) k_s_drift<<<nblk(sc.N + sc.S), NT, 0, s>>>(sc, h);
 }
 void launch_s_final(const Scene& sc, const SplitBuf& sb, int gen, double alpha, int friction_enable, int combine,
                     int blocks, cudaStream_t s) {
-    if (sc.N > 0) cudaMemsetAsync(sb.acc64, 0, sizeof(double) * 6 * (size_t)sc.N, s);
-    k_s_final_w<<<blocks, NT, 0, s>>>(sc, sb, gen);
     if (sc.N > 0) k_s_final_body<<<nblk(sc.N), NT, 0, s>>>(sc, sb);
     k_s_residual<<<blocks, NT, 0, s>>>(sc, sb, gen, alpha, friction_enable, combine);
     if (sc.N > 0) k_s_writeback<<<nblk(sc.N), NT, 0, s>>>(sc, sb);

@@ -11,6 +11,8 @@ namespace cdx {
 struct SplitScalars {
     int32_t done;
     int32_t iters;
+    unsigned int blocks_done;  // completion counter of the body pass (last block runs the check)
+    int32_t pad1;
     unsigned int maxd;  // bits of max ||dlambda_c|| (FP32, non-negative)
     unsigned int maxl;  // bits of max |lambda|
     float res_last;
@@ -27,14 +29,23 @@ struct SplitParams {
     int combine;
     int friction_enable;
     int prev_count;
+    // previous step's contact layout, for an O(1) warm-start lookup: static contact of slot k was
+    // contact prev_spos[k] when prev_sflags[k]; pair contacts of owner i were
+    // [prev_n_static + prev_poff[i], prev_n_static + prev_poff[i+1])
+    const int32_t* prev_sflags;
+    const int32_t* prev_spos;
+    const int32_t* prev_poff;
+    int prev_n_static;
 };
 
-// Contact records are float4-aligned so a warp reads them with 16-byte vector loads:
-//   ab   (body A or -(static)-1, body B)
-//   nmu  (n.x, n.y, n.z, mu)
-//   levR (rhoA, rhoB, R_n, R_t)        R = alpha / Delassus diagonal
-//   bias (R_n b_n, R_t b_t1, R_t b_t2)  static wall velocity and restitution terms
+// Contact records are two float4s so a warp reads them with 16-byte vector loads:
+//   rec0 (n.x, n.y, n.z, mu)        the sign bit of mu flags a contact with a velocity bias
+//   rec1 (rhoA, rhoB, A, B)          signed lever lengths along n; A = body index or -(static)-1
+//                                    and B stored as int bits
+//   bias (b_n, b_t1, b_t2)           static wall velocity and restitution terms (flagged contacts)
 //   lam  (lambda_n, lambda_t1, lambda_t2) per generation (warm start)
+// R = alpha / diag(W M^-1 W^T) is recomputed in the sweep from the inverse masses that come with
+// the velocity gathers: R_n = alpha / (1/mA + 1/mB), R_t = alpha / (1/mA + 1/mB + rhoA^2/IA + rhoB^2/IB).
 struct SplitBuf {
     int N = 0;
     int64_t cap = 0;
@@ -49,19 +60,24 @@ struct SplitBuf {
     float4* st_pt = nullptr;  // S: (anchor in scene coordinates, drum radius)
     float4* st_v = nullptr;   // S: (wall velocity, kind)
     float4* st_w = nullptr;   // S: (wall angular velocity world, mu)
-    int2* ab = nullptr;
-    float4* nmu = nullptr;
-    float4* levR = nullptr;
+    float4* rec0 = nullptr;
+    float4* rec1 = nullptr;
     float4* bias = nullptr;
     float4* lam[2] = {nullptr, nullptr};
     unsigned long long* key[2] = {nullptr, nullptr};
     float4* pt[2] = {nullptr, nullptr};
-    double* g64 = nullptr;    // 5*cap FP64 geometry (n, rhoA, rhoB) of the final pass
     int32_t* nc_dev = nullptr;
     SplitScalars* ss = nullptr;
+    float2* part = nullptr;   // per-block (max ||dlambda||, max |lambda|) of the contact sweep
+    int has_restitution = 0;  // pre-solve velocities are only needed for restitution terms
 };
 
 int split_grid_blocks(int64_t n, int sms);
+int launch_nr64_selftest(int n, const double* x, double* rcp, double* rsq, cudaStream_t s);
+int split_contact_blocks(int variant, int64_t n, int sms);
+constexpr int SPLIT_MAX_PARTS = 4096;  // capacity of the per-block partial maxima
+int split_num_variants();
+const char* split_variant_name(int v);
 void launch_s_prep(const Scene& sc, const SplitBuf& sb, double dt, const double* g, double h1, cudaStream_t s);
 void launch_s_static_flags(const Scene& sc, const SplitBuf& sb, float margin, int32_t* flags, cudaStream_t s);
 void launch_s_pair_count(const Scene& sc, const Grid& g, const SplitBuf& sb, const uint32_t* cell_body,
@@ -74,10 +90,11 @@ void launch_s_pair_write(const Scene& sc, const Grid& g, const SplitBuf& sb, con
                          int gen, const SplitParams& P, DevScalars* ds, cudaStream_t s);
 void launch_s_reset(const SplitBuf& sb, cudaStream_t s);
 void launch_s_apply_warm(const SplitBuf& sb, int gen, int blocks, cudaStream_t s);
-void launch_s_contact(const SplitBuf& sb, int gen, int blocks, cudaStream_t s);
-void launch_s_body(const SplitBuf& sb, int N, int blocks, int apply_only, cudaStream_t s);
-void launch_s_check(const SplitBuf& sb, int max_iter, float tol, cudaGraphConditionalHandle h, int use_handle,
-                    cudaStream_t s);
+void launch_s_contact(const SplitBuf& sb, int gen, float alpha, int variant, int blocks, cudaStream_t s);
+void launch_s_body(const SplitBuf& sb, int N, int blocks, int apply_only, int max_iter, float tol, int nparts,
+                   cudaGraphConditionalHandle h, int use_handle, cudaStream_t s);
+int split_body_blocks(int64_t n, int sms);
+void launch_s_drift(const Scene& sc, double h, cudaStream_t s);
 void launch_s_final(const Scene& sc, const SplitBuf& sb, int gen, double alpha, int friction_enable, int combine,
                     int blocks, cudaStream_t s);
 

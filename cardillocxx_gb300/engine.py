@@ -180,6 +180,14 @@ class PhysicsEngine:
         return {"ms_contact": vals[0].value, "ms_body": vals[1].value, "bytes_contact": vals[2].value,
                 "bytes_body": vals[3].value}
 
+    def selftest_nr64(self, x):
+        """Device Newton-Raphson reciprocal / inverse square root of x (diagnostic)."""
+        x = np.ascontiguousarray(x, np.float64)
+        r = np.empty_like(x)
+        q = np.empty_like(x)
+        self._check(self.L.cdx_selftest_nr64(self.h, x.shape[0], dp(x), dp(r), dp(q)))
+        return r, q
+
     def stream(self) -> int:
         return int(self.L.cdx_stream(self.h) or 0)
 

@@ -69,6 +69,7 @@ typedef struct cdx_config {
     int32_t gpu_block;                /* gpu.block: threads per block for contact kernels (0 = auto) */
     double gpu_contact_capacity_factor; /* gpu.contact_capacity: initial contact slots per body */
     int32_t gpu_use_graph;            /* gpu.graph: capture the solver loop in a CUDA graph (split form) */
+    int32_t gpu_autotune;             /* gpu.autotune: pick the contact-sweep launch shape by timing (split form) */
 } cdx_config;
 
 /* Scene: dynamic spheres plus static shapes (halfspaces, drums). Bodies of one scene are
@@ -115,6 +116,8 @@ typedef struct cdx_stats {
     double ms_integrate;
     double solve_bytes_per_iter; /* algorithmic bytes of one sweep (per-contact and per-body words) */
     int64_t kernel_launches;   /* cdx kernels launched so far */
+    int32_t contact_variant;   /* split form: launch shape of the contact sweep chosen by the autotuner */
+    int32_t autotune_runs;     /* split form: times the autotuner ran */
 } cdx_stats;
 
 typedef struct cdx_ctx cdx_ctx;
@@ -165,6 +168,10 @@ int cdx_pj_solve_csr(cdx_ctx* ctx, int32_t nrows, int32_t nv, int32_t nfl, const
                      const double* restitution, const double* minv, const double* mdiag, const double* v,
                      const double* f_ext, const double* f_gyro, double dt, double alpha, int32_t max_iter,
                      double tol_abs, double tol_rel, double* lambda_inout, double* x_out, int32_t* iterations);
+
+/* ---- diagnostics: the FP64 Newton-Raphson reciprocal and reciprocal square root of the split
+ * form's final pass, evaluated on the device for host-side checks against IEEE results ---- */
+int cdx_selftest_nr64(cdx_ctx* ctx, int32_t n, const double* x, double* rcp, double* rsqrt);
 
 /* ---- seeded scene generators for the benchmark scenes (host only) ---- */
 typedef struct cdx_gen_params {

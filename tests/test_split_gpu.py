@@ -36,7 +36,8 @@ def test_split_resting_and_sliding(gpu):
     st = e.state()
     m = s["mass"][0]
     np.testing.assert_allclose(st["vel"][0, 0], 1.0 - n * mu * G * H, rtol=F32_RTOL)
-    np.testing.assert_allclose(st["omega"][0, 1], n * H * 5 * mu * G / (2 * r), rtol=1e-4)
+    lever = r - 0.5e-5  # centre to contact point (midpoint of the 10 micrometre overlap)
+    np.testing.assert_allclose(st["omega"][0, 1], n * H * 5 * mu * G * lever / (2 * r * r), rtol=1e-4)
     lam = e.contacts()["lambda"][0]
     np.testing.assert_allclose(lam[0], m * G * H, rtol=F32_RTOL)
     assert e.stats()["residual"] < 1e-5
@@ -137,3 +138,17 @@ def test_split_batched_and_graph_off(gpu):
     assert np.isfinite(za).all() and np.isfinite(zb).all()
     assert abs(za.mean() - zb.mean()) < 1e-3
     assert a.stats()["iterations"] == b.stats()["iterations"] == 50
+
+
+def test_newton_raphson_fp64_matches_ieee(gpu):
+    # the split form's FP64 final pass uses Newton-Raphson reciprocals / inverse square roots;
+    # they must agree with correctly rounded IEEE results to a couple of ulps
+    from cardillocxx_gb300 import PhysicsEngine as PE
+    rng = np.random.default_rng(3)
+    x = np.concatenate([10.0 ** rng.uniform(-29, 29, 200000), rng.uniform(0.5, 2.0, 100000),
+                        [1.0, 2.0, 4.0, 1e-31, 1e31, 3.0]])
+    r, q = PE({}).selftest_nr64(x)
+    exact_r, exact_q = 1.0 / x, 1.0 / np.sqrt(x)
+    eps = np.finfo(float).eps
+    assert np.max(np.abs(r - exact_r) / np.abs(exact_r)) <= 2 * eps
+    assert np.max(np.abs(q - exact_q) / np.abs(exact_q)) <= 2 * eps
