@@ -65,6 +65,8 @@ void Engine::dfree(void* p) {
 Engine::~Engine() {
     if (stream) cudaStreamSynchronize(stream);
     destroy_split();
+    delete csr;
+    csr = nullptr;
     for (void* p : owned) cudaFree(p);
     owned.clear();
     if (hs) cudaFreeHost(hs);
@@ -218,6 +220,8 @@ int Engine::load_scene(const cdx_scene& s) {
     destroy_split();
     for (void* p : owned) cudaFree(p);
     owned.clear();
+    delete csr;  // its device buffers were in the owned list
+    csr = nullptr;
     sc = Scene{};
     C = Contacts{};
     inc = Incidence{};

@@ -11,6 +11,17 @@
 namespace cdx {
 const char* status_name(int st);
 struct SplitState;
+// work buffers of the solver-level CSR solve (engine_csr.cpp); device memory in Engine::owned
+struct CsrBuffers {
+    int64_t nnz_cap = 0, row_cap = 0, nv_cap = 0;
+    int32_t *ptr = nullptr, *col = nullptr, *rowidx = nullptr, *cstart = nullptr, *cend = nullptr;
+    uint32_t *ck_in = nullptr, *ck_out = nullptr, *nz_in = nullptr, *nz_out = nullptr;
+    double *val = nullptr, *RW = nullptr, *cb = nullptr, *mu = nullptr, *e = nullptr, *biasR = nullptr,
+           *lam = nullptr, *dlam = nullptr;
+    double *minv = nullptr, *mdiag = nullptr, *v = nullptr, *fext = nullptr, *fgyro = nullptr, *rhs = nullptr,
+           *x = nullptr;
+    DevScalars* ds = nullptr;
+};
 }  // namespace cdx
 
 struct Engine {
@@ -54,6 +65,7 @@ struct Engine {
     std::vector<double> trace_buf;
 
     cdx::SplitState* split = nullptr;
+    cdx::CsrBuffers* csr = nullptr;
 
     ~Engine();
     int fail(int st, const std::string& msg);

@@ -9,18 +9,6 @@
 
 using namespace cdx;
 
-namespace {
-struct CsrBuffers {
-    int64_t nnz_cap = 0, row_cap = 0, nv_cap = 0;
-    int32_t *ptr = nullptr, *col = nullptr, *rowidx = nullptr, *cstart = nullptr, *cend = nullptr;
-    uint32_t *ck_in = nullptr, *ck_out = nullptr, *nz_in = nullptr, *nz_out = nullptr;
-    double *val = nullptr, *RW = nullptr, *cb = nullptr, *mu = nullptr, *e = nullptr, *biasR = nullptr,
-           *lam = nullptr, *dlam = nullptr;
-    double *minv = nullptr, *mdiag = nullptr, *v = nullptr, *fext = nullptr, *fgyro = nullptr, *rhs = nullptr,
-           *x = nullptr;
-    DevScalars* ds = nullptr;
-};
-}  // namespace
 
 static int grow(Engine& E, CsrBuffers& B, int64_t nnz, int64_t nrows, int64_t nv) {
     int st;
@@ -63,12 +51,11 @@ static int grow(Engine& E, CsrBuffers& B, int64_t nnz, int64_t nrows, int64_t nv
     return E.ensure_tmp(std::max<int64_t>(nnz, nv + 1));
 }
 
+// the work buffers belong to the context: created on first use, their device memory is in the
+// context's owned list and goes away with it
 static CsrBuffers& buffers(Engine& E) {
-    static thread_local std::vector<std::pair<Engine*, CsrBuffers>> all;
-    for (auto& p : all)
-        if (p.first == &E) return p.second;
-    all.emplace_back(&E, CsrBuffers{});
-    return all.back().second;
+    if (!E.csr) E.csr = new CsrBuffers();
+    return *E.csr;
 }
 
 extern "C" int cdx_pj_solve_csr(cdx_ctx* ctx, int32_t nrows, int32_t nv, int32_t nfl, const int32_t* row_ptr,

@@ -179,3 +179,31 @@ def test_csr_solver_dropin(gpu, oracle_mod):
     xg, lg, itg = eng.pj_solve_csr(**args)
     assert ito == itg
     assert_same(xg, xo, "csr x (early exit)")
+
+
+def test_csr_dropin_across_fresh_contexts(gpu, oracle_mod):
+    # contexts created and destroyed in turn (a new one may reuse the old one's address) each keep
+    # their own work buffers
+    rng = np.random.default_rng(5)
+    nb, nv = 10, 60
+    cols, vals, ptr = [], [], [0]
+    for _ in range(3 * 8):
+        a, b = sorted(rng.choice(nb, 2, replace=False))
+        for body in (a, b):
+            for k in range(6):
+                cols.append(6 * body + k)
+                vals.append(rng.normal())
+        ptr.append(len(cols))
+    m = rng.uniform(0.5, 2.0, nv)
+    args = dict(row_ptr=np.array(ptr, np.int32), col=np.array(cols, np.int32), val=np.array(vals),
+                contact_bias=np.zeros(24), mu=np.full(24, 0.4), restitution=np.zeros(24), minv=1.0 / m,
+                mdiag=1.0 / (1.0 / m), v=rng.normal(size=nv), f_ext=rng.normal(size=nv), f_gyro=np.zeros(nv), dt=1e-3,
+                alpha=0.3, max_iter=30, tol_abs=0.0, tol_rel=0.0, lam0=np.zeros(24))
+    xo, lo, _ = oracle_mod.pj_solve_csr(**args)
+    for _ in range(4):
+        eng = PhysicsEngine({})
+        x, lam, _ = eng.pj_solve_csr(**args)
+        eng.close()
+        del eng
+        assert_same(x, xo, "csr x, fresh context")
+        assert_same(lam, lo, "csr lambda, fresh context")
