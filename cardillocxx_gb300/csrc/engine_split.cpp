@@ -25,7 +25,6 @@ struct SplitState {
     cudaGraphExec_t exec[2] = {nullptr, nullptr};
     cudaGraph_t graph[2] = {nullptr, nullptr};
     int graph_blocks = 0;
-    int graph_body_blocks = 0;
     int graph_maxit = -1;
     float graph_tol = -1.f;
     int64_t graph_cap = -1;
@@ -115,7 +114,8 @@ static int init_split(Engine& E) {
     const size_t n1 = std::max(1, N);
     if ((st = salloc(E, (void**)&b.pos4, sizeof(float4) * n1, "split bodies"))) return st;
     if ((st = salloc(E, (void**)&b.vel4, sizeof(float4) * 2 * n1, "split bodies"))) return st;
-    if ((st = salloc(E, (void**)&b.acc4, sizeof(float4) * 2 * n1, "split bodies"))) return st;
+    for (int k = 0; k < 3; ++k)
+        if ((st = salloc(E, (void**)&b.acc[k], sizeof(float4) * 2 * n1, "split bodies"))) return st;
     if ((st = salloc(E, (void**)&b.vn4, sizeof(float4) * 2 * n1, "split bodies"))) return st;
     if ((st = salloc(E, (void**)&b.vfree, sizeof(double) * 6 * n1, "split bodies"))) return st;
     if ((st = salloc(E, (void**)&b.acc64, sizeof(double) * 6 * n1, "split bodies"))) return st;
@@ -178,8 +178,7 @@ static int build_graph(Engine& E, int g) {
     cudaGraph_t body = p.conditional.phGraph_out[0];
     if ((st = E.cuda_check(cudaStreamBeginCaptureToGraph(E.stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed),
                            "capture"))) return st;
-    launch_s_contact(S->sb, g, (float)E.cfg.pj_alpha, S->variant, S->graph_blocks, E.stream);
-    launch_s_body(S->sb, E.sc.N, S->graph_body_blocks, 0, maxit, tol, S->graph_blocks, h, 1, E.stream);
+    launch_s_sweep(S->sb, g, (float)E.cfg.pj_alpha, S->variant, S->graph_blocks, maxit, tol, h, 1, E.stream);
     cudaGraph_t captured = nullptr;
     if ((st = E.cuda_check(cudaStreamEndCapture(E.stream, &captured), "end capture"))) return st;
     if ((st = E.cuda_check(cudaGraphInstantiate(&S->exec[g], graph, 0), "graph instantiate"))) return st;
@@ -252,11 +251,9 @@ int Engine::step_split() {
     // x0 = v_free + M^-1 W^T lambda_warm
     const int cblocks = split_grid_blocks(std::max(S->nc, 1), S->sms);
     const int sblocks = split_contact_blocks(S->variant, std::max(S->nc, 1), S->sms);
-    const int bblocks = split_body_blocks(std::max(N, 1), S->sms);
     launch_s_reset(sb, stream);
     launch_s_apply_warm(sb, gen, cblocks, stream);
-    launch_s_body(sb, N, bblocks, 1, 0, 0.f, 0, 0, 0, stream);
-    launches += 3;
+    launches += 2;
     if (timing) cudaEventRecord(ev[2], stream);
     const int maxit = std::max(1, cfg.pj_max_iterations);
     bool solved = false;
@@ -277,15 +274,14 @@ int Engine::step_split() {
             for (int r = 0; r < 2; ++r) {
                 const int vb = split_contact_blocks(v, S->nc, S->sms);
                 cudaEventRecord(S->tev[0], stream);
-                launch_s_contact(sb, gen, (float)cfg.pj_alpha, v, vb, stream);
+                launch_s_sweep(sb, gen, (float)cfg.pj_alpha, v, vb, maxit, (float)cfg.gpu_residual_tol, none, 0, stream);
                 cudaEventRecord(S->tev[1], stream);
-                launch_s_body(sb, N, bblocks, 0, maxit, (float)cfg.gpu_residual_tol, vb, none, 0, stream);
                 if ((st = cuda_check(cudaEventSynchronize(S->tev[1]), "autotune"))) return st;
                 float ms1 = 0;
                 cudaEventElapsedTime(&ms1, S->tev[0], S->tev[1]);
                 t += ms1;
             }
-            launches += 4;
+            launches += 2;
             if (t < best_t) {
                 best_t = t;
                 best = v;
@@ -308,7 +304,6 @@ int Engine::step_split() {
                 destroy_graphs(S);
                 S->graph_variant = S->variant;
                 S->graph_blocks = gblocks;
-                S->graph_body_blocks = bblocks;
                 if ((st = build_graph(*this, 0)) || (st = build_graph(*this, 1))) return st;
                 S->graph_cap = sb.cap;
                 S->graph_maxit = maxit;
@@ -324,8 +319,8 @@ int Engine::step_split() {
                     if ((st = cuda_check(cudaStreamSynchronize(stream), "poll"))) return st;
                     if (S->h_ss->done) break;
                 }
-                launch_s_contact(sb, gen, (float)cfg.pj_alpha, S->variant, sblocks, stream);
-                launch_s_body(sb, N, bblocks, 0, maxit, (float)cfg.gpu_residual_tol, sblocks, none, 0, stream);
+                launch_s_sweep(sb, gen, (float)cfg.pj_alpha, S->variant, sblocks, maxit, (float)cfg.gpu_residual_tol, none,
+                               0, stream);
             }
         }
     }
@@ -339,7 +334,7 @@ int Engine::step_split() {
     if ((st = cuda_check(cudaStreamSynchronize(stream), "split step"))) return st;
     if ((st = cuda_check(cudaGetLastError(), "split launch"))) return st;
     S->last_iters = S->nc > 0 ? S->h_ss->iters : 0;
-    launches += 2 * (int64_t)S->last_iters;
+    launches += (int64_t)S->last_iters;
     S->res_last = S->h_ss->res_last;
     S->res_final = S->nc > 0 ? S->h_ss->res_final : 0.0;
     S->prev_count = S->nc;
@@ -402,9 +397,9 @@ int Engine::get_contacts_split(int32_t* ia, int32_t* ib, double* point, double* 
 
 double Engine::split_bytes_per_iter() const {
     // per contact: n and mu (16), lever lengths and body indices (16), lambda read + write (24, its
-    // three words); per body: velocities read + write (48) and accumulators read + zeroed (48)
+    // three words); per body: the accumulator cleared for the sweep after next (24)
     const int n = split ? split->prev_count : 0;
-    return (double)n * (16 + 16 + 24) + (double)sc.N * 96.0;
+    return (double)n * (16 + 16 + 24) + (double)sc.N * 24.0;
 }
 
 // Kernel-level timing of the sweep (CUDA events around each launch, engine stream).
@@ -420,15 +415,13 @@ int Engine::time_sweeps(int n, double* msc, double* msb, double* bc, double* bb)
         SplitState* S = split;
         const int g = S->gen ^ 1;
         const int cblocks = split_contact_blocks(S->variant, S->prev_count, S->sms);
-        const int bblocks = split_body_blocks(std::max(sc.N, 1), S->sms);
         *S->h_nc = S->prev_count;
         cudaMemcpyAsync(S->sb.nc_dev, S->h_nc, sizeof(int32_t), cudaMemcpyHostToDevice, stream);
         cudaMemsetAsync(S->sb.ss, 0, sizeof(SplitScalars), stream);
         for (int k = 0; k < n; ++k) {
             cudaEventRecord(e[0], stream);
-            launch_s_contact(S->sb, g, (float)cfg.pj_alpha, S->variant, cblocks, stream);
+            launch_s_sweep(S->sb, g, (float)cfg.pj_alpha, S->variant, cblocks, 1 << 30, 0.f, 0, 0, stream);
             cudaEventRecord(e[1], stream);
-            launch_s_body(S->sb, sc.N, bblocks, 0, 1 << 30, 0.f, cblocks, 0, 0, stream);
             cudaEventRecord(e[2], stream);
             if ((st = cuda_check(cudaEventSynchronize(e[2]), "time sweeps"))) break;
             float a = 0, b = 0;
@@ -437,9 +430,11 @@ int Engine::time_sweeps(int n, double* msc, double* msb, double* bc, double* bb)
             tc += a;
             tb += b;
         }
-        launches += 2 * (int64_t)n;
-        if (bc) *bc = (double)S->prev_count * (16 + 16 + 24);
-        if (bb) *bb = (double)sc.N * 96.0;
+        launches += (int64_t)n;
+        // one sweep: per contact the two records (32) and lambda read + write (24); per body the
+        // accumulator cleared for the sweep after next (24)
+        if (bc) *bc = (double)S->prev_count * (16 + 16 + 24) + (double)sc.N * 24.0;
+        if (bb) *bb = 0.0;
     } else if (!sp && prev_count > 0) {
         const int g = gen ^ 1;
         cudaMemsetAsync(ds, 0, sizeof(DevScalars), stream);

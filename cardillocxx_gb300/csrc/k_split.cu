@@ -150,8 +150,10 @@ __global__ void k_s_prep(Scene sc, SplitBuf sb, double dt, double g0, double g1,
             sb.vn4[2 * i] = make_float4((float)v[0], (float)v[1], (float)v[2], 0.f);
             sb.vn4[2 * i + 1] = make_float4((float)ww[0], (float)ww[1], (float)ww[2], 0.f);
         }
-        sb.acc4[2 * i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        sb.acc4[2 * i + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+        sb.acc[0][2 * i] = sb.vel4[2 * i];
+        sb.acc[0][2 * i + 1] = sb.vel4[2 * i + 1];
+        sb.acc[1][2 * i] = sb.vel4[2 * i];
+        sb.acc[1][2 * i + 1] = sb.vel4[2 * i + 1];
         const int s = sc.body_scene[i];
         const double* o = &sb.origin[3 * s];
         sb.pos4[i] = make_float4((float)(x[0] - o[0]), (float)(x[1] - o[1]), (float)(x[2] - o[2]),
@@ -421,20 +423,21 @@ __global__ void k_s_pairs(Scene sc, Grid gr, SplitBuf sb, const uint32_t* cell_b
 
 // ------------------------------------------------------------------ projected Jacobi (FP32)
 // apply W^T dl (pre-scaled by M^-1) to the bodies of contact c with float4/float2 vector atomics
-__device__ __forceinline__ void scatter(SplitBuf& sb, int a, int b, float3 n, float3 t1, float3 t2, float rhoA,
+__device__ __forceinline__ void scatter(float4* acc, int a, int b, float3 n, float3 t1, float3 t2, float rhoA,
                                         float rhoB, float dln, float dlt1, float dlt2, float imb, float iib, float ima,
                                         float iia) {
+    // accumulator layout = velocity layout: (v.xyz, 1/m), (omega.xyz, 1/I); the .w lanes get +0
     const float3 P = dln * n + dlt1 * t1 + dlt2 * t2;
     const float3 tau = dlt1 * t2 - dlt2 * t1;
     {
         const float s = rhoB * iib;
-        atomicAdd(&sb.acc4[2 * b], make_float4(imb * P.x, imb * P.y, imb * P.z, s * tau.x));
-        atomicAdd(reinterpret_cast<float2*>(&sb.acc4[2 * b + 1]), make_float2(s * tau.y, s * tau.z));
+        atomicAdd(&acc[2 * b], make_float4(imb * P.x, imb * P.y, imb * P.z, 0.f));
+        atomicAdd(&acc[2 * b + 1], make_float4(s * tau.x, s * tau.y, s * tau.z, 0.f));
     }
     if (a >= 0) {
         const float s = -rhoA * iia;
-        atomicAdd(&sb.acc4[2 * a], make_float4(-ima * P.x, -ima * P.y, -ima * P.z, s * tau.x));
-        atomicAdd(reinterpret_cast<float2*>(&sb.acc4[2 * a + 1]), make_float2(s * tau.y, s * tau.z));
+        atomicAdd(&acc[2 * a], make_float4(-ima * P.x, -ima * P.y, -ima * P.z, 0.f));
+        atomicAdd(&acc[2 * a + 1], make_float4(s * tau.x, s * tau.y, s * tau.z, 0.f));
     }
 }
 
@@ -454,19 +457,46 @@ __global__ void k_s_apply_warm(SplitBuf sb, int gen) {
             ima = sb.vel4[2 * a].w;
             iia = sb.vel4[2 * a + 1].w;
         }
-        scatter(sb, a, b, n, t1, t2, r1.x, r1.y, l.x, l.y, l.z, imb, iib, ima, iia);
+        scatter(sb.acc[0], a, b, n, t1, t2, r1.x, r1.y, l.x, l.y, l.z, imb, iib, ima, iia);
     }
 }
 
-// One sweep over the contacts. The sweep is latency-bound (a dependent chain: contact record ->
-// body gathers -> atomics), so every thread takes UNROLL contacts and issues all their record
-// loads, then all their body gathers, before computing; read-only data goes through the
-// non-coherent path. The grid is sized to the resident capacity and strides over the contacts.
+// One projected Jacobi sweep, one kernel. PJ keeps x_k = x_free + M^-1 W^T lambda_k
+// (projected_jacobi.cpp:361-363, 134-137), so three rotating velocity buffers replace the body
+// pass: the sweep reads the body velocities x_k from A_k, computes lambda_{k+1} for every contact
+// and adds the full M^-1 W^T lambda_{k+1} into A_{k+1} (float4 vector atomics), which holds x_free;
+// A_{k+2}, untouched by this sweep, is reset to x_free for the next one. There is no separate body pass and no FP32 accumulation across
+// sweeps. The sweep is latency-bound (contact record -> body gathers -> atomics): each thread takes
+// UNROLL contacts and issues all record loads, then all gathers, before computing; read-only data
+// goes through the non-coherent path; the grid is a whole number of resident waves. The last block
+// to finish (completion counter, no waiting) reduces the per-block maxima and runs the stop rule.
 __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
 
+// stop rule after a sweep: iteration cap, complementarity residual of the iterate entering the
+// sweep (max_c ||dlambda_c|| / max |lambda|), or a non-finite value
+__device__ __forceinline__ void sweep_check(SplitScalars* ss, float maxd, float maxl, int max_iter, float tol,
+                                            cudaGraphConditionalHandle handle, int use_handle) {
+    if (!ss->done) {
+        const float r = maxd / fmaxf(maxl, 1e-30f);
+        ss->res_last = r;
+        ss->iters += 1;
+        if (ss->iters >= max_iter || (tol > 0.f && r <= tol) || !(r == r)) ss->done = 1;
+    }
+    if (use_handle) cudaGraphSetConditional(handle, ss->done ? 0u : 1u);
+}
+
 template <int UNROLL, int NTH, int MINB>
-__global__ void __launch_bounds__(NTH, MINB) k_s_contact_t(SplitBuf sb, int gen, float alpha) {
-    if (*(volatile int32_t*)&sb.ss->done) return;
+__global__ void __launch_bounds__(NTH, MINB) k_s_sweep_t(SplitBuf sb, int gen, float alpha, int max_iter, float tol,
+                                                         cudaGraphConditionalHandle handle, int use_handle) {
+    if (*(volatile int32_t*)&sb.ss->done) {
+        // the loop is over: make sure the while node sees it even if no check runs this time
+        if (use_handle && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(handle, 0u);
+        return;
+    }
+    const int k = sb.ss->iters;
+    const float4* __restrict__ Acur = sb.acc[k % 3];
+    float4* Anxt = sb.acc[(k + 1) % 3];
+    float4* Aclr = sb.acc[(k + 2) % 3];
     const int nc = *sb.nc_dev;
     float maxd = 0.f, maxl = 0.f;
     const int T = gridDim.x * blockDim.x;
@@ -489,11 +519,11 @@ __global__ void __launch_bounds__(NTH, MINB) k_s_contact_t(SplitBuf sb, int gen,
         for (int u = 0; u < UNROLL; ++u) {
             if (!ok[u]) continue;
             const int a = __float_as_int(r1[u].z), b = __float_as_int(r1[u].w);
-            vb[u] = ldg4(&sb.vel4[2 * b]);
-            wb[u] = ldg4(&sb.vel4[2 * b + 1]);
+            vb[u] = ldg4(&Acur[2 * b]);
+            wb[u] = ldg4(&Acur[2 * b + 1]);
             if (a >= 0) {
-                va[u] = ldg4(&sb.vel4[2 * a]);
-                wa[u] = ldg4(&sb.vel4[2 * a + 1]);
+                va[u] = ldg4(&Acur[2 * a]);
+                wa[u] = ldg4(&Acur[2 * a + 1]);
             } else {
                 va[u] = make_float4(0.f, 0.f, 0.f, 0.f);
                 wa[u] = va[u];
@@ -536,80 +566,33 @@ __global__ void __launch_bounds__(NTH, MINB) k_s_contact_t(SplitBuf sb, int gen,
             lamp[c] = make_float4(ln, lt1, lt2, 0.f);
             maxd = fmaxf(maxd, sqrtf(dln * dln + dlt1 * dlt1 + dlt2 * dlt2));
             maxl = fmaxf(maxl, fmaxf(fabsf(l[u].x), fmaxf(fabsf(l[u].y), fabsf(l[u].z))));
-            if (dln != 0.f || dlt1 != 0.f || dlt2 != 0.f)
-                scatter(sb, __float_as_int(r1[u].z), __float_as_int(r1[u].w), n, t1, t2, rA, rB, dln, dlt1, dlt2,
-                        vb[u].w, wb[u].w, va[u].w, wa[u].w);
+            if (ln != 0.f || lt1 != 0.f || lt2 != 0.f)
+                scatter(Anxt, __float_as_int(r1[u].z), __float_as_int(r1[u].w), n, t1, t2, rA, rB, ln, lt1, lt2, vb[u].w,
+                        wb[u].w, va[u].w, wa[u].w);
         }
+    }
+    // reset the accumulator of the sweep after next to the free velocities
+    const int N = sb.N;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += T) {
+        const float4 v0 = ldg4(&sb.vel4[2 * i]), w0 = ldg4(&sb.vel4[2 * i + 1]);
+        Aclr[2 * i] = v0;
+        Aclr[2 * i + 1] = w0;
     }
     block_max2(maxd, maxl);
-    if (threadIdx.x == 0) sb.part[blockIdx.x] = make_float2(maxd, maxl);
-}
-
-// stop rule after a sweep: iteration cap, complementarity residual of the iterate entering the
-// sweep (max_c ||dlambda_c|| / max |lambda|), or a non-finite value
-__device__ __forceinline__ void sweep_check(SplitScalars* ss, float maxd, float maxl, int max_iter, float tol,
-                                            cudaGraphConditionalHandle handle, int use_handle) {
-    if (!ss->done) {
-        const float r = maxd / fmaxf(maxl, 1e-30f);
-        ss->res_last = r;
-        ss->iters += 1;
-        if (ss->iters >= max_iter || (tol > 0.f && r <= tol) || !(r == r)) ss->done = 1;
-    }
-    if (use_handle) cudaGraphSetConditional(handle, ss->done ? 0u : 1u);
-}
-
-// v += M^-1 W^T dlambda for every body; the last block to finish reduces the contact sweep's
-// per-block maxima and runs the stop rule (a completion counter, no waiting), so a sweep is two
-// kernels. Two bodies per thread keep four 16-byte loads in flight per body pair.
-__global__ void __launch_bounds__(256) k_s_body(SplitBuf sb, int N, int apply_only, int max_iter, float tol,
-                                                int nparts, cudaGraphConditionalHandle handle, int use_handle) {
-    if (!apply_only && *(volatile int32_t*)&sb.ss->done) {
-        // the loop is over: make sure the while node sees it even if no check runs this time
-        if (use_handle && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(handle, 0u);
-        return;
-    }
-    const int T = gridDim.x * blockDim.x;
-    for (int i0 = blockIdx.x * blockDim.x + threadIdx.x; i0 < N; i0 += 2 * T) {
-        const int i1 = i0 + T;
-        float4 a0 = sb.acc4[2 * i0], a1 = sb.acc4[2 * i0 + 1];
-        float4 v = sb.vel4[2 * i0], w = sb.vel4[2 * i0 + 1];
-        float4 b0, b1, u, z;
-        const bool two = i1 < N;
-        if (two) {
-            b0 = sb.acc4[2 * i1];
-            b1 = sb.acc4[2 * i1 + 1];
-            u = sb.vel4[2 * i1];
-            z = sb.vel4[2 * i1 + 1];
-        }
-        v.x += a0.x; v.y += a0.y; v.z += a0.z;
-        w.x += a0.w; w.y += a1.x; w.z += a1.y;
-        sb.vel4[2 * i0] = v;
-        sb.vel4[2 * i0 + 1] = w;
-        sb.acc4[2 * i0] = make_float4(0.f, 0.f, 0.f, 0.f);
-        sb.acc4[2 * i0 + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (two) {
-            u.x += b0.x; u.y += b0.y; u.z += b0.z;
-            z.x += b0.w; z.y += b1.x; z.z += b1.y;
-            sb.vel4[2 * i1] = u;
-            sb.vel4[2 * i1 + 1] = z;
-            sb.acc4[2 * i1] = make_float4(0.f, 0.f, 0.f, 0.f);
-            sb.acc4[2 * i1 + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-    }
-    if (apply_only) return;
     __shared__ bool last;
-    __syncthreads();
     if (threadIdx.x == 0) {
+        sb.part[blockIdx.x] = make_float2(maxd, maxl);
         __threadfence();
         last = atomicAdd(&sb.ss->blocks_done, 1u) == gridDim.x - 1;
     }
     __syncthreads();
     if (!last) return;
+    __threadfence();
     float md = 0.f, ml = 0.f;
-    for (int p = threadIdx.x; p < nparts; p += blockDim.x) {
-        const float2 q = sb.part[p];
-        md = fmaxf(md, q.x);
-        ml = fmaxf(ml, q.y);
+    for (int p = threadIdx.x; p < (int)gridDim.x; p += blockDim.x) {
+        const volatile float* q = reinterpret_cast<volatile float*>(&sb.part[p]);
+        md = fmaxf(md, q[0]);
+        ml = fmaxf(ml, q[1]);
     }
     block_max2(md, ml);
     if (threadIdx.x == 0) {
@@ -623,6 +606,7 @@ __global__ void k_s_reset(SplitBuf sb) {
     ss->done = (*sb.nc_dev == 0) ? 1 : 0;
     ss->iters = 0;
     ss->blocks_done = 0u;
+    (void)0;
     ss->maxd = 0u;
     ss->maxl = 0u;
     ss->res_last = 0.f;
@@ -694,18 +678,21 @@ __device__ __forceinline__ void frame64(const double* n, double* t1, double* t2)
     f64::cross3(n, t1, t2);
 }
 
-// Final FP64 velocities (world frame): the FP64 free velocity plus the velocity increment the FP32
-// sweeps accumulated, v = v_free + (v32 - (float)v_free); the FP32 part only carries M^-1 W^T lambda.
+// Final FP64 velocities (world frame): v = v_free + M^-1 W^T lambda, the FP64 free velocity plus
+// the impulse part of the last sweep's FP32 velocities (their difference to the FP32 free velocity,
+// taken exactly in FP64).
 __global__ void k_s_final_body(Scene sc, SplitBuf sb) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= sc.N) return;
     const int N = sc.N;
-    const float4 v = sb.vel4[2 * i], w = sb.vel4[2 * i + 1];
-    const float vf[6] = {v.x, v.y, v.z, w.x, w.y, w.z};
+    const float4* A = sb.acc[sb.ss->iters % 3];
+    const float4 a0 = A[2 * i], a1 = A[2 * i + 1];
+    const float4 f0 = sb.vel4[2 * i], f1 = sb.vel4[2 * i + 1];
+    const double d[6] = {(double)a0.x - (double)f0.x, (double)a0.y - (double)f0.y, (double)a0.z - (double)f0.z,
+                         (double)a1.x - (double)f1.x, (double)a1.y - (double)f1.y, (double)a1.z - (double)f1.z};
     for (int k = 0; k < 6; ++k) {
         const size_t j = (size_t)k * N + i;
-        const double base = sb.vfree[j];
-        sb.acc64[j] = base + (double)(vf[k] - (float)base);
+        sb.acc64[j] = sb.vfree[j] + d[k];
     }
 }
 
@@ -899,16 +886,16 @@ int split_grid_blocks(int64_t n, int sms) {
 // Launch shapes of the contact sweep the autotuner chooses between: contacts per thread, threads
 // per block and the register budget (minimum resident blocks per SM).
 struct ContactVariant {
-    void (*kernel)(SplitBuf, int, float);
+    void (*kernel)(SplitBuf, int, float, int, float, cudaGraphConditionalHandle, int);
     int unroll, nth, minb;
     int per_sm;
 };
 static ContactVariant g_variants[] = {
-    {k_s_contact_t<1, 256, 4>, 1, 256, 4, 0},
-    {k_s_contact_t<1, 256, 5>, 1, 256, 5, 0},
-    {k_s_contact_t<2, 256, 2>, 2, 256, 2, 0},
-    {k_s_contact_t<1, 128, 8>, 1, 128, 8, 0},
-    {k_s_contact_t<2, 128, 4>, 2, 128, 4, 0},
+    {k_s_sweep_t<1, 256, 4>, 1, 256, 4, 0},
+    {k_s_sweep_t<1, 256, 5>, 1, 256, 5, 0},
+    {k_s_sweep_t<2, 256, 2>, 2, 256, 2, 0},
+    {k_s_sweep_t<1, 128, 8>, 1, 128, 8, 0},
+    {k_s_sweep_t<2, 128, 4>, 2, 128, 4, 0},
 };
 constexpr int N_VARIANTS = sizeof(g_variants) / sizeof(g_variants[0]);
 
@@ -969,20 +956,10 @@ void launch_s_reset(const SplitBuf& sb, cudaStream_t s) { k_s_reset<<<1, 1, 0, s
 void launch_s_apply_warm(const SplitBuf& sb, int gen, int blocks, cudaStream_t s) {
     k_s_apply_warm<<<blocks, NT, 0, s>>>(sb, gen);
 }
-void launch_s_contact(const SplitBuf& sb, int gen, float alpha, int variant, int blocks, cudaStream_t s) {
+void launch_s_sweep(const SplitBuf& sb, int gen, float alpha, int variant, int blocks, int max_iter, float tol,
+                    cudaGraphConditionalHandle h, int use_handle, cudaStream_t s) {
     const ContactVariant& cv = g_variants[variant / 2];
-    cv.kernel<<<blocks, cv.nth, 0, s>>>(sb, gen, alpha);
-}
-void launch_s_body(const SplitBuf& sb, int N, int blocks, int apply_only, int max_iter, float tol, int nparts,
-                   cudaGraphConditionalHandle h, int use_handle, cudaStream_t s) {
-    k_s_body<<<blocks, NT, 0, s>>>(sb, N, apply_only, max_iter, tol, nparts, h, use_handle);
-}
-
-// body-pass grid: two resident waves' worth of blocks at most (each thread takes two bodies)
-int split_body_blocks(int64_t n, int sms) {
-    const int64_t want = (n + 2 * (int64_t)NT - 1) / (2 * (int64_t)NT);
-    const int64_t cap = (int64_t)sms * 4;
-    return (int)(want < 1 ? 1 : (want < cap ? want : cap));
+    cv.kernel<<<blocks, cv.nth, 0, s>>>(sb, gen, alpha, max_iter, tol, h, use_handle);
 }
 void launch_s_drift(const Scene& sc, double h, cudaStream_t s) {
     if (sc.N + sc.S > 0) k_s_drift<<<nblk(sc.N + sc.S), NT, 0, s>>>(sc, h);

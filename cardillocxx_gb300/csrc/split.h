@@ -50,8 +50,8 @@ struct SplitBuf {
     int N = 0;
     int64_t cap = 0;
     float4* pos4 = nullptr;   // N: position relative to the scene origin, radius
-    float4* vel4 = nullptr;   // 2N: (v, 1/m), (omega_world, 1/I)
-    float4* acc4 = nullptr;   // 2N: M^-1 W^T dlambda accumulators
+    float4* vel4 = nullptr;   // 2N: free velocities (v_free, 1/m), (omega_free world, 1/I)
+    float4* acc[3] = {nullptr, nullptr, nullptr};  // 2N each: M^-1 W^T lambda of a sweep (rotating)
     float4* vn4 = nullptr;    // 2N: pre-solve velocities (v, omega_world)
     double* vfree = nullptr;  // 6N FP64 free velocities (world frame)
     double* acc64 = nullptr;  // 6N FP64 W^T lambda, then final velocities
@@ -90,10 +90,10 @@ void launch_s_pair_write(const Scene& sc, const Grid& g, const SplitBuf& sb, con
                          int gen, const SplitParams& P, DevScalars* ds, cudaStream_t s);
 void launch_s_reset(const SplitBuf& sb, cudaStream_t s);
 void launch_s_apply_warm(const SplitBuf& sb, int gen, int blocks, cudaStream_t s);
-void launch_s_contact(const SplitBuf& sb, int gen, float alpha, int variant, int blocks, cudaStream_t s);
-void launch_s_body(const SplitBuf& sb, int N, int blocks, int apply_only, int max_iter, float tol, int nparts,
-                   cudaGraphConditionalHandle h, int use_handle, cudaStream_t s);
-int split_body_blocks(int64_t n, int sms);
+// one projected Jacobi sweep (one kernel): reads A_k, scatters M^-1 W^T lambda_{k+1} into A_{k+1},
+// clears A_{k+2}; its last block runs the stop rule
+void launch_s_sweep(const SplitBuf& sb, int gen, float alpha, int variant, int blocks, int max_iter, float tol,
+                    cudaGraphConditionalHandle h, int use_handle, cudaStream_t s);
 void launch_s_drift(const Scene& sc, double h, cudaStream_t s);
 void launch_s_final(const Scene& sc, const SplitBuf& sb, int gen, double alpha, int friction_enable, int combine,
                     int blocks, cudaStream_t s);
