@@ -143,6 +143,9 @@ SIGNATURES = [
     ("cdx_pj_solve_csr", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, _PI, _PI, _P, _P, _P, _P, _P, _P,
                                    _P, _P, _P, C.c_double, C.c_double, C.c_int32, C.c_double, C.c_double, _P, _P,
                                    _PI]),
+    ("cdx_pj_solve_csr_noalloc", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, _PI, _PI, _P, _P, _P, _P,
+                                           _P, _P, _P, _P, _P, C.c_double, C.c_double, C.c_int32, C.c_double,
+                                           C.c_double, _P, _P, _PI, C.c_char_p, C.c_int32]),
     ("cdx_gen_create", C.c_int, [C.POINTER(CdxGenParams), C.POINTER(C.c_void_p)]),
     ("cdx_gen_view", C.c_int, [C.c_void_p, C.POINTER(CdxScene)]),
     ("cdx_gen_destroy", None, [C.c_void_p]),

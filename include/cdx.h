@@ -169,6 +169,25 @@ int cdx_pj_solve_csr(cdx_ctx* ctx, int32_t nrows, int32_t nv, int32_t nfl, const
                      const double* f_ext, const double* f_gyro, double dt, double alpha, int32_t max_iter,
                      double tol_abs, double tol_rel, double* lambda_inout, double* x_out, int32_t* iterations);
 
+/* ---- solver-level solve for callers that cannot allocate device memory ----
+ * No counterpart in the reference. Same inputs, outputs and results as cdx_pj_solve_csr, but no
+ * context and no cudaMalloc/cudaFree or other allocating call: every device buffer (staged inputs,
+ * work arrays, results) lives in one file-scope __device__ array of CDX_NOALLOC_SCRATCH_BYTES that
+ * each GPU loading the library keeps until exit. For hosts that own all device memory themselves
+ * (pre-reserved pools, real-time loops, code where allocation calls are not allowed).
+ *   - stream: cudaStream_t as void* (NULL = the legacy default stream).
+ *   - The first call on a device (with that device current) looks up the array's address with
+ *     cudaGetSymbolAddress; make it before any stream capture.
+ *   - Problems that do not fit return CDX_ERR_OVERFLOW with the message in err (errlen bytes).
+ *   - All calls share the array: calls that overlap on the GPU race; run them one at a time. */
+#define CDX_NOALLOC_SCRATCH_BYTES (16u << 20)
+int cdx_pj_solve_csr_noalloc(void* stream, int32_t nrows, int32_t nv, int32_t nfl, const int32_t* row_ptr,
+                             const int32_t* col, const double* val, const double* contact_bias, const double* mu,
+                             const double* restitution, const double* minv, const double* mdiag, const double* v,
+                             const double* f_ext, const double* f_gyro, double dt, double alpha, int32_t max_iter,
+                             double tol_abs, double tol_rel, double* lambda_inout, double* x_out, int32_t* iterations,
+                             char* err, int32_t errlen);
+
 /* ---- diagnostics: the FP64 Newton-Raphson reciprocal and reciprocal square root of the split
  * form's final pass, evaluated on the device for host-side checks against IEEE results ---- */
 int cdx_selftest_nr64(cdx_ctx* ctx, int32_t n, const double* x, double* rcp, double* rsqrt);
