@@ -54,6 +54,8 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-graph", action="store_true", help="launch the sweep kernels one by one (profiling)")
+    p.add_argument("--sweep-variant", default=None,
+                   help="pin the split-form solver shape (index or name; default: autotuned)")
     p.add_argument("--save-state", default=None, help="write the settled state (npz) and continue")
     p.add_argument("--load-state", default=None, help="start from a settled state written by --save-state")
     return p.parse_args()
@@ -207,6 +209,11 @@ def run_cdx(a, log):
     sscene = with_state(scene, state)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     run_cfg = dict(cfg, **{"gpu.precision": a.precision, "gpu.graph": not a.no_graph})
+    if a.sweep_variant is not None:
+        from cardillocxx_gb300 import PhysicsEngine
+        names = PhysicsEngine.split_variants()
+        v = a.sweep_variant
+        run_cfg["gpu.sweep_variant"] = names.index(v) if v in names else int(v)
     if world > 1:
         torch.distributed.barrier()
     clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
@@ -224,17 +231,28 @@ def run_cdx(a, log):
     log(f"{a.precision}: {ms_step:.3f} ms/step, contacts {contacts[-1]}, iters {iters[-1]}, residual {res[-1]:.2e}")
 
     # dominant kernel: the contact sweep, timed per launch with CUDA events on the engine stream
-    tsw = eng.time_sweeps(30)
+    tsw = eng.time_sweeps(60)
     achieved = tsw["bytes_contact"] / (tsw["ms_contact"] * 1e-3) / 1e9 if tsw["ms_contact"] > 0 else None
+    # the dominant kernel: the cooperative whole solve (timed per sweep inside one launch) or the
+    # streaming sweep kernel (one launch per sweep), whichever shape the autotuner chose
+    from cardillocxx_gb300 import PhysicsEngine
+    names = PhysicsEngine.split_variants()
+    cv = est.get("contact_variant", -1)
+    vname = names[cv] if a.precision == "split" and 0 <= cv < len(names) else None
+    if a.precision != "split":
+        kernel, per, units = "k_sweep_contact64", "contact", contacts[-1]
+    elif vname and vname.startswith("coop"):
+        kernel, per, units = "k_s_solve_coop", "body", N
+    else:
+        kernel, per, units = "k_s_sweep_t", "contact", contacts[-1]
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath):
         with open(tpath) as f:
             tj = json.load(f)
-        key = "split_contact_bytes_per_contact" if a.precision == "split" else "fp64_contact_bytes_per_contact"
-        if key in tj:
-            traffic = tj[key] * contacts[-1]
-    roofline = {"kernel": "k_s_contact" if a.precision == "split" else "k_sweep_contact64", "bound": "hbm",
+        if kernel in tj and tj[kernel].get("per") == per:
+            traffic = tj[kernel]["dram_bytes_per_sweep_per_unit"] * units
+    roofline = {"kernel": kernel, "variant": vname, "bound": "hbm", "launch": "one projected Jacobi sweep",
                 "achieved": achieved, "peak": hbm, "peak_kind": f"{peak_kind} hbm_gbs", "unit": "GB/s",
                 "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
                 "bytes_per_launch": tsw["bytes_contact"], "ms_per_launch": tsw["ms_contact"],

@@ -57,6 +57,7 @@ class CdxConfig(C.Structure):
         ("gpu_contact_capacity_factor", C.c_double),
         ("gpu_use_graph", C.c_int32),
         ("gpu_autotune", C.c_int32),
+        ("gpu_sweep_variant", C.c_int32),
     ]
 
 
@@ -140,6 +141,8 @@ SIGNATURES = [
     ("cdx_stream", C.c_void_p, [C.c_void_p]),
     ("cdx_time_sweeps", C.c_int, [C.c_void_p, C.c_int32, _P, _P, _P, _P]),
     ("cdx_selftest_nr64", C.c_int, [C.c_void_p, C.c_int32, _P, _P, _P]),
+    ("cdx_split_variant_count", C.c_int32, []),
+    ("cdx_split_variant_name", C.c_char_p, [C.c_int32]),
     ("cdx_pj_solve_csr", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, _PI, _PI, _P, _P, _P, _P, _P, _P,
                                    _P, _P, _P, C.c_double, C.c_double, C.c_int32, C.c_double, C.c_double, _P, _P,
                                    _PI]),

@@ -5,6 +5,7 @@
 
 #include "../../include/cdx.h"
 #include "engine.h"
+#include "split.h"
 
 extern "C" {
 
@@ -100,5 +101,8 @@ int cdx_time_sweeps(cdx_ctx* ctx, int32_t n, double* ms_contact, double* ms_body
     if (!ctx) return CDX_ERR_ARG;
     return ctx->eng.time_sweeps(n, ms_contact, ms_body, bytes_contact, bytes_body);
 }
+
+int32_t cdx_split_variant_count(void) { return cdx::split_num_variants(); }
+const char* cdx_split_variant_name(int32_t k) { return cdx::split_variant_name(k); }
 
 }  // extern "C"

@@ -104,6 +104,7 @@ static int split_contacts(Engine& E, int64_t need) {
 static int init_split(Engine& E) {
     E.split = new SplitState();
     SplitState* S = E.split;
+    if (E.cfg.gpu_sweep_variant >= 0) S->variant = std::min(E.cfg.gpu_sweep_variant, split_num_variants() - 1);
     SplitBuf& b = S->sb;
     const int N = E.sc.N, Ss = E.sc.S, nsc = E.sc.nscenes;
     b.N = N;
@@ -127,6 +128,7 @@ static int init_split(Engine& E) {
     if ((st = salloc(E, (void**)&b.nc_dev, sizeof(int32_t), "split"))) return st;
     if ((st = salloc(E, (void**)&b.ss, sizeof(SplitScalars), "split"))) return st;
     if ((st = salloc(E, (void**)&b.part, sizeof(float2) * SPLIT_MAX_PARTS, "split"))) return st;
+    if ((st = salloc(E, (void**)&b.recs, sizeof(float2) * 2 * SPLIT_MAX_PARTS, "split"))) return st;
     if ((st = E.cuda_check(cudaMallocHost((void**)&S->h_nc, sizeof(int32_t)), "pinned"))) return st;
     if ((st = E.cuda_check(cudaMallocHost((void**)&S->h_ss, sizeof(SplitScalars)), "pinned"))) return st;
     cudaMemsetAsync(b.ss, 0, sizeof(SplitScalars), E.stream);
@@ -178,7 +180,7 @@ static int build_graph(Engine& E, int g) {
     cudaGraph_t body = p.conditional.phGraph_out[0];
     if ((st = E.cuda_check(cudaStreamBeginCaptureToGraph(E.stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed),
                            "capture"))) return st;
-    launch_s_sweep(S->sb, g, (float)E.cfg.pj_alpha, S->variant, S->graph_blocks, maxit, tol, h, 1, E.stream);
+    launch_s_sweep(S->sb, g, (float)E.cfg.pj_alpha, S->graph_variant, S->graph_blocks, maxit, tol, h, 1, E.stream);
     cudaGraph_t captured = nullptr;
     if ((st = E.cuda_check(cudaStreamEndCapture(E.stream, &captured), "end capture"))) return st;
     if ((st = E.cuda_check(cudaGraphInstantiate(&S->exec[g], graph, 0), "graph instantiate"))) return st;
@@ -250,59 +252,94 @@ int Engine::step_split() {
     if (timing) cudaEventRecord(ev[1], stream);
     // x0 = v_free + M^-1 W^T lambda_warm
     const int cblocks = split_grid_blocks(std::max(S->nc, 1), S->sms);
-    const int sblocks = split_contact_blocks(S->variant, std::max(S->nc, 1), S->sms);
     launch_s_reset(sb, stream);
     launch_s_apply_warm(sb, gen, cblocks, stream);
     launches += 2;
     if (timing) cudaEventRecord(ev[2], stream);
     const int maxit = std::max(1, cfg.pj_max_iterations);
     bool solved = false;
-    if (S->nc > 0 && cfg.gpu_autotune && S->nc >= 4096 && (double)S->nc >= 1.5 * (double)S->tuned_at &&
-        maxit > 2 * split_num_variants()) {
-        // autotune: the first sweeps of this step run once with every launch shape; each is a full
-        // sweep of the same math, so the step's result does not depend on which shape ran them
+    const int nv = split_num_variants();
+    // sweeps the autotuner spends: two per streaming shape, eight per feasible cooperative one
+    int tune_sweeps = 0;
+    for (int v = 0; v < nv; ++v) tune_sweeps += split_variant_is_coop(v) ? 8 : 2;
+    if (S->nc > 0 && cfg.gpu_autotune && cfg.gpu_sweep_variant < 0 && S->nc >= 4096 &&
+        (double)S->nc >= 1.5 * (double)S->tuned_at && maxit > 2 * tune_sweeps) {
+        // autotune: the first sweeps of this step run with every shape; each is a full sweep of
+        // the same math, so the step's result does not depend on which shape ran them
         if (!S->tev[0]) {
             cudaEventCreate(&S->tev[0]);
             cudaEventCreate(&S->tev[1]);
         }
-        const int nv = split_num_variants();
         double best_t = 1e300;
         int best = S->variant;
         cudaGraphConditionalHandle none = 0;
-        for (int v = 0; v < nv; ++v) {
+        for (int v = 0; v < nv && !solved; ++v) {
             double t = 0;
-            for (int r = 0; r < 2; ++r) {
-                const int vb = split_contact_blocks(v, S->nc, S->sms);
-                cudaEventRecord(S->tev[0], stream);
-                launch_s_sweep(sb, gen, (float)cfg.pj_alpha, v, vb, maxit, (float)cfg.gpu_residual_tol, none, 0, stream);
-                cudaEventRecord(S->tev[1], stream);
-                if ((st = cuda_check(cudaEventSynchronize(S->tev[1]), "autotune"))) return st;
-                float ms1 = 0;
-                cudaEventElapsedTime(&ms1, S->tev[0], S->tev[1]);
-                t += ms1;
+            if (split_variant_is_coop(v)) {
+                // two launches of 2 and 6 sweeps: their difference is the cost of a sweep, the rest
+                // (loading and storing the contacts) is paid once per solve of maxit sweeps
+                CoopPlan plan;
+                if (!split_coop_plan(v, S->nc, sc.N, S->sms, &plan)) continue;
+                float ms[2] = {0.f, 0.f};
+                const int ks[2] = {2, 6};
+                for (int r = 0; r < 2; ++r) {
+                    cudaEventRecord(S->tev[0], stream);
+                    st = launch_s_solve_coop(sb, gen, (float)cfg.pj_alpha, v, plan, maxit, (float)cfg.gpu_residual_tol,
+                                             ks[r], stream);
+                    if ((st = cuda_check((cudaError_t)st, "cooperative launch"))) return st;
+                    cudaEventRecord(S->tev[1], stream);
+                    if ((st = cuda_check(cudaEventSynchronize(S->tev[1]), "autotune"))) return st;
+                    cudaEventElapsedTime(&ms[r], S->tev[0], S->tev[1]);
+                    ++launches;
+                }
+                const double per = std::max(0.0, (double)(ms[1] - ms[0]) / (ks[1] - ks[0]));
+                const double fixed = std::max(0.0, (double)ms[0] - ks[0] * per);
+                t = 2.0 * (per + fixed / maxit);
+            } else {
+                for (int r = 0; r < 2; ++r) {
+                    const int vb = split_contact_blocks(v, S->nc, S->sms);
+                    cudaEventRecord(S->tev[0], stream);
+                    launch_s_sweep(sb, gen, (float)cfg.pj_alpha, v, vb, maxit, (float)cfg.gpu_residual_tol, none, 0,
+                                   stream);
+                    cudaEventRecord(S->tev[1], stream);
+                    if ((st = cuda_check(cudaEventSynchronize(S->tev[1]), "autotune"))) return st;
+                    float ms1 = 0;
+                    cudaEventElapsedTime(&ms1, S->tev[0], S->tev[1]);
+                    t += ms1;
+                }
+                launches += 2;
             }
-            launches += 2;
             if (t < best_t) {
                 best_t = t;
                 best = v;
             }
+            cudaMemcpyAsync(&S->h_ss->done, &sb.ss->done, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+            if ((st = cuda_check(cudaStreamSynchronize(stream), "autotune"))) return st;
+            solved = S->h_ss->done != 0;
         }
         S->variant = best;
         S->tuned_at = S->nc;
         ++S->tune_runs;
-        cudaMemcpyAsync(&S->h_ss->done, &sb.ss->done, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
-        if ((st = cuda_check(cudaStreamSynchronize(stream), "autotune"))) return st;
-        solved = S->h_ss->done != 0;
     }
-    if (S->nc > 0 && !solved) {
+    CoopPlan plan;
+    const bool coop = S->nc > 0 && split_variant_is_coop(S->variant) &&
+                      split_coop_plan(S->variant, S->nc, sc.N, S->sms, &plan);
+    if (S->nc > 0 && !solved && coop) {
+        st = launch_s_solve_coop(sb, gen, (float)cfg.pj_alpha, S->variant, plan, maxit, (float)cfg.gpu_residual_tol,
+                                 maxit, stream);
+        if ((st = cuda_check((cudaError_t)st, "cooperative launch"))) return st;
+        ++launches;
+    } else if (S->nc > 0 && !solved) {
+        // streaming sweeps (a cooperative shape that does not fit this step runs as streaming shape 0)
+        const int sv = split_variant_is_coop(S->variant) ? 0 : S->variant;
+        const int sblocks = split_contact_blocks(sv, std::max(S->nc, 1), S->sms);
         if (cfg.gpu_use_graph) {
             // grid sized for the capacity so a graph serves every step until the buffers grow
-            const int gblocks = split_contact_blocks(S->variant, sb.cap, S->sms);
+            const int gblocks = split_contact_blocks(sv, sb.cap, S->sms);
             const float tol = (float)cfg.gpu_residual_tol;
-            if (S->graph_cap != sb.cap || S->graph_maxit != maxit || S->graph_tol != tol ||
-                S->graph_variant != S->variant) {
+            if (S->graph_cap != sb.cap || S->graph_maxit != maxit || S->graph_tol != tol || S->graph_variant != sv) {
                 destroy_graphs(S);
-                S->graph_variant = S->variant;
+                S->graph_variant = sv;
                 S->graph_blocks = gblocks;
                 if ((st = build_graph(*this, 0)) || (st = build_graph(*this, 1))) return st;
                 S->graph_cap = sb.cap;
@@ -319,8 +356,8 @@ int Engine::step_split() {
                     if ((st = cuda_check(cudaStreamSynchronize(stream), "poll"))) return st;
                     if (S->h_ss->done) break;
                 }
-                launch_s_sweep(sb, gen, (float)cfg.pj_alpha, S->variant, sblocks, maxit, (float)cfg.gpu_residual_tol, none,
-                               0, stream);
+                launch_s_sweep(sb, gen, (float)cfg.pj_alpha, sv, sblocks, maxit, (float)cfg.gpu_residual_tol, none, 0,
+                               stream);
             }
         }
     }
@@ -333,8 +370,9 @@ int Engine::step_split() {
     cudaMemcpyAsync(S->h_ss, sb.ss, sizeof(SplitScalars), cudaMemcpyDeviceToHost, stream);
     if ((st = cuda_check(cudaStreamSynchronize(stream), "split step"))) return st;
     if ((st = cuda_check(cudaGetLastError(), "split launch"))) return st;
+    if (S->h_ss->err) return fail(CDX_ERR_TIMEOUT, "cooperative solve: a grid barrier timed out");
     S->last_iters = S->nc > 0 ? S->h_ss->iters : 0;
-    launches += (int64_t)S->last_iters;
+    if (!coop) launches += (int64_t)S->last_iters;
     S->res_last = S->h_ss->res_last;
     S->res_final = S->nc > 0 ? S->h_ss->res_final : 0.0;
     S->prev_count = S->nc;
@@ -417,8 +455,26 @@ int Engine::time_sweeps(int n, double* msc, double* msb, double* bc, double* bb)
         const int cblocks = split_contact_blocks(S->variant, S->prev_count, S->sms);
         *S->h_nc = S->prev_count;
         cudaMemcpyAsync(S->sb.nc_dev, S->h_nc, sizeof(int32_t), cudaMemcpyHostToDevice, stream);
-        cudaMemsetAsync(S->sb.ss, 0, sizeof(SplitScalars), stream);
-        for (int k = 0; k < n; ++k) {
+        launch_s_reset(S->sb, stream);
+        CoopPlan plan;
+        if (split_variant_is_coop(S->variant) && split_coop_plan(S->variant, S->prev_count, sc.N, S->sms, &plan)) {
+            // one cooperative launch of n sweeps; reported per sweep
+            cudaEventRecord(e[0], stream);
+            st = launch_s_solve_coop(S->sb, g, (float)cfg.pj_alpha, S->variant, plan, 1 << 30, 0.f, n, stream);
+            cudaEventRecord(e[1], stream);
+            if (!(st = cuda_check((cudaError_t)st, "cooperative launch")) &&
+                !(st = cuda_check(cudaEventSynchronize(e[1]), "time sweeps"))) {
+                float a = 0;
+                cudaEventElapsedTime(&a, e[0], e[1]);
+                tc = a;
+            }
+            ++launches;
+            // one sweep, with the contact records and impulses on chip: per body the velocities read
+            // (24 B), the impulse sums added (24 B) and the accumulator reset (24 B)
+            if (bc) *bc = (double)sc.N * 72.0;
+            if (bb) *bb = 0.0;
+        } else {
+          for (int k = 0; k < n; ++k) {
             cudaEventRecord(e[0], stream);
             launch_s_sweep(S->sb, g, (float)cfg.pj_alpha, S->variant, cblocks, 1 << 30, 0.f, 0, 0, stream);
             cudaEventRecord(e[1], stream);
@@ -430,11 +486,12 @@ int Engine::time_sweeps(int n, double* msc, double* msb, double* bc, double* bb)
             tc += a;
             tb += b;
         }
-        launches += (int64_t)n;
-        // one sweep: per contact the two records (32) and lambda read + write (24); per body the
-        // accumulator cleared for the sweep after next (24)
-        if (bc) *bc = (double)S->prev_count * (16 + 16 + 24) + (double)sc.N * 24.0;
-        if (bb) *bb = 0.0;
+          launches += (int64_t)n;
+          // one sweep: per contact the two records (32) and lambda read + write (24); per body the
+          // accumulator cleared for the sweep after next (24)
+          if (bc) *bc = (double)S->prev_count * (16 + 16 + 24) + (double)sc.N * 24.0;
+          if (bb) *bb = 0.0;
+        }
     } else if (!sp && prev_count > 0) {
         const int g = gen ^ 1;
         cudaMemsetAsync(ds, 0, sizeof(DevScalars), stream);

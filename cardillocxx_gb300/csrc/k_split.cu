@@ -13,6 +13,8 @@
 // recomputed from the FP64 positions.
 #include <cuda_runtime.h>
 
+#include <cstdio>
+
 #include "cdx_internal.h"
 #include "fp64_math.cuh"
 #include "split.h"
@@ -473,11 +475,13 @@ __global__ void k_s_apply_warm(SplitBuf sb, int gen) {
 __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
 
 // stop rule after a sweep: iteration cap, complementarity residual of the iterate entering the
-// sweep (max_c ||dlambda_c|| / max |lambda|), or a non-finite value
-__device__ __forceinline__ void sweep_check(SplitScalars* ss, float maxd, float maxl, int max_iter, float tol,
+// sweep (max_c ||dlambda_c|| / max |lambda|; the sweep reduces squared norms, sqrt is monotone),
+// or a non-finite value
+__device__ __forceinline__ float sweep_residual(float maxd2, float maxl) { return sqrtf(maxd2) / fmaxf(maxl, 1e-30f); }
+__device__ __forceinline__ void sweep_check(SplitScalars* ss, float maxd2, float maxl, int max_iter, float tol,
                                             cudaGraphConditionalHandle handle, int use_handle) {
     if (!ss->done) {
-        const float r = maxd / fmaxf(maxl, 1e-30f);
+        const float r = sweep_residual(maxd2, maxl);
         ss->res_last = r;
         ss->iters += 1;
         if (ss->iters >= max_iter || (tol > 0.f && r <= tol) || !(r == r)) ss->done = 1;
@@ -485,7 +489,162 @@ __device__ __forceinline__ void sweep_check(SplitScalars* ss, float maxd, float 
     if (use_handle) cudaGraphSetConditional(handle, ss->done ? 0u : 1u);
 }
 
-template <int UNROLL, int NTH, int MINB>
+// float4 reduction without a return value (the sweep never reads what it adds)
+__device__ __forceinline__ void red4(float4* p, float x, float y, float z) {
+    asm volatile("red.relaxed.gpu.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(x), "f"(y), "f"(z),
+                 "f"(0.f)
+                 : "memory");
+}
+
+// Sums v over each run of equal keys among the lanes of a warp; the first lane of a run gets the
+// run's total. Pair contacts are stored grouped by their first body, so neighbouring lanes often
+// push to the same body: one reduction per run replaces a chain of same-address atomics.
+__device__ __forceinline__ bool warp_run_sum(int key, float (&v)[6]) {
+    const unsigned FULL = 0xffffffffu;
+    const unsigned lane = threadIdx.x & 31u;
+    const int pk = __shfl_up_sync(FULL, key, 1);
+    const bool head = lane == 0u || pk != key;
+    const unsigned heads = __ballot_sync(FULL, head);
+    if (heads != FULL) {
+        const unsigned above = heads & ~((2u << lane) - 1u);
+        const unsigned end = above ? (unsigned)(__ffs(above) - 1) : 32u;
+        for (unsigned off = 1; off < 32u; off <<= 1) {
+            const bool take = lane + off < end;
+            if (!__any_sync(FULL, take)) break;
+#pragma unroll
+            for (int q = 0; q < 6; ++q) {
+                const float t = __shfl_down_sync(FULL, v[q], off);
+                if (take) v[q] += t;
+            }
+        }
+    }
+    return head;
+}
+
+// Result of the projected Jacobi update of one contact.
+struct PJOut {
+    float4 lam;      // new impulse (normal, t1, t2, 0)
+    float3 pb, tb;   // M^-1 W^T lambda on body B: linear, angular (world frame)
+    float3 pa, ta;   // the same for body A (zero for a static)
+    float dn2, lm;   // ||lambda_new - lambda_old||^2, max |lambda_old|
+    bool push;       // lambda_new != 0
+};
+
+// R = alpha / Delassus diagonal (projected_jacobi.cpp:57-69) from the inverse masses and the
+// signed lever lengths: D_n = 1/m_A + 1/m_B, D_t = D_n + rho_A^2 / I_A + rho_B^2 / I_B
+__device__ __forceinline__ void pj_rdiag(float rA, float rB, float ima, float iia, float imb, float iib, float alpha,
+                                         float& Rn, float& Rt) {
+    const float Dn = ima + imb;
+    const float Dt = Dn + rA * rA * iia + rB * rB * iib;
+    Rn = alpha * __frcp_rn(Dn);
+    Rt = alpha * __frcp_rn(Dt);
+}
+
+// One contact of a sweep (projected_jacobi.cpp:121-138 with project :100-119): gamma = W x + b from
+// the accumulated velocities of both bodies, lambda <- Pi(lambda - R gamma), and the body shares of
+// M^-1 W^T lambda (the full impulse: the accumulator being filled starts at x_free).
+__device__ __forceinline__ void pj_core(float3 n, float3 t1, float3 t2, float rA, float rB, float muw, float4 l,
+                                        float4 va, float4 wa, float4 vb, float4 wb, const float4* bias_c, float Rn,
+                                        float Rt, PJOut& o) {
+    const float3 dv = f3(vb) - f3(va);
+    const float3 Om = rB * f3(wb) - rA * f3(wa);
+    float gn = dot(n, dv);
+    float gt1 = dot(t1, dv) + dot(t2, Om);
+    float gt2 = dot(t2, dv) - dot(t1, Om);
+    if (split_has_bias(muw)) {
+        const float4 bs = ldg4(bias_c);
+        gn += bs.x;
+        gt1 += bs.y;
+        gt2 += bs.z;
+    }
+    const float mu = fabsf(muw);
+    float ln = fmaxf(l.x - Rn * gn, 0.f);
+    float lt1 = l.y - Rt * gt1;
+    float lt2 = l.z - Rt * gt2;
+    const float tn2 = lt1 * lt1 + lt2 * lt2;
+    if (tn2 > 0.f) {
+        const float sc = fminf(1.f, mu * ln * rsqrtf(tn2));
+        lt1 *= sc;
+        lt2 *= sc;
+    }
+    const float dln = ln - l.x, dlt1 = lt1 - l.y, dlt2 = lt2 - l.z;
+    o.lam = make_float4(ln, lt1, lt2, 0.f);
+    o.dn2 = dln * dln + dlt1 * dlt1 + dlt2 * dlt2;
+    o.lm = fmaxf(fabsf(l.x), fmaxf(fabsf(l.y), fabsf(l.z)));
+    o.push = ln != 0.f || lt1 != 0.f || lt2 != 0.f;
+    // accumulator layout = velocity layout: (v.xyz, 1/m), (omega.xyz, 1/I); the .w lanes get +0
+    const float3 P = ln * n + lt1 * t1 + lt2 * t2;
+    const float3 tau = lt1 * t2 - lt2 * t1;
+    o.pb = vb.w * P;
+    o.tb = (rB * wb.w) * tau;
+    o.pa = (-va.w) * P;
+    o.ta = (-rA * wa.w) * tau;
+}
+
+// The same from the packed records alone: frame and R recomputed (the inverse masses ride in the
+// .w lanes of the gathered velocities)
+__device__ __forceinline__ void pj_contact(float4 r0, float4 r1, float4 l, float4 va, float4 wa, float4 vb, float4 wb,
+                                           const float4* bias_c, float alpha, PJOut& o) {
+    const float3 n = f3(r0);
+    float3 t1, t2;
+    frame32(n, t1, t2);
+    float Rn, Rt;
+    pj_rdiag(r1.x, r1.y, va.w, wa.w, vb.w, wb.w, alpha, Rn, Rt);
+    pj_core(n, t1, t2, r1.x, r1.y, r0.w, l, va, wa, vb, wb, bias_c, Rn, Rt, o);
+}
+
+// Adds a contact's shares into accumulator A. Every lane of the warp calls it (AGG 2 reduces across
+// the warp). AGG: 0 float4 atomicAdd, 1 float4 reductions (no return value), 2 reductions with
+// body A's share summed per run of equal body index. All three add the same terms; only the FP32
+// summation order differs.
+template <int AGG>
+__device__ __forceinline__ void pj_push(float4* A, bool ok, int a, int b, const PJOut& o) {
+    const bool go = ok && o.push;
+    if (AGG == 0) {
+        if (go) {
+            atomicAdd(&A[2 * b], make_float4(o.pb.x, o.pb.y, o.pb.z, 0.f));
+            atomicAdd(&A[2 * b + 1], make_float4(o.tb.x, o.tb.y, o.tb.z, 0.f));
+            if (a >= 0) {
+                atomicAdd(&A[2 * a], make_float4(o.pa.x, o.pa.y, o.pa.z, 0.f));
+                atomicAdd(&A[2 * a + 1], make_float4(o.ta.x, o.ta.y, o.ta.z, 0.f));
+            }
+        }
+    } else if (AGG == 1) {
+        if (go) {
+            red4(&A[2 * b], o.pb.x, o.pb.y, o.pb.z);
+            red4(&A[2 * b + 1], o.tb.x, o.tb.y, o.tb.z);
+            if (a >= 0) {
+                red4(&A[2 * a], o.pa.x, o.pa.y, o.pa.z);
+                red4(&A[2 * a + 1], o.ta.x, o.ta.y, o.ta.z);
+            }
+        }
+    } else {
+        if (go) {
+            red4(&A[2 * b], o.pb.x, o.pb.y, o.pb.z);
+            red4(&A[2 * b + 1], o.tb.x, o.tb.y, o.tb.z);
+        }
+        // lanes with nothing to add keep their key so a run stays contiguous; they add zeros
+        const int key = ok ? a : -1;
+        float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if (go && a >= 0) {
+            v[0] = o.pa.x;
+            v[1] = o.pa.y;
+            v[2] = o.pa.z;
+            v[3] = o.ta.x;
+            v[4] = o.ta.y;
+            v[5] = o.ta.z;
+        }
+        const bool head = warp_run_sum(key, v);
+        if (head && key >= 0 && (v[0] != 0.f || v[1] != 0.f || v[2] != 0.f || v[3] != 0.f || v[4] != 0.f || v[5] != 0.f)) {
+            red4(&A[2 * key], v[0], v[1], v[2]);
+            red4(&A[2 * key + 1], v[3], v[4], v[5]);
+        }
+    }
+}
+
+// One projected Jacobi sweep per launch (streaming form: contact records read from HBM/L2 every
+// sweep).
+template <int UNROLL, int NTH, int MINB, int AGG>
 __global__ void __launch_bounds__(NTH, MINB) k_s_sweep_t(SplitBuf sb, int gen, float alpha, int max_iter, float tol,
                                                          cudaGraphConditionalHandle handle, int use_handle) {
     if (*(volatile int32_t*)&sb.ss->done) {
@@ -501,7 +660,10 @@ __global__ void __launch_bounds__(NTH, MINB) k_s_sweep_t(SplitBuf sb, int gen, f
     float maxd = 0.f, maxl = 0.f;
     const int T = gridDim.x * blockDim.x;
     float4* __restrict__ lamp = sb.lam[gen];
-    for (int c0 = blockIdx.x * blockDim.x + threadIdx.x; c0 < nc; c0 += T * UNROLL) {
+    // the loop bound is the same for all lanes of a warp (the run reduction needs whole warps)
+    const int lane = threadIdx.x & 31;
+    for (int w0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31); w0 < nc; w0 += T * UNROLL) {
+        const int c0 = w0 + lane;
         float4 r0[UNROLL], r1[UNROLL], l[UNROLL];
         bool ok[UNROLL];
 #pragma unroll
@@ -531,44 +693,18 @@ __global__ void __launch_bounds__(NTH, MINB) k_s_sweep_t(SplitBuf sb, int gen, f
         }
 #pragma unroll
         for (int u = 0; u < UNROLL; ++u) {
-            if (!ok[u]) continue;
-            const int c = c0 + u * T;
-            const float3 n = f3(r0[u]);
-            float3 t1, t2;
-            frame32(n, t1, t2);
-            const float rA = r1[u].x, rB = r1[u].y;
-            const float3 dv = f3(vb[u]) - f3(va[u]);
-            const float3 Om = rB * f3(wb[u]) - rA * f3(wa[u]);
-            float gn = dot(n, dv);
-            float gt1 = dot(t1, dv) + dot(t2, Om);
-            float gt2 = dot(t2, dv) - dot(t1, Om);
-            if (split_has_bias(r0[u].w)) {
-                const float4 bs = ldg4(&sb.bias[c]);
-                gn += bs.x;
-                gt1 += bs.y;
-                gt2 += bs.z;
+            PJOut o = {};
+            int a = -1, b = 0;
+            if (ok[u]) {
+                const int c = c0 + u * T;
+                a = __float_as_int(r1[u].z);
+                b = __float_as_int(r1[u].w);
+                pj_contact(r0[u], r1[u], l[u], va[u], wa[u], vb[u], wb[u], &sb.bias[c], alpha, o);
+                lamp[c] = o.lam;
+                maxd = fmaxf(maxd, o.dn2);
+                maxl = fmaxf(maxl, o.lm);
             }
-            // R = alpha / Delassus diagonal, from the inverse masses carried in the .w lanes
-            const float Dn = va[u].w + vb[u].w;
-            const float Dt = Dn + rA * rA * wa[u].w + rB * rB * wb[u].w;
-            const float Rn = alpha * __frcp_rn(Dn), Rt = alpha * __frcp_rn(Dt);
-            const float mu = fabsf(r0[u].w);
-            float ln = fmaxf(l[u].x - Rn * gn, 0.f);
-            float lt1 = l[u].y - Rt * gt1;
-            float lt2 = l[u].z - Rt * gt2;
-            const float tn2 = lt1 * lt1 + lt2 * lt2;
-            if (tn2 > 0.f) {
-                const float sc = fminf(1.f, mu * ln * rsqrtf(tn2));
-                lt1 *= sc;
-                lt2 *= sc;
-            }
-            const float dln = ln - l[u].x, dlt1 = lt1 - l[u].y, dlt2 = lt2 - l[u].z;
-            lamp[c] = make_float4(ln, lt1, lt2, 0.f);
-            maxd = fmaxf(maxd, sqrtf(dln * dln + dlt1 * dlt1 + dlt2 * dlt2));
-            maxl = fmaxf(maxl, fmaxf(fabsf(l[u].x), fmaxf(fabsf(l[u].y), fabsf(l[u].z))));
-            if (ln != 0.f || lt1 != 0.f || lt2 != 0.f)
-                scatter(Anxt, __float_as_int(r1[u].z), __float_as_int(r1[u].w), n, t1, t2, rA, rB, ln, lt1, lt2, vb[u].w,
-                        wb[u].w, va[u].w, wa[u].w);
+            pj_push<AGG>(Anxt, ok[u], a, b, o);
         }
     }
     // reset the accumulator of the sweep after next to the free velocities
@@ -601,17 +737,204 @@ __global__ void __launch_bounds__(NTH, MINB) k_s_sweep_t(SplitBuf sb, int gen, f
     }
 }
 
+// ---- cooperative whole solve
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Grid barrier of a cooperative launch (all blocks resident) that also reduces the per-sweep maxima.
+// Block g writes (max ||dlambda||, max |lambda|) into its own record, then thread 0 adds one to the
+// arrival counter and waits until it reaches the barrier's target (epoch x blocks). After the
+// barrier warp 0 reads every block's record (independent loads, one round trip) and takes the
+// maxima, so all blocks see the same numbers. Records alternate between two banks by epoch parity:
+// a block can run one barrier ahead of a slow reader, never two. The wait is bounded: after
+// COOP_WAIT_NS, or once another block has given up, the block sets *err and returns false.
+constexpr unsigned long long COOP_WAIT_NS = 200000000ull;  // 0.2 s
+constexpr int COOP_MAX_GRID = 256;                         // records a lane reads: COOP_MAX_GRID / 32
+__device__ __forceinline__ bool grid_sync_max(unsigned* ctr, float2* recs, unsigned epoch, int32_t* err, float& maxd,
+                                              float& maxl) {
+    __shared__ float s_md, s_ml;
+    __shared__ int s_ok;
+    float2* bank = recs + (size_t)(epoch & 1u) * SPLIT_MAX_PARTS;
+    if (threadIdx.x == 0) bank[blockIdx.x] = make_float2(maxd, maxl);
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const unsigned FULL = 0xffffffffu;
+        int ok = 1;
+        if (threadIdx.x == 0) {
+            __threadfence();
+            atomicAdd(ctr, 1u);
+            const unsigned target = epoch * gridDim.x;
+            const unsigned long long t0 = global_ns();
+            while ((int)(ld_acquire(ctr) - target) < 0) {
+                if (ld_acquire(reinterpret_cast<const unsigned*>(err)) != 0u || global_ns() - t0 > COOP_WAIT_NS) {
+                    atomicExch(err, 1);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(20);
+            }
+            __threadfence();
+        }
+        ok = __shfl_sync(FULL, ok, 0);
+        float md = 0.f, ml = 0.f;
+        if (ok) {
+            float2 v[COOP_MAX_GRID / 32];
+#pragma unroll
+            for (int k = 0; k < COOP_MAX_GRID / 32; ++k) {
+                const int p = threadIdx.x + 32 * k;
+                v[k] = p < (int)gridDim.x ? __ldcg(&bank[p]) : make_float2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int k = 0; k < COOP_MAX_GRID / 32; ++k) {
+                md = fmaxf(md, v[k].x);
+                ml = fmaxf(ml, v[k].y);
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                md = fmaxf(md, __shfl_xor_sync(FULL, md, o));
+                ml = fmaxf(ml, __shfl_xor_sync(FULL, ml, o));
+            }
+        }
+        if (threadIdx.x == 0) {
+            s_md = md;
+            s_ml = ml;
+            s_ok = ok;
+        }
+    }
+    __syncthreads();
+    maxd = s_md;
+    maxl = s_ml;
+    return s_ok != 0;
+}
+
+// The whole projected Jacobi solve (up to max_sweeps sweeps) in one cooperative launch. Block g
+// owns contacts [g*cpb, (g+1)*cpb) and bodies [g*bpb, (g+1)*bpb). It loads its contact records and
+// impulses into shared memory once (48 B a contact) and keeps them there across sweeps; the frame
+// and R are recomputed each sweep (keeping t1 and R in shared memory as well measured slower: they
+// crowd the free velocities out and lengthen the chain after the gathers). Each sweep then touches
+// L2/HBM only for the body velocities (gathers from A_k, reductions into A_{k+1}, the reset of A_{k+2}
+// from the free velocities, which also sit in shared memory when they fit). Sweeps are separated by
+// a grid barrier that also gathers the per-sweep maxima, so every block evaluates the same stop
+// rule on the same numbers; block 0 records the iteration count for the host.
+template <int NTH, int UNROLL, int AGG>
+__global__ void __launch_bounds__(NTH, 1) k_s_solve_coop(SplitBuf sb, int gen, float alpha, int max_iter, float tol,
+                                                         int cpb, int bpb, int vf_smem, int max_sweeps) {
+    extern __shared__ float4 smem[];
+    SplitScalars* ss = sb.ss;
+    if (*(volatile int32_t*)&ss->done) return;
+    float4* s_q0 = smem;            // (n, mu with the bias flag)
+    float4* s_q1 = smem + cpb;      // (rho_A, rho_B, A, B)
+    float4* s_l = smem + 2 * cpb;   // lambda
+    float4* s_vf = smem + 3 * cpb;  // free velocities of the block's bodies
+    const int it0 = *(volatile int32_t*)&ss->iters;
+    unsigned epoch = *(volatile unsigned*)&ss->bar_base;
+    const int nc = *sb.nc_dev, N = sb.N, tid = threadIdx.x;
+    const int cb = blockIdx.x * cpb;
+    const int ncb = max(0, min(nc - cb, cpb));
+    const int bb = blockIdx.x * bpb;
+    const int nbb = max(0, min(N - bb, bpb));
+    float4* __restrict__ lamg = sb.lam[gen];
+    for (int i = tid; i < ncb; i += NTH) {
+        const float4 r0 = ldg4(&sb.rec0[cb + i]), r1 = ldg4(&sb.rec1[cb + i]), l = lamg[cb + i];
+        s_q0[i] = r0;
+        s_q1[i] = r1;
+        s_l[i] = l;
+    }
+    if (vf_smem)
+        for (int i = tid; i < 2 * nbb; i += NTH) s_vf[i] = ldg4(&sb.vel4[2 * bb + i]);
+    __syncthreads();
+    int it = it0, stop = 0;
+    float r = 0.f;
+    for (int j = 0; j < max_sweeps; ++j) {
+        // the accumulators change inside this launch: read them through L2 (ld.global.cg)
+        const float4* Acur = sb.acc[it % 3];
+        float4* Anxt = sb.acc[(it + 1) % 3];
+        float4* Aclr = sb.acc[(it + 2) % 3];
+        float maxd2 = 0.f, maxl = 0.f;
+        for (int base = 0; base < ncb; base += NTH * UNROLL) {
+            float4 q0[UNROLL], q1[UNROLL], l[UNROLL];
+            bool ok[UNROLL];
+#pragma unroll
+            for (int u = 0; u < UNROLL; ++u) {
+                const int i = base + u * NTH + tid;
+                ok[u] = i < ncb;
+                if (ok[u]) {
+                    q0[u] = s_q0[i];
+                    q1[u] = s_q1[i];
+                    l[u] = s_l[i];
+                }
+            }
+            float4 vb[UNROLL], wb[UNROLL], va[UNROLL], wa[UNROLL];
+#pragma unroll
+            for (int u = 0; u < UNROLL; ++u) {
+                if (!ok[u]) continue;
+                const int a = __float_as_int(q1[u].z), b = __float_as_int(q1[u].w);
+                vb[u] = __ldcg(&Acur[2 * b]);
+                wb[u] = __ldcg(&Acur[2 * b + 1]);
+                if (a >= 0) {
+                    va[u] = __ldcg(&Acur[2 * a]);
+                    wa[u] = __ldcg(&Acur[2 * a + 1]);
+                } else {
+                    va[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    wa[u] = va[u];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < UNROLL; ++u) {
+                PJOut o = {};
+                int a = -1, b = 0;
+                if (ok[u]) {
+                    const int i = base + u * NTH + tid;
+                    a = __float_as_int(q1[u].z);
+                    b = __float_as_int(q1[u].w);
+                    pj_contact(q0[u], q1[u], l[u], va[u], wa[u], vb[u], wb[u], &sb.bias[cb + i], alpha, o);
+                    s_l[i] = o.lam;
+                    maxd2 = fmaxf(maxd2, o.dn2);
+                    maxl = fmaxf(maxl, o.lm);
+                }
+                pj_push<AGG>(Anxt, ok[u], a, b, o);
+            }
+        }
+        for (int i = tid; i < 2 * nbb; i += NTH) __stcg(&Aclr[2 * bb + i], vf_smem ? s_vf[i] : ldg4(&sb.vel4[2 * bb + i]));
+        block_max2(maxd2, maxl);
+        if (!grid_sync_max(&ss->bar, sb.recs, ++epoch, &ss->err, maxd2, maxl)) return;
+        r = sweep_residual(maxd2, maxl);
+        ++it;
+        if (it >= max_iter || (tol > 0.f && r <= tol) || !(r == r)) {
+            stop = 1;
+            break;
+        }
+    }
+    for (int i = tid; i < ncb; i += NTH) lamg[cb + i] = s_l[i];
+    // every block has read the scalars by now (it passed a barrier with all of them)
+    if (blockIdx.x == 0 && tid == 0) {
+        ss->iters = it;
+        ss->res_last = r;
+        ss->done = stop;
+        ss->bar_base = epoch;
+    }
+}
+
 __global__ void k_s_reset(SplitBuf sb) {
     SplitScalars* ss = sb.ss;
     ss->done = (*sb.nc_dev == 0) ? 1 : 0;
     ss->iters = 0;
     ss->blocks_done = 0u;
-    (void)0;
     ss->maxd = 0u;
     ss->maxl = 0u;
     ss->res_last = 0.f;
     ss->maxd64 = 0ull;
     ss->maxl64 = 0ull;
+    ss->err = 0;
+    ss->bar = 0u;
+    ss->bar_base = 0u;
 }
 
 // ------------------------------------------------------------------ FP64 finalisation
@@ -883,37 +1206,55 @@ int split_grid_blocks(int64_t n, int sms) {
     return (int)(want < 1 ? 1 : (want < cap ? want : cap));
 }
 
-// Launch shapes of the contact sweep the autotuner chooses between: contacts per thread, threads
-// per block and the register budget (minimum resident blocks per SM).
-struct ContactVariant {
+// Solver shapes the autotuner chooses between.
+// Streaming sweeps (one launch per sweep): contacts per thread, threads per block, register budget
+// (minimum resident blocks per SM) and scatter mode.
+struct StreamVariant {
     void (*kernel)(SplitBuf, int, float, int, float, cudaGraphConditionalHandle, int);
-    int unroll, nth, minb;
+    int unroll, nth, minb, agg;
     int per_sm;
 };
-static ContactVariant g_variants[] = {
-    {k_s_sweep_t<1, 256, 4>, 1, 256, 4, 0},
-    {k_s_sweep_t<1, 256, 5>, 1, 256, 5, 0},
-    {k_s_sweep_t<2, 256, 2>, 2, 256, 2, 0},
-    {k_s_sweep_t<1, 128, 8>, 1, 128, 8, 0},
-    {k_s_sweep_t<2, 128, 4>, 2, 128, 4, 0},
+static StreamVariant g_stream[] = {
+    {k_s_sweep_t<1, 256, 4, 2>, 1, 256, 4, 2, 0}, {k_s_sweep_t<2, 256, 2, 2>, 2, 256, 2, 2, 0},
+    {k_s_sweep_t<1, 128, 8, 2>, 1, 128, 8, 2, 0}, {k_s_sweep_t<2, 128, 4, 2>, 2, 128, 4, 2, 0},
+    {k_s_sweep_t<1, 256, 4, 1>, 1, 256, 4, 1, 0}, {k_s_sweep_t<1, 256, 4, 0>, 1, 256, 4, 0, 0},
 };
-constexpr int N_VARIANTS = sizeof(g_variants) / sizeof(g_variants[0]);
+constexpr int N_STREAM = sizeof(g_stream) / sizeof(g_stream[0]);
+// Cooperative solves (one launch for all sweeps): threads per block and contacts per thread per pass.
+struct CoopVariant {
+    void (*kernel)(SplitBuf, int, float, int, float, int, int, int, int);
+    int nth, unroll, agg;
+    int per_sm;    // resident blocks per SM with the full shared-memory budget (0 = not queried)
+    int smem_max;  // dynamic shared memory budget of one block
+};
+static CoopVariant g_coop[] = {
+    {k_s_solve_coop<1024, 1, 2>, 1024, 1, 2, 0, 0},
+    {k_s_solve_coop<512, 2, 2>, 512, 2, 2, 0, 0},
+    {k_s_solve_coop<1024, 1, 1>, 1024, 1, 1, 0, 0},
+};
+constexpr int N_COOP = sizeof(g_coop) / sizeof(g_coop[0]);
 
-// a variant is a kernel shape and a grid of 1 or 2 resident waves (index = 2 * shape + waves - 1)
-int split_num_variants() { return 2 * N_VARIANTS; }
+int split_num_variants() { return N_STREAM + N_COOP; }
+bool split_variant_is_coop(int v) { return v >= N_STREAM && v < N_STREAM + N_COOP; }
 
 const char* split_variant_name(int v) {
-    static const char* names[] = {"u1-t256-b4-w1", "u1-t256-b4-w2", "u1-t256-b5-w1", "u1-t256-b5-w2",
-                                  "u2-t256-b2-w1", "u2-t256-b2-w2", "u1-t128-b8-w1", "u1-t128-b8-w2",
-                                  "u2-t128-b4-w1", "u2-t128-b4-w2"};
-    return (v >= 0 && v < 2 * N_VARIANTS) ? names[v] : "?";
+    static char names[N_STREAM + N_COOP][32];
+    if (v < 0 || v >= N_STREAM + N_COOP) return "?";
+    if (!names[v][0]) {
+        if (v < N_STREAM) {
+            const StreamVariant& cv = g_stream[v];
+            snprintf(names[v], sizeof(names[v]), "sweep-u%d-t%d-b%d-g%d", cv.unroll, cv.nth, cv.minb, cv.agg);
+        } else {
+            const CoopVariant& cv = g_coop[v - N_STREAM];
+            snprintf(names[v], sizeof(names[v]), "coop-t%d-u%d-g%d", cv.nth, cv.unroll, cv.agg);
+        }
+    }
+    return names[v];
 }
 
-// grid of a variant: the resident capacity of the GPU (no partial tail wave), or fewer blocks when
-// there is less work than one pass
+// grid of a streaming variant: one resident wave, or fewer blocks when there is less work
 int split_contact_blocks(int vi, int64_t n, int sms) {
-    ContactVariant& cv = g_variants[vi / 2];
-    const int waves = 1 + (vi & 1);
+    StreamVariant& cv = g_stream[(vi >= 0 && vi < N_STREAM) ? vi : 0];
     if (cv.per_sm == 0) {
         int b = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, cv.kernel, cv.nth, 0);
@@ -921,9 +1262,57 @@ int split_contact_blocks(int vi, int64_t n, int sms) {
     }
     const int64_t per_block = (int64_t)cv.nth * cv.unroll;
     const int64_t want = (n + per_block - 1) / per_block;
-    int64_t cap = (int64_t)sms * cv.per_sm * waves;
+    int64_t cap = (int64_t)sms * cv.per_sm;
     if (cap > SPLIT_MAX_PARTS) cap = SPLIT_MAX_PARTS;
     return (int)(want < 1 ? 1 : (want < cap ? want : cap));
+}
+
+// Partition of a cooperative solve: one block per SM (all resident), contiguous contact and body
+// ranges per block. Feasible when a block's contacts (48 B each) fit in its shared memory; its free
+// velocities (32 B a body) are kept there too when they also fit.
+bool split_coop_plan(int v, int64_t nc, int64_t nbodies, int sms, CoopPlan* p) {
+    if (!split_variant_is_coop(v) || nc <= 0) return false;
+    CoopVariant& cv = g_coop[v - N_STREAM];
+    if (cv.per_sm == 0) {
+        int dev = 0, optin = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        cudaFuncAttributes fa;
+        if (cudaFuncGetAttributes(&fa, cv.kernel) != cudaSuccess) return false;
+        cv.smem_max = optin - (int)fa.sharedSizeBytes;
+        if (cv.smem_max <= 0 ||
+            cudaFuncSetAttribute(cv.kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, cv.smem_max) != cudaSuccess)
+            return false;
+        int b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, cv.kernel, cv.nth, cv.smem_max);
+        cv.per_sm = b > 0 ? b : -1;
+    }
+    if (cv.per_sm < 1) return false;
+    const int64_t grid = (int64_t)sms * cv.per_sm;
+    if (grid > COOP_MAX_GRID) return false;
+    const int64_t cpb = (nc + grid - 1) / grid;
+    const int64_t bpb = (nbodies + grid - 1) / grid;
+    const int64_t need = cpb * 48;
+    if (need > cv.smem_max) return false;
+    const bool vf = need + bpb * 32 <= cv.smem_max;
+    p->grid = (int)grid;
+    p->nth = cv.nth;
+    p->cpb = (int)cpb;
+    p->bpb = (int)bpb;
+    p->vf = vf ? 1 : 0;
+    p->smem = (int)(need + (vf ? bpb * 32 : 0));
+    return true;
+}
+
+int launch_s_solve_coop(const SplitBuf& sb, int gen, float alpha, int v, const CoopPlan& p, int max_iter, float tol,
+                        int max_sweeps, cudaStream_t s) {
+    if (!split_variant_is_coop(v)) return (int)cudaErrorInvalidValue;
+    const CoopVariant& cv = g_coop[v - N_STREAM];
+    SplitBuf b = sb;
+    int g = gen, mi = max_iter, cpb = p.cpb, bpb = p.bpb, vf = p.vf, ms = max_sweeps;
+    float al = alpha, t = tol;
+    void* args[] = {&b, &g, &al, &mi, &t, &cpb, &bpb, &vf, &ms};
+    return (int)cudaLaunchCooperativeKernel((const void*)cv.kernel, dim3(p.grid), dim3(cv.nth), args, (size_t)p.smem, s);
 }
 
 void launch_s_prep(const Scene& sc, const SplitBuf& sb, double dt, const double* g, double h1, cudaStream_t s) {
@@ -958,7 +1347,7 @@ void launch_s_apply_warm(const SplitBuf& sb, int gen, int blocks, cudaStream_t s
 }
 void launch_s_sweep(const SplitBuf& sb, int gen, float alpha, int variant, int blocks, int max_iter, float tol,
                     cudaGraphConditionalHandle h, int use_handle, cudaStream_t s) {
-    const ContactVariant& cv = g_variants[variant / 2];
+    const StreamVariant& cv = g_stream[(variant >= 0 && variant < N_STREAM) ? variant : 0];
     cv.kernel<<<blocks, cv.nth, 0, s>>>(sb, gen, alpha, max_iter, tol, h, use_handle);
 }
 void launch_s_drift(const Scene& sc, double h, cudaStream_t s) {

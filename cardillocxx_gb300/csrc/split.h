@@ -20,6 +20,11 @@ struct SplitScalars {
     unsigned long long maxd64;  // FP64 residual pass
     unsigned long long maxl64;
     double res_final;
+    // cooperative solve: grid-barrier arrival counter, the barrier epoch at the start of the next
+    // launch (the counter's target is epoch x blocks), and the barrier timeout flag
+    unsigned int bar;
+    unsigned int bar_base;
+    int32_t err;
 };
 
 struct SplitParams {
@@ -69,6 +74,7 @@ struct SplitBuf {
     int32_t* nc_dev = nullptr;
     SplitScalars* ss = nullptr;
     float2* part = nullptr;   // per-block (max ||dlambda||, max |lambda|) of the contact sweep
+    float2* recs = nullptr;   // cooperative solve: 2 banks x per-block (max ||dlambda||, max |lambda|)
     int has_restitution = 0;  // pre-solve velocities are only needed for restitution terms
 };
 
@@ -78,6 +84,16 @@ int split_contact_blocks(int variant, int64_t n, int sms);
 constexpr int SPLIT_MAX_PARTS = 4096;  // capacity of the per-block partial maxima
 int split_num_variants();
 const char* split_variant_name(int v);
+bool split_variant_is_coop(int v);
+// cooperative whole-solve partition (grid = one block per SM, contact and body ranges per block)
+struct CoopPlan {
+    int grid = 0, nth = 0, cpb = 0, bpb = 0, vf = 0, smem = 0;
+};
+bool split_coop_plan(int v, int64_t nc, int64_t nbodies, int sms, CoopPlan* p);
+// the projected Jacobi solve, up to max_sweeps sweeps, in one cooperative launch; returns the
+// cudaError_t of the launch
+int launch_s_solve_coop(const SplitBuf& sb, int gen, float alpha, int v, const CoopPlan& p, int max_iter, float tol,
+                        int max_sweeps, cudaStream_t s);
 void launch_s_prep(const Scene& sc, const SplitBuf& sb, double dt, const double* g, double h1, cudaStream_t s);
 void launch_s_static_flags(const Scene& sc, const SplitBuf& sb, float margin, int32_t* flags, cudaStream_t s);
 void launch_s_pair_count(const Scene& sc, const Grid& g, const SplitBuf& sb, const uint32_t* cell_body,

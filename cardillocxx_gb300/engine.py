@@ -180,6 +180,12 @@ class PhysicsEngine:
         return {"ms_contact": vals[0].value, "ms_body": vals[1].value, "bytes_contact": vals[2].value,
                 "bytes_body": vals[3].value}
 
+    @staticmethod
+    def split_variants() -> list:
+        """Names of the split-form sweep launch shapes (index = gpu.sweep_variant)."""
+        L = _lib.lib()
+        return [L.cdx_split_variant_name(k).decode() for k in range(L.cdx_split_variant_count())]
+
     def selftest_nr64(self, x):
         """Device Newton-Raphson reciprocal / inverse square root of x (diagnostic)."""
         x = np.ascontiguousarray(x, np.float64)

@@ -70,6 +70,7 @@ typedef struct cdx_config {
     double gpu_contact_capacity_factor; /* gpu.contact_capacity: initial contact slots per body */
     int32_t gpu_use_graph;            /* gpu.graph: capture the solver loop in a CUDA graph (split form) */
     int32_t gpu_autotune;             /* gpu.autotune: pick the contact-sweep launch shape by timing (split form) */
+    int32_t gpu_sweep_variant;        /* gpu.sweep_variant: pin launch shape k (split form; -1 = default/autotuned) */
 } cdx_config;
 
 /* Scene: dynamic spheres plus static shapes (halfspaces, drums). Bodies of one scene are
@@ -155,6 +156,11 @@ void* cdx_stream(cdx_ctx* ctx);
  * temporaries (not the body state) modified: call it after the steps being measured. */
 int cdx_time_sweeps(cdx_ctx* ctx, int32_t n, double* ms_contact, double* ms_body, double* bytes_contact,
                     double* bytes_body);
+/* Launch shapes of the split-form sweep: how many there are, and the name of shape k
+ * ("u<contacts per thread>-t<threads>-b<blocks per SM>-g<scatter mode>-w<waves>"; "?" out of range).
+ * gpu.sweep_variant pins one of them. No counterpart in the reference (its solver has one loop). */
+int32_t cdx_split_variant_count(void);
+const char* cdx_split_variant_name(int32_t k);
 
 /* ---- solver-level drop-in: ProjectedJacobiSolver::solve(dt, theta)
  * (src/physics/solver/projected_jacobi.cpp:451-500) with S = diag(M) (pj_assembler.cpp:127-182).

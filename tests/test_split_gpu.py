@@ -87,6 +87,33 @@ def test_split_one_step_matches_fp64(gpu):
     np.testing.assert_allclose(e64.state()["pos"], e32.state()["pos"], rtol=0, atol=1e-7)
 
 
+def test_split_every_sweep_shape_computes_the_same_sweep(gpu):
+    # every launch shape and scatter mode (atomicAdd, reductions, per-warp run sums) runs the same
+    # projected Jacobi sweep; only the FP32 summation order of W^T lambda differs
+    s = scenes.generate("pile_1k", scale=0.3)
+    base = scenes.config_for("pile_1k")
+    ref = PhysicsEngine(base).load_scene(s)
+    ref.step(250)
+    st = ref.state()
+    c = dict(base, **{"gpu.precision": "split", "pj.warmstart": False, "pj.max_iterations": 200})
+    names = PhysicsEngine.split_variants()
+    assert len(names) >= 2
+    out = []
+    for v in range(len(names)):
+        e = PhysicsEngine(dict(c, **{"gpu.sweep_variant": v})).load_scene(s)
+        e.set_state(st["pos"], st["quat"], st["vel"], st["omega"])
+        e.step(1)
+        assert e.stats()["contact_variant"] == v, names[v]
+        out.append((e.contacts()["lambda"], e.state()["vel"]))
+    lam0, vel0 = out[0]
+    lmax = np.abs(lam0).max()
+    vscale = np.abs(st["vel"]).max() + G * H
+    for v, (lam, vel) in enumerate(out):
+        assert lam.shape == lam0.shape, names[v]
+        assert np.abs(lam - lam0).max() <= 1e-3 * lmax, names[v]
+        assert np.abs(vel - vel0).max() <= 1e-3 * vscale, names[v]
+
+
 def test_split_residual_is_fp64_and_decreases(gpu):
     s = scenes.generate("pile_1k", scale=0.3)
     base = scenes.config_for("pile_1k", **{"gpu.precision": "split"})
