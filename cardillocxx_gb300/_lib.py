@@ -141,6 +141,13 @@ SIGNATURES = [
     ("cdx_stream", C.c_void_p, [C.c_void_p]),
     ("cdx_time_sweeps", C.c_int, [C.c_void_p, C.c_int32, _P, _P, _P, _P]),
     ("cdx_selftest_nr64", C.c_int, [C.c_void_p, C.c_int32, _P, _P, _P]),
+    ("cdx_adj_create", C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
+    ("cdx_adj_destroy", None, [C.c_void_p]),
+    ("cdx_adj_last_error", C.c_char_p, [C.c_void_p]),
+    ("cdx_adj_forward", C.c_int, [C.c_void_p, C.c_int32, _P, _P, _P, _P, _P, _P, _P]),
+    ("cdx_adj_backward", C.c_int, [C.c_void_p, _P, _P, _P, _P, _P, _P, _P]),
+    ("cdx_adj_info", C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int32)]),
+    ("cdx_adj_contact_counts", C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
     ("cdx_split_variant_count", C.c_int32, []),
     ("cdx_split_variant_name", C.c_char_p, [C.c_int32]),
     ("cdx_pj_solve_csr", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, _PI, _PI, _P, _P, _P, _P, _P, _P,

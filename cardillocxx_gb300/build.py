@@ -49,7 +49,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         obj = os.path.join(OBJ, os.path.basename(src) + ".o")
         flags = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
                  "-Xptxas", "-warn-spills"] + ARCH
-        if os.path.basename(src).startswith(("k_fp64", "k_csr", "noalloc")):
+        if os.path.basename(src).startswith(("k_fp64", "k_csr", "noalloc", "k_adjoint")):
             flags += ["--fmad=false"]
         cmd = [os.path.join(cuda, "bin", "nvcc"), *flags, "-I", CSRC, "-c", src, "-o", obj]
         jobs.append((obj, [src] + headers, cmd))

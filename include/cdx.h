@@ -162,6 +162,33 @@ int cdx_time_sweeps(cdx_ctx* ctx, int32_t n, double* ms_contact, double* ms_body
 int32_t cdx_split_variant_count(void);
 const char* cdx_split_variant_name(int32_t k);
 
+/* ---- differentiable rollout (the step's adjoint)
+ * The reference has no adjoint; the differentiated map is its step for sphere scenes,
+ * MoreauIntegrator::step (src/physics/integration/moreau.cpp:6-13) with the contact rows of
+ * dynamics_assembler.cpp:211-332 and ProjectedJacobiSolver::solve (projected_jacobi.cpp:451-500),
+ * written on world-frame angular velocities (for a sphere the orientation does not enter the
+ * motion). Scope: spheres and halfspaces, scenes of at most 1024 spheres, a fixed sweep count
+ * (pj.max_iterations) from lambda = 0 (no warm start), one friction coefficient per scene.
+ * Config keys used: sim.dt, sim.gravity, moreau.theta, pj.alpha, pj.max_iterations,
+ * collision.security_margin, gpu.contact_capacity (contact slots per sphere).
+ * cdx_adj_forward keeps the state every checkpoint_every steps; cdx_adj_backward recomputes each
+ * segment from its checkpoint and each step's sweeps from the step's input, so memory does not grow
+ * with the rollout length. States are [3N] arrays: x, v, omega (world frame); mu is [num_scenes]. */
+typedef struct cdx_adj cdx_adj;
+int cdx_adj_create(const cdx_config* cfg, const cdx_scene* scene, int32_t checkpoint_every, cdx_adj** out);
+void cdx_adj_destroy(cdx_adj* h);
+const char* cdx_adj_last_error(cdx_adj* h);
+int cdx_adj_forward(cdx_adj* h, int32_t nsteps, const double* x0, const double* v0, const double* w0,
+                    const double* mu_scene, double* xT, double* vT, double* wT);
+/* gradient of <gxT, xT> + <gvT, vT> + <gwT, wT> (the last forward's outputs) with respect to
+ * x0, v0, w0 and mu_scene */
+int cdx_adj_backward(cdx_adj* h, const double* gxT, const double* gvT, const double* gwT, double* gx0, double* gv0,
+                     double* gw0, double* gmu);
+int cdx_adj_info(cdx_adj* h, int64_t* contact_slots, int64_t* device_bytes, int32_t* checkpoints);
+/* per scene, the contacts of the last forward summed over its steps: two rollouts with equal sums
+ * saw the same contact events (the loss is smooth between such events, not across them) */
+int cdx_adj_contact_counts(cdx_adj* h, int64_t* per_scene);
+
 /* ---- solver-level drop-in: ProjectedJacobiSolver::solve(dt, theta)
  * (src/physics/solver/projected_jacobi.cpp:451-500) with S = diag(M) (pj_assembler.cpp:127-182).
  * Inputs are what the solver pulls from DynamicsAssembler (dynamics_assembler.hpp:23-94):

@@ -100,6 +100,37 @@ int32_t or_pj_solve_csr(int32_t nrows, int32_t nv, int32_t nfl, const int32_t* r
                         const double* f_gyro, double dt, double alpha, int32_t max_iter, double tol_abs,
                         double tol_rel, double* lambda_inout, double* x_out);
 
+/* FP64 adjoint of the world-frame sphere step (cdx_adjoint.cpp): scenes of spheres and halfspaces,
+ * K fixed sweeps from lambda = 0, per-scene friction coefficient. */
+typedef struct or_adj_problem {
+    int32_t num_bodies;
+    const double* radius;       /* [N] */
+    const double* mass;         /* [N] */
+    const double* inertia;      /* [N] */
+    const int32_t* body_scene;  /* [N] or NULL */
+    int32_t num_scenes;
+    int32_t num_statics;        /* halfspaces */
+    const double* static_dir;   /* [3S] outward normal */
+    const double* static_pos;   /* [3S] a point on the plane */
+    const int32_t* static_scene;/* [S] or NULL */
+    double dt;
+    double gravity[3];
+    double theta;
+    double alpha;
+    int32_t iterations;
+    double margin;
+} or_adj_problem;
+
+void* or_adj_create(const or_adj_problem* p);
+void or_adj_destroy(void* h);
+/* x, v, omega_world: [3N] each; mu: [num_scenes] */
+int32_t or_adj_rollout(void* h, int32_t nsteps, const double* x0, const double* v0, const double* w0,
+                       const double* mu_scene, double* xT, double* vT, double* wT);
+/* gradient of <gxT, xT> + <gvT, vT> + <gwT, wT> with respect to x0, v0, w0 and mu */
+int32_t or_adj_gradient(void* h, int32_t nsteps, const double* x0, const double* v0, const double* w0,
+                        const double* mu_scene, const double* gxT, const double* gvT, const double* gwT, double* gx0,
+                        double* gv0, double* gw0, double* gmu);
+
 #ifdef __cplusplus
 }
 #endif

@@ -24,15 +24,15 @@ _lib = None
 
 def build(force: bool = False) -> str:
     """Compile the oracle with g++ (no FMA contraction, OpenMP)."""
-    src = os.path.join(HERE, "cdx_oracle.cpp")
+    srcs = [os.path.join(HERE, "cdx_oracle.cpp"), os.path.join(HERE, "cdx_adjoint.cpp")]
     hdr = os.path.join(HERE, "cdx_oracle.h")
     if (not force and os.path.exists(LIB)
-            and os.path.getmtime(LIB) >= max(os.path.getmtime(src), os.path.getmtime(hdr))):
+            and os.path.getmtime(LIB) >= max(os.path.getmtime(f) for f in srcs + [hdr])):
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     tmp = LIB + f".{os.getpid()}.tmp"
     cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
-           "-fno-fast-math", src, "-o", tmp]
+           "-fno-fast-math", *srcs, "-o", tmp]
     subprocess.check_call(cmd)
     os.replace(tmp, LIB)
     return LIB
@@ -218,3 +218,105 @@ def pj_solve_csr(row_ptr, col, val, contact_bias, mu, restitution, minv, mdiag, 
     it = L.or_pj_solve_csr(nrows, nv, int(nfl), _ip(row_ptr), _ip(col), *[_dp(a) for a in arrs], float(dt),
                            float(alpha), int(max_iter), float(tol_abs), float(tol_rel), _dp(lam), _dp(x))
     return x, lam, it
+
+
+# ---- FP64 CPU adjoint of the world-frame sphere step (cdx_adjoint.cpp)
+class OrAdjProblem(C.Structure):
+    _fields_ = [
+        ("num_bodies", C.c_int32),
+        ("radius", _P), ("mass", _P), ("inertia", _P),
+        ("body_scene", _PI),
+        ("num_scenes", C.c_int32),
+        ("num_statics", C.c_int32),
+        ("static_dir", _P), ("static_pos", _P),
+        ("static_scene", _PI),
+        ("dt", C.c_double),
+        ("gravity", C.c_double * 3),
+        ("theta", C.c_double),
+        ("alpha", C.c_double),
+        ("iterations", C.c_int32),
+        ("margin", C.c_double),
+    ]
+
+
+def _adj_lib():
+    L = lib()
+    if not getattr(L, "_adj_ready", False):
+        L.or_adj_create.restype = C.c_void_p
+        L.or_adj_create.argtypes = [C.POINTER(OrAdjProblem)]
+        L.or_adj_destroy.argtypes = [C.c_void_p]
+        L.or_adj_rollout.restype = C.c_int32
+        L.or_adj_rollout.argtypes = [C.c_void_p, C.c_int32, _P, _P, _P, _P, _P, _P, _P]
+        L.or_adj_gradient.restype = C.c_int32
+        L.or_adj_gradient.argtypes = [C.c_void_p, C.c_int32, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]
+        L._adj_ready = True
+    return L
+
+
+class AdjOracle:
+    """FP64 CPU rollout and adjoint of the world-frame sphere step (halfspaces only, lambda_0 = 0,
+    fixed sweep count, per-scene friction coefficient)."""
+
+    def __init__(self, scene: dict, cfg: dict):
+        kinds = np.asarray(scene.get("static_kind", np.zeros(0, np.int32)))
+        if kinds.size and np.any(kinds != 0):
+            raise ValueError("the adjoint model covers halfspaces only")
+        N = scene["pos"].shape[0]
+        S = kinds.size
+        self._keep = []
+
+        def arr(a, dt=np.float64):
+            a = np.ascontiguousarray(a, dt)
+            self._keep.append(a)
+            return a
+
+        p = OrAdjProblem()
+        p.num_bodies = N
+        p.radius = _dp(arr(scene["radius"]))
+        p.mass = _dp(arr(scene["mass"]))
+        p.inertia = _dp(arr(scene["inertia"]))
+        bs = scene.get("body_scene")
+        p.body_scene = _ip(arr(bs, np.int32)) if bs is not None else None
+        self.num_scenes = int(scene.get("num_scenes", 1))
+        p.num_scenes = self.num_scenes
+        p.num_statics = S
+        p.static_dir = _dp(arr(scene["static_dir"])) if S else None
+        p.static_pos = _dp(arr(scene["static_pos"])) if S else None
+        ss = scene.get("static_scene")
+        p.static_scene = _ip(arr(ss, np.int32)) if (S and ss is not None) else None
+        p.dt = float(cfg.get("sim.dt", 1e-3))
+        g = cfg.get("sim.gravity", (0.0, 0.0, -9.81))
+        for k in range(3):
+            p.gravity[k] = float(g[k])
+        p.theta = float(cfg.get("moreau.theta", 1.0))
+        p.alpha = float(cfg.get("pj.alpha", 0.3))
+        p.iterations = int(cfg.get("pj.max_iterations", 50))
+        p.margin = float(cfg.get("collision.security_margin", 0.0))
+        self.N = N
+        self._p = p
+        self.L = _adj_lib()
+        self.h = self.L.or_adj_create(C.byref(p))
+        if not self.h:
+            raise ValueError("or_adj_create failed")
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.or_adj_destroy(self.h)
+            self.h = None
+
+    def rollout(self, nsteps, x0, v0, w0, mu):
+        x0, v0, w0 = (np.ascontiguousarray(a, np.float64).reshape(self.N, 3) for a in (x0, v0, w0))
+        mu = np.ascontiguousarray(np.broadcast_to(mu, (self.num_scenes,)), np.float64)
+        out = [np.empty((self.N, 3)) for _ in range(3)]
+        self.L.or_adj_rollout(self.h, int(nsteps), _dp(x0), _dp(v0), _dp(w0), _dp(mu), *[_dp(o) for o in out])
+        return tuple(out)
+
+    def gradient(self, nsteps, x0, v0, w0, mu, gxT, gvT, gwT):
+        x0, v0, w0, gxT, gvT, gwT = (np.ascontiguousarray(a, np.float64).reshape(self.N, 3)
+                                     for a in (x0, v0, w0, gxT, gvT, gwT))
+        mu = np.ascontiguousarray(np.broadcast_to(mu, (self.num_scenes,)), np.float64)
+        out = [np.empty((self.N, 3)) for _ in range(3)]
+        gmu = np.empty(self.num_scenes)
+        self.L.or_adj_gradient(self.h, int(nsteps), _dp(x0), _dp(v0), _dp(w0), _dp(mu), _dp(gxT), _dp(gvT),
+                               _dp(gwT), *[_dp(o) for o in out], _dp(gmu))
+        return out[0], out[1], out[2], gmu
