@@ -36,6 +36,13 @@ struct SplitState {
     int64_t tuned_at = 0;    // contact count at the last tuning
     int tune_runs = 0;
     cudaEvent_t tev[2] = {nullptr, nullptr};
+    // batched scenes: one block per scene
+    int32_t* scene_order = nullptr;  // scene ids by decreasing body count (device)
+    int scene_nbmax = 0;             // bodies of the largest scene
+    int scene_best = -1;             // the fastest scenes shape once tuned (-2: the regular solver)
+    int scene_tried = 0;
+    double scene_ms[16] = {0};
+    int scene_timing = -1;           // shape timed in the current step
 };
 }  // namespace cdx
 
@@ -129,6 +136,19 @@ static int init_split(Engine& E) {
     if ((st = salloc(E, (void**)&b.ss, sizeof(SplitScalars), "split"))) return st;
     if ((st = salloc(E, (void**)&b.part, sizeof(float2) * SPLIT_MAX_PARTS, "split"))) return st;
     if ((st = salloc(E, (void**)&b.recs, sizeof(float2) * 2 * SPLIT_MAX_PARTS, "split"))) return st;
+    {
+        // batched scenes: largest first, so the longest solves start first
+        std::vector<int32_t> order(nsc);
+        for (int q = 0; q < nsc; ++q) order[q] = q;
+        const std::vector<int32_t>& bs = E.h_scene_body_start;
+        auto size = [&](int q) { return bs.size() > (size_t)q + 1 ? bs[q + 1] - bs[q] : 0; };
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return size(x) > size(y); });
+        S->scene_nbmax = nsc > 0 ? size(order[0]) : 0;
+        if ((st = salloc(E, (void**)&S->scene_order, sizeof(int32_t) * std::max(nsc, 1), "split scenes"))) return st;
+        if ((st = E.cuda_check(cudaMemcpy(S->scene_order, order.data(), sizeof(int32_t) * nsc, cudaMemcpyHostToDevice),
+                               "scene order")))
+            return st;
+    }
     if ((st = E.cuda_check(cudaMallocHost((void**)&S->h_nc, sizeof(int32_t)), "pinned"))) return st;
     if ((st = E.cuda_check(cudaMallocHost((void**)&S->h_ss, sizeof(SplitScalars)), "pinned"))) return st;
     cudaMemsetAsync(b.ss, 0, sizeof(SplitScalars), E.stream);
@@ -258,11 +278,59 @@ int Engine::step_split() {
     if (timing) cudaEventRecord(ev[2], stream);
     const int maxit = std::max(1, cfg.pj_max_iterations);
     bool solved = false;
+    // batched scenes: every scene solved by its own block. Untuned, successive steps try every
+    // scenes shape and then the regular solver (one step for its own tuning, one timed), one full
+    // solve each, and the fastest is kept.
+    const int pinned = cfg.gpu_sweep_variant;
+    const int nsv = split_num_scenes_variants();
+    const bool multi = S->nc > 0 && sc.nscenes > 1 && S->scene_nbmax > 0 && S->scene_nbmax <= 3584;
+    bool scenes = false;
+    int scene_v = -1;
+    S->scene_timing = -1;
+    if (multi) {
+        if (pinned >= 0) {
+            scenes = split_variant_is_scenes(pinned);
+            scene_v = pinned;
+        } else if (S->scene_best != -1) {
+            scenes = S->scene_best >= 0;
+            scene_v = S->scene_best;
+        } else if (cfg.gpu_autotune) {
+            const int trial = S->scene_tried;  // 0..nsv-1 scenes shapes, nsv and nsv+1 the regular solver
+            scenes = trial < nsv;
+            scene_v = scenes ? split_first_scenes_variant() + trial : -2;
+            if (trial != nsv) S->scene_timing = trial;
+        } else {
+            scenes = true;
+            scene_v = split_first_scenes_variant();
+        }
+    }
+    if (S->scene_timing >= 0) {
+        if (!S->tev[0]) {
+            cudaEventCreate(&S->tev[0]);
+            cudaEventCreate(&S->tev[1]);
+        }
+        cudaEventRecord(S->tev[0], stream);
+    }
+    if (scenes) {
+        st = launch_s_solve_scenes(sc, sb, gen, (float)cfg.pj_alpha, scene_v, maxit, (float)cfg.gpu_residual_tol,
+                                   nflag > 0 ? spos : nullptr, nflag > 0 ? sflags : nullptr, poff, S->scene_order,
+                                   S->scene_nbmax, stream);
+        if ((st = cuda_check((cudaError_t)st, "scenes solve"))) return st;
+        S->variant = scene_v;
+        ++launches;
+        solved = true;
+    }
     const int nv = split_num_variants();
     // sweeps the autotuner spends: two per streaming shape, eight per feasible cooperative one
     int tune_sweeps = 0;
-    for (int v = 0; v < nv; ++v) tune_sweeps += split_variant_is_coop(v) ? 8 : 2;
-    if (S->nc > 0 && cfg.gpu_autotune && cfg.gpu_sweep_variant < 0 && S->nc >= 4096 &&
+    for (int v = 0; v < nv; ++v) {
+        CoopPlan probe;
+        if (split_variant_is_coop(v))
+            tune_sweeps += (S->nc > 0 && split_coop_plan(v, S->nc, sc.N, S->sms, &probe)) ? 8 : 0;
+        else if (!split_variant_is_scenes(v))
+            tune_sweeps += 2;
+    }
+    if (!scenes && S->nc > 0 && cfg.gpu_autotune && cfg.gpu_sweep_variant < 0 && S->nc >= 4096 &&
         (double)S->nc >= 1.5 * (double)S->tuned_at && maxit > 2 * tune_sweeps) {
         // autotune: the first sweeps of this step run with every shape; each is a full sweep of
         // the same math, so the step's result does not depend on which shape ran them
@@ -275,6 +343,7 @@ int Engine::step_split() {
         cudaGraphConditionalHandle none = 0;
         for (int v = 0; v < nv && !solved; ++v) {
             double t = 0;
+            if (split_variant_is_scenes(v)) continue;
             if (split_variant_is_coop(v)) {
                 // two launches of 2 and 6 sweeps: their difference is the cost of a sweep, the rest
                 // (loading and storing the contacts) is paid once per solve of maxit sweeps
@@ -322,7 +391,7 @@ int Engine::step_split() {
         ++S->tune_runs;
     }
     CoopPlan plan;
-    const bool coop = S->nc > 0 && split_variant_is_coop(S->variant) &&
+    const bool coop = !scenes && S->nc > 0 && split_variant_is_coop(S->variant) &&
                       split_coop_plan(S->variant, S->nc, sc.N, S->sms, &plan);
     if (S->nc > 0 && !solved && coop) {
         st = launch_s_solve_coop(sb, gen, (float)cfg.pj_alpha, S->variant, plan, maxit, (float)cfg.gpu_residual_tol,
@@ -330,8 +399,9 @@ int Engine::step_split() {
         if ((st = cuda_check((cudaError_t)st, "cooperative launch"))) return st;
         ++launches;
     } else if (S->nc > 0 && !solved) {
-        // streaming sweeps (a cooperative shape that does not fit this step runs as streaming shape 0)
-        const int sv = split_variant_is_coop(S->variant) ? 0 : S->variant;
+        // streaming sweeps (a cooperative or batched shape that does not apply runs as streaming shape 0)
+        const int sv = (split_variant_is_coop(S->variant) || split_variant_is_scenes(S->variant)) ? 0 : S->variant;
+        S->variant = sv;
         const int sblocks = split_contact_blocks(sv, std::max(S->nc, 1), S->sms);
         if (cfg.gpu_use_graph) {
             // grid sized for the capacity so a graph serves every step until the buffers grow
@@ -361,6 +431,7 @@ int Engine::step_split() {
             }
         }
     }
+    if (S->scene_timing >= 0) cudaEventRecord(S->tev[1], stream);
     if (timing) cudaEventRecord(ev[3], stream);
     // FP64: final velocities, residual, write back, drift theta h
     launch_s_final(sc, sb, gen, cfg.pj_alpha, cfg.friction_enable, cfg.friction_combine, cblocks, stream);
@@ -372,7 +443,22 @@ int Engine::step_split() {
     if ((st = cuda_check(cudaGetLastError(), "split launch"))) return st;
     if (S->h_ss->err) return fail(CDX_ERR_TIMEOUT, "cooperative solve: a grid barrier timed out");
     S->last_iters = S->nc > 0 ? S->h_ss->iters : 0;
-    if (!coop) launches += (int64_t)S->last_iters;
+    if (!coop && !scenes) launches += (int64_t)S->last_iters;
+    if (multi && pinned < 0 && S->scene_best == -1 && cfg.gpu_autotune) {
+        const int trial = S->scene_tried++;
+        if (S->scene_timing >= 0) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, S->tev[0], S->tev[1]);
+            S->scene_ms[trial] = ms;
+        }
+        if (S->scene_tried > nsv + 1) {
+            int best = 0;
+            for (int q = 1; q <= nsv + 1; ++q)
+                if (q != nsv && S->scene_ms[q] < S->scene_ms[best]) best = q;
+            S->scene_best = best < nsv ? split_first_scenes_variant() + best : -2;
+            ++S->tune_runs;
+        }
+    }
     S->res_last = S->h_ss->res_last;
     S->res_final = S->nc > 0 ? S->h_ss->res_final : 0.0;
     S->prev_count = S->nc;

@@ -922,6 +922,148 @@ __global__ void __launch_bounds__(NTH, 1) k_s_solve_coop(SplitBuf sb, int gen, f
     }
 }
 
+// ---- batched scenes: one block per scene, the whole solve in shared memory
+// Adds a contact's shares into shared-memory accumulators (float atomics); body A's share is first
+// summed per run of equal index within the warp, as in pj_push.
+__device__ __forceinline__ void smem_add3(float4* p, float x, float y, float z) {
+    atomicAdd(&p->x, x);
+    atomicAdd(&p->y, y);
+    atomicAdd(&p->z, z);
+}
+__device__ __forceinline__ void pj_push_smem(float4* A, bool ok, int a, int b, const PJOut& o) {
+    const bool go = ok && o.push;
+    if (go) {
+        smem_add3(&A[2 * b], o.pb.x, o.pb.y, o.pb.z);
+        smem_add3(&A[2 * b + 1], o.tb.x, o.tb.y, o.tb.z);
+    }
+    const int key = ok ? a : -1;
+    float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (go && a >= 0) {
+        v[0] = o.pa.x;
+        v[1] = o.pa.y;
+        v[2] = o.pa.z;
+        v[3] = o.ta.x;
+        v[4] = o.ta.y;
+        v[5] = o.ta.z;
+    }
+    const bool head = warp_run_sum(key, v);
+    if (head && key >= 0 && (v[0] != 0.f || v[1] != 0.f || v[2] != 0.f || v[3] != 0.f || v[4] != 0.f || v[5] != 0.f)) {
+        smem_add3(&A[2 * key], v[0], v[1], v[2]);
+        smem_add3(&A[2 * key + 1], v[3], v[4], v[5]);
+    }
+}
+
+// The projected Jacobi solve of a batch of independent scenes. Block k solves scene order[k]
+// (scenes ordered by decreasing size, so the long solves start first): its bodies' accumulators
+// A_k and A_{k+1} live in shared memory (64 B a body) and, with CSM, so do its contact records and
+// impulses (48 B a contact, up to ccap contacts; a scene with more reads them from L1/L2 every
+// sweep). Sweeps are separated by __syncthreads only. Each scene runs its own stop rule (iteration
+// cap, residual <= tol, non-finite) on its own maxima. The final velocities go to accumulator 0;
+// the largest per-scene sweep count and residual go to the step's scalars.
+template <int NT, int UNROLL, int CSM>
+__global__ void __launch_bounds__(NT) k_s_solve_scenes(Scene sc, SplitBuf sb, int gen, float alpha, int max_iter,
+                                                       float tol, const int32_t* spos, const int32_t* sflags,
+                                                       const int32_t* poff, const int32_t* order, int L, int nbmax,
+                                                       int ccap) {
+    extern __shared__ float4 sm4[];
+    float4* Ac = sm4;
+    float4* An = sm4 + 2 * nbmax;
+    __shared__ float s_r;
+    const int s = order[blockIdx.x];
+    const int b0 = sc.scene_body_start[s], nb = sc.scene_body_start[s + 1] - b0;
+    const int tid = threadIdx.x;
+    const int64_t nflag = (int64_t)sc.N * L;
+    int n_static = 0;
+    if (nflag > 0) n_static = spos[nflag - 1] + sflags[nflag - 1];
+    int cs0 = 0, cs1 = 0;
+    if (L > 0) {
+        cs0 = spos[(int64_t)b0 * L];
+        cs1 = ((int64_t)(b0 + nb) * L < nflag) ? spos[(int64_t)(b0 + nb) * L] : n_static;
+    }
+    const int cp0 = n_static + poff[b0], cp1 = n_static + poff[b0 + nb];
+    const int ns = cs1 - cs0, nc = ns + (cp1 - cp0);
+    const bool local = CSM && nc <= ccap;  // block-uniform
+    float4* q0s = sm4 + 4 * nbmax;
+    float4* q1s = q0s + ccap;
+    float4* ls = q1s + ccap;
+    float4* __restrict__ lamp = sb.lam[gen];
+    for (int i = tid; i < 2 * nb; i += NT) {
+        Ac[i] = sb.acc[0][2 * b0 + i];
+        An[i] = sb.vel4[2 * b0 + i];
+    }
+    if (local)
+        for (int k = tid; k < nc; k += NT) {
+            const int c = k < ns ? cs0 + k : cp0 + (k - ns);
+            q0s[k] = ldg4(&sb.rec0[c]);
+            q1s[k] = ldg4(&sb.rec1[c]);
+            ls[k] = lamp[c];
+        }
+    __syncthreads();
+    int it = 0;
+    float r = 0.f;
+    const int lane = tid & 31;
+    while (true) {
+        float maxd2 = 0.f, maxl = 0.f;
+        for (int w0 = (tid & ~31); w0 < nc; w0 += NT * UNROLL) {
+#pragma unroll
+            for (int u = 0; u < UNROLL; ++u) {
+                const int k = w0 + u * NT + lane;
+                const bool ok = k < nc;
+                PJOut o = {};
+                int a = -1, b = 0;
+                if (ok) {
+                    const int c = k < ns ? cs0 + k : cp0 + (k - ns);
+                    float4 r0, r1, l;
+                    if (local) {
+                        r0 = q0s[k];
+                        r1 = q1s[k];
+                        l = ls[k];
+                    } else {
+                        r0 = ldg4(&sb.rec0[c]);
+                        r1 = ldg4(&sb.rec1[c]);
+                        l = lamp[c];
+                    }
+                    const int ag = __float_as_int(r1.z), bg = __float_as_int(r1.w);
+                    a = ag >= 0 ? ag - b0 : -1;
+                    b = bg - b0;
+                    const float4 vb = Ac[2 * b], wb = Ac[2 * b + 1];
+                    const float4 va = a >= 0 ? Ac[2 * a] : make_float4(0.f, 0.f, 0.f, 0.f);
+                    const float4 wa = a >= 0 ? Ac[2 * a + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
+                    pj_contact(r0, r1, l, va, wa, vb, wb, &sb.bias[c], alpha, o);
+                    if (local)
+                        ls[k] = o.lam;
+                    else
+                        lamp[c] = o.lam;
+                    maxd2 = fmaxf(maxd2, o.dn2);
+                    maxl = fmaxf(maxl, o.lm);
+                }
+                pj_push_smem(An, ok, a, b, o);
+            }
+        }
+        block_max2(maxd2, maxl);
+        if (tid == 0) s_r = sweep_residual(maxd2, maxl);
+        __syncthreads();
+        r = s_r;
+        ++it;
+        float4* t = Ac;
+        Ac = An;
+        An = t;
+        const bool stop = it >= max_iter || (tol > 0.f && r <= tol) || !(r == r);
+        if (stop) break;
+        for (int i = tid; i < 2 * nb; i += NT) An[i] = sb.vel4[2 * b0 + i];
+        __syncthreads();
+    }
+    for (int i = tid; i < 2 * nb; i += NT) sb.acc[0][2 * b0 + i] = Ac[i];
+    if (local)
+        for (int k = tid; k < nc; k += NT) lamp[k < ns ? cs0 + k : cp0 + (k - ns)] = ls[k];
+    if (tid == 0) {
+        if (blockIdx.x == 0) sb.ss->final_acc = 0;
+        atomicMax(&sb.ss->iters, it);
+        atomicMax(reinterpret_cast<unsigned*>(&sb.ss->res_last), __float_as_uint(r == r ? r : 0.f));
+        atomicAdd(&sb.ss->iters_sum, (unsigned long long)it);
+    }
+}
+
 __global__ void k_s_reset(SplitBuf sb) {
     SplitScalars* ss = sb.ss;
     ss->done = (*sb.nc_dev == 0) ? 1 : 0;
@@ -935,6 +1077,8 @@ __global__ void k_s_reset(SplitBuf sb) {
     ss->err = 0;
     ss->bar = 0u;
     ss->bar_base = 0u;
+    ss->final_acc = -1;
+    ss->iters_sum = 0ull;
 }
 
 // ------------------------------------------------------------------ FP64 finalisation
@@ -1008,7 +1152,8 @@ __global__ void k_s_final_body(Scene sc, SplitBuf sb) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= sc.N) return;
     const int N = sc.N;
-    const float4* A = sb.acc[sb.ss->iters % 3];
+    const int fa = sb.ss->final_acc >= 0 ? sb.ss->final_acc : sb.ss->iters % 3;
+    const float4* A = sb.acc[fa];
     const float4 a0 = A[2 * i], a1 = A[2 * i + 1];
     const float4 f0 = sb.vel4[2 * i], f1 = sb.vel4[2 * i + 1];
     const double d[6] = {(double)a0.x - (double)f0.x, (double)a0.y - (double)f0.y, (double)a0.z - (double)f0.z,
@@ -1234,22 +1379,63 @@ static CoopVariant g_coop[] = {
 };
 constexpr int N_COOP = sizeof(g_coop) / sizeof(g_coop[0]);
 
-int split_num_variants() { return N_STREAM + N_COOP; }
+// Batched scenes (one block per scene): threads per block and contacts per thread per pass.
+struct ScenesVariant {
+    void (*kernel)(Scene, SplitBuf, int, float, int, float, const int32_t*, const int32_t*, const int32_t*,
+                   const int32_t*, int, int, int);
+    int nth, unroll, csm;
+    int smem_set;  // dynamic shared memory the kernel has been opted in to
+};
+static ScenesVariant g_scenes[] = {
+    {k_s_solve_scenes<128, 1, 1>, 128, 1, 1, 0}, {k_s_solve_scenes<256, 1, 1>, 256, 1, 1, 0},
+    {k_s_solve_scenes<64, 1, 1>, 64, 1, 1, 0},   {k_s_solve_scenes<128, 1, 0>, 128, 1, 0, 0},
+    {k_s_solve_scenes<256, 1, 0>, 256, 1, 0, 0},
+};
+constexpr int N_SCENES = sizeof(g_scenes) / sizeof(g_scenes[0]);
+
+int split_num_variants() { return N_STREAM + N_COOP + N_SCENES; }
 bool split_variant_is_coop(int v) { return v >= N_STREAM && v < N_STREAM + N_COOP; }
+bool split_variant_is_scenes(int v) { return v >= N_STREAM + N_COOP && v < N_STREAM + N_COOP + N_SCENES; }
+int split_first_scenes_variant() { return N_STREAM + N_COOP; }
+int split_num_scenes_variants() { return N_SCENES; }
 
 const char* split_variant_name(int v) {
-    static char names[N_STREAM + N_COOP][32];
-    if (v < 0 || v >= N_STREAM + N_COOP) return "?";
+    static char names[N_STREAM + N_COOP + N_SCENES][32];
+    if (v < 0 || v >= N_STREAM + N_COOP + N_SCENES) return "?";
     if (!names[v][0]) {
         if (v < N_STREAM) {
             const StreamVariant& cv = g_stream[v];
             snprintf(names[v], sizeof(names[v]), "sweep-u%d-t%d-b%d-g%d", cv.unroll, cv.nth, cv.minb, cv.agg);
-        } else {
+        } else if (v < N_STREAM + N_COOP) {
             const CoopVariant& cv = g_coop[v - N_STREAM];
             snprintf(names[v], sizeof(names[v]), "coop-t%d-u%d-g%d", cv.nth, cv.unroll, cv.agg);
+        } else {
+            const ScenesVariant& cv = g_scenes[v - N_STREAM - N_COOP];
+            snprintf(names[v], sizeof(names[v]), "scenes-t%d-u%d-c%d", cv.nth, cv.unroll, cv.csm);
         }
     }
     return names[v];
+}
+
+int launch_s_solve_scenes(const Scene& sc, const SplitBuf& sb, int gen, float alpha, int v, int max_iter, float tol,
+                          const int32_t* spos, const int32_t* sflags, const int32_t* poff, const int32_t* order,
+                          int nbmax, cudaStream_t s) {
+    if (!split_variant_is_scenes(v) || sc.nscenes <= 0) return (int)cudaErrorInvalidValue;
+    ScenesVariant& cv = g_scenes[v - N_STREAM - N_COOP];
+    // shared memory: two accumulators (64 B a body) and, for the contact-resident shapes, 48 B for
+    // each of up to 4 contacts a body (a settled pile has about 2); larger scenes fall back to L1/L2
+    int ccap = cv.csm ? 4 * nbmax : 0;
+    if (64 * nbmax + 48 * ccap > 227 * 1024) ccap = 0;
+    const int smem = 64 * nbmax + 48 * ccap;
+    if (smem > 227 * 1024) return (int)cudaErrorInvalidValue;
+    if (smem > 48 * 1024 && smem > cv.smem_set) {
+        cudaError_t e = cudaFuncSetAttribute(cv.kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return (int)e;
+        cv.smem_set = smem;
+    }
+    cv.kernel<<<sc.nscenes, cv.nth, smem, s>>>(sc, sb, gen, alpha, max_iter, tol, spos, sflags, poff, order,
+                                              sc.max_statics, nbmax, ccap);
+    return (int)cudaGetLastError();
 }
 
 // grid of a streaming variant: one resident wave, or fewer blocks when there is less work

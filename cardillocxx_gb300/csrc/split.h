@@ -25,6 +25,8 @@ struct SplitScalars {
     unsigned int bar;
     unsigned int bar_base;
     int32_t err;
+    int32_t final_acc;                // accumulator holding the final velocities (-1: iters % 3)
+    unsigned long long iters_sum;     // batched scenes: sweeps summed over scenes
 };
 
 struct SplitParams {
@@ -85,6 +87,14 @@ constexpr int SPLIT_MAX_PARTS = 4096;  // capacity of the per-block partial maxi
 int split_num_variants();
 const char* split_variant_name(int v);
 bool split_variant_is_coop(int v);
+bool split_variant_is_scenes(int v);
+int split_first_scenes_variant();
+int split_num_scenes_variants();
+// batched scenes: the whole solve of every scene, one block per scene (order = scene ids by
+// decreasing size; nbmax = bodies of the largest scene). Returns a cudaError_t.
+int launch_s_solve_scenes(const Scene& sc, const SplitBuf& sb, int gen, float alpha, int v, int max_iter, float tol,
+                          const int32_t* spos, const int32_t* sflags, const int32_t* poff, const int32_t* order,
+                          int nbmax, cudaStream_t s);
 // cooperative whole-solve partition (grid = one block per SM, contact and body ranges per block)
 struct CoopPlan {
     int grid = 0, nth = 0, cpb = 0, bpb = 0, vf = 0, smem = 0;

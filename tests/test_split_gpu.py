@@ -103,7 +103,9 @@ def test_split_every_sweep_shape_computes_the_same_sweep(gpu):
         e = PhysicsEngine(dict(c, **{"gpu.sweep_variant": v})).load_scene(s)
         e.set_state(st["pos"], st["quat"], st["vel"], st["omega"])
         e.step(1)
-        assert e.stats()["contact_variant"] == v, names[v]
+        # a batched-scenes shape does not apply to a single scene: the streaming shape 0 runs instead
+        expect = 0 if names[v].startswith("scenes") else v
+        assert e.stats()["contact_variant"] == expect, names[v]
         out.append((e.contacts()["lambda"], e.state()["vel"]))
     lam0, vel0 = out[0]
     lmax = np.abs(lam0).max()
@@ -179,3 +181,36 @@ def test_newton_raphson_fp64_matches_ieee(gpu):
     eps = np.finfo(float).eps
     assert np.max(np.abs(r - exact_r) / np.abs(exact_r)) <= 2 * eps
     assert np.max(np.abs(q - exact_q) / np.abs(exact_q)) <= 2 * eps
+
+
+def test_batched_scenes_solver_matches_fp64_and_streaming(gpu):
+    # thousands-of-scenes workload at 40 scenes: the per-scene block solver (chosen automatically
+    # for several scenes) against the plain FP64 method and the streaming sweep on one converged step
+    s = scenes.generate("batch_4096", scale=40 / 4096)
+    assert s["num_scenes"] >= 30
+    base = scenes.config_for("batch_4096")
+    ref = PhysicsEngine(base).load_scene(s)
+    ref.step(150)
+    st = ref.state()
+    c = dict(base, **{"pj.warmstart": False, "pj.max_iterations": 2000})
+    e64 = PhysicsEngine(c).load_scene(s)
+    e32 = PhysicsEngine(dict(c, **{"gpu.precision": "split"})).load_scene(s)
+    e32s = PhysicsEngine(dict(c, **{"gpu.precision": "split", "gpu.sweep_variant": "0"})).load_scene(s)
+    for e in (e64, e32, e32s):
+        e.set_state(st["pos"], st["quat"], st["vel"], st["omega"])
+        e.step(1)
+    names = PhysicsEngine.split_variants()
+    assert names[e32.stats()["contact_variant"]].startswith("scenes"), names[e32.stats()["contact_variant"]]
+    assert e32.stats()["iterations"] == 2000
+    c64, c32 = e64.contacts(), e32.contacts()
+    assert np.array_equal(np.sort(c64["id_a"] * 10**7 + c64["id_b"]), np.sort(c32["id_a"] * 10**7 + c32["id_b"]))
+    vscale = np.abs(st["vel"]).max() + 9.81 * 1e-3
+    for other in (e64, e32s):
+        assert np.abs(other.state()["vel"] - e32.state()["vel"]).max() <= 5e-3 * vscale
+    np.testing.assert_allclose(e64.state()["pos"], e32.state()["pos"], rtol=0, atol=1e-7)
+    # then a run of the batched workload with warm start: stays finite and resting
+    e = PhysicsEngine(dict(base, **{"gpu.precision": "split"})).load_scene(s)
+    e.set_state(st["pos"], st["quat"], st["vel"], st["omega"])
+    e.step(50)
+    v = e.state()["vel"]
+    assert np.isfinite(v).all() and np.abs(v).max() < 5.0
