@@ -44,7 +44,7 @@ __device__ __forceinline__ void frame32(float3 n, float3& t1, float3& t2) {
         const float d = dot(n, t1);
         t1 = t1 - d * n;
     } else {
-        const float a = 1.f / (1.f + n.z);
+        const float a = __frcp_rn(1.f + n.z);  // = 1 / (1 + n.z), correctly rounded either way
         const float b = (-n.x * n.y) * a;
         t1 = make_float3(1.f - (n.x * n.x) * a, b, -n.x);
     }
@@ -211,7 +211,7 @@ __device__ __forceinline__ bool static_test32(const SplitBuf& sb, int s, float3 
     const float3 perp = rel - ax * u;
     const float rho = sqrtf(dot(perp, perp));
     if (!(((pp.w - rho) - r) <= margin)) return false;
-    g.n = rho > 0.f ? (-1.f / rho) * perp : make_float3(0.f, 0.f, 1.f);
+    g.n = rho > 0.f ? (-__frcp_rn(rho)) * perp : make_float3(0.f, 0.f, 1.f);
     g.rhoB = -0.5f * ((pp.w - rho) + r);
     g.sep = rho;
     return true;
@@ -414,7 +414,7 @@ __global__ void k_s_pairs(Scene sc, Grid gr, SplitBuf sb, const uint32_t* cell_b
         const float4 pj = sb.pos4[j];
         const float3 d = f3(pj) - f3(pi);
         const float dl = sqrtf(dot(d, d));
-        const float3 n = dl > 0.f ? (1.f / dl) * d : make_float3(0.f, 0.f, 1.f);
+        const float3 n = dl > 0.f ? __frcp_rn(dl) * d : make_float3(0.f, 0.f, 1.f);
         const float rhoA = 0.5f * (dl + pi.w - pj.w);
         const float rhoB = 0.5f * (pi.w - pj.w - dl);
         const float3 pt = f3(pi) + rhoA * n;
@@ -738,6 +738,20 @@ __global__ void __launch_bounds__(NTH, MINB) k_s_sweep_t(SplitBuf sb, int gen, f
 }
 
 // ---- cooperative whole solve
+// one body's (v, 1/m), (omega, 1/I) pair as a single 32-byte load through L2: one sector request
+// instead of two (the accumulators change inside the cooperative launch, so they bypass L1)
+__device__ __forceinline__ void ldcg_body(const float4* p, float4& v, float4& w) {
+    asm volatile("ld.global.cg.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w), "=f"(w.x), "=f"(w.y), "=f"(w.z), "=f"(w.w)
+                 : "l"(p)
+                 : "memory");
+}
+__device__ __forceinline__ void stcg_body(float4* p, float4 v, float4 w) {
+    asm volatile("st.global.cg.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(p), "f"(v.x), "f"(v.y), "f"(v.z),
+                 "f"(v.w), "f"(w.x), "f"(w.y), "f"(w.z), "f"(w.w)
+                 : "memory");
+}
+
 __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
     unsigned v;
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -876,11 +890,9 @@ __global__ void __launch_bounds__(NTH, 1) k_s_solve_coop(SplitBuf sb, int gen, f
             for (int u = 0; u < UNROLL; ++u) {
                 if (!ok[u]) continue;
                 const int a = __float_as_int(q1[u].z), b = __float_as_int(q1[u].w);
-                vb[u] = __ldcg(&Acur[2 * b]);
-                wb[u] = __ldcg(&Acur[2 * b + 1]);
+                ldcg_body(&Acur[2 * b], vb[u], wb[u]);
                 if (a >= 0) {
-                    va[u] = __ldcg(&Acur[2 * a]);
-                    wa[u] = __ldcg(&Acur[2 * a + 1]);
+                    ldcg_body(&Acur[2 * a], va[u], wa[u]);
                 } else {
                     va[u] = make_float4(0.f, 0.f, 0.f, 0.f);
                     wa[u] = va[u];
@@ -902,7 +914,11 @@ __global__ void __launch_bounds__(NTH, 1) k_s_solve_coop(SplitBuf sb, int gen, f
                 pj_push<AGG>(Anxt, ok[u], a, b, o);
             }
         }
-        for (int i = tid; i < 2 * nbb; i += NTH) __stcg(&Aclr[2 * bb + i], vf_smem ? s_vf[i] : ldg4(&sb.vel4[2 * bb + i]));
+        for (int i = tid; i < nbb; i += NTH) {
+            const float4 v0 = vf_smem ? s_vf[2 * i] : ldg4(&sb.vel4[2 * (bb + i)]);
+            const float4 w0 = vf_smem ? s_vf[2 * i + 1] : ldg4(&sb.vel4[2 * (bb + i) + 1]);
+            stcg_body(&Aclr[2 * (bb + i)], v0, w0);
+        }
         block_max2(maxd2, maxl);
         if (!grid_sync_max(&ss->bar, sb.recs, ++epoch, &ss->err, maxd2, maxl)) return;
         r = sweep_residual(maxd2, maxl);
