@@ -354,7 +354,7 @@ int Engine::step_split() {
                 for (int r = 0; r < 2; ++r) {
                     cudaEventRecord(S->tev[0], stream);
                     st = launch_s_solve_coop(sb, gen, (float)cfg.pj_alpha, v, plan, maxit, (float)cfg.gpu_residual_tol,
-                                             ks[r], stream);
+                                             ks[r], cfg.gpu_check_every, stream);
                     if ((st = cuda_check((cudaError_t)st, "cooperative launch"))) return st;
                     cudaEventRecord(S->tev[1], stream);
                     if ((st = cuda_check(cudaEventSynchronize(S->tev[1]), "autotune"))) return st;
@@ -395,7 +395,7 @@ int Engine::step_split() {
                       split_coop_plan(S->variant, S->nc, sc.N, S->sms, &plan);
     if (S->nc > 0 && !solved && coop) {
         st = launch_s_solve_coop(sb, gen, (float)cfg.pj_alpha, S->variant, plan, maxit, (float)cfg.gpu_residual_tol,
-                                 maxit, stream);
+                                 maxit, cfg.gpu_check_every, stream);
         if ((st = cuda_check((cudaError_t)st, "cooperative launch"))) return st;
         ++launches;
     } else if (S->nc > 0 && !solved) {
@@ -546,7 +546,8 @@ int Engine::time_sweeps(int n, double* msc, double* msb, double* bc, double* bb)
         if (split_variant_is_coop(S->variant) && split_coop_plan(S->variant, S->prev_count, sc.N, S->sms, &plan)) {
             // one cooperative launch of n sweeps; reported per sweep
             cudaEventRecord(e[0], stream);
-            st = launch_s_solve_coop(S->sb, g, (float)cfg.pj_alpha, S->variant, plan, 1 << 30, 0.f, n, stream);
+            st = launch_s_solve_coop(S->sb, g, (float)cfg.pj_alpha, S->variant, plan, 1 << 30, 0.f, n,
+                                     cfg.gpu_check_every, stream);
             cudaEventRecord(e[1], stream);
             if (!(st = cuda_check((cudaError_t)st, "cooperative launch")) &&
                 !(st = cuda_check(cudaEventSynchronize(e[1]), "time sweeps"))) {

@@ -772,12 +772,12 @@ __device__ __forceinline__ unsigned long long global_ns() {
 // COOP_WAIT_NS, or once another block has given up, the block sets *err and returns false.
 constexpr unsigned long long COOP_WAIT_NS = 200000000ull;  // 0.2 s
 constexpr int COOP_MAX_GRID = 256;                         // records a lane reads: COOP_MAX_GRID / 32
-__device__ __forceinline__ bool grid_sync_max(unsigned* ctr, float2* recs, unsigned epoch, int32_t* err, float& maxd,
-                                              float& maxl) {
+__device__ __forceinline__ bool grid_sync_max(unsigned* ctr, float2* recs, unsigned epoch, int32_t* err, bool reduce,
+                                              float& maxd, float& maxl) {
     __shared__ float s_md, s_ml;
     __shared__ int s_ok;
     float2* bank = recs + (size_t)(epoch & 1u) * SPLIT_MAX_PARTS;
-    if (threadIdx.x == 0) bank[blockIdx.x] = make_float2(maxd, maxl);
+    if (reduce && threadIdx.x == 0) bank[blockIdx.x] = make_float2(maxd, maxl);
     __syncthreads();
     if (threadIdx.x < 32) {
         const unsigned FULL = 0xffffffffu;
@@ -799,7 +799,7 @@ __device__ __forceinline__ bool grid_sync_max(unsigned* ctr, float2* recs, unsig
         }
         ok = __shfl_sync(FULL, ok, 0);
         float md = 0.f, ml = 0.f;
-        if (ok) {
+        if (ok && reduce) {
             float2 v[COOP_MAX_GRID / 32];
 #pragma unroll
             for (int k = 0; k < COOP_MAX_GRID / 32; ++k) {
@@ -839,7 +839,8 @@ __device__ __forceinline__ bool grid_sync_max(unsigned* ctr, float2* recs, unsig
 // rule on the same numbers; block 0 records the iteration count for the host.
 template <int NTH, int UNROLL, int AGG>
 __global__ void __launch_bounds__(NTH, 1) k_s_solve_coop(SplitBuf sb, int gen, float alpha, int max_iter, float tol,
-                                                         int cpb, int bpb, int vf_smem, int max_sweeps) {
+                                                         int cpb, int bpb, int vf_smem, int max_sweeps,
+                                                         int check_every) {
     extern __shared__ float4 smem[];
     SplitScalars* ss = sb.ss;
     if (*(volatile int32_t*)&ss->done) return;
@@ -919,13 +920,18 @@ __global__ void __launch_bounds__(NTH, 1) k_s_solve_coop(SplitBuf sb, int gen, f
             const float4 w0 = vf_smem ? s_vf[2 * i + 1] : ldg4(&sb.vel4[2 * (bb + i) + 1]);
             stcg_body(&Aclr[2 * (bb + i)], v0, w0);
         }
-        block_max2(maxd2, maxl);
-        if (!grid_sync_max(&ss->bar, sb.recs, ++epoch, &ss->err, maxd2, maxl)) return;
-        r = sweep_residual(maxd2, maxl);
+        // the stop rule runs every check_every sweeps (counted across launches) and at the cap; the
+        // other sweeps only synchronise
+        const bool check = (it + 1) % check_every == 0 || it + 1 >= max_iter;
+        if (check) block_max2(maxd2, maxl);
+        if (!grid_sync_max(&ss->bar, sb.recs, ++epoch, &ss->err, check, maxd2, maxl)) return;
         ++it;
-        if (it >= max_iter || (tol > 0.f && r <= tol) || !(r == r)) {
-            stop = 1;
-            break;
+        if (check) {
+            r = sweep_residual(maxd2, maxl);
+            if (it >= max_iter || (tol > 0.f && r <= tol) || !(r == r)) {
+                stop = 1;
+                break;
+            }
         }
     }
     for (int i = tid; i < ncb; i += NTH) lamg[cb + i] = s_l[i];
@@ -1383,7 +1389,7 @@ static StreamVariant g_stream[] = {
 constexpr int N_STREAM = sizeof(g_stream) / sizeof(g_stream[0]);
 // Cooperative solves (one launch for all sweeps): threads per block and contacts per thread per pass.
 struct CoopVariant {
-    void (*kernel)(SplitBuf, int, float, int, float, int, int, int, int);
+    void (*kernel)(SplitBuf, int, float, int, float, int, int, int, int, int);
     int nth, unroll, agg;
     int per_sm;    // resident blocks per SM with the full shared-memory budget (0 = not queried)
     int smem_max;  // dynamic shared memory budget of one block
@@ -1391,7 +1397,6 @@ struct CoopVariant {
 static CoopVariant g_coop[] = {
     {k_s_solve_coop<1024, 1, 2>, 1024, 1, 2, 0, 0},
     {k_s_solve_coop<512, 2, 2>, 512, 2, 2, 0, 0},
-    {k_s_solve_coop<1024, 1, 1>, 1024, 1, 1, 0, 0},
 };
 constexpr int N_COOP = sizeof(g_coop) / sizeof(g_coop[0]);
 
@@ -1507,13 +1512,13 @@ bool split_coop_plan(int v, int64_t nc, int64_t nbodies, int sms, CoopPlan* p) {
 }
 
 int launch_s_solve_coop(const SplitBuf& sb, int gen, float alpha, int v, const CoopPlan& p, int max_iter, float tol,
-                        int max_sweeps, cudaStream_t s) {
+                        int max_sweeps, int check_every, cudaStream_t s) {
     if (!split_variant_is_coop(v)) return (int)cudaErrorInvalidValue;
     const CoopVariant& cv = g_coop[v - N_STREAM];
     SplitBuf b = sb;
-    int g = gen, mi = max_iter, cpb = p.cpb, bpb = p.bpb, vf = p.vf, ms = max_sweeps;
+    int g = gen, mi = max_iter, cpb = p.cpb, bpb = p.bpb, vf = p.vf, ms = max_sweeps, ce = check_every > 0 ? check_every : 1;
     float al = alpha, t = tol;
-    void* args[] = {&b, &g, &al, &mi, &t, &cpb, &bpb, &vf, &ms};
+    void* args[] = {&b, &g, &al, &mi, &t, &cpb, &bpb, &vf, &ms, &ce};
     return (int)cudaLaunchCooperativeKernel((const void*)cv.kernel, dim3(p.grid), dim3(cv.nth), args, (size_t)p.smem, s);
 }
 

@@ -65,7 +65,7 @@ typedef struct cdx_config {
     int32_t collision_broadphase;     /* collision.broadphase: 0 uniform_grid (any reference value maps here) */
     int32_t gpu_precision;            /* gpu.precision: CDX_PRECISION_FP64 | CDX_PRECISION_SPLIT */
     double gpu_residual_tol;          /* gpu.residual_tol: stop when the complementarity residual <= tol (0 off) */
-    int32_t gpu_check_every;          /* gpu.check_every: host polls the stop flag every k sweeps */
+    int32_t gpu_check_every;          /* gpu.check_every: the split-form stop rule runs every k sweeps */
     int32_t gpu_block;                /* gpu.block: threads per block for contact kernels (0 = auto) */
     double gpu_contact_capacity_factor; /* gpu.contact_capacity: initial contact slots per body */
     int32_t gpu_use_graph;            /* gpu.graph: capture the solver loop in a CUDA graph (split form) */
