@@ -58,6 +58,7 @@ class CdxConfig(C.Structure):
         ("gpu_use_graph", C.c_int32),
         ("gpu_autotune", C.c_int32),
         ("gpu_sweep_variant", C.c_int32),
+        ("gpu_sync_counts", C.c_int32),
     ]
 
 
@@ -94,6 +95,7 @@ class CdxStats(C.Structure):
         ("kernel_launches", C.c_int64),
         ("contact_variant", C.c_int32),
         ("autotune_runs", C.c_int32),
+        ("redone_steps", C.c_int32),
     ]
 
 

@@ -92,6 +92,7 @@ int cdx_config_default(cdx_config* c) {
     c->gpu_use_graph = 1;
     c->gpu_autotune = 1;
     c->gpu_sweep_variant = -1;
+    c->gpu_sync_counts = 0;
     return CDX_OK;
 }
 
@@ -171,6 +172,8 @@ int cdx_config_set(cdx_config* c, const char* key_c, const char* val_c) {
         c->gpu_autotune = as_bool(val);
     } else if (key == "gpu.sweep_variant") {
         if (as_int(val, &i)) c->gpu_sweep_variant = std::max(-1, i);
+    } else if (key == "gpu.sync_counts") {
+        c->gpu_sync_counts = as_bool(val);
     }
     return CDX_OK;  // unknown keys are ignored, as in the reference
 }

@@ -633,6 +633,7 @@ void Engine::fill_stats(cdx_stats* s) {
     s->kernel_launches = launches;
     s->contact_variant = split_variant();
     s->autotune_runs = split_tune_runs();
+    s->redone_steps = split_redos();
 }
 
 double Engine::solve_bytes_per_iter() const {

@@ -95,6 +95,7 @@ struct Engine {
     double split_bytes_per_iter() const;
     int split_variant() const;
     int split_tune_runs() const;
+    int split_redos() const;
     int time_sweeps(int n, double* msc, double* msb, double* bc, double* bb);
 };
 

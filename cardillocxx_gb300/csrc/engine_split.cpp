@@ -32,6 +32,7 @@ struct SplitState {
     int last_iters = 0;
     double res_last = 0, res_final = 0;
     int variant = 0;         // contact-sweep launch shape (autotuned)
+    int last_variant = 0;    // the shape that ran the last step
     int graph_variant = -1;
     int64_t tuned_at = 0;    // contact count at the last tuning
     int tune_runs = 0;
@@ -43,6 +44,12 @@ struct SplitState {
     int scene_tried = 0;
     double scene_ms[16] = {0};
     int scene_timing = -1;           // shape timed in the current step
+    // steps that find their contact totals on the device: a snapshot of the state they change, so
+    // a step whose contacts outgrow the buffers or the plan can be undone and redone
+    double* snap = nullptr;   // 13 N: position, quaternion, velocity, omega (body field order)
+    double* ssnap = nullptr;  // 13 S: the same for the statics
+    bool force_sync = false;
+    int syncs = 0, redos = 0;
 };
 }  // namespace cdx
 
@@ -136,6 +143,8 @@ static int init_split(Engine& E) {
     if ((st = salloc(E, (void**)&b.ss, sizeof(SplitScalars), "split"))) return st;
     if ((st = salloc(E, (void**)&b.part, sizeof(float2) * SPLIT_MAX_PARTS, "split"))) return st;
     if ((st = salloc(E, (void**)&b.recs, sizeof(float2) * 2 * SPLIT_MAX_PARTS, "split"))) return st;
+    if ((st = salloc(E, (void**)&S->snap, sizeof(double) * 13 * n1, "split snapshot"))) return st;
+    if ((st = salloc(E, (void**)&S->ssnap, sizeof(double) * 13 * s1, "split snapshot"))) return st;
     {
         // batched scenes: largest first, so the longest solves start first
         std::vector<int32_t> order(nsc);
@@ -227,6 +236,37 @@ int Engine::step_split() {
     P.prev_poff = poff_prev;
     P.prev_n_static = S->prev_n_static;
     const int gen = S->gen;
+    const int maxit = std::max(1, cfg.pj_max_iterations);
+    const int pinned = cfg.gpu_sweep_variant;
+
+    // Once a step has sized the buffers, the next steps find their contact totals on the device and
+    // run to the end without stopping for the host: buffers and the cooperative plan come from the
+    // previous count with a margin. Steps that tune (timing needs the host) stay synchronous, and a
+    // step whose contacts outgrow the buffers or the plan is undone from a snapshot and redone
+    // synchronously.
+    auto tune_due = [&](int64_t n) {
+        if (!(n > 0 && cfg.gpu_autotune && pinned < 0 && n >= 4096 && (double)n >= 1.5 * (double)S->tuned_at))
+            return false;
+        int sweeps = 0;
+        for (int v = 0; v < split_num_variants(); ++v) {
+            CoopPlan probe;
+            if (split_variant_is_coop(v))
+                sweeps += split_coop_plan(v, n, sc.N, S->sms, &probe) ? 8 : 0;
+            else if (!split_variant_is_scenes(v))
+                sweeps += 2;
+        }
+        return maxit > 2 * sweeps;
+    };
+    const bool scene_tuning = sc.nscenes > 1 && pinned < 0 && S->scene_best == -1 && cfg.gpu_autotune;
+    const bool async = !cfg.gpu_sync_counts && S->prev_count > 0 && sb.cap > 0 && !S->force_sync && !scene_tuning &&
+                       !tune_due(S->prev_count);
+    S->force_sync = false;
+    if (async) {
+        cudaMemcpyAsync(S->snap, sc.B, sizeof(double) * 13 * (size_t)N, cudaMemcpyDeviceToDevice, stream);
+        if (sc.S > 0)
+            cudaMemcpyAsync(S->ssnap, sc.St, sizeof(double) * 13 * (size_t)sc.S, cudaMemcpyDeviceToDevice, stream);
+        ++S->syncs;
+    }
 
     if (timing) cudaEventRecord(ev[0], stream);
     launch_s_prep(sc, sb, dt, cfg.sim_gravity, (1.0 - th) * dt, stream);
@@ -246,28 +286,38 @@ int Engine::step_split() {
     launch_s_pair_count(sc, grid, sb, cell_val_out, cell_start, cell_end, pcount, P, ds, stream);
     if ((st = cuda_check(exclusive_scan(tmp, tmp_bytes, pcount, poff, N + 1, stream), "scan"))) return st;
     launches += 3;
-    int32_t tot[4] = {0, 0, 0, 0};
-    if (nflag > 0) {
-        cudaMemcpyAsync(&tot[0], spos + nflag - 1, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
-        cudaMemcpyAsync(&tot[1], sflags + nflag - 1, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
-    }
-    cudaMemcpyAsync(&tot[2], poff + N, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
-    cudaMemcpyAsync(&tot[3], &ds->overflow, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
-    if ((st = cuda_check(cudaStreamSynchronize(stream), "collision counts"))) return st;
-    if (tot[3]) return fail(CDX_ERR_OVERFLOW, "a sphere touches more than 64 higher-index spheres");
-    const int64_t n_static = (int64_t)tot[0] + tot[1];
-    const int64_t n_pair = tot[2];
-    if ((st = split_contacts(*this, n_static + n_pair))) return st;
-    S->nc = (int)(n_static + n_pair);
-    *S->h_nc = S->nc;
-    cudaMemcpyAsync(sb.nc_dev, S->h_nc, sizeof(int32_t), cudaMemcpyHostToDevice, stream);
-    if (nflag > 0 && n_static > 0) {
-        launch_s_static_write(sc, sb, sflags, spos, gen, P, stream);
+    int64_t n_static = 0, n_pair = 0;
+    if (async) {
+        launch_s_totals(sb, spos, sflags, nflag, poff, N, stream);
+        S->nc = S->prev_count;  // an estimate for the launch shapes; the device holds the count
+        if (nflag > 0) launch_s_static_write(sc, sb, sflags, spos, gen, P, stream);
+        launch_s_pair_write(sc, grid, sb, cell_val_out, cell_start, cell_end, poff, -1, gen, P, ds, stream);
+        launches += 3;
+    } else {
+        int32_t tot[4] = {0, 0, 0, 0};
+        if (nflag > 0) {
+            cudaMemcpyAsync(&tot[0], spos + nflag - 1, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+            cudaMemcpyAsync(&tot[1], sflags + nflag - 1, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+        }
+        cudaMemcpyAsync(&tot[2], poff + N, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+        cudaMemcpyAsync(&tot[3], &ds->overflow, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+        if ((st = cuda_check(cudaStreamSynchronize(stream), "collision counts"))) return st;
+        if (tot[3]) return fail(CDX_ERR_OVERFLOW, "a sphere touches more than 64 higher-index spheres");
+        n_static = (int64_t)tot[0] + tot[1];
+        n_pair = tot[2];
+        if ((st = split_contacts(*this, n_static + n_pair))) return st;
+        S->nc = (int)(n_static + n_pair);
+        launch_s_totals(sb, spos, sflags, nflag, poff, N, stream);
         ++launches;
-    }
-    if (n_pair > 0) {
-        launch_s_pair_write(sc, grid, sb, cell_val_out, cell_start, cell_end, poff, (int32_t)n_static, gen, P, ds, stream);
-        ++launches;
+        if (nflag > 0 && n_static > 0) {
+            launch_s_static_write(sc, sb, sflags, spos, gen, P, stream);
+            ++launches;
+        }
+        if (n_pair > 0) {
+            launch_s_pair_write(sc, grid, sb, cell_val_out, cell_start, cell_end, poff, (int32_t)n_static, gen, P, ds,
+                                stream);
+            ++launches;
+        }
     }
     if (timing) cudaEventRecord(ev[1], stream);
     // x0 = v_free + M^-1 W^T lambda_warm
@@ -276,12 +326,10 @@ int Engine::step_split() {
     launch_s_apply_warm(sb, gen, cblocks, stream);
     launches += 2;
     if (timing) cudaEventRecord(ev[2], stream);
-    const int maxit = std::max(1, cfg.pj_max_iterations);
     bool solved = false;
     // batched scenes: every scene solved by its own block. Untuned, successive steps try every
     // scenes shape and then the regular solver (one step for its own tuning, one timed), one full
     // solve each, and the fastest is kept.
-    const int pinned = cfg.gpu_sweep_variant;
     const int nsv = split_num_scenes_variants();
     const bool multi = S->nc > 0 && sc.nscenes > 1 && S->scene_nbmax > 0 && S->scene_nbmax <= 3584;
     bool scenes = false;
@@ -317,6 +365,7 @@ int Engine::step_split() {
                                    S->scene_nbmax, stream);
         if ((st = cuda_check((cudaError_t)st, "scenes solve"))) return st;
         S->variant = scene_v;
+        S->last_variant = scene_v;
         ++launches;
         solved = true;
     }
@@ -330,7 +379,7 @@ int Engine::step_split() {
         else if (!split_variant_is_scenes(v))
             tune_sweeps += 2;
     }
-    if (!scenes && S->nc > 0 && cfg.gpu_autotune && cfg.gpu_sweep_variant < 0 && S->nc >= 4096 &&
+    if (!async && !scenes && S->nc > 0 && cfg.gpu_autotune && cfg.gpu_sweep_variant < 0 && S->nc >= 4096 &&
         (double)S->nc >= 1.5 * (double)S->tuned_at && maxit > 2 * tune_sweeps) {
         // autotune: the first sweeps of this step run with every shape; each is a full sweep of
         // the same math, so the step's result does not depend on which shape ran them
@@ -387,21 +436,24 @@ int Engine::step_split() {
             solved = S->h_ss->done != 0;
         }
         S->variant = best;
+        S->last_variant = best;
         S->tuned_at = S->nc;
         ++S->tune_runs;
     }
     CoopPlan plan;
+    const int64_t plan_nc = async ? (int64_t)S->nc + S->nc / 16 + 64 : (int64_t)S->nc;
     const bool coop = !scenes && S->nc > 0 && split_variant_is_coop(S->variant) &&
-                      split_coop_plan(S->variant, S->nc, sc.N, S->sms, &plan);
+                      split_coop_plan(S->variant, plan_nc, sc.N, S->sms, &plan);
     if (S->nc > 0 && !solved && coop) {
         st = launch_s_solve_coop(sb, gen, (float)cfg.pj_alpha, S->variant, plan, maxit, (float)cfg.gpu_residual_tol,
                                  maxit, cfg.gpu_check_every, stream);
+        S->last_variant = S->variant;
         if ((st = cuda_check((cudaError_t)st, "cooperative launch"))) return st;
         ++launches;
     } else if (S->nc > 0 && !solved) {
         // streaming sweeps (a cooperative or batched shape that does not apply runs as streaming shape 0)
         const int sv = (split_variant_is_coop(S->variant) || split_variant_is_scenes(S->variant)) ? 0 : S->variant;
-        S->variant = sv;
+        S->last_variant = sv;
         const int sblocks = split_contact_blocks(sv, std::max(S->nc, 1), S->sms);
         if (cfg.gpu_use_graph) {
             // grid sized for the capacity so a graph serves every step until the buffers grow
@@ -439,9 +491,26 @@ int Engine::step_split() {
     launches += 5;
     if (timing) cudaEventRecord(ev[4], stream);
     cudaMemcpyAsync(S->h_ss, sb.ss, sizeof(SplitScalars), cudaMemcpyDeviceToHost, stream);
+    int32_t pair_overflow = 0;
+    if (async) cudaMemcpyAsync(&pair_overflow, &ds->overflow, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
     if ((st = cuda_check(cudaStreamSynchronize(stream), "split step"))) return st;
     if ((st = cuda_check(cudaGetLastError(), "split launch"))) return st;
+    if (pair_overflow) return fail(CDX_ERR_OVERFLOW, "a sphere touches more than 64 higher-index spheres");
+    if (async && (S->h_ss->cap_err || S->h_ss->err == 4)) {
+        // undo the step (state from the snapshot; everything else is rebuilt) and redo it synchronously
+        cudaMemcpyAsync(sc.B, S->snap, sizeof(double) * 13 * (size_t)N, cudaMemcpyDeviceToDevice, stream);
+        if (sc.S > 0)
+            cudaMemcpyAsync(sc.St, S->ssnap, sizeof(double) * 13 * (size_t)sc.S, cudaMemcpyDeviceToDevice, stream);
+        if ((st = cuda_check(cudaStreamSynchronize(stream), "undo step"))) return st;
+        ++S->redos;
+        S->force_sync = true;
+        return step_split();
+    }
     if (S->h_ss->err) return fail(CDX_ERR_TIMEOUT, "cooperative solve: a grid barrier timed out");
+    if (async) {
+        S->nc = S->h_ss->n_total;
+        n_static = S->h_ss->n_static;
+    }
     S->last_iters = S->nc > 0 ? S->h_ss->iters : 0;
     if (!coop && !scenes) launches += (int64_t)S->last_iters;
     if (multi && pinned < 0 && S->scene_best == -1 && cfg.gpu_autotune) {
@@ -610,8 +679,9 @@ int Engine::time_sweeps(int n, double* msc, double* msb, double* bc, double* bb)
     return CDX_OK;
 }
 
-int Engine::split_variant() const { return split ? split->variant : -1; }
+int Engine::split_variant() const { return split ? split->last_variant : -1; }
 int Engine::split_tune_runs() const { return split ? split->tune_runs : 0; }
+int Engine::split_redos() const { return split ? split->redos : 0; }
 
 extern "C" int cdx_selftest_nr64(cdx_ctx* ctx, int32_t n, const double* x, double* rcp, double* rsq) {
     if (!ctx || n < 0 || (n > 0 && (!x || !rcp || !rsq))) return CDX_ERR_ARG;

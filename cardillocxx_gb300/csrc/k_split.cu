@@ -13,6 +13,7 @@
 // recomputed from the FP64 positions.
 #include <cuda_runtime.h>
 
+#include <cstdint>
 #include <cstdio>
 
 #include "cdx_internal.h"
@@ -257,6 +258,7 @@ __device__ __forceinline__ void finish_contact32(const Scene& sc, SplitBuf& sb, 
                                                  float3 n, float rhoA, float rhoB, float3 pt, float mu_a,
                                                  float rn_a, float rt_a, const float3* wall_v, const float3* wall_w,
                                                  const float3* wall_p, const SplitParams& P, int prev_lo, int prev_hi) {
+    if (c >= sb.cap) return;  // more contacts than slots: the host sees cap_err and redoes the step
     float3 vna = make_float3(0.f, 0.f, 0.f), wna = vna;
     if (a >= 0 && sb.has_restitution) {
         vna = f3(sb.vn4[2 * a]);
@@ -401,7 +403,7 @@ __global__ void k_s_pairs(Scene sc, Grid gr, SplitBuf sb, const uint32_t* cell_b
         }
         list[b + 1] = v;
     }
-    const int c0 = base + offsets[i];
+    const int c0 = (base >= 0 ? base : sb.ss->n_static) + offsets[i];
     int plo = 0, phi = 0;
     if (P.prev_count > 0) {
         plo = P.prev_n_static + P.prev_poff[i];
@@ -851,8 +853,16 @@ __global__ void __launch_bounds__(NTH, 1) k_s_solve_coop(SplitBuf sb, int gen, f
     const int it0 = *(volatile int32_t*)&ss->iters;
     unsigned epoch = *(volatile unsigned*)&ss->bar_base;
     const int nc = *sb.nc_dev, N = sb.N, tid = threadIdx.x;
-    const int cb = blockIdx.x * cpb;
-    const int ncb = max(0, min(nc - cb, cpb));
+    if ((int64_t)nc > (int64_t)cpb * gridDim.x) {
+        // planned from an estimate of the contact count that fell short: every block returns (no
+        // barrier has been entered) and the host redoes the step with a plan from the true count
+        if (blockIdx.x == 0 && tid == 0) ss->err = 4;
+        return;
+    }
+    // contacts split evenly by the true count (cpb, planned from an estimate, sizes the arrays)
+    const int cpe = (nc + (int)gridDim.x - 1) / (int)gridDim.x;
+    const int cb = blockIdx.x * cpe;
+    const int ncb = max(0, min(nc - cb, cpe));
     const int bb = blockIdx.x * bpb;
     const int nbb = max(0, min(N - bb, bpb));
     float4* __restrict__ lamg = sb.lam[gen];
@@ -1084,6 +1094,17 @@ __global__ void __launch_bounds__(NT) k_s_solve_scenes(Scene sc, SplitBuf sb, in
         atomicMax(reinterpret_cast<unsigned*>(&sb.ss->res_last), __float_as_uint(r == r ? r : 0.f));
         atomicAdd(&sb.ss->iters_sum, (unsigned long long)it);
     }
+}
+
+__global__ void k_s_totals(SplitBuf sb, const int32_t* spos, const int32_t* sflags, int64_t nflag,
+                           const int32_t* poff, int N) {
+    SplitScalars* ss = sb.ss;
+    const int ns = nflag > 0 ? spos[nflag - 1] + sflags[nflag - 1] : 0;
+    const int64_t tot = (int64_t)ns + poff[N];
+    ss->n_static = ns;
+    ss->n_total = (int32_t)(tot < (int64_t)INT32_MAX ? tot : INT32_MAX);
+    ss->cap_err = tot > sb.cap ? 1 : 0;
+    *sb.nc_dev = (int32_t)(tot < sb.cap ? tot : sb.cap);
 }
 
 __global__ void k_s_reset(SplitBuf sb) {
@@ -1549,6 +1570,10 @@ void launch_s_pair_write(const Scene& sc, const Grid& g, const SplitBuf& sb, con
                                               ds);
 }
 void launch_s_reset(const SplitBuf& sb, cudaStream_t s) { k_s_reset<<<1, 1, 0, s>>>(sb); }
+void launch_s_totals(const SplitBuf& sb, const int32_t* spos, const int32_t* sflags, int64_t nflag, const int32_t* poff,
+                     int N, cudaStream_t s) {
+    k_s_totals<<<1, 1, 0, s>>>(sb, spos, sflags, nflag, poff, N);
+}
 void launch_s_apply_warm(const SplitBuf& sb, int gen, int blocks, cudaStream_t s) {
     k_s_apply_warm<<<blocks, NT, 0, s>>>(sb, gen);
 }

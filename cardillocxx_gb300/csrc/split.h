@@ -27,6 +27,10 @@ struct SplitScalars {
     int32_t err;
     int32_t final_acc;                // accumulator holding the final velocities (-1: iters % 3)
     unsigned long long iters_sum;     // batched scenes: sweeps summed over scenes
+    // contact totals found on the device (steps that do not stop for the host to size buffers)
+    int32_t n_static;                 // static contacts (the pair contacts start here)
+    int32_t n_total;                  // all contacts found (may exceed the capacity)
+    int32_t cap_err;                  // the contacts did not fit the buffers: the step is redone
 };
 
 struct SplitParams {
@@ -111,9 +115,13 @@ void launch_s_pair_count(const Scene& sc, const Grid& g, const SplitBuf& sb, con
                          DevScalars* ds, cudaStream_t s);
 void launch_s_static_write(const Scene& sc, const SplitBuf& sb, const int32_t* flags, const int32_t* pos, int gen,
                            const SplitParams& P, cudaStream_t s);
+// base = first pair slot, or taken from the device (SplitScalars::n_static) when base < 0
 void launch_s_pair_write(const Scene& sc, const Grid& g, const SplitBuf& sb, const uint32_t* cell_body,
                          const int32_t* cell_start, const int32_t* cell_end, const int32_t* offsets, int32_t base,
                          int gen, const SplitParams& P, DevScalars* ds, cudaStream_t s);
+// contact totals on the device: n_static, n_total, cap_err and nc_dev = min(total, capacity)
+void launch_s_totals(const SplitBuf& sb, const int32_t* spos, const int32_t* sflags, int64_t nflag, const int32_t* poff,
+                     int N, cudaStream_t s);
 void launch_s_reset(const SplitBuf& sb, cudaStream_t s);
 void launch_s_apply_warm(const SplitBuf& sb, int gen, int blocks, cudaStream_t s);
 // one projected Jacobi sweep (one kernel): reads A_k, scatters M^-1 W^T lambda_{k+1} into A_{k+1},

@@ -71,6 +71,7 @@ typedef struct cdx_config {
     int32_t gpu_use_graph;            /* gpu.graph: capture the solver loop in a CUDA graph (split form) */
     int32_t gpu_autotune;             /* gpu.autotune: pick the contact-sweep launch shape by timing (split form) */
     int32_t gpu_sweep_variant;        /* gpu.sweep_variant: pin launch shape k (split form; -1 = default/autotuned) */
+    int32_t gpu_sync_counts;          /* gpu.sync_counts: every split step stops for the host to size its contact buffers */
 } cdx_config;
 
 /* Scene: dynamic spheres plus static shapes (halfspaces, drums). Bodies of one scene are
@@ -119,6 +120,7 @@ typedef struct cdx_stats {
     int64_t kernel_launches;   /* cdx kernels launched so far */
     int32_t contact_variant;   /* split form: launch shape of the contact sweep chosen by the autotuner */
     int32_t autotune_runs;     /* split form: times the autotuner ran */
+    int32_t redone_steps;      /* split form: steps undone and redone because their contacts outgrew the buffers */
 } cdx_stats;
 
 typedef struct cdx_ctx cdx_ctx;

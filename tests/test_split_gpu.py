@@ -214,3 +214,39 @@ def test_batched_scenes_solver_matches_fp64_and_streaming(gpu):
     e.step(50)
     v = e.state()["vel"]
     assert np.isfinite(v).all() and np.abs(v).max() < 5.0
+
+
+def test_device_counted_steps_match_host_counted_and_redo_on_growth(gpu):
+    # after the first step the split form finds its contact totals on the device; a falling pile
+    # outgrows the buffers several times, so some steps are undone and redone synchronously.
+    # Host-counted steps (gpu.sync_counts) run the same physics.
+    s = scenes.generate("pile_1k")
+    base = dict(scenes.config_for("pile_1k"), **{"gpu.precision": "split", "gpu.contact_capacity": 0.1})
+    a = PhysicsEngine(base).load_scene(s)
+    b = PhysicsEngine(dict(base, **{"gpu.sync_counts": True})).load_scene(s)
+    a.step(1)
+    b.step(1)
+    za, zb = [], []
+    for k in range(10):
+        a.step(40)
+        b.step(40)
+        za.append(a.state()["pos"][:, 2].mean())
+        zb.append(b.state()["pos"][:, 2].mean())
+    assert a.stats()["redone_steps"] >= 1
+    assert b.stats()["redone_steps"] == 0
+    assert a.stats()["num_contacts"] > 1000
+    np.testing.assert_allclose(za, zb, rtol=0, atol=2e-3)
+    # one step from the same state without warm start (the two runs' histories differ): the same
+    # contacts, velocities to FP32 summation order; the second step of a2 counts on the device
+    st = a.state()
+    cold = dict(base, **{"pj.warmstart": False, "gpu.contact_capacity": 8})
+    a2 = PhysicsEngine(cold).load_scene(s)
+    b2 = PhysicsEngine(dict(cold, **{"gpu.sync_counts": True})).load_scene(s)
+    for e in (a2, b2):
+        for _ in range(2):
+            e.set_state(st["pos"], st["quat"], st["vel"], st["omega"])
+            e.step(1)
+    ca, cb = a2.contacts(), b2.contacts()
+    assert np.array_equal(ca["id_a"], cb["id_a"]) and np.array_equal(ca["id_b"], cb["id_b"])
+    vs = np.abs(st["vel"]).max() + 9.81e-3
+    assert np.abs(a2.state()["vel"] - b2.state()["vel"]).max() <= 1e-4 * vs
