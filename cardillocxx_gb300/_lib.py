@@ -96,6 +96,7 @@ class CdxStats(C.Structure):
         ("contact_variant", C.c_int32),
         ("autotune_runs", C.c_int32),
         ("redone_steps", C.c_int32),
+        ("graph_steps", C.c_int64),
     ]
 
 

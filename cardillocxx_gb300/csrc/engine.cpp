@@ -634,6 +634,7 @@ void Engine::fill_stats(cdx_stats* s) {
     s->contact_variant = split_variant();
     s->autotune_runs = split_tune_runs();
     s->redone_steps = split_redos();
+    s->graph_steps = split_graph_steps();
 }
 
 double Engine::solve_bytes_per_iter() const {

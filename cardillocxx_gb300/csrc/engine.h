@@ -96,6 +96,7 @@ struct Engine {
     int split_variant() const;
     int split_tune_runs() const;
     int split_redos() const;
+    int64_t split_graph_steps() const;
     int time_sweeps(int n, double* msc, double* msb, double* bc, double* bb);
 };
 

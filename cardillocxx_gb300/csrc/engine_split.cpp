@@ -50,6 +50,15 @@ struct SplitState {
     double* ssnap = nullptr;  // 13 S: the same for the statics
     bool force_sync = false;
     int syncs = 0, redos = 0;
+    // device-counted steps captured whole into a CUDA graph (one per generation), replayed while
+    // the buffers, the solver shape and the cooperative plan stay the same
+    cudaGraphExec_t sg_exec[2] = {nullptr, nullptr};
+    long long sg_key[2][8] = {{0}};
+    int64_t sg_launches[2] = {0, 0};  // kernels in each captured step
+    bool sg_failed = false;
+    CoopPlan gplan;
+    bool gplan_ok = false;
+    int64_t graph_steps = 0;
 };
 }  // namespace cdx
 
@@ -59,7 +68,15 @@ static int salloc(Engine& E, void** p, size_t bytes, const char* what) {
     return st;
 }
 
+static void destroy_step_graphs(SplitState* S) {
+    for (int g = 0; g < 2; ++g) {
+        if (S->sg_exec[g]) cudaGraphExecDestroy(S->sg_exec[g]);
+        S->sg_exec[g] = nullptr;
+    }
+}
+
 static void destroy_graphs(SplitState* S) {
+    destroy_step_graphs(S);
     for (int g = 0; g < 2; ++g) {
         if (S->exec[g]) cudaGraphExecDestroy(S->exec[g]);
         if (S->graph[g]) cudaGraphDestroy(S->graph[g]);
@@ -262,6 +279,72 @@ int Engine::step_split() {
                        !tune_due(S->prev_count);
     S->force_sync = false;
     if (async) {
+        // the warm-start layout of the last step is read on the device
+        if (cfg.pj_warmstart) P.prev_count = -1;
+        P.prev_n_static = -1;
+    }
+    // A device-counted step whose solver is the cooperative or the batched-scenes kernel is
+    // captured whole (snapshot to the final scalars) into a CUDA graph and replayed.
+    const bool multi0 = sc.nscenes > 1 && S->scene_nbmax > 0 && S->scene_nbmax <= 3584;
+    const bool scenes0 = async && multi0 && (pinned >= 0 ? split_variant_is_scenes(pinned) : S->scene_best >= 0);
+    bool use_graph = async && cfg.gpu_use_graph && !timing && !S->sg_failed;
+    if (use_graph && !scenes0) {
+        // the cooperative plan is kept while it holds the estimate (the kernel balances its blocks
+        // by the true count), so the graph stays valid across steps
+        const int64_t est = (int64_t)S->prev_count + S->prev_count / 16 + 64;
+        if (!split_variant_is_coop(S->variant)) {
+            use_graph = false;
+        } else if (!(S->gplan_ok && (int64_t)S->gplan.cpb * S->gplan.grid >= est)) {
+            S->gplan_ok = split_coop_plan(S->variant, est + est / 4, sc.N, S->sms, &S->gplan) ||
+                          split_coop_plan(S->variant, est, sc.N, S->sms, &S->gplan);
+            if (!S->gplan_ok) use_graph = false;
+        }
+    }
+    const long long gkey[8] = {(long long)sb.cap, (long long)S->variant, scenes0 ? 1 : 0, S->gplan.cpb, S->gplan.bpb,
+                               S->gplan.vf, S->gplan.smem, (long long)cfg.pj_warmstart};
+    bool capturing = false;
+    int64_t launches0 = launches;
+    int64_t n_static = 0;
+    bool coop = false, scenes = false, multi = false;
+    const int nsv = split_num_scenes_variants();
+    if (use_graph && S->sg_exec[gen] && std::memcmp(gkey, S->sg_key[gen], sizeof(gkey)) == 0) {
+        // replay the captured step
+        if ((st = cuda_check(cudaGraphLaunch(S->sg_exec[gen], stream), "step graph launch"))) return st;
+        ++S->graph_steps;
+        ++S->syncs;
+        S->nc = S->prev_count;
+        scenes = scenes0;
+        coop = !scenes0;
+        launches += S->sg_launches[gen];
+        goto step_issued;
+    }
+    if (use_graph) {
+        if (S->sg_exec[gen]) {
+            cudaGraphExecDestroy(S->sg_exec[gen]);
+            S->sg_exec[gen] = nullptr;
+        }
+        if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeRelaxed) == cudaSuccess)
+            capturing = true;
+        else {
+            cudaGetLastError();
+            S->sg_failed = true;
+        }
+    }
+  {
+    // ends a capture left open by an early error return
+    struct CaptureGuard {
+        cudaStream_t s;
+        bool* on;
+        ~CaptureGuard() {
+            if (*on) {
+                cudaGraph_t g = nullptr;
+                cudaStreamEndCapture(s, &g);
+                if (g) cudaGraphDestroy(g);
+                cudaGetLastError();
+            }
+        }
+    } guard{stream, &capturing};
+    if (async) {
         cudaMemcpyAsync(S->snap, sc.B, sizeof(double) * 13 * (size_t)N, cudaMemcpyDeviceToDevice, stream);
         if (sc.S > 0)
             cudaMemcpyAsync(S->ssnap, sc.St, sizeof(double) * 13 * (size_t)sc.S, cudaMemcpyDeviceToDevice, stream);
@@ -286,7 +369,7 @@ int Engine::step_split() {
     launch_s_pair_count(sc, grid, sb, cell_val_out, cell_start, cell_end, pcount, P, ds, stream);
     if ((st = cuda_check(exclusive_scan(tmp, tmp_bytes, pcount, poff, N + 1, stream), "scan"))) return st;
     launches += 3;
-    int64_t n_static = 0, n_pair = 0;
+    int64_t n_pair = 0;
     if (async) {
         launch_s_totals(sb, spos, sflags, nflag, poff, N, stream);
         S->nc = S->prev_count;  // an estimate for the launch shapes; the device holds the count
@@ -320,8 +403,8 @@ int Engine::step_split() {
         }
     }
     if (timing) cudaEventRecord(ev[1], stream);
-    // x0 = v_free + M^-1 W^T lambda_warm
-    const int cblocks = split_grid_blocks(std::max(S->nc, 1), S->sms);
+    // x0 = v_free + M^-1 W^T lambda_warm (a captured step sizes its grids by the capacity)
+    const int cblocks = split_grid_blocks(capturing ? std::max<int64_t>(sb.cap, 1) : std::max(S->nc, 1), S->sms);
     launch_s_reset(sb, stream);
     launch_s_apply_warm(sb, gen, cblocks, stream);
     launches += 2;
@@ -330,9 +413,8 @@ int Engine::step_split() {
     // batched scenes: every scene solved by its own block. Untuned, successive steps try every
     // scenes shape and then the regular solver (one step for its own tuning, one timed), one full
     // solve each, and the fastest is kept.
-    const int nsv = split_num_scenes_variants();
-    const bool multi = S->nc > 0 && sc.nscenes > 1 && S->scene_nbmax > 0 && S->scene_nbmax <= 3584;
-    bool scenes = false;
+    multi = S->nc > 0 && multi0;
+    scenes = false;
     int scene_v = -1;
     S->scene_timing = -1;
     if (multi) {
@@ -442,11 +524,23 @@ int Engine::step_split() {
     }
     CoopPlan plan;
     const int64_t plan_nc = async ? (int64_t)S->nc + S->nc / 16 + 64 : (int64_t)S->nc;
-    const bool coop = !scenes && S->nc > 0 && split_variant_is_coop(S->variant) &&
-                      split_coop_plan(S->variant, plan_nc, sc.N, S->sms, &plan);
+    if (capturing && !scenes && split_variant_is_coop(S->variant)) plan = S->gplan;
+    coop = !scenes && S->nc > 0 && split_variant_is_coop(S->variant) &&
+           (capturing ? S->gplan_ok : split_coop_plan(S->variant, plan_nc, sc.N, S->sms, &plan));
     if (S->nc > 0 && !solved && coop) {
         st = launch_s_solve_coop(sb, gen, (float)cfg.pj_alpha, S->variant, plan, maxit, (float)cfg.gpu_residual_tol,
                                  maxit, cfg.gpu_check_every, stream);
+        if (st != 0 && capturing) {
+            // a cooperative launch that cannot be captured: nothing of the step ran; end the capture
+            // and issue steps directly from now on
+            cudaGraph_t g = nullptr;
+            cudaStreamEndCapture(stream, &g);
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            capturing = false;
+            S->sg_failed = true;
+            return step_split();
+        }
         S->last_variant = S->variant;
         if ((st = cuda_check((cudaError_t)st, "cooperative launch"))) return st;
         ++launches;
@@ -490,12 +584,33 @@ int Engine::step_split() {
     launch_s_drift(sc, th * dt, stream);
     launches += 5;
     if (timing) cudaEventRecord(ev[4], stream);
+    launch_s_end_step(sb, ds, stream);
+    ++launches;
     cudaMemcpyAsync(S->h_ss, sb.ss, sizeof(SplitScalars), cudaMemcpyDeviceToHost, stream);
-    int32_t pair_overflow = 0;
-    if (async) cudaMemcpyAsync(&pair_overflow, &ds->overflow, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+    if (capturing) {
+        cudaGraph_t g = nullptr;
+        capturing = false;
+        cudaError_t e = cudaStreamEndCapture(stream, &g);
+        cudaGraphExec_t x = nullptr;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&x, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            // the step could not be captured (nothing of it ran): issue it directly from now on
+            cudaGetLastError();
+            S->sg_failed = true;
+            return step_split();
+        }
+        S->sg_exec[gen] = x;
+        std::memcpy(S->sg_key[gen], gkey, sizeof(gkey));
+        S->sg_launches[gen] = launches - launches0;
+        if ((st = cuda_check(cudaGraphLaunch(x, stream), "step graph launch"))) return st;
+        ++S->graph_steps;
+    }
+  }
+step_issued:
     if ((st = cuda_check(cudaStreamSynchronize(stream), "split step"))) return st;
     if ((st = cuda_check(cudaGetLastError(), "split launch"))) return st;
-    if (pair_overflow) return fail(CDX_ERR_OVERFLOW, "a sphere touches more than 64 higher-index spheres");
+    if (S->h_ss->pair_overflow) return fail(CDX_ERR_OVERFLOW, "a sphere touches more than 64 higher-index spheres");
     if (async && (S->h_ss->cap_err || S->h_ss->err == 4)) {
         // undo the step (state from the snapshot; everything else is rebuilt) and redo it synchronously
         cudaMemcpyAsync(sc.B, S->snap, sizeof(double) * 13 * (size_t)N, cudaMemcpyDeviceToDevice, stream);
@@ -504,6 +619,7 @@ int Engine::step_split() {
         if ((st = cuda_check(cudaStreamSynchronize(stream), "undo step"))) return st;
         ++S->redos;
         S->force_sync = true;
+        if (S->h_ss->err == 4) S->gplan_ok = false;
         return step_split();
     }
     if (S->h_ss->err) return fail(CDX_ERR_TIMEOUT, "cooperative solve: a grid barrier timed out");
@@ -682,6 +798,7 @@ int Engine::time_sweeps(int n, double* msc, double* msb, double* bc, double* bb)
 int Engine::split_variant() const { return split ? split->last_variant : -1; }
 int Engine::split_tune_runs() const { return split ? split->tune_runs : 0; }
 int Engine::split_redos() const { return split ? split->redos : 0; }
+int64_t Engine::split_graph_steps() const { return split ? split->graph_steps : 0; }
 
 extern "C" int cdx_selftest_nr64(cdx_ctx* ctx, int32_t n, const double* x, double* rcp, double* rsq) {
     if (!ctx || n < 0 || (n > 0 && (!x || !rcp || !rsq))) return CDX_ERR_ARG;

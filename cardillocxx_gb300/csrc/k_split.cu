@@ -292,7 +292,8 @@ __device__ __forceinline__ void finish_contact32(const Scene& sc, SplitBuf& sb, 
     const uint32_t idb = (uint32_t)(sc.S + b);
     const unsigned long long key = ((unsigned long long)ida << 32) | idb;
     float4 lam0 = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (P.prev_count > 0) warm_start(sb, gen, prev_lo, prev_hi, key, pt, P.match2, lam0);
+    if ((P.prev_count >= 0 ? P.prev_count : sb.ss->prev_count_dev) > 0)
+        warm_start(sb, gen, prev_lo, prev_hi, key, pt, P.match2, lam0);
     if (mu == 0.f) { lam0.y = 0.f; lam0.z = 0.f; }
     const bool has_bias = bias.x != 0.f || bias.y != 0.f || bias.z != 0.f;
     sb.rec0[c] = make_float4(n.x, n.y, n.z, has_bias ? -mu - 0.f : mu);
@@ -322,7 +323,7 @@ __global__ void k_s_static_write(Scene sc, SplitBuf sb, const int32_t* flags, co
         const float3 wv = f3(sb.st_v[st]), ww = f3(sb.st_w[st]), wp = f3(sb.st_pt[st]);
         const bool moving = (wv.x != 0.f || wv.y != 0.f || wv.z != 0.f || ww.x != 0.f || ww.y != 0.f || ww.z != 0.f);
         int plo = 0, phi = 0;
-        if (P.prev_count > 0 && P.prev_sflags[slot]) {
+        if ((P.prev_count >= 0 ? P.prev_count : sb.ss->prev_count_dev) > 0 && P.prev_sflags[slot]) {
             plo = P.prev_spos[slot];
             phi = plo + 1;
         }
@@ -405,9 +406,10 @@ __global__ void k_s_pairs(Scene sc, Grid gr, SplitBuf sb, const uint32_t* cell_b
     }
     const int c0 = (base >= 0 ? base : sb.ss->n_static) + offsets[i];
     int plo = 0, phi = 0;
-    if (P.prev_count > 0) {
-        plo = P.prev_n_static + P.prev_poff[i];
-        phi = P.prev_n_static + P.prev_poff[i + 1];
+    if ((P.prev_count >= 0 ? P.prev_count : sb.ss->prev_count_dev) > 0) {
+        const int pns = P.prev_count >= 0 ? P.prev_n_static : sb.ss->prev_n_static_dev;
+        plo = pns + P.prev_poff[i];
+        phi = pns + P.prev_poff[i + 1];
     }
     const float mu_a = (float)sc.bf(BF_MU)[i];
     const float rn_a = (float)sc.bf(BF_RN)[i], rt_a = (float)sc.bf(BF_RT)[i];
@@ -1107,6 +1109,13 @@ __global__ void k_s_totals(SplitBuf sb, const int32_t* spos, const int32_t* sfla
     *sb.nc_dev = (int32_t)(tot < sb.cap ? tot : sb.cap);
 }
 
+__global__ void k_s_end_step(SplitBuf sb, const DevScalars* ds) {
+    SplitScalars* ss = sb.ss;
+    ss->prev_count_dev = *sb.nc_dev;
+    ss->prev_n_static_dev = ss->n_static;
+    ss->pair_overflow = ds->overflow;
+}
+
 __global__ void k_s_reset(SplitBuf sb) {
     SplitScalars* ss = sb.ss;
     ss->done = (*sb.nc_dev == 0) ? 1 : 0;
@@ -1570,6 +1579,9 @@ void launch_s_pair_write(const Scene& sc, const Grid& g, const SplitBuf& sb, con
                                               ds);
 }
 void launch_s_reset(const SplitBuf& sb, cudaStream_t s) { k_s_reset<<<1, 1, 0, s>>>(sb); }
+void launch_s_end_step(const SplitBuf& sb, const DevScalars* ds, cudaStream_t s) {
+    k_s_end_step<<<1, 1, 0, s>>>(sb, ds);
+}
 void launch_s_totals(const SplitBuf& sb, const int32_t* spos, const int32_t* sflags, int64_t nflag, const int32_t* poff,
                      int N, cudaStream_t s) {
     k_s_totals<<<1, 1, 0, s>>>(sb, spos, sflags, nflag, poff, N);

@@ -31,6 +31,11 @@ struct SplitScalars {
     int32_t n_static;                 // static contacts (the pair contacts start here)
     int32_t n_total;                  // all contacts found (may exceed the capacity)
     int32_t cap_err;                  // the contacts did not fit the buffers: the step is redone
+    // the last completed step's contact layout for the warm start, kept on the device for steps
+    // launched from a CUDA graph (their parameters are fixed at capture)
+    int32_t prev_count_dev;
+    int32_t prev_n_static_dev;
+    int32_t pair_overflow;            // copy of the narrow phase's neighbour-overflow flag
 };
 
 struct SplitParams {
@@ -39,7 +44,7 @@ struct SplitParams {
     float match2;
     int combine;
     int friction_enable;
-    int prev_count;
+    int prev_count;  // < 0: read SplitScalars::prev_count_dev / prev_n_static_dev on the device
     // previous step's contact layout, for an O(1) warm-start lookup: static contact of slot k was
     // contact prev_spos[k] when prev_sflags[k]; pair contacts of owner i were
     // [prev_n_static + prev_poff[i], prev_n_static + prev_poff[i+1])
@@ -123,6 +128,8 @@ void launch_s_pair_write(const Scene& sc, const Grid& g, const SplitBuf& sb, con
 void launch_s_totals(const SplitBuf& sb, const int32_t* spos, const int32_t* sflags, int64_t nflag, const int32_t* poff,
                      int N, cudaStream_t s);
 void launch_s_reset(const SplitBuf& sb, cudaStream_t s);
+// end of a step: the warm-start layout for the next step and the neighbour-overflow flag, on the device
+void launch_s_end_step(const SplitBuf& sb, const DevScalars* ds, cudaStream_t s);
 void launch_s_apply_warm(const SplitBuf& sb, int gen, int blocks, cudaStream_t s);
 // one projected Jacobi sweep (one kernel): reads A_k, scatters M^-1 W^T lambda_{k+1} into A_{k+1},
 // clears A_{k+2}; its last block runs the stop rule

@@ -121,6 +121,7 @@ typedef struct cdx_stats {
     int32_t contact_variant;   /* split form: launch shape of the contact sweep chosen by the autotuner */
     int32_t autotune_runs;     /* split form: times the autotuner ran */
     int32_t redone_steps;      /* split form: steps undone and redone because their contacts outgrew the buffers */
+    int64_t graph_steps;       /* split form: steps replayed whole from a captured CUDA graph */
 } cdx_stats;
 
 typedef struct cdx_ctx cdx_ctx;
