@@ -59,6 +59,10 @@ class CdxConfig(C.Structure):
         ("gpu_autotune", C.c_int32),
         ("gpu_sweep_variant", C.c_int32),
         ("gpu_sync_counts", C.c_int32),
+        ("pj_nesterov", C.c_int32),
+        ("pj_nesterov_beta_threshold", C.c_double),
+        ("pj_nesterov_restart_limit", C.c_int32),
+        ("pj_chebyshev", C.c_int32),
     ]
 
 

@@ -121,6 +121,14 @@ struct DevScalars {
     int32_t pad[4];
 };
 
+// state of the accelerated projected Jacobi loops (device)
+struct AccelState {
+    double thk, err_prev, coef, omega, rho, rho2, lambda;
+    double sum_err, sum_dot;  // outputs of the fixed-order reductions
+    int32_t restarts, disabled, mode, nonfinite, power_stop;
+};
+enum AccelReduce : int { ACC_VELRES = 0, ACC_NORM2 = 1, ACC_DOT = 2, ACC_ONES = 3 };
+
 struct Incidence {
     int64_t cap = 0;
     uint32_t* key_in = nullptr;
@@ -167,6 +175,21 @@ void launch_sweep_body64(const Scene& sc, const Contacts& C, const Incidence& in
                          double tol_rel, int want_velres, DevScalars* ds, cudaStream_t s);
 void launch_check(DevScalars* ds, int iter, double residual_tol, int nv, int check_vel, cudaStream_t s);
 void launch_final_residual(DevScalars* ds, cudaStream_t s);
+// accelerated loops (Nesterov, Chebyshev) of the plain FP64 method
+int accel_chunks(int N);
+void launch_accel_init(AccelState* st, cudaStream_t s);
+void launch_accel_reduce(int N, int op, const double* a, const double* b, const double* c, double tol_rel,
+                         double tol_abs, double* part, AccelState* st, double* out, const DevScalars* ds,
+                         cudaStream_t s);
+void launch_accel_copy(double* xd, const double* xs, int64_t nx, double* ld, const double* ls, int64_t nl,
+                       const DevScalars* ds, cudaStream_t s);
+void launch_nesterov_step(AccelState* st, DevScalars* ds, int nv, double beta_threshold, int restart_limit, double* xy,
+                          double* xk, const double* xk1, int64_t nx, double* py, double* pk, const double* pk1,
+                          int64_t nl, cudaStream_t s);
+void launch_chebyshev_step(AccelState* st, DevScalars* ds, int nv, int iter, const double* x, double* xk, double* xk1,
+                           int64_t nx, const double* lam, double* pk, double* pk1, int64_t nl, cudaStream_t s);
+void launch_spectral_radius(const Scene& sc, Contacts& C, const Incidence& inc, int nc, double* v, double* Mv,
+                            double* part, AccelState* st, cudaStream_t s);
 void launch_writeback64(const Scene& sc, const double* x, cudaStream_t s);
 void launch_trace64(const Contacts& C, int gen, int nc, const int32_t* fl_scan, const int32_t* isfl, double* out,
                     cudaStream_t s);

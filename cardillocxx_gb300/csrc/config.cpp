@@ -93,6 +93,10 @@ int cdx_config_default(cdx_config* c) {
     c->gpu_autotune = 1;
     c->gpu_sweep_variant = -1;
     c->gpu_sync_counts = 0;
+    c->pj_nesterov = 0;
+    c->pj_nesterov_beta_threshold = 1.0;
+    c->pj_nesterov_restart_limit = 10000;
+    c->pj_chebyshev = 0;
     return CDX_OK;
 }
 
@@ -174,6 +178,14 @@ int cdx_config_set(cdx_config* c, const char* key_c, const char* val_c) {
         if (as_int(val, &i)) c->gpu_sweep_variant = std::max(-1, i);
     } else if (key == "gpu.sync_counts") {
         c->gpu_sync_counts = as_bool(val);
+    } else if (key_is(key, "pj.nesterov")) {
+        c->pj_nesterov = as_bool(val);
+    } else if (key_is(key, "pj.nesterov_beta_threshold")) {
+        if (as_double(val, &d)) c->pj_nesterov_beta_threshold = d;
+    } else if (key_is(key, "pj.nesterov_restart_limit")) {
+        if (as_int(val, &i)) c->pj_nesterov_restart_limit = std::max(0, i);
+    } else if (key_is(key, "pj.chebyshev")) {
+        c->pj_chebyshev = as_bool(val);
     }
     return CDX_OK;  // unknown keys are ignored, as in the reference
 }

@@ -439,6 +439,90 @@ int Engine::setup64() {
     return CDX_OK;
 }
 
+int Engine::ensure_accel() {
+    const int64_t nx = 6 * (int64_t)sc.N, nl = 3 * C.cap;
+    if (acc_st && nx == acc_nx && nl == acc_nl) return CDX_OK;
+    double** bufs[] = {&acc_xk, &acc_xk1, &acc_xy, &acc_pk, &acc_pk1, &acc_py, &acc_part};
+    for (auto b : bufs)
+        if (*b) {
+            dfree(*b);
+            *b = nullptr;
+        }
+    if (acc_st) {
+        dfree(acc_st);
+        acc_st = nullptr;
+    }
+    int st;
+    for (int k = 0; k < 3; ++k)
+        if ((st = dalloc((void**)bufs[k], sizeof(double) * std::max<int64_t>(nx, 1), "accelerated loop"))) return st;
+    for (int k = 3; k < 6; ++k)
+        if ((st = dalloc((void**)bufs[k], sizeof(double) * std::max<int64_t>(nl, 1), "accelerated loop"))) return st;
+    if ((st = dalloc((void**)&acc_part, sizeof(double) * std::max(accel_chunks(sc.N), 1), "accelerated loop"))) return st;
+    if ((st = dalloc((void**)&acc_st, sizeof(AccelState), "accelerated loop"))) return st;
+    acc_nx = nx;
+    acc_nl = nl;
+    return CDX_OK;
+}
+
+// nesterov_loop / chebyshev_loop (projected_jacobi.cpp:379-449, 179-222) of ProjectedJacobiSolver,
+// plain FP64: the same sweeps as the standard loop, with the extrapolations, restarts and stop
+// tests of the reference run as small device kernels so the loop needs no host decisions; the
+// host polls the stop flag every gpu.check_every sweeps.
+int Engine::solve64_accel() {
+    const int N = sc.N, nv = 6 * N;
+    int st;
+    if ((st = ensure_accel())) return st;
+    const int64_t nx = acc_nx, nl = acc_nl;
+    double* lam = C.lam[gen];
+    const bool nes = cfg.pj_nesterov != 0;
+    cudaMemsetAsync(ds, 0, sizeof(DevScalars), stream);
+    launch_accel_init(acc_st, stream);
+    if (!nes) launch_spectral_radius(sc, C, inc, nc, acc_xy, acc_xk, acc_part, acc_st, stream);
+    // xk = xk1 (= xy) = x0, pk = pk1 (= py) = lambda0
+    launch_accel_copy(acc_xk, x, nx, acc_pk, lam, nl, nullptr, stream);
+    launch_accel_copy(acc_xk1, x, nx, acc_pk1, lam, nl, nullptr, stream);
+    launch_accel_copy(acc_xy, x, nx, acc_py, lam, nl, nullptr, stream);
+    const int maxit = std::max(1, cfg.pj_max_iterations);
+    const int every = std::max(1, cfg.gpu_check_every);
+    int it = 0;
+    for (; it < maxit; ++it) {
+        // the sweep starts from y (Nesterov) or from the extrapolated iterate xk1 (Chebyshev)
+        if (nes)
+            launch_accel_copy(x, acc_xy, nx, lam, acc_py, nl, ds, stream);
+        else
+            launch_accel_copy(x, acc_xk1, nx, lam, acc_pk1, nl, ds, stream);
+        launch_sweep_contact64(sc, C, gen, nc, x, ds, 0, stream);
+        launch_sweep_body64(sc, C, inc, x, 0.0, 0.0, 0, ds, stream);
+        launch_check(ds, it, 0.0, nv, 0, stream);  // res_last and the sweep count
+        if (nes) {
+            launch_accel_copy(acc_xk1, x, nx, acc_pk1, lam, nl, ds, stream);
+            launch_accel_reduce(N, ACC_VELRES, acc_xk1, acc_xy, nullptr, cfg.pj_tol_rel, cfg.pj_tol_abs, acc_part,
+                                acc_st, &acc_st->sum_err, ds, stream);
+            launch_accel_reduce(N, ACC_DOT, acc_xy, acc_xk1, acc_xk, 0.0, 0.0, acc_part, acc_st, &acc_st->sum_dot,
+                                ds, stream);
+            launch_nesterov_step(acc_st, ds, nv, cfg.pj_nesterov_beta_threshold, cfg.pj_nesterov_restart_limit, acc_xy,
+                                 acc_xk, acc_xk1, nx, acc_py, acc_pk, acc_pk1, nl, stream);
+            launches += 9;
+        } else {
+            launch_accel_reduce(N, ACC_VELRES, x, acc_xk1, nullptr, cfg.pj_tol_rel, cfg.pj_tol_abs, acc_part, acc_st,
+                                &acc_st->sum_err, ds, stream);
+            launch_chebyshev_step(acc_st, ds, nv, it, x, acc_xk, acc_xk1, nx, lam, acc_pk, acc_pk1, nl, stream);
+            launches += 7;
+        }
+        if ((it + 1) % every == 0 && it + 1 < maxit) {
+            cudaMemcpyAsync(&hs->done, &ds->done, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+            if ((st = cuda_check(cudaStreamSynchronize(stream), "poll"))) return st;
+            if (hs->done) break;
+        }
+    }
+    // the result is the loop's current iterate (xk1, pk1), as in the reference
+    launch_accel_copy(x, acc_xk1, nx, lam, acc_pk1, nl, nullptr, stream);
+    launch_sweep_contact64(sc, C, gen, nc, x, ds, 1, stream);
+    launch_final_residual(ds, stream);
+    launches += 3;
+    return CDX_OK;
+}
+
 int Engine::solve64() {
     const int N = sc.N;
     int st;
@@ -449,6 +533,7 @@ int Engine::solve64() {
     last_res = 0;
     last_res_final = 0;
     if (nc == 0) return CDX_OK;
+    if ((cfg.pj_nesterov || cfg.pj_chebyshev) && !trace_next) return solve64_accel();
     cudaMemsetAsync(ds, 0, sizeof(DevScalars), stream);
     const int maxit = std::max(1, cfg.pj_max_iterations);
     const bool check_vel = !(cfg.pj_tol_abs == 0.0 && cfg.pj_tol_rel == 0.0);

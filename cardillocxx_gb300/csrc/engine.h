@@ -47,6 +47,13 @@ struct Engine {
     cdx::Contacts C;
     cdx::Incidence inc;
     cdx::DevScalars* ds = nullptr;
+    // accelerated loops: iterate copies (6N velocities, 3 cap impulses), reduction partials, state
+    double *acc_xk = nullptr, *acc_xk1 = nullptr, *acc_xy = nullptr;
+    double *acc_pk = nullptr, *acc_pk1 = nullptr, *acc_py = nullptr, *acc_part = nullptr;
+    cdx::AccelState* acc_st = nullptr;
+    int64_t acc_nx = 0, acc_nl = 0;
+    int ensure_accel();
+    int solve64_accel();
     cdx::DevScalars* hs = nullptr;  // pinned mirror
     void* tmp = nullptr;
     size_t tmp_bytes = 0;

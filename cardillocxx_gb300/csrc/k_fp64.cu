@@ -688,6 +688,238 @@ __global__ void k_check(DevScalars* ds, int iter, double residual_tol, int nv, i
     ds->velres = 0.0;
 }
 
+// ---- accelerated loops (projected_jacobi.cpp:179-222 Chebyshev, :379-449 Nesterov)
+// Reductions run in a fixed order that the oracle uses too: sums over chunks of RED_CHUNK
+// consecutive entries of the stacked velocity vector (entry 6 i + k = component k of body i, the
+// reference's layout), each chunk left to right, then the chunk sums left to right.
+constexpr int RED_CHUNK = 256;
+__device__ __forceinline__ double stacked(const double* v, int N, int j) { return v[(size_t)(j % 6) * N + j / 6]; }
+
+__global__ void k_chunk_partials(int N, int op, const double* a, const double* b, const double* c, double tol_rel,
+                                 double tol_abs, double* part, AccelState* st, const DevScalars* ds) {
+    if (ds && *(volatile const int32_t*)&ds->done) return;
+    const int nv = 6 * N;
+    const int nch = (nv + RED_CHUNK - 1) / RED_CHUNK;
+    const int ch = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ch >= nch) return;
+    const int j0 = ch * RED_CHUNK, j1 = min(nv, j0 + RED_CHUNK);
+    double s = 0.0;
+    bool finite = true;
+    for (int j = j0; j < j1; ++j) {
+        double t;
+        if (op == ACC_VELRES) {
+            const double x = stacked(a, N, j), xp = stacked(b, N, j);
+            const double q = smax(fabs(x), fabs(xp)) * tol_rel + tol_abs;
+            const double d = (x - xp) / q;
+            t = d * d;
+            finite = finite && isfinite(x);
+        } else if (op == ACC_NORM2) {
+            const double x = stacked(a, N, j);
+            t = x * x;
+        } else if (op == ACC_DOT) {
+            const double y = stacked(a, N, j), x1 = stacked(b, N, j), x0 = stacked(c, N, j);
+            t = (y - x1) * (x1 - x0);
+        } else {
+            t = 1.0;
+        }
+        s = s + t;
+    }
+    part[ch] = s;
+    if (!finite) st->nonfinite = 1;
+}
+
+__global__ void k_chunk_total(const double* part, int nch, double* out, const DevScalars* ds) {
+    if (ds && *(volatile const int32_t*)&ds->done) return;
+    double tot = 0.0;
+    for (int k = 0; k < nch; ++k) tot = tot + part[k];
+    *out = tot;
+}
+
+// dst = src for the velocity (6 x N, field-major) and impulse (3 x cap) vectors, unless done
+__global__ void k_accel_copy(double* xd, const double* xs, int64_t nx, double* ld, const double* ls, int64_t nl,
+                             const DevScalars* ds) {
+    if (ds && *(volatile const int32_t*)&ds->done) return;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nx + nl; i += (int64_t)gridDim.x * blockDim.x) {
+        if (i < nx)
+            xd[i] = xs[i];
+        else
+            ld[i - nx] = ls[i - nx];
+    }
+}
+
+// Nesterov: err and the restart tests (nesterov_loop), then the momentum coefficient
+__global__ void k_nesterov_decide(AccelState* st, DevScalars* ds, int nv, double beta_threshold, int restart_limit) {
+    if (ds->done) return;
+    const double err = 1.0 / sqrt((double)nv) * sqrt(st->sum_err);
+    if (err <= 1.0) {
+        ds->done = 1;
+        return;
+    }
+    const double thk = st->thk;
+    const double thk1 = 0.5 * (1.0 + sqrt(4.0 * thk * thk + 1.0));
+    const double betak1 = (thk - 1.0) / thk1;
+    bool restart = false;
+    if (!isfinite(err)) {
+        restart = true;
+    } else if (st->err_prev < INFINITY && err > 1.05 * st->err_prev) {
+        restart = true;
+    } else if (betak1 > beta_threshold) {
+        restart = true;
+    } else if (!isfinite(betak1) || betak1 < 0.0 || betak1 > 1.0) {
+        restart = true;
+    } else if (st->sum_dot > 0.0) {
+        restart = true;
+    }
+    if (restart) {
+        st->mode = 0;
+        st->thk = 1.0;
+        if (++st->restarts >= restart_limit) st->disabled = 1;
+    } else if (st->disabled) {
+        st->mode = 0;
+        st->thk = 1.0;
+    } else {
+        st->mode = 1;
+        st->coef = betak1;
+        st->thk = thk1;
+    }
+    st->err_prev = err;
+}
+
+// xy = mode ? xk1 + beta (xk1 - xk) : xk1;  xk = xk1   (and the same for the impulses)
+__global__ void k_nesterov_update(double* xy, double* xk, const double* xk1, int64_t nx, double* py, double* pk,
+                                  const double* pk1, int64_t nl, const AccelState* st, const DevScalars* ds) {
+    if (*(volatile const int32_t*)&ds->done) return;
+    const int mode = st->mode;
+    const double b = st->coef;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nx + nl; i += (int64_t)gridDim.x * blockDim.x) {
+        double *y, *k0;
+        const double* k1;
+        int64_t q;
+        if (i < nx) {
+            y = xy; k0 = xk; k1 = xk1; q = i;
+        } else {
+            y = py; k0 = pk; k1 = pk1; q = i - nx;
+        }
+        y[q] = mode ? k1[q] + b * (k1[q] - k0[q]) : k1[q];
+        k0[q] = k1[q];
+    }
+}
+
+// Chebyshev: err, then the next omega or the fallback to a plain step (chebyshev_loop)
+__global__ void k_chebyshev_decide(AccelState* st, DevScalars* ds, int nv, int iter) {
+    if (ds->done) return;
+    const double err = 1.0 / sqrt((double)nv) * sqrt(st->sum_err);
+    if (err <= 1.0) {
+        ds->done = 1;
+        return;
+    }
+    double omega_next = (iter == 0) ? (1.0 / (1.0 - st->rho2 * 0.5)) : (1.0 / (1.0 - (st->rho2 * 0.25) * st->omega));
+    if (!isfinite(omega_next) || omega_next <= 0.0 || st->nonfinite) {
+        st->mode = 0;
+        omega_next = 1.0;
+    } else {
+        st->mode = 1;
+    }
+    st->coef = omega_next;
+    st->omega = omega_next;
+    st->nonfinite = 0;
+}
+
+// t = mode ? omega (x - xk) + xk : x;  xk = xk1;  xk1 = t   (and the same for the impulses)
+__global__ void k_chebyshev_update(const double* x, double* xk, double* xk1, int64_t nx, const double* lam, double* pk,
+                                   double* pk1, int64_t nl, const AccelState* st, const DevScalars* ds) {
+    if (*(volatile const int32_t*)&ds->done) return;
+    const int mode = st->mode;
+    const double w = st->coef;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nx + nl; i += (int64_t)gridDim.x * blockDim.x) {
+        const double* cur;
+        double *k0, *k1;
+        int64_t q;
+        if (i < nx) {
+            cur = x; k0 = xk; k1 = xk1; q = i;
+        } else {
+            cur = lam; k0 = pk; k1 = pk1; q = i - nx;
+        }
+        const double t = mode ? w * (cur[q] - k0[q]) + k0[q] : cur[q];
+        k0[q] = k1[q];
+        k1[q] = t;
+    }
+}
+
+// Power iteration of estimateSpectralRadius (projected_jacobi.cpp:154-177): delta = R W v per
+// row (the sweep's row product without bias), then M v = v - S^-1 W^T delta per body
+__global__ void k_linear_contact64(Scene sc, Contacts C, int nc, const double* v) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    const int64_t cap = C.cap;
+    const int N = sc.N;
+    const int a = C.a[c], b = C.b[c];
+    const int nr = (C.flags[c] & CF_FRICTIONAL) ? 3 : 1;
+    double xA[6], xB[6];
+    if (a >= 0)
+        for (int k = 0; k < 6; ++k) xA[k] = v[(size_t)k * N + a];
+    for (int k = 0; k < 6; ++k) xB[k] = v[(size_t)k * N + b];
+    for (int r = 0; r < nr; ++r) {
+        double t = 0.0;
+        if (a >= 0) {
+            for (int k = 0; k < 3; ++k) t = t + (-C.rd[(3 * r + k) * cap + c]) * xA[k];
+            for (int k = 0; k < 3; ++k) t = t + (-C.rcA[(3 * r + k) * cap + c]) * xA[3 + k];
+        }
+        for (int k = 0; k < 3; ++k) t = t + C.rd[(3 * r + k) * cap + c] * xB[k];
+        for (int k = 0; k < 3; ++k) t = t + C.rcB[(3 * r + k) * cap + c] * xB[3 + k];
+        C.dlam[r * cap + c] = t;
+    }
+}
+__global__ void k_linear_body64(Scene sc, Contacts C, Incidence inc, const double* v, double* Mv) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sc.N) return;
+    const int N = sc.N;
+    double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    gather_wt<1>(C, C.dlam, inc, i, acc);
+    const double Ml = sc.bf(BF_ML)[i], Ma = sc.bf(BF_MA)[i];
+    for (int k = 0; k < 6; ++k) Mv[(size_t)k * N + i] = v[(size_t)k * N + i] - acc[k] / (k < 3 ? Ml : Ma);
+}
+__global__ void k_power_fill(double* v, int64_t n, const AccelState* st) {
+    const double f = 1.0 / sqrt(st->sum_err);  // sum_err holds the chunked count of entries here
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        v[i] = f;
+}
+// one power step: n = ||M v||; stop with rho = 0 when M v vanishes; else lambda = n, v = M v / n
+__global__ void k_power_norm(AccelState* st) {
+    if (st->power_stop) return;
+    const double n = sqrt(st->sum_err);
+    if (!(n > 1e-300)) {
+        st->power_stop = 1;
+        st->lambda = 0.0;
+        return;
+    }
+    st->lambda = n;
+}
+__global__ void k_power_scale(double* v, const double* Mv, int64_t n, const AccelState* st) {
+    if (st->power_stop) return;
+    const double d = st->lambda;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        v[i] = Mv[i] / d;
+}
+__global__ void k_power_finish(AccelState* st) {
+    const double rho = st->power_stop ? 0.0 : smin(st->lambda, 0.995);
+    st->rho = rho;
+    st->rho2 = rho * rho;
+    st->omega = 1.0;
+}
+__global__ void k_accel_init(AccelState* st) {
+    st->thk = 1.0;
+    st->err_prev = INFINITY;
+    st->restarts = 0;
+    st->disabled = 0;
+    st->mode = 0;
+    st->coef = 0.0;
+    st->omega = 1.0;
+    st->nonfinite = 0;
+    st->power_stop = 0;
+    st->lambda = 0.0;
+}
+
 __global__ void k_final_residual(DevScalars* ds) {
     const double maxd = __longlong_as_double((long long)ds->maxd);
     const double maxl = __longlong_as_double((long long)ds->maxl);
@@ -788,6 +1020,47 @@ void launch_check(DevScalars* ds, int iter, double residual_tol, int nv, int che
     k_check<<<1, 1, 0, s>>>(ds, iter, residual_tol, nv, check_vel);
 }
 void launch_final_residual(DevScalars* ds, cudaStream_t s) { k_final_residual<<<1, 1, 0, s>>>(ds); }
+
+int accel_chunks(int N) { return (6 * N + RED_CHUNK - 1) / RED_CHUNK; }
+void launch_accel_reduce(int N, int op, const double* a, const double* b, const double* c, double tol_rel,
+                         double tol_abs, double* part, AccelState* st, double* out, const DevScalars* ds,
+                         cudaStream_t s) {
+    const int nch = accel_chunks(N);
+    k_chunk_partials<<<nblk(nch, 128), 128, 0, s>>>(N, op, a, b, c, tol_rel, tol_abs, part, st, ds);
+    k_chunk_total<<<1, 1, 0, s>>>(part, nch, out, ds);
+}
+void launch_accel_copy(double* xd, const double* xs, int64_t nx, double* ld, const double* ls, int64_t nl,
+                       const DevScalars* ds, cudaStream_t s) {
+    k_accel_copy<<<nblk(nx + nl), NT, 0, s>>>(xd, xs, nx, ld, ls, nl, ds);
+}
+void launch_nesterov_step(AccelState* st, DevScalars* ds, int nv, double beta_threshold, int restart_limit, double* xy,
+                          double* xk, const double* xk1, int64_t nx, double* py, double* pk, const double* pk1,
+                          int64_t nl, cudaStream_t s) {
+    k_nesterov_decide<<<1, 1, 0, s>>>(st, ds, nv, beta_threshold, restart_limit);
+    k_nesterov_update<<<nblk(nx + nl), NT, 0, s>>>(xy, xk, xk1, nx, py, pk, pk1, nl, st, ds);
+}
+void launch_chebyshev_step(AccelState* st, DevScalars* ds, int nv, int iter, const double* x, double* xk, double* xk1,
+                           int64_t nx, const double* lam, double* pk, double* pk1, int64_t nl, cudaStream_t s) {
+    k_chebyshev_decide<<<1, 1, 0, s>>>(st, ds, nv, iter);
+    k_chebyshev_update<<<nblk(nx + nl), NT, 0, s>>>(x, xk, xk1, nx, lam, pk, pk1, nl, st, ds);
+}
+void launch_spectral_radius(const Scene& sc, Contacts& C, const Incidence& inc, int nc, double* v, double* Mv,
+                            double* part, AccelState* st, cudaStream_t s) {
+    const int N = sc.N;
+    const int64_t n = 6 * (int64_t)N;
+    k_accel_init<<<1, 1, 0, s>>>(st);
+    launch_accel_reduce(N, ACC_ONES, nullptr, nullptr, nullptr, 0.0, 0.0, part, st, &st->sum_err, nullptr, s);
+    k_power_fill<<<nblk(n), NT, 0, s>>>(v, n, st);
+    for (int it = 0; it < 8; ++it) {
+        if (nc > 0) k_linear_contact64<<<nblk(nc), NT, 0, s>>>(sc, C, nc, v);
+        k_linear_body64<<<nblk(N), NT, 0, s>>>(sc, C, inc, v, Mv);
+        launch_accel_reduce(N, ACC_NORM2, Mv, nullptr, nullptr, 0.0, 0.0, part, st, &st->sum_err, nullptr, s);
+        k_power_norm<<<1, 1, 0, s>>>(st);
+        k_power_scale<<<nblk(n), NT, 0, s>>>(v, Mv, n, st);
+    }
+    k_power_finish<<<1, 1, 0, s>>>(st);
+}
+void launch_accel_init(AccelState* st, cudaStream_t s) { k_accel_init<<<1, 1, 0, s>>>(st); }
 void launch_writeback64(const Scene& sc, const double* x, cudaStream_t s) {
     if (sc.N == 0) return;
     k_writeback64<<<nblk(sc.N), NT, 0, s>>>(sc, x);

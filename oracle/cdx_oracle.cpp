@@ -598,6 +598,177 @@ SolveResult pj_solve(PJ& P, double* rhs, const double* Mdiag, double* lam, doubl
     return res;
 }
 
+// Reductions of the accelerated loops (norms, the velocity-increment residual, dot products)
+// in a fixed order: sums over consecutive chunks of RED_CHUNK entries, each left to right, then
+// the chunk sums left to right. The GPU reduces in the same order, so both agree bit for bit
+// (Eigen's vectorised reductions have an order of their own; any fixed order restates them).
+constexpr int RED_CHUNK = 256;
+template <class F>
+double chunk_sum(int n, F term) {
+    double tot = 0.0;
+    for (int c0 = 0; c0 < n; c0 += RED_CHUNK) {
+        double s = 0.0;
+        const int c1 = std::min(n, c0 + RED_CHUNK);
+        for (int j = c0; j < c1; ++j) s = s + term(j);
+        tot = tot + s;
+    }
+    return tot;
+}
+
+// projected_jacobi.cpp:140-144 (residual) with the chunked sum
+double vel_residual_chunked(const double* x, const double* xp, int nv, double tol_rel, double tol_abs) {
+    const double s = chunk_sum(nv, [&](int j) {
+        const double q = std::max(std::fabs(x[j]), std::fabs(xp[j])) * tol_rel + tol_abs;
+        const double d = (x[j] - xp[j]) / q;
+        return d * d;
+    });
+    return 1.0 / std::sqrt((double)nv) * std::sqrt(s);
+}
+
+void pj_init(PJ& P, double* rhs, const double* Mdiag, double* lam, double* x, int omp_all) {
+    wt_accumulate(P, lam, rhs, omp_all);  // rhs_init += W^T p
+    for (int j = 0; j < P.nv; ++j) x[j] = rhs[j] / Mdiag[j];
+}
+
+// nesterov_loop (projected_jacobi.cpp:379-449)
+SolveResult pj_solve_nesterov(PJ& P, double* rhs, const double* Mdiag, double* lam, double* x, int max_iter,
+                              double tol_abs, double tol_rel, double beta_threshold, int restart_limit, int omp_all,
+                              std::vector<double>* trace) {
+    SolveResult res;
+    pj_init(P, rhs, Mdiag, lam, x, omp_all);
+    if (P.nrows == 0) return res;
+    const int nv = P.nv, nr = P.nrows;
+    std::vector<double> dlam(nr), acc(nv);
+    std::vector<double> xk(x, x + nv), pk(lam, lam + nr), xk1(xk), pk1(pk), xy(xk), py(pk);
+    double thk = 1.0, err_prev = INFINITY;
+    int restarts = 0;
+    bool disabled = false;
+    for (int it = 0; it < std::max(1, max_iter); ++it) {
+        std::copy(xy.begin(), xy.end(), x);
+        std::copy(py.begin(), py.end(), lam);
+        SweepOut so = pj_sweep(P, x, lam, dlam.data(), acc.data(), Mdiag, omp_all);
+        std::copy(x, x + nv, xk1.begin());
+        std::copy(lam, lam + nr, pk1.begin());
+        res.iters = it + 1;
+        res.res_last = rel_residual(so);
+        if (trace) trace->insert(trace->end(), lam, lam + nr);
+        const double err = vel_residual_chunked(xk1.data(), xy.data(), nv, tol_rel, tol_abs);
+        if (err <= 1.0) break;
+        const double thk1 = 0.5 * (1.0 + std::sqrt(4.0 * thk * thk + 1.0));
+        const double betak1 = (thk - 1.0) / thk1;
+        bool restart = false;
+        if (!std::isfinite(err)) {
+            restart = true;
+        } else if (err_prev < INFINITY && err > 1.05 * err_prev) {
+            restart = true;
+        } else if (betak1 > beta_threshold) {
+            restart = true;
+        } else if (!std::isfinite(betak1) || betak1 < 0.0 || betak1 > 1.0) {
+            restart = true;
+        } else {
+            const double dot = chunk_sum(nv, [&](int j) { return (xy[j] - xk1[j]) * (xk1[j] - xk[j]); });
+            if (dot > 0.0) restart = true;
+        }
+        if (restart) {
+            xy = xk1;
+            py = pk1;
+            xk = xk1;
+            pk = pk1;
+            thk = 1.0;
+            if (++restarts >= restart_limit) disabled = true;
+        } else {
+            if (disabled) {
+                xy = xk1;
+                py = pk1;
+                thk = 1.0;
+            } else {
+                for (int j = 0; j < nv; ++j) xy[j] = xk1[j] + betak1 * (xk1[j] - xk[j]);
+                for (int r = 0; r < nr; ++r) py[r] = pk1[r] + betak1 * (pk1[r] - pk[r]);
+                thk = thk1;
+            }
+            xk = xk1;
+            pk = pk1;
+        }
+        err_prev = err;
+    }
+    std::copy(xk1.begin(), xk1.end(), x);
+    std::copy(pk1.begin(), pk1.end(), lam);
+    SweepOut fin = pj_sweep(P, x, lam, dlam.data(), acc.data(), Mdiag, omp_all, false);
+    res.res_final = rel_residual(fin);
+    return res;
+}
+
+// estimateSpectralRadius (projected_jacobi.cpp:154-177): power iteration on the linear part of
+// the sweep map, M v = v - S^-1 W^T (R W v), eight steps, clamped below 0.995
+double spectral_radius(const PJ& P, const double* Mdiag, int omp_all) {
+    const int nv = P.nv, nr = P.nrows;
+    if (nv <= 0) return 0.0;
+    const double n0 = std::sqrt(chunk_sum(nv, [](int) { return 1.0; }));
+    std::vector<double> v(nv, 1.0 / n0), delta(nr), acc(nv), Mv(nv);
+    double lambda = 0.0;
+    for (int it = 0; it < 8; ++it) {
+        for (int r = 0; r < nr; ++r) {
+            double t = 0.0;
+            for (int k = P.ptr[r]; k < P.ptr[r + 1]; ++k) t = t + P.RW[k] * v[P.col[k]];
+            delta[r] = t;
+        }
+        std::fill(acc.begin(), acc.end(), 0.0);
+        wt_accumulate(P, delta.data(), acc.data(), omp_all);
+        for (int j = 0; j < nv; ++j) Mv[j] = v[j] - acc[j] / Mdiag[j];
+        const double n = std::sqrt(chunk_sum(nv, [&](int j) { return Mv[j] * Mv[j]; }));
+        if (!(n > 1e-300)) return 0.0;
+        lambda = n;
+        for (int j = 0; j < nv; ++j) v[j] = Mv[j] / n;
+    }
+    return std::min(lambda, 0.995);
+}
+
+// chebyshev_loop (projected_jacobi.cpp:179-222)
+SolveResult pj_solve_chebyshev(PJ& P, double* rhs, const double* Mdiag, double* lam, double* x, int max_iter,
+                               double tol_abs, double tol_rel, int omp_all, std::vector<double>* trace) {
+    SolveResult res;
+    pj_init(P, rhs, Mdiag, lam, x, omp_all);
+    if (P.nrows == 0) return res;
+    const int nv = P.nv, nr = P.nrows;
+    const double rho = spectral_radius(P, Mdiag, omp_all);
+    std::vector<double> dlam(nr), acc(nv);
+    std::vector<double> xk(x, x + nv), pk(lam, lam + nr), xk1(xk), pk1(pk), xk2(nv), pk2(nr);
+    const double rho2 = rho * rho;
+    double omega = 1.0;
+    for (int it = 0; it < std::max(1, max_iter); ++it) {
+        std::copy(xk1.begin(), xk1.end(), x);
+        std::copy(pk1.begin(), pk1.end(), lam);
+        SweepOut so = pj_sweep(P, x, lam, dlam.data(), acc.data(), Mdiag, omp_all);
+        res.iters = it + 1;
+        res.res_last = rel_residual(so);
+        if (trace) trace->insert(trace->end(), lam, lam + nr);
+        const double err = vel_residual_chunked(x, xk1.data(), nv, tol_rel, tol_abs);
+        if (err <= 1.0) break;
+        double omega_next = (it == 0) ? (1.0 / (1.0 - rho2 * 0.5)) : (1.0 / (1.0 - (rho2 * 0.25) * omega));
+        bool finite = true;
+        for (int j = 0; j < nv && finite; ++j) finite = std::isfinite(x[j]);
+        if (!std::isfinite(omega_next) || omega_next <= 0.0 || !finite) {
+            std::copy(x, x + nv, xk2.begin());
+            std::copy(lam, lam + nr, pk2.begin());
+            omega_next = 1.0;
+        } else {
+            for (int j = 0; j < nv; ++j) xk2[j] = omega_next * (x[j] - xk[j]) + xk[j];
+            for (int r = 0; r < nr; ++r) pk2[r] = omega_next * (lam[r] - pk[r]) + pk[r];
+        }
+        xk = xk1;
+        pk = pk1;
+        xk1 = xk2;
+        pk1 = pk2;
+        omega = omega_next;
+    }
+    // as the reference: the loop's current extrapolated iterate is the result
+    std::copy(xk1.begin(), xk1.end(), x);
+    std::copy(pk1.begin(), pk1.end(), lam);
+    SweepOut fin = pj_sweep(P, x, lam, dlam.data(), acc.data(), Mdiag, omp_all, false);
+    res.res_final = rel_residual(fin);
+    return res;
+}
+
 // MoreauIntegrator::step (src/physics/integration/moreau.cpp:6-13)
 void step_once(Engine& E) {
     const int N = E.N, S = E.S, nv = 6 * N;
@@ -670,9 +841,19 @@ void step_once(Engine& E) {
     if (C.empty()) {
         for (int j = 0; j < nv; ++j) x[j] = rhs[j] / E.Mdiag[j];
     } else {
-        sr = pj_solve(P, rhs.data(), E.Mdiag.data(), lam.data(), x.data(), E.cfg.pj_max_iterations,
-                      E.cfg.pj_tol_abs, E.cfg.pj_tol_rel, E.cfg.residual_tol, omp_all,
-                      E.trace_on ? &E.trace : nullptr);
+        // loop selection as ProjectedJacobiSolver::solve (projected_jacobi.cpp:470-491): Nesterov
+        // takes precedence over Chebyshev, then the standard loop
+        std::vector<double>* tr = E.trace_on ? &E.trace : nullptr;
+        if (E.cfg.pj_nesterov)
+            sr = pj_solve_nesterov(P, rhs.data(), E.Mdiag.data(), lam.data(), x.data(), E.cfg.pj_max_iterations,
+                                   E.cfg.pj_tol_abs, E.cfg.pj_tol_rel, E.cfg.pj_nesterov_beta_threshold,
+                                   E.cfg.pj_nesterov_restart_limit, omp_all, tr);
+        else if (E.cfg.pj_chebyshev)
+            sr = pj_solve_chebyshev(P, rhs.data(), E.Mdiag.data(), lam.data(), x.data(), E.cfg.pj_max_iterations,
+                                    E.cfg.pj_tol_abs, E.cfg.pj_tol_rel, omp_all, tr);
+        else
+            sr = pj_solve(P, rhs.data(), E.Mdiag.data(), lam.data(), x.data(), E.cfg.pj_max_iterations,
+                          E.cfg.pj_tol_abs, E.cfg.pj_tol_rel, E.cfg.residual_tol, omp_all, tr);
     }
     E.trace_on = false;
     // storeImpulse (warmstart.hpp:41-56) and the tracker's memory for the next step

@@ -39,6 +39,10 @@ typedef struct or_config {
     double residual_tol;   /* new complementarity-residual stop rule; 0 = off */
     int32_t omp_mode;      /* 0 = faithful (OpenMP on the projection only), 1 = all loops */
     int32_t num_threads;   /* 0 = OpenMP default */
+    int32_t pj_nesterov;                 /* pj.nesterov */
+    double pj_nesterov_beta_threshold;   /* pj.nesterov_beta_threshold */
+    int32_t pj_nesterov_restart_limit;   /* pj.nesterov_restart_limit */
+    int32_t pj_chebyshev;                /* pj.chebyshev */
 } or_config;
 
 typedef struct or_scene {

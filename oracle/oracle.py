@@ -55,6 +55,10 @@ class OrConfig(C.Structure):
         ("residual_tol", C.c_double),
         ("omp_mode", C.c_int32),
         ("num_threads", C.c_int32),
+        ("pj_nesterov", C.c_int32),
+        ("pj_nesterov_beta_threshold", C.c_double),
+        ("pj_nesterov_restart_limit", C.c_int32),
+        ("pj_chebyshev", C.c_int32),
     ]
 
 
@@ -138,6 +142,10 @@ def config_from(cfg: dict, omp_mode: int = 0, num_threads: int = 0) -> OrConfig:
     c.collision_security_margin = float(cfg.get("collision.security_margin", 0.0))
     c.collision_match_max_dist = float(cfg.get("collision.match_max_dist", 0.02))
     c.residual_tol = float(cfg.get("gpu.residual_tol", 0.0))
+    c.pj_nesterov = int(bool(cfg.get("pj.nesterov", False)))
+    c.pj_nesterov_beta_threshold = float(cfg.get("pj.nesterov_beta_threshold", 1.0))
+    c.pj_nesterov_restart_limit = int(cfg.get("pj.nesterov_restart_limit", 10000))
+    c.pj_chebyshev = int(bool(cfg.get("pj.chebyshev", False)))
     c.omp_mode = omp_mode
     c.num_threads = num_threads
     return c

@@ -129,3 +129,14 @@ def test_create_without_device_reports_error(cdxlib):
     with pytest.raises(CdxError) as e:
         PhysicsEngine({})
     assert "CUDA" in str(e.value) or "cuda" in str(e.value)
+
+
+def test_acceleration_keys(cdxlib):
+    from cardillocxx_gb300.engine import Config
+    c = Config()
+    assert c.get("pj_nesterov") == 0 and c.get("pj_chebyshev") == 0
+    assert c.get("pj_nesterov_beta_threshold") == 1.0 and c.get("pj_nesterov_restart_limit") == 10000
+    c.set("pj.nesterov", "on").set("solver.chebyshev", "true").set("pj.nesterov_beta_threshold", 0.9)
+    c.set("pj.nesterov_restart_limit", 7)
+    assert c.get("pj_nesterov") == 1 and c.get("pj_chebyshev") == 1
+    assert c.get("pj_nesterov_beta_threshold") == 0.9 and c.get("pj_nesterov_restart_limit") == 7
