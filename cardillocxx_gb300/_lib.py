@@ -63,6 +63,8 @@ class CdxConfig(C.Structure):
         ("pj_nesterov_beta_threshold", C.c_double),
         ("pj_nesterov_restart_limit", C.c_int32),
         ("pj_chebyshev", C.c_int32),
+        ("pj_anderson", C.c_int32),
+        ("pj_anderson_m", C.c_int32),
     ]
 
 

@@ -129,6 +129,25 @@ struct AccelState {
 };
 enum AccelReduce : int { ACC_VELRES = 0, ACC_NORM2 = 1, ACC_DOT = 2, ACC_ONES = 3 };
 
+// Anderson loop (device): the dense iterate z = [velocities in stacked order 6 i + k; impulse rows
+// in the reference's row order], a ring of the last m + 1 iterates and residuals (oldest at head),
+// and the mode of the current step (0 plain step, 1 mixed candidate, 2 failed least squares)
+struct AndersonState {
+    int32_t head, count, mode, nonfinite;
+};
+struct AndersonBufs {
+    int m = 0;             // history window
+    int64_t nt = 0;        // 6 N + rows of this solve
+    int64_t nt_cap = 0;    // allocated length of each dense vector
+    double *z = nullptr, *w = nullptr, *f = nullptr, *cand = nullptr;
+    double *zh = nullptr, *fh = nullptr;  // (m + 1) x nt_cap each
+    double *part = nullptr;               // sums x chunks
+    double *ls = nullptr;                 // normal equations (m x m), right side (m), gamma (m)
+    int32_t* rowmap = nullptr;            // impulse row -> index into the 3 x cap impulse array
+    int64_t rowmap_cap = 0;
+    AndersonState* st = nullptr;
+};
+
 struct Incidence {
     int64_t cap = 0;
     uint32_t* key_in = nullptr;
@@ -188,6 +207,13 @@ void launch_nesterov_step(AccelState* st, DevScalars* ds, int nv, double beta_th
                           int64_t nl, cudaStream_t s);
 void launch_chebyshev_step(AccelState* st, DevScalars* ds, int nv, int iter, const double* x, double* xk, double* xk1,
                            int64_t nx, const double* lam, double* pk, double* pk1, int64_t nl, cudaStream_t s);
+int anderson_sums(int m);
+int anderson_chunks(int64_t n);
+void launch_anderson_begin(const Contacts& C, int gen, int nc, const int32_t* fl_scan, const int32_t* isfl, int N,
+                           const double* x, AndersonBufs& A, cudaStream_t s);
+void launch_anderson_scatter(int N, double* x, double* lam, const AndersonBufs& A, const DevScalars* ds, cudaStream_t s);
+void launch_anderson_mix(int N, const double* x, const double* lam, const AndersonBufs& A, double tol_rel,
+                         double tol_abs, DevScalars* ds, cudaStream_t s);
 void launch_spectral_radius(const Scene& sc, Contacts& C, const Incidence& inc, int nc, double* v, double* Mv,
                             double* part, AccelState* st, cudaStream_t s);
 void launch_writeback64(const Scene& sc, const double* x, cudaStream_t s);

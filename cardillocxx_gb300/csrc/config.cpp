@@ -97,6 +97,8 @@ int cdx_config_default(cdx_config* c) {
     c->pj_nesterov_beta_threshold = 1.0;
     c->pj_nesterov_restart_limit = 10000;
     c->pj_chebyshev = 0;
+    c->pj_anderson = 0;
+    c->pj_anderson_m = 2;
     return CDX_OK;
 }
 
@@ -186,6 +188,10 @@ int cdx_config_set(cdx_config* c, const char* key_c, const char* val_c) {
         if (as_int(val, &i)) c->pj_nesterov_restart_limit = std::max(0, i);
     } else if (key_is(key, "pj.chebyshev")) {
         c->pj_chebyshev = as_bool(val);
+    } else if (key_is(key, "pj.anderson")) {
+        c->pj_anderson = as_bool(val);
+    } else if (key_is(key, "pj.anderson_m")) {
+        if (as_int(val, &i)) c->pj_anderson_m = std::max(1, i);
     }
     return CDX_OK;  // unknown keys are ignored, as in the reference
 }

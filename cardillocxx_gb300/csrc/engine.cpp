@@ -523,6 +523,78 @@ int Engine::solve64_accel() {
     return CDX_OK;
 }
 
+int Engine::ensure_anderson(int64_t nt) {
+    AndersonBufs& A = anderson;
+    const int m = std::max(1, cfg.pj_anderson_m);
+    if (A.st && A.m == m && nt <= A.nt_cap && A.rowmap_cap >= 3 * C.cap) {
+        A.nt = nt;
+        return CDX_OK;
+    }
+    double** bufs[] = {&A.z, &A.w, &A.f, &A.cand, &A.zh, &A.fh, &A.part, &A.ls};
+    for (auto b : bufs)
+        if (*b) {
+            dfree(*b);
+            *b = nullptr;
+        }
+    if (A.rowmap) dfree(A.rowmap);
+    if (A.st) dfree(A.st);
+    A.rowmap = nullptr;
+    A.st = nullptr;
+    const int64_t cap = std::max<int64_t>(nt + nt / 4, 16);
+    int st;
+    for (int k = 0; k < 4; ++k)
+        if ((st = dalloc((void**)bufs[k], sizeof(double) * cap, "Anderson loop"))) return st;
+    for (int k = 4; k < 6; ++k)
+        if ((st = dalloc((void**)bufs[k], sizeof(double) * cap * (m + 1), "Anderson loop"))) return st;
+    if ((st = dalloc((void**)&A.part, sizeof(double) * anderson_chunks(cap) * anderson_sums(m), "Anderson loop")))
+        return st;
+    if ((st = dalloc((void**)&A.ls, sizeof(double) * ((int64_t)m * m + 2 * m), "Anderson loop"))) return st;
+    if ((st = dalloc((void**)&A.rowmap, sizeof(int32_t) * std::max<int64_t>(3 * C.cap, 1), "Anderson loop"))) return st;
+    if ((st = dalloc((void**)&A.st, sizeof(AndersonState), "Anderson loop"))) return st;
+    A.m = m;
+    A.nt = nt;
+    A.nt_cap = cap;
+    A.rowmap_cap = 3 * C.cap;
+    return CDX_OK;
+}
+
+// anderson_loop (projected_jacobi.cpp:242-314) of ProjectedJacobiSolver, plain FP64: z = [x; impulse
+// rows], one sweep g(z), and the mixed step z = g(z) - (dZ + dF) gamma over the last m residual
+// differences, with gamma from the normal equations of the least squares problem (the reference
+// solves it by a column-pivoted QR; both give the minimiser for a full-rank dF, and a singular
+// system falls back to a plain step and drops the history as a non-finite gamma does there).
+// Every decision runs on the device; the host polls the stop flag every gpu.check_every sweeps.
+int Engine::solve64_anderson() {
+    const int N = sc.N, nv = 6 * N;
+    int st;
+    const int nrows = nfl_rows();
+    if ((st = ensure_anderson((int64_t)nv + nrows))) return st;
+    double* lam = C.lam[gen];
+    cudaMemsetAsync(ds, 0, sizeof(DevScalars), stream);
+    launch_anderson_begin(C, gen, nc, flscan, isfl, N, x, anderson, stream);
+    const int maxit = std::max(1, cfg.pj_max_iterations);
+    const int every = std::max(1, cfg.gpu_check_every);
+    for (int it = 0; it < maxit; ++it) {
+        launch_anderson_scatter(N, x, lam, anderson, ds, stream);
+        launch_sweep_contact64(sc, C, gen, nc, x, ds, 0, stream);
+        launch_sweep_body64(sc, C, inc, x, 0.0, 0.0, 0, ds, stream);
+        launch_check(ds, it, 0.0, nv, 0, stream);  // res_last and the sweep count
+        launch_anderson_mix(N, x, lam, anderson, cfg.pj_tol_rel, cfg.pj_tol_abs, ds, stream);
+        launches += 12;
+        if ((it + 1) % every == 0 && it + 1 < maxit) {
+            cudaMemcpyAsync(&hs->done, &ds->done, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+            if ((st = cuda_check(cudaStreamSynchronize(stream), "poll"))) return st;
+            if (hs->done) break;
+        }
+    }
+    // stopped: (x, lambda) hold g(z); otherwise the result is the loop's z
+    launch_anderson_scatter(N, x, lam, anderson, ds, stream);
+    launch_sweep_contact64(sc, C, gen, nc, x, ds, 1, stream);
+    launch_final_residual(ds, stream);
+    launches += 3;
+    return CDX_OK;
+}
+
 int Engine::solve64() {
     const int N = sc.N;
     int st;
@@ -534,6 +606,7 @@ int Engine::solve64() {
     last_res_final = 0;
     if (nc == 0) return CDX_OK;
     if ((cfg.pj_nesterov || cfg.pj_chebyshev) && !trace_next) return solve64_accel();
+    if (cfg.pj_anderson && !trace_next) return solve64_anderson();
     cudaMemsetAsync(ds, 0, sizeof(DevScalars), stream);
     const int maxit = std::max(1, cfg.pj_max_iterations);
     const bool check_vel = !(cfg.pj_tol_abs == 0.0 && cfg.pj_tol_rel == 0.0);

@@ -54,6 +54,9 @@ struct Engine {
     int64_t acc_nx = 0, acc_nl = 0;
     int ensure_accel();
     int solve64_accel();
+    cdx::AndersonBufs anderson;
+    int ensure_anderson(int64_t nt);
+    int solve64_anderson();
     cdx::DevScalars* hs = nullptr;  // pinned mirror
     void* tmp = nullptr;
     size_t tmp_bytes = 0;

@@ -12,6 +12,7 @@
 //   k_sweep_body64    pj_sweep's x += S^-1 W^T dlambda (projected_jacobi.cpp:134-137)
 // W is never formed: each contact keeps its three directions and body-frame lever products, W^T
 // is applied as a per-body gather over the body's incidence list in solver row order.
+#include <algorithm>
 #include <cstdio>
 
 #include "cdx_internal.h"
@@ -940,6 +941,230 @@ __global__ void k_writeback64(Scene sc, const double* x) {
     sc.bf(BF_WZ)[i] = x[5 * (size_t)N + i];
 }
 
+// ---- Anderson loop (anderson_loop, projected_jacobi.cpp:242-314) on the dense iterate
+// z = [x (stacked index 6 i + k); impulse rows (frictionless contacts by rank, then three rows per
+// frictional contact)]. Dot products use the chunked order of the other accelerated loops.
+__device__ __forceinline__ int ring_slot(const AndersonState* as, int m, int j) { return (as->head + j) % (m + 1); }
+
+__global__ void k_and_rowmap(Contacts C, int nc, const int32_t* fl_scan, const int32_t* isfl, int32_t* rowmap) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    const int nfl = fl_scan[nc - 1] + isfl[nc - 1];
+    const int rank = C.rank[c];
+    if (rank < nfl) {
+        rowmap[rank] = c;
+    } else {
+        const int row = nfl + 3 * (rank - nfl);
+        for (int r = 0; r < 3; ++r) rowmap[row + r] = (int32_t)(r * C.cap + c);
+    }
+}
+
+// dense <- (x, lam); mode 0: z only (start), mode 1: w, f = w - z and the newest history slot
+__global__ void k_and_gather(int N, const double* x, const double* lam, const int32_t* rowmap, int64_t nt, int m,
+                             int64_t ld, double* z, double* w, double* f, double* zh, double* fh,
+                             const AndersonState* as, const DevScalars* ds, int mode) {
+    if (ds && *(volatile const int32_t*)&ds->done) return;
+    const int64_t nv = 6 * (int64_t)N;
+    const int slot = mode ? ring_slot(as, m, as->count - 1) : 0;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt; t += (int64_t)gridDim.x * blockDim.x) {
+        const double v = t < nv ? x[(size_t)(t % 6) * N + t / 6] : lam[rowmap[t - nv]];
+        if (!mode) {
+            z[t] = v;
+        } else {
+            const double zt = z[t];
+            const double ft = v - zt;
+            w[t] = v;
+            f[t] = ft;
+            zh[(size_t)slot * ld + t] = zt;
+            fh[(size_t)slot * ld + t] = ft;
+        }
+    }
+}
+
+__global__ void k_and_scatter(int N, double* x, double* lam, const int32_t* rowmap, int64_t nt, const double* z,
+                              const DevScalars* ds) {
+    if (ds && *(volatile const int32_t*)&ds->done) return;
+    const int64_t nv = 6 * (int64_t)N;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt; t += (int64_t)gridDim.x * blockDim.x) {
+        if (t < nv)
+            x[(size_t)(t % 6) * N + t / 6] = z[t];
+        else
+            lam[rowmap[t - nv]] = z[t];
+    }
+}
+
+// push: the newest (z, f) takes the next ring slot, the oldest leaves once m + 1 are kept
+__global__ void k_and_push(AndersonState* as, int m, const DevScalars* ds) {
+    if (ds->done) return;
+    if (as->count < m + 1)
+        ++as->count;
+    else
+        as->head = (as->head + 1) % (m + 1);
+}
+
+// partial sums per chunk: sum 0 = the scaled velocity increment (w vs z over the velocities),
+// then (dF_j . dF_l) for l <= j < mk and (dF_j . f) for j < mk, dF_j = F_{j+1} - F_j (oldest first)
+__global__ void k_and_partials(int N, int64_t nt, int m, int64_t ld, const double* z, const double* w, const double* f,
+                               const double* fh, double tol_rel, double tol_abs, double* part, int nch_t,
+                               const AndersonState* as, const DevScalars* ds) {
+    if (ds && *(volatile const int32_t*)&ds->done) return;
+    const int ch = blockIdx.x * blockDim.x + threadIdx.x;
+    const int sidx = blockIdx.y;
+    const int mk = as->count - 1;
+    const int64_t nv = 6 * (int64_t)N;
+    const int nsums = 1 + mk * (mk + 1) / 2 + (mk > 0 ? mk : 0);
+    if (sidx >= nsums) return;
+    const int64_t n = sidx == 0 ? nv : nt;
+    const int64_t j0 = (int64_t)ch * RED_CHUNK;
+    if (ch >= nch_t || j0 >= n) return;
+    const int64_t j1 = j0 + RED_CHUNK < n ? j0 + RED_CHUNK : n;
+    double s = 0.0;
+    if (sidx == 0) {
+        for (int64_t t = j0; t < j1; ++t) {
+            const double a = w[t], b = z[t];
+            const double q = smax(fabs(a), fabs(b)) * tol_rel + tol_abs;
+            const double d = (a - b) / q;
+            s = s + d * d;
+        }
+    } else {
+        const int q = sidx - 1;
+        const int na = mk * (mk + 1) / 2;
+        int j, l;
+        if (q < na) {
+            j = 0;
+            while ((j + 1) * (j + 2) / 2 <= q) ++j;
+            l = q - j * (j + 1) / 2;
+        } else {
+            j = q - na;
+            l = -1;
+        }
+        const double* fa0 = fh + (size_t)ring_slot(as, m, j) * ld;
+        const double* fa1 = fh + (size_t)ring_slot(as, m, j + 1) * ld;
+        if (l >= 0) {
+            const double* fb0 = fh + (size_t)ring_slot(as, m, l) * ld;
+            const double* fb1 = fh + (size_t)ring_slot(as, m, l + 1) * ld;
+            for (int64_t t = j0; t < j1; ++t) s = s + (fa1[t] - fa0[t]) * (fb1[t] - fb0[t]);
+        } else {
+            for (int64_t t = j0; t < j1; ++t) s = s + (fa1[t] - fa0[t]) * f[t];
+        }
+    }
+    part[(size_t)sidx * nch_t + ch] = s;
+}
+
+// one thread: the stop test, then gamma from the normal equations by Gaussian elimination with
+// partial pivoting (mode 1), or a plain step (mode 0, fewer than two residuals kept), or a failed
+// solve (mode 2: singular or not finite)
+__global__ void k_and_solve(int nv, int nch_v, int nch_t, const double* part, double* ls, int m, AndersonState* as,
+                            DevScalars* ds) {
+    if (ds->done) return;
+    double sv = 0.0;
+    for (int k = 0; k < nch_v; ++k) sv = sv + part[k];
+    const double err = 1.0 / sqrt((double)nv) * sqrt(sv);
+    as->nonfinite = 0;
+    if (err <= 1.0) {
+        ds->done = 1;
+        return;
+    }
+    const int mk = as->count - 1;
+    if (mk < 1) {
+        as->mode = 0;
+        return;
+    }
+    double* A = ls;
+    double* b = ls + (size_t)m * m;
+    double* g = b + m;
+    const int na = mk * (mk + 1) / 2;
+    for (int j = 0; j < mk; ++j) {
+        for (int l = 0; l <= j; ++l) {
+            const double* p = part + (size_t)(1 + j * (j + 1) / 2 + l) * nch_t;
+            double d = 0.0;
+            for (int k = 0; k < nch_t; ++k) d = d + p[k];
+            A[j * mk + l] = d;
+            A[l * mk + j] = d;
+        }
+        const double* p = part + (size_t)(1 + na + j) * nch_t;
+        double d = 0.0;
+        for (int k = 0; k < nch_t; ++k) d = d + p[k];
+        b[j] = d;
+    }
+    for (int c = 0; c < mk; ++c) {
+        int piv = c;
+        for (int r = c + 1; r < mk; ++r)
+            if (fabs(A[r * mk + c]) > fabs(A[piv * mk + c])) piv = r;
+        if (!(fabs(A[piv * mk + c]) > 0.0)) {
+            as->mode = 2;
+            return;
+        }
+        if (piv != c) {
+            for (int k = 0; k < mk; ++k) {
+                const double t = A[c * mk + k];
+                A[c * mk + k] = A[piv * mk + k];
+                A[piv * mk + k] = t;
+            }
+            const double t = b[c];
+            b[c] = b[piv];
+            b[piv] = t;
+        }
+        for (int r = c + 1; r < mk; ++r) {
+            const double fct = A[r * mk + c] / A[c * mk + c];
+            for (int k = c; k < mk; ++k) A[r * mk + k] = A[r * mk + k] - fct * A[c * mk + k];
+            b[r] = b[r] - fct * b[c];
+        }
+    }
+    for (int r = mk - 1; r >= 0; --r) {
+        double t = b[r];
+        for (int k = r + 1; k < mk; ++k) t = t - A[r * mk + k] * g[k];
+        g[r] = t / A[r * mk + r];
+    }
+    for (int j = 0; j < mk; ++j)
+        if (!isfinite(g[j])) {
+            as->mode = 2;
+            return;
+        }
+    as->mode = 1;
+}
+
+// candidate = w - (dZ + dF) gamma (mode 1 only); flags a non-finite entry
+__global__ void k_and_candidate(int64_t nt, int m, int64_t ld, const double* w, const double* zh, const double* fh,
+                                const double* gam, double* cand, AndersonState* as, const DevScalars* ds) {
+    if (*(volatile const int32_t*)&ds->done || as->mode != 1) return;
+    const int mk = as->count - 1;
+    bool bad = false;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt; t += (int64_t)gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int j = 0; j < mk; ++j) {
+            const size_t a0 = (size_t)ring_slot(as, m, j) * ld + t, a1 = (size_t)ring_slot(as, m, j + 1) * ld + t;
+            s = s + ((zh[a1] - zh[a0]) + (fh[a1] - fh[a0])) * gam[j];
+        }
+        const double c = w[t] - s;
+        cand[t] = c;
+        bad = bad || !isfinite(c);
+    }
+    if (bad) as->nonfinite = 1;
+}
+
+// z = candidate when it exists and is finite, else w; a failed step drops the history
+__global__ void k_and_select(int64_t nt, double* z, const double* w, const double* cand, AndersonState* as,
+                             const DevScalars* ds) {
+    if (*(volatile const int32_t*)&ds->done) return;
+    const bool take = as->mode == 1 && !as->nonfinite;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt; t += (int64_t)gridDim.x * blockDim.x)
+        z[t] = take ? cand[t] : w[t];
+}
+__global__ void k_and_drop(AndersonState* as, const DevScalars* ds) {
+    if (ds->done) return;
+    if (as->mode == 2 || (as->mode == 1 && as->nonfinite)) {
+        as->count = 0;
+        as->head = 0;
+    }
+}
+__global__ void k_and_init(AndersonState* as) {
+    as->head = 0;
+    as->count = 0;
+    as->mode = 0;
+    as->nonfinite = 0;
+}
+
 __global__ void k_trace64(Contacts C, int gen, int nc, const int32_t* fl_scan, const int32_t* isfl, double* out) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nc) return;
@@ -1061,6 +1286,36 @@ void launch_spectral_radius(const Scene& sc, Contacts& C, const Incidence& inc, 
     k_power_finish<<<1, 1, 0, s>>>(st);
 }
 void launch_accel_init(AccelState* st, cudaStream_t s) { k_accel_init<<<1, 1, 0, s>>>(st); }
+
+int anderson_sums(int m) { return 1 + m * (m + 1) / 2 + m; }
+int anderson_chunks(int64_t n) { return (int)((n + RED_CHUNK - 1) / RED_CHUNK); }
+static int grid_of(int64_t n) { return (int)std::min<int64_t>(std::max<int64_t>(nblk(n), 1), 4096); }
+void launch_anderson_begin(const Contacts& C, int gen, int nc, const int32_t* fl_scan, const int32_t* isfl, int N,
+                           const double* x, AndersonBufs& A, cudaStream_t s) {
+    k_and_init<<<1, 1, 0, s>>>(A.st);
+    if (nc > 0) k_and_rowmap<<<nblk(nc), NT, 0, s>>>(C, nc, fl_scan, isfl, A.rowmap);
+    k_and_gather<<<grid_of(A.nt), NT, 0, s>>>(N, x, C.lam[gen], A.rowmap, A.nt, A.m, A.nt_cap, A.z, A.w, A.f, A.zh,
+                                              A.fh, A.st, nullptr, 0);
+}
+void launch_anderson_scatter(int N, double* x, double* lam, const AndersonBufs& A, const DevScalars* ds,
+                             cudaStream_t s) {
+    k_and_scatter<<<grid_of(A.nt), NT, 0, s>>>(N, x, lam, A.rowmap, A.nt, A.z, ds);
+}
+void launch_anderson_mix(int N, const double* x, const double* lam, const AndersonBufs& A, double tol_rel,
+                         double tol_abs, DevScalars* ds, cudaStream_t s) {
+    const int nch_t = anderson_chunks(A.nt), nch_v = anderson_chunks(6 * (int64_t)N);
+    k_and_push<<<1, 1, 0, s>>>(A.st, A.m, ds);
+    k_and_gather<<<grid_of(A.nt), NT, 0, s>>>(N, x, lam, A.rowmap, A.nt, A.m, A.nt_cap, A.z, A.w, A.f, A.zh, A.fh,
+                                              A.st, ds, 1);
+    dim3 g((unsigned)nblk(nch_t, 128), (unsigned)anderson_sums(A.m));
+    k_and_partials<<<g, 128, 0, s>>>(N, A.nt, A.m, A.nt_cap, A.z, A.w, A.f, A.fh, tol_rel, tol_abs, A.part, nch_t,
+                                     A.st, ds);
+    k_and_solve<<<1, 1, 0, s>>>(6 * N, nch_v, nch_t, A.part, A.ls, A.m, A.st, ds);
+    const double* gam = A.ls + (size_t)A.m * A.m + A.m;
+    k_and_candidate<<<grid_of(A.nt), NT, 0, s>>>(A.nt, A.m, A.nt_cap, A.w, A.zh, A.fh, gam, A.cand, A.st, ds);
+    k_and_select<<<grid_of(A.nt), NT, 0, s>>>(A.nt, A.z, A.w, A.cand, A.st, ds);
+    k_and_drop<<<1, 1, 0, s>>>(A.st, ds);
+}
 void launch_writeback64(const Scene& sc, const double* x, cudaStream_t s) {
     if (sc.N == 0) return;
     k_writeback64<<<nblk(sc.N), NT, 0, s>>>(sc, x);

@@ -72,12 +72,14 @@ typedef struct cdx_config {
     int32_t gpu_autotune;             /* gpu.autotune: pick the contact-sweep launch shape by timing (split form) */
     int32_t gpu_sweep_variant;        /* gpu.sweep_variant: pin launch shape k (split form; -1 = default/autotuned) */
     int32_t gpu_sync_counts;          /* gpu.sync_counts: every split step stops for the host to size its contact buffers */
-    /* accelerated loops of ProjectedJacobiSolver (config.hpp:85-102; projected_jacobi.cpp:179-222,
-     * 379-449), plain FP64 method: Nesterov takes precedence over Chebyshev */
+    /* accelerated loops of ProjectedJacobiSolver (config.hpp:85-110; projected_jacobi.cpp:179-222,
+     * 242-314, 379-449), plain FP64 method: Nesterov > Chebyshev > Anderson */
     int32_t pj_nesterov;              /* pj.nesterov */
     double pj_nesterov_beta_threshold; /* pj.nesterov_beta_threshold */
     int32_t pj_nesterov_restart_limit; /* pj.nesterov_restart_limit */
     int32_t pj_chebyshev;             /* pj.chebyshev */
+    int32_t pj_anderson;              /* pj.anderson */
+    int32_t pj_anderson_m;            /* pj.anderson_m: history window (>= 1) */
 } cdx_config;
 
 /* Scene: dynamic spheres plus static shapes (halfspaces, drums). Bodies of one scene are

@@ -769,6 +769,118 @@ SolveResult pj_solve_chebyshev(PJ& P, double* rhs, const double* Mdiag, double* 
     return res;
 }
 
+// Least squares min ||f - dF g|| of the Anderson step by its normal equations (dF^T dF) g = dF^T f,
+// solved by Gaussian elimination with partial pivoting. The reference uses a column-pivoted QR
+// (projected_jacobi.cpp:292); for a full-rank dF both give the same minimiser. The dot products
+// use the chunked order. Returns false when the system is singular or not finite.
+bool anderson_ls(const std::vector<std::vector<double>>& dF, const std::vector<double>& f, int n, std::vector<double>& g) {
+    const int mk = (int)dF.size();
+    std::vector<double> A((size_t)mk * mk), b(mk);
+    for (int j = 0; j < mk; ++j) {
+        for (int l = 0; l <= j; ++l) {
+            const double d = chunk_sum(n, [&](int t) { return dF[j][t] * dF[l][t]; });
+            A[(size_t)j * mk + l] = d;
+            A[(size_t)l * mk + j] = d;
+        }
+        b[j] = chunk_sum(n, [&](int t) { return dF[j][t] * f[t]; });
+    }
+    for (int c = 0; c < mk; ++c) {
+        int piv = c;
+        for (int r = c + 1; r < mk; ++r)
+            if (std::fabs(A[(size_t)r * mk + c]) > std::fabs(A[(size_t)piv * mk + c])) piv = r;
+        if (!(std::fabs(A[(size_t)piv * mk + c]) > 0.0)) return false;
+        if (piv != c) {
+            for (int k = 0; k < mk; ++k) std::swap(A[(size_t)c * mk + k], A[(size_t)piv * mk + k]);
+            std::swap(b[c], b[piv]);
+        }
+        for (int r = c + 1; r < mk; ++r) {
+            const double fct = A[(size_t)r * mk + c] / A[(size_t)c * mk + c];
+            for (int k = c; k < mk; ++k) A[(size_t)r * mk + k] = A[(size_t)r * mk + k] - fct * A[(size_t)c * mk + k];
+            b[r] = b[r] - fct * b[c];
+        }
+    }
+    g.assign(mk, 0.0);
+    for (int r = mk - 1; r >= 0; --r) {
+        double t = b[r];
+        for (int k = r + 1; k < mk; ++k) t = t - A[(size_t)r * mk + k] * g[k];
+        g[r] = t / A[(size_t)r * mk + r];
+    }
+    for (int j = 0; j < mk; ++j)
+        if (!std::isfinite(g[j])) return false;
+    return true;
+}
+
+// anderson_loop (projected_jacobi.cpp:242-314): z = [x; lambda], f = g(z) - z with g one sweep,
+// z_{k+1} = g(z_k) - (dZ + dF) gamma over the last m residual differences
+SolveResult pj_solve_anderson(PJ& P, double* rhs, const double* Mdiag, double* lam, double* x, int max_iter,
+                              double tol_abs, double tol_rel, int m, int omp_all, std::vector<double>* trace) {
+    SolveResult res;
+    pj_init(P, rhs, Mdiag, lam, x, omp_all);
+    if (P.nrows == 0) return res;
+    const int nv = P.nv, nr = P.nrows, nt = nv + nr;
+    m = std::max(1, m);
+    std::vector<double> dlam(nr), acc(nv), z(nt), w(nt), f(nt), xprev(nv), cand(nt);
+    std::copy(x, x + nv, z.begin());
+    std::copy(lam, lam + nr, z.begin() + nv);
+    std::vector<std::vector<double>> Zh, Fh;
+    for (int it = 0; it < std::max(1, max_iter); ++it) {
+        std::copy(z.begin(), z.begin() + nv, x);
+        std::copy(z.begin() + nv, z.end(), lam);
+        std::copy(x, x + nv, xprev.begin());
+        SweepOut so = pj_sweep(P, x, lam, dlam.data(), acc.data(), Mdiag, omp_all);
+        std::copy(x, x + nv, w.begin());
+        std::copy(lam, lam + nr, w.begin() + nv);
+        for (int t = 0; t < nt; ++t) f[t] = w[t] - z[t];
+        res.iters = it + 1;
+        res.res_last = rel_residual(so);
+        if (trace) trace->insert(trace->end(), lam, lam + nr);
+        const double err = vel_residual_chunked(x, xprev.data(), nv, tol_rel, tol_abs);
+        if (err <= 1.0) {
+            z = w;
+            break;
+        }
+        Zh.push_back(z);
+        Fh.push_back(f);
+        if ((int)Fh.size() > m + 1) {
+            Zh.erase(Zh.begin());
+            Fh.erase(Fh.begin());
+        }
+        const int mk = (int)Fh.size() - 1;
+        if (mk < 1) {
+            z = w;
+            continue;
+        }
+        std::vector<std::vector<double>> dF(mk, std::vector<double>(nt)), dZ(mk, std::vector<double>(nt));
+        for (int j = 0; j < mk; ++j)
+            for (int t = 0; t < nt; ++t) {
+                dF[j][t] = Fh[j + 1][t] - Fh[j][t];
+                dZ[j][t] = Zh[j + 1][t] - Zh[j][t];
+            }
+        std::vector<double> gam;
+        bool ok = anderson_ls(dF, f, nt, gam);
+        if (ok) {
+            for (int t = 0; t < nt && ok; ++t) {
+                double s = 0.0;
+                for (int j = 0; j < mk; ++j) s = s + (dZ[j][t] + dF[j][t]) * gam[j];
+                cand[t] = w[t] - s;
+                ok = std::isfinite(cand[t]);
+            }
+        }
+        if (ok) {
+            z = cand;
+        } else {
+            z = w;
+            Zh.clear();
+            Fh.clear();
+        }
+    }
+    std::copy(z.begin(), z.begin() + nv, x);
+    std::copy(z.begin() + nv, z.end(), lam);
+    SweepOut fin = pj_sweep(P, x, lam, dlam.data(), acc.data(), Mdiag, omp_all, false);
+    res.res_final = rel_residual(fin);
+    return res;
+}
+
 // MoreauIntegrator::step (src/physics/integration/moreau.cpp:6-13)
 void step_once(Engine& E) {
     const int N = E.N, S = E.S, nv = 6 * N;
@@ -851,6 +963,9 @@ void step_once(Engine& E) {
         else if (E.cfg.pj_chebyshev)
             sr = pj_solve_chebyshev(P, rhs.data(), E.Mdiag.data(), lam.data(), x.data(), E.cfg.pj_max_iterations,
                                     E.cfg.pj_tol_abs, E.cfg.pj_tol_rel, omp_all, tr);
+        else if (E.cfg.pj_anderson)
+            sr = pj_solve_anderson(P, rhs.data(), E.Mdiag.data(), lam.data(), x.data(), E.cfg.pj_max_iterations,
+                                   E.cfg.pj_tol_abs, E.cfg.pj_tol_rel, E.cfg.pj_anderson_m, omp_all, tr);
         else
             sr = pj_solve(P, rhs.data(), E.Mdiag.data(), lam.data(), x.data(), E.cfg.pj_max_iterations,
                           E.cfg.pj_tol_abs, E.cfg.pj_tol_rel, E.cfg.residual_tol, omp_all, tr);

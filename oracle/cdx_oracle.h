@@ -43,6 +43,8 @@ typedef struct or_config {
     double pj_nesterov_beta_threshold;   /* pj.nesterov_beta_threshold */
     int32_t pj_nesterov_restart_limit;   /* pj.nesterov_restart_limit */
     int32_t pj_chebyshev;                /* pj.chebyshev */
+    int32_t pj_anderson;                 /* pj.anderson */
+    int32_t pj_anderson_m;               /* pj.anderson_m */
 } or_config;
 
 typedef struct or_scene {

@@ -59,6 +59,8 @@ class OrConfig(C.Structure):
         ("pj_nesterov_beta_threshold", C.c_double),
         ("pj_nesterov_restart_limit", C.c_int32),
         ("pj_chebyshev", C.c_int32),
+        ("pj_anderson", C.c_int32),
+        ("pj_anderson_m", C.c_int32),
     ]
 
 
@@ -146,6 +148,8 @@ def config_from(cfg: dict, omp_mode: int = 0, num_threads: int = 0) -> OrConfig:
     c.pj_nesterov_beta_threshold = float(cfg.get("pj.nesterov_beta_threshold", 1.0))
     c.pj_nesterov_restart_limit = int(cfg.get("pj.nesterov_restart_limit", 10000))
     c.pj_chebyshev = int(bool(cfg.get("pj.chebyshev", False)))
+    c.pj_anderson = int(bool(cfg.get("pj.anderson", False)))
+    c.pj_anderson_m = int(cfg.get("pj.anderson_m", 2))
     c.omp_mode = omp_mode
     c.num_threads = num_threads
     return c

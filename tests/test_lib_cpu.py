@@ -140,3 +140,8 @@ def test_acceleration_keys(cdxlib):
     c.set("pj.nesterov_restart_limit", 7)
     assert c.get("pj_nesterov") == 1 and c.get("pj_chebyshev") == 1
     assert c.get("pj_nesterov_beta_threshold") == 0.9 and c.get("pj_nesterov_restart_limit") == 7
+    assert c.get("pj_anderson") == 0 and c.get("pj_anderson_m") == 2
+    c.set("solver.anderson", "yes").set("pj.anderson_m", 0)
+    assert c.get("pj_anderson") == 1 and c.get("pj_anderson_m") == 1  # the window is at least 1
+    c.set("pj.anderson_m", 5)
+    assert c.get("pj_anderson_m") == 5

@@ -179,3 +179,34 @@ def test_omp_modes_bit_identical(oracle_mod):
     b.step(120)
     for k in ("pos", "quat", "vel", "omega"):
         assert np.array_equal(a.state()[k], b.state()[k]), k
+
+
+def test_accelerated_loops_precedence_and_fixed_point(oracle_mod):
+    # precedence of the flags (projected_jacobi.cpp:470-489): Nesterov > Chebyshev > Anderson; and
+    # every loop converges to the plain loop's fixed point (same step, tight tolerances)
+    from cardillocxx_gb300 import scenes
+    s = scenes.generate("pile_1k", scale=0.1)
+    base = scenes.config_for("pile_1k")
+    warm = oracle_mod.Oracle(s, base)
+    warm.step(60)
+    st = warm.state()
+    s2 = dict(s, pos=st["pos"], quat=st["quat"], vel=st["vel"], omega=st["omega"])
+
+    def one(**extra):
+        c = scenes.config_for("pile_1k", **{"pj.tol_abs": 1e-10, "pj.tol_rel": 1e-9, "pj.max_iterations": 20000,
+                                            "pj.warmstart": False, **extra})
+        o = oracle_mod.Oracle(s2, c)
+        o.step(1)
+        return o.state()["vel"], o.stats()["iterations"]
+
+    v_plain, it_plain = one()
+    v_cheb, _ = one(**{"pj.chebyshev": True})
+    v_and, it_and = one(**{"pj.anderson": True})
+    v_and5, _ = one(**{"pj.anderson": True, "pj.anderson_m": 5})
+    v_nes, _ = one(**{"pj.nesterov": True})
+    assert np.array_equal(one(**{"pj.chebyshev": True, "pj.anderson": True})[0], v_cheb)
+    assert np.array_equal(one(**{"pj.nesterov": True, "pj.anderson": True})[0], v_nes)
+    scale = np.max(np.abs(v_plain))
+    for v in (v_cheb, v_and, v_and5, v_nes):
+        assert np.max(np.abs(v - v_plain)) <= 1e-5 * scale
+    assert it_and < it_plain

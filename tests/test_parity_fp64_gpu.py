@@ -214,7 +214,8 @@ def test_accelerated_loops_bit_identical(gpu, oracle_mod):
     # GPU runs the same sweeps, extrapolations, restarts and stop tests as the oracle, bit for bit
     s = scenes.generate("pile_1k", scale=0.2)
     for extra in ({"pj.nesterov": True}, {"pj.chebyshev": True},
-                  {"pj.nesterov": True, "pj.nesterov_beta_threshold": 0.5, "pj.nesterov_restart_limit": 3}):
+                  {"pj.nesterov": True, "pj.nesterov_beta_threshold": 0.5, "pj.nesterov_restart_limit": 3},
+                  {"pj.anderson": True}, {"pj.anderson": True, "pj.anderson_m": 5}):
         cfg = scenes.config_for("pile_1k", **{"pj.tol_abs": 1e-6, "pj.tol_rel": 1e-5, "pj.max_iterations": 400,
                                               **extra})
         eng, orc = run_pair(oracle_mod, s, cfg, 150, 50)
@@ -222,10 +223,10 @@ def test_accelerated_loops_bit_identical(gpu, oracle_mod):
 
 
 def test_accelerated_loops_with_zero_tolerances_run_the_cap(gpu, oracle_mod):
-    # with both tolerances 0 the reference's residual is not finite: Nesterov restarts every sweep
-    # and Chebyshev never stops early; both still match the oracle
+    # with both tolerances 0 the reference's residual is not finite: Nesterov restarts every sweep,
+    # Chebyshev and Anderson never stop early; all still match the oracle
     s = scenes.generate("pile_1k", scale=0.15)
-    for extra in ({"pj.nesterov": True}, {"pj.chebyshev": True}):
+    for extra in ({"pj.nesterov": True}, {"pj.chebyshev": True}, {"pj.anderson": True}):
         cfg = scenes.config_for("pile_1k", **extra)
         eng, orc = run_pair(oracle_mod, s, cfg, 60, 30)
         assert orc.stats()["iterations"] == cfg["pj.max_iterations"]
