@@ -66,7 +66,7 @@ typedef struct cdx_config {
     int32_t gpu_precision;            /* gpu.precision: CDX_PRECISION_FP64 | CDX_PRECISION_SPLIT */
     double gpu_residual_tol;          /* gpu.residual_tol: stop when the complementarity residual <= tol (0 off) */
     int32_t gpu_check_every;          /* gpu.check_every: the split-form stop rule runs every k sweeps */
-    int32_t gpu_block;                /* gpu.block: threads per block for contact kernels (0 = auto) */
+    int32_t gpu_block;                /* gpu.block: reserved, ignored (each kernel has its own launch shape) */
     double gpu_contact_capacity_factor; /* gpu.contact_capacity: initial contact slots per body */
     int32_t gpu_use_graph;            /* gpu.graph: capture the solver loop in a CUDA graph (split form) */
     int32_t gpu_autotune;             /* gpu.autotune: pick the contact-sweep launch shape by timing (split form) */
