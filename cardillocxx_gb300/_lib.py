@@ -65,6 +65,7 @@ class CdxConfig(C.Structure):
         ("pj_chebyshev", C.c_int32),
         ("pj_anderson", C.c_int32),
         ("pj_anderson_m", C.c_int32),
+        ("pj_rdiag_true_delassus", C.c_int32),
     ]
 
 

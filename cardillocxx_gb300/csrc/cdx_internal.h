@@ -84,6 +84,8 @@ struct Contacts {
     double* cb = nullptr;     // 3*cap
     double* biasR = nullptr;  // 3*cap
     double* dlam = nullptr;   // 3*cap
+    double* rb = nullptr;     // 9*cap: inverse Delassus block / alpha (pj.rdiag_true_delassus only)
+    int32_t* rb_full = nullptr;  // device flag: some block is not diagonal (full 3x3 products)
     double* mu = nullptr;
     double* eN = nullptr;
     double* eT = nullptr;
@@ -190,6 +192,7 @@ void launch_xinit64(const Scene& sc, const Contacts& C, int gen, const Incidence
                     cudaStream_t s);
 void launch_sweep_contact64(const Scene& sc, Contacts& C, int gen, int nc, const double* x, DevScalars* ds, int dry,
                             cudaStream_t s);
+void launch_block_invert64(const Contacts& C, int nc, cudaStream_t s);
 void launch_sweep_body64(const Scene& sc, const Contacts& C, const Incidence& inc, double* x, double tol_abs,
                          double tol_rel, int want_velres, DevScalars* ds, cudaStream_t s);
 void launch_check(DevScalars* ds, int iter, double residual_tol, int nv, int check_vel, cudaStream_t s);

@@ -99,6 +99,7 @@ int cdx_config_default(cdx_config* c) {
     c->pj_chebyshev = 0;
     c->pj_anderson = 0;
     c->pj_anderson_m = 2;
+    c->pj_rdiag_true_delassus = 0;
     return CDX_OK;
 }
 
@@ -192,6 +193,8 @@ int cdx_config_set(cdx_config* c, const char* key_c, const char* val_c) {
         c->pj_anderson = as_bool(val);
     } else if (key_is(key, "pj.anderson_m")) {
         if (as_int(val, &i)) c->pj_anderson_m = std::max(1, i);
+    } else if (key_is(key, "pj.rdiag_true_delassus")) {
+        c->pj_rdiag_true_delassus = as_bool(val);
     }
     return CDX_OK;  // unknown keys are ignored, as in the reference
 }

@@ -321,6 +321,10 @@ int Engine::ensure_contacts(int64_t need) {
     double** d1[] = {&n.mu, &n.eN, &n.eT};
     for (auto p : d1)
         if ((st = dalloc((void**)p, sizeof(double) * cap, "contacts"))) return st;
+    if (cfg.pj_rdiag_true_delassus && cfg.gpu_precision == CDX_PRECISION_FP64) {
+        if ((st = dalloc((void**)&n.rb, sizeof(double) * 9 * cap, "contact blocks"))) return st;
+        if ((st = dalloc((void**)&n.rb_full, sizeof(int32_t), "contact blocks"))) return st;
+    }
     for (int gidx = 0; gidx < 2; ++gidx) {
         if ((st = dalloc((void**)&n.key[gidx], sizeof(unsigned long long) * cap, "contacts"))) return st;
         if ((st = dalloc((void**)&n.point[gidx], sizeof(double) * 3 * cap, "contacts"))) return st;
@@ -342,7 +346,8 @@ int Engine::ensure_contacts(int64_t need) {
     }
     if (C.cap > 0) {
         void* old[] = {C.a, C.b, C.flags, C.rank, C.dir, C.cA, C.cB, C.rd, C.rcA, C.rcB, C.cb, C.biasR, C.dlam,
-                       C.mu, C.eN, C.eT, C.key[0], C.key[1], C.point[0], C.point[1], C.lam[0], C.lam[1]};
+                       C.mu, C.eN, C.eT, C.key[0], C.key[1], C.point[0], C.point[1], C.lam[0], C.lam[1],
+                       C.rb, C.rb_full};
         for (void* p : old) dfree(p);
         ++reallocations;
     }
@@ -414,9 +419,11 @@ int Engine::collide64() {
 int Engine::setup64() {
     int st;
     const double match2 = cfg.collision_match_max_dist * cfg.collision_match_max_dist;
+    if (C.rb_full) cudaMemsetAsync(C.rb_full, 0, sizeof(int32_t), stream);
     launch_contact_setup64(sc, C, gen, nc, prev_count, cfg.pj_alpha, match2, cfg.pj_warmstart, stream);
+    launch_block_invert64(C, nc, stream);
     launch_frictionless_flags(C, nc, isfl, stream);
-    launches += nc > 0 ? 2 : 0;
+    launches += nc > 0 ? (C.rb ? 3 : 2) : 0;
     if (nc > 0) {
         if ((st = cuda_check(exclusive_scan(tmp, tmp_bytes, isfl, flscan, nc, stream), "scan"))) return st;
         launches += 2;

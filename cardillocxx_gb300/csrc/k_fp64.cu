@@ -446,6 +446,8 @@ __global__ void k_contact_setup64(Scene sc, Contacts C, int gen, int nc, int pre
         mB[0] = ml; mB[1] = ml; mB[2] = ml; mB[3] = ma; mB[4] = ma; mB[5] = ma;
     }
     const int nr = fr ? 3 : 1;
+    const bool block = C.rb != nullptr;
+    double D0 = 0.0;
     for (int r = 0; r < 3; ++r) {
         if (r >= nr) {
 #pragma unroll
@@ -475,7 +477,9 @@ __global__ void k_contact_setup64(Scene sc, Contacts C, int gen, int nc, int pre
         const double e = r == 0 ? C.eN[c] : C.eT[c];
         const double bias = cbv[r] + e * vp;
         for (int k = 0; k < ne; ++k) D = D + (val[k] * val[k]) * mi[k];
-        const double Rr = (D > 0.0) ? (alpha / D) : 0.0;
+        if (r == 0) D0 = D;
+        // pj.rdiag_true_delassus keeps W and the bias unscaled (projected_jacobi.cpp:341-343)
+        const double Rr = block ? 1.0 : ((D > 0.0) ? (alpha / D) : 0.0);
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             C.rd[(3 * r + k) * cap + c] = Rr * d[3 * r + k];
@@ -484,6 +488,128 @@ __global__ void k_contact_setup64(Scene sc, Contacts C, int gen, int nc, int pre
         }
         C.biasR[r * cap + c] = Rr * bias;
     }
+    if (block) {
+        // the contact's Delassus block / alpha (buildBlockPreconditioner, projected_jacobi.cpp:81-98):
+        // D_rs = sum over the row entries (A linear, A angular, B linear, B angular) of
+        // (W_rk Minv_k) W_sk; inverted by k_block_invert64 once every block of the step is known
+        const double inv_alpha = (alpha > 0.0) ? (1.0 / alpha) : 0.0;
+        if (!fr) {
+            C.rb[c] = D0 * inv_alpha;
+        } else {
+            double w[3][12], mm[12];
+            int ne = 0;
+            for (int r = 0; r < 3; ++r) {
+                ne = 0;
+                if (a >= 0) {
+                    for (int k = 0; k < 3; ++k) { w[r][ne] = -d[3 * r + k]; mm[ne] = mA[k]; ++ne; }
+                    for (int k = 0; k < 3; ++k) { w[r][ne] = -cA[3 * r + k]; mm[ne] = mA[3 + k]; ++ne; }
+                }
+                for (int k = 0; k < 3; ++k) { w[r][ne] = d[3 * r + k]; mm[ne] = mB[k]; ++ne; }
+                for (int k = 0; k < 3; ++k) { w[r][ne] = cB[3 * r + k]; mm[ne] = mB[3 + k]; ++ne; }
+            }
+            double Db[9];
+            for (int r = 0; r < 3; ++r)
+                for (int s = 0; s < 3; ++s) {
+                    double acc = 0.0;
+                    for (int q = 0; q < ne; ++q) acc = acc + (w[r][q] * mm[q]) * w[s][q];
+                    Db[3 * r + s] = acc * inv_alpha;
+                }
+            for (int k = 0; k < 9; ++k) C.rb[(size_t)k * cap + c] = Db[k];
+            // MatrixBase::isDiagonal (Eigen 3, precision 1e-12); one non-diagonal block switches
+            // every block of the step to the full inverse (BlockDiagonal::calculateInverse)
+            double md = -1.0;
+            for (int j = 0; j < 3; ++j) md = smax(md, fabs(Db[4 * j]));
+            bool diag = true;
+            for (int j = 0; j < 3; ++j)
+                for (int i = 0; i < j; ++i)
+                    diag = diag && (fabs(Db[3 * i + j]) <= md * 1e-12) && (fabs(Db[3 * j + i]) <= md * 1e-12);
+            if (!diag) *C.rb_full = 1;
+        }
+    }
+}
+
+// invertSmallSpd (misc/block_diagonal.hpp:15-27) for n <= 3, row-major: Cholesky from the lower
+// triangle, column by column, then forward and back substitution of each identity column; a
+// pivot that is not positive takes the reference's last fallback, the diagonal inverse
+__device__ void spd_inverse_dev(const double* A, int n, double* X) {
+    double L[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    bool ok = true;
+    for (int j = 0; j < n && ok; ++j) {
+        double s = A[j * n + j];
+        for (int k = 0; k < j; ++k) s = s - L[j * 3 + k] * L[j * 3 + k];
+        if (!(s > 0.0)) {
+            ok = false;
+            break;
+        }
+        L[j * 3 + j] = sqrt(s);
+        for (int i = j + 1; i < n; ++i) {
+            double t = A[i * n + j];
+            for (int k = 0; k < j; ++k) t = t - L[i * 3 + k] * L[j * 3 + k];
+            L[i * 3 + j] = t / L[j * 3 + j];
+        }
+    }
+    if (!ok) {
+        for (int i = 0; i < n * n; ++i) X[i] = 0.0;
+        for (int i = 0; i < n; ++i) X[i * n + i] = 1.0 / A[i * n + i];
+        return;
+    }
+    for (int c = 0; c < n; ++c) {
+        double y[3];
+        for (int i = 0; i < n; ++i) {
+            double t = (i == c) ? 1.0 : 0.0;
+            for (int k = 0; k < i; ++k) t = t - L[i * 3 + k] * y[k];
+            y[i] = t / L[i * 3 + i];
+        }
+        for (int i = n - 1; i >= 0; --i) {
+            double t = y[i];
+            for (int k = i + 1; k < n; ++k) t = t - L[k * 3 + i] * X[k * n + c];
+            X[i * n + c] = t / L[i * 3 + i];
+        }
+    }
+}
+
+// R_block = (D / alpha)^-1 per contact: per diagonal entry when every block of the step is
+// diagonal, else the SPD inverse of every block (1 x 1 blocks included)
+__global__ void k_block_invert64(Contacts C, int nc) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    const int64_t cap = C.cap;
+    const bool full = *(const volatile int32_t*)C.rb_full != 0;
+    if (!(C.flags[c] & CF_FRICTIONAL)) {
+        const double d = C.rb[c];
+        double x;
+        if (full) spd_inverse_dev(&d, 1, &x);
+        else x = 1.0 / d;
+        C.rb[c] = x;
+        return;
+    }
+    double D[9], X[9];
+    for (int k = 0; k < 9; ++k) D[k] = C.rb[(size_t)k * cap + c];
+    if (full) {
+        spd_inverse_dev(D, 3, X);
+    } else {
+        for (int k = 0; k < 9; ++k) X[k] = 0.0;
+        for (int j = 0; j < 3; ++j) X[4 * j] = 1.0 / D[4 * j];
+    }
+    for (int k = 0; k < 9; ++k) C.rb[(size_t)k * cap + c] = X[k];
+}
+
+// BlockDiagonal::applyTo (misc/block_diagonal.hpp:107-126) on one contact's rows g
+__device__ __forceinline__ void block_apply64(const Contacts& C, int c, bool fr, double* g) {
+    const int64_t cap = C.cap;
+    const bool full = *C.rb_full != 0;
+    if (!fr) {
+        g[0] = full ? C.rb[c] * g[0] : g[0] * C.rb[c];
+        return;
+    }
+    if (!full) {
+        for (int j = 0; j < 3; ++j) g[j] = g[j] * C.rb[(size_t)(4 * j) * cap + c];
+        return;
+    }
+    double B[9], s[3];
+    for (int k = 0; k < 9; ++k) B[k] = C.rb[(size_t)k * cap + c];
+    for (int j = 0; j < 3; ++j) s[j] = B[3 * j] * g[0] + B[3 * j + 1] * g[1] + B[3 * j + 2] * g[2];
+    for (int j = 0; j < 3; ++j) g[j] = s[j];
 }
 
 __global__ void k_frictionless_flags(Contacts C, int nc, int32_t* isfl) {
@@ -593,7 +719,7 @@ __global__ void k_sweep_contact64(Scene sc, Contacts C, int gen, int nc, const d
 #pragma unroll
         for (int k = 0; k < 6; ++k) xB[k] = x[(size_t)k * N + b];
         double* lamp = C.lam[gen];
-        double lold[3], lnew[3];
+        double lold[3], lnew[3], gr[3];
         for (int r = 0; r < nr; ++r) {
             double t = 0.0;
             if (a >= 0) {
@@ -606,10 +732,11 @@ __global__ void k_sweep_contact64(Scene sc, Contacts C, int gen, int nc, const d
             for (int k = 0; k < 3; ++k) t = t + C.rd[(3 * r + k) * cap + c] * xB[k];
 #pragma unroll
             for (int k = 0; k < 3; ++k) t = t + C.rcB[(3 * r + k) * cap + c] * xB[3 + k];
-            const double g = t + C.biasR[r * cap + c];
+            gr[r] = t + C.biasR[r * cap + c];
             lold[r] = lamp[r * cap + c];
-            lnew[r] = lold[r] - g;
         }
+        if (C.rb) block_apply64(C, c, fr, gr);
+        for (int r = 0; r < nr; ++r) lnew[r] = lold[r] - gr[r];
         // project (projected_jacobi.cpp:100-119)
         lnew[0] = smax(lnew[0], 0.0);
         if (fr) {
@@ -855,7 +982,9 @@ __global__ void k_linear_contact64(Scene sc, Contacts C, int nc, const double* v
     const int64_t cap = C.cap;
     const int N = sc.N;
     const int a = C.a[c], b = C.b[c];
-    const int nr = (C.flags[c] & CF_FRICTIONAL) ? 3 : 1;
+    const bool fr = (C.flags[c] & CF_FRICTIONAL) != 0;
+    const int nr = fr ? 3 : 1;
+    double gr[3];
     double xA[6], xB[6];
     if (a >= 0)
         for (int k = 0; k < 6; ++k) xA[k] = v[(size_t)k * N + a];
@@ -868,8 +997,10 @@ __global__ void k_linear_contact64(Scene sc, Contacts C, int nc, const double* v
         }
         for (int k = 0; k < 3; ++k) t = t + C.rd[(3 * r + k) * cap + c] * xB[k];
         for (int k = 0; k < 3; ++k) t = t + C.rcB[(3 * r + k) * cap + c] * xB[3 + k];
-        C.dlam[r * cap + c] = t;
+        gr[r] = t;
     }
+    if (C.rb) block_apply64(C, c, fr, gr);
+    for (int r = 0; r < nr; ++r) C.dlam[r * cap + c] = gr[r];
 }
 __global__ void k_linear_body64(Scene sc, Contacts C, Incidence inc, const double* v, double* Mv) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1216,6 +1347,10 @@ void launch_contact_setup64(const Scene& sc, Contacts& C, int gen, int nc, int p
                             double match2, int warmstart, cudaStream_t s) {
     if (nc == 0) return;
     k_contact_setup64<<<nblk(nc), NT, 0, s>>>(sc, C, gen, nc, prev_count, alpha, match2, warmstart);
+}
+void launch_block_invert64(const Contacts& C, int nc, cudaStream_t s) {
+    if (nc == 0 || !C.rb) return;
+    k_block_invert64<<<nblk(nc), NT, 0, s>>>(C, nc);
 }
 void launch_frictionless_flags(const Contacts& C, int nc, int32_t* isfl, cudaStream_t s) {
     if (nc == 0) return;

@@ -80,6 +80,7 @@ typedef struct cdx_config {
     int32_t pj_chebyshev;             /* pj.chebyshev */
     int32_t pj_anderson;              /* pj.anderson */
     int32_t pj_anderson_m;            /* pj.anderson_m: history window (>= 1) */
+    int32_t pj_rdiag_true_delassus;   /* pj.rdiag_true_delassus: per-contact Delassus block preconditioner (plain FP64) */
 } cdx_config;
 
 /* Scene: dynamic spheres plus static shapes (halfspaces, drums). Bodies of one scene are

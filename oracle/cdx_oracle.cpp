@@ -444,6 +444,10 @@ struct PJ {
     const int32_t* col = nullptr;
     const double* val = nullptr;
     std::vector<double> RW, biasR, mu;
+    // pj.rdiag_true_delassus: 0 off (R folded into RW and biasR), 1 every contact block diagonal
+    // (R applied per row), 2 full blocks; Rb1 per frictionless row, Rb9 per frictional contact
+    int bmode = 0;
+    std::vector<double> Rb1, Rb9;
     // column-major copy of W (for the all-OpenMP W^T gather; same per-column row order)
     std::vector<int32_t> cptr, crow;
     std::vector<double> cval;
@@ -461,9 +465,124 @@ inline void project_rows(double* lam, int r, bool frictional, double mu) {
     lam[r + 2] = s * t2;
 }
 
-// build_workspace (projected_jacobi.cpp:316-369) + rdiag_sparse (:57-69)
+// MatrixBase::isDiagonal of Eigen 3 with its default precision for double (1e-12): every
+// off-diagonal entry at most 1e-12 times the largest diagonal magnitude
+bool block_is_diagonal(const double* A, int n) {
+    double md = -1.0;
+    for (int j = 0; j < n; ++j) md = std::max(md, std::fabs(A[j * n + j]));
+    for (int j = 0; j < n; ++j)
+        for (int i = 0; i < j; ++i)
+            if (!(std::fabs(A[i * n + j]) <= md * 1e-12) || !(std::fabs(A[j * n + i]) <= md * 1e-12)) return false;
+    return true;
+}
+
+// invertSmallSpd (misc/block_diagonal.hpp:15-27): Cholesky A = L L^T from the lower triangle,
+// column by column, then the inverse column by column (forward, then back substitution of the
+// identity). A block of a contact between spheres of positive mass is positive definite, so the
+// reference's LDLT fallback is not reached; a failed pivot takes its last fallback, the diagonal.
+void spd_inverse(const double* A, int n, double* X) {
+    double L[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    bool ok = true;
+    for (int j = 0; j < n && ok; ++j) {
+        double s = A[j * n + j];
+        for (int k = 0; k < j; ++k) s = s - L[j * 3 + k] * L[j * 3 + k];
+        if (!(s > 0.0)) { ok = false; break; }
+        L[j * 3 + j] = std::sqrt(s);
+        for (int i = j + 1; i < n; ++i) {
+            double t = A[i * n + j];
+            for (int k = 0; k < j; ++k) t = t - L[i * 3 + k] * L[j * 3 + k];
+            L[i * 3 + j] = t / L[j * 3 + j];
+        }
+    }
+    if (!ok) {
+        for (int i = 0; i < n * n; ++i) X[i] = 0.0;
+        for (int i = 0; i < n; ++i) X[i * n + i] = 1.0 / A[i * n + i];
+        return;
+    }
+    for (int c = 0; c < n; ++c) {
+        double y[3];
+        for (int i = 0; i < n; ++i) {
+            double t = (i == c) ? 1.0 : 0.0;
+            for (int k = 0; k < i; ++k) t = t - L[i * 3 + k] * y[k];
+            y[i] = t / L[i * 3 + i];
+        }
+        for (int i = n - 1; i >= 0; --i) {
+            double t = y[i];
+            for (int k = i + 1; k < n; ++k) t = t - L[k * 3 + i] * X[k * n + c];
+            X[i * n + c] = t / L[i * 3 + i];
+        }
+    }
+}
+
+// buildBlockPreconditioner (projected_jacobi.cpp:81-98) and BlockDiagonal::calculateInverse
+// (misc/block_diagonal.hpp:86-98): per contact D / alpha, D its block of W M^-1 W^T (the rows of
+// one contact share their columns; D_ab = sum over those columns of (W_ak Minv_k) W_bk, the
+// order of W_sel * Minv * W_sel^T), inverted per block, or per diagonal entry when every block
+// of the step is diagonal
+void block_setup(PJ& P, const double* minv, double alpha) {
+    const double inv_alpha = (alpha > 0.0) ? (1.0 / alpha) : 0.0;
+    const int nb = (P.nrows - P.nfl) / 3;
+    std::vector<double> D1(P.nfl), D9(9 * (size_t)nb);
+    for (int r = 0; r < P.nfl; ++r) {
+        double d = 0.0;
+        for (int k = P.ptr[r]; k < P.ptr[r + 1]; ++k) d = d + P.val[k] * P.val[k] * minv[P.col[k]];
+        D1[r] = d * inv_alpha;
+    }
+    bool diag = true;
+    for (int b = 0; b < nb; ++b) {
+        const int r0 = P.nfl + 3 * b;
+        const int len = P.ptr[r0 + 1] - P.ptr[r0];
+        for (int a = 0; a < 3; ++a)
+            for (int c = 0; c < 3; ++c) {
+                const int pa = P.ptr[r0 + a], pc = P.ptr[r0 + c];
+                double d = 0.0;
+                for (int q = 0; q < len; ++q) d = d + (P.val[pa + q] * minv[P.col[pa + q]]) * P.val[pc + q];
+                D9[9 * (size_t)b + 3 * a + c] = d * inv_alpha;
+            }
+        diag = diag && block_is_diagonal(&D9[9 * (size_t)b], 3);
+    }
+    P.Rb1.assign(P.nfl, 0.0);
+    P.Rb9.assign(9 * (size_t)nb, 0.0);
+    P.bmode = diag ? 1 : 2;
+    for (int r = 0; r < P.nfl; ++r) {
+        if (diag) P.Rb1[r] = 1.0 / D1[r];
+        else spd_inverse(&D1[r], 1, &P.Rb1[r]);
+    }
+    for (int b = 0; b < nb; ++b) {
+        const double* D = &D9[9 * (size_t)b];
+        double* X = &P.Rb9[9 * (size_t)b];
+        if (diag) {
+            for (int a = 0; a < 3; ++a) X[4 * a] = 1.0 / D[4 * a];
+        } else {
+            spd_inverse(D, 3, X);
+        }
+    }
+}
+
+// BlockDiagonal::applyTo (misc/block_diagonal.hpp:107-126): g <- R_block g, per row when every
+// block is diagonal, else per contact block (rows a: (B_a0 g0 + B_a1 g1) + B_a2 g2)
+void block_apply(const PJ& P, double* g) {
+    const int nb = (P.nrows - P.nfl) / 3;
+    if (P.bmode == 1) {
+        for (int r = 0; r < P.nfl; ++r) g[r] = g[r] * P.Rb1[r];
+        for (int b = 0; b < nb; ++b)
+            for (int a = 0; a < 3; ++a) g[P.nfl + 3 * b + a] = g[P.nfl + 3 * b + a] * P.Rb9[9 * (size_t)b + 4 * a];
+        return;
+    }
+    for (int r = 0; r < P.nfl; ++r) g[r] = P.Rb1[r] * g[r];
+    for (int b = 0; b < nb; ++b) {
+        double* v = g + P.nfl + 3 * b;
+        const double* B = &P.Rb9[9 * (size_t)b];
+        double s[3];
+        for (int a = 0; a < 3; ++a) s[a] = B[3 * a] * v[0] + B[3 * a + 1] * v[1] + B[3 * a + 2] * v[2];
+        for (int a = 0; a < 3; ++a) v[a] = s[a];
+    }
+}
+
+// build_workspace (projected_jacobi.cpp:316-369) + rdiag_sparse (:57-69); with block = 1 the rows
+// and the bias stay unscaled and R_block is built instead (:341-347)
 void pj_setup(PJ& P, const double* cb, const double* e, const double* mu, const double* minv, const double* vn,
-              double alpha, int omp_all) {
+              double alpha, int omp_all, int block = 0) {
     P.RW.assign(P.ptr[P.nrows], 0.0);
     P.biasR.assign(P.nrows, 0.0);
     P.mu.assign(mu, mu + P.nrows);
@@ -474,10 +593,17 @@ void pj_setup(PJ& P, const double* cb, const double* e, const double* mu, const 
         vp = vp + cb[r];
         const double bias = cb[r] + e[r] * vp;
         for (int k = P.ptr[r]; k < P.ptr[r + 1]; ++k) D = D + (P.val[k] * P.val[k]) * minv[P.col[k]];
+        if (block) {
+            for (int k = P.ptr[r]; k < P.ptr[r + 1]; ++k) P.RW[k] = P.val[k];
+            P.biasR[r] = bias;
+            continue;
+        }
         const double R = (D > 0.0) ? (alpha / D) : 0.0;
         for (int k = P.ptr[r]; k < P.ptr[r + 1]; ++k) P.RW[k] = R * P.val[k];
         P.biasR[r] = R * bias;
     }
+    P.bmode = 0;
+    if (block) block_setup(P, minv, alpha);
     if (omp_all) {
         std::vector<int32_t> cnt(P.nv + 1, 0);
         for (int k = 0; k < P.ptr[P.nrows]; ++k) cnt[P.col[k] + 1]++;
@@ -526,9 +652,10 @@ SweepOut pj_sweep(PJ& P, double* x, double* lam, double* dlam, double* acc, cons
     for (int r = 0; r < nr; ++r) {
         double t = 0.0;
         for (int k = P.ptr[r]; k < P.ptr[r + 1]; ++k) t = t + P.RW[k] * x[P.col[k]];
-        const double g = t + P.biasR[r];
-        lnew[r] = lam[r] - g;
+        lnew[r] = t + P.biasR[r];
     }
+    if (P.bmode) block_apply(P, lnew.data());
+    for (int r = 0; r < nr; ++r) lnew[r] = lam[r] - lnew[r];
     // project(): frictionless rows, then frictional blocks (OpenMP, as the reference)
     for (int r = 0; r < P.nfl; ++r) project_rows(lnew.data(), r, false, 0.0);
     const int nb = (nr - P.nfl) / 3;
@@ -712,6 +839,7 @@ double spectral_radius(const PJ& P, const double* Mdiag, int omp_all) {
             for (int k = P.ptr[r]; k < P.ptr[r + 1]; ++k) t = t + P.RW[k] * v[P.col[k]];
             delta[r] = t;
         }
+        if (P.bmode) block_apply(P, delta.data());
         std::fill(acc.begin(), acc.end(), 0.0);
         wt_accumulate(P, delta.data(), acc.data(), omp_all);
         for (int j = 0; j < nv; ++j) Mv[j] = v[j] - acc[j] / Mdiag[j];
@@ -941,7 +1069,8 @@ void step_once(Engine& E) {
     P.ptr = W.ptr.data();
     P.col = W.col.data();
     P.val = W.val.data();
-    pj_setup(P, W.cb.data(), W.e.data(), W.mu.data(), E.minv.data(), vn.data(), E.cfg.pj_alpha, omp_all);
+    pj_setup(P, W.cb.data(), W.e.data(), W.mu.data(), E.minv.data(), vn.data(), E.cfg.pj_alpha, omp_all,
+             E.cfg.pj_rdiag_true_delassus);
     std::vector<double> lam(W.nrows, 0.0), x(nv);
     for (size_t ci = 0; ci < C.size(); ++ci) {
         const int r0 = W.row_base[ci];
@@ -1119,6 +1248,12 @@ int32_t or_pj_solve_csr(int32_t nrows, int32_t nv, int32_t nfl, const int32_t* r
     pj_setup(P, contact_bias, restitution, mu, minv, v, alpha, 0);
     SolveResult r = pj_solve(P, rhs.data(), mdiag, lambda_inout, x_out, max_iter, tol_abs, tol_rel, 0.0, 0, nullptr);
     return r.iters;
+}
+
+int32_t or_block_inverse(const double* A, int32_t n, double* X) {
+    if (n < 1 || n > 3) return -1;
+    spd_inverse(A, n, X);
+    return block_is_diagonal(A, n) ? 1 : 0;
 }
 
 }  // extern "C"

@@ -61,6 +61,7 @@ class OrConfig(C.Structure):
         ("pj_chebyshev", C.c_int32),
         ("pj_anderson", C.c_int32),
         ("pj_anderson_m", C.c_int32),
+        ("pj_rdiag_true_delassus", C.c_int32),
     ]
 
 
@@ -114,8 +115,21 @@ def lib():
             L.or_pj_solve_csr.argtypes = [C.c_int32, C.c_int32, C.c_int32, _PI, _PI, _P, _P, _P, _P, _P, _P,
                                           _P, _P, _P, C.c_double, C.c_double, C.c_int32, C.c_double,
                                           C.c_double, _P, _P]
+            L.or_block_inverse.restype = C.c_int32
+            L.or_block_inverse.argtypes = [_P, C.c_int32, _P]
             _lib = L
     return _lib
+
+
+def block_inverse(A):
+    """(inverse, counts_as_diagonal) of a small SPD block as the pj.rdiag_true_delassus setup makes it."""
+    A = np.ascontiguousarray(np.asarray(A, np.float64))
+    n = A.shape[0]
+    X = np.zeros((n, n))
+    d = lib().or_block_inverse(_dp(A), n, _dp(X))
+    if d < 0:
+        raise ValueError("block size must be 1..3")
+    return X, bool(d)
 
 
 def _dp(a):
@@ -150,6 +164,7 @@ def config_from(cfg: dict, omp_mode: int = 0, num_threads: int = 0) -> OrConfig:
     c.pj_chebyshev = int(bool(cfg.get("pj.chebyshev", False)))
     c.pj_anderson = int(bool(cfg.get("pj.anderson", False)))
     c.pj_anderson_m = int(cfg.get("pj.anderson_m", 2))
+    c.pj_rdiag_true_delassus = int(bool(cfg.get("pj.rdiag_true_delassus", False)))
     c.omp_mode = omp_mode
     c.num_threads = num_threads
     return c

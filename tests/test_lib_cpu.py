@@ -145,3 +145,5 @@ def test_acceleration_keys(cdxlib):
     assert c.get("pj_anderson") == 1 and c.get("pj_anderson_m") == 1  # the window is at least 1
     c.set("pj.anderson_m", 5)
     assert c.get("pj_anderson_m") == 5
+    assert c.get("pj_rdiag_true_delassus") == 0
+    assert c.set("solver.rdiag_true_delassus", "on").get("pj_rdiag_true_delassus") == 1

@@ -210,3 +210,37 @@ def test_accelerated_loops_precedence_and_fixed_point(oracle_mod):
     for v in (v_cheb, v_and, v_and5, v_nes):
         assert np.max(np.abs(v - v_plain)) <= 1e-5 * scale
     assert it_and < it_plain
+
+
+def test_delassus_block_inverse(oracle_mod):
+    # invertSmallSpd (misc/block_diagonal.hpp:15-27) restated as a Cholesky inverse; Eigen's
+    # isDiagonal test (off-diagonals <= 1e-12 of the largest diagonal) picks the per-row path
+    rng = np.random.default_rng(7)
+    M = rng.normal(size=(3, 3))
+    A = M @ M.T + 3 * np.eye(3)
+    X, diag = oracle_mod.block_inverse(A)
+    assert not diag
+    np.testing.assert_allclose(X @ A, np.eye(3), atol=1e-13)
+    X1, d1 = oracle_mod.block_inverse([[4.0]])
+    assert d1 and X1[0, 0] == 0.25
+    near = np.diag([2.0, 5.0, 5.0])
+    near[0, 1] = near[1, 0] = 1e-13 * 5.0
+    assert oracle_mod.block_inverse(near)[1]
+    near[0, 1] = 1e-11 * 5.0
+    assert not oracle_mod.block_inverse(near)[1]
+
+
+def test_true_delassus_block_matches_row_scale_for_spheres(oracle_mod):
+    # for sphere contacts with isotropic inertia a contact's 3x3 Delassus block is diagonal up to
+    # rounding, so pj.rdiag_true_delassus (projected_jacobi.cpp:81-98, 341-347) takes the per-row
+    # path and ends where the default row scale ends, up to rounding
+    from cardillocxx_gb300 import scenes
+    s = scenes.generate("pile_1k", scale=0.2)
+    out = []
+    for blk in (False, True):
+        o = oracle_mod.Oracle(s, scenes.config_for("pile_1k", **{"pj.rdiag_true_delassus": blk}))
+        o.step(120)
+        out.append((o.state(), o.stats()))
+    assert out[0][1]["num_contacts"] == out[1][1]["num_contacts"] > 0
+    np.testing.assert_allclose(out[1][0]["vel"], out[0][0]["vel"], rtol=0, atol=1e-10)
+    assert not np.array_equal(out[1][0]["vel"], out[0][0]["vel"])  # different rounding: the key is live

@@ -230,3 +230,14 @@ def test_accelerated_loops_with_zero_tolerances_run_the_cap(gpu, oracle_mod):
         cfg = scenes.config_for("pile_1k", **extra)
         eng, orc = run_pair(oracle_mod, s, cfg, 60, 30)
         assert orc.stats()["iterations"] == cfg["pj.max_iterations"]
+
+
+def test_true_delassus_block_preconditioner(gpu, oracle_mod):
+    # pj.rdiag_true_delassus (projected_jacobi.cpp:81-98, 341-347): per-contact Delassus blocks,
+    # the step-wide diagonal test and the per-row application, with frictionless contacts mixed in,
+    # under the standard and the Chebyshev loop; bit for bit against the oracle
+    s = scenes.generate("pile_1k", scale=0.15)
+    s["mu"][::3] = 0.0
+    for extra in ({}, {"pj.chebyshev": True}, {"friction.enable": False}):
+        cfg = scenes.config_for("pile_1k", **{"pj.rdiag_true_delassus": True, "friction.combine": "min", **extra})
+        run_pair(oracle_mod, s, cfg, 80, 40)
