@@ -157,6 +157,8 @@ __global__ void k_s_prep(Scene sc, SplitBuf sb, double dt, double g0, double g1,
         sb.acc[0][2 * i + 1] = sb.vel4[2 * i + 1];
         sb.acc[1][2 * i] = sb.vel4[2 * i];
         sb.acc[1][2 * i + 1] = sb.vel4[2 * i + 1];
+        sb.acc[2][2 * i] = sb.vel4[2 * i];
+        sb.acc[2][2 * i + 1] = sb.vel4[2 * i + 1];
         const int s = sc.body_scene[i];
         const double* o = &sb.origin[3 * s];
         sb.pos4[i] = make_float4((float)(x[0] - o[0]), (float)(x[1] - o[1]), (float)(x[2] - o[2]),
@@ -468,11 +470,11 @@ __global__ void k_s_apply_warm(SplitBuf sb, int gen) {
 }
 
 // One projected Jacobi sweep, one kernel. PJ keeps x_k = x_free + M^-1 W^T lambda_k
-// (projected_jacobi.cpp:361-363, 134-137), so three rotating velocity buffers replace the body
+// (projected_jacobi.cpp:361-363, 134-137), so four rotating velocity buffers replace the body
 // pass: the sweep reads the body velocities x_k from A_k, computes lambda_{k+1} for every contact
 // and adds the full M^-1 W^T lambda_{k+1} into A_{k+1} (float4 vector atomics), which holds x_free;
-// A_{k+2}, untouched by this sweep, is reset to x_free for the next one. There is no separate body pass and no FP32 accumulation across
-// sweeps. The sweep is latency-bound (contact record -> body gathers -> atomics): each thread takes
+// A_{k-1}, read by the previous sweep, is reset to x_free for sweep k + 2 to add into. There is no
+// separate body pass and no FP32 accumulation across sweeps. The sweep is latency-bound (contact record -> body gathers -> atomics): each thread takes
 // UNROLL contacts and issues all record loads, then all gathers, before computing; read-only data
 // goes through the non-coherent path; the grid is a whole number of resident waves. The last block
 // to finish (completion counter, no waiting) reduces the per-block maxima and runs the stop rule.
@@ -657,9 +659,9 @@ __global__ void __launch_bounds__(NTH, MINB) k_s_sweep_t(SplitBuf sb, int gen, f
         return;
     }
     const int k = sb.ss->iters;
-    const float4* __restrict__ Acur = sb.acc[k % 3];
-    float4* Anxt = sb.acc[(k + 1) % 3];
-    float4* Aclr = sb.acc[(k + 2) % 3];
+    const float4* __restrict__ Acur = sb.acc[k % SPLIT_NACC];
+    float4* Anxt = sb.acc[(k + 1) % SPLIT_NACC];
+    float4* Aclr = sb.acc[(k + 3) % SPLIT_NACC];
     const int nc = *sb.nc_dev;
     float maxd = 0.f, maxl = 0.f;
     const int T = gridDim.x * blockDim.x;
@@ -767,7 +769,8 @@ __device__ __forceinline__ unsigned long long global_ns() {
     return t;
 }
 
-// Grid barrier of a cooperative launch (all blocks resident) that also reduces the per-sweep maxima.
+// Grid barrier of a cooperative launch (all blocks resident) that also reduces the per-sweep maxima,
+// in two halves (grid_arrive, grid_wait_max) so a block can do independent work in between.
 // Block g writes (max ||dlambda||, max |lambda|) into its own record, then thread 0 adds one to the
 // arrival counter and waits until it reaches the barrier's target (epoch x blocks). After the
 // barrier warp 0 reads every block's record (independent loads, one round trip) and takes the
@@ -776,19 +779,28 @@ __device__ __forceinline__ unsigned long long global_ns() {
 // COOP_WAIT_NS, or once another block has given up, the block sets *err and returns false.
 constexpr unsigned long long COOP_WAIT_NS = 200000000ull;  // 0.2 s
 constexpr int COOP_MAX_GRID = 256;                         // records a lane reads: COOP_MAX_GRID / 32
-__device__ __forceinline__ bool grid_sync_max(unsigned* ctr, float2* recs, unsigned epoch, int32_t* err, bool reduce,
+// Arrival half: publish the block's maxima and add one to the counter (after every thread's
+// writes of the sweep, through __syncthreads and a fence).
+__device__ __forceinline__ void grid_arrive(unsigned* ctr, float2* recs, unsigned epoch, bool reduce, float maxd,
+                                            float maxl) {
+    float2* bank = recs + (size_t)(epoch & 1u) * SPLIT_MAX_PARTS;
+    if (reduce && threadIdx.x == 0) bank[blockIdx.x] = make_float2(maxd, maxl);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(ctr, 1u);
+    }
+}
+// Waiting half: thread 0 waits (bounded) for every block's arrival, then warp 0 reduces the records.
+__device__ __forceinline__ bool grid_wait_max(unsigned* ctr, float2* recs, unsigned epoch, int32_t* err, bool reduce,
                                               float& maxd, float& maxl) {
     __shared__ float s_md, s_ml;
     __shared__ int s_ok;
     float2* bank = recs + (size_t)(epoch & 1u) * SPLIT_MAX_PARTS;
-    if (reduce && threadIdx.x == 0) bank[blockIdx.x] = make_float2(maxd, maxl);
-    __syncthreads();
     if (threadIdx.x < 32) {
         const unsigned FULL = 0xffffffffu;
         int ok = 1;
         if (threadIdx.x == 0) {
-            __threadfence();
-            atomicAdd(ctr, 1u);
             const unsigned target = epoch * gridDim.x;
             const unsigned long long t0 = global_ns();
             while ((int)(ld_acquire(ctr) - target) < 0) {
@@ -837,10 +849,14 @@ __device__ __forceinline__ bool grid_sync_max(unsigned* ctr, float2* recs, unsig
 // impulses into shared memory once (48 B a contact) and keeps them there across sweeps; the frame
 // and R are recomputed each sweep (keeping t1 and R in shared memory as well measured slower: they
 // crowd the free velocities out and lengthen the chain after the gathers). Each sweep then touches
-// L2/HBM only for the body velocities (gathers from A_k, reductions into A_{k+1}, the reset of A_{k+2}
+// L2/HBM only for the body velocities (gathers from A_k, reductions into A_{k+1}, the reset of A_{k-1}
 // from the free velocities, which also sit in shared memory when they fit). Sweeps are separated by
-// a grid barrier that also gathers the per-sweep maxima, so every block evaluates the same stop
-// rule on the same numbers; block 0 records the iteration count for the host.
+// a split grid barrier that also gathers the per-sweep maxima, so every block evaluates the same
+// stop rule on the same numbers: a block arrives once its reductions are issued, resets A_{k-1}
+// while the others arrive, then waits. A_{k-1} is safe to reset there: every block finished sweep
+// k - 1 (its last reader) before this barrier's previous one let anybody through, and the first
+// sweep to add into it again (k + 2) starts only after this block arrives at the next barrier.
+// Block 0 records the iteration count for the host.
 template <int NTH, int UNROLL, int AGG>
 __global__ void __launch_bounds__(NTH, 1) k_s_solve_coop(SplitBuf sb, int gen, float alpha, int max_iter, float tol,
                                                          int cpb, int bpb, int vf_smem, int max_sweeps,
@@ -881,9 +897,9 @@ __global__ void __launch_bounds__(NTH, 1) k_s_solve_coop(SplitBuf sb, int gen, f
     float r = 0.f;
     for (int j = 0; j < max_sweeps; ++j) {
         // the accumulators change inside this launch: read them through L2 (ld.global.cg)
-        const float4* Acur = sb.acc[it % 3];
-        float4* Anxt = sb.acc[(it + 1) % 3];
-        float4* Aclr = sb.acc[(it + 2) % 3];
+        const float4* Acur = sb.acc[it % SPLIT_NACC];
+        float4* Anxt = sb.acc[(it + 1) % SPLIT_NACC];
+        float4* Aclr = sb.acc[(it + 3) % SPLIT_NACC];
         float maxd2 = 0.f, maxl = 0.f;
         for (int base = 0; base < ncb; base += NTH * UNROLL) {
             float4 q0[UNROLL], q1[UNROLL], l[UNROLL];
@@ -927,16 +943,17 @@ __global__ void __launch_bounds__(NTH, 1) k_s_solve_coop(SplitBuf sb, int gen, f
                 pj_push<AGG>(Anxt, ok[u], a, b, o);
             }
         }
+        // the stop rule runs every check_every sweeps (counted across launches) and at the cap; the
+        // other sweeps only synchronise
+        const bool check = (it + 1) % check_every == 0 || it + 1 >= max_iter;
+        if (check) block_max2(maxd2, maxl);
+        grid_arrive(&ss->bar, sb.recs, ++epoch, check, maxd2, maxl);
         for (int i = tid; i < nbb; i += NTH) {
             const float4 v0 = vf_smem ? s_vf[2 * i] : ldg4(&sb.vel4[2 * (bb + i)]);
             const float4 w0 = vf_smem ? s_vf[2 * i + 1] : ldg4(&sb.vel4[2 * (bb + i) + 1]);
             stcg_body(&Aclr[2 * (bb + i)], v0, w0);
         }
-        // the stop rule runs every check_every sweeps (counted across launches) and at the cap; the
-        // other sweeps only synchronise
-        const bool check = (it + 1) % check_every == 0 || it + 1 >= max_iter;
-        if (check) block_max2(maxd2, maxl);
-        if (!grid_sync_max(&ss->bar, sb.recs, ++epoch, &ss->err, check, maxd2, maxl)) return;
+        if (!grid_wait_max(&ss->bar, sb.recs, epoch, &ss->err, check, maxd2, maxl)) return;
         ++it;
         if (check) {
             r = sweep_residual(maxd2, maxl);
@@ -1204,7 +1221,7 @@ __global__ void k_s_final_body(Scene sc, SplitBuf sb) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= sc.N) return;
     const int N = sc.N;
-    const int fa = sb.ss->final_acc >= 0 ? sb.ss->final_acc : sb.ss->iters % 3;
+    const int fa = sb.ss->final_acc >= 0 ? sb.ss->final_acc : sb.ss->iters % SPLIT_NACC;
     const float4* A = sb.acc[fa];
     const float4 a0 = A[2 * i], a1 = A[2 * i + 1];
     const float4 f0 = sb.vel4[2 * i], f1 = sb.vel4[2 * i + 1];

@@ -62,12 +62,15 @@ struct SplitParams {
 //   lam  (lambda_n, lambda_t1, lambda_t2) per generation (warm start)
 // R = alpha / diag(W M^-1 W^T) is recomputed in the sweep from the inverse masses that come with
 // the velocity gathers: R_n = alpha / (1/mA + 1/mB), R_t = alpha / (1/mA + 1/mB + rhoA^2/IA + rhoB^2/IB).
+constexpr int SPLIT_NACC = 4;  // rotating velocity accumulators of the sweeps
 struct SplitBuf {
     int N = 0;
     int64_t cap = 0;
     float4* pos4 = nullptr;   // N: position relative to the scene origin, radius
     float4* vel4 = nullptr;   // 2N: free velocities (v_free, 1/m), (omega_free world, 1/I)
-    float4* acc[3] = {nullptr, nullptr, nullptr};  // 2N each: M^-1 W^T lambda of a sweep (rotating)
+    // 2N each, rotating by sweep k: gather A[k % 4], add into A[(k + 1) % 4], reset A[(k + 3) % 4]
+    // (read in sweep k - 1, next added into in sweep k + 2) to the free velocities
+    float4* acc[SPLIT_NACC] = {nullptr, nullptr, nullptr, nullptr};
     float4* vn4 = nullptr;    // 2N: pre-solve velocities (v, omega_world)
     double* vfree = nullptr;  // 6N FP64 free velocities (world frame)
     double* acc64 = nullptr;  // 6N FP64 W^T lambda, then final velocities
