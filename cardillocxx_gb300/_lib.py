@@ -66,6 +66,10 @@ class CdxConfig(C.Structure):
         ("pj_anderson", C.c_int32),
         ("pj_anderson_m", C.c_int32),
         ("pj_rdiag_true_delassus", C.c_int32),
+        ("output_interval_steps", C.c_int32),
+        ("output_write_contact_manifolds", C.c_int32),
+        ("output_folder", C.c_char * 256),
+        ("output_filename_prefix", C.c_char * 128),
     ]
 
 
@@ -145,6 +149,8 @@ SIGNATURES = [
     ("cdx_set_state", C.c_int, [C.c_void_p, _P, _P, _P, _P]),
     ("cdx_get_stats", C.c_int, [C.c_void_p, C.POINTER(CdxStats)]),
     ("cdx_get_contacts", C.c_int, [C.c_void_p, _PI, _PI, _P, _P, _P, _PI]),
+    ("cdx_track", C.c_int, [C.c_void_p, C.c_int32, C.c_char_p]),
+    ("cdx_output_flush", C.c_int, [C.c_void_p]),
     ("cdx_set_trace", C.c_int, [C.c_void_p, C.c_int32]),
     ("cdx_get_trace", C.c_int, [C.c_void_p, _P, C.c_int64, C.POINTER(C.c_int64)]),
     ("cdx_set_timing", C.c_int, [C.c_void_p, C.c_int32]),

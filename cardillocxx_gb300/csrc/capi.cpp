@@ -71,6 +71,20 @@ int cdx_get_contacts(cdx_ctx* ctx, int32_t* id_a, int32_t* id_b, double* point, 
     return ctx->eng.get_contacts(id_a, id_b, point, lambda, normal, count);
 }
 
+int cdx_track(cdx_ctx* ctx, int32_t body, const char* name) {
+    if (!ctx) return CDX_ERR_ARG;
+    try {
+        return ctx->eng.track(body, name);
+    } catch (const std::exception& e) {
+        return ctx->eng.fail(CDX_ERR_ARG, e.what());
+    }
+}
+
+int cdx_output_flush(cdx_ctx* ctx) {
+    if (!ctx) return CDX_ERR_ARG;
+    return ctx->eng.output_flush();
+}
+
 int cdx_set_trace(cdx_ctx* ctx, int32_t on) {
     if (!ctx) return CDX_ERR_ARG;
     ctx->eng.trace_next = on != 0;

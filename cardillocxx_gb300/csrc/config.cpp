@@ -5,6 +5,7 @@
 // booleans are 1/true/yes/on (case-insensitive), a missing file yields the defaults.
 #include <algorithm>
 #include <cctype>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
@@ -100,6 +101,11 @@ int cdx_config_default(cdx_config* c) {
     c->pj_anderson = 0;
     c->pj_anderson_m = 2;
     c->pj_rdiag_true_delassus = 0;
+    // frames are off unless asked for (the reference writes every 50 steps by default)
+    c->output_interval_steps = 0;
+    c->output_write_contact_manifolds = 1;
+    std::snprintf(c->output_folder, sizeof(c->output_folder), "%s", "./vtk_out");
+    std::snprintf(c->output_filename_prefix, sizeof(c->output_filename_prefix), "%s", "scene");
     return CDX_OK;
 }
 
@@ -195,6 +201,16 @@ int cdx_config_set(cdx_config* c, const char* key_c, const char* val_c) {
         if (as_int(val, &i)) c->pj_anderson_m = std::max(1, i);
     } else if (key_is(key, "pj.rdiag_true_delassus")) {
         c->pj_rdiag_true_delassus = as_bool(val);
+    } else if (key == "output.interval_steps") {
+        if (as_int(val, &i)) c->output_interval_steps = std::max(0, i);
+    } else if (key == "output.write_contact_manifolds") {
+        c->output_write_contact_manifolds = as_bool(val);
+    } else if (key == "output.folder") {
+        if (val.size() >= sizeof(c->output_folder)) return CDX_ERR_ARG;
+        std::snprintf(c->output_folder, sizeof(c->output_folder), "%s", val.c_str());
+    } else if (key == "output.filename_prefix") {
+        if (val.size() >= sizeof(c->output_filename_prefix)) return CDX_ERR_ARG;
+        std::snprintf(c->output_filename_prefix, sizeof(c->output_filename_prefix), "%s", val.c_str());
     }
     return CDX_OK;  // unknown keys are ignored, as in the reference
 }

@@ -63,6 +63,8 @@ void Engine::dfree(void* p) {
 }
 
 Engine::~Engine() {
+    delete out;  // drains the writer queue
+    out = nullptr;
     if (stream) cudaStreamSynchronize(stream);
     destroy_split();
     delete csr;
@@ -76,6 +78,7 @@ Engine::~Engine() {
 
 int Engine::init(const cdx_config& c) {
     cfg = c;
+    if (cfg.output_interval_steps > 0) out = new cdx::Output(cfg);
     if (cfg.moreau_implicit_gyroscopy) return fail(CDX_ERR_UNSUPPORTED, "moreau.implicit_gyroscopy=on is not supported");
     if (cfg.solver_type != 0) return fail(CDX_ERR_UNSUPPORTED, "only solver.type=projected_jacobi is on this path");
     int st = cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
@@ -283,6 +286,30 @@ int Engine::load_scene(const cdx_scene& s) {
     const int64_t cap0 = std::max<int64_t>(1024, (int64_t)(cfg.gpu_contact_capacity_factor * std::max(1, N)));
     if ((st = ensure_contacts(cap0))) return st;
     if ((st = ensure_tmp(std::max<int64_t>(nflag, N + 1)))) return st;
+    // host copies for the frame output
+    oscene = cdx::OutputScene{};
+    oscene.N = N;
+    oscene.S = S;
+    oscene.radius.assign(s.radius, s.radius + N);
+    oscene.mu.assign(s.mu, s.mu + N);
+    oscene.pos0.assign(s.pos, s.pos + 3 * (size_t)N);
+    if (S > 0) {
+        oscene.skind.assign(s.static_kind, s.static_kind + S);
+        oscene.spos.assign(s.static_pos, s.static_pos + 3 * (size_t)S);
+        oscene.sdir.assign(s.static_dir, s.static_dir + 3 * (size_t)S);
+        oscene.smu.assign(s.static_mu, s.static_mu + S);
+        oscene.srad.assign(S, 0.0);
+        if (s.static_radius) oscene.srad.assign(s.static_radius, s.static_radius + S);
+    }
+    if (out) {
+        out->flush();
+        delete out;  // a new scene starts new collections and rewrites the static geometry
+        out = new cdx::Output(cfg);
+        out->set_scene(oscene);
+    }
+    tracked.clear();
+    out_time = 0.0;
+    out_started = false;
     loaded = true;
     steps = 0;
     return CDX_OK;
@@ -713,11 +740,93 @@ int Engine::step64() {
 
 int Engine::step(int nsteps) {
     if (!loaded) return fail(CDX_ERR_STATE, "no scene loaded");
+    int st;
+    // PhysicsPipeline::step (physics_pipeline.cpp:91-113): the first frame before the first
+    // step, then a frame every output.interval_steps and the tracked rows every step
+    if (out && out->vtk_on() && !out_started && nsteps > 0) {
+        out_started = true;
+        if ((st = output_frame())) return st;
+    }
     for (int k = 0; k < nsteps; ++k) {
-        int st = (cfg.gpu_precision == CDX_PRECISION_SPLIT) ? step_split() : step64();
+        st = (cfg.gpu_precision == CDX_PRECISION_SPLIT) ? step_split() : step64();
         if (st) return st;
+        if (out) {
+            out_time += cfg.sim_dt;
+            if (out->due(steps) && (st = output_frame())) return st;
+            if (!tracked.empty() && (st = output_tracked())) return st;
+        }
     }
     return CDX_OK;
+}
+
+int Engine::output_frame() {
+    cdx::OutputFrame f;
+    const size_t N = (size_t)sc.N;
+    f.step = steps;
+    f.time = out_time;
+    f.pos.resize(3 * N);
+    f.quat.resize(4 * N);
+    f.vel.resize(3 * N);
+    f.omega.resize(3 * N);
+    int st;
+    if ((st = get_state(f.pos.data(), f.quat.data(), f.vel.data(), f.omega.data()))) return st;
+    int32_t nc = 0;
+    if ((st = get_contacts(nullptr, nullptr, nullptr, nullptr, nullptr, &nc))) return st;
+    f.nc = nc;
+    f.ia.resize(nc);
+    f.ib.resize(nc);
+    f.point.resize(3 * (size_t)nc);
+    f.lambda.resize(3 * (size_t)nc);
+    f.normal.resize(3 * (size_t)nc);
+    if (nc > 0 && (st = get_contacts(f.ia.data(), f.ib.data(), f.point.data(), f.lambda.data(), f.normal.data(), &nc)))
+        return st;
+    out->frame(std::move(f));
+    return CDX_OK;
+}
+
+int Engine::output_tracked() {
+    const size_t N = (size_t)sc.N;
+    launch_pack_state(sc, stage, stream);
+    ++launches;
+    std::vector<cdx::TrackedRow> rows(tracked.size());
+    int st;
+    for (size_t k = 0; k < tracked.size(); ++k) {
+        const size_t i = (size_t)tracked[k].first;
+        cdx::TrackedRow& r = rows[k];
+        r.name = tracked[k].second;
+        if ((st = cuda_check(cudaMemcpyAsync(r.p, stage + 3 * i, 24, cudaMemcpyDeviceToHost, stream), "tracked")) ||
+            (st = cuda_check(cudaMemcpyAsync(r.q, stage + 3 * N + 4 * i, 32, cudaMemcpyDeviceToHost, stream), "tracked")) ||
+            (st = cuda_check(cudaMemcpyAsync(r.v, stage + 7 * N + 3 * i, 24, cudaMemcpyDeviceToHost, stream), "tracked")) ||
+            (st = cuda_check(cudaMemcpyAsync(r.w, stage + 10 * N + 3 * i, 24, cudaMemcpyDeviceToHost, stream), "tracked")))
+            return st;
+    }
+    if ((st = cuda_check(cudaStreamSynchronize(stream), "tracked"))) return st;
+    out->tracked(out_time, std::move(rows));
+    return CDX_OK;
+}
+
+int Engine::track(int32_t body, const char* name) {
+    if (!loaded) return fail(CDX_ERR_STATE, "no scene loaded");
+    if (body < 0 || body >= sc.N || !name) return fail(CDX_ERR_ARG, "track: body index out of range");
+    if (!out) {
+        out = new cdx::Output(cfg);
+        out->set_scene(oscene);
+        out_started = steps > 0;  // frames (when on) start at the next due step
+    }
+    for (auto& t : tracked)
+        if (t.first == body) {
+            t.second = name;
+            return CDX_OK;
+        }
+    tracked.emplace_back(body, name);
+    return CDX_OK;
+}
+
+int Engine::output_flush() {
+    if (!out) return CDX_OK;
+    out->flush();
+    const std::string e = out->last_error();
+    return e.empty() ? CDX_OK : fail(CDX_ERR_STATE, e);
 }
 
 int Engine::get_state(double* pos, double* quat, double* vel, double* omega) {

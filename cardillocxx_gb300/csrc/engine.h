@@ -7,6 +7,7 @@
 
 #include "../../include/cdx.h"
 #include "cdx_internal.h"
+#include "output.h"
 
 namespace cdx {
 const char* status_name(int st);
@@ -73,6 +74,17 @@ struct Engine {
     int trace_rows = 0;
     double* trace_dev = nullptr;
     std::vector<double> trace_buf;
+
+    // frame output (output.cpp): writer, scene copies, tracked spheres, simulated time
+    cdx::Output* out = nullptr;
+    cdx::OutputScene oscene;
+    std::vector<std::pair<int32_t, std::string>> tracked;
+    double out_time = 0.0;
+    bool out_started = false;
+    int output_frame();
+    int output_tracked();
+    int track(int32_t body, const char* name);
+    int output_flush();
 
     cdx::SplitState* split = nullptr;
     cdx::CsrBuffers* csr = nullptr;

@@ -163,6 +163,14 @@ class PhysicsEngine:
         self._check(self.L.cdx_get_contacts(self.h, ip(ia), ip(ib), dp(pt), dp(lam), dp(nrm), C.byref(n)))
         return {"id_a": ia, "id_b": ib, "point": pt, "lambda": lam, "normal": nrm}
 
+    def track(self, body: int, name: str):
+        """Write sphere `body` to <output.folder>/<output.filename_prefix>_tracked.csv every step."""
+        self._check(self.L.cdx_track(self.h, int(body), str(name).encode()))
+
+    def flush_output(self):
+        """Wait until the background writer has written every queued frame."""
+        self._check(self.L.cdx_output_flush(self.h))
+
     def set_trace(self, on: bool = True):
         self._check(self.L.cdx_set_trace(self.h, int(on)))
 

@@ -81,6 +81,11 @@ typedef struct cdx_config {
     int32_t pj_anderson;              /* pj.anderson */
     int32_t pj_anderson_m;            /* pj.anderson_m: history window (>= 1) */
     int32_t pj_rdiag_true_delassus;   /* pj.rdiag_true_delassus: per-contact Delassus block preconditioner (plain FP64) */
+    /* frame output (PhysicsPipeline, physics_pipeline.cpp:62-113; config.hpp:20-23) */
+    int32_t output_interval_steps;          /* output.interval_steps: VTK frames every k steps (0 = off) */
+    int32_t output_write_contact_manifolds; /* output.write_contact_manifolds */
+    char output_folder[256];                /* output.folder */
+    char output_filename_prefix[128];       /* output.filename_prefix */
 } cdx_config;
 
 /* Scene: dynamic spheres plus static shapes (halfspaces, drums). Bodies of one scene are
@@ -156,6 +161,12 @@ int cdx_get_stats(cdx_ctx* ctx, cdx_stats* out);
  * pass NULL arrays to query the count */
 int cdx_get_contacts(cdx_ctx* ctx, int32_t* id_a, int32_t* id_b, double* point, double* lambda, double* normal,
                      int32_t* count);
+/* track a sphere in <output.folder>/<output.filename_prefix>_tracked.csv, one row every step
+ * (World::track, world.cpp:38-45; CsvWriter::writeTrackedState, csv_writer.hpp:43-52) */
+int cdx_track(cdx_ctx* ctx, int32_t body, const char* name);
+/* wait until the background writer has written every queued frame; CDX_ERR_STATE (with
+ * cdx_last_error) when a file could not be written */
+int cdx_output_flush(cdx_ctx* ctx);
 /* per-sweep impulse trace of the next step (rows in solver order), for parity checks */
 int cdx_set_trace(cdx_ctx* ctx, int32_t on);
 int cdx_get_trace(cdx_ctx* ctx, double* out, int64_t max_values, int64_t* num_values);

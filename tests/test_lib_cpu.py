@@ -147,3 +147,18 @@ def test_acceleration_keys(cdxlib):
     assert c.get("pj_anderson_m") == 5
     assert c.get("pj_rdiag_true_delassus") == 0
     assert c.set("solver.rdiag_true_delassus", "on").get("pj_rdiag_true_delassus") == 1
+
+
+def test_output_keys(cdxlib):
+    # output.* keys of the reference (config.hpp:20-23); frames are off unless interval_steps is set
+    from cardillocxx_gb300 import CdxError
+    from cardillocxx_gb300.engine import Config
+    c = Config()
+    assert c.get("output_interval_steps") == 0 and c.get("output_write_contact_manifolds") == 1
+    assert c.get("output_folder") == b"./vtk_out" and c.get("output_filename_prefix") == b"scene"
+    c.set("output.interval_steps", 25).set("output.folder", "/tmp/frames").set("output.filename_prefix", "drum")
+    c.set("output.write_contact_manifolds", "off")
+    assert c.get("output_interval_steps") == 25 and c.get("output_write_contact_manifolds") == 0
+    assert c.get("output_folder") == b"/tmp/frames" and c.get("output_filename_prefix") == b"drum"
+    with pytest.raises(CdxError):
+        c.set("output.folder", "x" * 300)
