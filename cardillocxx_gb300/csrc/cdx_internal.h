@@ -170,6 +170,9 @@ void launch_cell_keys(const Scene& sc, const Grid& g, uint32_t* keys, uint32_t* 
 void launch_ranges(const uint32_t* sorted_keys, int64_t n, int32_t* start, int32_t* end, cudaStream_t s);
 // state staging: 13 doubles per body, interleaved as the C ABI's host arrays
 void launch_pack_state(const Scene& sc, double* out, cudaStream_t s);
+void launch_pack_state4(const Scene& sc, double* pos, double* quat, double* vel, double* omega, cudaStream_t s);
+void launch_unpack_state4(const Scene& sc, const double* pos, const double* quat, const double* vel,
+                          const double* omega, cudaStream_t s);
 void launch_unpack_state(const Scene& sc, const double* in, int mask, cudaStream_t s);
 
 // ---- FP64 plain method (k_fp64.cu) ----

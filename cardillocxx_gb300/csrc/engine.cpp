@@ -829,11 +829,35 @@ int Engine::output_flush() {
     return e.empty() ? CDX_OK : fail(CDX_ERR_STATE, e);
 }
 
+// The device address of a host array the GPU can read and write directly (pinned or registered
+// memory), else nullptr (pageable memory goes through the staging buffer and the copy engines).
+static void* device_view(const void* p) {
+    if (!p) return nullptr;
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return (at.type == cudaMemoryTypeHost && at.devicePointer) ? at.devicePointer : nullptr;
+}
+
 int Engine::get_state(double* pos, double* quat, double* vel, double* omega) {
     if (!loaded) return fail(CDX_ERR_STATE, "no scene loaded");
     const size_t N = (size_t)sc.N;
     if (N == 0) return CDX_OK;
     int st;
+    {
+        // pinned caller arrays: one kernel writes them directly (coalesced, over the host link)
+        double* dv[4] = {pos, quat, vel, omega};
+        bool direct = true;
+        for (auto& p : dv)
+            if (p && !(p = (double*)device_view(p))) direct = false;
+        if (direct) {
+            launch_pack_state4(sc, dv[0], dv[1], dv[2], dv[3], stream);
+            ++launches;
+            return cuda_check(cudaStreamSynchronize(stream), "download");
+        }
+    }
     launch_pack_state(sc, stage, stream);
     ++launches;
     // one copy per requested array straight into the caller's buffers
@@ -849,6 +873,19 @@ int Engine::set_state(const double* pos, const double* quat, const double* vel, 
     const size_t N = (size_t)sc.N;
     if (N == 0) return CDX_OK;
     int st;
+    {
+        // pinned caller arrays: one kernel reads them directly; like a copy from pinned memory this
+        // runs asynchronously on the engine's stream
+        const double* dv[4] = {pos, quat, vel, omega};
+        bool direct = true;
+        for (auto& p : dv)
+            if (p && !(p = (const double*)device_view(p))) direct = false;
+        if (direct) {
+            launch_unpack_state4(sc, dv[0], dv[1], dv[2], dv[3], stream);
+            ++launches;
+            return CDX_OK;
+        }
+    }
     int mask = 0;
     if (pos && (st = cuda_check(cudaMemcpyAsync(stage, pos, 8 * 3 * N, cudaMemcpyHostToDevice, stream), "upload"))) return st;
     if (quat && (st = cuda_check(cudaMemcpyAsync(stage + 3 * N, quat, 8 * 4 * N, cudaMemcpyHostToDevice, stream), "upload"))) return st;

@@ -100,7 +100,53 @@ __global__ void k_unpack_state(Scene sc, const double* in, int mask) {
     if (mask & 2)
         for (int k = 0; k < 4; ++k) sc.bf(BF_QX + k)[i] = in[3 * N + 4 * (size_t)i + k];
 }
+// The state as the caller's four arrays (pos 3N, quat 4N, vel 3N, omega 3N; a NULL array is
+// skipped), element by element so that consecutive threads touch consecutive doubles of the
+// caller's arrays: coalesced when those live in host memory that the GPU reads or writes directly.
+__global__ void k_pack_state4(Scene sc, double* pos, double* quat, double* vel, double* omega) {
+    const int64_t N = sc.N, total = 13 * N;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        if (e < 3 * N) {
+            if (pos) pos[e] = sc.bf(BF_PX + (int)(e % 3))[e / 3];
+        } else if (e < 7 * N) {
+            const int64_t j = e - 3 * N;
+            if (quat) quat[j] = sc.bf(BF_QX + (int)(j % 4))[j / 4];
+        } else if (e < 10 * N) {
+            const int64_t j = e - 7 * N;
+            if (vel) vel[j] = sc.bf(BF_VX + (int)(j % 3))[j / 3];
+        } else {
+            const int64_t j = e - 10 * N;
+            if (omega) omega[j] = sc.bf(BF_WX + (int)(j % 3))[j / 3];
+        }
+    }
+}
+__global__ void k_unpack_state4(Scene sc, const double* pos, const double* quat, const double* vel,
+                                const double* omega) {
+    const int64_t N = sc.N, total = 13 * N;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        if (e < 3 * N) {
+            if (pos) sc.bf(BF_PX + (int)(e % 3))[e / 3] = pos[e];
+        } else if (e < 7 * N) {
+            const int64_t j = e - 3 * N;
+            if (quat) sc.bf(BF_QX + (int)(j % 4))[j / 4] = quat[j];
+        } else if (e < 10 * N) {
+            const int64_t j = e - 7 * N;
+            if (vel) sc.bf(BF_VX + (int)(j % 3))[j / 3] = vel[j];
+        } else {
+            const int64_t j = e - 10 * N;
+            if (omega) sc.bf(BF_WX + (int)(j % 3))[j / 3] = omega[j];
+        }
+    }
+}
 }  // namespace
+void launch_pack_state4(const Scene& sc, double* pos, double* quat, double* vel, double* omega, cudaStream_t s) {
+    if (sc.N) k_pack_state4<<<(int)std::min<int64_t>(nblk(13 * (int64_t)sc.N), 8192), NT, 0, s>>>(sc, pos, quat, vel, omega);
+}
+void launch_unpack_state4(const Scene& sc, const double* pos, const double* quat, const double* vel,
+                          const double* omega, cudaStream_t s) {
+    if (sc.N)
+        k_unpack_state4<<<(int)std::min<int64_t>(nblk(13 * (int64_t)sc.N), 8192), NT, 0, s>>>(sc, pos, quat, vel, omega);
+}
 void launch_pack_state(const Scene& sc, double* out, cudaStream_t s) {
     if (sc.N) k_pack_state<<<nblk(sc.N), NT, 0, s>>>(sc, out);
 }
