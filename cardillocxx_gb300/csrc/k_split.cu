@@ -45,7 +45,7 @@ __device__ __forceinline__ void frame32(float3 n, float3& t1, float3& t2) {
         const float d = dot(n, t1);
         t1 = t1 - d * n;
     } else {
-        const float a = __frcp_rn(1.f + n.z);  // = 1 / (1 + n.z), correctly rounded either way
+        const float a = __fdividef(1.f, 1.f + n.z);  // 1 + n.z >= 1e-7 on this branch
         const float b = (-n.x * n.y) * a;
         t1 = make_float3(1.f - (n.x * n.x) * a, b, -n.x);
     }
@@ -542,8 +542,8 @@ __device__ __forceinline__ void pj_rdiag(float rA, float rB, float ima, float ii
                                          float& Rn, float& Rt) {
     const float Dn = ima + imb;
     const float Dt = Dn + rA * rA * iia + rB * rB * iib;
-    Rn = alpha * __frcp_rn(Dn);
-    Rt = alpha * __frcp_rn(Dt);
+    Rn = __fdividef(alpha, Dn);  // the inverse masses keep Dn, Dt far inside __fdividef's range
+    Rt = __fdividef(alpha, Dt);
 }
 
 // One contact of a sweep (projected_jacobi.cpp:121-138 with project :100-119): gamma = W x + b from
@@ -780,18 +780,18 @@ __device__ __forceinline__ unsigned long long global_ns() {
 constexpr unsigned long long COOP_WAIT_NS = 200000000ull;  // 0.2 s
 constexpr int COOP_MAX_GRID = 256;                         // records a lane reads: COOP_MAX_GRID / 32
 // Arrival half: publish the block's maxima and add one to the counter (after every thread's
-// writes of the sweep, through __syncthreads and a fence).
+// writes of the sweep, through __syncthreads and a release reduction).
 __device__ __forceinline__ void grid_arrive(unsigned* ctr, float2* recs, unsigned epoch, bool reduce, float maxd,
                                             float maxl) {
     float2* bank = recs + (size_t)(epoch & 1u) * SPLIT_MAX_PARTS;
     if (reduce && threadIdx.x == 0) bank[blockIdx.x] = make_float2(maxd, maxl);
     __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        atomicAdd(ctr, 1u);
-    }
+    // a release reduction: the block's writes (ordered before it by __syncthreads) become
+    // visible to any block whose acquire load sees the new count
+    if (threadIdx.x == 0) asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(ctr) : "memory");
 }
-// Waiting half: thread 0 waits (bounded) for every block's arrival, then warp 0 reduces the records.
+// Waiting half: thread 0 waits (bounded, acquire loads) for every block's arrival, then warp 0
+// reduces the records.
 __device__ __forceinline__ bool grid_wait_max(unsigned* ctr, float2* recs, unsigned epoch, int32_t* err, bool reduce,
                                               float& maxd, float& maxl) {
     __shared__ float s_md, s_ml;
@@ -811,7 +811,6 @@ __device__ __forceinline__ bool grid_wait_max(unsigned* ctr, float2* recs, unsig
                 }
                 __nanosleep(20);
             }
-            __threadfence();
         }
         ok = __shfl_sync(FULL, ok, 0);
         float md = 0.f, ml = 0.f;
