@@ -339,8 +339,11 @@ template <bool WRITE>
 __global__ void k_s_pairs(Scene sc, Grid gr, SplitBuf sb, const uint32_t* cell_body, const int32_t* cell_start,
                           const int32_t* cell_end, int32_t* counts, const int32_t* offsets, int32_t base, int gen,
                           SplitParams P, DevScalars* ds) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= sc.N) return;
+    // threads take the bodies in cell order, so a warp walks neighbouring cells (shared cache
+    // lines); every body's contacts still go to its own slots (counts[i], offsets[i])
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= sc.N) return;
+    const int i = (int)cell_body[t];
     const float4 pi = sb.pos4[i];
     const int si = sc.body_scene[i];
     // cell of body i from its FP64 position (identical to the key kernel)
