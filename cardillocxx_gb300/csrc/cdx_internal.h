@@ -166,7 +166,8 @@ size_t sort_temp_bytes(int64_t n);
 cudaError_t exclusive_scan(void* tmp, size_t tmp_bytes, const int32_t* in, int32_t* out, int64_t n, cudaStream_t s);
 cudaError_t sort_pairs(void* tmp, size_t tmp_bytes, const uint32_t* kin, uint32_t* kout, const uint32_t* vin,
                        uint32_t* vout, int64_t n, int end_bit, cudaStream_t s);
-void launch_cell_keys(const Scene& sc, const Grid& g, uint32_t* keys, uint32_t* vals, cudaStream_t s);
+void launch_cell_keys(const Scene& sc, const Grid& g, uint32_t* keys, uint32_t* vals, cudaStream_t s,
+                      int by_inverse = 0);
 void launch_ranges(const uint32_t* sorted_keys, int64_t n, int32_t* start, int32_t* end, cudaStream_t s);
 // state staging: 13 doubles per body, interleaved as the C ABI's host arrays
 void launch_pack_state(const Scene& sc, double* out, cudaStream_t s);

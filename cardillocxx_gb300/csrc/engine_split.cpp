@@ -353,7 +353,7 @@ int Engine::step_split() {
 
     if (timing) cudaEventRecord(ev[0], stream);
     launch_s_prep(sc, sb, dt, cfg.sim_gravity, (1.0 - th) * dt, stream);
-    launch_cell_keys(sc, grid, cell_key_in, cell_val_in, stream);
+    launch_cell_keys(sc, grid, cell_key_in, cell_val_in, stream, 1);
     if ((st = cuda_check(sort_pairs(tmp, tmp_bytes, cell_key_in, cell_key_out, cell_val_in, cell_val_out, N,
                                     grid.key_bits, stream), "sort cells"))) return st;
     cudaMemsetAsync(cell_start, 0, sizeof(int32_t) * grid.ncells, stream);
@@ -366,7 +366,7 @@ int Engine::step_split() {
         if ((st = cuda_check(exclusive_scan(tmp, tmp_bytes, sflags, spos, nflag, stream), "scan"))) return st;
         launches += 3;
     }
-    launch_s_pair_count(sc, grid, sb, cell_val_out, cell_start, cell_end, pcount, P, ds, stream);
+    launch_s_pair_count(sc, grid, sb, cell_val_out, cell_key_out, cell_start, cell_end, pcount, P, ds, stream);
     if ((st = cuda_check(exclusive_scan(tmp, tmp_bytes, pcount, poff, N + 1, stream), "scan"))) return st;
     launches += 3;
     int64_t n_pair = 0;
@@ -374,7 +374,7 @@ int Engine::step_split() {
         launch_s_totals(sb, spos, sflags, nflag, poff, N, stream);
         S->nc = S->prev_count;  // an estimate for the launch shapes; the device holds the count
         if (nflag > 0) launch_s_static_write(sc, sb, sflags, spos, gen, P, stream);
-        launch_s_pair_write(sc, grid, sb, cell_val_out, cell_start, cell_end, poff, -1, gen, P, ds, stream);
+        launch_s_pair_write(sc, grid, sb, cell_val_out, cell_key_out, cell_start, cell_end, poff, -1, gen, P, ds, stream);
         launches += 3;
     } else {
         int32_t tot[4] = {0, 0, 0, 0};
@@ -397,7 +397,7 @@ int Engine::step_split() {
             ++launches;
         }
         if (n_pair > 0) {
-            launch_s_pair_write(sc, grid, sb, cell_val_out, cell_start, cell_end, poff, (int32_t)n_static, gen, P, ds,
+            launch_s_pair_write(sc, grid, sb, cell_val_out, cell_key_out, cell_start, cell_end, poff, (int32_t)n_static, gen, P, ds,
                                 stream);
             ++launches;
         }

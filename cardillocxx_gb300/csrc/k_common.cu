@@ -12,14 +12,16 @@ namespace {
 constexpr int NT = 256;
 inline int nblk(int64_t n, int nt = NT) { return (int)((n + nt - 1) / nt); }
 
-__global__ void k_cell_keys(Scene sc, Grid g, uint32_t* keys, uint32_t* vals) {
+// by_inverse: multiply by 1 / cell instead of dividing (the split form, whose pair kernels read
+// the keys back instead of recomputing cells); the plain FP64 method divides, as its pair kernels do
+__global__ void k_cell_keys(Scene sc, Grid g, uint32_t* keys, uint32_t* vals, int by_inverse, double inv_cell) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= sc.N) return;
     const double p[3] = {sc.bf(BF_PX)[i], sc.bf(BF_PY)[i], sc.bf(BF_PZ)[i]};
     int ci[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        double f = floor((p[k] - g.lo[k]) / g.cell);
+        double f = by_inverse ? floor((p[k] - g.lo[k]) * inv_cell) : floor((p[k] - g.lo[k]) / g.cell);
         if (!(f >= 0.0)) f = 0.0;
         if (f > (double)(g.dim[k] - 1)) f = (double)(g.dim[k] - 1);
         ci[k] = (int)f;
@@ -62,9 +64,10 @@ cudaError_t sort_pairs(void* tmp, size_t tmp_bytes, const uint32_t* kin, uint32_
     return cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, kin, kout, vin, vout, (int)n, 0, end_bit, s);
 }
 
-void launch_cell_keys(const Scene& sc, const Grid& g, uint32_t* keys, uint32_t* vals, cudaStream_t s) {
+void launch_cell_keys(const Scene& sc, const Grid& g, uint32_t* keys, uint32_t* vals, cudaStream_t s,
+                      int by_inverse) {
     if (sc.N == 0) return;
-    k_cell_keys<<<nblk(sc.N), NT, 0, s>>>(sc, g, keys, vals);
+    k_cell_keys<<<nblk(sc.N), NT, 0, s>>>(sc, g, keys, vals, by_inverse, 1.0 / g.cell);
 }
 
 void launch_ranges(const uint32_t* sorted_keys, int64_t n, int32_t* start, int32_t* end, cudaStream_t s) {

@@ -336,9 +336,9 @@ __global__ void k_s_static_write(Scene sc, SplitBuf sb, const int32_t* flags, co
 }
 
 template <bool WRITE>
-__global__ void k_s_pairs(Scene sc, Grid gr, SplitBuf sb, const uint32_t* cell_body, const int32_t* cell_start,
-                          const int32_t* cell_end, int32_t* counts, const int32_t* offsets, int32_t base, int gen,
-                          SplitParams P, DevScalars* ds) {
+__global__ void k_s_pairs(Scene sc, Grid gr, SplitBuf sb, const uint32_t* cell_body, const uint32_t* cell_key,
+                          const int32_t* cell_start, const int32_t* cell_end, int32_t* counts, const int32_t* offsets,
+                          int32_t base, int gen, SplitParams P, DevScalars* ds) {
     // threads take the bodies in cell order, so a warp walks neighbouring cells (shared cache
     // lines); every body's contacts still go to its own slots (counts[i], offsets[i])
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -346,16 +346,14 @@ __global__ void k_s_pairs(Scene sc, Grid gr, SplitBuf sb, const uint32_t* cell_b
     const int i = (int)cell_body[t];
     const float4 pi = sb.pos4[i];
     const int si = sc.body_scene[i];
-    // cell of body i from its FP64 position (identical to the key kernel)
+    // cell of body i: its key in the sorted key array, ((z dim_y) + y) dim_x + x
     int ci[3];
     {
-        const double p[3] = {sc.bf(BF_PX)[i], sc.bf(BF_PY)[i], sc.bf(BF_PZ)[i]};
-        for (int k = 0; k < 3; ++k) {
-            double f = floor((p[k] - gr.lo[k]) / gr.cell);
-            if (!(f >= 0.0)) f = 0.0;
-            if (f > (double)(gr.dim[k] - 1)) f = (double)(gr.dim[k] - 1);
-            ci[k] = (int)f;
-        }
+        const uint32_t key = cell_key[t];
+        const uint32_t dx = (uint32_t)gr.dim[0], dy = (uint32_t)gr.dim[1];
+        ci[0] = (int)(key % dx);
+        ci[1] = (int)((key / dx) % dy);
+        ci[2] = (int)(key / (dx * dy));
     }
     int list[MAX_PAIR];
     int cnt = 0;
@@ -1580,10 +1578,11 @@ void launch_s_static_flags(const Scene& sc, const SplitBuf& sb, float margin, in
     k_s_static_flags<<<nblk(sc.N), NT, 0, s>>>(sc, sb, margin, flags);
 }
 void launch_s_pair_count(const Scene& sc, const Grid& g, const SplitBuf& sb, const uint32_t* cell_body,
-                         const int32_t* cell_start, const int32_t* cell_end, int32_t* counts, const SplitParams& P,
-                         DevScalars* ds, cudaStream_t s) {
+                         const uint32_t* cell_key, const int32_t* cell_start, const int32_t* cell_end, int32_t* counts,
+                         const SplitParams& P, DevScalars* ds, cudaStream_t s) {
     if (sc.N == 0) return;
-    k_s_pairs<false><<<nblk(sc.N), NT, 0, s>>>(sc, g, sb, cell_body, cell_start, cell_end, counts, nullptr, 0, 0, P, ds);
+    k_s_pairs<false><<<nblk(sc.N), NT, 0, s>>>(sc, g, sb, cell_body, cell_key, cell_start, cell_end, counts, nullptr, 0,
+                                               0, P, ds);
 }
 void launch_s_static_write(const Scene& sc, const SplitBuf& sb, const int32_t* flags, const int32_t* pos, int gen,
                            const SplitParams& P, cudaStream_t s) {
@@ -1591,11 +1590,12 @@ void launch_s_static_write(const Scene& sc, const SplitBuf& sb, const int32_t* f
     k_s_static_write<<<nblk(sc.N), NT, 0, s>>>(sc, sb, flags, pos, gen, P);
 }
 void launch_s_pair_write(const Scene& sc, const Grid& g, const SplitBuf& sb, const uint32_t* cell_body,
-                         const int32_t* cell_start, const int32_t* cell_end, const int32_t* offsets, int32_t base,
-                         int gen, const SplitParams& P, DevScalars* ds, cudaStream_t s) {
+                         const uint32_t* cell_key, const int32_t* cell_start, const int32_t* cell_end,
+                         const int32_t* offsets, int32_t base, int gen, const SplitParams& P, DevScalars* ds,
+                         cudaStream_t s) {
     if (sc.N == 0) return;
-    k_s_pairs<true><<<nblk(sc.N), NT, 0, s>>>(sc, g, sb, cell_body, cell_start, cell_end, nullptr, offsets, base, gen, P,
-                                              ds);
+    k_s_pairs<true><<<nblk(sc.N), NT, 0, s>>>(sc, g, sb, cell_body, cell_key, cell_start, cell_end, nullptr, offsets,
+                                              base, gen, P, ds);
 }
 void launch_s_reset(const SplitBuf& sb, cudaStream_t s) { k_s_reset<<<1, 1, 0, s>>>(sb); }
 void launch_s_end_step(const SplitBuf& sb, const DevScalars* ds, cudaStream_t s) {

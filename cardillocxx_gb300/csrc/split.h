@@ -118,15 +118,17 @@ int launch_s_solve_coop(const SplitBuf& sb, int gen, float alpha, int v, const C
                         int max_sweeps, int check_every, cudaStream_t s);
 void launch_s_prep(const Scene& sc, const SplitBuf& sb, double dt, const double* g, double h1, cudaStream_t s);
 void launch_s_static_flags(const Scene& sc, const SplitBuf& sb, float margin, int32_t* flags, cudaStream_t s);
+// cell_body / cell_key: the bodies and their cell keys sorted by cell
 void launch_s_pair_count(const Scene& sc, const Grid& g, const SplitBuf& sb, const uint32_t* cell_body,
-                         const int32_t* cell_start, const int32_t* cell_end, int32_t* counts, const SplitParams& P,
-                         DevScalars* ds, cudaStream_t s);
+                         const uint32_t* cell_key, const int32_t* cell_start, const int32_t* cell_end, int32_t* counts,
+                         const SplitParams& P, DevScalars* ds, cudaStream_t s);
 void launch_s_static_write(const Scene& sc, const SplitBuf& sb, const int32_t* flags, const int32_t* pos, int gen,
                            const SplitParams& P, cudaStream_t s);
 // base = first pair slot, or taken from the device (SplitScalars::n_static) when base < 0
 void launch_s_pair_write(const Scene& sc, const Grid& g, const SplitBuf& sb, const uint32_t* cell_body,
-                         const int32_t* cell_start, const int32_t* cell_end, const int32_t* offsets, int32_t base,
-                         int gen, const SplitParams& P, DevScalars* ds, cudaStream_t s);
+                         const uint32_t* cell_key, const int32_t* cell_start, const int32_t* cell_end,
+                         const int32_t* offsets, int32_t base, int gen, const SplitParams& P, DevScalars* ds,
+                         cudaStream_t s);
 // contact totals on the device: n_static, n_total, cap_err and nc_dev = min(total, capacity)
 void launch_s_totals(const SplitBuf& sb, const int32_t* spos, const int32_t* sflags, int64_t nflag, const int32_t* poff,
                      int N, cudaStream_t s);
