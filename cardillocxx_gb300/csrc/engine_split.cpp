@@ -274,7 +274,10 @@ int Engine::step_split() {
         }
         return maxit > 2 * sweeps;
     };
-    const bool scene_tuning = sc.nscenes > 1 && pinned < 0 && S->scene_best == -1 && cfg.gpu_autotune;
+    // the per-scene kernel (one block a scene, its bodies in shared memory) is a candidate for
+    // batches and for a single scene small enough for one block
+    const bool scene_fit = S->scene_nbmax > 0 && S->scene_nbmax <= 3584;
+    const bool scene_tuning = scene_fit && pinned < 0 && S->scene_best == -1 && cfg.gpu_autotune;
     const bool async = !cfg.gpu_sync_counts && S->prev_count > 0 && sb.cap > 0 && !S->force_sync && !scene_tuning &&
                        !tune_due(S->prev_count);
     S->force_sync = false;
@@ -285,7 +288,7 @@ int Engine::step_split() {
     }
     // A device-counted step whose solver is the cooperative or the batched-scenes kernel is
     // captured whole (snapshot to the final scalars) into a CUDA graph and replayed.
-    const bool multi0 = sc.nscenes > 1 && S->scene_nbmax > 0 && S->scene_nbmax <= 3584;
+    const bool multi0 = scene_fit;
     const bool scenes0 = async && multi0 && (pinned >= 0 ? split_variant_is_scenes(pinned) : S->scene_best >= 0);
     bool use_graph = async && cfg.gpu_use_graph && !timing && !S->sg_failed;
     if (use_graph && !scenes0) {

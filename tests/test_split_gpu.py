@@ -103,9 +103,8 @@ def test_split_every_sweep_shape_computes_the_same_sweep(gpu):
         e = PhysicsEngine(dict(c, **{"gpu.sweep_variant": v})).load_scene(s)
         e.set_state(st["pos"], st["quat"], st["vel"], st["omega"])
         e.step(1)
-        # a batched-scenes shape does not apply to a single scene: the streaming shape 0 runs instead
-        expect = 0 if names[v].startswith("scenes") else v
-        assert e.stats()["contact_variant"] == expect, names[v]
+        # the per-scene shapes apply to a single scene too (it fits one block)
+        assert e.stats()["contact_variant"] == v, names[v]
         out.append((e.contacts()["lambda"], e.state()["vel"]))
     lam0, vel0 = out[0]
     lmax = np.abs(lam0).max()
