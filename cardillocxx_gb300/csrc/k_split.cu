@@ -1017,6 +1017,9 @@ __global__ void __launch_bounds__(NT) k_s_solve_scenes(Scene sc, SplitBuf sb, in
                                                        const int32_t* poff, const int32_t* order, int L, int nbmax,
                                                        int ccap) {
     extern __shared__ float4 sm4[];
+    // a device-counted step whose contacts overflowed the buffers wrote only the slots below the
+    // capacity, while the scene ranges below count them all: nothing runs, the host redoes the step
+    if (*(volatile const int32_t*)&sb.ss->cap_err) return;
     float4* Ac = sm4;
     float4* An = sm4 + 2 * nbmax;
     __shared__ float s_r;

@@ -293,3 +293,25 @@ def test_pinned_state_transfers_match_pageable(gpu):
     st2 = eng2.state()
     for k in ref:
         assert np.array_equal(st2[k], ref[k]), k
+
+
+def test_per_scene_solver_on_overflowing_device_counted_steps(gpu):
+    # the per-scene kernel (pinned) on device-counted steps whose contacts outgrow the buffers (a
+    # step that overflowed them solves nothing and is redone); the run matches host-counted steps
+    names = PhysicsEngine.split_variants()
+    v = names.index("scenes-t128-u1-c1")
+    s = scenes.generate("pile_1k")
+    base = dict(scenes.config_for("pile_1k"), **{"gpu.precision": "split", "gpu.contact_capacity": 0.1,
+                                                 "gpu.sweep_variant": v})
+    a = PhysicsEngine(base).load_scene(s)
+    b = PhysicsEngine(dict(base, **{"gpu.sync_counts": True})).load_scene(s)
+    za, zb = [], []
+    for _ in range(10):
+        a.step(40)
+        b.step(40)
+        za.append(a.state()["pos"][:, 2].mean())
+        zb.append(b.state()["pos"][:, 2].mean())
+    assert b.stats()["redone_steps"] == 0
+    assert a.stats()["num_contacts"] > 1024  # more than the 1,024 slots it started with
+    assert a.stats()["contact_variant"] == v
+    np.testing.assert_allclose(za, zb, rtol=0, atol=2e-3)
