@@ -169,6 +169,8 @@ SIGNATURES = [
     ("cdx_pj_solve_csr", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, _PI, _PI, _P, _P, _P, _P, _P, _P,
                                    _P, _P, _P, C.c_double, C.c_double, C.c_int32, C.c_double, C.c_double, _P, _P,
                                    _PI]),
+    ("cdx_pj_solve_csr_cfg", C.c_int, [C.c_void_p, C.POINTER(CdxConfig), C.c_int32, C.c_int32, C.c_int32, _PI, _PI,
+                                       _P, _P, _P, _P, _P, _P, _P, _P, _P, C.c_double, _P, _P, _PI]),
     ("cdx_pj_solve_csr_noalloc", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, _PI, _PI, _P, _P, _P, _P,
                                            _P, _P, _P, _P, _P, C.c_double, C.c_double, C.c_int32, C.c_double,
                                            C.c_double, _P, _P, _PI, C.c_char_p, C.c_int32]),

@@ -13,6 +13,7 @@
 #pragma once
 #include <cstddef>
 #include <cstdint>
+#include <functional>
 
 #include <cuda_runtime.h>
 
@@ -147,6 +148,7 @@ struct AndersonBufs {
     double *ls = nullptr;                 // normal equations (m x m), right side (m), gamma (m)
     int32_t* rowmap = nullptr;            // impulse row -> index into the 3 x cap impulse array
     int64_t rowmap_cap = 0;
+    int plain = 0;                        // 1: x in stacked order and lam in row order (CSR drop-in)
     AndersonState* st = nullptr;
 };
 
@@ -204,9 +206,10 @@ void launch_final_residual(DevScalars* ds, cudaStream_t s);
 // accelerated loops (Nesterov, Chebyshev) of the plain FP64 method
 int accel_chunks(int N);
 void launch_accel_init(AccelState* st, cudaStream_t s);
+// plain = 1: vectors of length N in stacked order (the solver-level drop-in), else 6 x N field-major
 void launch_accel_reduce(int N, int op, const double* a, const double* b, const double* c, double tol_rel,
                          double tol_abs, double* part, AccelState* st, double* out, const DevScalars* ds,
-                         cudaStream_t s);
+                         cudaStream_t s, int plain = 0);
 void launch_accel_copy(double* xd, const double* xs, int64_t nx, double* ld, const double* ls, int64_t nl,
                        const DevScalars* ds, cudaStream_t s);
 void launch_nesterov_step(AccelState* st, DevScalars* ds, int nv, double beta_threshold, int restart_limit, double* xy,
@@ -218,9 +221,15 @@ int anderson_sums(int m);
 int anderson_chunks(int64_t n);
 void launch_anderson_begin(const Contacts& C, int gen, int nc, const int32_t* fl_scan, const int32_t* isfl, int N,
                            const double* x, AndersonBufs& A, cudaStream_t s);
+void launch_anderson_begin_plain(int nv, const double* x, const double* lam, AndersonBufs& A, cudaStream_t s);
+// N: bodies (6 x N field-major velocities), or the velocity count when A.plain
 void launch_anderson_scatter(int N, double* x, double* lam, const AndersonBufs& A, const DevScalars* ds, cudaStream_t s);
 void launch_anderson_mix(int N, const double* x, const double* lam, const AndersonBufs& A, double tol_rel,
                          double tol_abs, DevScalars* ds, cudaStream_t s);
+// estimateSpectralRadius's eight power steps; apply() launches Mv = M v (N bodies, or N velocities
+// when plain)
+void launch_power_iteration(int N, int plain, double* v, double* Mv, double* part, AccelState* st,
+                            const std::function<void()>& apply, cudaStream_t s);
 void launch_spectral_radius(const Scene& sc, Contacts& C, const Incidence& inc, int nc, double* v, double* Mv,
                             double* part, AccelState* st, cudaStream_t s);
 void launch_writeback64(const Scene& sc, const double* x, cudaStream_t s);
@@ -235,14 +244,25 @@ void launch_csr_rhs(int nv, const double* mdiag, const double* v, const double* 
                     double* rhs, cudaStream_t s);
 void launch_csr_rowidx(int nrows, const int32_t* ptr, int32_t* rowidx, uint32_t* colkey, uint32_t* nzid,
                        const int32_t* col, cudaStream_t s);
+// block = 1: pj.rdiag_true_delassus (W and the bias unscaled; the blocks come from launch_csr_blocks)
 void launch_csr_setup(int nrows, const int32_t* ptr, const int32_t* col, const double* val, const double* cb,
                       const double* e, const double* minv, const double* v, double alpha, double* RW, double* biasR,
-                      cudaStream_t s);
+                      cudaStream_t s, int block = 0);
+// per-unit inverse Delassus blocks / alpha (9 doubles a unit) and the flag of a non-diagonal block
+void launch_csr_blocks(int nrows, int nfl, const int32_t* ptr, const int32_t* col, const double* val,
+                       const double* minv, double alpha, double* Rb, int32_t* full, cudaStream_t s);
+// Mv = v - S^-1 W^T R_block (RW v): the linear part of the sweep map (power iteration)
+void launch_csr_linear(int nrows, int nfl, int nv, const int32_t* ptr, const int32_t* col, const double* RW,
+                       const double* Rb, const int32_t* full, const int32_t* cstart, const int32_t* cend,
+                       const uint32_t* nz_sorted, const int32_t* rowidx, const double* val, const double* mdiag,
+                       const double* v, double* delta, double* Mv, cudaStream_t s);
 void launch_csr_cols(int nv, const int32_t* cstart, const int32_t* cend, const uint32_t* nz_sorted,
                      const int32_t* rowidx, const double* val, const double* y, const double* base,
                      const double* mdiag, double* x, int mode, double tol_abs, double tol_rel, int want_velres,
                      DevScalars* ds, cudaStream_t s);
+// Rb/full: the block preconditioner (nullptr: the row scale folded into RW); dry: residual only
 void launch_csr_rows(int nrows, int nfl, const int32_t* ptr, const int32_t* col, const double* RW,
                      const double* biasR, const double* mu, const double* x, double* lam, double* dlam,
-                     DevScalars* ds, cudaStream_t s);
+                     DevScalars* ds, cudaStream_t s, const double* Rb = nullptr, const int32_t* full = nullptr,
+                     int dry = 0);
 }  // namespace cdx

@@ -22,6 +22,14 @@ struct CsrBuffers {
     double *minv = nullptr, *mdiag = nullptr, *v = nullptr, *fext = nullptr, *fgyro = nullptr, *rhs = nullptr,
            *x = nullptr;
     DevScalars* ds = nullptr;
+    // block preconditioner (9 doubles a unit) and the accelerated loops' copies, grown on demand
+    int64_t unit_cap = 0, acc_rows = 0, acc_nv = 0;
+    double* Rb = nullptr;
+    int32_t* full = nullptr;
+    double *xk = nullptr, *xk1 = nullptr, *xy = nullptr, *pk = nullptr, *pk1 = nullptr, *py = nullptr,
+           *part = nullptr;
+    AccelState* st = nullptr;
+    AndersonBufs anderson;
 };
 }  // namespace cdx
 

@@ -108,5 +108,55 @@ __device__ __forceinline__ double combine_mu(int mode, double a, double b) {
     return smin(a, b);
 }
 
+// invertSmallSpd (misc/block_diagonal.hpp:15-27) for n <= 3, row-major: Cholesky from the lower
+// triangle, column by column, then forward and back substitution of each identity column; a
+// pivot that is not positive takes the reference's last fallback, the diagonal inverse
+static __device__ __noinline__ void spd_inverse_dev(const double* A, int n, double* X) {
+    double L[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    bool ok = true;
+    for (int j = 0; j < n && ok; ++j) {
+        double s = A[j * n + j];
+        for (int k = 0; k < j; ++k) s = s - L[j * 3 + k] * L[j * 3 + k];
+        if (!(s > 0.0)) {
+            ok = false;
+            break;
+        }
+        L[j * 3 + j] = sqrt(s);
+        for (int i = j + 1; i < n; ++i) {
+            double t = A[i * n + j];
+            for (int k = 0; k < j; ++k) t = t - L[i * 3 + k] * L[j * 3 + k];
+            L[i * 3 + j] = t / L[j * 3 + j];
+        }
+    }
+    if (!ok) {
+        for (int i = 0; i < n * n; ++i) X[i] = 0.0;
+        for (int i = 0; i < n; ++i) X[i * n + i] = 1.0 / A[i * n + i];
+        return;
+    }
+    for (int c = 0; c < n; ++c) {
+        double y[3];
+        for (int i = 0; i < n; ++i) {
+            double t = (i == c) ? 1.0 : 0.0;
+            for (int k = 0; k < i; ++k) t = t - L[i * 3 + k] * y[k];
+            y[i] = t / L[i * 3 + i];
+        }
+        for (int i = n - 1; i >= 0; --i) {
+            double t = y[i];
+            for (int k = i + 1; k < n; ++k) t = t - L[k * 3 + i] * X[k * n + c];
+            X[i * n + c] = t / L[i * 3 + i];
+        }
+    }
+}
+
+// MatrixBase::isDiagonal (Eigen 3) with its default precision for double, 1e-12, on a 3x3 block
+__device__ __forceinline__ bool block_is_diagonal3(const double* D) {
+    double md = -1.0;
+    for (int j = 0; j < 3; ++j) md = smax(md, fabs(D[4 * j]));
+    bool diag = true;
+    for (int j = 0; j < 3; ++j)
+        for (int i = 0; i < j; ++i) diag = diag && (fabs(D[3 * i + j]) <= md * 1e-12) && (fabs(D[3 * j + i]) <= md * 1e-12);
+    return diag;
+}
+
 }  // namespace f64
 }  // namespace cdx

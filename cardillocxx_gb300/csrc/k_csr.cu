@@ -31,10 +31,11 @@ __global__ void k_csr_rowidx(int nrows, const int32_t* ptr, int32_t* rowidx, uin
     }
 }
 
-// build_workspace + rdiag_sparse per row
+// build_workspace + rdiag_sparse per row; with block, W and the bias stay unscaled
+// (pj.rdiag_true_delassus, projected_jacobi.cpp:341-343)
 __global__ void k_csr_setup(int nrows, const int32_t* ptr, const int32_t* col, const double* val, const double* cb,
                             const double* e, const double* minv, const double* v, double alpha, double* RW,
-                            double* biasR) {
+                            double* biasR, int block) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nrows) return;
     double vp = 0.0, D = 0.0;
@@ -42,9 +43,119 @@ __global__ void k_csr_setup(int nrows, const int32_t* ptr, const int32_t* col, c
     vp = vp + cb[r];
     const double bias = cb[r] + e[r] * vp;
     for (int k = ptr[r]; k < ptr[r + 1]; ++k) D = D + (val[k] * val[k]) * minv[col[k]];
+    if (block) {
+        for (int k = ptr[r]; k < ptr[r + 1]; ++k) RW[k] = val[k];
+        biasR[r] = bias;
+        return;
+    }
     const double R = (D > 0.0) ? (alpha / D) : 0.0;
     for (int k = ptr[r]; k < ptr[r + 1]; ++k) RW[k] = R * val[k];
     biasR[r] = R * bias;
+}
+
+// buildBlockPreconditioner (projected_jacobi.cpp:81-98): per unit (a frictionless row, or the three
+// rows of a frictional contact) its block of W M^-1 W^T / alpha into Rb (9 a unit, row-major;
+// a frictionless unit uses Rb[0]). The rows of one contact share their columns, so
+// D_ab = sum_q (W_aq Minv_q) W_bq over them. A block that is not diagonal sets *full.
+__global__ void k_csr_blocks(int nrows, int nfl, const int32_t* ptr, const int32_t* col, const double* val,
+                             const double* minv, double alpha, double* Rb, int32_t* full) {
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nunits = nfl + (nrows - nfl) / 3;
+    if (u >= nunits) return;
+    const double inv_alpha = (alpha > 0.0) ? (1.0 / alpha) : 0.0;
+    double* B = Rb + 9 * (size_t)u;
+    if (u < nfl) {
+        double d = 0.0;
+        for (int k = ptr[u]; k < ptr[u + 1]; ++k) d = d + val[k] * val[k] * minv[col[k]];
+        B[0] = d * inv_alpha;
+        return;
+    }
+    const int r0 = nfl + 3 * (u - nfl);
+    const int len = ptr[r0 + 1] - ptr[r0];
+    double D[9];
+    for (int a = 0; a < 3; ++a)
+        for (int c = 0; c < 3; ++c) {
+            const int pa = ptr[r0 + a], pc = ptr[r0 + c];
+            double d = 0.0;
+            for (int q = 0; q < len; ++q) d = d + (val[pa + q] * minv[col[pa + q]]) * val[pc + q];
+            D[3 * a + c] = d * inv_alpha;
+        }
+    for (int k = 0; k < 9; ++k) B[k] = D[k];
+    if (!block_is_diagonal3(D)) *full = 1;
+}
+
+// BlockDiagonal::calculateInverse: per diagonal entry when every block is diagonal, else the SPD
+// inverse of every block (1 x 1 blocks included)
+__global__ void k_csr_block_inv(int nrows, int nfl, double* Rb, const int32_t* full) {
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nunits = nfl + (nrows - nfl) / 3;
+    if (u >= nunits) return;
+    const bool f = *full != 0;
+    double* B = Rb + 9 * (size_t)u;
+    if (u < nfl) {
+        const double d = B[0];
+        double x;
+        if (f) spd_inverse_dev(&d, 1, &x);
+        else x = 1.0 / d;
+        B[0] = x;
+        return;
+    }
+    double D[9], X[9];
+    for (int k = 0; k < 9; ++k) D[k] = B[k];
+    if (f) {
+        spd_inverse_dev(D, 3, X);
+    } else {
+        for (int k = 0; k < 9; ++k) X[k] = 0.0;
+        for (int j = 0; j < 3; ++j) X[4 * j] = 1.0 / D[4 * j];
+    }
+    for (int k = 0; k < 9; ++k) B[k] = X[k];
+}
+
+// BlockDiagonal::applyTo (misc/block_diagonal.hpp:107-126) on one unit's rows g
+__device__ __forceinline__ void csr_block_apply(const double* B, bool fr, bool full, double* g) {
+    if (!fr) {
+        g[0] = full ? B[0] * g[0] : g[0] * B[0];
+        return;
+    }
+    if (!full) {
+        for (int j = 0; j < 3; ++j) g[j] = g[j] * B[4 * j];
+        return;
+    }
+    double s[3];
+    for (int j = 0; j < 3; ++j) s[j] = B[3 * j] * g[0] + B[3 * j + 1] * g[1] + B[3 * j + 2] * g[2];
+    for (int j = 0; j < 3; ++j) g[j] = s[j];
+}
+
+// linear part of the sweep map for the power iteration: delta = R_block (RW v) per unit
+__global__ void k_csr_linear_rows(int nrows, int nfl, const int32_t* ptr, const int32_t* col, const double* RW,
+                                  const double* Rb, const int32_t* full, const double* v, double* delta) {
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nunits = nfl + (nrows - nfl) / 3;
+    if (u >= nunits) return;
+    const bool fr = u >= nfl;
+    const int r0 = fr ? nfl + 3 * (u - nfl) : u;
+    const int nr = fr ? 3 : 1;
+    double g[3];
+    for (int q = 0; q < nr; ++q) {
+        double t = 0.0;
+        for (int k = ptr[r0 + q]; k < ptr[r0 + q + 1]; ++k) t = t + RW[k] * v[col[k]];
+        g[q] = t;
+    }
+    if (Rb) csr_block_apply(Rb + 9 * (size_t)u, fr, *full != 0, g);
+    for (int q = 0; q < nr; ++q) delta[r0 + q] = g[q];
+}
+// Mv_j = v_j - (sum over column j's entries, row order, of W delta) / M_j
+__global__ void k_csr_linear_cols(int nv, const int32_t* cstart, const int32_t* cend, const uint32_t* nz_sorted,
+                                  const int32_t* rowidx, const double* val, const double* delta, const double* mdiag,
+                                  const double* v, double* Mv) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nv) return;
+    double acc = 0.0;
+    for (int p = cstart[j]; p < cend[j]; ++p) {
+        const int k = (int)nz_sorted[p];
+        acc = acc + val[k] * delta[rowidx[k]];
+    }
+    Mv[j] = v[j] - acc / mdiag[j];
 }
 
 // dst_j (+)= sum over column j's entries (row order) of val * y[row]; then x_j = (dst or x + dst)/M
@@ -90,8 +201,8 @@ __global__ void k_csr_cols(int nv, const int32_t* cstart, const int32_t* cend, c
 // one thread per contact unit: a frictionless row, or a 3-row frictional block
 __global__ void k_csr_rows(int nrows, int nfl, const int32_t* ptr, const int32_t* col, const double* RW,
                            const double* biasR, const double* mu, const double* x, double* lam, double* dlam,
-                           DevScalars* ds) {
-    if (*(volatile int32_t*)&ds->done) return;
+                           DevScalars* ds, const double* Rb, const int32_t* full, int dry) {
+    if (!dry && *(volatile int32_t*)&ds->done) return;
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
     const int nunits = nfl + (nrows - nfl) / 3;
     double maxd = 0.0, maxl = 0.0;
@@ -99,15 +210,16 @@ __global__ void k_csr_rows(int nrows, int nfl, const int32_t* ptr, const int32_t
         const bool fr = u >= nfl;
         const int r0 = fr ? nfl + 3 * (u - nfl) : u;
         const int nr = fr ? 3 : 1;
-        double lo[3], ln[3];
+        double lo[3], ln[3], g[3];
         for (int q = 0; q < nr; ++q) {
             const int r = r0 + q;
             double t = 0.0;
             for (int k = ptr[r]; k < ptr[r + 1]; ++k) t = t + RW[k] * x[col[k]];
-            const double g = t + biasR[r];
+            g[q] = t + biasR[r];
             lo[q] = lam[r];
-            ln[q] = lo[q] - g;
         }
+        if (Rb) csr_block_apply(Rb + 9 * (size_t)u, fr, *full != 0, g);
+        for (int q = 0; q < nr; ++q) ln[q] = lo[q] - g[q];
         ln[0] = smax(ln[0], 0.0);
         if (fr) {
             const double t1 = ln[1], t2 = ln[2];
@@ -123,8 +235,10 @@ __global__ void k_csr_rows(int nrows, int nfl, const int32_t* ptr, const int32_t
             const double d = ln[q] - lo[q];
             s2 = s2 + d * d;
             maxl = smax(maxl, fabs(lo[q]));
-            lam[r0 + q] = ln[q];
-            dlam[r0 + q] = d;
+            if (!dry) {
+                lam[r0 + q] = ln[q];
+                dlam[r0 + q] = d;
+            }
         }
         maxd = sqrt(s2);
     }
@@ -163,8 +277,26 @@ void launch_csr_rowidx(int nrows, const int32_t* ptr, int32_t* rowidx, uint32_t*
 }
 void launch_csr_setup(int nrows, const int32_t* ptr, const int32_t* col, const double* val, const double* cb,
                       const double* e, const double* minv, const double* v, double alpha, double* RW, double* biasR,
-                      cudaStream_t s) {
-    if (nrows > 0) k_csr_setup<<<nblk(nrows), NT, 0, s>>>(nrows, ptr, col, val, cb, e, minv, v, alpha, RW, biasR);
+                      cudaStream_t s, int block) {
+    if (nrows > 0)
+        k_csr_setup<<<nblk(nrows), NT, 0, s>>>(nrows, ptr, col, val, cb, e, minv, v, alpha, RW, biasR, block);
+}
+void launch_csr_blocks(int nrows, int nfl, const int32_t* ptr, const int32_t* col, const double* val,
+                       const double* minv, double alpha, double* Rb, int32_t* full, cudaStream_t s) {
+    const int nunits = nfl + (nrows - nfl) / 3;
+    if (nunits <= 0) return;
+    cudaMemsetAsync(full, 0, sizeof(int32_t), s);
+    k_csr_blocks<<<nblk(nunits), NT, 0, s>>>(nrows, nfl, ptr, col, val, minv, alpha, Rb, full);
+    k_csr_block_inv<<<nblk(nunits), NT, 0, s>>>(nrows, nfl, Rb, full);
+}
+void launch_csr_linear(int nrows, int nfl, int nv, const int32_t* ptr, const int32_t* col, const double* RW,
+                       const double* Rb, const int32_t* full, const int32_t* cstart, const int32_t* cend,
+                       const uint32_t* nz_sorted, const int32_t* rowidx, const double* val, const double* mdiag,
+                       const double* v, double* delta, double* Mv, cudaStream_t s) {
+    const int nunits = nfl + (nrows - nfl) / 3;
+    if (nunits > 0) k_csr_linear_rows<<<nblk(nunits), NT, 0, s>>>(nrows, nfl, ptr, col, RW, Rb, full, v, delta);
+    if (nv > 0)
+        k_csr_linear_cols<<<nblk(nv), NT, 0, s>>>(nv, cstart, cend, nz_sorted, rowidx, val, delta, mdiag, v, Mv);
 }
 void launch_csr_cols(int nv, const int32_t* cstart, const int32_t* cend, const uint32_t* nz_sorted,
                      const int32_t* rowidx, const double* val, const double* y, const double* base,
@@ -176,9 +308,10 @@ void launch_csr_cols(int nv, const int32_t* cstart, const int32_t* cend, const u
 }
 void launch_csr_rows(int nrows, int nfl, const int32_t* ptr, const int32_t* col, const double* RW,
                      const double* biasR, const double* mu, const double* x, double* lam, double* dlam,
-                     DevScalars* ds, cudaStream_t s) {
+                     DevScalars* ds, cudaStream_t s, const double* Rb, const int32_t* full, int dry) {
     const int nunits = nfl + (nrows - nfl) / 3;
-    if (nunits > 0) k_csr_rows<<<nblk(nunits), NT, 0, s>>>(nrows, nfl, ptr, col, RW, biasR, mu, x, lam, dlam, ds);
+    if (nunits > 0)
+        k_csr_rows<<<nblk(nunits), NT, 0, s>>>(nrows, nfl, ptr, col, RW, biasR, mu, x, lam, dlam, ds, Rb, full, dry);
 }
 
 }  // namespace cdx

@@ -14,6 +14,7 @@
 // is applied as a per-body gather over the body's incidence list in solver row order.
 #include <algorithm>
 #include <cstdio>
+#include <functional>
 
 #include "cdx_internal.h"
 #include "fp64_math.cuh"
@@ -517,53 +518,7 @@ __global__ void k_contact_setup64(Scene sc, Contacts C, int gen, int nc, int pre
             for (int k = 0; k < 9; ++k) C.rb[(size_t)k * cap + c] = Db[k];
             // MatrixBase::isDiagonal (Eigen 3, precision 1e-12); one non-diagonal block switches
             // every block of the step to the full inverse (BlockDiagonal::calculateInverse)
-            double md = -1.0;
-            for (int j = 0; j < 3; ++j) md = smax(md, fabs(Db[4 * j]));
-            bool diag = true;
-            for (int j = 0; j < 3; ++j)
-                for (int i = 0; i < j; ++i)
-                    diag = diag && (fabs(Db[3 * i + j]) <= md * 1e-12) && (fabs(Db[3 * j + i]) <= md * 1e-12);
-            if (!diag) *C.rb_full = 1;
-        }
-    }
-}
-
-// invertSmallSpd (misc/block_diagonal.hpp:15-27) for n <= 3, row-major: Cholesky from the lower
-// triangle, column by column, then forward and back substitution of each identity column; a
-// pivot that is not positive takes the reference's last fallback, the diagonal inverse
-__device__ void spd_inverse_dev(const double* A, int n, double* X) {
-    double L[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    bool ok = true;
-    for (int j = 0; j < n && ok; ++j) {
-        double s = A[j * n + j];
-        for (int k = 0; k < j; ++k) s = s - L[j * 3 + k] * L[j * 3 + k];
-        if (!(s > 0.0)) {
-            ok = false;
-            break;
-        }
-        L[j * 3 + j] = sqrt(s);
-        for (int i = j + 1; i < n; ++i) {
-            double t = A[i * n + j];
-            for (int k = 0; k < j; ++k) t = t - L[i * 3 + k] * L[j * 3 + k];
-            L[i * 3 + j] = t / L[j * 3 + j];
-        }
-    }
-    if (!ok) {
-        for (int i = 0; i < n * n; ++i) X[i] = 0.0;
-        for (int i = 0; i < n; ++i) X[i * n + i] = 1.0 / A[i * n + i];
-        return;
-    }
-    for (int c = 0; c < n; ++c) {
-        double y[3];
-        for (int i = 0; i < n; ++i) {
-            double t = (i == c) ? 1.0 : 0.0;
-            for (int k = 0; k < i; ++k) t = t - L[i * 3 + k] * y[k];
-            y[i] = t / L[i * 3 + i];
-        }
-        for (int i = n - 1; i >= 0; --i) {
-            double t = y[i];
-            for (int k = i + 1; k < n; ++k) t = t - L[k * 3 + i] * X[k * n + c];
-            X[i * n + c] = t / L[i * 3 + i];
+            if (!block_is_diagonal3(Db)) *C.rb_full = 1;
         }
     }
 }
@@ -822,11 +777,15 @@ __global__ void k_check(DevScalars* ds, int iter, double residual_tol, int nv, i
 // reference's layout), each chunk left to right, then the chunk sums left to right.
 constexpr int RED_CHUNK = 256;
 __device__ __forceinline__ double stacked(const double* v, int N, int j) { return v[(size_t)(j % 6) * N + j / 6]; }
+__device__ __forceinline__ double elem(const double* v, int N, int j, int plain) {
+    return plain ? v[j] : stacked(v, N, j);
+}
 
+// plain: the vectors are already in stacked order (the solver-level drop-in, N = their length)
 __global__ void k_chunk_partials(int N, int op, const double* a, const double* b, const double* c, double tol_rel,
-                                 double tol_abs, double* part, AccelState* st, const DevScalars* ds) {
+                                 double tol_abs, double* part, AccelState* st, const DevScalars* ds, int plain) {
     if (ds && *(volatile const int32_t*)&ds->done) return;
-    const int nv = 6 * N;
+    const int nv = plain ? N : 6 * N;
     const int nch = (nv + RED_CHUNK - 1) / RED_CHUNK;
     const int ch = blockIdx.x * blockDim.x + threadIdx.x;
     if (ch >= nch) return;
@@ -836,16 +795,16 @@ __global__ void k_chunk_partials(int N, int op, const double* a, const double* b
     for (int j = j0; j < j1; ++j) {
         double t;
         if (op == ACC_VELRES) {
-            const double x = stacked(a, N, j), xp = stacked(b, N, j);
+            const double x = elem(a, N, j, plain), xp = elem(b, N, j, plain);
             const double q = smax(fabs(x), fabs(xp)) * tol_rel + tol_abs;
             const double d = (x - xp) / q;
             t = d * d;
             finite = finite && isfinite(x);
         } else if (op == ACC_NORM2) {
-            const double x = stacked(a, N, j);
+            const double x = elem(a, N, j, plain);
             t = x * x;
         } else if (op == ACC_DOT) {
-            const double y = stacked(a, N, j), x1 = stacked(b, N, j), x0 = stacked(c, N, j);
+            const double y = elem(a, N, j, plain), x1 = elem(b, N, j, plain), x0 = elem(c, N, j, plain);
             t = (y - x1) * (x1 - x0);
         } else {
             t = 1.0;
@@ -1091,14 +1050,17 @@ __global__ void k_and_rowmap(Contacts C, int nc, const int32_t* fl_scan, const i
 }
 
 // dense <- (x, lam); mode 0: z only (start), mode 1: w, f = w - z and the newest history slot
+// plain: x of length N already in stacked order and lam in row order (no row map): the
+// solver-level drop-in; else x is 6 x N field-major and lam goes through the row map
 __global__ void k_and_gather(int N, const double* x, const double* lam, const int32_t* rowmap, int64_t nt, int m,
                              int64_t ld, double* z, double* w, double* f, double* zh, double* fh,
-                             const AndersonState* as, const DevScalars* ds, int mode) {
+                             const AndersonState* as, const DevScalars* ds, int mode, int plain) {
     if (ds && *(volatile const int32_t*)&ds->done) return;
-    const int64_t nv = 6 * (int64_t)N;
+    const int64_t nv = plain ? (int64_t)N : 6 * (int64_t)N;
     const int slot = mode ? ring_slot(as, m, as->count - 1) : 0;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt; t += (int64_t)gridDim.x * blockDim.x) {
-        const double v = t < nv ? x[(size_t)(t % 6) * N + t / 6] : lam[rowmap[t - nv]];
+        const double v = t < nv ? (plain ? x[t] : x[(size_t)(t % 6) * N + t / 6])
+                                : lam[plain ? t - nv : rowmap[t - nv]];
         if (!mode) {
             z[t] = v;
         } else {
@@ -1113,14 +1075,14 @@ __global__ void k_and_gather(int N, const double* x, const double* lam, const in
 }
 
 __global__ void k_and_scatter(int N, double* x, double* lam, const int32_t* rowmap, int64_t nt, const double* z,
-                              const DevScalars* ds) {
+                              const DevScalars* ds, int plain) {
     if (ds && *(volatile const int32_t*)&ds->done) return;
-    const int64_t nv = 6 * (int64_t)N;
+    const int64_t nv = plain ? (int64_t)N : 6 * (int64_t)N;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt; t += (int64_t)gridDim.x * blockDim.x) {
         if (t < nv)
-            x[(size_t)(t % 6) * N + t / 6] = z[t];
+            x[plain ? (size_t)t : (size_t)(t % 6) * N + t / 6] = z[t];
         else
-            lam[rowmap[t - nv]] = z[t];
+            lam[plain ? t - nv : rowmap[t - nv]] = z[t];
     }
 }
 
@@ -1137,12 +1099,12 @@ __global__ void k_and_push(AndersonState* as, int m, const DevScalars* ds) {
 // then (dF_j . dF_l) for l <= j < mk and (dF_j . f) for j < mk, dF_j = F_{j+1} - F_j (oldest first)
 __global__ void k_and_partials(int N, int64_t nt, int m, int64_t ld, const double* z, const double* w, const double* f,
                                const double* fh, double tol_rel, double tol_abs, double* part, int nch_t,
-                               const AndersonState* as, const DevScalars* ds) {
+                               const AndersonState* as, const DevScalars* ds, int plain) {
     if (ds && *(volatile const int32_t*)&ds->done) return;
     const int ch = blockIdx.x * blockDim.x + threadIdx.x;
     const int sidx = blockIdx.y;
     const int mk = as->count - 1;
-    const int64_t nv = 6 * (int64_t)N;
+    const int64_t nv = plain ? (int64_t)N : 6 * (int64_t)N;
     const int nsums = 1 + mk * (mk + 1) / 2 + (mk > 0 ? mk : 0);
     if (sidx >= nsums) return;
     const int64_t n = sidx == 0 ? nv : nt;
@@ -1384,9 +1346,9 @@ void launch_final_residual(DevScalars* ds, cudaStream_t s) { k_final_residual<<<
 int accel_chunks(int N) { return (6 * N + RED_CHUNK - 1) / RED_CHUNK; }
 void launch_accel_reduce(int N, int op, const double* a, const double* b, const double* c, double tol_rel,
                          double tol_abs, double* part, AccelState* st, double* out, const DevScalars* ds,
-                         cudaStream_t s) {
-    const int nch = accel_chunks(N);
-    k_chunk_partials<<<nblk(nch, 128), 128, 0, s>>>(N, op, a, b, c, tol_rel, tol_abs, part, st, ds);
+                         cudaStream_t s, int plain) {
+    const int nch = plain ? (N + RED_CHUNK - 1) / RED_CHUNK : accel_chunks(N);
+    k_chunk_partials<<<nblk(nch, 128), 128, 0, s>>>(N, op, a, b, c, tol_rel, tol_abs, part, st, ds, plain);
     k_chunk_total<<<1, 1, 0, s>>>(part, nch, out, ds);
 }
 void launch_accel_copy(double* xd, const double* xs, int64_t nx, double* ld, const double* ls, int64_t nl,
@@ -1404,21 +1366,27 @@ void launch_chebyshev_step(AccelState* st, DevScalars* ds, int nv, int iter, con
     k_chebyshev_decide<<<1, 1, 0, s>>>(st, ds, nv, iter);
     k_chebyshev_update<<<nblk(nx + nl), NT, 0, s>>>(x, xk, xk1, nx, lam, pk, pk1, nl, st, ds);
 }
-void launch_spectral_radius(const Scene& sc, Contacts& C, const Incidence& inc, int nc, double* v, double* Mv,
-                            double* part, AccelState* st, cudaStream_t s) {
-    const int N = sc.N;
-    const int64_t n = 6 * (int64_t)N;
+void launch_power_iteration(int N, int plain, double* v, double* Mv, double* part, AccelState* st,
+                            const std::function<void()>& apply, cudaStream_t s) {
+    const int64_t n = plain ? (int64_t)N : 6 * (int64_t)N;
     k_accel_init<<<1, 1, 0, s>>>(st);
-    launch_accel_reduce(N, ACC_ONES, nullptr, nullptr, nullptr, 0.0, 0.0, part, st, &st->sum_err, nullptr, s);
+    launch_accel_reduce(N, ACC_ONES, nullptr, nullptr, nullptr, 0.0, 0.0, part, st, &st->sum_err, nullptr, s, plain);
     k_power_fill<<<nblk(n), NT, 0, s>>>(v, n, st);
     for (int it = 0; it < 8; ++it) {
-        if (nc > 0) k_linear_contact64<<<nblk(nc), NT, 0, s>>>(sc, C, nc, v);
-        k_linear_body64<<<nblk(N), NT, 0, s>>>(sc, C, inc, v, Mv);
-        launch_accel_reduce(N, ACC_NORM2, Mv, nullptr, nullptr, 0.0, 0.0, part, st, &st->sum_err, nullptr, s);
+        apply();
+        launch_accel_reduce(N, ACC_NORM2, Mv, nullptr, nullptr, 0.0, 0.0, part, st, &st->sum_err, nullptr, s, plain);
         k_power_norm<<<1, 1, 0, s>>>(st);
         k_power_scale<<<nblk(n), NT, 0, s>>>(v, Mv, n, st);
     }
     k_power_finish<<<1, 1, 0, s>>>(st);
+}
+void launch_spectral_radius(const Scene& sc, Contacts& C, const Incidence& inc, int nc, double* v, double* Mv,
+                            double* part, AccelState* st, cudaStream_t s) {
+    const int N = sc.N;
+    launch_power_iteration(N, 0, v, Mv, part, st, [&]() {
+        if (nc > 0) k_linear_contact64<<<nblk(nc), NT, 0, s>>>(sc, C, nc, v);
+        k_linear_body64<<<nblk(N), NT, 0, s>>>(sc, C, inc, v, Mv);
+    }, s);
 }
 void launch_accel_init(AccelState* st, cudaStream_t s) { k_accel_init<<<1, 1, 0, s>>>(st); }
 
@@ -1430,22 +1398,28 @@ void launch_anderson_begin(const Contacts& C, int gen, int nc, const int32_t* fl
     k_and_init<<<1, 1, 0, s>>>(A.st);
     if (nc > 0) k_and_rowmap<<<nblk(nc), NT, 0, s>>>(C, nc, fl_scan, isfl, A.rowmap);
     k_and_gather<<<grid_of(A.nt), NT, 0, s>>>(N, x, C.lam[gen], A.rowmap, A.nt, A.m, A.nt_cap, A.z, A.w, A.f, A.zh,
-                                              A.fh, A.st, nullptr, 0);
+                                              A.fh, A.st, nullptr, 0, 0);
+}
+void launch_anderson_begin_plain(int nv, const double* x, const double* lam, AndersonBufs& A, cudaStream_t s) {
+    k_and_init<<<1, 1, 0, s>>>(A.st);
+    k_and_gather<<<grid_of(A.nt), NT, 0, s>>>(nv, x, lam, nullptr, A.nt, A.m, A.nt_cap, A.z, A.w, A.f, A.zh, A.fh,
+                                              A.st, nullptr, 0, 1);
 }
 void launch_anderson_scatter(int N, double* x, double* lam, const AndersonBufs& A, const DevScalars* ds,
                              cudaStream_t s) {
-    k_and_scatter<<<grid_of(A.nt), NT, 0, s>>>(N, x, lam, A.rowmap, A.nt, A.z, ds);
+    k_and_scatter<<<grid_of(A.nt), NT, 0, s>>>(N, x, lam, A.rowmap, A.nt, A.z, ds, A.plain);
 }
 void launch_anderson_mix(int N, const double* x, const double* lam, const AndersonBufs& A, double tol_rel,
                          double tol_abs, DevScalars* ds, cudaStream_t s) {
-    const int nch_t = anderson_chunks(A.nt), nch_v = anderson_chunks(6 * (int64_t)N);
+    const int nv = A.plain ? N : 6 * N;
+    const int nch_t = anderson_chunks(A.nt), nch_v = anderson_chunks(nv);
     k_and_push<<<1, 1, 0, s>>>(A.st, A.m, ds);
     k_and_gather<<<grid_of(A.nt), NT, 0, s>>>(N, x, lam, A.rowmap, A.nt, A.m, A.nt_cap, A.z, A.w, A.f, A.zh, A.fh,
-                                              A.st, ds, 1);
+                                              A.st, ds, 1, A.plain);
     dim3 g((unsigned)nblk(nch_t, 128), (unsigned)anderson_sums(A.m));
     k_and_partials<<<g, 128, 0, s>>>(N, A.nt, A.m, A.nt_cap, A.z, A.w, A.f, A.fh, tol_rel, tol_abs, A.part, nch_t,
-                                     A.st, ds);
-    k_and_solve<<<1, 1, 0, s>>>(6 * N, nch_v, nch_t, A.part, A.ls, A.m, A.st, ds);
+                                     A.st, ds, A.plain);
+    k_and_solve<<<1, 1, 0, s>>>(nv, nch_v, nch_t, A.part, A.ls, A.m, A.st, ds);
     const double* gam = A.ls + (size_t)A.m * A.m + A.m;
     k_and_candidate<<<grid_of(A.nt), NT, 0, s>>>(A.nt, A.m, A.nt_cap, A.w, A.zh, A.fh, gam, A.cand, A.st, ds);
     k_and_select<<<grid_of(A.nt), NT, 0, s>>>(A.nt, A.z, A.w, A.cand, A.st, ds);

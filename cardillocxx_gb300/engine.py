@@ -221,3 +221,22 @@ class PhysicsEngine:
                                             *[dp(a) for a in arrs], float(dt), float(alpha), int(max_iter),
                                             float(tol_abs), float(tol_rel), dp(lam), dp(x), C.byref(it)))
         return x, lam, it.value
+
+    def pj_solve_csr_cfg(self, cfg, row_ptr, col, val, contact_bias, mu, restitution, minv, mdiag, v, f_ext, f_gyro,
+                         dt, lam0, nfl=0):
+        """The solver-level drop-in under a configuration (loop, block preconditioner, stop rules)."""
+        if not isinstance(cfg, Config):
+            cfg = Config(cfg)
+        row_ptr = np.ascontiguousarray(row_ptr, np.int32)
+        col = np.ascontiguousarray(col, np.int32)
+        arrs = [np.ascontiguousarray(a, np.float64) for a in (val, contact_bias, mu, restitution, minv, mdiag, v,
+                                                              f_ext, f_gyro)]
+        nrows = row_ptr.shape[0] - 1
+        nv = arrs[4].shape[0]
+        lam = np.array(lam0, np.float64, copy=True)
+        x = np.empty(nv)
+        it = C.c_int32(0)
+        self._check(self.L.cdx_pj_solve_csr_cfg(self.h, C.byref(cfg.struct), nrows, nv, int(nfl), ip(row_ptr),
+                                                ip(col), *[dp(a) for a in arrs], float(dt), dp(lam), dp(x),
+                                                C.byref(it)))
+        return x, lam, it.value

@@ -224,6 +224,16 @@ int cdx_pj_solve_csr(cdx_ctx* ctx, int32_t nrows, int32_t nv, int32_t nfl, const
                      const double* restitution, const double* minv, const double* mdiag, const double* v,
                      const double* f_ext, const double* f_gyro, double dt, double alpha, int32_t max_iter,
                      double tol_abs, double tol_rel, double* lambda_inout, double* x_out, int32_t* iterations);
+/* The same solve under a configuration, as ProjectedJacobiSolver reads it (projected_jacobi.cpp:
+ * 451-500): pj.alpha, pj.max_iterations, pj.tol_abs, pj.tol_rel, the loop (pj.nesterov > pj.chebyshev >
+ * pj.anderson > standard, with their parameters), pj.rdiag_true_delassus (per-contact Delassus
+ * blocks; the three rows of a frictional contact must share their columns), gpu.residual_tol and
+ * gpu.check_every. dt is the step of the solve (SolverBase::solve(dt, theta)). */
+int cdx_pj_solve_csr_cfg(cdx_ctx* ctx, const cdx_config* cfg, int32_t nrows, int32_t nv, int32_t nfl,
+                         const int32_t* row_ptr, const int32_t* col, const double* val, const double* contact_bias,
+                         const double* mu, const double* restitution, const double* minv, const double* mdiag,
+                         const double* v, const double* f_ext, const double* f_gyro, double dt, double* lambda_inout,
+                         double* x_out, int32_t* iterations);
 
 /* ---- solver-level solve for callers that cannot allocate device memory ----
  * No counterpart in the reference. Same inputs, outputs and results as cdx_pj_solve_csr, but no

@@ -8,7 +8,8 @@
 //      selected in PhysicsPipeline's solver factory (src/physics/pipeline/physics_pipeline.cpp:34-51).
 //      It pulls the same inputs from DynamicsAssembler (dynamics_assembler.hpp:23-94), applies
 //      and stores the warm start with WarmstartProvider (warmstart.hpp:26-56), and calls
-//      cdx_pj_solve_csr (include/cdx.h) for the sweeps.
+//      cdx_pj_solve_csr_cfg (include/cdx.h) with the reference's pj.* settings (the loop, the
+//      block preconditioner, the tolerances) for the sweeps.
 //  * GpuMoreauIntegrator : cardillo::integration::IntegrationBase
 //      replaces MoreauIntegrator (src/physics/integration/moreau.cpp:6-13) for sphere scenes:
 //      the whole step (collision, contact rows, PJ, drift) runs in cdx_step.
@@ -53,12 +54,26 @@ class GpuProjectedJacobiSolver : public SolverBase {
         VectorXr e = m_dyn.restitutionVec().head(nrows);
         VectorXr x(nv);
         int32_t iters = 0;
-        const int st = cdx_pj_solve_csr(m_ctx, nrows, nv, m_dyn.numFrictionlessContacts(), W.outerIndexPtr(),
-                                        W.innerIndexPtr(), W.valuePtr(), m_dyn.contactVVec().data(),
-                                        m_dyn.muVec().data(), e.data(), m_dyn.MinvDiag().data(), m_dyn.MDiag().data(),
-                                        m_dyn.vVec().data(), m_dyn.fVecExternal().data(), f_gyro.data(), dt,
-                                        m_cfg.pj_alpha, m_cfg.pj_max_iterations, m_cfg.pj_tol_abs, m_cfg.pj_tol_rel,
-                                        p.data(), x.data(), &iters);
+        // the reference's solver settings (config.hpp:79-112)
+        cdx_config c;
+        cdx_config_default(&c);
+        c.pj_alpha = m_cfg.pj_alpha;
+        c.pj_max_iterations = m_cfg.pj_max_iterations;
+        c.pj_tol_abs = m_cfg.pj_tol_abs;
+        c.pj_tol_rel = m_cfg.pj_tol_rel;
+        c.pj_nesterov = m_cfg.pj_nesterov;
+        c.pj_nesterov_beta_threshold = m_cfg.pj_nesterov_beta_threshold;
+        c.pj_nesterov_restart_limit = m_cfg.pj_nesterov_restart_limit;
+        c.pj_chebyshev = m_cfg.pj_chebyshev;
+        c.pj_anderson = m_cfg.pj_anderson;
+        c.pj_anderson_m = m_cfg.pj_anderson_m;
+        c.pj_rdiag_true_delassus = m_cfg.pj_rdiag_true_delassus;
+        c.gpu_check_every = 10;
+        const int st = cdx_pj_solve_csr_cfg(m_ctx, &c, nrows, nv, m_dyn.numFrictionlessContacts(), W.outerIndexPtr(),
+                                            W.innerIndexPtr(), W.valuePtr(), m_dyn.contactVVec().data(),
+                                            m_dyn.muVec().data(), e.data(), m_dyn.MinvDiag().data(),
+                                            m_dyn.MDiag().data(), m_dyn.vVec().data(), m_dyn.fVecExternal().data(),
+                                            f_gyro.data(), dt, p.data(), x.data(), &iters);
         if (st != CDX_OK) throw std::runtime_error(std::string("GpuProjectedJacobiSolver: ") + cdx_last_error(m_ctx));
         m_last_iters = iters;
         WarmstartProvider::storeImpulse(p, m_dyn);

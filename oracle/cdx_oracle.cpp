@@ -1009,6 +1009,23 @@ SolveResult pj_solve_anderson(PJ& P, double* rhs, const double* Mdiag, double* l
     return res;
 }
 
+// loop selection as ProjectedJacobiSolver::solve (projected_jacobi.cpp:470-491): Nesterov, then
+// Chebyshev, then Anderson, then the standard loop
+SolveResult solve_dispatch(PJ& P, const or_config& cfg, double* rhs, const double* Mdiag, double* lam, double* x,
+                           double residual_tol, int omp_all, std::vector<double>* tr) {
+    if (cfg.pj_nesterov)
+        return pj_solve_nesterov(P, rhs, Mdiag, lam, x, cfg.pj_max_iterations, cfg.pj_tol_abs, cfg.pj_tol_rel,
+                                 cfg.pj_nesterov_beta_threshold, cfg.pj_nesterov_restart_limit, omp_all, tr);
+    if (cfg.pj_chebyshev)
+        return pj_solve_chebyshev(P, rhs, Mdiag, lam, x, cfg.pj_max_iterations, cfg.pj_tol_abs, cfg.pj_tol_rel,
+                                  omp_all, tr);
+    if (cfg.pj_anderson)
+        return pj_solve_anderson(P, rhs, Mdiag, lam, x, cfg.pj_max_iterations, cfg.pj_tol_abs, cfg.pj_tol_rel,
+                                 cfg.pj_anderson_m, omp_all, tr);
+    return pj_solve(P, rhs, Mdiag, lam, x, cfg.pj_max_iterations, cfg.pj_tol_abs, cfg.pj_tol_rel, residual_tol, omp_all,
+                    tr);
+}
+
 // MoreauIntegrator::step (src/physics/integration/moreau.cpp:6-13)
 void step_once(Engine& E) {
     const int N = E.N, S = E.S, nv = 6 * N;
@@ -1082,22 +1099,9 @@ void step_once(Engine& E) {
     if (C.empty()) {
         for (int j = 0; j < nv; ++j) x[j] = rhs[j] / E.Mdiag[j];
     } else {
-        // loop selection as ProjectedJacobiSolver::solve (projected_jacobi.cpp:470-491): Nesterov
-        // takes precedence over Chebyshev, then the standard loop
         std::vector<double>* tr = E.trace_on ? &E.trace : nullptr;
-        if (E.cfg.pj_nesterov)
-            sr = pj_solve_nesterov(P, rhs.data(), E.Mdiag.data(), lam.data(), x.data(), E.cfg.pj_max_iterations,
-                                   E.cfg.pj_tol_abs, E.cfg.pj_tol_rel, E.cfg.pj_nesterov_beta_threshold,
-                                   E.cfg.pj_nesterov_restart_limit, omp_all, tr);
-        else if (E.cfg.pj_chebyshev)
-            sr = pj_solve_chebyshev(P, rhs.data(), E.Mdiag.data(), lam.data(), x.data(), E.cfg.pj_max_iterations,
-                                    E.cfg.pj_tol_abs, E.cfg.pj_tol_rel, omp_all, tr);
-        else if (E.cfg.pj_anderson)
-            sr = pj_solve_anderson(P, rhs.data(), E.Mdiag.data(), lam.data(), x.data(), E.cfg.pj_max_iterations,
-                                   E.cfg.pj_tol_abs, E.cfg.pj_tol_rel, E.cfg.pj_anderson_m, omp_all, tr);
-        else
-            sr = pj_solve(P, rhs.data(), E.Mdiag.data(), lam.data(), x.data(), E.cfg.pj_max_iterations,
-                          E.cfg.pj_tol_abs, E.cfg.pj_tol_rel, E.cfg.residual_tol, omp_all, tr);
+        sr = solve_dispatch(P, E.cfg, rhs.data(), E.Mdiag.data(), lam.data(), x.data(), E.cfg.residual_tol, omp_all,
+                            tr);
     }
     E.trace_on = false;
     // storeImpulse (warmstart.hpp:41-56) and the tracker's memory for the next step
@@ -1247,6 +1251,30 @@ int32_t or_pj_solve_csr(int32_t nrows, int32_t nv, int32_t nfl, const int32_t* r
     }
     pj_setup(P, contact_bias, restitution, mu, minv, v, alpha, 0);
     SolveResult r = pj_solve(P, rhs.data(), mdiag, lambda_inout, x_out, max_iter, tol_abs, tol_rel, 0.0, 0, nullptr);
+    return r.iters;
+}
+
+// the solver-level drop-in with the configuration's loop, block preconditioner and stop rules
+int32_t or_pj_solve_csr_cfg(const or_config* cfg, int32_t nrows, int32_t nv, int32_t nfl, const int32_t* row_ptr,
+                            const int32_t* col, const double* val, const double* contact_bias, const double* mu,
+                            const double* restitution, const double* minv, const double* mdiag, const double* v,
+                            const double* f_ext, const double* f_gyro, double dt, double* lambda_inout,
+                            double* x_out) {
+    PJ P;
+    P.nrows = nrows;
+    P.nv = nv;
+    P.nfl = nfl;
+    P.ptr = row_ptr;
+    P.col = col;
+    P.val = val;
+    std::vector<double> rhs(nv);
+    for (int j = 0; j < nv; ++j) rhs[j] = (mdiag[j] * v[j] + dt * f_ext[j]) + dt * f_gyro[j];
+    if (nrows == 0) {
+        for (int j = 0; j < nv; ++j) x_out[j] = rhs[j] / mdiag[j];
+        return 0;
+    }
+    pj_setup(P, contact_bias, restitution, mu, minv, v, cfg->pj_alpha, 0, cfg->pj_rdiag_true_delassus);
+    SolveResult r = solve_dispatch(P, *cfg, rhs.data(), mdiag, lambda_inout, x_out, cfg->residual_tol, 0, nullptr);
     return r.iters;
 }
 

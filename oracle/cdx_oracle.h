@@ -101,6 +101,12 @@ int32_t or_get_trace(void* h, double* out, int64_t max_values);
  * W given as CSR (rows x nv), per-row contact bias, mu (at normal rows), restitution;
  * nfl = number of leading frictionless rows (1 row per contact), the rest are 3-row blocks.
  * x_out = solved velocities, lambda_inout = warm start in / impulses out. Returns iterations. */
+/* the solver-level drop-in with a configuration (loop, block preconditioner, stop rules) */
+int32_t or_pj_solve_csr_cfg(const or_config* cfg, int32_t nrows, int32_t nv, int32_t nfl, const int32_t* row_ptr,
+                            const int32_t* col, const double* val, const double* contact_bias, const double* mu,
+                            const double* restitution, const double* minv, const double* mdiag, const double* v,
+                            const double* f_ext, const double* f_gyro, double dt, double* lambda_inout,
+                            double* x_out);
 /* the Delassus block inverse of pj.rdiag_true_delassus (n <= 3, row-major); returns 1 when the
  * block counts as diagonal, 0 otherwise, -1 for a bad size */
 int32_t or_block_inverse(const double* A, int32_t n, double* X);

@@ -115,6 +115,9 @@ def lib():
             L.or_pj_solve_csr.argtypes = [C.c_int32, C.c_int32, C.c_int32, _PI, _PI, _P, _P, _P, _P, _P, _P,
                                           _P, _P, _P, C.c_double, C.c_double, C.c_int32, C.c_double,
                                           C.c_double, _P, _P]
+            L.or_pj_solve_csr_cfg.restype = C.c_int32
+            L.or_pj_solve_csr_cfg.argtypes = [C.POINTER(OrConfig), C.c_int32, C.c_int32, C.c_int32, _PI, _PI, _P, _P,
+                                              _P, _P, _P, _P, _P, _P, _P, C.c_double, _P, _P]
             L.or_block_inverse.restype = C.c_int32
             L.or_block_inverse.argtypes = [_P, C.c_int32, _P]
             _lib = L
@@ -228,6 +231,24 @@ class Oracle:
         out = np.empty(n)
         self.L.or_get_trace(self.h, _dp(out), n)
         return out.reshape(-1, nrows) if nrows else out
+
+
+def pj_solve_csr_cfg(cfg: dict, row_ptr, col, val, contact_bias, mu, restitution, minv, mdiag, v, f_ext, f_gyro, dt,
+                     lam0, nfl=0):
+    """Oracle for the solver-level drop-in with a configuration (the keys of the engine's config)."""
+    L = lib()
+    c = config_from(cfg)
+    row_ptr = np.ascontiguousarray(row_ptr, np.int32)
+    col = np.ascontiguousarray(col, np.int32)
+    arrs = [np.ascontiguousarray(a, np.float64) for a in (val, contact_bias, mu, restitution, minv, mdiag, v,
+                                                          f_ext, f_gyro)]
+    nrows = row_ptr.shape[0] - 1
+    nv = arrs[4].shape[0]
+    lam = np.array(lam0, np.float64, copy=True)
+    x = np.empty(nv)
+    it = L.or_pj_solve_csr_cfg(C.byref(c), nrows, nv, int(nfl), _ip(row_ptr), _ip(col), *[_dp(a) for a in arrs],
+                               float(dt), _dp(lam), _dp(x))
+    return x, lam, it
 
 
 def pj_solve_csr(row_ptr, col, val, contact_bias, mu, restitution, minv, mdiag, v, f_ext, f_gyro, dt, alpha,

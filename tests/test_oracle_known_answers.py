@@ -10,6 +10,7 @@ import numpy as np
 import pytest
 
 from cardillocxx_gb300.scenes import make_scene
+from tests.csr_cases import csr_problem
 
 G = 9.81
 H = 1e-3
@@ -244,3 +245,24 @@ def test_true_delassus_block_matches_row_scale_for_spheres(oracle_mod):
     assert out[0][1]["num_contacts"] == out[1][1]["num_contacts"] > 0
     np.testing.assert_allclose(out[1][0]["vel"], out[0][0]["vel"], rtol=0, atol=1e-10)
     assert not np.array_equal(out[1][0]["vel"], out[0][0]["vel"])  # different rounding: the key is live
+
+
+def test_csr_with_configuration(oracle_mod):
+    # the solver-level drop-in under the configuration: the plain loop equals the explicit-argument
+    # form bit for bit; every loop reaches the plain loop's fixed point. The Delassus block
+    # preconditioner changes the metric of the cone projection (its blocks are not diagonal here),
+    # so it has a fixed point of its own, which its accelerated loops reach too.
+    p = csr_problem()
+    keys = {"pj.alpha": 0.3, "pj.max_iterations": 60, "pj.tol_abs": 0.0, "pj.tol_rel": 0.0}
+    x0, l0, it0 = oracle_mod.pj_solve_csr(**{k: v for k, v in p.items()}, alpha=0.3, max_iter=60, tol_abs=0.0,
+                                          tol_rel=0.0)
+    x1, l1, it1 = oracle_mod.pj_solve_csr_cfg(keys, **p)
+    assert it0 == it1 == 60 and np.array_equal(x0, x1) and np.array_equal(l0, l1)
+    tight = {"pj.alpha": 0.3, "pj.max_iterations": 50000, "pj.tol_abs": 1e-12, "pj.tol_rel": 1e-11}
+    for base in ({}, {"pj.rdiag_true_delassus": True}):
+        ref, _, it_ref = oracle_mod.pj_solve_csr_cfg(dict(tight, **base), **p)
+        assert it_ref < 50000
+        for extra in ({"pj.nesterov": True}, {"pj.chebyshev": True}, {"pj.anderson": True, "pj.anderson_m": 3}):
+            x, lam, it = oracle_mod.pj_solve_csr_cfg(dict(tight, **base, **extra), **p)
+            assert it < 50000, extra
+            np.testing.assert_allclose(x, ref, rtol=0, atol=1e-7 * np.abs(ref).max(), err_msg=str((base, extra)))

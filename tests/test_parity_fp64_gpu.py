@@ -241,3 +241,24 @@ def test_true_delassus_block_preconditioner(gpu, oracle_mod):
     for extra in ({}, {"pj.chebyshev": True}, {"friction.enable": False}):
         cfg = scenes.config_for("pile_1k", **{"pj.rdiag_true_delassus": True, "friction.combine": "min", **extra})
         run_pair(oracle_mod, s, cfg, 80, 40)
+
+
+def test_csr_dropin_with_configuration(gpu, oracle_mod):
+    # cdx_pj_solve_csr_cfg: the solver-level drop-in under the reference's pj.* settings, bit for bit
+    # against the oracle: every loop, with and without the Delassus block preconditioner. W here is
+    # general (its 3x3 blocks are not diagonal), so the blocks take the Cholesky inverse.
+    from tests.csr_cases import csr_problem
+    p = csr_problem()
+    eng = PhysicsEngine(scenes.config_for("pile_1k"))
+    base = {"pj.alpha": 0.3, "pj.max_iterations": 400, "pj.tol_abs": 1e-9, "pj.tol_rel": 1e-8}
+    for block in (False, True):
+        for extra in ({}, {"pj.nesterov": True}, {"pj.chebyshev": True}, {"pj.anderson": True},
+                      {"pj.anderson": True, "pj.anderson_m": 4},
+                      {"pj.nesterov": True, "pj.nesterov_beta_threshold": 0.5, "pj.nesterov_restart_limit": 3}):
+            cfg = dict(base, **extra, **{"pj.rdiag_true_delassus": block})
+            xo, lo, ito = oracle_mod.pj_solve_csr_cfg(cfg, **p)
+            xg, lg, itg = eng.pj_solve_csr_cfg(cfg, **p)
+            what = f"block={block} {extra}"
+            assert itg == ito, what
+            assert_same(xg, xo, "x " + what)
+            assert_same(lg, lo, "lambda " + what)
