@@ -162,3 +162,21 @@ def test_output_keys(cdxlib):
     assert c.get("output_folder") == b"/tmp/frames" and c.get("output_filename_prefix") == b"drum"
     with pytest.raises(CdxError):
         c.set("output.folder", "x" * 300)
+
+
+def test_reference_adapter_compiles_against_interface_stubs(tmp_path):
+    # include/cdx_reference_adapter.hpp only builds inside the reference tree; against stand-ins of
+    # the reference interfaces it uses (tests/adapter_stub) it must compile, calls into the C ABI
+    # included (syntax only: nothing is linked or run)
+    import os
+    import subprocess
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src = tmp_path / "adapter_tu.cpp"
+    src.write_text('#include "cdx_reference_adapter.hpp"\n'
+                   'static cardillo::solver::SolverBase* make(cardillo::physics::DynamicsAssembler& d, '
+                   'const cardillo::config::Config& c) { return new cardillo::solver::GpuProjectedJacobiSolver(d, c); }\n'
+                   'int main() { (void)&make; return 0; }\n')
+    cmd = ["g++", "-std=c++17", "-fsyntax-only", "-Wall", "-Werror", "-DCDX_WITH_CARDILLO",
+           "-I", os.path.join(root, "include"), "-I", os.path.join(root, "tests", "adapter_stub"), str(src)]
+    p = subprocess.run(cmd, capture_output=True, text=True)
+    assert p.returncode == 0, p.stderr
