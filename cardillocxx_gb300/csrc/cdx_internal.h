@@ -179,7 +179,7 @@ void launch_unpack_state4(const Scene& sc, const double* pos, const double* quat
 void launch_unpack_state(const Scene& sc, const double* in, int mask, cudaStream_t s);
 
 // ---- FP64 plain method (k_fp64.cu) ----
-void launch_rhs64(const Scene& sc, double dt, const double* g, double* rhs, cudaStream_t s);
+void launch_rhs64(const Scene& sc, double dt, const double* g, double* rhs, cudaStream_t s, int implicit_gyro = 0);
 void launch_drift64(const Scene& sc, double h, int compute_R, cudaStream_t s);
 void launch_static_flags64(const Scene& sc, double margin, int32_t* flags, cudaStream_t s);
 void launch_pair_count64(const Scene& sc, const Grid& g, const uint32_t* cell_body, const int32_t* cell_start,

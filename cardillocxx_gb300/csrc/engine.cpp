@@ -79,7 +79,6 @@ Engine::~Engine() {
 int Engine::init(const cdx_config& c) {
     cfg = c;
     if (cfg.output_interval_steps > 0) out = new cdx::Output(cfg);
-    if (cfg.moreau_implicit_gyroscopy) return fail(CDX_ERR_UNSUPPORTED, "moreau.implicit_gyroscopy=on is not supported");
     if (cfg.solver_type != 0) return fail(CDX_ERR_UNSUPPORTED, "only solver.type=projected_jacobi is on this path");
     int st = cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
     if (st) return st;
@@ -704,7 +703,7 @@ int Engine::step64() {
     const double dt = cfg.sim_dt, th = cfg.moreau_theta;
     int st;
     if (timing) cudaEventRecord(ev[0], stream);
-    launch_rhs64(sc, dt, cfg.sim_gravity, rhs, stream);
+    launch_rhs64(sc, dt, cfg.sim_gravity, rhs, stream, cfg.moreau_implicit_gyroscopy);
     launch_drift64(sc, (1.0 - th) * dt, 1, stream);
     launches += 2;
     if ((st = collide64())) return st;

@@ -185,7 +185,9 @@ __device__ __forceinline__ void write_contact(const Scene& sc, Contacts& C, int 
     C.flags[c] = (friction_enable && mu > 0.0) ? CF_FRICTIONAL : 0;
 }
 
-__global__ void k_rhs64(Scene sc, double dt, double g0, double g1, double g2, double* rhs) {
+// PjAssembler::rhs (pj_assembler.cpp:127-153); implicit_gyro leaves dt f_gyro out (for isotropic
+// spheres the implicit gyroscopic block of S is exactly zero)
+__global__ void k_rhs64(Scene sc, double dt, double g0, double g1, double g2, double* rhs, int implicit_gyro) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= sc.N) return;
     const int N = sc.N;
@@ -201,7 +203,7 @@ __global__ void k_rhs64(Scene sc, double dt, double g0, double g1, double g2, do
     for (int k = 0; k < 3; ++k) {
         const double fext = m * g[k];
         rhs[(size_t)k * N + i] = (Ml * v[k] + dt * fext) + dt * 0.0;
-        rhs[(size_t)(3 + k) * N + i] = (Ma * w[k] + dt * 0.0) + dt * (-c[k]);
+        rhs[(size_t)(3 + k) * N + i] = implicit_gyro ? (Ma * w[k] + dt * 0.0) : (Ma * w[k] + dt * 0.0) + dt * (-c[k]);
     }
 }
 
@@ -1274,9 +1276,9 @@ __global__ void k_trace64(Contacts C, int gen, int nc, const int32_t* fl_scan, c
 
 }  // namespace
 
-void launch_rhs64(const Scene& sc, double dt, const double* g, double* rhs, cudaStream_t s) {
+void launch_rhs64(const Scene& sc, double dt, const double* g, double* rhs, cudaStream_t s, int implicit_gyro) {
     if (sc.N == 0) return;
-    k_rhs64<<<nblk(sc.N), NT, 0, s>>>(sc, dt, g[0], g[1], g[2], rhs);
+    k_rhs64<<<nblk(sc.N), NT, 0, s>>>(sc, dt, g[0], g[1], g[2], rhs, implicit_gyro);
 }
 void launch_drift64(const Scene& sc, double h, int compute_R, cudaStream_t s) {
     if (sc.N + sc.S == 0) return;

@@ -112,7 +112,8 @@ __device__ __forceinline__ void drift_fast(double* x, double* q, const double* v
 }
 
 // ------------------------------------------------------------------ per-body preparation (FP64)
-__global__ void k_s_prep(Scene sc, SplitBuf sb, double dt, double g0, double g1, double g2, double h1) {
+__global__ void k_s_prep(Scene sc, SplitBuf sb, double dt, double g0, double g1, double g2, double h1,
+                         int implicit_gyro) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < sc.N) {
         const int N = sc.N;
@@ -130,7 +131,7 @@ __global__ void k_s_prep(Scene sc, SplitBuf sb, double dt, double g0, double g1,
         double vf[3], wf[3];
         for (int k = 0; k < 3; ++k) {
             vf[k] = v[k] + dt * g[k];
-            wf[k] = w[k] + dt * ia * (-c[k]);
+            wf[k] = implicit_gyro ? w[k] : w[k] + dt * ia * (-c[k]);
         }
         drift_fast(x, q, v, w, h1);
         sc.bf(BF_PX)[i] = x[0]; sc.bf(BF_PY)[i] = x[1]; sc.bf(BF_PZ)[i] = x[2];
@@ -1572,9 +1573,10 @@ int launch_s_solve_coop(const SplitBuf& sb, int gen, float alpha, int v, const C
     return (int)cudaLaunchCooperativeKernel((const void*)cv.kernel, dim3(p.grid), dim3(cv.nth), args, (size_t)p.smem, s);
 }
 
-void launch_s_prep(const Scene& sc, const SplitBuf& sb, double dt, const double* g, double h1, cudaStream_t s) {
+void launch_s_prep(const Scene& sc, const SplitBuf& sb, double dt, const double* g, double h1, cudaStream_t s,
+                   int implicit_gyro) {
     if (sc.N + sc.S == 0) return;
-    k_s_prep<<<nblk(sc.N + sc.S), NT, 0, s>>>(sc, sb, dt, g[0], g[1], g[2], h1);
+    k_s_prep<<<nblk(sc.N + sc.S), NT, 0, s>>>(sc, sb, dt, g[0], g[1], g[2], h1, implicit_gyro);
 }
 void launch_s_static_flags(const Scene& sc, const SplitBuf& sb, float margin, int32_t* flags, cudaStream_t s) {
     if (sc.N == 0) return;

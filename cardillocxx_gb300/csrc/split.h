@@ -116,7 +116,8 @@ bool split_coop_plan(int v, int64_t nc, int64_t nbodies, int sms, CoopPlan* p);
 // stop rule every check_every sweeps; returns the cudaError_t of the launch
 int launch_s_solve_coop(const SplitBuf& sb, int gen, float alpha, int v, const CoopPlan& p, int max_iter, float tol,
                         int max_sweeps, int check_every, cudaStream_t s);
-void launch_s_prep(const Scene& sc, const SplitBuf& sb, double dt, const double* g, double h1, cudaStream_t s);
+void launch_s_prep(const Scene& sc, const SplitBuf& sb, double dt, const double* g, double h1, cudaStream_t s,
+                   int implicit_gyro = 0);
 void launch_s_static_flags(const Scene& sc, const SplitBuf& sb, float margin, int32_t* flags, cudaStream_t s);
 // cell_body / cell_key: the bodies and their cell keys sorted by cell
 void launch_s_pair_count(const Scene& sc, const Grid& g, const SplitBuf& sb, const uint32_t* cell_body,

@@ -47,7 +47,8 @@ typedef struct cdx_config {
     double sim_T;                     /* sim.T */
     double sim_gravity[3];            /* sim.gravity */
     double moreau_theta;              /* moreau.theta (0.5 = midpoint) */
-    int32_t moreau_implicit_gyroscopy;/* moreau.implicit_gyroscopy (only 0 is supported) */
+    int32_t moreau_implicit_gyroscopy;/* moreau.implicit_gyroscopy: for isotropic spheres the linearised
+                                         gyroscopic block is exactly zero, so this only drops dt f_gyro */
     int32_t friction_enable;          /* friction.enable */
     int32_t friction_combine;         /* friction.combine: 0 min, 1 arith, 2 geom */
     double friction_default_mu;       /* friction.default_mu (scene generators) */

@@ -1031,7 +1031,11 @@ void step_once(Engine& E) {
     const int N = E.N, S = E.S, nv = 6 * N;
     const double dt = E.cfg.sim_dt, th = E.cfg.moreau_theta;
     const int omp_all = E.cfg.omp_mode == 1;
-    // refreshState: f_ext = m g, f_gyro = -w x (I w)  (world.cpp:113-173); rhs (pj_assembler.cpp:152-153)
+    // refreshState: f_ext = m g, f_gyro = -w x (I w)  (world.cpp:113-173); rhs (pj_assembler.cpp:152-153).
+    // With moreau.implicit_gyroscopy the rhs leaves dt f_gyro out and S gains -dt G_rot with
+    // G_rot = (([I w]x - [w]x I) / 2 (pj_assembler.cpp:32-61); for an isotropic I every entry of
+    // G_rot is i w_k - w_k i = 0 exactly, so S stays diag(M).
+    const bool implicit_gyro = E.cfg.moreau_implicit_gyroscopy != 0;
     std::vector<double> rhs(nv), vn(nv);
     for (int i = 0; i < N; ++i) {
         const double* w = &E.w[3 * (size_t)i];
@@ -1043,7 +1047,7 @@ void step_once(Engine& E) {
             const double Ml = E.Mdiag[6 * i + k];
             rhs[6 * i + k] = (Ml * E.v[3 * (size_t)i + k] + dt * fext) + dt * 0.0;
             const double Ma = E.Mdiag[6 * i + 3 + k];
-            rhs[6 * i + 3 + k] = (Ma * w[k] + dt * 0.0) + dt * (-c[k]);
+            rhs[6 * i + 3 + k] = implicit_gyro ? (Ma * w[k] + dt * 0.0) : (Ma * w[k] + dt * 0.0) + dt * (-c[k]);
             vn[6 * i + k] = E.v[3 * (size_t)i + k];
             vn[6 * i + 3 + k] = w[k];
         }

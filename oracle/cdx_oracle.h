@@ -46,6 +46,7 @@ typedef struct or_config {
     int32_t pj_anderson;                 /* pj.anderson */
     int32_t pj_anderson_m;               /* pj.anderson_m */
     int32_t pj_rdiag_true_delassus;      /* pj.rdiag_true_delassus */
+    int32_t moreau_implicit_gyroscopy;   /* moreau.implicit_gyroscopy */
 } or_config;
 
 typedef struct or_scene {

@@ -62,6 +62,7 @@ class OrConfig(C.Structure):
         ("pj_anderson", C.c_int32),
         ("pj_anderson_m", C.c_int32),
         ("pj_rdiag_true_delassus", C.c_int32),
+        ("moreau_implicit_gyroscopy", C.c_int32),
     ]
 
 
@@ -168,6 +169,7 @@ def config_from(cfg: dict, omp_mode: int = 0, num_threads: int = 0) -> OrConfig:
     c.pj_anderson = int(bool(cfg.get("pj.anderson", False)))
     c.pj_anderson_m = int(cfg.get("pj.anderson_m", 2))
     c.pj_rdiag_true_delassus = int(bool(cfg.get("pj.rdiag_true_delassus", False)))
+    c.moreau_implicit_gyroscopy = int(bool(cfg.get("moreau.implicit_gyroscopy", False)))
     c.omp_mode = omp_mode
     c.num_threads = num_threads
     return c

@@ -266,3 +266,17 @@ def test_csr_with_configuration(oracle_mod):
             x, lam, it = oracle_mod.pj_solve_csr_cfg(dict(tight, **base, **extra), **p)
             assert it < 50000, extra
             np.testing.assert_allclose(x, ref, rtol=0, atol=1e-7 * np.abs(ref).max(), err_msg=str((base, extra)))
+
+
+def test_implicit_gyroscopy_drops_the_gyroscopic_force(oracle_mod):
+    # moreau.implicit_gyroscopy (pj_assembler.cpp:32-61, 152-153): for isotropic spheres the
+    # linearised gyroscopic block of S is exactly zero, so only dt f_gyro leaves the right-hand side.
+    # A spinning sphere in free flight keeps its body-frame spin exactly; the explicit form differs
+    # from that by the rounding of w x (I w) only
+    s = make_scene([{"pos": (0.0, 0.0, 1.0), "radius": 0.05, "omega": (3.0, -7.0, 11.0)}], [GROUND])
+    o_imp = oracle_mod.Oracle(s, cfg(**{"moreau.implicit_gyroscopy": True}))
+    o_imp.step(20)
+    assert np.array_equal(o_imp.state()["omega"][0], [3.0, -7.0, 11.0])
+    o_exp = oracle_mod.Oracle(s, cfg())
+    o_exp.step(20)
+    np.testing.assert_allclose(o_exp.state()["omega"][0], [3.0, -7.0, 11.0], rtol=1e-12)

@@ -262,3 +262,17 @@ def test_csr_dropin_with_configuration(gpu, oracle_mod):
             assert itg == ito, what
             assert_same(xg, xo, "x " + what)
             assert_same(lg, lo, "lambda " + what)
+
+
+def test_implicit_gyroscopy_parity(gpu, oracle_mod):
+    # moreau.implicit_gyroscopy: spinning spheres, bit for bit against the oracle; the split form
+    # follows the plain method to FP32 order
+    s = scenes.generate("pile_1k", scale=0.15)
+    s["omega"] = np.random.default_rng(3).normal(size=s["omega"].shape) * 20.0
+    cfg = scenes.config_for("pile_1k", **{"moreau.implicit_gyroscopy": True})
+    run_pair(oracle_mod, s, cfg, 60, 30)
+    e32 = PhysicsEngine(dict(cfg, **{"gpu.precision": "split"})).load_scene(s)
+    e32.step(60)
+    e64 = PhysicsEngine(cfg).load_scene(s)
+    e64.step(60)
+    np.testing.assert_allclose(e32.state()["pos"], e64.state()["pos"], rtol=0, atol=1e-5)
