@@ -104,6 +104,7 @@ int cdx_config_default(cdx_config* c) {
     // frames are off unless asked for (the reference writes every 50 steps by default)
     c->output_interval_steps = 0;
     c->output_write_contact_manifolds = 1;
+    c->gpu_coop_smem_contacts = 0;
     std::snprintf(c->output_folder, sizeof(c->output_folder), "%s", "./vtk_out");
     std::snprintf(c->output_filename_prefix, sizeof(c->output_filename_prefix), "%s", "scene");
     return CDX_OK;
@@ -185,6 +186,8 @@ int cdx_config_set(cdx_config* c, const char* key_c, const char* val_c) {
         c->gpu_autotune = as_bool(val);
     } else if (key == "gpu.sweep_variant") {
         if (as_int(val, &i)) c->gpu_sweep_variant = std::max(-1, i);
+    } else if (key == "gpu.coop_smem_contacts") {
+        if (as_int(val, &i)) c->gpu_coop_smem_contacts = std::max(0, i);
     } else if (key == "gpu.sync_counts") {
         c->gpu_sync_counts = as_bool(val);
     } else if (key_is(key, "pj.nesterov")) {

@@ -268,7 +268,7 @@ int Engine::step_split() {
         for (int v = 0; v < split_num_variants(); ++v) {
             CoopPlan probe;
             if (split_variant_is_coop(v))
-                sweeps += split_coop_plan(v, n, sc.N, S->sms, &probe) ? 8 : 0;
+                sweeps += split_coop_plan(v, n, sc.N, S->sms, &probe, cfg.gpu_coop_smem_contacts) ? 8 : 0;
             else if (!split_variant_is_scenes(v))
                 sweeps += 2;
         }
@@ -298,8 +298,8 @@ int Engine::step_split() {
         if (!split_variant_is_coop(S->variant)) {
             use_graph = false;
         } else if (!(S->gplan_ok && (int64_t)S->gplan.cpb * S->gplan.grid >= est)) {
-            S->gplan_ok = split_coop_plan(S->variant, est + est / 4, sc.N, S->sms, &S->gplan) ||
-                          split_coop_plan(S->variant, est, sc.N, S->sms, &S->gplan);
+            S->gplan_ok = split_coop_plan(S->variant, est + est / 4, sc.N, S->sms, &S->gplan, cfg.gpu_coop_smem_contacts) ||
+                          split_coop_plan(S->variant, est, sc.N, S->sms, &S->gplan, cfg.gpu_coop_smem_contacts);
             if (!S->gplan_ok) use_graph = false;
         }
     }
@@ -460,7 +460,7 @@ int Engine::step_split() {
     for (int v = 0; v < nv; ++v) {
         CoopPlan probe;
         if (split_variant_is_coop(v))
-            tune_sweeps += (S->nc > 0 && split_coop_plan(v, S->nc, sc.N, S->sms, &probe)) ? 8 : 0;
+            tune_sweeps += (S->nc > 0 && split_coop_plan(v, S->nc, sc.N, S->sms, &probe, cfg.gpu_coop_smem_contacts)) ? 8 : 0;
         else if (!split_variant_is_scenes(v))
             tune_sweeps += 2;
     }
@@ -482,7 +482,7 @@ int Engine::step_split() {
                 // two launches of 2 and 6 sweeps: their difference is the cost of a sweep, the rest
                 // (loading and storing the contacts) is paid once per solve of maxit sweeps
                 CoopPlan plan;
-                if (!split_coop_plan(v, S->nc, sc.N, S->sms, &plan)) continue;
+                if (!split_coop_plan(v, S->nc, sc.N, S->sms, &plan, cfg.gpu_coop_smem_contacts)) continue;
                 float ms[2] = {0.f, 0.f};
                 const int ks[2] = {2, 6};
                 for (int r = 0; r < 2; ++r) {
@@ -529,7 +529,7 @@ int Engine::step_split() {
     const int64_t plan_nc = async ? (int64_t)S->nc + S->nc / 16 + 64 : (int64_t)S->nc;
     if (capturing && !scenes && split_variant_is_coop(S->variant)) plan = S->gplan;
     coop = !scenes && S->nc > 0 && split_variant_is_coop(S->variant) &&
-           (capturing ? S->gplan_ok : split_coop_plan(S->variant, plan_nc, sc.N, S->sms, &plan));
+           (capturing ? S->gplan_ok : split_coop_plan(S->variant, plan_nc, sc.N, S->sms, &plan, cfg.gpu_coop_smem_contacts));
     if (S->nc > 0 && !solved && coop) {
         st = launch_s_solve_coop(sb, gen, (float)cfg.pj_alpha, S->variant, plan, maxit, (float)cfg.gpu_residual_tol,
                                  maxit, cfg.gpu_check_every, stream);
@@ -731,7 +731,7 @@ int Engine::time_sweeps(int n, double* msc, double* msb, double* bc, double* bb)
         cudaMemcpyAsync(S->sb.nc_dev, S->h_nc, sizeof(int32_t), cudaMemcpyHostToDevice, stream);
         launch_s_reset(S->sb, stream);
         CoopPlan plan;
-        if (split_variant_is_coop(S->variant) && split_coop_plan(S->variant, S->prev_count, sc.N, S->sms, &plan)) {
+        if (split_variant_is_coop(S->variant) && split_coop_plan(S->variant, S->prev_count, sc.N, S->sms, &plan, cfg.gpu_coop_smem_contacts)) {
             // one cooperative launch of n sweeps; reported per sweep
             cudaEventRecord(e[0], stream);
             st = launch_s_solve_coop(S->sb, g, (float)cfg.pj_alpha, S->variant, plan, 1 << 30, 0.f, n,

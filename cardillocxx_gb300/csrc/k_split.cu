@@ -858,7 +858,10 @@ __device__ __forceinline__ bool grid_wait_max(unsigned* ctr, float2* recs, unsig
 // k - 1 (its last reader) before this barrier's previous one let anybody through, and the first
 // sweep to add into it again (k + 2) starts only after this block arrives at the next barrier.
 // Block 0 records the iteration count for the host.
-template <int NTH, int UNROLL, int AGG>
+// HYB: a block's range may hold more contacts than its shared memory (cpb); the first cpb stay in
+// shared memory and the rest are read from memory every sweep (records through the read-only
+// path, impulses through L2), so problems of any size run as one launch.
+template <int NTH, int UNROLL, int AGG, int HYB>
 __global__ void __launch_bounds__(NTH, 1) k_s_solve_coop(SplitBuf sb, int gen, float alpha, int max_iter, float tol,
                                                          int cpb, int bpb, int vf_smem, int max_sweeps,
                                                          int check_every) {
@@ -872,7 +875,7 @@ __global__ void __launch_bounds__(NTH, 1) k_s_solve_coop(SplitBuf sb, int gen, f
     const int it0 = *(volatile int32_t*)&ss->iters;
     unsigned epoch = *(volatile unsigned*)&ss->bar_base;
     const int nc = *sb.nc_dev, N = sb.N, tid = threadIdx.x;
-    if ((int64_t)nc > (int64_t)cpb * gridDim.x) {
+    if (!HYB && (int64_t)nc > (int64_t)cpb * gridDim.x) {
         // planned from an estimate of the contact count that fell short: every block returns (no
         // barrier has been entered) and the host redoes the step with a plan from the true count
         if (blockIdx.x == 0 && tid == 0) ss->err = 4;
@@ -884,8 +887,9 @@ __global__ void __launch_bounds__(NTH, 1) k_s_solve_coop(SplitBuf sb, int gen, f
     const int ncb = max(0, min(nc - cb, cpe));
     const int bb = blockIdx.x * bpb;
     const int nbb = max(0, min(N - bb, bpb));
+    const int ncs = HYB ? min(ncb, cpb) : ncb;  // contacts kept in shared memory
     float4* __restrict__ lamg = sb.lam[gen];
-    for (int i = tid; i < ncb; i += NTH) {
+    for (int i = tid; i < ncs; i += NTH) {
         const float4 r0 = ldg4(&sb.rec0[cb + i]), r1 = ldg4(&sb.rec1[cb + i]), l = lamg[cb + i];
         s_q0[i] = r0;
         s_q1[i] = r1;
@@ -910,9 +914,15 @@ __global__ void __launch_bounds__(NTH, 1) k_s_solve_coop(SplitBuf sb, int gen, f
                 const int i = base + u * NTH + tid;
                 ok[u] = i < ncb;
                 if (ok[u]) {
-                    q0[u] = s_q0[i];
-                    q1[u] = s_q1[i];
-                    l[u] = s_l[i];
+                    if (!HYB || i < ncs) {
+                        q0[u] = s_q0[i];
+                        q1[u] = s_q1[i];
+                        l[u] = s_l[i];
+                    } else {
+                        q0[u] = ldg4(&sb.rec0[cb + i]);
+                        q1[u] = ldg4(&sb.rec1[cb + i]);
+                        l[u] = __ldcg(&lamg[cb + i]);
+                    }
                 }
             }
             float4 vb[UNROLL], wb[UNROLL], va[UNROLL], wa[UNROLL];
@@ -937,7 +947,10 @@ __global__ void __launch_bounds__(NTH, 1) k_s_solve_coop(SplitBuf sb, int gen, f
                     a = __float_as_int(q1[u].z);
                     b = __float_as_int(q1[u].w);
                     pj_contact(q0[u], q1[u], l[u], va[u], wa[u], vb[u], wb[u], &sb.bias[cb + i], alpha, o);
-                    s_l[i] = o.lam;
+                    if (!HYB || i < ncs)
+                        s_l[i] = o.lam;
+                    else
+                        __stcg(&lamg[cb + i], o.lam);
                     maxd2 = fmaxf(maxd2, o.dn2);
                     maxl = fmaxf(maxl, o.lm);
                 }
@@ -964,7 +977,7 @@ __global__ void __launch_bounds__(NTH, 1) k_s_solve_coop(SplitBuf sb, int gen, f
             }
         }
     }
-    for (int i = tid; i < ncb; i += NTH) lamg[cb + i] = s_l[i];
+    for (int i = tid; i < ncs; i += NTH) lamg[cb + i] = s_l[i];
     // every block has read the scalars by now (it passed a barrier with all of them)
     if (blockIdx.x == 0 && tid == 0) {
         ss->iters = it;
@@ -1441,13 +1454,14 @@ constexpr int N_STREAM = sizeof(g_stream) / sizeof(g_stream[0]);
 // Cooperative solves (one launch for all sweeps): threads per block and contacts per thread per pass.
 struct CoopVariant {
     void (*kernel)(SplitBuf, int, float, int, float, int, int, int, int, int);
-    int nth, unroll, agg;
+    int nth, unroll, agg, hyb;
     int per_sm;    // resident blocks per SM with the full shared-memory budget (0 = not queried)
     int smem_max;  // dynamic shared memory budget of one block
 };
 static CoopVariant g_coop[] = {
-    {k_s_solve_coop<1024, 1, 2>, 1024, 1, 2, 0, 0},
-    {k_s_solve_coop<512, 2, 2>, 512, 2, 2, 0, 0},
+    {k_s_solve_coop<1024, 1, 2, 0>, 1024, 1, 2, 0, 0, 0},
+    {k_s_solve_coop<512, 2, 2, 0>, 512, 2, 2, 0, 0, 0},
+    {k_s_solve_coop<1024, 1, 2, 1>, 1024, 1, 2, 1, 0, 0},
 };
 constexpr int N_COOP = sizeof(g_coop) / sizeof(g_coop[0]);
 
@@ -1480,7 +1494,8 @@ const char* split_variant_name(int v) {
             snprintf(names[v], sizeof(names[v]), "sweep-u%d-t%d-b%d-g%d", cv.unroll, cv.nth, cv.minb, cv.agg);
         } else if (v < N_STREAM + N_COOP) {
             const CoopVariant& cv = g_coop[v - N_STREAM];
-            snprintf(names[v], sizeof(names[v]), "coop-t%d-u%d-g%d", cv.nth, cv.unroll, cv.agg);
+            snprintf(names[v], sizeof(names[v]), cv.hyb ? "coop-hyb-t%d-u%d-g%d" : "coop-t%d-u%d-g%d", cv.nth,
+                     cv.unroll, cv.agg);
         } else {
             const ScenesVariant& cv = g_scenes[v - N_STREAM - N_COOP];
             snprintf(names[v], sizeof(names[v]), "scenes-t%d-u%d-c%d", cv.nth, cv.unroll, cv.csm);
@@ -1528,7 +1543,7 @@ int split_contact_blocks(int vi, int64_t n, int sms) {
 // Partition of a cooperative solve: one block per SM (all resident), contiguous contact and body
 // ranges per block. Feasible when a block's contacts (48 B each) fit in its shared memory; its free
 // velocities (32 B a body) are kept there too when they also fit.
-bool split_coop_plan(int v, int64_t nc, int64_t nbodies, int sms, CoopPlan* p) {
+bool split_coop_plan(int v, int64_t nc, int64_t nbodies, int sms, CoopPlan* p, int smem_contacts) {
     if (!split_variant_is_coop(v) || nc <= 0) return false;
     CoopVariant& cv = g_coop[v - N_STREAM];
     if (cv.per_sm == 0) {
@@ -1548,10 +1563,19 @@ bool split_coop_plan(int v, int64_t nc, int64_t nbodies, int sms, CoopPlan* p) {
     if (cv.per_sm < 1) return false;
     const int64_t grid = (int64_t)sms * cv.per_sm;
     if (grid > COOP_MAX_GRID) return false;
-    const int64_t cpb = (nc + grid - 1) / grid;
+    int64_t cpb = (nc + grid - 1) / grid;
     const int64_t bpb = (nbodies + grid - 1) / grid;
+    // contacts a block keeps in shared memory: all that fit, or gpu.coop_smem_contacts
+    int64_t fit = cv.smem_max / 48;
+    if (smem_contacts > 0) fit = std::min<int64_t>(fit, smem_contacts);
+    if (cv.hyb) {
+        if (cpb <= fit) return false;  // it all fits: the plain cooperative shapes cover it
+        cpb = fit;
+    } else if (cpb > fit) {
+        return false;
+    }
     const int64_t need = cpb * 48;
-    if (need > cv.smem_max) return false;
+    if (need > cv.smem_max || cpb < 1) return false;
     const bool vf = need + bpb * 32 <= cv.smem_max;
     p->grid = (int)grid;
     p->nth = cv.nth;

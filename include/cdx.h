@@ -87,6 +87,8 @@ typedef struct cdx_config {
     int32_t output_write_contact_manifolds; /* output.write_contact_manifolds */
     char output_folder[256];                /* output.folder */
     char output_filename_prefix[128];       /* output.filename_prefix */
+    int32_t gpu_coop_smem_contacts;         /* gpu.coop_smem_contacts: cap on the contacts a block of the
+                                               cooperative solve keeps in shared memory (0 = all that fit) */
 } cdx_config;
 
 /* Scene: dynamic spheres plus static shapes (halfspaces, drums). Bodies of one scene are

@@ -100,7 +100,9 @@ def test_split_every_sweep_shape_computes_the_same_sweep(gpu):
     assert len(names) >= 2
     out = []
     for v in range(len(names)):
-        e = PhysicsEngine(dict(c, **{"gpu.sweep_variant": v})).load_scene(s)
+        # the hybrid cooperative shape runs when a block's contacts exceed its shared-memory cap
+        cap = {"gpu.coop_smem_contacts": 1} if "hyb" in names[v] else {}
+        e = PhysicsEngine(dict(c, **{"gpu.sweep_variant": v}, **cap)).load_scene(s)
         e.set_state(st["pos"], st["quat"], st["vel"], st["omega"])
         e.step(1)
         # the per-scene shapes apply to a single scene too (it fits one block)
@@ -315,3 +317,31 @@ def test_per_scene_solver_on_overflowing_device_counted_steps(gpu):
     assert a.stats()["num_contacts"] > 1024  # more than the 1,024 slots it started with
     assert a.stats()["contact_variant"] == v
     np.testing.assert_allclose(za, zb, rtol=0, atol=2e-3)
+
+
+def test_hybrid_cooperative_solve_streams_what_shared_memory_cannot_hold(gpu):
+    # a cap on the contacts a block keeps in shared memory: the plain cooperative shape no longer
+    # fits and falls back to streaming; the hybrid shape keeps the first contacts of every block in
+    # shared memory and reads the rest every sweep, in one launch. Same sweeps, FP32 order apart.
+    s = scenes.generate("pile_1k")
+    base = scenes.config_for("pile_1k")
+    ref = PhysicsEngine(base).load_scene(s)
+    ref.step(300)
+    st = ref.state()
+    names = PhysicsEngine.split_variants()
+    c = dict(base, **{"gpu.precision": "split", "pj.warmstart": False, "pj.max_iterations": 100,
+                      "gpu.coop_smem_contacts": 4})
+    out = {}
+    for name in ("coop-t1024-u1-g2", "coop-hyb-t1024-u1-g2", "sweep-u1-t256-b4-g2"):
+        e = PhysicsEngine(dict(c, **{"gpu.sweep_variant": names.index(name)})).load_scene(s)
+        e.set_state(st["pos"], st["quat"], st["vel"], st["omega"])
+        e.step(1)
+        out[name] = (e.stats(), e.contacts()["lambda"], e.state()["vel"])
+    assert out["coop-t1024-u1-g2"][0]["contact_variant"] == names.index("sweep-u1-t256-b4-g2")  # did not fit
+    assert out["coop-hyb-t1024-u1-g2"][0]["contact_variant"] == names.index("coop-hyb-t1024-u1-g2")
+    assert out["coop-hyb-t1024-u1-g2"][0]["num_contacts"] > 4 * 152  # more than the cap holds
+    lam0, vel0 = out["sweep-u1-t256-b4-g2"][1:]
+    lam1, vel1 = out["coop-hyb-t1024-u1-g2"][1:]
+    assert np.abs(lam1 - lam0).max() <= 1e-3 * np.abs(lam0).max()
+    vscale = np.abs(st["vel"]).max() + G * H
+    assert np.abs(vel1 - vel0).max() <= 1e-3 * vscale
