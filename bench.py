@@ -246,7 +246,7 @@ def run_cdx(a, log):
     # streaming sweep kernel (one launch per sweep), whichever shape the autotuner chose
     from cardillocxx_gb300 import PhysicsEngine
     names = PhysicsEngine.split_variants()
-    cv = est.get("contact_variant", -1)
+    cv = est.get("sweep_variant", -1)
     vname = names[cv] if a.precision == "split" and 0 <= cv < len(names) else None
     if a.precision != "split":
         kernel, per, units = "k_sweep_contact64", "contact", contacts[-1]

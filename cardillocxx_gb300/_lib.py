@@ -109,6 +109,7 @@ class CdxStats(C.Structure):
         ("autotune_runs", C.c_int32),
         ("redone_steps", C.c_int32),
         ("graph_steps", C.c_int64),
+        ("sweep_variant", C.c_int32),
     ]
 
 

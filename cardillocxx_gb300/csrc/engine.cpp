@@ -945,6 +945,7 @@ void Engine::fill_stats(cdx_stats* s) {
     s->autotune_runs = split_tune_runs();
     s->redone_steps = split_redos();
     s->graph_steps = split_graph_steps();
+    s->sweep_variant = split_sweep_variant();
 }
 
 double Engine::solve_bytes_per_iter() const {

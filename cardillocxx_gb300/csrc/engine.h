@@ -124,6 +124,7 @@ struct Engine {
     int get_contacts_split(int32_t* ia, int32_t* ib, double* point, double* lambda, double* normal, int32_t* count);
     double split_bytes_per_iter() const;
     int split_variant() const;
+    int split_sweep_variant() const;
     int split_tune_runs() const;
     int split_redos() const;
     int64_t split_graph_steps() const;

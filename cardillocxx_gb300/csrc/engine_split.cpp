@@ -42,6 +42,7 @@ struct SplitState {
     int scene_nbmax = 0;             // bodies of the largest scene
     int scene_best = -1;             // the fastest scenes shape once tuned (-2: the regular solver)
     int scene_tried = 0;
+    int64_t scene_tuned_at = 0;      // contact count when the scenes shapes were last timed
     double scene_ms[16] = {0};
     int scene_timing = -1;           // shape timed in the current step
     // steps that find their contact totals on the device: a snapshot of the state they change, so
@@ -135,7 +136,8 @@ static int split_contacts(Engine& E, int64_t need) {
 static int init_split(Engine& E) {
     E.split = new SplitState();
     SplitState* S = E.split;
-    if (E.cfg.gpu_sweep_variant >= 0) S->variant = std::min(E.cfg.gpu_sweep_variant, split_num_variants() - 1);
+    S->variant = E.cfg.gpu_sweep_variant >= 0 ? std::min(E.cfg.gpu_sweep_variant, split_num_variants() - 1)
+                                              : split_first_coop_variant();
     SplitBuf& b = S->sb;
     const int N = E.sc.N, Ss = E.sc.S, nsc = E.sc.nscenes;
     b.N = N;
@@ -277,6 +279,13 @@ int Engine::step_split() {
     // the per-scene kernel (one block a scene, its bodies in shared memory) is a candidate for
     // batches and for a single scene small enough for one block
     const bool scene_fit = S->scene_nbmax > 0 && S->scene_nbmax <= 3584;
+    // shapes timed while the scenes had few contacts (a pile that is still falling) say little about
+    // the settled problem: time them again once the count has grown by half
+    if (scene_fit && pinned < 0 && cfg.gpu_autotune && S->scene_best != -1 && S->prev_count >= 64 &&
+        (double)S->prev_count >= 1.5 * (double)S->scene_tuned_at) {
+        S->scene_best = -1;
+        S->scene_tried = 0;
+    }
     const bool scene_tuning = scene_fit && pinned < 0 && S->scene_best == -1 && cfg.gpu_autotune;
     const bool async = !cfg.gpu_sync_counts && S->prev_count > 0 && sb.cap > 0 && !S->force_sync && !scene_tuning &&
                        !tune_due(S->prev_count);
@@ -449,7 +458,6 @@ int Engine::step_split() {
                                    nflag > 0 ? spos : nullptr, nflag > 0 ? sflags : nullptr, poff, S->scene_order,
                                    S->scene_nbmax, stream);
         if ((st = cuda_check((cudaError_t)st, "scenes solve"))) return st;
-        S->variant = scene_v;
         S->last_variant = scene_v;
         ++launches;
         solved = true;
@@ -644,6 +652,7 @@ step_issued:
             for (int q = 1; q <= nsv + 1; ++q)
                 if (q != nsv && S->scene_ms[q] < S->scene_ms[best]) best = q;
             S->scene_best = best < nsv ? split_first_scenes_variant() + best : -2;
+            S->scene_tuned_at = std::max<int64_t>(S->nc, 1);
             ++S->tune_runs;
         }
     }
@@ -726,16 +735,17 @@ int Engine::time_sweeps(int n, double* msc, double* msb, double* bc, double* bb)
     if (sp && split && split->prev_count > 0) {
         SplitState* S = split;
         const int g = S->gen ^ 1;
-        const int cblocks = split_contact_blocks(S->variant, S->prev_count, S->sms);
+        const int tv = split_sweep_variant();
+        const int cblocks = split_contact_blocks(tv, S->prev_count, S->sms);
         *S->h_nc = S->prev_count;
         cudaMemcpyAsync(S->sb.nc_dev, S->h_nc, sizeof(int32_t), cudaMemcpyHostToDevice, stream);
         launch_s_reset(S->sb, stream);
         CoopPlan plan;
-        if (split_variant_is_coop(S->variant) && split_coop_plan(S->variant, S->prev_count, sc.N, S->sms, &plan, cfg.gpu_coop_smem_contacts)) {
+        if (split_variant_is_coop(tv) && split_coop_plan(tv, S->prev_count, sc.N, S->sms, &plan, cfg.gpu_coop_smem_contacts)) {
             // one cooperative launch of n sweeps; reported per sweep
             cudaEventRecord(e[0], stream);
-            st = launch_s_solve_coop(S->sb, g, (float)cfg.pj_alpha, S->variant, plan, 1 << 30, 0.f, n,
-                                     cfg.gpu_check_every, stream);
+            st = launch_s_solve_coop(S->sb, g, (float)cfg.pj_alpha, tv, plan, 1 << 30, 0.f, n, cfg.gpu_check_every,
+                                     stream);
             cudaEventRecord(e[1], stream);
             if (!(st = cuda_check((cudaError_t)st, "cooperative launch")) &&
                 !(st = cuda_check(cudaEventSynchronize(e[1]), "time sweeps"))) {
@@ -751,7 +761,7 @@ int Engine::time_sweeps(int n, double* msc, double* msb, double* bc, double* bb)
         } else {
           for (int k = 0; k < n; ++k) {
             cudaEventRecord(e[0], stream);
-            launch_s_sweep(S->sb, g, (float)cfg.pj_alpha, S->variant, cblocks, 1 << 30, 0.f, 0, 0, stream);
+            launch_s_sweep(S->sb, g, (float)cfg.pj_alpha, tv, cblocks, 1 << 30, 0.f, 0, 0, stream);
             cudaEventRecord(e[1], stream);
             cudaEventRecord(e[2], stream);
             if ((st = cuda_check(cudaEventSynchronize(e[2]), "time sweeps"))) break;
@@ -799,6 +809,17 @@ int Engine::time_sweeps(int n, double* msc, double* msb, double* bc, double* bb)
 }
 
 int Engine::split_variant() const { return split ? split->last_variant : -1; }
+// the whole-problem shape for the last step's contacts: the cooperative solve where its plan fits,
+// else a streaming shape (the first one when a cooperative or batched shape is selected)
+int Engine::split_sweep_variant() const {
+    if (!split) return -1;
+    const SplitState* S = split;
+    CoopPlan plan;
+    if (split_variant_is_coop(S->variant) && S->prev_count > 0 &&
+        split_coop_plan(S->variant, S->prev_count, sc.N, S->sms, &plan, cfg.gpu_coop_smem_contacts))
+        return S->variant;
+    return (split_variant_is_coop(S->variant) || split_variant_is_scenes(S->variant)) ? 0 : S->variant;
+}
 int Engine::split_tune_runs() const { return split ? split->tune_runs : 0; }
 int Engine::split_redos() const { return split ? split->redos : 0; }
 int64_t Engine::split_graph_steps() const { return split ? split->graph_steps : 0; }

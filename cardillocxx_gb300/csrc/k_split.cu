@@ -1483,6 +1483,7 @@ int split_num_variants() { return N_STREAM + N_COOP + N_SCENES; }
 bool split_variant_is_coop(int v) { return v >= N_STREAM && v < N_STREAM + N_COOP; }
 bool split_variant_is_scenes(int v) { return v >= N_STREAM + N_COOP && v < N_STREAM + N_COOP + N_SCENES; }
 int split_first_scenes_variant() { return N_STREAM + N_COOP; }
+int split_first_coop_variant() { return N_STREAM; }
 int split_num_scenes_variants() { return N_SCENES; }
 
 const char* split_variant_name(int v) {

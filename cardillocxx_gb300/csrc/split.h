@@ -101,6 +101,9 @@ const char* split_variant_name(int v);
 bool split_variant_is_coop(int v);
 bool split_variant_is_scenes(int v);
 int split_first_scenes_variant();
+// the shape used until the autotuner has timed the others: the cooperative solve (where its plan
+// fits; otherwise the first streaming shape runs)
+int split_first_coop_variant();
 int split_num_scenes_variants();
 // batched scenes: the whole solve of every scene, one block per scene (order = scene ids by
 // decreasing size; nbmax = bodies of the largest scene). Returns a cudaError_t.

@@ -139,6 +139,8 @@ typedef struct cdx_stats {
     int32_t autotune_runs;     /* split form: times the autotuner ran */
     int32_t redone_steps;      /* split form: steps undone and redone because their contacts outgrew the buffers */
     int64_t graph_steps;       /* split form: steps replayed whole from a captured CUDA graph */
+    int32_t sweep_variant;     /* split form: the shape cdx_time_sweeps times (the whole-problem solver,
+                                  also when a batched-scenes shape ran the step) */
 } cdx_stats;
 
 typedef struct cdx_ctx cdx_ctx;
