@@ -59,6 +59,8 @@ def parse():
                    help="pin the split-form solver shape (index or name; default: autotuned)")
     p.add_argument("--save-state", default=None, help="write the settled state (npz) and continue")
     p.add_argument("--load-state", default=None, help="start from a settled state written by --save-state")
+    p.add_argument("--set", action="append", default=[], metavar="KEY=VALUE",
+                   help="extra configuration key for the timed engine (repeatable), e.g. gpu.coop_blocks=8")
     return p.parse_args()
 
 
@@ -210,6 +212,9 @@ def run_cdx(a, log):
     sscene = with_state(scene, state)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     run_cfg = dict(cfg, **{"gpu.precision": a.precision, "gpu.graph": not a.no_graph})
+    for kv in a.set:
+        k, _, v = kv.partition("=")
+        run_cfg[k.strip()] = v.strip()
     if a.sweep_variant is not None:
         from cardillocxx_gb300 import PhysicsEngine
         names = PhysicsEngine.split_variants()

@@ -71,6 +71,7 @@ class CdxConfig(C.Structure):
         ("output_folder", C.c_char * 256),
         ("output_filename_prefix", C.c_char * 128),
         ("gpu_coop_smem_contacts", C.c_int32),
+        ("gpu_coop_blocks", C.c_int32),
     ]
 
 

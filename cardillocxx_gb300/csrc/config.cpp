@@ -105,6 +105,7 @@ int cdx_config_default(cdx_config* c) {
     c->output_interval_steps = 0;
     c->output_write_contact_manifolds = 1;
     c->gpu_coop_smem_contacts = 0;
+    c->gpu_coop_blocks = 0;
     std::snprintf(c->output_folder, sizeof(c->output_folder), "%s", "./vtk_out");
     std::snprintf(c->output_filename_prefix, sizeof(c->output_filename_prefix), "%s", "scene");
     return CDX_OK;
@@ -188,6 +189,8 @@ int cdx_config_set(cdx_config* c, const char* key_c, const char* val_c) {
         if (as_int(val, &i)) c->gpu_sweep_variant = std::max(-1, i);
     } else if (key == "gpu.coop_smem_contacts") {
         if (as_int(val, &i)) c->gpu_coop_smem_contacts = std::max(0, i);
+    } else if (key == "gpu.coop_blocks") {
+        if (as_int(val, &i)) c->gpu_coop_blocks = std::max(0, i);
     } else if (key == "gpu.sync_counts") {
         c->gpu_sync_counts = as_bool(val);
     } else if (key_is(key, "pj.nesterov")) {

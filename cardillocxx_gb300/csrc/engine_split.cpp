@@ -133,6 +133,11 @@ static int split_contacts(Engine& E, int64_t need) {
     return E.ensure_tmp(cap);
 }
 
+// cooperative plan for n contacts under the context's gpu.coop_* keys
+static bool coop_plan(const Engine& E, int v, int64_t n, CoopPlan* p) {
+    return split_coop_plan(v, n, E.sc.N, E.split->sms, p, E.cfg.gpu_coop_smem_contacts, E.cfg.gpu_coop_blocks);
+}
+
 static int init_split(Engine& E) {
     E.split = new SplitState();
     SplitState* S = E.split;
@@ -270,7 +275,7 @@ int Engine::step_split() {
         for (int v = 0; v < split_num_variants(); ++v) {
             CoopPlan probe;
             if (split_variant_is_coop(v))
-                sweeps += split_coop_plan(v, n, sc.N, S->sms, &probe, cfg.gpu_coop_smem_contacts) ? 8 : 0;
+                sweeps += coop_plan(*this, v, n, &probe) ? 8 : 0;
             else if (!split_variant_is_scenes(v))
                 sweeps += 2;
         }
@@ -307,8 +312,8 @@ int Engine::step_split() {
         if (!split_variant_is_coop(S->variant)) {
             use_graph = false;
         } else if (!(S->gplan_ok && (int64_t)S->gplan.cpb * S->gplan.grid >= est)) {
-            S->gplan_ok = split_coop_plan(S->variant, est + est / 4, sc.N, S->sms, &S->gplan, cfg.gpu_coop_smem_contacts) ||
-                          split_coop_plan(S->variant, est, sc.N, S->sms, &S->gplan, cfg.gpu_coop_smem_contacts);
+            S->gplan_ok = coop_plan(*this, S->variant, est + est / 4, &S->gplan) ||
+                          coop_plan(*this, S->variant, est, &S->gplan);
             if (!S->gplan_ok) use_graph = false;
         }
     }
@@ -468,7 +473,7 @@ int Engine::step_split() {
     for (int v = 0; v < nv; ++v) {
         CoopPlan probe;
         if (split_variant_is_coop(v))
-            tune_sweeps += (S->nc > 0 && split_coop_plan(v, S->nc, sc.N, S->sms, &probe, cfg.gpu_coop_smem_contacts)) ? 8 : 0;
+            tune_sweeps += (S->nc > 0 && coop_plan(*this, v, S->nc, &probe)) ? 8 : 0;
         else if (!split_variant_is_scenes(v))
             tune_sweeps += 2;
     }
@@ -490,7 +495,7 @@ int Engine::step_split() {
                 // two launches of 2 and 6 sweeps: their difference is the cost of a sweep, the rest
                 // (loading and storing the contacts) is paid once per solve of maxit sweeps
                 CoopPlan plan;
-                if (!split_coop_plan(v, S->nc, sc.N, S->sms, &plan, cfg.gpu_coop_smem_contacts)) continue;
+                if (!coop_plan(*this, v, S->nc, &plan)) continue;
                 float ms[2] = {0.f, 0.f};
                 const int ks[2] = {2, 6};
                 for (int r = 0; r < 2; ++r) {
@@ -537,7 +542,7 @@ int Engine::step_split() {
     const int64_t plan_nc = async ? (int64_t)S->nc + S->nc / 16 + 64 : (int64_t)S->nc;
     if (capturing && !scenes && split_variant_is_coop(S->variant)) plan = S->gplan;
     coop = !scenes && S->nc > 0 && split_variant_is_coop(S->variant) &&
-           (capturing ? S->gplan_ok : split_coop_plan(S->variant, plan_nc, sc.N, S->sms, &plan, cfg.gpu_coop_smem_contacts));
+           (capturing ? S->gplan_ok : coop_plan(*this, S->variant, plan_nc, &plan));
     if (S->nc > 0 && !solved && coop) {
         st = launch_s_solve_coop(sb, gen, (float)cfg.pj_alpha, S->variant, plan, maxit, (float)cfg.gpu_residual_tol,
                                  maxit, cfg.gpu_check_every, stream);
@@ -741,7 +746,7 @@ int Engine::time_sweeps(int n, double* msc, double* msb, double* bc, double* bb)
         cudaMemcpyAsync(S->sb.nc_dev, S->h_nc, sizeof(int32_t), cudaMemcpyHostToDevice, stream);
         launch_s_reset(S->sb, stream);
         CoopPlan plan;
-        if (split_variant_is_coop(tv) && split_coop_plan(tv, S->prev_count, sc.N, S->sms, &plan, cfg.gpu_coop_smem_contacts)) {
+        if (split_variant_is_coop(tv) && coop_plan(*this, tv, S->prev_count, &plan)) {
             // one cooperative launch of n sweeps; reported per sweep
             cudaEventRecord(e[0], stream);
             st = launch_s_solve_coop(S->sb, g, (float)cfg.pj_alpha, tv, plan, 1 << 30, 0.f, n, cfg.gpu_check_every,
@@ -816,7 +821,7 @@ int Engine::split_sweep_variant() const {
     const SplitState* S = split;
     CoopPlan plan;
     if (split_variant_is_coop(S->variant) && S->prev_count > 0 &&
-        split_coop_plan(S->variant, S->prev_count, sc.N, S->sms, &plan, cfg.gpu_coop_smem_contacts))
+        coop_plan(*this, S->variant, S->prev_count, &plan))
         return S->variant;
     return (split_variant_is_coop(S->variant) || split_variant_is_scenes(S->variant)) ? 0 : S->variant;
 }

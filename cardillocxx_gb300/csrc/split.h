@@ -114,8 +114,10 @@ int launch_s_solve_scenes(const Scene& sc, const SplitBuf& sb, int gen, float al
 struct CoopPlan {
     int grid = 0, nth = 0, cpb = 0, bpb = 0, vf = 0, smem = 0;
 };
-// smem_contacts > 0 caps the contacts a block keeps in shared memory (gpu.coop_smem_contacts)
-bool split_coop_plan(int v, int64_t nc, int64_t nbodies, int sms, CoopPlan* p, int smem_contacts = 0);
+// smem_contacts > 0 caps the contacts a block keeps in shared memory (gpu.coop_smem_contacts);
+// blocks > 0 sets the grid (gpu.coop_blocks, capped at one block per SM), 0 = one per SM
+bool split_coop_plan(int v, int64_t nc, int64_t nbodies, int sms, CoopPlan* p, int smem_contacts = 0,
+                     int blocks = 0);
 // the projected Jacobi solve, up to max_sweeps sweeps, in one cooperative launch, evaluating the
 // stop rule every check_every sweeps; returns the cudaError_t of the launch
 int launch_s_solve_coop(const SplitBuf& sb, int gen, float alpha, int v, const CoopPlan& p, int max_iter, float tol,

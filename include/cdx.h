@@ -89,6 +89,8 @@ typedef struct cdx_config {
     char output_filename_prefix[128];       /* output.filename_prefix */
     int32_t gpu_coop_smem_contacts;         /* gpu.coop_smem_contacts: cap on the contacts a block of the
                                                cooperative solve keeps in shared memory (0 = all that fit) */
+    int32_t gpu_coop_blocks;                /* gpu.coop_blocks: blocks of the cooperative solve (0 = one per SM;
+                                               more than that is capped) */
 } cdx_config;
 
 /* Scene: dynamic spheres plus static shapes (halfspaces, drums). Bodies of one scene are

@@ -68,6 +68,10 @@ def test_config_defaults_and_keys(cdxlib):
     assert c.get("friction_combine") == 2 and c.get("sim_dt") == 1e-3
     assert c.get("collision_match_max_dist") == 0.0
     assert c.get("sim_gravity") == [0.0, 0.0, -1.62]
+    # cooperative-solve keys of this build: non-negative integers, 0 = automatic
+    assert c.get("gpu_coop_blocks") == 0 and c.get("gpu_coop_smem_contacts") == 0
+    c.set("gpu.coop_blocks", "16").set("gpu.coop_smem_contacts", "-5")
+    assert c.get("gpu_coop_blocks") == 16 and c.get("gpu_coop_smem_contacts") == 0
 
 
 def test_config_file_parsing(cdxlib, tmp_path):

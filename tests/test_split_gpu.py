@@ -99,22 +99,24 @@ def test_split_every_sweep_shape_computes_the_same_sweep(gpu):
     names = PhysicsEngine.split_variants()
     assert len(names) >= 2
     out = []
-    for v in range(len(names)):
+    runs = [(v, {"gpu.coop_smem_contacts": 1} if "hyb" in names[v] else {}) for v in range(len(names))]
+    # a cooperative solve on a reduced grid: more contacts and bodies a block, the same sweep
+    runs.append((names.index("coop-t1024-u1-g2"), {"gpu.coop_blocks": 3}))
+    for v, extra in runs:
         # the hybrid cooperative shape runs when a block's contacts exceed its shared-memory cap
-        cap = {"gpu.coop_smem_contacts": 1} if "hyb" in names[v] else {}
-        e = PhysicsEngine(dict(c, **{"gpu.sweep_variant": v}, **cap)).load_scene(s)
+        e = PhysicsEngine(dict(c, **{"gpu.sweep_variant": v}, **extra)).load_scene(s)
         e.set_state(st["pos"], st["quat"], st["vel"], st["omega"])
         e.step(1)
         # the per-scene shapes apply to a single scene too (it fits one block)
         assert e.stats()["contact_variant"] == v, names[v]
-        out.append((e.contacts()["lambda"], e.state()["vel"]))
-    lam0, vel0 = out[0]
+        out.append((f"{names[v]} {extra}", e.contacts()["lambda"], e.state()["vel"]))
+    _, lam0, vel0 = out[0]
     lmax = np.abs(lam0).max()
     vscale = np.abs(st["vel"]).max() + G * H
-    for v, (lam, vel) in enumerate(out):
-        assert lam.shape == lam0.shape, names[v]
-        assert np.abs(lam - lam0).max() <= 1e-3 * lmax, names[v]
-        assert np.abs(vel - vel0).max() <= 1e-3 * vscale, names[v]
+    for label, lam, vel in out:
+        assert lam.shape == lam0.shape, label
+        assert np.abs(lam - lam0).max() <= 1e-3 * lmax, label
+        assert np.abs(vel - vel0).max() <= 1e-3 * vscale, label
 
 
 def test_split_residual_is_fp64_and_decreases(gpu):
