@@ -85,6 +85,10 @@ struct Contacts {
     double* cb = nullptr;     // 3*cap
     double* biasR = nullptr;  // 3*cap
     double* dlam = nullptr;   // 3*cap
+    // 36*cap (plain FP64 method): per contact side (index 2c + side) and row r, the products
+    // (s d_r) dlam_r of the W^T gather, 6 a row (direction, then lever part), written by the contact
+    // sweep so the body sweep reads 144 contiguous bytes a contact side
+    double* term = nullptr;
     double* rb = nullptr;     // 9*cap: inverse Delassus block / alpha (pj.rdiag_true_delassus only)
     int32_t* rb_full = nullptr;  // device flag: some block is not diagonal (full 3x3 products)
     double* mu = nullptr;

@@ -347,6 +347,8 @@ int Engine::ensure_contacts(int64_t need) {
     double** d1[] = {&n.mu, &n.eN, &n.eT};
     for (auto p : d1)
         if ((st = dalloc((void**)p, sizeof(double) * cap, "contacts"))) return st;
+    if (cfg.gpu_precision == CDX_PRECISION_FP64)
+        if ((st = dalloc((void**)&n.term, sizeof(double) * 36 * cap, "contact terms"))) return st;
     if (cfg.pj_rdiag_true_delassus && cfg.gpu_precision == CDX_PRECISION_FP64) {
         if ((st = dalloc((void**)&n.rb, sizeof(double) * 9 * cap, "contact blocks"))) return st;
         if ((st = dalloc((void**)&n.rb_full, sizeof(int32_t), "contact blocks"))) return st;
@@ -373,7 +375,7 @@ int Engine::ensure_contacts(int64_t need) {
     if (C.cap > 0) {
         void* old[] = {C.a, C.b, C.flags, C.rank, C.dir, C.cA, C.cB, C.rd, C.rcA, C.rcB, C.cb, C.biasR, C.dlam,
                        C.mu, C.eN, C.eT, C.key[0], C.key[1], C.point[0], C.point[1], C.lam[0], C.lam[1],
-                       C.rb, C.rb_full};
+                       C.rb, C.rb_full, C.term};
         for (void* p : old) dfree(p);
         ++reallocations;
     }

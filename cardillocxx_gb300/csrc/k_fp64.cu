@@ -713,6 +713,19 @@ __global__ void k_sweep_contact64(Scene sc, Contacts C, int gen, int nc, const d
             if (!dry) {
                 lamp[r * cap + c] = lnew[r];
                 C.dlam[r * cap + c] = dl;
+                if (C.term) {
+                    // the body sweep's products (s d) y, with s = +-1 exact: (-d) y for side A
+                    double2* tb = reinterpret_cast<double2*>(C.term + (size_t)(2 * c + 1) * 18 + 6 * r);
+                    tb[0] = make_double2(C.dir[(3 * r) * cap + c] * dl, C.dir[(3 * r + 1) * cap + c] * dl);
+                    tb[1] = make_double2(C.dir[(3 * r + 2) * cap + c] * dl, C.cB[(3 * r) * cap + c] * dl);
+                    tb[2] = make_double2(C.cB[(3 * r + 1) * cap + c] * dl, C.cB[(3 * r + 2) * cap + c] * dl);
+                    if (a >= 0) {
+                        double2* ta = reinterpret_cast<double2*>(C.term + (size_t)(2 * c) * 18 + 6 * r);
+                        ta[0] = make_double2((-C.dir[(3 * r) * cap + c]) * dl, (-C.dir[(3 * r + 1) * cap + c]) * dl);
+                        ta[1] = make_double2((-C.dir[(3 * r + 2) * cap + c]) * dl, (-C.cA[(3 * r) * cap + c]) * dl);
+                        ta[2] = make_double2((-C.cA[(3 * r + 1) * cap + c]) * dl, (-C.cA[(3 * r + 2) * cap + c]) * dl);
+                    }
+                }
             }
         }
         maxd = sqrt(s2);
@@ -733,7 +746,27 @@ __global__ void k_sweep_body64(Scene sc, Contacts C, Incidence inc, double* x, d
     if (i < sc.N) {
         const int N = sc.N;
         double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-        gather_wt<1>(C, C.dlam, inc, i, acc);
+        if (C.term) {
+            // the same sums in the same order (incidences in row order, rows in order) from the
+            // products the contact sweep stored
+            const int e = inc.end[i];
+            for (int p = inc.start[i]; p < e; ++p) {
+                const uint32_t code = inc.val_out[p];
+                const int nr = (C.flags[code >> 1] & CF_FRICTIONAL) ? 3 : 1;
+                const double2* t = reinterpret_cast<const double2*>(C.term + (size_t)code * 18);
+                for (int r = 0; r < nr; ++r) {
+                    const double2 u0 = t[3 * r], u1 = t[3 * r + 1], u2 = t[3 * r + 2];
+                    acc[0] = acc[0] + u0.x;
+                    acc[1] = acc[1] + u0.y;
+                    acc[2] = acc[2] + u1.x;
+                    acc[3] = acc[3] + u1.y;
+                    acc[4] = acc[4] + u2.x;
+                    acc[5] = acc[5] + u2.y;
+                }
+            }
+        } else {
+            gather_wt<1>(C, C.dlam, inc, i, acc);
+        }
         const double Ml = sc.bf(BF_ML)[i], Ma = sc.bf(BF_MA)[i];
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
