@@ -799,10 +799,12 @@ int Engine::time_sweeps(int n, double* msc, double* msb, double* bc, double* bb)
             tb += b;
         }
         launches += 2 * (int64_t)n;
-        // contact kernel: ids, flags, RW (27 words), bias (3), mu, lambda read+write, dlambda write
-        if (bc) *bc = (double)prev_count * (8 + 4 + 27 * 8 + 3 * 8 + 8 + 6 * 8 + 3 * 8);
-        // body kernel: incidence ranges, x read+write, M, and the gathered rows (dir, lever, dlambda)
-        if (bb) *bb = (double)sc.N * (8 + 12 * 8 + 2 * 8) + (double)prev_count * (9 + 9 + 9 + 3) * 8;
+        // contact kernel: ids, flags, RW (27 words), bias (3), mu, lambda read+write, dlambda write,
+        // and the W^T products for the body sweep (directions and lever parts read, 36 words written)
+        if (bc) *bc = (double)prev_count * (8 + 4 + 27 * 8 + 3 * 8 + 8 + 6 * 8 + 3 * 8 + 27 * 8 + 36 * 8);
+        // body kernel: incidence ranges, x read+write, M; per contact side its incidence code,
+        // the contact's flags and the 18 stored products
+        if (bb) *bb = (double)sc.N * (8 + 12 * 8 + 2 * 8) + (double)prev_count * 2 * (4 + 4 + 18 * 8);
     } else {
         st = fail(CDX_ERR_STATE, "no contacts from a previous step");
     }
