@@ -240,7 +240,7 @@ __global__ void k_csr_rows(int nrows, int nfl, const int32_t* ptr, const int32_t
                 dlam[r0 + q] = d;
             }
         }
-        maxd = sqrt(s2);
+        maxd = s2;  // squared: the root of the block maximum equals the maximum of the roots
     }
     __shared__ double sh[2][32];
     for (int o = 16; o > 0; o >>= 1) {
@@ -260,7 +260,7 @@ __global__ void k_csr_rows(int nrows, int nfl, const int32_t* ptr, const int32_t
             maxl = fmax(maxl, __shfl_xor_sync(0xffffffffu, maxl, o));
         }
         if (threadIdx.x == 0) {
-            atomicMax(&ds->maxd, (unsigned long long)__double_as_longlong(maxd));
+            atomicMax(&ds->maxd, (unsigned long long)__double_as_longlong(sqrt(maxd)));
             atomicMax(&ds->maxl, (unsigned long long)__double_as_longlong(maxl));
         }
     }

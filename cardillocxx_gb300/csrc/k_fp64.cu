@@ -728,12 +728,12 @@ __global__ void k_sweep_contact64(Scene sc, Contacts C, int gen, int nc, const d
                 }
             }
         }
-        maxd = sqrt(s2);
+        maxd = s2;  // squared: the root of the block maximum equals the maximum of the roots
     }
     maxd = block_max(maxd);
     maxl = block_max(maxl);
     if (threadIdx.x == 0) {
-        atomic_max_nonneg(&ds->maxd, maxd);
+        atomic_max_nonneg(&ds->maxd, sqrt(maxd));
         atomic_max_nonneg(&ds->maxl, maxl);
     }
 }
