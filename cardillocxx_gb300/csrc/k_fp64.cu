@@ -285,8 +285,11 @@ template <bool WRITE>
 __global__ void k_pairs64(Scene sc, Grid gr, const uint32_t* cell_body, const int32_t* cell_start,
                           const int32_t* cell_end, double margin, int32_t* counts, const int32_t* offsets,
                           int32_t base, Contacts C, int gen, int combine, int friction_enable, DevScalars* ds) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= sc.N) return;
+    // threads take the spheres in cell order, so a warp walks neighbouring cells; each sphere's
+    // count and contacts are its own (same values, written at its own offset)
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= sc.N) return;
+    const int i = (int)cell_body[t];
     const double xi[3] = {sc.bf(BF_PX)[i], sc.bf(BF_PY)[i], sc.bf(BF_PZ)[i]};
     const double ri = sc.bf(BF_RAD)[i];
     const int si = sc.body_scene[i];
