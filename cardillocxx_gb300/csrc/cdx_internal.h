@@ -186,13 +186,18 @@ void launch_unpack_state(const Scene& sc, const double* in, int mask, cudaStream
 void launch_rhs64(const Scene& sc, double dt, const double* g, double* rhs, cudaStream_t s, int implicit_gyro = 0);
 void launch_drift64(const Scene& sc, double h, int compute_R, cudaStream_t s);
 void launch_static_flags64(const Scene& sc, double margin, int32_t* flags, cudaStream_t s);
+// FP32 copy of the positions (relative to the grid origin) and radii: the pair kernels' conservative
+// pre-test, so that only pairs near contact reach the FP64 test
+void launch_pos32(const Scene& sc, const Grid& g, float4* p32, cudaStream_t s);
 void launch_pair_count64(const Scene& sc, const Grid& g, const uint32_t* cell_body, const int32_t* cell_start,
-                         const int32_t* cell_end, double margin, int32_t* counts, DevScalars* ds, cudaStream_t s);
+                         const int32_t* cell_end, const float4* p32, double margin, int32_t* counts, DevScalars* ds,
+                         cudaStream_t s);
 void launch_static_write64(const Scene& sc, double margin, const int32_t* flags, const int32_t* pos,
                            Contacts& C, int gen, int combine, int friction_enable, cudaStream_t s);
 void launch_pair_write64(const Scene& sc, const Grid& g, const uint32_t* cell_body, const int32_t* cell_start,
-                         const int32_t* cell_end, double margin, const int32_t* offsets, int32_t base,
-                         Contacts& C, int gen, int combine, int friction_enable, DevScalars* ds, cudaStream_t s);
+                         const int32_t* cell_end, const float4* p32, double margin, const int32_t* offsets,
+                         int32_t base, Contacts& C, int gen, int combine, int friction_enable, DevScalars* ds,
+                         cudaStream_t s);
 void launch_contact_setup64(const Scene& sc, Contacts& C, int gen, int nc, int prev_count, double alpha,
                             double match2, int warmstart, cudaStream_t s);
 void launch_frictionless_flags(const Contacts& C, int nc, int32_t* isfl, cudaStream_t s);

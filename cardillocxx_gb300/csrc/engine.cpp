@@ -267,6 +267,7 @@ int Engine::load_scene(const cdx_scene& s) {
     if ((st = dalloc((void**)&cell_val_in, sizeof(uint32_t) * std::max(1, N), "grid"))) return st;
     if ((st = dalloc((void**)&cell_key_out, sizeof(uint32_t) * std::max(1, N), "grid"))) return st;
     if ((st = dalloc((void**)&cell_val_out, sizeof(uint32_t) * std::max(1, N), "grid"))) return st;
+    if ((st = dalloc((void**)&pos32, sizeof(float4) * std::max(1, N), "grid"))) return st;
     if ((st = dalloc((void**)&cell_start, sizeof(int32_t) * ncells, "grid"))) return st;
     if ((st = dalloc((void**)&cell_end, sizeof(int32_t) * ncells, "grid"))) return st;
     const int64_t nflag = (int64_t)std::max(1, N) * std::max(1, maxst);
@@ -414,8 +415,9 @@ int Engine::collide64() {
         if ((st = cuda_check(exclusive_scan(tmp, tmp_bytes, sflags, spos, nflag, stream), "scan"))) return st;
         launches += 2;
     }
-    launch_pair_count64(sc, grid, cell_val_out, cell_start, cell_end, margin, pcount, ds, stream);
-    ++launches;
+    launch_pos32(sc, grid, pos32, stream);
+    launch_pair_count64(sc, grid, cell_val_out, cell_start, cell_end, pos32, margin, pcount, ds, stream);
+    launches += 2;
     if ((st = cuda_check(exclusive_scan(tmp, tmp_bytes, pcount, poff, N + 1, stream), "scan"))) return st;
     launches += 2;
     // totals to the host (one synchronisation per step: the contact count sizes everything after)
@@ -437,7 +439,7 @@ int Engine::collide64() {
         ++launches;
     }
     if (n_pair > 0) {
-        launch_pair_write64(sc, grid, cell_val_out, cell_start, cell_end, margin, poff, (int32_t)n_static, C, gen,
+        launch_pair_write64(sc, grid, cell_val_out, cell_start, cell_end, pos32, margin, poff, (int32_t)n_static, C, gen,
                             cfg.friction_combine, cfg.friction_enable, ds, stream);
         ++launches;
     }

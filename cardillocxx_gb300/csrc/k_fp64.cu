@@ -281,16 +281,40 @@ __global__ void k_static_write64(Scene sc, double margin, const int32_t* flags, 
     }
 }
 
+__global__ void k_pos32(Scene sc, Grid gr, float4* p32) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sc.N) return;
+    p32[i] = make_float4((float)(sc.bf(BF_PX)[i] - gr.lo[0]), (float)(sc.bf(BF_PY)[i] - gr.lo[1]),
+                         (float)(sc.bf(BF_PZ)[i] - gr.lo[2]), (float)sc.bf(BF_RAD)[i]);
+}
+
+// Conservative FP32 pre-test of a sphere pair: false only when the FP64 test (pair_touch) is
+// certain to reject it too. Every FP32 quantity here is within a relative 2^-22 of its FP64 value
+// (positions and radii rounded once, differences and sums a few more times), so the distance is
+// within 2^-21 (|x_i| + |x_j|) + 2^-21 d of the exact one. The limit therefore widens the FP64
+// limit (r_i + r_j) 1.000001 + |margin| by a relative 9e-6 and by 1e-6 (|x_i| + |x_j|) (> 2^-21 of
+// it). NaN positions compare false and go on to the FP64 test.
+__device__ __forceinline__ bool pair_near32(float4 pi, float ei, float4 pj, float mf) {
+    const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+    const float ej = fmaxf(fabsf(pj.x), fmaxf(fabsf(pj.y), fabsf(pj.z)));
+    const float lim = (pi.w + pj.w) * 1.00001f + mf + 1e-6f * (ei + ej) + 1e-30f;
+    return !(dx * dx + dy * dy + dz * dz > lim * lim);
+}
+
 template <bool WRITE>
 __global__ void k_pairs64(Scene sc, Grid gr, const uint32_t* cell_body, const int32_t* cell_start,
-                          const int32_t* cell_end, double margin, int32_t* counts, const int32_t* offsets,
-                          int32_t base, Contacts C, int gen, int combine, int friction_enable, DevScalars* ds) {
+                          const int32_t* cell_end, const float4* p32, double margin, int32_t* counts,
+                          const int32_t* offsets, int32_t base, Contacts C, int gen, int combine,
+                          int friction_enable, DevScalars* ds) {
     // threads take the spheres in cell order, so a warp walks neighbouring cells; each sphere's
     // count and contacts are its own (same values, written at its own offset)
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= sc.N) return;
     const int i = (int)cell_body[t];
     const double xi[3] = {sc.bf(BF_PX)[i], sc.bf(BF_PY)[i], sc.bf(BF_PZ)[i]};
+    const float4 pi = p32[i];
+    const float ei = fmaxf(fabsf(pi.x), fmaxf(fabsf(pi.y), fabsf(pi.z)));
+    const float mf = (float)fabs(margin) * 1.00001f;
     const double ri = sc.bf(BF_RAD)[i];
     const int si = sc.body_scene[i];
     int ci[3];
@@ -311,6 +335,7 @@ __global__ void k_pairs64(Scene sc, Grid gr, const uint32_t* cell_body, const in
                 for (int p = cell_start[cell]; p < e; ++p) {
                     const int j = (int)cell_body[p];
                     if (j <= i || sc.body_scene[j] != si) continue;
+                    if (!pair_near32(pi, ei, p32[j], mf)) continue;
                     const double xj[3] = {sc.bf(BF_PX)[j], sc.bf(BF_PY)[j], sc.bf(BF_PZ)[j]};
                     if (!pair_touch(xi, ri, xj, sc.bf(BF_RAD)[j], margin)) continue;
                     if (WRITE) {
@@ -1324,12 +1349,16 @@ void launch_static_flags64(const Scene& sc, double margin, int32_t* flags, cudaS
     if (sc.N == 0) return;
     k_static_flags64<<<nblk(sc.N), NT, 0, s>>>(sc, margin, flags);
 }
+void launch_pos32(const Scene& sc, const Grid& g, float4* p32, cudaStream_t s) {
+    if (sc.N) k_pos32<<<nblk(sc.N), NT, 0, s>>>(sc, g, p32);
+}
 void launch_pair_count64(const Scene& sc, const Grid& g, const uint32_t* cell_body, const int32_t* cell_start,
-                         const int32_t* cell_end, double margin, int32_t* counts, DevScalars* ds, cudaStream_t s) {
+                         const int32_t* cell_end, const float4* p32, double margin, int32_t* counts, DevScalars* ds,
+                         cudaStream_t s) {
     if (sc.N == 0) return;
     Contacts dummy;
-    k_pairs64<false><<<nblk(sc.N), NT, 0, s>>>(sc, g, cell_body, cell_start, cell_end, margin, counts, nullptr, 0,
-                                                dummy, 0, 0, 0, ds);
+    k_pairs64<false><<<nblk(sc.N), NT, 0, s>>>(sc, g, cell_body, cell_start, cell_end, p32, margin, counts, nullptr,
+                                                0, dummy, 0, 0, 0, ds);
 }
 void launch_static_write64(const Scene& sc, double margin, const int32_t* flags, const int32_t* pos,
                            Contacts& C, int gen, int combine, int friction_enable, cudaStream_t s) {
@@ -1337,11 +1366,12 @@ void launch_static_write64(const Scene& sc, double margin, const int32_t* flags,
     k_static_write64<<<nblk(sc.N), NT, 0, s>>>(sc, margin, flags, pos, C, gen, combine, friction_enable);
 }
 void launch_pair_write64(const Scene& sc, const Grid& g, const uint32_t* cell_body, const int32_t* cell_start,
-                         const int32_t* cell_end, double margin, const int32_t* offsets, int32_t base,
-                         Contacts& C, int gen, int combine, int friction_enable, DevScalars* ds, cudaStream_t s) {
+                         const int32_t* cell_end, const float4* p32, double margin, const int32_t* offsets,
+                         int32_t base, Contacts& C, int gen, int combine, int friction_enable, DevScalars* ds,
+                         cudaStream_t s) {
     if (sc.N == 0) return;
-    k_pairs64<true><<<nblk(sc.N), NT, 0, s>>>(sc, g, cell_body, cell_start, cell_end, margin, nullptr, offsets, base,
-                                               C, gen, combine, friction_enable, ds);
+    k_pairs64<true><<<nblk(sc.N), NT, 0, s>>>(sc, g, cell_body, cell_start, cell_end, p32, margin, nullptr, offsets,
+                                               base, C, gen, combine, friction_enable, ds);
 }
 void launch_contact_setup64(const Scene& sc, Contacts& C, int gen, int nc, int prev_count, double alpha,
                             double match2, int warmstart, cudaStream_t s) {
