@@ -281,8 +281,8 @@ int Engine::step_split() {
         }
         return maxit > 2 * sweeps;
     };
-    // the per-scene kernel (one block a scene, its bodies in shared memory) is a candidate for
-    // batches and for a single scene small enough for one block
+    // the per-scene kernel (one block a scene) is a candidate for batches and for a single scene
+    // small enough that one block can carry it
     const bool scene_fit = S->scene_nbmax > 0 && S->scene_nbmax <= 3584;
     // shapes timed while the scenes had few contacts (a pile that is still falling) say little about
     // the settled problem: time them again once the count has grown by half

@@ -988,55 +988,27 @@ __global__ void __launch_bounds__(NTH, 1) k_s_solve_coop(SplitBuf sb, int gen, f
     }
 }
 
-// ---- batched scenes: one block per scene, the whole solve in shared memory
-// Adds a contact's shares into shared-memory accumulators (float atomics); body A's share is first
-// summed per run of equal index within the warp, as in pj_push.
-__device__ __forceinline__ void smem_add3(float4* p, float x, float y, float z) {
-    atomicAdd(&p->x, x);
-    atomicAdd(&p->y, y);
-    atomicAdd(&p->z, z);
-}
-__device__ __forceinline__ void pj_push_smem(float4* A, bool ok, int a, int b, const PJOut& o) {
-    const bool go = ok && o.push;
-    if (go) {
-        smem_add3(&A[2 * b], o.pb.x, o.pb.y, o.pb.z);
-        smem_add3(&A[2 * b + 1], o.tb.x, o.tb.y, o.tb.z);
-    }
-    const int key = ok ? a : -1;
-    float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    if (go && a >= 0) {
-        v[0] = o.pa.x;
-        v[1] = o.pa.y;
-        v[2] = o.pa.z;
-        v[3] = o.ta.x;
-        v[4] = o.ta.y;
-        v[5] = o.ta.z;
-    }
-    const bool head = warp_run_sum(key, v);
-    if (head && key >= 0 && (v[0] != 0.f || v[1] != 0.f || v[2] != 0.f || v[3] != 0.f || v[4] != 0.f || v[5] != 0.f)) {
-        smem_add3(&A[2 * key], v[0], v[1], v[2]);
-        smem_add3(&A[2 * key + 1], v[3], v[4], v[5]);
-    }
-}
-
+// ---- batched scenes: one block per scene
 // The projected Jacobi solve of a batch of independent scenes. Block k solves scene order[k]
-// (scenes ordered by decreasing size, so the long solves start first): its bodies' accumulators
-// A_k and A_{k+1} live in shared memory (64 B a body) and, with CSM, so do its contact records and
-// impulses (48 B a contact, up to ccap contacts; a scene with more reads them from L1/L2 every
-// sweep). Sweeps are separated by __syncthreads only. Each scene runs its own stop rule (iteration
-// cap, residual <= tol, non-finite) on its own maxima. The final velocities go to accumulator 0;
-// the largest per-scene sweep count and residual go to the step's scalars.
-template <int NT, int UNROLL, int CSM>
+// (scenes ordered by decreasing size, so the long solves start first). Each scene runs its own
+// stop rule (iteration cap, residual <= tol, non-finite) on its own maxima, and sweeps are
+// separated by __syncthreads only, never by a grid barrier.
+// The scene's velocity accumulators are the global ones, three rotating buffers: sweep k gathers
+// A_k through L2 (32-byte loads), adds into A_{k+1} with L2 reductions and per-warp run sums (as
+// the cooperative solve does), and resets A_{k+2} (last read in sweep k - 1) to the free
+// velocities. Summing in shared memory instead (float atomics) measured three times slower on
+// 4,096 scenes. With CSM the scene's contact records and impulses sit in shared memory (48 B a
+// contact, up to ccap contacts; a larger scene reads them from L1/L2 every sweep).
+// The final velocities go to accumulator 0; the largest per-scene sweep count and residual go to
+// the step's scalars.
+template <int NT, int CSM>
 __global__ void __launch_bounds__(NT) k_s_solve_scenes(Scene sc, SplitBuf sb, int gen, float alpha, int max_iter,
                                                        float tol, const int32_t* spos, const int32_t* sflags,
-                                                       const int32_t* poff, const int32_t* order, int L, int nbmax,
-                                                       int ccap) {
+                                                       const int32_t* poff, const int32_t* order, int L, int ccap) {
     extern __shared__ float4 sm4[];
     // a device-counted step whose contacts overflowed the buffers wrote only the slots below the
     // capacity, while the scene ranges below count them all: nothing runs, the host redoes the step
     if (*(volatile const int32_t*)&sb.ss->cap_err) return;
-    float4* Ac = sm4;
-    float4* An = sm4 + 2 * nbmax;
     __shared__ float s_r;
     const int s = order[blockIdx.x];
     const int b0 = sc.scene_body_start[s], nb = sc.scene_body_start[s + 1] - b0;
@@ -1052,14 +1024,12 @@ __global__ void __launch_bounds__(NT) k_s_solve_scenes(Scene sc, SplitBuf sb, in
     const int cp0 = n_static + poff[b0], cp1 = n_static + poff[b0 + nb];
     const int ns = cs1 - cs0, nc = ns + (cp1 - cp0);
     const bool local = CSM && nc <= ccap;  // block-uniform
-    float4* q0s = sm4 + 4 * nbmax;
+    float4* q0s = sm4;
     float4* q1s = q0s + ccap;
     float4* ls = q1s + ccap;
     float4* __restrict__ lamp = sb.lam[gen];
-    for (int i = tid; i < 2 * nb; i += NT) {
-        Ac[i] = sb.acc[0][2 * b0 + i];
-        An[i] = sb.vel4[2 * b0 + i];
-    }
+    // A_0 holds the starting velocities; A_1 starts at the free velocities
+    for (int i = tid; i < 2 * nb; i += NT) sb.acc[1][2 * b0 + i] = sb.vel4[2 * b0 + i];
     if (local)
         for (int k = tid; k < nc; k += NT) {
             const int c = k < ns ? cs0 + k : cp0 + (k - ns);
@@ -1073,56 +1043,68 @@ __global__ void __launch_bounds__(NT) k_s_solve_scenes(Scene sc, SplitBuf sb, in
     const int lane = tid & 31;
     while (true) {
         float maxd2 = 0.f, maxl = 0.f;
-        for (int w0 = (tid & ~31); w0 < nc; w0 += NT * UNROLL) {
-#pragma unroll
-            for (int u = 0; u < UNROLL; ++u) {
-                const int k = w0 + u * NT + lane;
-                const bool ok = k < nc;
-                PJOut o = {};
-                int a = -1, b = 0;
-                if (ok) {
-                    const int c = k < ns ? cs0 + k : cp0 + (k - ns);
-                    float4 r0, r1, l;
-                    if (local) {
-                        r0 = q0s[k];
-                        r1 = q1s[k];
-                        l = ls[k];
-                    } else {
-                        r0 = ldg4(&sb.rec0[c]);
-                        r1 = ldg4(&sb.rec1[c]);
-                        l = lamp[c];
-                    }
-                    const int ag = __float_as_int(r1.z), bg = __float_as_int(r1.w);
-                    a = ag >= 0 ? ag - b0 : -1;
-                    b = bg - b0;
-                    const float4 vb = Ac[2 * b], wb = Ac[2 * b + 1];
-                    const float4 va = a >= 0 ? Ac[2 * a] : make_float4(0.f, 0.f, 0.f, 0.f);
-                    const float4 wa = a >= 0 ? Ac[2 * a + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
-                    pj_contact(r0, r1, l, va, wa, vb, wb, &sb.bias[c], alpha, o);
-                    if (local)
-                        ls[k] = o.lam;
-                    else
-                        lamp[c] = o.lam;
-                    maxd2 = fmaxf(maxd2, o.dn2);
-                    maxl = fmaxf(maxl, o.lm);
+        const float4* Gc = sb.acc[it % 3];
+        float4* Gn = sb.acc[(it + 1) % 3];
+        float4* Gr = sb.acc[(it + 2) % 3];
+        // the loop bound is the same for all lanes of a warp (the run sum needs whole warps)
+        for (int w0 = (tid & ~31); w0 < nc; w0 += NT) {
+            const int k = w0 + lane;
+            const bool ok = k < nc;
+            PJOut o = {};
+            int a = -1, b = 0;
+            if (ok) {
+                const int c = k < ns ? cs0 + k : cp0 + (k - ns);
+                float4 r0, r1, l;
+                if (local) {
+                    r0 = q0s[k];
+                    r1 = q1s[k];
+                    l = ls[k];
+                } else {
+                    r0 = ldg4(&sb.rec0[c]);
+                    r1 = ldg4(&sb.rec1[c]);
+                    l = lamp[c];
                 }
-                pj_push_smem(An, ok, a, b, o);
+                a = __float_as_int(r1.z);
+                b = __float_as_int(r1.w);
+                float4 va, wa, vb, wb;
+                ldcg_body(&Gc[2 * b], vb, wb);
+                if (a >= 0) {
+                    ldcg_body(&Gc[2 * a], va, wa);
+                } else {
+                    va = make_float4(0.f, 0.f, 0.f, 0.f);
+                    wa = va;
+                }
+                pj_contact(r0, r1, l, va, wa, vb, wb, &sb.bias[c], alpha, o);
+                if (local)
+                    ls[k] = o.lam;
+                else
+                    lamp[c] = o.lam;
+                maxd2 = fmaxf(maxd2, o.dn2);
+                maxl = fmaxf(maxl, o.lm);
             }
+            pj_push<2>(Gn, ok, a, b, o);
         }
+        for (int i = tid; i < nb; i += NT) {
+            const float4 v0 = ldg4(&sb.vel4[2 * (b0 + i)]), w0 = ldg4(&sb.vel4[2 * (b0 + i) + 1]);
+            stcg_body(&Gr[2 * (b0 + i)], v0, w0);
+        }
+        // the barriers below also order this sweep's reductions before the next sweep's gathers
         block_max2(maxd2, maxl);
         if (tid == 0) s_r = sweep_residual(maxd2, maxl);
         __syncthreads();
         r = s_r;
         ++it;
-        float4* t = Ac;
-        Ac = An;
-        An = t;
-        const bool stop = it >= max_iter || (tol > 0.f && r <= tol) || !(r == r);
-        if (stop) break;
-        for (int i = tid; i < 2 * nb; i += NT) An[i] = sb.vel4[2 * b0 + i];
-        __syncthreads();
+        if (it >= max_iter || (tol > 0.f && r <= tol) || !(r == r)) break;
     }
-    for (int i = tid; i < 2 * nb; i += NT) sb.acc[0][2 * b0 + i] = Ac[i];
+    // the final velocities to accumulator 0, where the final FP64 pass reads them
+    if (it % 3 != 0) {
+        const float4* Gf = sb.acc[it % 3];
+        for (int i = tid; i < nb; i += NT) {
+            float4 v0, w0;
+            ldcg_body(&Gf[2 * (b0 + i)], v0, w0);
+            stcg_body(&sb.acc[0][2 * (b0 + i)], v0, w0);
+        }
+    }
     if (local)
         for (int k = tid; k < nc; k += NT) lamp[k < ns ? cs0 + k : cp0 + (k - ns)] = ls[k];
     if (tid == 0) {
@@ -1469,14 +1451,16 @@ constexpr int N_COOP = sizeof(g_coop) / sizeof(g_coop[0]);
 // Batched scenes (one block per scene): threads per block and contacts per thread per pass.
 struct ScenesVariant {
     void (*kernel)(Scene, SplitBuf, int, float, int, float, const int32_t*, const int32_t*, const int32_t*,
-                   const int32_t*, int, int, int);
-    int nth, unroll, csm;
+                   const int32_t*, int, int);
+    int nth, csm;
     int smem_set;  // dynamic shared memory the kernel has been opted in to
 };
+// measured on 4,096 scenes of 16-512 spheres (1.25 M contacts, 50 sweeps): records from L1/L2 with
+// 256 threads 2.49 ms a step, records in shared memory 2.66 ms (fewer blocks fit), 128 threads 2.84
 static ScenesVariant g_scenes[] = {
-    {k_s_solve_scenes<128, 1, 1>, 128, 1, 1, 0}, {k_s_solve_scenes<256, 1, 1>, 256, 1, 1, 0},
-    {k_s_solve_scenes<64, 1, 1>, 64, 1, 1, 0},   {k_s_solve_scenes<128, 1, 0>, 128, 1, 0, 0},
-    {k_s_solve_scenes<256, 1, 0>, 256, 1, 0, 0},
+    {k_s_solve_scenes<256, 0>, 256, 0, 0},
+    {k_s_solve_scenes<256, 1>, 256, 1, 0},
+    {k_s_solve_scenes<128, 0>, 128, 0, 0},
 };
 constexpr int N_SCENES = sizeof(g_scenes) / sizeof(g_scenes[0]);
 
@@ -1500,7 +1484,7 @@ const char* split_variant_name(int v) {
                      cv.unroll, cv.agg);
         } else {
             const ScenesVariant& cv = g_scenes[v - N_STREAM - N_COOP];
-            snprintf(names[v], sizeof(names[v]), "scenes-t%d-u%d-c%d", cv.nth, cv.unroll, cv.csm);
+            snprintf(names[v], sizeof(names[v]), "scenes-t%d-c%d", cv.nth, cv.csm);
         }
     }
     return names[v];
@@ -1511,11 +1495,11 @@ int launch_s_solve_scenes(const Scene& sc, const SplitBuf& sb, int gen, float al
                           int nbmax, cudaStream_t s) {
     if (!split_variant_is_scenes(v) || sc.nscenes <= 0) return (int)cudaErrorInvalidValue;
     ScenesVariant& cv = g_scenes[v - N_STREAM - N_COOP];
-    // shared memory: two accumulators (64 B a body) and, for the contact-resident shapes, 48 B for
-    // each of up to 4 contacts a body (a settled pile has about 2); larger scenes fall back to L1/L2
-    int ccap = cv.csm ? 4 * nbmax : 0;
-    if (64 * nbmax + 48 * ccap > 227 * 1024) ccap = 0;
-    const int smem = 64 * nbmax + 48 * ccap;
+    // shared memory (contact-resident shapes): 48 B for each of up to 3 contacts a body (a settled
+    // pile has about 2.3); larger scenes read their records from L1/L2
+    int ccap = cv.csm ? 3 * nbmax : 0;
+    if (48 * ccap > 227 * 1024) ccap = 0;
+    const int smem = 48 * ccap;
     if (smem > 227 * 1024) return (int)cudaErrorInvalidValue;
     if (smem > 48 * 1024 && smem > cv.smem_set) {
         cudaError_t e = cudaFuncSetAttribute(cv.kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
@@ -1523,7 +1507,7 @@ int launch_s_solve_scenes(const Scene& sc, const SplitBuf& sb, int gen, float al
         cv.smem_set = smem;
     }
     cv.kernel<<<sc.nscenes, cv.nth, smem, s>>>(sc, sb, gen, alpha, max_iter, tol, spos, sflags, poff, order,
-                                              sc.max_statics, nbmax, ccap);
+                                              sc.max_statics, ccap);
     return (int)cudaGetLastError();
 }
 

@@ -303,7 +303,7 @@ def test_per_scene_solver_on_overflowing_device_counted_steps(gpu):
     # the per-scene kernel (pinned) on device-counted steps whose contacts outgrow the buffers (a
     # step that overflowed them solves nothing and is redone); the run matches host-counted steps
     names = PhysicsEngine.split_variants()
-    v = names.index("scenes-t128-u1-c1")
+    v = names.index("scenes-t256-c1")
     s = scenes.generate("pile_1k")
     base = dict(scenes.config_for("pile_1k"), **{"gpu.precision": "split", "gpu.contact_capacity": 0.1,
                                                  "gpu.sweep_variant": v})
