@@ -359,7 +359,18 @@ __global__ void k_s_pairs(Scene sc, Grid gr, SplitBuf sb, const uint32_t* cell_b
     }
     int list[MAX_PAIR];
     int cnt = 0;
-    for (int dz = -1; dz <= 1; ++dz) {
+    // the write pass takes the partners the count pass kept when they all fitted; the count comes
+    // from the offsets it was scanned into (the same walk, the same test, so the same partners)
+    bool walk = true;
+    if (WRITE) {
+        const int kept = offsets[i + 1] - offsets[i];
+        if (kept <= SPLIT_PLIST) {
+            for (int k = 0; k < kept; ++k) list[k] = sb.plist[(size_t)i * SPLIT_PLIST + k];
+            cnt = kept;
+            walk = false;
+        }
+    }
+    for (int dz = -1; dz <= 1 && walk; ++dz) {
         const int z = ci[2] + dz;
         if (z < 0 || z >= gr.dim[2]) continue;
         for (int dy = -1; dy <= 1; ++dy) {
@@ -389,6 +400,8 @@ __global__ void k_s_pairs(Scene sc, Grid gr, SplitBuf sb, const uint32_t* cell_b
                 if (sc.body_scene[j] != si) continue;
                 if (WRITE) {
                     if (cnt < MAX_PAIR) list[cnt] = j;
+                } else if (cnt < SPLIT_PLIST) {
+                    sb.plist[(size_t)i * SPLIT_PLIST + cnt] = j;
                 }
                 ++cnt;
             }

@@ -63,10 +63,14 @@ struct SplitParams {
 // R = alpha / diag(W M^-1 W^T) is recomputed in the sweep from the inverse masses that come with
 // the velocity gathers: R_n = alpha / (1/mA + 1/mB), R_t = alpha / (1/mA + 1/mB + rhoA^2/IA + rhoB^2/IB).
 constexpr int SPLIT_NACC = 4;  // rotating velocity accumulators of the sweeps
+constexpr int SPLIT_PLIST = 8;  // partners a body keeps from the count pass
 struct SplitBuf {
     int N = 0;
     int64_t cap = 0;
     float4* pos4 = nullptr;   // N: position relative to the scene origin, radius
+    // SPLIT_PLIST per body: the partners the narrow phase's count pass found (when they fit), so
+    // the write pass does not walk the neighbour cells again
+    int32_t* plist = nullptr;
     float4* vel4 = nullptr;   // 2N: free velocities (v_free, 1/m), (omega_free world, 1/I)
     // 2N each, rotating by sweep k: gather A[k % 4], add into A[(k + 1) % 4], reset A[(k + 3) % 4]
     // (read in sweep k - 1, next added into in sweep k + 2) to the free velocities
