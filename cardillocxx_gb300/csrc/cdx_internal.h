@@ -189,15 +189,17 @@ void launch_static_flags64(const Scene& sc, double margin, int32_t* flags, cudaS
 // FP32 copy of the positions (relative to the grid origin) and radii: the pair kernels' conservative
 // pre-test, so that only pairs near contact reach the FP64 test
 void launch_pos32(const Scene& sc, const Grid& g, float4* p32, cudaStream_t s);
+// plist: PLIST64 partners per sphere, filled by the count pass and read by the write pass
+constexpr int PLIST64 = 8;
 void launch_pair_count64(const Scene& sc, const Grid& g, const uint32_t* cell_body, const int32_t* cell_start,
-                         const int32_t* cell_end, const float4* p32, double margin, int32_t* counts, DevScalars* ds,
-                         cudaStream_t s);
+                         const int32_t* cell_end, const float4* p32, int32_t* plist, double margin, int32_t* counts,
+                         DevScalars* ds, cudaStream_t s);
 void launch_static_write64(const Scene& sc, double margin, const int32_t* flags, const int32_t* pos,
                            Contacts& C, int gen, int combine, int friction_enable, cudaStream_t s);
 void launch_pair_write64(const Scene& sc, const Grid& g, const uint32_t* cell_body, const int32_t* cell_start,
-                         const int32_t* cell_end, const float4* p32, double margin, const int32_t* offsets,
-                         int32_t base, Contacts& C, int gen, int combine, int friction_enable, DevScalars* ds,
-                         cudaStream_t s);
+                         const int32_t* cell_end, const float4* p32, int32_t* plist, double margin,
+                         const int32_t* offsets, int32_t base, Contacts& C, int gen, int combine, int friction_enable,
+                         DevScalars* ds, cudaStream_t s);
 void launch_contact_setup64(const Scene& sc, Contacts& C, int gen, int nc, int prev_count, double alpha,
                             double match2, int warmstart, cudaStream_t s);
 void launch_frictionless_flags(const Contacts& C, int nc, int32_t* isfl, cudaStream_t s);

@@ -268,6 +268,7 @@ int Engine::load_scene(const cdx_scene& s) {
     if ((st = dalloc((void**)&cell_key_out, sizeof(uint32_t) * std::max(1, N), "grid"))) return st;
     if ((st = dalloc((void**)&cell_val_out, sizeof(uint32_t) * std::max(1, N), "grid"))) return st;
     if ((st = dalloc((void**)&pos32, sizeof(float4) * std::max(1, N), "grid"))) return st;
+    if ((st = dalloc((void**)&plist64, sizeof(int32_t) * PLIST64 * std::max(1, N), "grid"))) return st;
     if ((st = dalloc((void**)&cell_start, sizeof(int32_t) * ncells, "grid"))) return st;
     if ((st = dalloc((void**)&cell_end, sizeof(int32_t) * ncells, "grid"))) return st;
     const int64_t nflag = (int64_t)std::max(1, N) * std::max(1, maxst);
@@ -416,7 +417,7 @@ int Engine::collide64() {
         launches += 2;
     }
     launch_pos32(sc, grid, pos32, stream);
-    launch_pair_count64(sc, grid, cell_val_out, cell_start, cell_end, pos32, margin, pcount, ds, stream);
+    launch_pair_count64(sc, grid, cell_val_out, cell_start, cell_end, pos32, plist64, margin, pcount, ds, stream);
     launches += 2;
     if ((st = cuda_check(exclusive_scan(tmp, tmp_bytes, pcount, poff, N + 1, stream), "scan"))) return st;
     launches += 2;
@@ -439,7 +440,8 @@ int Engine::collide64() {
         ++launches;
     }
     if (n_pair > 0) {
-        launch_pair_write64(sc, grid, cell_val_out, cell_start, cell_end, pos32, margin, poff, (int32_t)n_static, C, gen,
+        launch_pair_write64(sc, grid, cell_val_out, cell_start, cell_end, pos32, plist64, margin, poff,
+                            (int32_t)n_static, C, gen,
                             cfg.friction_combine, cfg.friction_enable, ds, stream);
         ++launches;
     }

@@ -50,6 +50,7 @@ struct Engine {
     double* stage = nullptr;  // 13 N doubles: state staging for get/set_state
     uint32_t *cell_key_in = nullptr, *cell_val_in = nullptr, *cell_key_out = nullptr, *cell_val_out = nullptr;
     float4* pos32 = nullptr;  // plain FP64 method: FP32 positions and radii for the pair pre-test
+    int32_t* plist64 = nullptr;  // plain FP64 method: partners kept by the narrow phase's count pass
     int32_t *cell_start = nullptr, *cell_end = nullptr;
     int32_t *sflags = nullptr, *spos = nullptr, *pcount = nullptr, *poff = nullptr;
     int32_t *sflags_prev = nullptr, *spos_prev = nullptr, *poff_prev = nullptr;  // split form warm start

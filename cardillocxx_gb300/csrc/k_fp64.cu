@@ -303,8 +303,8 @@ __device__ __forceinline__ bool pair_near32(float4 pi, float ei, float4 pj, floa
 
 template <bool WRITE>
 __global__ void k_pairs64(Scene sc, Grid gr, const uint32_t* cell_body, const int32_t* cell_start,
-                          const int32_t* cell_end, const float4* p32, double margin, int32_t* counts,
-                          const int32_t* offsets, int32_t base, Contacts C, int gen, int combine,
+                          const int32_t* cell_end, const float4* p32, int32_t* plist, double margin,
+                          int32_t* counts, const int32_t* offsets, int32_t base, Contacts C, int gen, int combine,
                           int friction_enable, DevScalars* ds) {
     // threads take the spheres in cell order, so a warp walks neighbouring cells; each sphere's
     // count and contacts are its own (same values, written at its own offset)
@@ -321,7 +321,18 @@ __global__ void k_pairs64(Scene sc, Grid gr, const uint32_t* cell_body, const in
     cell_of(gr, xi[0], xi[1], xi[2], ci);
     int list[MAX_PAIR];
     int cnt = 0;
-    for (int dz = -1; dz <= 1; ++dz) {
+    // the write pass takes the partners the count pass kept when they all fitted (the same walk
+    // and the same tests found them); the count comes from the scanned offsets
+    bool walk = true;
+    if (WRITE) {
+        const int kept = offsets[i + 1] - offsets[i];
+        if (kept <= PLIST64) {
+            for (int k = 0; k < kept; ++k) list[k] = plist[(size_t)i * PLIST64 + k];
+            cnt = kept;
+            walk = false;
+        }
+    }
+    for (int dz = -1; dz <= 1 && walk; ++dz) {
         const int z = ci[2] + dz;
         if (z < 0 || z >= gr.dim[2]) continue;
         for (int dy = -1; dy <= 1; ++dy) {
@@ -340,6 +351,8 @@ __global__ void k_pairs64(Scene sc, Grid gr, const uint32_t* cell_body, const in
                     if (!pair_touch(xi, ri, xj, sc.bf(BF_RAD)[j], margin)) continue;
                     if (WRITE) {
                         if (cnt < MAX_PAIR) list[cnt] = j;
+                    } else if (cnt < PLIST64) {
+                        plist[(size_t)i * PLIST64 + cnt] = j;
                     }
                     ++cnt;
                 }
@@ -1353,12 +1366,12 @@ void launch_pos32(const Scene& sc, const Grid& g, float4* p32, cudaStream_t s) {
     if (sc.N) k_pos32<<<nblk(sc.N), NT, 0, s>>>(sc, g, p32);
 }
 void launch_pair_count64(const Scene& sc, const Grid& g, const uint32_t* cell_body, const int32_t* cell_start,
-                         const int32_t* cell_end, const float4* p32, double margin, int32_t* counts, DevScalars* ds,
-                         cudaStream_t s) {
+                         const int32_t* cell_end, const float4* p32, int32_t* plist, double margin, int32_t* counts,
+                         DevScalars* ds, cudaStream_t s) {
     if (sc.N == 0) return;
     Contacts dummy;
-    k_pairs64<false><<<nblk(sc.N), NT, 0, s>>>(sc, g, cell_body, cell_start, cell_end, p32, margin, counts, nullptr,
-                                                0, dummy, 0, 0, 0, ds);
+    k_pairs64<false><<<nblk(sc.N), NT, 0, s>>>(sc, g, cell_body, cell_start, cell_end, p32, plist, margin, counts,
+                                                nullptr, 0, dummy, 0, 0, 0, ds);
 }
 void launch_static_write64(const Scene& sc, double margin, const int32_t* flags, const int32_t* pos,
                            Contacts& C, int gen, int combine, int friction_enable, cudaStream_t s) {
@@ -1366,12 +1379,12 @@ void launch_static_write64(const Scene& sc, double margin, const int32_t* flags,
     k_static_write64<<<nblk(sc.N), NT, 0, s>>>(sc, margin, flags, pos, C, gen, combine, friction_enable);
 }
 void launch_pair_write64(const Scene& sc, const Grid& g, const uint32_t* cell_body, const int32_t* cell_start,
-                         const int32_t* cell_end, const float4* p32, double margin, const int32_t* offsets,
-                         int32_t base, Contacts& C, int gen, int combine, int friction_enable, DevScalars* ds,
-                         cudaStream_t s) {
+                         const int32_t* cell_end, const float4* p32, int32_t* plist, double margin,
+                         const int32_t* offsets, int32_t base, Contacts& C, int gen, int combine, int friction_enable,
+                         DevScalars* ds, cudaStream_t s) {
     if (sc.N == 0) return;
-    k_pairs64<true><<<nblk(sc.N), NT, 0, s>>>(sc, g, cell_body, cell_start, cell_end, p32, margin, nullptr, offsets,
-                                               base, C, gen, combine, friction_enable, ds);
+    k_pairs64<true><<<nblk(sc.N), NT, 0, s>>>(sc, g, cell_body, cell_start, cell_end, p32, plist, margin, nullptr,
+                                               offsets, base, C, gen, combine, friction_enable, ds);
 }
 void launch_contact_setup64(const Scene& sc, Contacts& C, int gen, int nc, int prev_count, double alpha,
                             double match2, int warmstart, cudaStream_t s) {
