@@ -1014,8 +1014,9 @@ __global__ void __launch_bounds__(NTH, 1) k_s_solve_coop(SplitBuf sb, int gen, f
 // contact, up to ccap contacts; a larger scene reads them from L1/L2 every sweep).
 // The final velocities go to accumulator 0; the largest per-scene sweep count and residual go to
 // the step's scalars.
+// 1024 / NT blocks an SM at least: 64 registers a thread, 32 warps an SM
 template <int NT, int CSM>
-__global__ void __launch_bounds__(NT) k_s_solve_scenes(Scene sc, SplitBuf sb, int gen, float alpha, int max_iter,
+__global__ void __launch_bounds__(NT, 1024 / NT) k_s_solve_scenes(Scene sc, SplitBuf sb, int gen, float alpha, int max_iter,
                                                        float tol, const int32_t* spos, const int32_t* sflags,
                                                        const int32_t* poff, const int32_t* order, int L, int ccap) {
     extern __shared__ float4 sm4[];
@@ -1468,12 +1469,13 @@ struct ScenesVariant {
     int nth, csm;
     int smem_set;  // dynamic shared memory the kernel has been opted in to
 };
-// measured on 4,096 scenes of 16-512 spheres (1.25 M contacts, 50 sweeps): records from L1/L2 with
-// 256 threads 2.49 ms a step, records in shared memory 2.66 ms (fewer blocks fit), 128 threads 2.84
+// measured on 4,096 scenes of 16-512 spheres (1.25 M contacts, 50 sweeps), 64 registers a thread:
+// records from L1/L2 with 128 threads 2.29 ms a step, with 256 threads 2.44, with 64 threads 2.72;
+// records in shared memory 2.58 (fewer blocks fit)
 static ScenesVariant g_scenes[] = {
+    {k_s_solve_scenes<128, 0>, 128, 0, 0},
     {k_s_solve_scenes<256, 0>, 256, 0, 0},
     {k_s_solve_scenes<256, 1>, 256, 1, 0},
-    {k_s_solve_scenes<128, 0>, 128, 0, 0},
 };
 constexpr int N_SCENES = sizeof(g_scenes) / sizeof(g_scenes[0]);
 
