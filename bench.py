@@ -59,6 +59,10 @@ def parse():
                    help="pin the split-form solver shape (index or name; default: autotuned)")
     p.add_argument("--save-state", default=None, help="write the settled state (npz) and continue")
     p.add_argument("--load-state", default=None, help="start from a settled state written by --save-state")
+    p.add_argument("--adjoint", action="store_true",
+                   help="time the differentiable rollout (forward with checkpoints, then the adjoint) of "
+                        "--scene (default diff_256x256) over --rollout-steps steps instead of the step bench")
+    p.add_argument("--rollout-steps", type=int, default=200)
     p.add_argument("--set", action="append", default=[], metavar="KEY=VALUE",
                    help="extra configuration key for the timed engine (repeatable), e.g. gpu.coop_blocks=8")
     return p.parse_args()
@@ -421,6 +425,47 @@ def run_reference(a, log):
     print(json.dumps(out), flush=True)
 
 
+def run_adjoint(a, log):
+    """The differentiation workload: 256 scenes of 256 spheres, a COM loss on the final state,
+    gradients w.r.t. the initial state and the per-scene friction through the adjoint kernels
+    (checkpoints every 20 steps). Prints one JSON line with the forward and adjoint wall times
+    (both calls return after the device finished)."""
+    import numpy as np
+    from cardillocxx_gb300 import scenes
+    from cardillocxx_gb300.adjoint import Rollout
+    name = a.scene if a.scene != "pile_200k" else "diff_256x256"
+    s = scenes.generate(name, scale=a.scale)
+    cfg = scenes.config_for(name)
+    nsc = int(s["num_scenes"])
+    sc, m = s["body_scene"], s["mass"]
+    M = np.bincount(sc, weights=m, minlength=nsc)
+    target = np.random.default_rng(6).uniform((0.2, 0.2, 0.1), (0.8, 0.8, 0.5), size=(nsc, 3))
+    R = Rollout(s, cfg, checkpoint_every=20)
+    mu = np.full(nsc, 0.3)
+    T = a.rollout_steps
+    fwd, bwd = [], []
+    for k in range(a.warmup + a.steps):
+        t0 = time.perf_counter()
+        xT, _, _ = R.forward(T, s["pos"], s["vel"], s["omega"], mu)
+        t1 = time.perf_counter()
+        com = np.stack([np.bincount(sc, weights=m * xT[:, q], minlength=nsc) for q in range(3)], 1) / M[:, None]
+        gx = 2 * (com - target)[sc] * (m / M[sc])[:, None]
+        t2 = time.perf_counter()
+        R.backward(gx, np.zeros_like(gx), np.zeros_like(gx))
+        t3 = time.perf_counter()
+        if k >= a.warmup:
+            fwd.append(1e3 * (t1 - t0))
+            bwd.append(1e3 * (t3 - t2))
+        log(f"rollout {k}: forward {1e3 * (t1 - t0):.1f} ms, adjoint {1e3 * (t3 - t2):.1f} ms")
+    f, b = float(np.median(fwd)), float(np.median(bwd))
+    print(json.dumps({"metric": "differentiable rollout ms (forward with checkpoints + adjoint)",
+                      "value": f + b, "unit": "ms", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
+                      "higher_is_better": False, "dtype": "f64", "data": f"synthetic: seeded {name}",
+                      "config": {"workload": name, "scenes": nsc, "bodies": int(s["pos"].shape[0]),
+                                 "rollout_steps": T, "checkpoint_every": 20, "info": R.info()},
+                      "forward_ms": f, "adjoint_ms": b}), flush=True)
+
+
 def main():
     a = parse()
     if a.gpus > 1 and "LOCAL_RANK" in os.environ:
@@ -433,6 +478,8 @@ def main():
 
     if a.impl == "reference":
         run_reference(a, log)
+    elif a.adjoint:
+        run_adjoint(a, log)
     else:
         run_cdx(a, log)
 

@@ -302,14 +302,19 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adj_step(AdjProblem P, AdjStep 
         nc += tot;
         __syncthreads();
     }
-    // sphere pairs in (i, j) order, i < j
+    // sphere pairs in (i, j) order, i < j. A pair farther apart than (r_i + r_j + |margin|)
+    // (1 + 1e-9) in squared distance cannot pass the exact test (its rounding errors are below
+    // 1e-15 relative), so the square root is taken only for near pairs; the same d2 feeds it.
     for (int i = t; i < nb; i += T) {
         int n = 0;
         const double ri = P.rad[b0 + i];
         for (int j = i + 1; j < nb; ++j) {
             double d[3];
             for (int k = 0; k < 3; ++k) d[k] = S.Y[3 * j + k] - S.Y[3 * i + k];
-            const double L = sqrt(dot3(d, d));
+            const double d2 = dot3(d, d);
+            const double lim = (ri + P.rad[b0 + j] + fabs(P.margin)) * (1.0 + 1e-9);
+            if (d2 > lim * lim) continue;
+            const double L = sqrt(d2);
             if ((L - ri) - P.rad[b0 + j] <= P.margin && L > 0.0) ++n;
         }
         S.cnt[i] = n;
@@ -322,8 +327,11 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adj_step(AdjProblem P, AdjStep 
         for (int j = i + 1; j < nb; ++j) {
             double d[3];
             for (int q = 0; q < 3; ++q) d[q] = S.Y[3 * j + q] - S.Y[3 * i + q];
-            const double L = sqrt(dot3(d, d));
             const double rj = P.rad[b0 + j];
+            const double d2 = dot3(d, d);
+            const double lim = (ri + rj + fabs(P.margin)) * (1.0 + 1e-9);
+            if (d2 > lim * lim) continue;
+            const double L = sqrt(d2);
             if (!((L - ri) - rj <= P.margin && L > 0.0)) continue;
             if (k < cap) {
                 const int c = c0 + k;
