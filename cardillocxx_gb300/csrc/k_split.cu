@@ -1264,18 +1264,18 @@ __global__ void k_s_residual(Scene sc, SplitBuf sb, int gen, double alpha, int f
             dv[k] = sb.acc64[(size_t)k * N + ab.y];
             Om[k] = rB * sb.acc64[(size_t)(3 + k) * N + ab.y];
         }
-        double ima = 0.0, iia = 0.0;
         if (ab.x >= 0) {
             for (int k = 0; k < 3; ++k) {
                 dv[k] -= sb.acc64[(size_t)k * N + ab.x];
                 Om[k] -= rA * sb.acc64[(size_t)(3 + k) * N + ab.x];
             }
-            ima = sc.bf(BF_MINVL)[ab.x];
-            iia = sc.bf(BF_MINVA)[ab.x];
         }
-        const double imb = sc.bf(BF_MINVL)[ab.y], iib = sc.bf(BF_MINVA)[ab.y];
-        const double Dn = ima + imb, Dt = Dn + rA * rA * iia + rB * rB * iib;
-        const double Rn = Dn > 0 ? alpha * rcp_nr(Dn) : 0.0, Rt = Dt > 0 ? alpha * rcp_nr(Dt) : 0.0;
+        // R only scales the residual (which impulses are fixed points does not depend on it): the
+        // solver's own FP32 R, from the same lever lengths and inverse masses as the sweeps
+        const float imaf = ab.x >= 0 ? sb.vel4[2 * ab.x].w : 0.f, iiaf = ab.x >= 0 ? sb.vel4[2 * ab.x + 1].w : 0.f;
+        float Rn32, Rt32;
+        pj_rdiag(r1.x, r1.y, imaf, iiaf, sb.vel4[2 * ab.y].w, sb.vel4[2 * ab.y + 1].w, (float)alpha, Rn32, Rt32);
+        const double Rn = Rn32, Rt = Rt32;
         double g[3];
         g[0] = n[0] * dv[0] + n[1] * dv[1] + n[2] * dv[2];
         g[1] = (t1[0] * dv[0] + t1[1] * dv[1] + t1[2] * dv[2]) + (t2[0] * Om[0] + t2[1] * Om[1] + t2[2] * Om[2]);
