@@ -597,9 +597,8 @@ int Engine::step_split() {
     if (S->scene_timing >= 0) cudaEventRecord(S->tev[1], stream);
     if (timing) cudaEventRecord(ev[3], stream);
     // FP64: final velocities, residual, write back, drift theta h
-    launch_s_final(sc, sb, gen, cfg.pj_alpha, cfg.friction_enable, cfg.friction_combine, cblocks, stream);
-    launch_s_drift(sc, th * dt, stream);
-    launches += 5;
+    launch_s_final(sc, sb, gen, cfg.pj_alpha, cfg.friction_enable, cfg.friction_combine, cblocks, th * dt, stream);
+    launches += 4;
     if (timing) cudaEventRecord(ev[4], stream);
     launch_s_end_step(sb, ds, stream);
     ++launches;

@@ -1367,14 +1367,27 @@ __global__ void k_s_residual(Scene sc, SplitBuf sb, int gen, double alpha, int f
     }
 }
 
-__global__ void k_s_drift(Scene sc, double h) {
+// the write-back fused with the closing drift theta h (moreau.cpp:12): the new velocities go to the
+// state and move the positions and orientations without a second pass over the bodies
+__global__ void k_s_writeback_drift(Scene sc, SplitBuf sb, double h) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < sc.N) {
+        const int N = sc.N;
+        double R[9];
+        for (int k = 0; k < 9; ++k) R[k] = sc.bf(BF_R0 + k)[i];
+        const double ww[3] = {sb.acc64[3 * (size_t)N + i], sb.acc64[4 * (size_t)N + i], sb.acc64[5 * (size_t)N + i]};
+        double wb[3];
+        f64::matTvec(R, ww, wb);
+        const double v[3] = {sb.acc64[i], sb.acc64[(size_t)N + i], sb.acc64[2 * (size_t)N + i]};
+        sc.bf(BF_VX)[i] = v[0];
+        sc.bf(BF_VY)[i] = v[1];
+        sc.bf(BF_VZ)[i] = v[2];
+        sc.bf(BF_WX)[i] = wb[0];
+        sc.bf(BF_WY)[i] = wb[1];
+        sc.bf(BF_WZ)[i] = wb[2];
         double x[3] = {sc.bf(BF_PX)[i], sc.bf(BF_PY)[i], sc.bf(BF_PZ)[i]};
         double q[4] = {sc.bf(BF_QX)[i], sc.bf(BF_QY)[i], sc.bf(BF_QZ)[i], sc.bf(BF_QW)[i]};
-        const double v[3] = {sc.bf(BF_VX)[i], sc.bf(BF_VY)[i], sc.bf(BF_VZ)[i]};
-        const double w[3] = {sc.bf(BF_WX)[i], sc.bf(BF_WY)[i], sc.bf(BF_WZ)[i]};
-        drift_fast(x, q, v, w, h);
+        drift_fast(x, q, v, wb, h);
         sc.bf(BF_PX)[i] = x[0]; sc.bf(BF_PY)[i] = x[1]; sc.bf(BF_PZ)[i] = x[2];
         sc.bf(BF_QX)[i] = q[0]; sc.bf(BF_QY)[i] = q[1]; sc.bf(BF_QZ)[i] = q[2]; sc.bf(BF_QW)[i] = q[3];
     } else if (i < sc.N + sc.S) {
@@ -1387,24 +1400,6 @@ __global__ void k_s_drift(Scene sc, double h) {
         sc.sf(SF_PX)[s] = x[0]; sc.sf(SF_PY)[s] = x[1]; sc.sf(SF_PZ)[s] = x[2];
         sc.sf(SF_QX)[s] = q[0]; sc.sf(SF_QY)[s] = q[1]; sc.sf(SF_QZ)[s] = q[2]; sc.sf(SF_QW)[s] = q[3];
     }
-}
-
-// write the FP64 velocities back into the state (angular velocity to the body frame)
-__global__ void k_s_writeback(Scene sc, SplitBuf sb) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= sc.N) return;
-    const int N = sc.N;
-    double R[9];
-    for (int k = 0; k < 9; ++k) R[k] = sc.bf(BF_R0 + k)[i];
-    const double ww[3] = {sb.acc64[3 * (size_t)N + i], sb.acc64[4 * (size_t)N + i], sb.acc64[5 * (size_t)N + i]};
-    double wb[3];
-    f64::matTvec(R, ww, wb);
-    sc.bf(BF_VX)[i] = sb.acc64[i];
-    sc.bf(BF_VY)[i] = sb.acc64[(size_t)N + i];
-    sc.bf(BF_VZ)[i] = sb.acc64[2 * (size_t)N + i];
-    sc.bf(BF_WX)[i] = wb[0];
-    sc.bf(BF_WY)[i] = wb[1];
-    sc.bf(BF_WZ)[i] = wb[2];
 }
 
 __global__ void k_s_final_scalar(SplitBuf sb) {
@@ -1646,14 +1641,11 @@ void launch_s_sweep(const SplitBuf& sb, int gen, float alpha, int variant, int b
     const StreamVariant& cv = g_stream[(variant >= 0 && variant < N_STREAM) ? variant : 0];
     cv.kernel<<<blocks, cv.nth, 0, s>>>(sb, gen, alpha, max_iter, tol, h, use_handle);
 }
-void launch_s_drift(const Scene& sc, double h, cudaStream_t s) {
-    if (sc.N + sc.S > 0) k_s_drift<<<nblk(sc.N + sc.S), NT, 0, s>>>(sc, h);
-}
 void launch_s_final(const Scene& sc, const SplitBuf& sb, int gen, double alpha, int friction_enable, int combine,
-                    int blocks, cudaStream_t s) {
+                    int blocks, double drift_h, cudaStream_t s) {
     if (sc.N > 0) k_s_final_body<<<nblk(sc.N), NT, 0, s>>>(sc, sb);
     k_s_residual<<<blocks, NT, 0, s>>>(sc, sb, gen, alpha, friction_enable, combine);
-    if (sc.N > 0) k_s_writeback<<<nblk(sc.N), NT, 0, s>>>(sc, sb);
+    if (sc.N + sc.S > 0) k_s_writeback_drift<<<nblk(sc.N + sc.S), NT, 0, s>>>(sc, sb, drift_h);
     k_s_final_scalar<<<1, 1, 0, s>>>(sb);
 }
 

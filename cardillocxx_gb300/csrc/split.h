@@ -151,8 +151,8 @@ void launch_s_apply_warm(const SplitBuf& sb, int gen, int blocks, cudaStream_t s
 // clears A_{k+2}; its last block runs the stop rule
 void launch_s_sweep(const SplitBuf& sb, int gen, float alpha, int variant, int blocks, int max_iter, float tol,
                     cudaGraphConditionalHandle h, int use_handle, cudaStream_t s);
-void launch_s_drift(const Scene& sc, double h, cudaStream_t s);
+// final FP64 velocities, residual, write-back and the closing drift by drift_h
 void launch_s_final(const Scene& sc, const SplitBuf& sb, int gen, double alpha, int friction_enable, int combine,
-                    int blocks, cudaStream_t s);
+                    int blocks, double drift_h, cudaStream_t s);
 
 }  // namespace cdx
