@@ -72,6 +72,8 @@ class CdxConfig(C.Structure):
         ("output_filename_prefix", C.c_char * 128),
         ("gpu_coop_smem_contacts", C.c_int32),
         ("gpu_coop_blocks", C.c_int32),
+        ("gpu_pad0", C.c_int32),
+        ("gpu_coop_wait_ns", C.c_int64),
     ]
 
 
@@ -152,6 +154,8 @@ SIGNATURES = [
     ("cdx_set_state", C.c_int, [C.c_void_p, _P, _P, _P, _P]),
     ("cdx_get_stats", C.c_int, [C.c_void_p, C.POINTER(CdxStats)]),
     ("cdx_get_contacts", C.c_int, [C.c_void_p, _PI, _PI, _P, _P, _P, _PI]),
+    ("cdx_set_contacts", C.c_int, [C.c_void_p, C.c_int32, _PI, _PI, _P, _P]),
+    ("cdx_set_config", C.c_int, [C.c_void_p, C.POINTER(CdxConfig)]),
     ("cdx_track", C.c_int, [C.c_void_p, C.c_int32, C.c_char_p]),
     ("cdx_output_flush", C.c_int, [C.c_void_p]),
     ("cdx_set_trace", C.c_int, [C.c_void_p, C.c_int32]),

@@ -24,6 +24,11 @@ int cdx_create(const cdx_config* cfg, cdx_ctx** out) {
 
 void cdx_destroy(cdx_ctx* ctx) { delete ctx; }
 
+int cdx_set_config(cdx_ctx* ctx, const cdx_config* cfg) {
+    if (!ctx || !cfg) return CDX_ERR_ARG;
+    return ctx->eng.set_config(*cfg);
+}
+
 const char* cdx_last_error(const cdx_ctx* ctx) { return ctx ? ctx->eng.err.c_str() : "null context"; }
 
 int cdx_load_scene(cdx_ctx* ctx, const cdx_scene* scene) {
@@ -69,6 +74,16 @@ int cdx_get_contacts(cdx_ctx* ctx, int32_t* id_a, int32_t* id_b, double* point, 
                      int32_t* count) {
     if (!ctx) return CDX_ERR_ARG;
     return ctx->eng.get_contacts(id_a, id_b, point, lambda, normal, count);
+}
+
+int cdx_set_contacts(cdx_ctx* ctx, int32_t count, const int32_t* id_a, const int32_t* id_b, const double* point,
+                     const double* lambda) {
+    if (!ctx) return CDX_ERR_ARG;
+    try {
+        return ctx->eng.set_contacts(count, id_a, id_b, point, lambda);
+    } catch (const std::exception& e) {
+        return ctx->eng.fail(CDX_ERR_ARG, e.what());
+    }
 }
 
 int cdx_track(cdx_ctx* ctx, int32_t body, const char* name) {

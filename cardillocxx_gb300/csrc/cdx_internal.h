@@ -184,7 +184,8 @@ void launch_unpack_state(const Scene& sc, const double* in, int mask, cudaStream
 
 // ---- FP64 plain method (k_fp64.cu) ----
 void launch_rhs64(const Scene& sc, double dt, const double* g, double* rhs, cudaStream_t s, int implicit_gyro = 0);
-void launch_drift64(const Scene& sc, double h, int compute_R, cudaStream_t s);
+// nonfinite (optional): set to 1 when a body's state after the drift is not finite
+void launch_drift64(const Scene& sc, double h, int compute_R, cudaStream_t s, int32_t* nonfinite = nullptr);
 void launch_static_flags64(const Scene& sc, double margin, int32_t* flags, cudaStream_t s);
 // FP32 copy of the positions (relative to the grid origin) and radii: the pair kernels' conservative
 // pre-test, so that only pairs near contact reach the FP64 test
@@ -225,9 +226,10 @@ void launch_accel_copy(double* xd, const double* xs, int64_t nx, double* ld, con
                        const DevScalars* ds, cudaStream_t s);
 void launch_nesterov_step(AccelState* st, DevScalars* ds, int nv, double beta_threshold, int restart_limit, double* xy,
                           double* xk, const double* xk1, int64_t nx, double* py, double* pk, const double* pk1,
-                          int64_t nl, cudaStream_t s);
+                          int64_t nl, double residual_tol, cudaStream_t s);
 void launch_chebyshev_step(AccelState* st, DevScalars* ds, int nv, int iter, const double* x, double* xk, double* xk1,
-                           int64_t nx, const double* lam, double* pk, double* pk1, int64_t nl, cudaStream_t s);
+                           int64_t nx, const double* lam, double* pk, double* pk1, int64_t nl, double residual_tol,
+                           cudaStream_t s);
 int anderson_sums(int m);
 int anderson_chunks(int64_t n);
 void launch_anderson_begin(const Contacts& C, int gen, int nc, const int32_t* fl_scan, const int32_t* isfl, int N,
@@ -235,8 +237,10 @@ void launch_anderson_begin(const Contacts& C, int gen, int nc, const int32_t* fl
 void launch_anderson_begin_plain(int nv, const double* x, const double* lam, AndersonBufs& A, cudaStream_t s);
 // N: bodies (6 x N field-major velocities), or the velocity count when A.plain
 void launch_anderson_scatter(int N, double* x, double* lam, const AndersonBufs& A, const DevScalars* ds, cudaStream_t s);
+// residual_tol (gpu.residual_tol, 0 = off): the accelerated loops also end once the sweep's
+// complementarity residual is at most tol, tested right after the reference's own exit
 void launch_anderson_mix(int N, const double* x, const double* lam, const AndersonBufs& A, double tol_rel,
-                         double tol_abs, DevScalars* ds, cudaStream_t s);
+                         double tol_abs, double residual_tol, DevScalars* ds, cudaStream_t s);
 // estimateSpectralRadius's eight power steps; apply() launches Mv = M v (N bodies, or N velocities
 // when plain)
 void launch_power_iteration(int N, int plain, double* v, double* Mv, double* part, AccelState* st,

@@ -191,6 +191,8 @@ int cdx_config_set(cdx_config* c, const char* key_c, const char* val_c) {
         if (as_int(val, &i)) c->gpu_coop_smem_contacts = std::max(0, i);
     } else if (key == "gpu.coop_blocks") {
         if (as_int(val, &i)) c->gpu_coop_blocks = std::max(0, i);
+    } else if (key == "gpu.coop_wait_ns") {
+        if (as_double(val, &d) && d >= 0 && d < 9e18) c->gpu_coop_wait_ns = (int64_t)d;
     } else if (key == "gpu.sync_counts") {
         c->gpu_sync_counts = as_bool(val);
     } else if (key_is(key, "pj.nesterov")) {

@@ -80,6 +80,12 @@ int Engine::init(const cdx_config& c) {
     cfg = c;
     if (cfg.output_interval_steps > 0) out = new cdx::Output(cfg);
     if (cfg.solver_type != 0) return fail(CDX_ERR_UNSUPPORTED, "only solver.type=projected_jacobi is on this path");
+    // the split form runs the reference's Nesterov loop and the standard loop's tolerance exit in its
+    // cooperative solve; Chebyshev and Anderson (selected when Nesterov is off, as in
+    // projected_jacobi.cpp:470-491) run in the plain FP64 method only
+    if (cfg.gpu_precision == CDX_PRECISION_SPLIT && !cfg.pj_nesterov && (cfg.pj_chebyshev || cfg.pj_anderson))
+        return fail(CDX_ERR_UNSUPPORTED, "pj.chebyshev and pj.anderson run in the plain FP64 method only "
+                                         "(gpu.precision=fp64); the split form runs pj.nesterov and the standard loop");
     int st = cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
     if (st) return st;
     st = cuda_check(cudaMallocHost((void**)&hs, sizeof(DevScalars)), "cudaMallocHost");
@@ -89,6 +95,28 @@ int Engine::init(const cdx_config& c) {
         st = cuda_check(cudaEventCreate(&e), "cudaEventCreate");
         if (st) return st;
     }
+    return CDX_OK;
+}
+
+// ProjectedJacobiSolver holds a reference to the Config and reads its pj.* settings at every solve
+// (projected_jacobi.cpp:451-500), so a caller may change them between steps. Here the new settings
+// apply from the next step; the precision (which selects the buffers) and the frame output (whose
+// writer is set up at creation) stay as created.
+int Engine::set_config(const cdx_config& c) {
+    if (c.solver_type != 0) return fail(CDX_ERR_UNSUPPORTED, "only solver.type=projected_jacobi is on this path");
+    if (c.gpu_precision != cfg.gpu_precision)
+        return fail(CDX_ERR_STATE, "gpu.precision is fixed when the context is created");
+    if (c.gpu_precision == CDX_PRECISION_SPLIT && !c.pj_nesterov && (c.pj_chebyshev || c.pj_anderson))
+        return fail(CDX_ERR_UNSUPPORTED, "pj.chebyshev and pj.anderson run in the plain FP64 method only "
+                                         "(gpu.precision=fp64); the split form runs pj.nesterov and the standard loop");
+    cdx_config n = c;
+    n.output_interval_steps = cfg.output_interval_steps;
+    n.output_write_contact_manifolds = cfg.output_write_contact_manifolds;
+    std::memcpy(n.output_folder, cfg.output_folder, sizeof(n.output_folder));
+    std::memcpy(n.output_filename_prefix, cfg.output_filename_prefix, sizeof(n.output_filename_prefix));
+    if (stream) cudaStreamSynchronize(stream);
+    cfg = n;
+    split_config_changed();
     return CDX_OK;
 }
 
@@ -540,12 +568,13 @@ int Engine::solve64_accel() {
             launch_accel_reduce(N, ACC_DOT, acc_xy, acc_xk1, acc_xk, 0.0, 0.0, acc_part, acc_st, &acc_st->sum_dot,
                                 ds, stream);
             launch_nesterov_step(acc_st, ds, nv, cfg.pj_nesterov_beta_threshold, cfg.pj_nesterov_restart_limit, acc_xy,
-                                 acc_xk, acc_xk1, nx, acc_py, acc_pk, acc_pk1, nl, stream);
+                                 acc_xk, acc_xk1, nx, acc_py, acc_pk, acc_pk1, nl, cfg.gpu_residual_tol, stream);
             launches += 9;
         } else {
             launch_accel_reduce(N, ACC_VELRES, x, acc_xk1, nullptr, cfg.pj_tol_rel, cfg.pj_tol_abs, acc_part, acc_st,
                                 &acc_st->sum_err, ds, stream);
-            launch_chebyshev_step(acc_st, ds, nv, it, x, acc_xk, acc_xk1, nx, lam, acc_pk, acc_pk1, nl, stream);
+            launch_chebyshev_step(acc_st, ds, nv, it, x, acc_xk, acc_xk1, nx, lam, acc_pk, acc_pk1, nl,
+                                  cfg.gpu_residual_tol, stream);
             launches += 7;
         }
         if ((it + 1) % every == 0 && it + 1 < maxit) {
@@ -618,7 +647,7 @@ int Engine::solve64_anderson() {
         launch_sweep_contact64(sc, C, gen, nc, x, ds, 0, stream);
         launch_sweep_body64(sc, C, inc, x, 0.0, 0.0, 0, ds, stream);
         launch_check(ds, it, 0.0, nv, 0, stream);  // res_last and the sweep count
-        launch_anderson_mix(N, x, lam, anderson, cfg.pj_tol_rel, cfg.pj_tol_abs, ds, stream);
+        launch_anderson_mix(N, x, lam, anderson, cfg.pj_tol_rel, cfg.pj_tol_abs, cfg.gpu_residual_tol, ds, stream);
         launches += 12;
         if ((it + 1) % every == 0 && it + 1 < maxit) {
             cudaMemcpyAsync(&hs->done, &ds->done, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
@@ -709,6 +738,7 @@ int Engine::step64() {
     const double dt = cfg.sim_dt, th = cfg.moreau_theta;
     int st;
     if (timing) cudaEventRecord(ev[0], stream);
+    cudaMemsetAsync(&ds->nonfinite, 0, sizeof(int32_t), stream);
     launch_rhs64(sc, dt, cfg.sim_gravity, rhs, stream, cfg.moreau_implicit_gyroscopy);
     launch_drift64(sc, (1.0 - th) * dt, 1, stream);
     launches += 2;
@@ -719,7 +749,7 @@ int Engine::step64() {
     if ((st = solve64())) return st;
     if (timing) cudaEventRecord(ev[3], stream);
     launch_writeback64(sc, x, stream);
-    launch_drift64(sc, th * dt, 0, stream);
+    launch_drift64(sc, th * dt, 0, stream, &ds->nonfinite);
     launches += 2;
     if (timing) cudaEventRecord(ev[4], stream);
     cudaMemcpyAsync(hs, ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, stream);
@@ -730,6 +760,7 @@ int Engine::step64() {
     last_res_final = nc > 0 ? hs->res_final : 0.0;
     last_rows = nc > 0 ? nfl_rows() : 0;
     prev_count = nc;
+    contacts_loaded = false;
     gen ^= 1;
     ++steps;
     if (timing) {
@@ -740,6 +771,9 @@ int Engine::step64() {
         cudaEventElapsedTime(&d, ev[3], ev[4]);
         ms[0] = a; ms[1] = b; ms[2] = c2; ms[3] = d;
     }
+    // a state that is no longer finite (an input NaN, or a blow-up) ends the step with an error;
+    // the step itself completed and the context stays usable (cdx_set_state can repair the state)
+    if (hs->nonfinite) return fail(CDX_ERR_NONFINITE, "the state after the step is not finite (NaN or infinity)");
     return CDX_OK;
 }
 
@@ -918,7 +952,9 @@ int Engine::get_contacts(int32_t* ia, int32_t* ib, double* point, double* lambda
     for (int k = 0; k < 3; ++k) {
         if ((st = cuda_check(cudaMemcpy(p.data() + (size_t)k * n, C.point[g] + k * C.cap, sizeof(double) * n, cudaMemcpyDeviceToHost), "download"))) return st;
         if ((st = cuda_check(cudaMemcpy(l.data() + (size_t)k * n, C.lam[g] + k * C.cap, sizeof(double) * n, cudaMemcpyDeviceToHost), "download"))) return st;
-        if ((st = cuda_check(cudaMemcpy(nn.data() + (size_t)k * n, C.dir + k * C.cap, sizeof(double) * n, cudaMemcpyDeviceToHost), "download"))) return st;
+        // normals belong to a step's contacts: a memory loaded by set_contacts has none yet
+        if (!contacts_loaded &&
+            (st = cuda_check(cudaMemcpy(nn.data() + (size_t)k * n, C.dir + k * C.cap, sizeof(double) * n, cudaMemcpyDeviceToHost), "download"))) return st;
     }
     for (int c = 0; c < n; ++c) {
         if (ia) ia[c] = (int32_t)(keys[c] >> 32);
@@ -929,6 +965,63 @@ int Engine::get_contacts(int32_t* ia, int32_t* ib, double* point, double* lambda
             if (normal) normal[3 * (size_t)c + k] = nn[(size_t)k * n + c];
         }
     }
+    return CDX_OK;
+}
+
+// Loads the warm-start memory the next step matches against (the reference's ContactTracker keeps
+// the last step's contacts with their points and impulses, contact_tracker.cpp:11-72, and
+// WarmstartProvider copies the matched impulses in, warmstart.hpp:26-39). Together with
+// cdx_get_contacts and the state calls this checkpoints and resumes a simulation, warm start
+// included. Pairs are entity ids (statics 0..S-1, sphere i = S + i), each at most once.
+int Engine::set_contacts(int32_t n, const int32_t* ia, const int32_t* ib, const double* point,
+                         const double* lambda) {
+    if (!loaded) return fail(CDX_ERR_STATE, "no scene loaded");
+    if (n < 0 || (n > 0 && (!ia || !ib || !point || !lambda))) return fail(CDX_ERR_ARG, "contact arrays missing");
+    const int64_t S = sc.S, N = sc.N;
+    std::vector<int64_t> order(n);
+    std::vector<unsigned long long> key(n);
+    for (int32_t c = 0; c < n; ++c) {
+        const int64_t a = ia[c], b = ib[c];
+        if (a < 0 || b < S || b >= S + N || a >= b)
+            return fail(CDX_ERR_ARG, "contact pairs must be (static or sphere id, higher sphere id) in range");
+        if (a >= S) {
+            if (h_body_scene_of(a - S) != h_body_scene_of(b - S)) return fail(CDX_ERR_ARG, "pair across scenes");
+        } else if (h_static_scene_of(a) != h_body_scene_of(b - S)) {
+            return fail(CDX_ERR_ARG, "pair across scenes");
+        }
+        for (int k = 0; k < 3; ++k)
+            if (!std::isfinite(point[3 * (size_t)c + k]) || !std::isfinite(lambda[3 * (size_t)c + k]))
+                return fail(CDX_ERR_ARG, "contact points and impulses must be finite");
+        key[c] = ((unsigned long long)a << 32) | (unsigned long long)b;
+        order[c] = c;
+    }
+    std::sort(order.begin(), order.end(), [&](int64_t x, int64_t y) { return key[x] < key[y]; });
+    for (int32_t c = 1; c < n; ++c)
+        if (key[order[c]] == key[order[c - 1]]) return fail(CDX_ERR_ARG, "a pair appears twice");
+    int st;
+    if (stream && (st = cuda_check(cudaStreamSynchronize(stream), "set contacts"))) return st;
+    if (cfg.gpu_precision == CDX_PRECISION_SPLIT) return set_contacts_split(order, ia, ib, point, lambda);
+    if ((st = ensure_contacts(std::max<int64_t>(n, 1)))) return st;
+    const int g = gen ^ 1;
+    std::vector<unsigned long long> ks(n);
+    std::vector<double> p(3 * (size_t)n), l(3 * (size_t)n);
+    for (int32_t c = 0; c < n; ++c) {
+        const int64_t o = order[c];
+        ks[c] = key[o];
+        for (int k = 0; k < 3; ++k) {
+            p[(size_t)k * n + c] = point[3 * (size_t)o + k];
+            l[(size_t)k * n + c] = lambda[3 * (size_t)o + k];
+        }
+    }
+    if (n > 0) {
+        if ((st = cuda_check(cudaMemcpy(C.key[g], ks.data(), sizeof(unsigned long long) * n, cudaMemcpyHostToDevice), "upload"))) return st;
+        for (int k = 0; k < 3; ++k) {
+            if ((st = cuda_check(cudaMemcpy(C.point[g] + k * C.cap, p.data() + (size_t)k * n, sizeof(double) * n, cudaMemcpyHostToDevice), "upload"))) return st;
+            if ((st = cuda_check(cudaMemcpy(C.lam[g] + k * C.cap, l.data() + (size_t)k * n, sizeof(double) * n, cudaMemcpyHostToDevice), "upload"))) return st;
+        }
+    }
+    prev_count = n;
+    contacts_loaded = true;
     return CDX_OK;
 }
 

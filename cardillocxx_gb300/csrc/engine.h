@@ -1,5 +1,6 @@
 // Host engine state (one per cdx_ctx).
 #pragma once
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -43,6 +44,15 @@ struct Engine {
     cdx::Grid grid{};
     double rmax = 0;
     std::vector<int32_t> h_scene_body_start, h_scene_static_start;
+    // scene of sphere i / of static s (host copies of the scene ranges)
+    int h_body_scene_of(int64_t i) const {
+        return (int)(std::upper_bound(h_scene_body_start.begin(), h_scene_body_start.end(), (int32_t)i) -
+                     h_scene_body_start.begin()) - 1;
+    }
+    int h_static_scene_of(int64_t s) const {
+        return (int)(std::upper_bound(h_scene_static_start.begin(), h_scene_static_start.end(), (int32_t)s) -
+                     h_scene_static_start.begin()) - 1;
+    }
     std::vector<void*> owned;
 
     double* rhs = nullptr;
@@ -105,6 +115,9 @@ struct Engine {
     int dalloc(void** p, size_t bytes, const char* what);
     void dfree(void* p);
     int init(const cdx_config& c);
+    // replace the configuration between steps (the solver reads its settings every solve)
+    int set_config(const cdx_config& c);
+    void split_config_changed();
     int load_scene(const cdx_scene& s);
     int ensure_tmp(int64_t n);
     int ensure_contacts(int64_t need);
@@ -124,6 +137,11 @@ struct Engine {
     int step_split();
     void destroy_split();
     int get_contacts_split(int32_t* ia, int32_t* ib, double* point, double* lambda, double* normal, int32_t* count);
+    // the warm-start memory of the next step (the contacts of a last step: pair ids, points, impulses)
+    int set_contacts(int32_t n, const int32_t* ia, const int32_t* ib, const double* point, const double* lambda);
+    int set_contacts_split(const std::vector<int64_t>& order, const int32_t* ia, const int32_t* ib,
+                           const double* point, const double* lambda);
+    bool contacts_loaded = false;  // the memory came from set_contacts (no normals until the next step)
     double split_bytes_per_iter() const;
     int split_variant() const;
     int split_sweep_variant() const;

@@ -243,11 +243,12 @@ static int csr_solve(cdx_ctx* ctx, const CsrOpts& o, int32_t nrows, int32_t nv, 
                     launch_accel_reduce(nv, ACC_DOT, B.xy, B.xk1, B.xk, 0.0, 0.0, B.part, B.st, &B.st->sum_dot, B.ds,
                                         s, 1);
                     launch_nesterov_step(B.st, B.ds, nv, o.beta_threshold, o.restart_limit, B.xy, B.xk, B.xk1, nv,
-                                         B.py, B.pk, B.pk1, nrows, s);
+                                         B.py, B.pk, B.pk1, nrows, o.residual_tol, s);
                 } else {
                     launch_accel_reduce(nv, ACC_VELRES, B.x, B.xk1, nullptr, o.tol_rel, o.tol_abs, B.part, B.st,
                                         &B.st->sum_err, B.ds, s, 1);
-                    launch_chebyshev_step(B.st, B.ds, nv, it, B.x, B.xk, B.xk1, nv, B.lam, B.pk, B.pk1, nrows, s);
+                    launch_chebyshev_step(B.st, B.ds, nv, it, B.x, B.xk, B.xk1, nv, B.lam, B.pk, B.pk1, nrows,
+                                          o.residual_tol, s);
                 }
                 bool stop;
                 if ((st = poll(it, stop))) return st;
@@ -261,7 +262,7 @@ static int csr_solve(cdx_ctx* ctx, const CsrOpts& o, int32_t nrows, int32_t nv, 
             for (int it = 0; it < maxit; ++it) {
                 launch_anderson_scatter(nv, B.x, B.lam, A, B.ds, s);
                 sweep(it);
-                launch_anderson_mix(nv, B.x, B.lam, A, o.tol_rel, o.tol_abs, B.ds, s);
+                launch_anderson_mix(nv, B.x, B.lam, A, o.tol_rel, o.tol_abs, o.residual_tol, B.ds, s);
                 bool stop;
                 if ((st = poll(it, stop))) return st;
                 if (stop) break;

@@ -3,6 +3,7 @@
 // the check kernel ends the loop at the iteration cap or when the complementarity residual
 // reaches gpu.residual_tol, so a step needs no host round trip per sweep.
 #include <algorithm>
+#include <cstddef>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -87,6 +88,23 @@ static void destroy_graphs(SplitState* S) {
     S->graph_cap = -1;
 }
 
+// captured graphs hold the solver settings as kernel arguments, and the shapes were chosen for the
+// old loop: after a configuration change they are rebuilt and the shapes chosen again
+void Engine::split_config_changed() {
+    if (!split) return;
+    SplitState* S = split;
+    destroy_graphs(S);
+    S->gplan_ok = false;
+    S->graph_variant = -1;
+    S->variant = cfg.gpu_sweep_variant >= 0 ? std::min(cfg.gpu_sweep_variant, split_num_variants() - 1)
+                                            : split_first_coop_variant();
+    S->tuned_at = 0;
+    S->scene_best = -1;
+    S->scene_tried = 0;
+    S->scene_tuned_at = 0;
+    S->force_sync = true;
+}
+
 void Engine::destroy_split() {
     if (!split) return;
     destroy_graphs(split);
@@ -112,6 +130,7 @@ static int split_contacts(Engine& E, int64_t need) {
         if ((st = salloc(E, (void**)p, sizeof(float4) * cap, "split contacts"))) return st;
     if ((st = salloc(E, (void**)&n.key[0], sizeof(unsigned long long) * cap, "split contacts"))) return st;
     if ((st = salloc(E, (void**)&n.key[1], sizeof(unsigned long long) * cap, "split contacts"))) return st;
+    if (E.cfg.pj_nesterov && (st = salloc(E, (void**)&n.lamk, sizeof(float4) * cap, "split contacts"))) return st;
     if (b.cap > 0 && S->prev_count > 0) {
         const int pg = S->gen ^ 1;
         cudaMemcpyAsync(n.key[pg], b.key[pg], sizeof(unsigned long long) * S->prev_count, cudaMemcpyDeviceToDevice, E.stream);
@@ -120,8 +139,9 @@ static int split_contacts(Engine& E, int64_t need) {
         if ((st = E.cuda_check(cudaStreamSynchronize(E.stream), "split grow"))) return st;
     }
     if (b.cap > 0) {
-        void* old[] = {b.rec0, b.rec1, b.bias, b.lam[0], b.lam[1], b.pt[0], b.pt[1], b.key[0], b.key[1]};
+        void* old[] = {b.rec0, b.rec1, b.bias, b.lam[0], b.lam[1], b.pt[0], b.pt[1], b.key[0], b.key[1], b.lamk};
         for (void* p : old) {
+            if (!p) continue;
             auto& v = S->bufs;
             v.erase(std::remove(v.begin(), v.end(), p), v.end());
             E.dfree(p);
@@ -133,9 +153,52 @@ static int split_contacts(Engine& E, int64_t need) {
     return E.ensure_tmp(cap);
 }
 
+// The reference's loop controls that the split form honours, in its cooperative solve: 2 = Nesterov's
+// loop (pj.nesterov), 1 = the standard loop with the velocity-increment exit (pj.tol_abs and
+// pj.tol_rel not both 0), 0 = neither (every solver shape applies). pj.chebyshev and pj.anderson are
+// refused when the engine is created; pj.rdiag_true_delassus needs nothing: for sphere contacts the
+// Delassus blocks are diagonal, so the block preconditioner is the row scale R = alpha / D the sweep
+// already uses.
+static int split_loop(const cdx_config& c) {
+    if (c.pj_nesterov) return 2;
+    return (c.pj_tol_abs == 0.0 && c.pj_tol_rel == 0.0) ? 0 : 1;
+}
+
 // cooperative plan for n contacts under the context's gpu.coop_* keys
 static bool coop_plan(const Engine& E, int v, int64_t n, CoopPlan* p) {
-    return split_coop_plan(v, n, E.sc.N, E.split->sms, p, E.cfg.gpu_coop_smem_contacts, E.cfg.gpu_coop_blocks);
+    return split_coop_plan(v, n, E.sc.N, E.split->sms, p, E.cfg.gpu_coop_smem_contacts, E.cfg.gpu_coop_blocks,
+                           split_loop(E.cfg));
+}
+
+// Under the loop controls only the 1024-thread cooperative shapes run: the plain one while a block's
+// contacts fit in shared memory, else the hybrid one. Returns the shape for n contacts, or -1.
+static int loop_coop_variant(const Engine& E, int64_t n) {
+    const int v0 = split_first_coop_variant();
+    for (int v = v0; v < split_num_variants() && split_variant_is_coop(v); ++v) {
+        CoopPlan p;
+        if (coop_plan(E, v, std::max<int64_t>(n, 1), &p)) return v;
+    }
+    return -1;
+}
+
+// launches the cooperative solve of the configured loop
+static int launch_coop(const Engine& E, const SplitBuf& sb, int gen, int v, const CoopPlan& plan, int max_iter,
+                       float tol, int max_sweeps, cudaStream_t s) {
+    const cdx_config& c = E.cfg;
+    const int loop = split_loop(c);
+    const unsigned long long wait_ns = c.gpu_coop_wait_ns > 0 ? (unsigned long long)c.gpu_coop_wait_ns : 0ull;
+    if (!loop)
+        return launch_s_solve_coop(sb, gen, (float)c.pj_alpha, v, plan, max_iter, tol, max_sweeps, c.gpu_check_every, s,
+                                   wait_ns);
+    CoopLoopArgs la = {};
+    la.tol_abs = c.pj_tol_abs;
+    la.tol_rel = c.pj_tol_rel;
+    la.beta_threshold = c.pj_nesterov_beta_threshold;
+    la.check_vel = (c.pj_tol_abs == 0.0 && c.pj_tol_rel == 0.0) ? 0 : 1;
+    la.restart_limit = c.pj_nesterov_restart_limit;
+    la.nv = 6 * E.sc.N;
+    return launch_s_solve_coop_loop(sb, gen, (float)c.pj_alpha, v, plan, max_iter, tol, max_sweeps, c.gpu_check_every,
+                                    loop, la, wait_ns, s);
 }
 
 static int init_split(Engine& E) {
@@ -168,6 +231,7 @@ static int init_split(Engine& E) {
     if ((st = salloc(E, (void**)&b.ss, sizeof(SplitScalars), "split"))) return st;
     if ((st = salloc(E, (void**)&b.part, sizeof(float2) * SPLIT_MAX_PARTS, "split"))) return st;
     if ((st = salloc(E, (void**)&b.recs, sizeof(float2) * 2 * SPLIT_MAX_PARTS, "split"))) return st;
+    if ((st = salloc(E, (void**)&b.sums, sizeof(double2) * 2 * SPLIT_MAX_PARTS, "split"))) return st;
     if ((st = salloc(E, (void**)&S->snap, sizeof(double) * 13 * n1, "split snapshot"))) return st;
     if ((st = salloc(E, (void**)&S->ssnap, sizeof(double) * 13 * s1, "split snapshot"))) return st;
     {
@@ -269,8 +333,15 @@ int Engine::step_split() {
     // previous count with a margin. Steps that tune (timing needs the host) stay synchronous, and a
     // step whose contacts outgrow the buffers or the plan is undone from a snapshot and redone
     // synchronously.
+    // under the reference's loop controls only the cooperative solve runs (nothing to tune)
+    const int loopk = split_loop(cfg);
+    if (loopk && pinned < 0) {
+        const int v = loop_coop_variant(*this, (int64_t)S->prev_count + S->prev_count / 16 + 64);
+        S->variant = v >= 0 ? v : split_first_coop_variant();
+    }
     auto tune_due = [&](int64_t n) {
-        if (!(n > 0 && cfg.gpu_autotune && pinned < 0 && n >= 4096 && (double)n >= 1.5 * (double)S->tuned_at))
+        if (!(n > 0 && !loopk && cfg.gpu_autotune && pinned < 0 && n >= 4096 &&
+              (double)n >= 1.5 * (double)S->tuned_at))
             return false;
         int sweeps = 0;
         for (int v = 0; v < split_num_variants(); ++v) {
@@ -284,7 +355,7 @@ int Engine::step_split() {
     };
     // the per-scene kernel (one block a scene) is a candidate for batches and for a single scene
     // small enough that one block can carry it
-    const bool scene_fit = S->scene_nbmax > 0 && S->scene_nbmax <= 3584;
+    const bool scene_fit = !loopk && S->scene_nbmax > 0 && S->scene_nbmax <= 3584;
     // shapes timed while the scenes had few contacts (a pile that is still falling) say little about
     // the settled problem: time them again once the count has grown by half
     if (scene_fit && pinned < 0 && cfg.gpu_autotune && S->scene_best != -1 && S->prev_count >= 64 &&
@@ -478,7 +549,7 @@ int Engine::step_split() {
         else if (!split_variant_is_scenes(v))
             tune_sweeps += 2;
     }
-    if (!async && !scenes && S->nc > 0 && cfg.gpu_autotune && cfg.gpu_sweep_variant < 0 && S->nc >= 4096 &&
+    if (!async && !scenes && !loopk && S->nc > 0 && cfg.gpu_autotune && cfg.gpu_sweep_variant < 0 && S->nc >= 4096 &&
         (double)S->nc >= 1.5 * (double)S->tuned_at && maxit > 2 * tune_sweeps) {
         // autotune: the first sweeps of this step run with every shape; each is a full sweep of
         // the same math, so the step's result does not depend on which shape ran them
@@ -501,8 +572,7 @@ int Engine::step_split() {
                 const int ks[2] = {2, 6};
                 for (int r = 0; r < 2; ++r) {
                     cudaEventRecord(S->tev[0], stream);
-                    st = launch_s_solve_coop(sb, gen, (float)cfg.pj_alpha, v, plan, maxit, (float)cfg.gpu_residual_tol,
-                                             ks[r], cfg.gpu_check_every, stream);
+                    st = launch_coop(*this, sb, gen, v, plan, maxit, (float)cfg.gpu_residual_tol, ks[r], stream);
                     if ((st = cuda_check((cudaError_t)st, "cooperative launch"))) return st;
                     cudaEventRecord(S->tev[1], stream);
                     if ((st = cuda_check(cudaEventSynchronize(S->tev[1]), "autotune"))) return st;
@@ -541,12 +611,21 @@ int Engine::step_split() {
     }
     CoopPlan plan;
     const int64_t plan_nc = async ? (int64_t)S->nc + S->nc / 16 + 64 : (int64_t)S->nc;
+    if (loopk && !capturing && pinned < 0 && S->nc > 0) {
+        // the loop controls run in the cooperative solve only: the plain shape, or the hybrid one
+        // once a block's contacts outgrow its shared memory
+        const int v = loop_coop_variant(*this, plan_nc);
+        if (v >= 0) S->variant = v;
+    }
     if (capturing && !scenes && split_variant_is_coop(S->variant)) plan = S->gplan;
     coop = !scenes && S->nc > 0 && split_variant_is_coop(S->variant) &&
            (capturing ? S->gplan_ok : coop_plan(*this, S->variant, plan_nc, &plan));
+    if (loopk && S->nc > 0 && !coop)
+        return fail(CDX_ERR_UNSUPPORTED, "pj.nesterov and pj.tol_abs/pj.tol_rel run in the cooperative solve of the "
+                                         "split form, which cannot be launched here (gpu.sweep_variant must name a "
+                                         "1024-thread cooperative shape)");
     if (S->nc > 0 && !solved && coop) {
-        st = launch_s_solve_coop(sb, gen, (float)cfg.pj_alpha, S->variant, plan, maxit, (float)cfg.gpu_residual_tol,
-                                 maxit, cfg.gpu_check_every, stream);
+        st = launch_coop(*this, sb, gen, S->variant, plan, maxit, (float)cfg.gpu_residual_tol, maxit, stream);
         if (st != 0 && capturing) {
             // a cooperative launch that cannot be captured: nothing of the step ran; end the capture
             // and issue steps directly from now on
@@ -671,6 +750,7 @@ step_issued:
     std::swap(poff, poff_prev);
     // mirror into the common stats fields
     prev_count = S->nc;
+    contacts_loaded = false;
     last_iters = S->last_iters;
     last_rows = 3 * S->nc;
     last_res = S->res_last;
@@ -684,6 +764,89 @@ step_issued:
         cudaEventElapsedTime(&d, ev[3], ev[4]);
         ms[0] = a; ms[1] = b; ms[2] = c2; ms[3] = d;
     }
+    // a state that is no longer finite ends the step with an error (the step completed; the context
+    // stays usable and cdx_set_state can repair the state)
+    if (S->h_ss->nonfinite) return fail(CDX_ERR_NONFINITE, "the state after the step is not finite (NaN or infinity)");
+    return CDX_OK;
+}
+
+// The warm-start memory of the split form: the previous step's contacts in its own layout (static
+// contacts by scene, static slot and sphere; pair contacts grouped by their lower sphere, ascending)
+// with the slot tables its narrow phase reads for the O(1) lookup. `order` sorts the input by pair.
+int Engine::set_contacts_split(const std::vector<int64_t>& order, const int32_t* ia, const int32_t* ib,
+                               const double* point, const double* lambda) {
+    int st;
+    if (!split && (st = init_split(*this))) return st;
+    SplitState* S = split;
+    const int n = (int)order.size(), N = sc.N, Sn = sc.S, L = sc.max_statics;
+    if ((st = split_contacts(*this, std::max(n, 1)))) return st;
+    SplitBuf& sb = S->sb;
+    const size_t nflag = (size_t)N * L;
+    std::vector<int32_t> flags(std::max<size_t>(nflag, 1), 0), spos(std::max<size_t>(nflag, 1), 0), cnt(N + 1, 0);
+    std::vector<size_t> slot_of(n, 0);
+    int nstat = 0;
+    for (int c = 0; c < n; ++c) {
+        const int64_t o = order[c];
+        const int a = ia[o], bi = ib[o] - Sn;
+        const int scn = h_body_scene_of(bi);
+        if (a < Sn) {
+            const int b0 = h_scene_body_start[scn], nsb = h_scene_body_start[scn + 1] - b0;
+            const int l = a - h_scene_static_start[scn];
+            slot_of[c] = (size_t)b0 * L + (size_t)l * nsb + (size_t)(bi - b0);
+            flags[slot_of[c]] = 1;
+            ++nstat;
+        } else {
+            ++cnt[a - Sn];
+        }
+    }
+    int acc = 0;
+    for (size_t k = 0; k < nflag; ++k) {
+        spos[k] = acc;
+        acc += flags[k];
+    }
+    std::vector<int32_t> poff(N + 1, 0);
+    for (int i = 0; i < N; ++i) poff[i + 1] = poff[i] + cnt[i];
+    std::vector<double> org(3 * (size_t)std::max(sc.nscenes, 1));
+    if ((st = cuda_check(cudaMemcpy(org.data(), sb.origin, 8 * 3 * (size_t)sc.nscenes, cudaMemcpyDeviceToHost), "origins")))
+        return st;
+    std::vector<unsigned long long> keys(std::max(n, 1));
+    std::vector<float4> pt(std::max(n, 1)), lam(std::max(n, 1));
+    std::vector<int32_t> fill(N, 0);
+    for (int c = 0; c < n; ++c) {
+        const int64_t o = order[c];
+        const int a = ia[o], bi = ib[o] - Sn;
+        const int scn = h_body_scene_of(bi);
+        const int slot = a < Sn ? spos[slot_of[c]] : nstat + poff[a - Sn] + fill[a - Sn]++;
+        keys[slot] = ((unsigned long long)a << 32) | (unsigned long long)ib[o];
+        const double* q = point + 3 * o;
+        const double* l = lambda + 3 * o;
+        pt[slot] = make_float4((float)(q[0] - org[3 * scn]), (float)(q[1] - org[3 * scn + 1]),
+                               (float)(q[2] - org[3 * scn + 2]), 0.f);
+        lam[slot] = make_float4((float)l[0], (float)l[1], (float)l[2], 0.f);
+    }
+    const int pg = S->gen ^ 1;
+    if (n > 0) {
+        if ((st = cuda_check(cudaMemcpy(sb.key[pg], keys.data(), 8 * (size_t)n, cudaMemcpyHostToDevice), "upload"))) return st;
+        if ((st = cuda_check(cudaMemcpy(sb.pt[pg], pt.data(), 16 * (size_t)n, cudaMemcpyHostToDevice), "upload"))) return st;
+        if ((st = cuda_check(cudaMemcpy(sb.lam[pg], lam.data(), 16 * (size_t)n, cudaMemcpyHostToDevice), "upload"))) return st;
+    }
+    if (nflag > 0) {
+        if ((st = cuda_check(cudaMemcpy(sflags_prev, flags.data(), 4 * nflag, cudaMemcpyHostToDevice), "upload"))) return st;
+        if ((st = cuda_check(cudaMemcpy(spos_prev, spos.data(), 4 * nflag, cudaMemcpyHostToDevice), "upload"))) return st;
+    }
+    if ((st = cuda_check(cudaMemcpy(poff_prev, poff.data(), 4 * (size_t)(N + 1), cudaMemcpyHostToDevice), "upload")))
+        return st;
+    const int32_t dev2[2] = {n, nstat};
+    static_assert(offsetof(SplitScalars, prev_n_static_dev) == offsetof(SplitScalars, prev_count_dev) + 4,
+                  "the warm-start layout scalars are adjacent");
+    if ((st = cuda_check(cudaMemcpy(&sb.ss->prev_count_dev, dev2, sizeof(dev2), cudaMemcpyHostToDevice), "upload")))
+        return st;
+    S->prev_count = n;
+    S->prev_n_static = nstat;
+    S->nc = n;
+    S->force_sync = true;
+    prev_count = n;
+    contacts_loaded = true;
     return CDX_OK;
 }
 
@@ -700,7 +863,8 @@ int Engine::get_contacts_split(int32_t* ia, int32_t* ib, double* point, double* 
     if ((st = cuda_check(cudaMemcpy(keys.data(), sb.key[g], 8 * (size_t)n, cudaMemcpyDeviceToHost), "download"))) return st;
     if ((st = cuda_check(cudaMemcpy(pt.data(), sb.pt[g], 16 * (size_t)n, cudaMemcpyDeviceToHost), "download"))) return st;
     if ((st = cuda_check(cudaMemcpy(lam.data(), sb.lam[g], 16 * (size_t)n, cudaMemcpyDeviceToHost), "download"))) return st;
-    if ((st = cuda_check(cudaMemcpy(nm.data(), sb.rec0, 16 * (size_t)n, cudaMemcpyDeviceToHost), "download"))) return st;
+    if (!contacts_loaded &&
+        (st = cuda_check(cudaMemcpy(nm.data(), sb.rec0, 16 * (size_t)n, cudaMemcpyDeviceToHost), "download"))) return st;
     std::vector<double> org(3 * (size_t)sc.nscenes);
     if ((st = cuda_check(cudaMemcpy(org.data(), sb.origin, 8 * org.size(), cudaMemcpyDeviceToHost), "download"))) return st;
     std::vector<int32_t> bscene(sc.N);
@@ -749,8 +913,7 @@ int Engine::time_sweeps(int n, double* msc, double* msb, double* bc, double* bb)
         if (split_variant_is_coop(tv) && coop_plan(*this, tv, S->prev_count, &plan)) {
             // one cooperative launch of n sweeps; reported per sweep
             cudaEventRecord(e[0], stream);
-            st = launch_s_solve_coop(S->sb, g, (float)cfg.pj_alpha, tv, plan, 1 << 30, 0.f, n, cfg.gpu_check_every,
-                                     stream);
+            st = launch_coop(*this, S->sb, g, tv, plan, 1 << 30, 0.f, n, stream);
             cudaEventRecord(e[1], stream);
             if (!(st = cuda_check((cudaError_t)st, "cooperative launch")) &&
                 !(st = cuda_check(cudaEventSynchronize(e[1]), "time sweeps"))) {

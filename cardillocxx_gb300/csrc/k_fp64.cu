@@ -207,7 +207,8 @@ __global__ void k_rhs64(Scene sc, double dt, double g0, double g1, double g2, do
     }
 }
 
-__global__ void k_drift64(Scene sc, double h, int compute_R) {
+// nonfinite (the closing drift of a step): set when a body's new state holds a NaN or infinity
+__global__ void k_drift64(Scene sc, double h, int compute_R, int32_t* nonfinite) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < sc.N) {
         double x[3] = {sc.bf(BF_PX)[i], sc.bf(BF_PY)[i], sc.bf(BF_PZ)[i]};
@@ -217,6 +218,12 @@ __global__ void k_drift64(Scene sc, double h, int compute_R) {
         drift(x, q, v, w, h);
         sc.bf(BF_PX)[i] = x[0]; sc.bf(BF_PY)[i] = x[1]; sc.bf(BF_PZ)[i] = x[2];
         sc.bf(BF_QX)[i] = q[0]; sc.bf(BF_QY)[i] = q[1]; sc.bf(BF_QZ)[i] = q[2]; sc.bf(BF_QW)[i] = q[3];
+        if (nonfinite) {
+            bool ok = true;
+            for (int k = 0; k < 3; ++k) ok = ok && isfinite(x[k]) && isfinite(v[k]) && isfinite(w[k]);
+            for (int k = 0; k < 4; ++k) ok = ok && isfinite(q[k]);
+            if (!ok) *nonfinite = 1;
+        }
         if (compute_R) {
             double R[9];
             rotmat(q, R);
@@ -911,10 +918,13 @@ __global__ void k_accel_copy(double* xd, const double* xs, int64_t nx, double* l
 }
 
 // Nesterov: err and the restart tests (nesterov_loop), then the momentum coefficient
-__global__ void k_nesterov_decide(AccelState* st, DevScalars* ds, int nv, double beta_threshold, int restart_limit) {
+// (gpu.residual_tol: the loop also ends once the sweep's complementarity residual is at most tol,
+// tested right after the reference's own exit)
+__global__ void k_nesterov_decide(AccelState* st, DevScalars* ds, int nv, double beta_threshold, int restart_limit,
+                                  double residual_tol) {
     if (ds->done) return;
     const double err = 1.0 / sqrt((double)nv) * sqrt(st->sum_err);
-    if (err <= 1.0) {
+    if (err <= 1.0 || (residual_tol > 0 && ds->res_last <= residual_tol)) {
         ds->done = 1;
         return;
     }
@@ -969,10 +979,10 @@ __global__ void k_nesterov_update(double* xy, double* xk, const double* xk1, int
 }
 
 // Chebyshev: err, then the next omega or the fallback to a plain step (chebyshev_loop)
-__global__ void k_chebyshev_decide(AccelState* st, DevScalars* ds, int nv, int iter) {
+__global__ void k_chebyshev_decide(AccelState* st, DevScalars* ds, int nv, int iter, double residual_tol) {
     if (ds->done) return;
     const double err = 1.0 / sqrt((double)nv) * sqrt(st->sum_err);
-    if (err <= 1.0) {
+    if (err <= 1.0 || (residual_tol > 0 && ds->res_last <= residual_tol)) {
         ds->done = 1;
         return;
     }
@@ -1224,13 +1234,13 @@ __global__ void k_and_partials(int N, int64_t nt, int m, int64_t ld, const doubl
 // partial pivoting (mode 1), or a plain step (mode 0, fewer than two residuals kept), or a failed
 // solve (mode 2: singular or not finite)
 __global__ void k_and_solve(int nv, int nch_v, int nch_t, const double* part, double* ls, int m, AndersonState* as,
-                            DevScalars* ds) {
+                            DevScalars* ds, double residual_tol) {
     if (ds->done) return;
     double sv = 0.0;
     for (int k = 0; k < nch_v; ++k) sv = sv + part[k];
     const double err = 1.0 / sqrt((double)nv) * sqrt(sv);
     as->nonfinite = 0;
-    if (err <= 1.0) {
+    if (err <= 1.0 || (residual_tol > 0 && ds->res_last <= residual_tol)) {
         ds->done = 1;
         return;
     }
@@ -1354,9 +1364,9 @@ void launch_rhs64(const Scene& sc, double dt, const double* g, double* rhs, cuda
     if (sc.N == 0) return;
     k_rhs64<<<nblk(sc.N), NT, 0, s>>>(sc, dt, g[0], g[1], g[2], rhs, implicit_gyro);
 }
-void launch_drift64(const Scene& sc, double h, int compute_R, cudaStream_t s) {
+void launch_drift64(const Scene& sc, double h, int compute_R, cudaStream_t s, int32_t* nonfinite) {
     if (sc.N + sc.S == 0) return;
-    k_drift64<<<nblk(sc.N + sc.S), NT, 0, s>>>(sc, h, compute_R);
+    k_drift64<<<nblk(sc.N + sc.S), NT, 0, s>>>(sc, h, compute_R, nonfinite);
 }
 void launch_static_flags64(const Scene& sc, double margin, int32_t* flags, cudaStream_t s) {
     if (sc.N == 0) return;
@@ -1438,13 +1448,14 @@ void launch_accel_copy(double* xd, const double* xs, int64_t nx, double* ld, con
 }
 void launch_nesterov_step(AccelState* st, DevScalars* ds, int nv, double beta_threshold, int restart_limit, double* xy,
                           double* xk, const double* xk1, int64_t nx, double* py, double* pk, const double* pk1,
-                          int64_t nl, cudaStream_t s) {
-    k_nesterov_decide<<<1, 1, 0, s>>>(st, ds, nv, beta_threshold, restart_limit);
+                          int64_t nl, double residual_tol, cudaStream_t s) {
+    k_nesterov_decide<<<1, 1, 0, s>>>(st, ds, nv, beta_threshold, restart_limit, residual_tol);
     k_nesterov_update<<<nblk(nx + nl), NT, 0, s>>>(xy, xk, xk1, nx, py, pk, pk1, nl, st, ds);
 }
 void launch_chebyshev_step(AccelState* st, DevScalars* ds, int nv, int iter, const double* x, double* xk, double* xk1,
-                           int64_t nx, const double* lam, double* pk, double* pk1, int64_t nl, cudaStream_t s) {
-    k_chebyshev_decide<<<1, 1, 0, s>>>(st, ds, nv, iter);
+                           int64_t nx, const double* lam, double* pk, double* pk1, int64_t nl, double residual_tol,
+                           cudaStream_t s) {
+    k_chebyshev_decide<<<1, 1, 0, s>>>(st, ds, nv, iter, residual_tol);
     k_chebyshev_update<<<nblk(nx + nl), NT, 0, s>>>(x, xk, xk1, nx, lam, pk, pk1, nl, st, ds);
 }
 void launch_power_iteration(int N, int plain, double* v, double* Mv, double* part, AccelState* st,
@@ -1491,7 +1502,7 @@ void launch_anderson_scatter(int N, double* x, double* lam, const AndersonBufs& 
     k_and_scatter<<<grid_of(A.nt), NT, 0, s>>>(N, x, lam, A.rowmap, A.nt, A.z, ds, A.plain);
 }
 void launch_anderson_mix(int N, const double* x, const double* lam, const AndersonBufs& A, double tol_rel,
-                         double tol_abs, DevScalars* ds, cudaStream_t s) {
+                         double tol_abs, double residual_tol, DevScalars* ds, cudaStream_t s) {
     const int nv = A.plain ? N : 6 * N;
     const int nch_t = anderson_chunks(A.nt), nch_v = anderson_chunks(nv);
     k_and_push<<<1, 1, 0, s>>>(A.st, A.m, ds);
@@ -1500,7 +1511,7 @@ void launch_anderson_mix(int N, const double* x, const double* lam, const Anders
     dim3 g((unsigned)nblk(nch_t, 128), (unsigned)anderson_sums(A.m));
     k_and_partials<<<g, 128, 0, s>>>(N, A.nt, A.m, A.nt_cap, A.z, A.w, A.f, A.fh, tol_rel, tol_abs, A.part, nch_t,
                                      A.st, ds, A.plain);
-    k_and_solve<<<1, 1, 0, s>>>(nv, nch_v, nch_t, A.part, A.ls, A.m, A.st, ds);
+    k_and_solve<<<1, 1, 0, s>>>(nv, nch_v, nch_t, A.part, A.ls, A.m, A.st, ds, residual_tol);
     const double* gam = A.ls + (size_t)A.m * A.m + A.m;
     k_and_candidate<<<grid_of(A.nt), NT, 0, s>>>(A.nt, A.m, A.nt_cap, A.w, A.zh, A.fh, gam, A.cand, A.st, ds);
     k_and_select<<<grid_of(A.nt), NT, 0, s>>>(A.nt, A.z, A.w, A.cand, A.st, ds);

@@ -809,7 +809,7 @@ __device__ __forceinline__ void grid_arrive(unsigned* ctr, float2* recs, unsigne
 // Waiting half: thread 0 waits (bounded, acquire loads) for every block's arrival, then warp 0
 // reduces the records.
 __device__ __forceinline__ bool grid_wait_max(unsigned* ctr, float2* recs, unsigned epoch, int32_t* err, bool reduce,
-                                              float& maxd, float& maxl) {
+                                              float& maxd, float& maxl, unsigned long long wait_ns) {
     __shared__ float s_md, s_ml;
     __shared__ int s_ok;
     float2* bank = recs + (size_t)(epoch & 1u) * SPLIT_MAX_PARTS;
@@ -820,7 +820,7 @@ __device__ __forceinline__ bool grid_wait_max(unsigned* ctr, float2* recs, unsig
             const unsigned target = epoch * gridDim.x;
             const unsigned long long t0 = global_ns();
             while ((int)(ld_acquire(ctr) - target) < 0) {
-                if (ld_acquire(reinterpret_cast<const unsigned*>(err)) != 0u || global_ns() - t0 > COOP_WAIT_NS) {
+                if (ld_acquire(reinterpret_cast<const unsigned*>(err)) != 0u || global_ns() - t0 > wait_ns) {
                     atomicExch(err, 1);
                     ok = 0;
                     break;
@@ -878,7 +878,7 @@ __device__ __forceinline__ bool grid_wait_max(unsigned* ctr, float2* recs, unsig
 template <int NTH, int UNROLL, int AGG, int HYB>
 __global__ void __launch_bounds__(NTH, 1) k_s_solve_coop(SplitBuf sb, int gen, float alpha, int max_iter, float tol,
                                                          int cpb, int bpb, int vf_smem, int max_sweeps,
-                                                         int check_every) {
+                                                         int check_every, unsigned long long wait_ns) {
     extern __shared__ float4 smem[];
     SplitScalars* ss = sb.ss;
     if (*(volatile int32_t*)&ss->done) return;
@@ -981,7 +981,7 @@ __global__ void __launch_bounds__(NTH, 1) k_s_solve_coop(SplitBuf sb, int gen, f
             const float4 w0 = vf_smem ? s_vf[2 * i + 1] : ldg4(&sb.vel4[2 * (bb + i) + 1]);
             stcg_body(&Aclr[2 * (bb + i)], v0, w0);
         }
-        if (!grid_wait_max(&ss->bar, sb.recs, epoch, &ss->err, check, maxd2, maxl)) return;
+        if (!grid_wait_max(&ss->bar, sb.recs, epoch, &ss->err, check, maxd2, maxl, wait_ns)) return;
         ++it;
         if (check) {
             r = sweep_residual(maxd2, maxl);
@@ -998,6 +998,390 @@ __global__ void __launch_bounds__(NTH, 1) k_s_solve_coop(SplitBuf sb, int gen, f
         ss->res_last = r;
         ss->done = stop;
         ss->bar_base = epoch;
+    }
+}
+
+// ---- cooperative solve under the reference's loop controls
+// Sum of two doubles over the block (the result is valid in warp 0).
+__device__ __forceinline__ void block_sum2d(double& a, double& b) {
+    __shared__ double sh[2][32];
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) {
+        sh[0][wid] = a;
+        sh[1][wid] = b;
+    }
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+        a = lane < nw ? sh[0][lane] : 0.0;
+        b = lane < nw ? sh[1][lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_xor_sync(0xffffffffu, a, o);
+            b += __shfl_xor_sync(0xffffffffu, b, o);
+        }
+    }
+}
+
+// Grid barrier that also sums one (a, b) record per block. Every block adds the records in the
+// same order (lane-wise over blocks lane, lane + 32, ..., then a butterfly over the lanes), so
+// all blocks get bit-identical sums and take the same decisions from them.
+__device__ __forceinline__ void grid_arrive_sum(unsigned* ctr, double2* sums, unsigned epoch, double a, double b) {
+    double2* bank = sums + (size_t)(epoch & 1u) * SPLIT_MAX_PARTS;
+    if (threadIdx.x == 0) bank[blockIdx.x] = make_double2(a, b);
+    __syncthreads();
+    if (threadIdx.x == 0) asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(ctr) : "memory");
+}
+__device__ __forceinline__ bool grid_wait_sum(unsigned* ctr, double2* sums, unsigned epoch, int32_t* err, double& a,
+                                              double& b, unsigned long long wait_ns) {
+    __shared__ double s_a, s_b;
+    __shared__ int s_ok;
+    double2* bank = sums + (size_t)(epoch & 1u) * SPLIT_MAX_PARTS;
+    if (threadIdx.x < 32) {
+        const unsigned FULL = 0xffffffffu;
+        int ok = 1;
+        if (threadIdx.x == 0) {
+            const unsigned target = epoch * gridDim.x;
+            const unsigned long long t0 = global_ns();
+            while ((int)(ld_acquire(ctr) - target) < 0) {
+                if (ld_acquire(reinterpret_cast<const unsigned*>(err)) != 0u || global_ns() - t0 > wait_ns) {
+                    atomicExch(err, 1);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(20);
+            }
+        }
+        ok = __shfl_sync(FULL, ok, 0);
+        double sa = 0.0, sb2 = 0.0;
+        if (ok) {
+            for (int p = threadIdx.x; p < (int)gridDim.x; p += 32) {
+                const double2 v = __ldcg(&bank[p]);
+                sa += v.x;
+                sb2 += v.y;
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                sa += __shfl_xor_sync(FULL, sa, o);
+                sb2 += __shfl_xor_sync(FULL, sb2, o);
+            }
+        }
+        if (threadIdx.x == 0) {
+            s_a = sa;
+            s_b = sb2;
+            s_ok = ok;
+        }
+    }
+    __syncthreads();
+    a = s_a;
+    b = s_b;
+    return s_ok != 0;
+}
+
+// The terms of residual() (projected_jacobi.cpp:140-144) for one body's six velocities:
+// sum of ((x - xp) / (tol_rel max(|x|, |xp|) + tol_abs))^2, evaluated in FP64 (a tolerance far
+// below FP32's range, as a caller may set to switch the exit off, stays exact).
+__device__ __forceinline__ double velres_body(float4 xv, float4 xw, float4 pv, float4 pw, double tr, double ta) {
+    const float x[6] = {xv.x, xv.y, xv.z, xw.x, xw.y, xw.z};
+    const float p[6] = {pv.x, pv.y, pv.z, pw.x, pw.y, pw.z};
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        const double a = x[k], b = p[k];
+        const double q = fmax(fabs(a), fabs(b)) * tr + ta;
+        const double d = (a - b) / q;
+        s += d * d;
+    }
+    return s;
+}
+// (y - x1) . (x1 - x0) over one body's six velocities (nesterov_loop's restart test), in FP64
+__device__ __forceinline__ double nes_dot_body(float4 yv, float4 yw, float4 v1, float4 w1, float4 v0, float4 w0) {
+    return ((double)yv.x - v1.x) * ((double)v1.x - v0.x) + ((double)yv.y - v1.y) * ((double)v1.y - v0.y) +
+           ((double)yv.z - v1.z) * ((double)v1.z - v0.z) + ((double)yw.x - w1.x) * ((double)w1.x - w0.x) +
+           ((double)yw.y - w1.y) * ((double)w1.y - w0.y) + ((double)yw.z - w1.z) * ((double)w1.z - w0.z);
+}
+__device__ __forceinline__ float4 extrap4(float4 x1, float4 x0, float c) {
+    // x1 + c (x1 - x0); the .w lanes carry the inverse masses, equal in both, so they stay exact
+    return make_float4(x1.x + c * (x1.x - x0.x), x1.y + c * (x1.y - x0.y), x1.z + c * (x1.z - x0.z),
+                       x1.w + c * (x1.w - x0.w));
+}
+
+// The cooperative whole solve (one block per SM, contacts in shared memory, the same sweep as
+// k_s_solve_coop with one contact per thread and pass) under the loop controls of
+// ProjectedJacobiSolver::solve (projected_jacobi.cpp:451-500):
+//   NES = 0, standard_loop (:371-377): after sweep k (counting from 0) with k % 10 == 0 the
+//     velocity-increment residual err = sqrt(1/Nv) ||(x_{k+1} - x_k) / q|| (:140-144) is formed
+//     over all bodies (one extra grid reduction) and the loop ends when err <= 1;
+//   NES = 1, nesterov_loop (:379-449): the sweep runs from the extrapolated pair (y, p_y) and
+//     gives (x_{k+1}, p_{k+1}); err = residual(x_{k+1}, y); the loop ends when err <= 1, else
+//     theta and beta are updated and momentum restarts when err is not finite, err grew by more
+//     than 5 %, beta exceeds pj.nesterov_beta_threshold or leaves [0, 1], or (y - x_{k+1}) .
+//     (x_{k+1} - x_k) > 0; after pj.nesterov_restart_limit restarts momentum stays off. Then
+//     y = x_{k+1} + beta (x_{k+1} - x_k) and p_y = p_{k+1} + beta (p_{k+1} - p_k).
+// Velocities are linear in the impulses (x = x_free + M^-1 W^T lambda), so each block
+// extrapolates its own bodies' velocities and its own contacts' impulses with no scatter. One
+// Nesterov iteration takes three grid barriers: after the sweep (x_{k+1} complete), after the
+// reductions of err and the dot product (every block then takes the same decision from the same
+// sums), and after the extrapolation (y complete for the next sweep's gathers). Accumulators:
+// y (read by the sweep, overwritten in place by the extrapolation once every block has passed
+// the second barrier), x_{k+1} (reset to the free velocities before the sweep adds into it) and
+// x_k; the last two swap roles each iteration.
+// gpu.residual_tol and the iteration cap end the loop as in the plain cooperative solve (every
+// check_every sweeps). The result is (x_{k+1}, p_{k+1}) of the last sweep, as in the reference.
+// Shared memory a contact: records and impulses (48 B), plus p_k for Nesterov (64 B).
+// The loop state lives in shared memory (thread 0 updates it; every block's thread 0 computes the
+// same values from the same sums), which keeps it out of the sweep's registers.
+struct CoopLoopState {
+    double thk, err_prev, verr, dot;
+    int restarts, disabled, iy, ix1, ixk;
+    float coef;
+};
+template <int NTH, int HYB, int NES>
+__global__ void __launch_bounds__(NTH, 1) k_s_solve_coop_loop(SplitBuf sb, int gen, float alpha, int max_iter,
+                                                              float tol, int cpb, int bpb, int vf_smem, int max_sweeps,
+                                                              int check_every, CoopLoopArgs la,
+                                                              unsigned long long wait_ns) {
+    extern __shared__ float4 smem[];
+    __shared__ CoopLoopState L;
+    SplitScalars* ss = sb.ss;
+    if (*(volatile int32_t*)&ss->done) return;
+    float4* s_q0 = smem;
+    float4* s_q1 = smem + cpb;
+    float4* s_l = smem + 2 * cpb;                 // lambda (Nesterov: p_y before the sweep, p_{k+1} after)
+    float4* s_pk = smem + 3 * cpb;                // Nesterov: p_k
+    float4* s_vf = smem + (NES ? 4 : 3) * cpb;    // free velocities of the block's bodies
+    const int it0 = *(volatile int32_t*)&ss->iters;
+    unsigned epoch = *(volatile unsigned*)&ss->bar_base;
+    const int nc = *sb.nc_dev, N = sb.N, tid = threadIdx.x;
+    if (!HYB && (int64_t)nc > (int64_t)cpb * gridDim.x) {
+        if (blockIdx.x == 0 && tid == 0) ss->err = 4;
+        return;
+    }
+    const int cpe = (nc + (int)gridDim.x - 1) / (int)gridDim.x;
+    const int cb = blockIdx.x * cpe;
+    const int ncb = max(0, min(nc - cb, cpe));
+    const int bb = blockIdx.x * bpb;
+    const int nbb = max(0, min(N - bb, bpb));
+    const int ncs = HYB ? min(ncb, cpb) : ncb;
+    float4* __restrict__ lamg = sb.lam[gen];
+    float4* __restrict__ pkg = sb.lamk;
+    for (int i = tid; i < ncs; i += NTH) {
+        s_q0[i] = ldg4(&sb.rec0[cb + i]);
+        s_q1[i] = ldg4(&sb.rec1[cb + i]);
+        s_l[i] = lamg[cb + i];
+        if (NES) s_pk[i] = it0 == 0 ? s_l[i] : pkg[cb + i];
+    }
+    if (NES && HYB && it0 == 0)
+        for (int i = ncs + tid; i < ncb; i += NTH) pkg[cb + i] = lamg[cb + i];
+    if (vf_smem)
+        for (int i = tid; i < 2 * nbb; i += NTH) s_vf[i] = ldg4(&sb.vel4[2 * bb + i]);
+    if (tid == 0) {
+        L.thk = ss->nes_thk;
+        L.err_prev = ss->nes_err_prev;
+        L.verr = ss->vel_err;
+        L.dot = 0.0;
+        L.restarts = ss->nes_restarts;
+        L.disabled = ss->nes_disabled;
+        L.iy = ss->nes_iy;
+        L.ix1 = ss->nes_ix1;
+        L.ixk = ss->nes_ixk;
+        L.coef = 0.f;
+    }
+    __syncthreads();
+    if (NES && it0 == 0) {
+        // x_k = x_0 at the start: the block's own bodies, read back by this block only
+        const float4* Y0 = sb.acc[L.iy];
+        float4* XK0 = sb.acc[L.ixk];
+        for (int i = tid; i < nbb; i += NTH) {
+            float4 v0, w0;
+            ldcg_body(&Y0[2 * (bb + i)], v0, w0);
+            stcg_body(&XK0[2 * (bb + i)], v0, w0);
+        }
+        __syncthreads();
+    }
+    int it = it0, stop = 0;
+    float r = 0.f;
+    for (int j = 0; j < max_sweeps; ++j) {
+        const float4* G = sb.acc[NES ? L.iy : it % SPLIT_NACC];
+        float4* Add = sb.acc[NES ? L.ix1 : (it + 1) % SPLIT_NACC];
+        float maxd2 = 0.f, maxl = 0.f;
+        for (int base = 0; base < ncb; base += NTH) {
+            const int i = base + tid;
+            const bool ok = i < ncb;
+            PJOut o = {};
+            int a = -1, b = 0;
+            if (ok) {
+                float4 q0, q1, l;
+                if (!HYB || i < ncs) {
+                    q0 = s_q0[i];
+                    q1 = s_q1[i];
+                    l = s_l[i];
+                } else {
+                    q0 = ldg4(&sb.rec0[cb + i]);
+                    q1 = ldg4(&sb.rec1[cb + i]);
+                    l = __ldcg(&lamg[cb + i]);
+                }
+                a = __float_as_int(q1.z);
+                b = __float_as_int(q1.w);
+                float4 va, wa, vb, wb;
+                ldcg_body(&G[2 * b], vb, wb);
+                if (a >= 0) {
+                    ldcg_body(&G[2 * a], va, wa);
+                } else {
+                    va = make_float4(0.f, 0.f, 0.f, 0.f);
+                    wa = va;
+                }
+                pj_contact(q0, q1, l, va, wa, vb, wb, &sb.bias[cb + i], alpha, o);
+                if (!HYB || i < ncs)
+                    s_l[i] = o.lam;
+                else
+                    __stcg(&lamg[cb + i], o.lam);
+                maxd2 = fmaxf(maxd2, o.dn2);
+                maxl = fmaxf(maxl, o.lm);
+            }
+            pj_push<2>(Add, ok, a, b, o);
+        }
+        const bool check = (it + 1) % check_every == 0 || it + 1 >= max_iter;
+        const bool velchk = NES || (la.check_vel && it % 10 == 0);
+        if (check) block_max2(maxd2, maxl);
+        grid_arrive(&ss->bar, sb.recs, ++epoch, check, maxd2, maxl);
+        if (!NES) {
+            // the standard loop's accumulator rotation: reset A_{k-1} while the others arrive
+            float4* Clr = sb.acc[(it + 3) % SPLIT_NACC];
+            for (int i = tid; i < nbb; i += NTH) {
+                const float4 v0 = vf_smem ? s_vf[2 * i] : ldg4(&sb.vel4[2 * (bb + i)]);
+                const float4 w0 = vf_smem ? s_vf[2 * i + 1] : ldg4(&sb.vel4[2 * (bb + i) + 1]);
+                stcg_body(&Clr[2 * (bb + i)], v0, w0);
+            }
+        }
+        if (!grid_wait_max(&ss->bar, sb.recs, epoch, &ss->err, check, maxd2, maxl, wait_ns)) return;
+        if (velchk) {
+            // the velocity-increment residual between the new velocities and those the sweep read
+            // (and Nesterov's restart dot product), over the block's own bodies, then over the grid
+            double e = 0.0, d = 0.0;
+            const float4* XK = sb.acc[L.ixk];
+            for (int i = tid; i < nbb; i += NTH) {
+                float4 v1, w1, v0, w0;
+                ldcg_body(&Add[2 * (bb + i)], v1, w1);
+                ldcg_body(&G[2 * (bb + i)], v0, w0);
+                e += velres_body(v1, w1, v0, w0, la.tol_rel, la.tol_abs);
+                if (NES) {
+                    float4 vk, wk;
+                    ldcg_body(&XK[2 * (bb + i)], vk, wk);
+                    d += nes_dot_body(v0, w0, v1, w1, vk, wk);
+                }
+            }
+            block_sum2d(e, d);
+            grid_arrive_sum(&ss->bar, sb.sums, ++epoch, e, d);
+            if (!grid_wait_sum(&ss->bar, sb.sums, epoch, &ss->err, e, d, wait_ns)) return;
+            if (tid == 0) {
+                L.verr = (1.0 / sqrt((double)la.nv)) * sqrt(e);
+                L.dot = d;
+            }
+            __syncthreads();
+        }
+        ++it;
+        bool fin = velchk && L.verr <= 1.0;
+        if (check) {
+            r = sweep_residual(maxd2, maxl);
+            if (it >= max_iter || (tol > 0.f && r <= tol) || !(r == r)) fin = true;
+        }
+        if (fin) {
+            stop = 1;
+            break;
+        }
+        if (NES) {
+            if (tid == 0) {
+                // nesterov_loop's momentum update (every block takes the same decision)
+                const double verr = L.verr, thk = L.thk;
+                const double thk1 = 0.5 * (1.0 + sqrt(4.0 * thk * thk + 1.0));
+                const double betak1 = (thk - 1.0) / thk1;
+                bool restart = false;
+                if (!isfinite(verr)) {
+                    restart = true;
+                } else if (isfinite(L.err_prev) && verr > 1.05 * L.err_prev) {
+                    restart = true;
+                } else if (betak1 > la.beta_threshold) {
+                    restart = true;
+                } else if (!isfinite(betak1) || betak1 < 0.0 || betak1 > 1.0) {
+                    restart = true;
+                } else if (L.dot > 0.0) {
+                    restart = true;
+                }
+                L.coef = 0.f;
+                if (restart) {
+                    L.thk = 1.0;
+                    if (++L.restarts >= la.restart_limit) L.disabled = 1;
+                } else if (L.disabled) {
+                    L.thk = 1.0;
+                } else {
+                    L.coef = (float)betak1;
+                    L.thk = thk1;
+                }
+                L.err_prev = verr;
+            }
+            __syncthreads();
+            const float coef = L.coef;
+            // y = x_{k+1} + beta (x_{k+1} - x_k) for the block's bodies; x_k's buffer is reset to the
+            // free velocities and becomes the next x_{k+1}
+            float4* Y = sb.acc[L.iy];
+            const float4* X1 = sb.acc[L.ix1];
+            float4* XK = sb.acc[L.ixk];
+            for (int i = tid; i < nbb; i += NTH) {
+                float4 v1, w1, v0, w0;
+                ldcg_body(&X1[2 * (bb + i)], v1, w1);
+                ldcg_body(&XK[2 * (bb + i)], v0, w0);
+                stcg_body(&Y[2 * (bb + i)], extrap4(v1, v0, coef), extrap4(w1, w0, coef));
+                const float4 f0 = vf_smem ? s_vf[2 * i] : ldg4(&sb.vel4[2 * (bb + i)]);
+                const float4 f1 = vf_smem ? s_vf[2 * i + 1] : ldg4(&sb.vel4[2 * (bb + i) + 1]);
+                stcg_body(&XK[2 * (bb + i)], f0, f1);
+            }
+            // p_y = p_{k+1} + beta (p_{k+1} - p_k), p_k = p_{k+1} for the block's contacts
+            for (int i = tid; i < ncb; i += NTH) {
+                if (!HYB || i < ncs) {
+                    const float4 l1 = s_l[i], l0 = s_pk[i];
+                    s_pk[i] = l1;
+                    s_l[i] = extrap4(l1, l0, coef);
+                } else {
+                    const float4 l1 = __ldcg(&lamg[cb + i]), l0 = __ldcg(&pkg[cb + i]);
+                    __stcg(&pkg[cb + i], l1);
+                    __stcg(&lamg[cb + i], extrap4(l1, l0, coef));
+                }
+            }
+            // y complete before any block gathers from it (the barrier's __syncthreads also orders
+            // the swap below after every thread's use of the old indices)
+            grid_arrive(&ss->bar, sb.recs, ++epoch, false, 0.f, 0.f);
+            if (tid == 0) {
+                const int t = L.ix1;
+                L.ix1 = L.ixk;
+                L.ixk = t;
+            }
+            float u0, u1;
+            if (!grid_wait_max(&ss->bar, sb.recs, epoch, &ss->err, false, u0, u1, wait_ns)) return;
+        }
+    }
+    for (int i = tid; i < ncs; i += NTH) {
+        lamg[cb + i] = s_l[i];
+        if (NES && !stop) pkg[cb + i] = s_pk[i];
+    }
+    if (blockIdx.x == 0 && tid == 0) {
+        ss->iters = it;
+        ss->res_last = r;
+        ss->done = stop;
+        ss->bar_base = epoch;
+        ss->vel_err = L.verr;
+        if (NES) {
+            ss->final_acc = L.ix1;
+            ss->nes_thk = L.thk;
+            ss->nes_err_prev = L.err_prev;
+            ss->nes_restarts = L.restarts;
+            ss->nes_disabled = L.disabled;
+            ss->nes_iy = L.iy;
+            ss->nes_ix1 = L.ix1;
+            ss->nes_ixk = L.ixk;
+        }
     }
 }
 
@@ -1162,6 +1546,15 @@ __global__ void k_s_reset(SplitBuf sb) {
     ss->bar_base = 0u;
     ss->final_acc = -1;
     ss->iters_sum = 0ull;
+    ss->nonfinite = 0;
+    ss->nes_thk = 1.0;
+    ss->vel_err = INFINITY;
+    ss->nes_err_prev = INFINITY;
+    ss->nes_restarts = 0;
+    ss->nes_disabled = 0;
+    ss->nes_iy = 0;
+    ss->nes_ix1 = 1;
+    ss->nes_ixk = 2;
 }
 
 // ------------------------------------------------------------------ FP64 finalisation
@@ -1390,6 +1783,11 @@ __global__ void k_s_writeback_drift(Scene sc, SplitBuf sb, double h) {
         drift_fast(x, q, v, wb, h);
         sc.bf(BF_PX)[i] = x[0]; sc.bf(BF_PY)[i] = x[1]; sc.bf(BF_PZ)[i] = x[2];
         sc.bf(BF_QX)[i] = q[0]; sc.bf(BF_QY)[i] = q[1]; sc.bf(BF_QZ)[i] = q[2]; sc.bf(BF_QW)[i] = q[3];
+        // the step's state must stay finite: the host reports CDX_ERR_NONFINITE otherwise
+        bool ok = true;
+        for (int k = 0; k < 3; ++k) ok = ok && isfinite(x[k]) && isfinite(v[k]) && isfinite(wb[k]);
+        for (int k = 0; k < 4; ++k) ok = ok && isfinite(q[k]);
+        if (!ok) sb.ss->nonfinite = 1;
     } else if (i < sc.N + sc.S) {
         const int s = i - sc.N;
         double x[3] = {sc.sf(SF_PX)[s], sc.sf(SF_PY)[s], sc.sf(SF_PZ)[s]};
@@ -1445,7 +1843,7 @@ static StreamVariant g_stream[] = {
 constexpr int N_STREAM = sizeof(g_stream) / sizeof(g_stream[0]);
 // Cooperative solves (one launch for all sweeps): threads per block and contacts per thread per pass.
 struct CoopVariant {
-    void (*kernel)(SplitBuf, int, float, int, float, int, int, int, int, int);
+    void (*kernel)(SplitBuf, int, float, int, float, int, int, int, int, int, unsigned long long);
     int nth, unroll, agg, hyb;
     int per_sm;    // resident blocks per SM with the full shared-memory budget (0 = not queried)
     int smem_max;  // dynamic shared memory budget of one block
@@ -1456,6 +1854,16 @@ static CoopVariant g_coop[] = {
     {k_s_solve_coop<1024, 1, 2, 1>, 1024, 1, 2, 1, 0, 0},
 };
 constexpr int N_COOP = sizeof(g_coop) / sizeof(g_coop[0]);
+// The same shapes under the reference's loop controls (1024 threads, one contact per thread and
+// pass): [hybrid][Nesterov]
+struct CoopLoopVariant {
+    void (*kernel)(SplitBuf, int, float, int, float, int, int, int, int, int, CoopLoopArgs, unsigned long long);
+    int per_sm, smem_max;
+};
+static CoopLoopVariant g_coop_loop[2][2] = {
+    {{k_s_solve_coop_loop<1024, 0, 0>, 0, 0}, {k_s_solve_coop_loop<1024, 0, 1>, 0, 0}},
+    {{k_s_solve_coop_loop<1024, 1, 0>, 0, 0}, {k_s_solve_coop_loop<1024, 1, 1>, 0, 0}},
+};
 
 // Batched scenes (one block per scene): threads per block and contacts per thread per pass.
 struct ScenesVariant {
@@ -1539,28 +1947,47 @@ int split_contact_blocks(int vi, int64_t n, int sms) {
 // Partition of a cooperative solve: one block per SM (all resident), contiguous contact and body
 // ranges per block. Feasible when a block's contacts (48 B each) fit in its shared memory; its free
 // velocities (32 B a body) are kept there too when they also fit.
-bool split_coop_plan(int v, int64_t nc, int64_t nbodies, int sms, CoopPlan* p, int smem_contacts, int blocks) {
-    if (!split_variant_is_coop(v) || nc <= 0) return false;
-    CoopVariant& cv = g_coop[v - N_STREAM];
-    if (cv.per_sm == 0) {
+// the shared-memory budget and residency of a cooperative kernel, queried once
+template <class K>
+static bool coop_setup(K kernel, int nth, int* per_sm, int* smem_max) {
+    if (*per_sm == 0) {
         int dev = 0, optin = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         cudaFuncAttributes fa;
-        if (cudaFuncGetAttributes(&fa, cv.kernel) != cudaSuccess) return false;
-        cv.smem_max = optin - (int)fa.sharedSizeBytes;
-        if (cv.smem_max <= 0 ||
-            cudaFuncSetAttribute(cv.kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, cv.smem_max) != cudaSuccess)
+        if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess) return false;
+        *smem_max = optin - (int)fa.sharedSizeBytes;
+        if (*smem_max <= 0 ||
+            cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, *smem_max) != cudaSuccess)
             return false;
         int b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, cv.kernel, cv.nth, cv.smem_max);
-        cv.per_sm = b > 0 ? b : -1;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, nth, *smem_max);
+        *per_sm = b > 0 ? b : -1;
     }
-    if (cv.per_sm < 1) return false;
-    const int64_t full = (int64_t)sms * cv.per_sm;
+    return *per_sm >= 1;
+}
+
+bool split_coop_plan(int v, int64_t nc, int64_t nbodies, int sms, CoopPlan* p, int smem_contacts, int blocks,
+                     int loop) {
+    if (!split_variant_is_coop(v) || nc <= 0) return false;
+    CoopVariant& cv = g_coop[v - N_STREAM];
+    int per_sm = 0, smem_max = 0;
+    if (loop) {
+        if (cv.nth != 1024 || cv.unroll != 1) return false;
+        CoopLoopVariant& lv = g_coop_loop[cv.hyb][loop == 2 ? 1 : 0];
+        if (!coop_setup(lv.kernel, cv.nth, &lv.per_sm, &lv.smem_max)) return false;
+        per_sm = lv.per_sm;
+        smem_max = lv.smem_max;
+    } else {
+        if (!coop_setup(cv.kernel, cv.nth, &cv.per_sm, &cv.smem_max)) return false;
+        per_sm = cv.per_sm;
+        smem_max = cv.smem_max;
+    }
+    const int64_t full = (int64_t)sms * per_sm;
     if (full > COOP_MAX_GRID) return false;
     // contacts a block keeps in shared memory: all that fit, or gpu.coop_smem_contacts
-    int64_t fit = cv.smem_max / 48;
+    const int64_t bpc = loop == 2 ? 64 : 48;
+    int64_t fit = smem_max / bpc;
     if (smem_contacts > 0) fit = std::min<int64_t>(fit, smem_contacts);
     // one block per SM: on a 2k-contact pile a grid of 16-64 blocks measured the same per sweep
     // (3.0 us; the barrier's cost barely depends on the block count) and fewer blocks were slower
@@ -1573,9 +2000,9 @@ bool split_coop_plan(int v, int64_t nc, int64_t nbodies, int sms, CoopPlan* p, i
     } else if (cpb > fit) {
         return false;
     }
-    const int64_t need = cpb * 48;
-    if (need > cv.smem_max || cpb < 1) return false;
-    const bool vf = need + bpb * 32 <= cv.smem_max;
+    const int64_t need = cpb * bpc;
+    if (need > smem_max || cpb < 1) return false;
+    const bool vf = need + bpb * 32 <= smem_max;
     p->grid = (int)grid;
     p->nth = cv.nth;
     p->cpb = (int)cpb;
@@ -1586,14 +2013,31 @@ bool split_coop_plan(int v, int64_t nc, int64_t nbodies, int sms, CoopPlan* p, i
 }
 
 int launch_s_solve_coop(const SplitBuf& sb, int gen, float alpha, int v, const CoopPlan& p, int max_iter, float tol,
-                        int max_sweeps, int check_every, cudaStream_t s) {
+                        int max_sweeps, int check_every, cudaStream_t s, unsigned long long wait_ns) {
     if (!split_variant_is_coop(v)) return (int)cudaErrorInvalidValue;
     const CoopVariant& cv = g_coop[v - N_STREAM];
     SplitBuf b = sb;
     int g = gen, mi = max_iter, cpb = p.cpb, bpb = p.bpb, vf = p.vf, ms = max_sweeps, ce = check_every > 0 ? check_every : 1;
     float al = alpha, t = tol;
-    void* args[] = {&b, &g, &al, &mi, &t, &cpb, &bpb, &vf, &ms, &ce};
+    unsigned long long wn = wait_ns > 0 ? wait_ns : COOP_WAIT_NS;
+    void* args[] = {&b, &g, &al, &mi, &t, &cpb, &bpb, &vf, &ms, &ce, &wn};
     return (int)cudaLaunchCooperativeKernel((const void*)cv.kernel, dim3(p.grid), dim3(cv.nth), args, (size_t)p.smem, s);
+}
+
+int launch_s_solve_coop_loop(const SplitBuf& sb, int gen, float alpha, int v, const CoopPlan& p, int max_iter,
+                             float tol, int max_sweeps, int check_every, int loop, const CoopLoopArgs& la,
+                             unsigned long long wait_ns, cudaStream_t s) {
+    if (!split_variant_is_coop(v) || loop < 1 || loop > 2) return (int)cudaErrorInvalidValue;
+    const CoopVariant& cv = g_coop[v - N_STREAM];
+    if (cv.nth != 1024 || cv.unroll != 1) return (int)cudaErrorInvalidValue;
+    const CoopLoopVariant& lv = g_coop_loop[cv.hyb][loop == 2 ? 1 : 0];
+    SplitBuf b = sb;
+    int g = gen, mi = max_iter, cpb = p.cpb, bpb = p.bpb, vf = p.vf, ms = max_sweeps, ce = check_every > 0 ? check_every : 1;
+    float al = alpha, t = tol;
+    CoopLoopArgs a = la;
+    unsigned long long wn = wait_ns > 0 ? wait_ns : COOP_WAIT_NS;
+    void* args[] = {&b, &g, &al, &mi, &t, &cpb, &bpb, &vf, &ms, &ce, &a, &wn};
+    return (int)cudaLaunchCooperativeKernel((const void*)lv.kernel, dim3(p.grid), dim3(cv.nth), args, (size_t)p.smem, s);
 }
 
 void launch_s_prep(const Scene& sc, const SplitBuf& sb, double dt, const double* g, double h1, cudaStream_t s,

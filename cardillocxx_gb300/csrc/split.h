@@ -36,6 +36,29 @@ struct SplitScalars {
     int32_t prev_count_dev;
     int32_t prev_n_static_dev;
     int32_t pair_overflow;            // copy of the narrow phase's neighbour-overflow flag
+    int32_t nonfinite;                // the step's final state holds a value that is not finite
+    // the cooperative solve under the reference's loop controls (pj.nesterov, pj.tol_abs/tol_rel),
+    // carried across launches: Nesterov's theta, last err and restart count, and which accumulators
+    // hold y (the extrapolated iterate), x_{k+1} (being formed) and x_k
+    double nes_thk;
+    double vel_err;                   // the last velocity-increment residual evaluated (err)
+    double nes_err_prev;
+    int32_t nes_restarts;
+    int32_t nes_disabled;
+    int32_t nes_iy, nes_ix1, nes_ixk;
+    int32_t pad2;
+};
+
+// Loop controls of ProjectedJacobiSolver that the cooperative solve honours (projected_jacobi.cpp:
+// 140-144, 371-377, 379-449): the velocity-increment exit every 10 sweeps of the standard loop, or
+// Nesterov's loop with its restart tests and exit.
+struct CoopLoopArgs {
+    double tol_abs, tol_rel;   // pj.tol_abs, pj.tol_rel
+    double beta_threshold;     // pj.nesterov_beta_threshold
+    int check_vel;             // standard loop: the exit is on (the tolerances are not both 0)
+    int restart_limit;         // pj.nesterov_restart_limit
+    int nv;                    // velocities (6 per body)
+    int pad;
 };
 
 struct SplitParams {
@@ -93,6 +116,8 @@ struct SplitBuf {
     SplitScalars* ss = nullptr;
     float2* part = nullptr;   // per-block (max ||dlambda||, max |lambda|) of the contact sweep
     float2* recs = nullptr;   // cooperative solve: 2 banks x per-block (max ||dlambda||, max |lambda|)
+    double2* sums = nullptr;  // cooperative solve: 2 banks x per-block sums (velocity-increment residual, dot)
+    float4* lamk = nullptr;   // Nesterov: the previous iterate's impulses (contacts outside shared memory)
     int has_restitution = 0;  // pre-solve velocities are only needed for restitution terms
 };
 
@@ -120,12 +145,21 @@ struct CoopPlan {
 };
 // smem_contacts > 0 caps the contacts a block keeps in shared memory (gpu.coop_smem_contacts);
 // blocks > 0 sets the grid (gpu.coop_blocks, capped at one block per SM), 0 = one per SM
+// loop = 0: the plain cooperative kernel; 1: the standard loop with the velocity-increment exit;
+// 2: Nesterov's loop (64 B of shared memory a contact instead of 48). Loop kernels exist for the
+// 1024-thread shapes only.
 bool split_coop_plan(int v, int64_t nc, int64_t nbodies, int sms, CoopPlan* p, int smem_contacts = 0,
-                     int blocks = 0);
+                     int blocks = 0, int loop = 0);
 // the projected Jacobi solve, up to max_sweeps sweeps, in one cooperative launch, evaluating the
-// stop rule every check_every sweeps; returns the cudaError_t of the launch
+// stop rule every check_every sweeps; a block waits at most wait_ns at a grid barrier (0 = 0.2 s);
+// returns the cudaError_t of the launch
 int launch_s_solve_coop(const SplitBuf& sb, int gen, float alpha, int v, const CoopPlan& p, int max_iter, float tol,
-                        int max_sweeps, int check_every, cudaStream_t s);
+                        int max_sweeps, int check_every, cudaStream_t s, unsigned long long wait_ns = 0);
+// the same under the reference's loop controls (loop = 1 standard loop with the velocity-increment
+// exit, 2 Nesterov); the plan must come from split_coop_plan with the same loop
+int launch_s_solve_coop_loop(const SplitBuf& sb, int gen, float alpha, int v, const CoopPlan& p, int max_iter,
+                             float tol, int max_sweeps, int check_every, int loop, const CoopLoopArgs& la,
+                             unsigned long long wait_ns, cudaStream_t s);
 void launch_s_prep(const Scene& sc, const SplitBuf& sb, double dt, const double* g, double h1, cudaStream_t s,
                    int implicit_gyro = 0);
 void launch_s_static_flags(const Scene& sc, const SplitBuf& sb, float margin, int32_t* flags, cudaStream_t s);

@@ -118,6 +118,14 @@ class PhysicsEngine:
         except Exception:
             pass
 
+    def set_config(self, cfg: "Config | dict"):
+        """Replace the configuration from the next step on (gpu.precision stays as created)."""
+        if not isinstance(cfg, Config):
+            cfg = Config(cfg)
+        self._check(self.L.cdx_set_config(self.h, C.byref(cfg.struct)))
+        self.cfg = cfg
+        return self
+
     def load_scene(self, scene: dict):
         s, keep = scene_struct(scene)
         self._check(self.L.cdx_load_scene(self.h, C.byref(s)))
@@ -162,6 +170,17 @@ class PhysicsEngine:
         pt = np.empty((m, 3)); lam = np.empty((m, 3)); nrm = np.empty((m, 3))
         self._check(self.L.cdx_get_contacts(self.h, ip(ia), ip(ib), dp(pt), dp(lam), dp(nrm), C.byref(n)))
         return {"id_a": ia, "id_b": ib, "point": pt, "lambda": lam, "normal": nrm}
+
+    def set_contacts(self, contacts: dict):
+        """Load the warm-start memory of the next step (id_a, id_b, point, lambda as contacts() gives)."""
+        ia = np.ascontiguousarray(contacts["id_a"], np.int32)
+        ib = np.ascontiguousarray(contacts["id_b"], np.int32)
+        pt = np.ascontiguousarray(contacts["point"], np.float64).reshape(-1, 3)
+        lam = np.ascontiguousarray(contacts["lambda"], np.float64).reshape(-1, 3)
+        n = ia.shape[0]
+        assert ib.shape[0] == n and pt.shape[0] == n and lam.shape[0] == n
+        self._check(self.L.cdx_set_contacts(self.h, n, ip(ia), ip(ib), dp(pt), dp(lam)))
+        return self
 
     def track(self, body: int, name: str):
         """Write sphere `body` to <output.folder>/<output.filename_prefix>_tracked.csv every step."""

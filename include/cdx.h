@@ -74,14 +74,17 @@ typedef struct cdx_config {
     int32_t gpu_sweep_variant;        /* gpu.sweep_variant: pin launch shape k (split form; -1 = default/autotuned) */
     int32_t gpu_sync_counts;          /* gpu.sync_counts: every split step stops for the host to size its contact buffers */
     /* accelerated loops of ProjectedJacobiSolver (config.hpp:85-110; projected_jacobi.cpp:179-222,
-     * 242-314, 379-449), plain FP64 method: Nesterov > Chebyshev > Anderson */
+     * 242-314, 379-449): Nesterov > Chebyshev > Anderson in the plain FP64 method; the split form runs
+     * Nesterov and the standard loop's pj.tol_abs/pj.tol_rel exit in its cooperative solve and refuses
+     * Chebyshev and Anderson with CDX_ERR_UNSUPPORTED */
     int32_t pj_nesterov;              /* pj.nesterov */
     double pj_nesterov_beta_threshold; /* pj.nesterov_beta_threshold */
     int32_t pj_nesterov_restart_limit; /* pj.nesterov_restart_limit */
     int32_t pj_chebyshev;             /* pj.chebyshev */
     int32_t pj_anderson;              /* pj.anderson */
     int32_t pj_anderson_m;            /* pj.anderson_m: history window (>= 1) */
-    int32_t pj_rdiag_true_delassus;   /* pj.rdiag_true_delassus: per-contact Delassus block preconditioner (plain FP64) */
+    int32_t pj_rdiag_true_delassus;   /* pj.rdiag_true_delassus: per-contact Delassus block preconditioner (plain FP64;
+                                         the split form's row scale is that block for sphere contacts) */
     /* frame output (PhysicsPipeline, physics_pipeline.cpp:62-113; config.hpp:20-23) */
     int32_t output_interval_steps;          /* output.interval_steps: VTK frames every k steps (0 = off) */
     int32_t output_write_contact_manifolds; /* output.write_contact_manifolds */
@@ -91,6 +94,10 @@ typedef struct cdx_config {
                                                cooperative solve keeps in shared memory (0 = all that fit) */
     int32_t gpu_coop_blocks;                /* gpu.coop_blocks: blocks of the cooperative solve (0 = one per SM;
                                                more than that is capped) */
+    int32_t gpu_pad0;
+    int64_t gpu_coop_wait_ns;               /* gpu.coop_wait_ns: longest wait of a block of the cooperative solve
+                                               at a grid barrier before the step fails with CDX_ERR_TIMEOUT
+                                               (0 = 0.2 s) */
 } cdx_config;
 
 /* Scene: dynamic spheres plus static shapes (halfspaces, drums). Bodies of one scene are
@@ -157,6 +164,10 @@ int cdx_config_from_file(const char* path, cdx_config* cfg);              /* con
  * IntegrationBase::step, integration_base.hpp:19) ---- */
 int cdx_create(const cdx_config* cfg, cdx_ctx** out);
 void cdx_destroy(cdx_ctx* ctx);
+/* Replace the configuration between steps, from the next step on: ProjectedJacobiSolver keeps a
+ * reference to the Config and reads its pj.* settings at every solve (projected_jacobi.cpp:451-500).
+ * gpu.precision cannot change (CDX_ERR_STATE); output.* keep their values from cdx_create. */
+int cdx_set_config(cdx_ctx* ctx, const cdx_config* cfg);
 const char* cdx_last_error(const cdx_ctx* ctx);
 int cdx_load_scene(cdx_ctx* ctx, const cdx_scene* scene);
 int cdx_step(cdx_ctx* ctx, int32_t nsteps);
@@ -168,6 +179,14 @@ int cdx_get_stats(cdx_ctx* ctx, cdx_stats* out);
  * pass NULL arrays to query the count */
 int cdx_get_contacts(cdx_ctx* ctx, int32_t* id_a, int32_t* id_b, double* point, double* lambda, double* normal,
                      int32_t* count);
+/* Load the warm-start memory the next step matches against: the contacts of a last step (entity id
+ * pairs, each at most once, points and impulses n/t1/t2 as cdx_get_contacts returns them). The
+ * reference keeps this memory in its ContactTracker (contact_tracker.cpp:11-72) and the solver
+ * copies matched impulses in (WarmstartProvider::applyWarmstart, warmstart.hpp:26-39); with the
+ * state calls it checkpoints and resumes a run, warm start included. Until the next step
+ * cdx_get_contacts returns this memory with zero normals. */
+int cdx_set_contacts(cdx_ctx* ctx, int32_t count, const int32_t* id_a, const int32_t* id_b, const double* point,
+                     const double* lambda);
 /* track a sphere in <output.folder>/<output.filename_prefix>_tracked.csv, one row every step
  * (World::track, world.cpp:38-45; CsvWriter::writeTrackedState, csv_writer.hpp:43-52) */
 int cdx_track(cdx_ctx* ctx, int32_t body, const char* name);

@@ -315,6 +315,23 @@ void detect(Engine& E, std::vector<Contact>& out) {
     const int N = E.N, S = E.S;
     // static contacts, ordered by (static, sphere)
     for (int s = 0; s < S; ++s) {
+        if (E.cfg.omp_mode == 1) {
+            // a static schedule hands thread t the t-th contiguous range of spheres, so appending
+            // the threads' lists in thread order keeps the sphere order
+            std::vector<std::vector<Contact>> part(omp_get_max_threads());
+#pragma omp parallel
+            {
+                std::vector<Contact>& mine = part[omp_get_thread_num()];
+#pragma omp for schedule(static)
+                for (int i = 0; i < N; ++i) {
+                    if (E.scene[i] != E.sscene[s]) continue;
+                    Contact c;
+                    if (make_contact(E, s, -1, i, c)) mine.push_back(c);
+                }
+            }
+            for (auto& p : part) out.insert(out.end(), p.begin(), p.end());
+            continue;
+        }
         for (int i = 0; i < N; ++i) {
             if (E.scene[i] != E.sscene[s]) continue;
             Contact c;
@@ -655,6 +672,8 @@ SweepOut pj_sweep(PJ& P, double* x, double* lam, double* dlam, double* acc, cons
         lnew[r] = t + P.biasR[r];
     }
     if (P.bmode) block_apply(P, lnew.data());
+    // elementwise loops below run in OpenMP too: each entry's arithmetic is the same in any order
+#pragma omp parallel for schedule(static) if (omp_all)
     for (int r = 0; r < nr; ++r) lnew[r] = lam[r] - lnew[r];
     // project(): frictionless rows, then frictional blocks (OpenMP, as the reference)
     for (int r = 0; r < P.nfl; ++r) project_rows(lnew.data(), r, false, 0.0);
@@ -679,10 +698,14 @@ SweepOut pj_sweep(PJ& P, double* x, double* lam, double* dlam, double* acc, cons
     for (int r = 0; r < P.nfl; ++r) upd(r, 1);
     for (int b = 0; b < nb; ++b) upd(P.nfl + 3 * b, 3);
     if (!apply) return so;
+    const int nv = P.nv;
+#pragma omp parallel for schedule(static) if (omp_all)
     for (int r = 0; r < nr; ++r) lam[r] = lnew[r];
-    std::fill(acc, acc + P.nv, 0.0);
+#pragma omp parallel for schedule(static) if (omp_all)
+    for (int j = 0; j < nv; ++j) acc[j] = 0.0;
     wt_accumulate(P, dlam, acc, omp_all);
-    for (int j = 0; j < P.nv; ++j) x[j] = x[j] + acc[j] / Mdiag[j];
+#pragma omp parallel for schedule(static) if (omp_all)
+    for (int j = 0; j < nv; ++j) x[j] = x[j] + acc[j] / Mdiag[j];
     return so;
 }
 
@@ -711,13 +734,16 @@ SolveResult pj_solve(PJ& P, double* rhs, const double* Mdiag, double* lam, doubl
     if (P.nrows == 0) return res;
     std::vector<double> dlam(P.nrows), acc(P.nv), xprev(P.nv);
     const int maxit = std::max(1, max_iter);
+    // with both tolerances 0 every term of residual() is a division by zero (inf or NaN), so the
+    // test is never met: the copy and the test are skipped, which changes nothing
+    const bool check_vel = !(tol_abs == 0.0 && tol_rel == 0.0);
     for (int it = 0; it < maxit; ++it) {
-        std::copy(x, x + P.nv, xprev.begin());
+        if (check_vel) std::copy(x, x + P.nv, xprev.begin());
         SweepOut so = pj_sweep(P, x, lam, dlam.data(), acc.data(), Mdiag, omp_all);
         res.iters = it + 1;
         res.res_last = rel_residual(so);
         if (trace) trace->insert(trace->end(), lam, lam + P.nrows);
-        if (it % 10 == 0 && vel_residual(x, xprev.data(), P.nv, tol_rel, tol_abs) <= 1) break;
+        if (check_vel && it % 10 == 0 && vel_residual(x, xprev.data(), P.nv, tol_rel, tol_abs) <= 1) break;
         if (residual_tol > 0 && res.res_last <= residual_tol) break;
     }
     SweepOut fin = pj_sweep(P, x, lam, dlam.data(), acc.data(), Mdiag, omp_all, false);
@@ -758,9 +784,11 @@ void pj_init(PJ& P, double* rhs, const double* Mdiag, double* lam, double* x, in
 }
 
 // nesterov_loop (projected_jacobi.cpp:379-449)
+// residual_tol (gpu.residual_tol, 0 = off): the loop also ends once the sweep's complementarity
+// residual is at most tol, tested right after the reference's own exit (in all three loops)
 SolveResult pj_solve_nesterov(PJ& P, double* rhs, const double* Mdiag, double* lam, double* x, int max_iter,
                               double tol_abs, double tol_rel, double beta_threshold, int restart_limit, int omp_all,
-                              std::vector<double>* trace) {
+                              std::vector<double>* trace, double residual_tol = 0.0) {
     SolveResult res;
     pj_init(P, rhs, Mdiag, lam, x, omp_all);
     if (P.nrows == 0) return res;
@@ -780,7 +808,7 @@ SolveResult pj_solve_nesterov(PJ& P, double* rhs, const double* Mdiag, double* l
         res.res_last = rel_residual(so);
         if (trace) trace->insert(trace->end(), lam, lam + nr);
         const double err = vel_residual_chunked(xk1.data(), xy.data(), nv, tol_rel, tol_abs);
-        if (err <= 1.0) break;
+        if (err <= 1.0 || (residual_tol > 0 && res.res_last <= residual_tol)) break;
         const double thk1 = 0.5 * (1.0 + std::sqrt(4.0 * thk * thk + 1.0));
         const double betak1 = (thk - 1.0) / thk1;
         bool restart = false;
@@ -853,7 +881,8 @@ double spectral_radius(const PJ& P, const double* Mdiag, int omp_all) {
 
 // chebyshev_loop (projected_jacobi.cpp:179-222)
 SolveResult pj_solve_chebyshev(PJ& P, double* rhs, const double* Mdiag, double* lam, double* x, int max_iter,
-                               double tol_abs, double tol_rel, int omp_all, std::vector<double>* trace) {
+                               double tol_abs, double tol_rel, int omp_all, std::vector<double>* trace,
+                               double residual_tol = 0.0) {
     SolveResult res;
     pj_init(P, rhs, Mdiag, lam, x, omp_all);
     if (P.nrows == 0) return res;
@@ -871,7 +900,7 @@ SolveResult pj_solve_chebyshev(PJ& P, double* rhs, const double* Mdiag, double* 
         res.res_last = rel_residual(so);
         if (trace) trace->insert(trace->end(), lam, lam + nr);
         const double err = vel_residual_chunked(x, xk1.data(), nv, tol_rel, tol_abs);
-        if (err <= 1.0) break;
+        if (err <= 1.0 || (residual_tol > 0 && res.res_last <= residual_tol)) break;
         double omega_next = (it == 0) ? (1.0 / (1.0 - rho2 * 0.5)) : (1.0 / (1.0 - (rho2 * 0.25) * omega));
         bool finite = true;
         for (int j = 0; j < nv && finite; ++j) finite = std::isfinite(x[j]);
@@ -941,7 +970,8 @@ bool anderson_ls(const std::vector<std::vector<double>>& dF, const std::vector<d
 // anderson_loop (projected_jacobi.cpp:242-314): z = [x; lambda], f = g(z) - z with g one sweep,
 // z_{k+1} = g(z_k) - (dZ + dF) gamma over the last m residual differences
 SolveResult pj_solve_anderson(PJ& P, double* rhs, const double* Mdiag, double* lam, double* x, int max_iter,
-                              double tol_abs, double tol_rel, int m, int omp_all, std::vector<double>* trace) {
+                              double tol_abs, double tol_rel, int m, int omp_all, std::vector<double>* trace,
+                              double residual_tol = 0.0) {
     SolveResult res;
     pj_init(P, rhs, Mdiag, lam, x, omp_all);
     if (P.nrows == 0) return res;
@@ -963,7 +993,7 @@ SolveResult pj_solve_anderson(PJ& P, double* rhs, const double* Mdiag, double* l
         res.res_last = rel_residual(so);
         if (trace) trace->insert(trace->end(), lam, lam + nr);
         const double err = vel_residual_chunked(x, xprev.data(), nv, tol_rel, tol_abs);
-        if (err <= 1.0) {
+        if (err <= 1.0 || (residual_tol > 0 && res.res_last <= residual_tol)) {
             z = w;
             break;
         }
@@ -1015,13 +1045,14 @@ SolveResult solve_dispatch(PJ& P, const or_config& cfg, double* rhs, const doubl
                            double residual_tol, int omp_all, std::vector<double>* tr) {
     if (cfg.pj_nesterov)
         return pj_solve_nesterov(P, rhs, Mdiag, lam, x, cfg.pj_max_iterations, cfg.pj_tol_abs, cfg.pj_tol_rel,
-                                 cfg.pj_nesterov_beta_threshold, cfg.pj_nesterov_restart_limit, omp_all, tr);
+                                 cfg.pj_nesterov_beta_threshold, cfg.pj_nesterov_restart_limit, omp_all, tr,
+                                 residual_tol);
     if (cfg.pj_chebyshev)
         return pj_solve_chebyshev(P, rhs, Mdiag, lam, x, cfg.pj_max_iterations, cfg.pj_tol_abs, cfg.pj_tol_rel,
-                                  omp_all, tr);
+                                  omp_all, tr, residual_tol);
     if (cfg.pj_anderson)
         return pj_solve_anderson(P, rhs, Mdiag, lam, x, cfg.pj_max_iterations, cfg.pj_tol_abs, cfg.pj_tol_rel,
-                                 cfg.pj_anderson_m, omp_all, tr);
+                                 cfg.pj_anderson_m, omp_all, tr, residual_tol);
     return pj_solve(P, rhs, Mdiag, lam, x, cfg.pj_max_iterations, cfg.pj_tol_abs, cfg.pj_tol_rel, residual_tol, omp_all,
                     tr);
 }
@@ -1037,6 +1068,8 @@ void step_once(Engine& E) {
     // G_rot is i w_k - w_k i = 0 exactly, so S stays diag(M).
     const bool implicit_gyro = E.cfg.moreau_implicit_gyroscopy != 0;
     std::vector<double> rhs(nv), vn(nv);
+    // the per-body loops of the step are elementwise: OpenMP in the all-threads mode
+#pragma omp parallel for schedule(static) if (omp_all)
     for (int i = 0; i < N; ++i) {
         const double* w = &E.w[3 * (size_t)i];
         const double Iw[3] = {E.inertia[i] * w[0], E.inertia[i] * w[1], E.inertia[i] * w[2]};
@@ -1054,8 +1087,10 @@ void step_once(Engine& E) {
     }
     // drift 1: (1 - theta) h, every entity with a velocity (statics included)
     const double h1 = (1.0 - th) * dt;
+#pragma omp parallel for schedule(static) if (omp_all)
     for (int i = 0; i < N; ++i) drift(&E.pos[3 * (size_t)i], &E.q[4 * (size_t)i], &E.v[3 * (size_t)i], &E.w[3 * (size_t)i], h1);
     for (int s = 0; s < S; ++s) drift(&E.spos[3 * s], &E.sq[4 * s], &E.sv[3 * s], &E.sw[3 * s], h1);
+#pragma omp parallel for schedule(static) if (omp_all)
     for (int i = 0; i < N; ++i) rotmat(&E.q[4 * (size_t)i], &E.R[9 * (size_t)i]);
     for (int s = 0; s < S; ++s) rotmat(&E.sq[4 * s], &E.sR[9 * s]);
 
@@ -1101,6 +1136,7 @@ void step_once(Engine& E) {
     E.trace.clear();
     SolveResult sr;
     if (C.empty()) {
+#pragma omp parallel for schedule(static) if (omp_all)
         for (int j = 0; j < nv; ++j) x[j] = rhs[j] / E.Mdiag[j];
     } else {
         std::vector<double>* tr = E.trace_on ? &E.trace : nullptr;
@@ -1122,6 +1158,7 @@ void step_once(Engine& E) {
     E.last = C;
     E.last_lambda = E.prev_lambda;
     // writeVelocityToSystem (dynamics_assembler.cpp:145-188)
+#pragma omp parallel for schedule(static) if (omp_all)
     for (int i = 0; i < N; ++i)
         for (int k = 0; k < 3; ++k) {
             E.v[3 * (size_t)i + k] = x[6 * i + k];
@@ -1129,6 +1166,7 @@ void step_once(Engine& E) {
         }
     // drift 2: theta h
     const double h2 = th * dt;
+#pragma omp parallel for schedule(static) if (omp_all)
     for (int i = 0; i < N; ++i) drift(&E.pos[3 * (size_t)i], &E.q[4 * (size_t)i], &E.v[3 * (size_t)i], &E.w[3 * (size_t)i], h2);
     for (int s = 0; s < S; ++s) drift(&E.spos[3 * s], &E.sq[4 * s], &E.sv[3 * s], &E.sw[3 * s], h2);
     E.stats.num_contacts = (int32_t)C.size();
@@ -1223,6 +1261,28 @@ int32_t or_get_contacts(void* h, int32_t* id_a, int32_t* id_b, double* point, do
         }
     }
     return (int32_t)C;
+}
+
+// the tracker's memory for the next step's warm start (contact_tracker.cpp:11-72): pairs sorted by
+// key, their contact points and impulses
+void or_set_contacts(void* h, int32_t n, const int32_t* id_a, const int32_t* id_b, const double* point,
+                     const double* lambda) {
+    Engine* E = (Engine*)h;
+    std::vector<size_t> order(n);
+    for (int32_t i = 0; i < n; ++i) order[i] = (size_t)i;
+    auto key = [&](size_t i) { return ((uint64_t)(uint32_t)id_a[i] << 32) | (uint64_t)(uint32_t)id_b[i]; };
+    std::sort(order.begin(), order.end(), [&](size_t x, size_t y) { return key(x) < key(y); });
+    E->prev_keys.resize(n);
+    E->prev_point.resize(3 * (size_t)n);
+    E->prev_lambda.resize(3 * (size_t)n);
+    for (int32_t c = 0; c < n; ++c) {
+        const size_t o = order[c];
+        E->prev_keys[c] = key(o);
+        for (int k = 0; k < 3; ++k) {
+            E->prev_point[3 * (size_t)c + k] = point[3 * o + k];
+            E->prev_lambda[3 * (size_t)c + k] = lambda[3 * o + k];
+        }
+    }
 }
 
 void or_set_trace(void* h, int32_t on) { ((Engine*)h)->trace_on = on != 0; }

@@ -93,6 +93,9 @@ void or_get_stats(void* h, or_stats* out);
 /* contacts of the last step, canonical order: ids (statics first, then spheres offset by S),
  * contact points, impulses (n,t1,t2), normals */
 int32_t or_get_contacts(void* h, int32_t* id_a, int32_t* id_b, double* point, double* lambda, double* normal);
+/* the warm-start memory of the next step: contacts of a last step (id pairs, points, impulses) */
+void or_set_contacts(void* h, int32_t n, const int32_t* id_a, const int32_t* id_b, const double* point,
+                     const double* lambda);
 /* per-iteration impulse trace of the next step: after or_set_trace(h,1) the next step records
  * lambda (rows in canonical contact order, 3 per contact) after every sweep */
 void or_set_trace(void* h, int32_t on);

@@ -110,6 +110,7 @@ def lib():
             L.or_get_contacts.restype = C.c_int32
             L.or_get_contacts.argtypes = [C.c_void_p, _PI, _PI, _P, _P, _P]
             L.or_set_trace.argtypes = [C.c_void_p, C.c_int32]
+            L.or_set_contacts.argtypes = [C.c_void_p, C.c_int32, _PI, _PI, _P, _P]
             L.or_get_trace.restype = C.c_int32
             L.or_get_trace.argtypes = [C.c_void_p, _P, C.c_int64]
             L.or_pj_solve_csr.restype = C.c_int32
@@ -224,6 +225,15 @@ class Oracle:
         pt = np.empty((n, 3)); lam = np.empty((n, 3)); nrm = np.empty((n, 3))
         self.L.or_get_contacts(self.h, _ip(ia), _ip(ib), _dp(pt), _dp(lam), _dp(nrm))
         return {"id_a": ia, "id_b": ib, "point": pt, "lambda": lam, "normal": nrm}
+
+    def set_contacts(self, contacts: dict):
+        """Warm-start memory of the next step (id_a, id_b, point, lambda)."""
+        ia = np.ascontiguousarray(contacts["id_a"], np.int32)
+        ib = np.ascontiguousarray(contacts["id_b"], np.int32)
+        pt = np.ascontiguousarray(contacts["point"], np.float64).reshape(-1, 3)
+        lam = np.ascontiguousarray(contacts["lambda"], np.float64).reshape(-1, 3)
+        self.L.or_set_contacts(self.h, int(ia.shape[0]), _ip(ia), _ip(ib), _dp(pt), _dp(lam))
+        return self
 
     def set_trace(self, on: bool = True):
         self.L.or_set_trace(self.h, int(on))

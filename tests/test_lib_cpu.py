@@ -153,6 +153,24 @@ def test_acceleration_keys(cdxlib):
     assert c.set("solver.rdiag_true_delassus", "on").get("pj_rdiag_true_delassus") == 1
 
 
+def test_split_form_refuses_the_loops_it_does_not_run(cdxlib):
+    # the split form runs Nesterov and the standard loop (with its tolerance exit); Chebyshev and
+    # Anderson, selected when Nesterov is off (projected_jacobi.cpp:470-491), are refused when the
+    # context is created, before any device call, instead of silently running another loop
+    from cardillocxx_gb300 import CdxError, PhysicsEngine
+    from cardillocxx_gb300._lib import STATUS
+    for key in ("pj.chebyshev", "pj.anderson"):
+        with pytest.raises(CdxError) as e:
+            PhysicsEngine({"gpu.precision": "split", key: True})
+        assert e.value.status == 6 and STATUS[6] == "CDX_ERR_UNSUPPORTED"
+        assert "plain FP64" in str(e.value)
+    from cardillocxx_gb300.engine import Config
+    c = Config({"gpu.coop_wait_ns": 5000})
+    assert c.get("gpu_coop_wait_ns") == 5000
+    assert Config().get("gpu_coop_wait_ns") == 0
+    assert Config({"gpu.coop_wait_ns": -1}).get("gpu_coop_wait_ns") == 0  # bad values keep the default
+
+
 def test_output_keys(cdxlib):
     # output.* keys of the reference (config.hpp:20-23); frames are off unless interval_steps is set
     from cardillocxx_gb300 import CdxError

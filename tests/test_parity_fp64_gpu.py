@@ -276,3 +276,55 @@ def test_implicit_gyroscopy_parity(gpu, oracle_mod):
     e64 = PhysicsEngine(cfg).load_scene(s)
     e64.step(60)
     np.testing.assert_allclose(e32.state()["pos"], e64.state()["pos"], rtol=0, atol=1e-5)
+
+
+def with_state(scene, st):
+    s = dict(scene)
+    for k in ("pos", "quat", "vel", "omega"):
+        s[k] = st[k].copy()
+    return s
+
+
+def test_checkpoint_and_resume_with_the_warm_start_memory(oracle_mod):
+    # state + contact memory (cdx_get_state / cdx_get_contacts) taken after 120 steps and loaded
+    # into a fresh context (cdx_set_state / cdx_set_contacts) and into the oracle: the resumed runs
+    # continue bit for bit as the uninterrupted one, warm start included
+    s = scenes.generate("pile_1k", scale=0.3)
+    cfg = scenes.config_for("pile_1k")
+    run = PhysicsEngine(cfg).load_scene(s)
+    run.step(120)
+    st, mem = run.state(), run.contacts()
+    assert mem["id_a"].shape[0] > 50
+    resumed = PhysicsEngine(cfg).load_scene(with_state(s, st))
+    resumed.set_contacts({k: mem[k][::-1] for k in ("id_a", "id_b", "point", "lambda")})  # any order
+    back = resumed.contacts()
+    for k in ("id_a", "id_b", "point", "lambda"):
+        assert_same(back[k], mem[k], f"loaded memory {k}")
+    orc = oracle_mod.Oracle(with_state(s, st), cfg).set_contacts(mem)
+    cold = PhysicsEngine(cfg).load_scene(with_state(s, st))
+    for e in (run, resumed, orc, cold):
+        e.step(5)
+    a, b, o = run.state(), resumed.state(), orc.state()
+    for k in ("pos", "quat", "vel", "omega"):
+        assert_same(b[k], a[k], f"resumed {k}")
+        assert_same(o[k], a[k], f"oracle resumed {k}")
+    assert_same(resumed.contacts()["lambda"], run.contacts()["lambda"], "impulses after resuming")
+    # without the memory the first step starts from zero impulses and the run differs
+    assert not np.array_equal(cold.state()["vel"], a["vel"])
+
+
+def test_contact_memory_is_validated():
+    s = scenes.generate("pile_1k", scale=0.05)
+    e = PhysicsEngine(scenes.config_for("pile_1k")).load_scene(s)
+    S = s["static_kind"].shape[0]
+    ok = {"id_a": np.array([0]), "id_b": np.array([S]), "point": np.zeros((1, 3)), "lambda": np.ones((1, 3))}
+    e.set_contacts(ok)
+    from cardillocxx_gb300 import CdxError
+    for bad in ({"id_b": np.array([S + 10 ** 6])}, {"id_a": np.array([S + 1]), "id_b": np.array([S])},
+                {"lambda": np.full((1, 3), np.nan)}):
+        with pytest.raises(CdxError):
+            e.set_contacts(dict(ok, **bad))
+    with pytest.raises(CdxError):
+        e.set_contacts({k: np.concatenate([v, v]) for k, v in ok.items()})  # a pair twice
+    e.set_contacts({k: v[:0] for k, v in ok.items()})
+    e.step(1)
