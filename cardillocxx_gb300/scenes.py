@@ -120,6 +120,51 @@ def generate(preset: str, scale: float = 1.0, seed: int | None = None, **kw) -> 
     return out
 
 
+def settled_pile(path: str) -> dict:
+    """The settled pile stored by tests/golden/make_pile_200k_settled.py as a scene dict, at rest.
+
+    Positions and radii are the stored FP32 values; velocities are zero and orientations the
+    identity; mass and inertia follow from the radius and the stored density (solid spheres). NumPy
+    only: building the scene loads no native code, so a CPU-only process can use it too.
+    """
+    d = np.load(path)
+    pos = d["pos"].astype(np.float64)
+    r = d["radius"].astype(np.float64)
+    N = pos.shape[0]
+    mass = float(d["density"]) * ((4.0 / 3.0) * math.pi * r * r * r)
+    out = {"pos": pos, "quat": np.tile(np.array([0.0, 0.0, 0.0, 1.0]), (N, 1)), "vel": np.zeros((N, 3)),
+           "omega": np.zeros((N, 3)), "radius": r, "mass": mass, "inertia": (2.0 / 5.0) * r * r * mass,
+           "mu": np.full(N, float(d["mu"])), "rest_n": np.zeros(N), "rest_t": np.zeros(N),
+           "body_scene": np.zeros(N, np.int32)}
+    for k in ("static_kind", "static_pos", "static_quat", "static_vel", "static_omega", "static_dir",
+              "static_radius", "static_mu", "static_rest_n", "static_rest_t"):
+        out[k] = np.array(d[k])
+    out["static_scene"] = np.zeros(out["static_kind"].shape[0], np.int32)
+    out["num_scenes"] = 1
+    return out
+
+
+def scene_digest(scene: dict) -> str:
+    """SHA-256 (first 16 hex digits) of a scene's arrays, to show two processes start alike."""
+    import hashlib
+    h = hashlib.sha256()
+    for k in sorted(scene):
+        v = scene[k]
+        if isinstance(v, np.ndarray):
+            h.update(k.encode())
+            h.update(np.ascontiguousarray(v).tobytes())
+    return h.hexdigest()[:16]
+
+
+def state_digest(state: dict) -> str:
+    """SHA-256 (first 16 hex digits) of a body state (positions, orientations, velocities)."""
+    import hashlib
+    h = hashlib.sha256()
+    for k in ("pos", "quat", "vel", "omega"):
+        h.update(np.ascontiguousarray(state[k], np.float64).tobytes())
+    return h.hexdigest()[:16]
+
+
 def make_scene(bodies: list[dict], statics: list[dict], scene_ids=None, static_scene_ids=None) -> dict:
     """Hand-built scene from per-body dicts (pos, radius, density|mass, vel, omega, quat, mu, rest_n)
     and statics (kind 'halfspace'|'drum', pos, dir, radius, vel, omega, mu)."""

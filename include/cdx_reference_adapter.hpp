@@ -12,7 +12,8 @@
 //      block preconditioner, the tolerances) for the sweeps.
 //  * GpuMoreauIntegrator : cardillo::integration::IntegrationBase
 //      replaces MoreauIntegrator (src/physics/integration/moreau.cpp:6-13) for sphere scenes:
-//      the whole step (collision, contact rows, PJ, drift) runs in cdx_step.
+//      the whole step (collision, contact rows, PJ, drift) runs in cdx_step; the ECS components
+//      of the spheres are uploaded before and written back after each step.
 #pragma once
 #ifdef CDX_WITH_CARDILLO
 
@@ -21,9 +22,11 @@
 #include <vector>
 
 #include "cdx.h"
+#include "physics/ecs_types.hpp"
 #include "physics/integration/integration_base.hpp"
 #include "physics/solver/solver_base.hpp"
 #include "physics/solver/warmstart.hpp"
+#include "physics/world.hpp"
 
 namespace cardillo::solver {
 
@@ -92,19 +95,208 @@ class GpuProjectedJacobiSolver : public SolverBase {
 
 namespace cardillo::integration {
 
-// Whole-step drop-in for sphere scenes. The scene is mirrored once (and again whenever the ECS
-// structure changes); each step uploads the state, runs cdx_step, and writes the state back.
+// Whole-step drop-in for sphere scenes: MoreauIntegrator::step (src/physics/integration/moreau.cpp:
+// 6-13) behind IntegrationBase::step (integration_base.hpp:19). Selected where the pipeline builds
+// its integrator (physics_pipeline.cpp:34-51), e.g. for integrator=gpu_moreau.
+//  - Dynamic spheres are the entities with C_RB_Sphere, C_Radius and C_PhysicsObject; static
+//    halfspaces the entities with C_RB_Plane and no C_PhysicsObject (the components
+//    RigidBodyFactory::create gives them, rigid_body_factory.cpp:110-209). Entity ids in the
+//    context: the statics first, then the spheres, each in view order.
+//  - The scene is mirrored into one cdx context when the world's structure changes
+//    (World::m_structure_dirty, consumed here because this step replaces the assembler's) or dt
+//    changes. Each step uploads the spheres' state from the ECS (a user may have edited it),
+//    runs cdx_step(1) (refreshState, the (1 - theta) h drift, collision and contact rows, the
+//    projected Jacobi solve, writeVelocityToSystem and the theta h drift), and writes the new
+//    state back into C_Position3, C_Orientation (setValue keeps the rotation in sync),
+//    C_LinearVelocity3 and C_AngularVelocity3 (body frame). The warm-start memory stays in the
+//    context across steps.
+//  - Other dynamic shapes (boxes, meshes, capsules, cones, cylinders), dynamic planes, point
+//    masses without C_RB_Sphere, constraints and soft bodies are not on this path: step() throws
+//    std::runtime_error, as the reference's own components throw on what they cannot handle.
+//  - precision: CDX_PRECISION_FP64 (bit-identical to the reference restatement) or
+//    CDX_PRECISION_SPLIT (FP32 contacts and solve, FP64 state).
 class GpuMoreauIntegrator : public IntegrationBase {
    public:
-    using IntegrationBase::IntegrationBase;
+    GpuMoreauIntegrator(World& world, solver::SolverBase& solver, physics::DynamicsAssembler& dyn,
+                        misc::TimingManager& timings, config::Config& config,
+                        int32_t precision = CDX_PRECISION_FP64)
+        : IntegrationBase(world, solver, dyn, timings, config), m_precision(precision) {}
     ~GpuMoreauIntegrator() override { cdx_destroy(m_ctx); }
 
-    void step(real_t dt) override;  // defined in gpu_moreau.cpp next to moreau.cpp: gathers the
-                                    // sphere/halfspace entities into a cdx_scene, cdx_set_state,
-                                    // cdx_step(1), cdx_get_state, then writes C_Position3,
-                                    // C_Orientation, C_LinearVelocity3, C_AngularVelocity3
+    void step(real_t dt) override {
+        if (!m_ctx || m_world.m_structure_dirty || dt != m_dt) rebuild(dt);
+        auto& reg = m_world.ecs();
+        const size_t n = m_spheres.size();
+        for (size_t i = 0; i < n; ++i) {
+            const entt::entity e = m_spheres[i];
+            const auto& x = reg.get<C_Position3>(e).value;
+            const auto& q = reg.get<C_Orientation>(e).value;
+            const auto& v = reg.get<C_LinearVelocity3>(e).value;
+            const auto& w = reg.get<C_AngularVelocity3>(e).value;
+            for (int k = 0; k < 3; ++k) {
+                m_pos[3 * i + k] = x[k];
+                m_vel[3 * i + k] = v[k];
+                m_omega[3 * i + k] = w[k];
+            }
+            m_quat[4 * i + 0] = q.x();
+            m_quat[4 * i + 1] = q.y();
+            m_quat[4 * i + 2] = q.z();
+            m_quat[4 * i + 3] = q.w();
+        }
+        check(cdx_set_state(m_ctx, m_pos.data(), m_quat.data(), m_vel.data(), m_omega.data()));
+        check(cdx_step(m_ctx, 1));
+        check(cdx_get_state(m_ctx, m_pos.data(), m_quat.data(), m_vel.data(), m_omega.data()));
+        for (size_t i = 0; i < n; ++i) {
+            const entt::entity e = m_spheres[i];
+            auto& x = reg.get<C_Position3>(e).value;
+            auto& v = reg.get<C_LinearVelocity3>(e).value;
+            auto& w = reg.get<C_AngularVelocity3>(e).value;
+            for (int k = 0; k < 3; ++k) {
+                x[k] = m_pos[3 * i + k];
+                v[k] = m_vel[3 * i + k];
+                w[k] = m_omega[3 * i + k];
+            }
+            reg.get<C_Orientation>(e).setValue(
+                Quaternion4r(m_quat[4 * i + 3], m_quat[4 * i + 0], m_quat[4 * i + 1], m_quat[4 * i + 2]));
+        }
+    }
+
    private:
+    void check(int st) const {
+        if (st != CDX_OK)
+            throw std::runtime_error(std::string("GpuMoreauIntegrator: ") + (m_ctx ? cdx_last_error(m_ctx) : "cdx"));
+    }
+
+    // the reference's settings for the step (config.hpp:12-237) in the context's configuration
+    cdx_config make_config(real_t dt) const {
+        cdx_config c;
+        cdx_config_default(&c);
+        const config::Config& r = m_config;
+        c.sim_dt = dt;
+        const auto& g = m_world.gravity();
+        for (int k = 0; k < 3; ++k) c.sim_gravity[k] = g[k];
+        c.moreau_theta = r.moreau_theta;
+        c.moreau_implicit_gyroscopy = r.moreau_implicit_gyroscopy ? 1 : 0;
+        c.friction_enable = r.friction_enable ? 1 : 0;
+        c.friction_combine = r.friction_combine == "arith" ? 1 : (r.friction_combine == "geom" ? 2 : 0);
+        c.restitution_default_normal = r.restitution_default_normal;
+        c.restitution_default_tangential = r.restitution_default_tangential;
+        c.pj_alpha = r.pj_alpha;
+        c.pj_max_iterations = r.pj_max_iterations;
+        c.pj_warmstart = r.pj_warmstart ? 1 : 0;
+        c.pj_tol_abs = r.pj_tol_abs;
+        c.pj_tol_rel = r.pj_tol_rel;
+        c.pj_nesterov = r.pj_nesterov ? 1 : 0;
+        c.pj_nesterov_beta_threshold = r.pj_nesterov_beta_threshold;
+        c.pj_nesterov_restart_limit = r.pj_nesterov_restart_limit;
+        c.pj_chebyshev = r.pj_chebyshev ? 1 : 0;
+        c.pj_anderson = r.pj_anderson ? 1 : 0;
+        c.pj_anderson_m = r.pj_anderson_m;
+        c.pj_rdiag_true_delassus = r.pj_rdiag_true_delassus ? 1 : 0;
+        c.collision_security_margin = r.collision_security_margin;
+        c.collision_match_max_dist = r.collision_match_max_dist;
+        c.gpu_precision = m_precision;
+        return c;
+    }
+
+    void rebuild(real_t dt) {
+        auto& reg = m_world.ecs();
+        m_spheres.clear();
+        std::vector<entt::entity> planes;
+        size_t dynamic = 0;
+        for (auto e : reg.view<C_PhysicsObject>()) {
+            ++dynamic;
+            if (!reg.all_of<C_RB_Sphere, C_Radius, C_Mass, C_InertiaDiag>(e))
+                throw std::runtime_error("GpuMoreauIntegrator: only rigid spheres move on the GPU path");
+            m_spheres.push_back(e);
+        }
+        for (auto e : reg.view<C_RB_Plane>()) {
+            if (reg.all_of<C_PhysicsObject>(e))
+                throw std::runtime_error("GpuMoreauIntegrator: dynamic planes are not on the GPU path");
+            planes.push_back(e);
+        }
+        const size_t n = m_spheres.size(), ns = planes.size();
+        (void)dynamic;
+        std::vector<double> rad(n), mass(n), inertia(n), mu(n), rn(n), rt(n);
+        m_pos.assign(3 * n, 0.0);
+        m_quat.assign(4 * n, 0.0);
+        m_vel.assign(3 * n, 0.0);
+        m_omega.assign(3 * n, 0.0);
+        const config::Config& r = m_config;
+        for (size_t i = 0; i < n; ++i) {
+            const entt::entity e = m_spheres[i];
+            rad[i] = reg.get<C_Radius>(e).r;
+            mass[i] = reg.get<C_Mass>(e).m;
+            inertia[i] = reg.get<C_InertiaDiag>(e).I[0];  // isotropic for a sphere
+            mu[i] = reg.all_of<C_Friction>(e) ? reg.get<C_Friction>(e).mu : r.friction_default_mu;
+            rn[i] = reg.all_of<C_Restitution>(e) ? reg.get<C_Restitution>(e).normal : 0.0;
+            rt[i] = reg.all_of<C_Restitution>(e) ? reg.get<C_Restitution>(e).tangential : 0.0;
+        }
+        std::vector<int32_t> kind(ns, CDX_STATIC_HALFSPACE);
+        std::vector<double> spos(3 * ns), squat(4 * ns), svel(3 * ns, 0.0), somega(3 * ns, 0.0), sdir(3 * ns),
+            srad(ns, 0.0), smu(ns), srn(ns), srt(ns);
+        for (size_t s = 0; s < ns; ++s) {
+            const entt::entity e = planes[s];
+            const auto& x = reg.get<C_Position3>(e).value;
+            const auto& o = reg.get<C_Orientation>(e);
+            // the halfspace normal in the world frame (CollisionCoal builds it from C_RB_Plane's
+            // normal and the entity pose, collision_coal.cpp:290-296)
+            const Vector3r nw = o.rotation * reg.get<C_RB_Plane>(e).normal.normalized();
+            for (int k = 0; k < 3; ++k) {
+                spos[3 * s + k] = x[k];
+                sdir[3 * s + k] = nw[k];
+            }
+            squat[4 * s + 0] = o.value.x();
+            squat[4 * s + 1] = o.value.y();
+            squat[4 * s + 2] = o.value.z();
+            squat[4 * s + 3] = o.value.w();
+            if (reg.all_of<C_LinearVelocity3>(e))
+                for (int k = 0; k < 3; ++k) svel[3 * s + k] = reg.get<C_LinearVelocity3>(e).value[k];
+            if (reg.all_of<C_AngularVelocity3>(e))
+                for (int k = 0; k < 3; ++k) somega[3 * s + k] = reg.get<C_AngularVelocity3>(e).value[k];
+            smu[s] = reg.all_of<C_Friction>(e) ? reg.get<C_Friction>(e).mu : r.friction_default_mu;
+            srn[s] = reg.all_of<C_Restitution>(e) ? reg.get<C_Restitution>(e).normal : 0.0;
+            srt[s] = reg.all_of<C_Restitution>(e) ? reg.get<C_Restitution>(e).tangential : 0.0;
+        }
+        cdx_destroy(m_ctx);
+        m_ctx = nullptr;
+        const cdx_config c = make_config(dt);
+        check(cdx_create(&c, &m_ctx));
+        cdx_scene sc{};
+        sc.num_bodies = (int32_t)n;
+        sc.pos = m_pos.data();
+        sc.quat = m_quat.data();
+        sc.vel = m_vel.data();
+        sc.omega = m_omega.data();
+        for (size_t i = 0; i < n; ++i) m_quat[4 * i + 3] = 1.0;  // overwritten by the first upload
+        sc.radius = rad.data();
+        sc.mass = mass.data();
+        sc.inertia = inertia.data();
+        sc.mu = mu.data();
+        sc.rest_n = rn.data();
+        sc.rest_t = rt.data();
+        sc.num_statics = (int32_t)ns;
+        sc.static_kind = kind.data();
+        sc.static_pos = spos.data();
+        sc.static_quat = squat.data();
+        sc.static_vel = svel.data();
+        sc.static_omega = somega.data();
+        sc.static_dir = sdir.data();
+        sc.static_radius = srad.data();
+        sc.static_mu = smu.data();
+        sc.static_rest_n = srn.data();
+        sc.static_rest_t = srt.data();
+        sc.num_scenes = 1;
+        check(cdx_load_scene(m_ctx, &sc));
+        m_dt = dt;
+        m_world.m_structure_dirty = false;
+    }
+
+    int32_t m_precision;
     cdx_ctx* m_ctx = nullptr;
+    real_t m_dt = 0;
+    std::vector<entt::entity> m_spheres;
+    std::vector<double> m_pos, m_quat, m_vel, m_omega;
 };
 
 }  // namespace cardillo::integration

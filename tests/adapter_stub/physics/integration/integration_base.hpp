@@ -1,27 +1,28 @@
-// Stand-in for IntegrationBase (integration_base.hpp:19): its constructor and step(dt).
+// Stand-in for IntegrationBase (integration_base.hpp:12-32): its constructor, step(dt) and the
+// protected references under their reference names.
 #pragma once
 #include "../solver/solver_base.hpp"
+#include "../world.hpp"
 
 namespace cardillo {
-class World {};
 namespace misc {
 class TimingManager {};
 }
 namespace integration {
 class IntegrationBase {
    public:
-    IntegrationBase(World& w, solver::SolverBase& s, physics::DynamicsAssembler& d, misc::TimingManager& t,
-                    config::Config& c)
-        : m_world(w), m_solver(s), m_dyn(d), m_timings(t), m_cfg(c) {}
+    explicit IntegrationBase(World& world, solver::SolverBase& solver, physics::DynamicsAssembler& dyn,
+                             misc::TimingManager& timings, config::Config& config)
+        : m_world(world), m_dyn(dyn), m_timings(timings), m_solver(solver), m_config(config) {}
     virtual ~IntegrationBase() = default;
     virtual void step(real_t dt) = 0;
 
    protected:
     World& m_world;
-    solver::SolverBase& m_solver;
     physics::DynamicsAssembler& m_dyn;
     misc::TimingManager& m_timings;
-    config::Config& m_cfg;
+    solver::SolverBase& m_solver;
+    config::Config& m_config;
 };
 }  // namespace integration
 }  // namespace cardillo

@@ -1,8 +1,9 @@
 // Minimal stand-ins for the reference interfaces the adapter header uses (names and signatures of
 // SolverBase, DynamicsAssembler, Config; solver_base.hpp:14-37, dynamics_assembler.hpp:23-94,
-// config.hpp:79-112), so the adapter can be compiled syntax-only without Eigen and EnTT.
+// config.hpp:12-237), so the adapter can be compiled syntax-only without Eigen and EnTT.
 #pragma once
 #include <cstdint>
+#include <string>
 #include <vector>
 
 namespace cardillo {
@@ -24,6 +25,15 @@ struct VectorXr {
 
 namespace config {
 struct Config {
+    real_t sim_dt{1e-3};
+    real_t moreau_theta{1.0};
+    bool friction_enable{false};
+    std::string friction_combine{"min"};
+    real_t friction_default_mu{0.3};
+    real_t restitution_default_normal{0.0};
+    real_t restitution_default_tangential{0.0};
+    real_t collision_security_margin{0.0};
+    real_t collision_match_max_dist{0.02};
     bool pj_warmstart{true};
     bool moreau_implicit_gyroscopy{false};
     real_t pj_alpha{1.0};

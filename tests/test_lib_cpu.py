@@ -197,7 +197,13 @@ def test_reference_adapter_compiles_against_interface_stubs(tmp_path):
     src.write_text('#include "cdx_reference_adapter.hpp"\n'
                    'static cardillo::solver::SolverBase* make(cardillo::physics::DynamicsAssembler& d, '
                    'const cardillo::config::Config& c) { return new cardillo::solver::GpuProjectedJacobiSolver(d, c); }\n'
-                   'int main() { (void)&make; return 0; }\n')
+                   'static cardillo::integration::IntegrationBase* make_int(cardillo::World& w, '
+                   'cardillo::solver::SolverBase& s, cardillo::physics::DynamicsAssembler& d, '
+                   'cardillo::misc::TimingManager& t, cardillo::config::Config& c) {\n'
+                   '  auto* g = new cardillo::integration::GpuMoreauIntegrator(w, s, d, t, c, CDX_PRECISION_SPLIT);\n'
+                   '  g->step(1e-3);\n'
+                   '  return g; }\n'
+                   'int main() { (void)&make; (void)&make_int; return 0; }\n')
     cmd = ["g++", "-std=c++17", "-fsyntax-only", "-Wall", "-Werror", "-DCDX_WITH_CARDILLO",
            "-I", os.path.join(root, "include"), "-I", os.path.join(root, "tests", "adapter_stub"), str(src)]
     p = subprocess.run(cmd, capture_output=True, text=True)

@@ -5,6 +5,8 @@ trajectories within 1e-9 over the run; the plain method is built to be bit-ident
 operation order, no FMA contraction, deterministic gathers), so these tests assert exact equality
 and report the largest difference when it fails.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -328,3 +330,32 @@ def test_contact_memory_is_validated():
         e.set_contacts({k: np.concatenate([v, v]) for k, v in ok.items()})  # a pair twice
     e.set_contacts({k: v[:0] for k, v in ok.items()})
     e.step(1)
+
+
+PILE_200K = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "pile_200k_settled.npz")
+
+
+def test_settled_pile_200k_is_bit_identical_to_the_oracle(oracle_mod):
+    # the benchmark's input at full size: 200,000 settled spheres, about 480,000 contacts, 100 sweeps a
+    # step from zero impulses, then warm-started steps. Three steps of the plain FP64 method against the
+    # oracle (OpenMP over all host threads, bit-identical to its sequential mode): states, contacts,
+    # impulses and sweep counts equal bit for bit after every step
+    s = scenes.settled_pile(PILE_200K)
+    cfg = scenes.config_for("pile_200k")
+    assert s["pos"].shape[0] == 200000
+    eng = PhysicsEngine(dict(cfg, **{"gpu.precision": "fp64"})).load_scene(s)
+    orc = oracle_mod.Oracle(s, cfg, omp_mode=1, num_threads=os.cpu_count() or 1)
+    for k in range(3):
+        eng.step(1)
+        orc.step(1)
+        g, o = eng.state(), orc.state()
+        for key in ("pos", "quat", "vel", "omega"):
+            assert_same(g[key], o[key], f"{key} after step {k + 1}")
+        gc, oc = eng.contacts(), orc.contacts()
+        assert gc["id_a"].shape[0] > 400000
+        for key in ("id_a", "id_b", "point", "lambda", "normal"):
+            assert_same(gc[key], oc[key], f"contact {key} after step {k + 1}")
+        gs, os_ = eng.stats(), orc.stats()
+        assert gs["iterations"] == os_["iterations"] == 100
+        assert gs["num_rows"] == os_["num_rows"]
+        assert gs["residual"] == os_["residual"]

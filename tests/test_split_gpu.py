@@ -14,6 +14,11 @@ pytestmark = pytest.mark.gpu
 G = 9.81
 H = 1e-3
 F32_RTOL = 2e-5  # FP32 contact arithmetic: relative tolerance on impulses and velocities
+# split form against the FP64 method on a converged step with the same contact set (FP32 rounding
+# of the contact algebra and of the summation of W^T lambda)
+SAME_CONTACTS_RTOL = 1e-5
+# two split-form shapes (the same FP32 sweep, another summation order) after a few hundred sweeps
+SAME_SWEEP_RTOL = 1e-4
 
 
 def cfg(**kw):
@@ -79,11 +84,13 @@ def test_split_one_step_matches_fp64(gpu):
         e.step(1)
     c64, c32 = e64.contacts(), e32.contacts()
     assert np.array_equal(c64["id_a"], c32["id_a"]) and np.array_equal(c64["id_b"], c32["id_b"])
+    # the same contacts: the two forms differ by FP32 rounding only (measured 2-5e-7 relative)
     lmax = np.abs(c64["lambda"]).max()
-    assert np.abs(c64["lambda"][:, 0] - c32["lambda"][:, 0]).max() <= 5e-3 * lmax
+    dl = np.abs(c64["lambda"] - c32["lambda"]).max() / lmax
     v64, v32 = e64.state()["vel"], e32.state()["vel"]
     vscale = np.abs(st["vel"]).max() + G * H
-    assert np.abs(v64 - v32).max() <= 5e-3 * vscale
+    dv = np.abs(v64 - v32).max() / vscale
+    assert dl <= SAME_CONTACTS_RTOL and dv <= SAME_CONTACTS_RTOL, (dl, dv)
     np.testing.assert_allclose(e64.state()["pos"], e32.state()["pos"], rtol=0, atol=1e-7)
 
 
@@ -115,8 +122,8 @@ def test_split_every_sweep_shape_computes_the_same_sweep(gpu):
     vscale = np.abs(st["vel"]).max() + G * H
     for label, lam, vel in out:
         assert lam.shape == lam0.shape, label
-        assert np.abs(lam - lam0).max() <= 1e-3 * lmax, label
-        assert np.abs(vel - vel0).max() <= 1e-3 * vscale, label
+        dl, dv = np.abs(lam - lam0).max() / lmax, np.abs(vel - vel0).max() / vscale
+        assert dl <= SAME_SWEEP_RTOL and dv <= SAME_SWEEP_RTOL, (label, dl, dv)
 
 
 def test_split_residual_is_fp64_and_decreases(gpu):
@@ -209,7 +216,8 @@ def test_batched_scenes_solver_matches_fp64_and_streaming(gpu):
     assert np.array_equal(np.sort(c64["id_a"] * 10**7 + c64["id_b"]), np.sort(c32["id_a"] * 10**7 + c32["id_b"]))
     vscale = np.abs(st["vel"]).max() + 9.81 * 1e-3
     for other in (e64, e32s):
-        assert np.abs(other.state()["vel"] - e32.state()["vel"]).max() <= 5e-3 * vscale
+        dv = np.abs(other.state()["vel"] - e32.state()["vel"]).max() / vscale
+        assert dv <= SAME_CONTACTS_RTOL, dv
     np.testing.assert_allclose(e64.state()["pos"], e32.state()["pos"], rtol=0, atol=1e-7)
     # then a run of the batched workload with warm start: stays finite and resting
     e = PhysicsEngine(dict(base, **{"gpu.precision": "split"})).load_scene(s)
@@ -344,6 +352,6 @@ def test_hybrid_cooperative_solve_streams_what_shared_memory_cannot_hold(gpu):
     assert out["coop-hyb-t1024-u1-g2"][0]["num_contacts"] > 4 * 152  # more than the cap holds
     lam0, vel0 = out["sweep-u1-t256-b4-g2"][1:]
     lam1, vel1 = out["coop-hyb-t1024-u1-g2"][1:]
-    assert np.abs(lam1 - lam0).max() <= 1e-3 * np.abs(lam0).max()
     vscale = np.abs(st["vel"]).max() + G * H
-    assert np.abs(vel1 - vel0).max() <= 1e-3 * vscale
+    dl, dv = np.abs(lam1 - lam0).max() / np.abs(lam0).max(), np.abs(vel1 - vel0).max() / vscale
+    assert dl <= SAME_SWEEP_RTOL and dv <= SAME_SWEEP_RTOL, (dl, dv)
