@@ -9,7 +9,9 @@ from __future__ import annotations
 
 import concurrent.futures as cf
 import glob
+import hashlib
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -32,11 +34,31 @@ def _cuda_home() -> str:
     raise RuntimeError("CUDA toolkit not found")
 
 
-def _needs(obj: str, deps: list[str]) -> bool:
-    if not os.path.exists(obj):
+def _stamp(cmd: list[str], deps: list[str]) -> str:
+    """Digest of what an output is built from: the command, the machine and every input's bytes."""
+    h = hashlib.sha256()
+    h.update(" ".join(cmd).encode())
+    h.update(platform.machine().encode())
+    for d in sorted(deps):
+        h.update(d.encode())
+        with open(d, "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()
+
+
+def _needs(out: str, stamp: str) -> bool:
+    """An output is rebuilt unless it exists with a stamp equal to its inputs' digest (file times
+    are not trusted: a copied tree may carry objects newer than their sources, or built for
+    another machine)."""
+    if not os.path.exists(out) or not os.path.exists(out + ".stamp"):
         return True
-    t = os.path.getmtime(obj)
-    return any(os.path.getmtime(d) > t for d in deps)
+    with open(out + ".stamp") as f:
+        return f.read().strip() != stamp
+
+
+def _mark(out: str, stamp: str) -> None:
+    with open(out + ".stamp", "w") as f:
+        f.write(stamp + "\n")
 
 
 def build(verbose: bool = False, force: bool = False) -> str:
@@ -61,11 +83,13 @@ def build(verbose: bool = False, force: bool = False) -> str:
 
     def run(job):
         obj, deps, cmd = job
-        if not force and not _needs(obj, deps):
+        stamp = _stamp(cmd, deps)
+        if not force and not _needs(obj, stamp):
             return obj, ""
         p = subprocess.run(cmd, capture_output=True, text=True)
         if p.returncode != 0:
             raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{p.stdout}\n{p.stderr}")
+        _mark(obj, stamp)
         return obj, p.stderr
 
     objs = []
@@ -74,15 +98,18 @@ def build(verbose: bool = False, force: bool = False) -> str:
             objs.append(obj)
             if verbose and log.strip():
                 print(log, file=sys.stderr)
-    if force or _needs(LIB, objs):
-        libdir = os.path.join(cuda, "lib64")
+    libdir = os.path.join(cuda, "lib64")
+    link = ["g++", "-shared", "-o", LIB, *objs, "-L", libdir, "-lcudart_static", "-ldl", "-lrt", "-lpthread",
+            "-Wl,--no-undefined"]
+    lstamp = _stamp(link, objs)
+    if force or _needs(LIB, lstamp):
         tmp = LIB + f".{os.getpid()}.tmp"
-        cmd = ["g++", "-shared", "-o", tmp, *objs, "-L", libdir, "-lcudart_static", "-ldl", "-lrt", "-lpthread",
-               "-Wl,--no-undefined"]
+        cmd = [tmp if c == LIB else c for c in link]
         p = subprocess.run(cmd, capture_output=True, text=True)
         if p.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{p.stdout}\n{p.stderr}")
         os.replace(tmp, LIB)
+        _mark(LIB, lstamp)
     return LIB
 
 

@@ -10,10 +10,13 @@
 // library holds that array until the process exits.
 //
 // Setup: the first call on a device, with that device current, looks up the array's device
-// address with cudaGetSymbolAddress (host code cannot use the symbol itself as a device pointer).
-// Make that first call before any stream capture. All calls share the one array and it keeps the
-// last call's contents; everything that must start at zero is cleared by each call. Calls that
-// overlap on the GPU (different streams or host threads at the same time) race on the array.
+// address with cudaGetSymbolAddress (host code cannot use the symbol itself as a device pointer)
+// and keeps it for that device. Make that first call before any stream capture. cudaDeviceReset
+// discards the array with the context, and the kept address then no longer holds: do not reset a
+// device between calls. A call returns once its work on the stream has finished (it waits on the
+// stream). All calls share the one array and it keeps the last call's contents; everything that
+// must start at zero is cleared by each call. Calls that overlap on the GPU (different streams
+// or host threads at the same time) race on the array.
 #include <cstdio>
 #include <cstring>
 #include <mutex>

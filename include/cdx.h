@@ -269,7 +269,9 @@ int cdx_pj_solve_csr_cfg(cdx_ctx* ctx, const cdx_config* cfg, int32_t nrows, int
  * (pre-reserved pools, real-time loops, code where allocation calls are not allowed).
  *   - stream: cudaStream_t as void* (NULL = the legacy default stream).
  *   - The first call on a device (with that device current) looks up the array's address with
- *     cudaGetSymbolAddress; make it before any stream capture.
+ *     cudaGetSymbolAddress and keeps it; make it before any stream capture. cudaDeviceReset
+ *     discards the array, and the kept address with it: do not reset the device between calls.
+ *   - A call returns once its work on the stream has finished.
  *   - Problems that do not fit return CDX_ERR_OVERFLOW with the message in err (errlen bytes).
  *   - All calls share the array: calls that overlap on the GPU race; run them one at a time. */
 #define CDX_NOALLOC_SCRATCH_BYTES (16u << 20)

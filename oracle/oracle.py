@@ -23,18 +23,29 @@ _lib = None
 
 
 def build(force: bool = False) -> str:
-    """Compile the oracle with g++ (no FMA contraction, OpenMP)."""
+    """Compile the oracle with g++ (no FMA contraction, OpenMP). Rebuilt unless the library carries
+    a stamp equal to the digest of its sources, command and machine (file times are not trusted)."""
+    import hashlib
+    import platform
     srcs = [os.path.join(HERE, "cdx_oracle.cpp"), os.path.join(HERE, "cdx_adjoint.cpp")]
     hdr = os.path.join(HERE, "cdx_oracle.h")
-    if (not force and os.path.exists(LIB)
-            and os.path.getmtime(LIB) >= max(os.path.getmtime(f) for f in srcs + [hdr])):
-        return LIB
+    cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+           "-fno-fast-math", *srcs, "-o", LIB]
+    h = hashlib.sha256((" ".join(cmd) + platform.machine()).encode())
+    for f in srcs + [hdr]:
+        with open(f, "rb") as fh:
+            h.update(fh.read())
+    stamp = h.hexdigest()
+    if not force and os.path.exists(LIB) and os.path.exists(LIB + ".stamp"):
+        with open(LIB + ".stamp") as fh:
+            if fh.read().strip() == stamp:
+                return LIB
     os.makedirs(BUILD, exist_ok=True)
     tmp = LIB + f".{os.getpid()}.tmp"
-    cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
-           "-fno-fast-math", *srcs, "-o", tmp]
-    subprocess.check_call(cmd)
+    subprocess.check_call([tmp if c == LIB else c for c in cmd])
     os.replace(tmp, LIB)
+    with open(LIB + ".stamp", "w") as fh:
+        fh.write(stamp + "\n")
     return LIB
 
 

@@ -71,3 +71,17 @@ def test_noalloc_rejects_oversized_problem(gpu):
     st, _, _, _, msg = _noalloc(gpu, p, 5, 0.0, 0.0)
     assert st == 3  # CDX_ERR_OVERFLOW
     assert "scratch array" in msg
+
+
+def test_noalloc_without_contacts_matches_allocating_entry_point(gpu):
+    # no contact rows: both entry points return the free velocities S^-1 rhs and no sweeps
+    from cardillocxx_gb300 import PhysicsEngine
+    eng = PhysicsEngine({})
+    p = _problem(10, nfl=0, nfr=0)
+    assert p["row_ptr"].shape[0] == 1
+    x_ref, lam_ref, it_ref = eng.pj_solve_csr(**p, dt=1e-3, alpha=0.3, max_iter=50, tol_abs=0.0, tol_rel=0.0)
+    for _ in range(2):
+        st, x, lam, it, msg = _noalloc(gpu, p, 50, 0.0, 0.0)
+        assert st == 0, msg
+        assert it == it_ref and lam.shape == (0,)
+        assert np.array_equal(x, x_ref)
