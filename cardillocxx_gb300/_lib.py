@@ -74,6 +74,8 @@ class CdxConfig(C.Structure):
         ("gpu_coop_blocks", C.c_int32),
         ("gpu_pad0", C.c_int32),
         ("gpu_coop_wait_ns", C.c_int64),
+        ("condensed_sweep_mode", C.c_int32),
+        ("pad1", C.c_int32),
     ]
 
 

@@ -156,6 +156,33 @@ struct AndersonBufs {
     AndersonState* st = nullptr;
 };
 
+// condensed solver, colored sweeps (plain FP64 method): per contact 1/G_ii, rhs and the internal
+// impulses (3 rows, field-major by cap), the block's degree and color; per body the free
+// velocities, u_corr and its previous sweep (6 x N, field-major); the blocks sorted by color
+#define CDX_COND_MAX_COLORS 128
+struct CondBufs {
+    int64_t cap = 0;
+    int N = 0;
+    double* ginv = nullptr;
+    double* rhs = nullptr;
+    double* lam = nullptr;
+    int32_t* deg = nullptr;
+    int32_t* col = nullptr;
+    int32_t* col2 = nullptr;
+    double* uf = nullptr;
+    double* u = nullptr;
+    double* up = nullptr;
+    double* part = nullptr;
+    int32_t* flags = nullptr;  // [0] diverged, [1] uncolored after a round, [2] more colors than the limit
+    double* err = nullptr;     // the last residual (err) evaluated
+    uint32_t* kin = nullptr;   // sort by color: keys (colors) and values (contacts), in and out
+    uint32_t* vin = nullptr;
+    uint32_t* kout = nullptr;
+    uint32_t* vout = nullptr;
+    int32_t* cstart = nullptr;  // CDX_COND_MAX_COLORS per-color ranges of vout
+    int32_t* cend = nullptr;
+};
+
 struct Incidence {
     int64_t cap = 0;
     uint32_t* key_in = nullptr;
@@ -184,6 +211,23 @@ void launch_unpack_state(const Scene& sc, const double* in, int mask, cudaStream
 
 // ---- FP64 plain method (k_fp64.cu) ----
 void launch_rhs64(const Scene& sc, double dt, const double* g, double* rhs, cudaStream_t s, int implicit_gyro = 0);
+// condensed solver, colored sweeps (k_fp64_condensed.cu)
+void launch_cond_setup(const Scene& sc, Contacts& C, int gen, int nc, double dt, const double* g, int implicit_gyro,
+                       int warmstart, CondBufs& B, const Incidence& inc, cudaStream_t s);
+void launch_cond_color_round(const Contacts& C, int nc, const CondBufs& B, const Incidence& inc,
+                             const int32_t* col_in, int32_t* col_out, int32_t* uncolored, int32_t* too_many,
+                             cudaStream_t s);
+void launch_cond_sweep_color(const Scene& sc, const Contacts& C, const CondBufs& B, const uint32_t* blocks, int n,
+                             double relax, double alpha, double* u, const DevScalars* ds, cudaStream_t s);
+int cond_chunks(int N);
+void launch_cond_sort_keys(int nc, const int32_t* col, CondBufs& B, cudaStream_t s);
+void launch_cond_check(int N, const CondBufs& B, double tol_rel, double tol_abs, int iter, DevScalars* ds,
+                       cudaStream_t s);
+void launch_cond_copy(int n, const double* src, double* dst, const DevScalars* ds, cudaStream_t s);
+// pj_convention < 0: x = u_free - u_corr; 0: impulses as stored for the warm start; 1: impulses in
+// the projected Jacobi convention (for the complementarity residual)
+void launch_cond_final(const Scene& sc, Contacts& C, int gen, int nc, const CondBufs& B, double* x, int pj_convention,
+                       cudaStream_t s);
 // nonfinite (optional): set to 1 when a body's state after the drift is not finite
 void launch_drift64(const Scene& sc, double h, int compute_R, cudaStream_t s, int32_t* nonfinite = nullptr);
 void launch_static_flags64(const Scene& sc, double margin, int32_t* flags, cudaStream_t s);
@@ -205,7 +249,8 @@ void launch_contact_setup64(const Scene& sc, Contacts& C, int gen, int nc, int p
                             double match2, int warmstart, cudaStream_t s);
 void launch_frictionless_flags(const Contacts& C, int nc, int32_t* isfl, cudaStream_t s);
 void launch_rank_and_incidence(const Scene& sc, Contacts& C, int nc, const int32_t* fl_scan, const int32_t* isfl,
-                               Incidence& inc, cudaStream_t s);
+                               Incidence& inc, cudaStream_t s,
+                               int by_contact = 0);
 void launch_xinit64(const Scene& sc, const Contacts& C, int gen, const Incidence& inc, const double* rhs, double* x,
                     cudaStream_t s);
 void launch_sweep_contact64(const Scene& sc, Contacts& C, int gen, int nc, const double* x, DevScalars* ds, int dry,

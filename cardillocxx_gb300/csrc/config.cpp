@@ -81,6 +81,7 @@ int cdx_config_default(cdx_config* c) {
     c->pj_alpha = 0.3;
     c->pj_relaxation = 1.0;
     c->solver_type = 0;
+    c->condensed_sweep_mode = 0;  // condensed.sweep_mode = gauss_seidel (config.hpp:118)
     c->collision_security_margin = 0.0;
     c->collision_match_max_dist = 0.02;
     c->collision_broadphase = 0;
@@ -131,7 +132,14 @@ int cdx_config_set(cdx_config* c, const char* key_c, const char* val_c) {
     } else if (key == "solver.type") {
         const std::string v = lower(val);
         if (v == "projected_jacobi" || v == "projectedjacobi" || v == "pj" || v == "gpu_pj") c->solver_type = 0;
+        else if (v == "condensed" || v == "condensed_solver") c->solver_type = 1;
         else return CDX_ERR_UNSUPPORTED;  // other solvers are not on this path
+    } else if (key == "condensed.sweep_mode") {
+        const std::string v = lower(val);
+        if (v == "gauss_seidel") c->condensed_sweep_mode = 0;
+        else if (v == "jacobi") c->condensed_sweep_mode = 1;
+        else if (v == "colored") c->condensed_sweep_mode = 2;
+        else if (v == "chaotic") c->condensed_sweep_mode = 3;
     } else if (key == "moreau.theta" || key == "solver.theta") {
         if (as_double(val, &d)) c->moreau_theta = d;
     } else if (key == "moreau.implicit_gyroscopy" || key == "solver.implicit_gyroscopy") {

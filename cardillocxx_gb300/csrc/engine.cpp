@@ -79,13 +79,7 @@ Engine::~Engine() {
 int Engine::init(const cdx_config& c) {
     cfg = c;
     if (cfg.output_interval_steps > 0) out = new cdx::Output(cfg);
-    if (cfg.solver_type != 0) return fail(CDX_ERR_UNSUPPORTED, "only solver.type=projected_jacobi is on this path");
-    // the split form runs the reference's Nesterov loop and the standard loop's tolerance exit in its
-    // cooperative solve; Chebyshev and Anderson (selected when Nesterov is off, as in
-    // projected_jacobi.cpp:470-491) run in the plain FP64 method only
-    if (cfg.gpu_precision == CDX_PRECISION_SPLIT && !cfg.pj_nesterov && (cfg.pj_chebyshev || cfg.pj_anderson))
-        return fail(CDX_ERR_UNSUPPORTED, "pj.chebyshev and pj.anderson run in the plain FP64 method only "
-                                         "(gpu.precision=fp64); the split form runs pj.nesterov and the standard loop");
+    if (int st0 = check_solver_config(cfg)) return st0;
     int st = cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
     if (st) return st;
     st = cuda_check(cudaMallocHost((void**)&hs, sizeof(DevScalars)), "cudaMallocHost");
@@ -98,17 +92,37 @@ int Engine::init(const cdx_config& c) {
     return CDX_OK;
 }
 
+// The solver settings this library runs, and a clear refusal for the others:
+//  - the split form runs the reference's Nesterov loop and the standard loop's tolerance exit in
+//    its cooperative solve; Chebyshev and Anderson (selected when Nesterov is off, as in
+//    projected_jacobi.cpp:470-491) run in the plain FP64 method only;
+//  - solver.type=condensed runs in the plain FP64 method with condensed.sweep_mode=colored (its
+//    other sweep modes, and its Nesterov and Chebyshev loops, are not built).
+int Engine::check_solver_config(const cdx_config& c) {
+    if (c.solver_type != 0 && c.solver_type != 1)
+        return fail(CDX_ERR_UNSUPPORTED, "only solver.type=projected_jacobi and condensed are on this path");
+    if (c.gpu_precision == CDX_PRECISION_SPLIT && !c.pj_nesterov && (c.pj_chebyshev || c.pj_anderson))
+        return fail(CDX_ERR_UNSUPPORTED, "pj.chebyshev and pj.anderson run in the plain FP64 method only "
+                                         "(gpu.precision=fp64); the split form runs pj.nesterov and the standard loop");
+    if (c.solver_type == 1) {
+        if (c.gpu_precision != CDX_PRECISION_FP64)
+            return fail(CDX_ERR_UNSUPPORTED, "solver.type=condensed runs in the plain FP64 method (gpu.precision=fp64)");
+        if (c.condensed_sweep_mode != 2)
+            return fail(CDX_ERR_UNSUPPORTED, "solver.type=condensed runs with condensed.sweep_mode=colored on the GPU");
+        if (c.pj_nesterov || c.pj_chebyshev)
+            return fail(CDX_ERR_UNSUPPORTED, "solver.type=condensed runs its standard loop (no pj.nesterov or pj.chebyshev)");
+    }
+    return CDX_OK;
+}
+
 // ProjectedJacobiSolver holds a reference to the Config and reads its pj.* settings at every solve
 // (projected_jacobi.cpp:451-500), so a caller may change them between steps. Here the new settings
 // apply from the next step; the precision (which selects the buffers) and the frame output (whose
 // writer is set up at creation) stay as created.
 int Engine::set_config(const cdx_config& c) {
-    if (c.solver_type != 0) return fail(CDX_ERR_UNSUPPORTED, "only solver.type=projected_jacobi is on this path");
     if (c.gpu_precision != cfg.gpu_precision)
         return fail(CDX_ERR_STATE, "gpu.precision is fixed when the context is created");
-    if (c.gpu_precision == CDX_PRECISION_SPLIT && !c.pj_nesterov && (c.pj_chebyshev || c.pj_anderson))
-        return fail(CDX_ERR_UNSUPPORTED, "pj.chebyshev and pj.anderson run in the plain FP64 method only "
-                                         "(gpu.precision=fp64); the split form runs pj.nesterov and the standard loop");
+    if (int st0 = check_solver_config(c)) return st0;
     cdx_config n = c;
     n.output_interval_steps = cfg.output_interval_steps;
     n.output_write_contact_manifolds = cfg.output_write_contact_manifolds;
@@ -488,7 +502,7 @@ int Engine::setup64() {
         if ((st = cuda_check(exclusive_scan(tmp, tmp_bytes, isfl, flscan, nc, stream), "scan"))) return st;
         launches += 2;
     }
-    launch_rank_and_incidence(sc, C, nc, flscan, isfl, inc, stream);
+    launch_rank_and_incidence(sc, C, nc, flscan, isfl, inc, stream, cfg.solver_type == 1 ? 1 : 0);
     int key_bits = 1;
     while (((int64_t)1 << key_bits) <= sc.N) ++key_bits;
     if (nc > 0) {
@@ -746,7 +760,7 @@ int Engine::step64() {
     if (timing) cudaEventRecord(ev[1], stream);
     if ((st = setup64())) return st;
     if (timing) cudaEventRecord(ev[2], stream);
-    if ((st = solve64())) return st;
+    if ((st = (cfg.solver_type == 1 ? solve_condensed() : solve64()))) return st;
     if (timing) cudaEventRecord(ev[3], stream);
     launch_writeback64(sc, x, stream);
     launch_drift64(sc, th * dt, 0, stream, &ds->nonfinite);
@@ -774,6 +788,9 @@ int Engine::step64() {
     // a state that is no longer finite (an input NaN, or a blow-up) ends the step with an error;
     // the step itself completed and the context stays usable (cdx_set_state can repair the state)
     if (hs->nonfinite) return fail(CDX_ERR_NONFINITE, "the state after the step is not finite (NaN or infinity)");
+    if (cond_diverged)
+        return fail(CDX_ERR_NONFINITE, "condensed solver diverged: the velocity-increment residual is not finite "
+                                       "(pj.tol_abs and pj.tol_rel must not both be 0)");
     return CDX_OK;
 }
 

@@ -117,6 +117,12 @@ struct Engine {
     int init(const cdx_config& c);
     // replace the configuration between steps (the solver reads its settings every solve)
     int set_config(const cdx_config& c);
+    int check_solver_config(const cdx_config& c);
+    // condensed solver, colored sweeps (plain FP64 method; engine_condensed.cpp)
+    cdx::CondBufs cond;
+    int cond_diverged = 0;
+    int ensure_cond();
+    int solve_condensed();
     void split_config_changed();
     int load_scene(const cdx_scene& s);
     int ensure_tmp(int64_t n);

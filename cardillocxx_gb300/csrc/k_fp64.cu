@@ -625,18 +625,21 @@ __global__ void k_frictionless_flags(Contacts C, int nc, int32_t* isfl) {
 
 // solver row order: frictionless contacts first, then frictional ones, each in canonical order
 // (rebuildW_'s two passes, dynamics_assembler.cpp:236-324); incidence list input in that order
+// by_contact: the incidence lists keep contact order instead of solver row order (the condensed
+// solver's blocks are in contact order)
 __global__ void k_rank_incidence(int N, Contacts C, int nc, const int32_t* fl_scan, const int32_t* isfl,
-                                 Incidence inc) {
+                                 Incidence inc, int by_contact) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nc) return;
     const int nfl = fl_scan[nc - 1] + isfl[nc - 1];
     const int rank = isfl[c] ? fl_scan[c] : nfl + (c - fl_scan[c]);
     C.rank[c] = rank;
+    const int pos = by_contact ? c : rank;
     const int a = C.a[c];
-    inc.key_in[2 * (size_t)rank] = a >= 0 ? (uint32_t)a : (uint32_t)N;
-    inc.val_in[2 * (size_t)rank] = (uint32_t)(2 * c);
-    inc.key_in[2 * (size_t)rank + 1] = (uint32_t)C.b[c];
-    inc.val_in[2 * (size_t)rank + 1] = (uint32_t)(2 * c + 1);
+    inc.key_in[2 * (size_t)pos] = a >= 0 ? (uint32_t)a : (uint32_t)N;
+    inc.val_in[2 * (size_t)pos] = (uint32_t)(2 * c);
+    inc.key_in[2 * (size_t)pos + 1] = (uint32_t)C.b[c];
+    inc.val_in[2 * (size_t)pos + 1] = (uint32_t)(2 * c + 1);
 }
 
 // body gather of W^T y over the incidence list (rows in solver order); acc is accumulated in place
@@ -1410,9 +1413,9 @@ void launch_frictionless_flags(const Contacts& C, int nc, int32_t* isfl, cudaStr
     k_frictionless_flags<<<nblk(nc), NT, 0, s>>>(C, nc, isfl);
 }
 void launch_rank_and_incidence(const Scene& sc, Contacts& C, int nc, const int32_t* fl_scan, const int32_t* isfl,
-                               Incidence& inc, cudaStream_t s) {
+                               Incidence& inc, cudaStream_t s, int by_contact) {
     if (nc == 0) return;
-    k_rank_incidence<<<nblk(nc), NT, 0, s>>>(sc.N, C, nc, fl_scan, isfl, inc);
+    k_rank_incidence<<<nblk(nc), NT, 0, s>>>(sc.N, C, nc, fl_scan, isfl, inc, by_contact);
 }
 void launch_xinit64(const Scene& sc, const Contacts& C, int gen, const Incidence& inc, const double* rhs, double* x,
                     cudaStream_t s) {

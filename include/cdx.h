@@ -60,7 +60,8 @@ typedef struct cdx_config {
     double pj_tol_rel;                /* pj.tol_rel */
     double pj_alpha;                  /* pj.alpha */
     double pj_relaxation;             /* pj.relaxation (accepted, unused by PJ as in the reference) */
-    int32_t solver_type;              /* solver.type: 0 projected_jacobi (the only one here) */
+    int32_t solver_type;              /* solver.type: 0 projected_jacobi, 1 condensed (plain FP64 method,
+                                         condensed.sweep_mode=colored) */
     double collision_security_margin; /* collision.security_margin */
     double collision_match_max_dist;  /* collision.match_max_dist */
     int32_t collision_broadphase;     /* collision.broadphase: 0 uniform_grid (any reference value maps here) */
@@ -98,6 +99,9 @@ typedef struct cdx_config {
     int64_t gpu_coop_wait_ns;               /* gpu.coop_wait_ns: longest wait of a block of the cooperative solve
                                                at a grid barrier before the step fails with CDX_ERR_TIMEOUT
                                                (0 = 0.2 s) */
+    int32_t condensed_sweep_mode;           /* condensed.sweep_mode: 0 gauss_seidel (default), 1 jacobi,
+                                               2 colored (the one run on the GPU), 3 chaotic */
+    int32_t pad1;
 } cdx_config;
 
 /* Scene: dynamic spheres plus static shapes (halfspaces, drums). Bodies of one scene are

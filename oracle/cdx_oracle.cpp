@@ -141,6 +141,7 @@ struct Engine {
     std::vector<double> trace;
     or_stats stats{};
     double rmax = 0;
+    int status = 0;  // 4 once a condensed solve diverged
 };
 
 // Sphere mass matrix, src/physics/assembly/dynamics_assembler.cpp:41-62 (rebuildMass_) with
@@ -1057,6 +1058,242 @@ SolveResult solve_dispatch(PJ& P, const or_config& cfg, double* rhs, const doubl
                     tr);
 }
 
+// ---- the condensed solver's colored sweep, src/physics/solver/condensed_solver.cpp ----
+// CondensedSolver::solve (condensed_solver.cpp:443-760) with condensed.sweep_mode=colored, the
+// projection local solve, natural ordering, no true_schur / auto_alpha, and the standard loop, for
+// sphere contacts. One block per contact in contact order (condensed_assembler.cpp:203-262); its
+// rows are the contact's W rows split by side: Ja = -[d_r, r_A x d_r] on body A (when dynamic),
+// Jb = +[d_r, r_B x d_r] on body B. Internally the normal impulse is <= 0 (PGS's convention,
+// projectBlock :41-52) and the velocity is u = u_free - u_corr.
+struct CondBlock {
+    int ci, dim, a, b;  // contact, rows, dynamic body of side A (-1: static) and of side B
+    double Ja[18], Jb[18];  // dim x 6, row major
+    double ginv[3], rhs[3], mu;
+};
+
+// Welsh-Powell greedy coloring (misc/graph_coloring.cpp:8-40) of the blocks' shared-body graph
+// (buildBlockAdjacency, condensed_solver.cpp:175-199): blocks by decreasing degree, each taking the
+// smallest color no already-colored neighbour uses. Equal degrees keep block order (a stable
+// sort; the reference's std::sort leaves their order unspecified). Returns the color of each block.
+std::vector<int> color_blocks(const std::vector<CondBlock>& B, int nbodies, int* ncolors) {
+    const int n = (int)B.size();
+    std::vector<std::vector<int>> inc(nbodies);
+    for (int i = 0; i < n; ++i) {
+        if (B[i].a >= 0) inc[B[i].a].push_back(i);
+        inc[B[i].b].push_back(i);
+    }
+    std::vector<std::vector<int>> adj(n);
+    for (const auto& list : inc)
+        for (size_t x = 0; x < list.size(); ++x)
+            for (size_t y = x + 1; y < list.size(); ++y) {
+                adj[list[x]].push_back(list[y]);
+                adj[list[y]].push_back(list[x]);
+            }
+    for (auto& v : adj) {
+        std::sort(v.begin(), v.end());
+        v.erase(std::unique(v.begin(), v.end()), v.end());
+    }
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return adj[x].size() > adj[y].size(); });
+    std::vector<int> color(n, -1), stamp;
+    int st = 0, nc = 0;
+    for (int node : order) {
+        ++st;
+        for (int nb : adj[node]) {
+            const int c = color[nb];
+            if (c < 0) continue;
+            if (c >= (int)stamp.size()) stamp.resize(c + 1, -1);
+            stamp[c] = st;
+        }
+        int chosen = 0;
+        while (chosen < (int)stamp.size() && stamp[chosen] == st) ++chosen;
+        color[node] = chosen;
+        nc = std::max(nc, chosen + 1);
+    }
+    *ncolors = nc;
+    return color;
+}
+
+// u_corr += M^-1 J^T delta for one side (scatterDelta, condensed_solver.cpp:78-96)
+inline void cond_scatter(const double* J, int dim, const double* d, const double* minv, double* u) {
+    for (int k = 0; k < 6; ++k) {
+        double t = J[k] * d[0];
+        for (int r = 1; r < dim; ++r) t = t + J[6 * r + k] * d[r];
+        u[k] = u[k] + minv[k] * t;
+    }
+}
+// sum_k J_rk u_k of one row against one body's six velocities
+inline double cond_row(const double* Jr, const double* u) {
+    double t = Jr[0] * u[0];
+    for (int k = 1; k < 6; ++k) t = t + Jr[k] * u[k];
+    return t;
+}
+
+// One block of the colored sweep: coloredSweep's body (condensed_solver.cpp:205-226) with
+// blockResidual (:62-69), computeBlockUpdate (:139-158) and projectBlock (:41-52).
+void cond_block_update(const CondBlock& k, double relax, double alpha, const double* minv, double* lam, double* u) {
+    const int dim = k.dim;
+    double r[3], lo[3], ln[3], d[3];
+    for (int q = 0; q < dim; ++q) {
+        double o = k.rhs[q];
+        if (k.a >= 0) o = o - cond_row(&k.Ja[6 * q], &u[6 * (size_t)k.a]);
+        o = o - cond_row(&k.Jb[6 * q], &u[6 * (size_t)k.b]);
+        o = o - 0.0 * lam[q];  // contact rows carry no compliance
+        r[q] = o;
+        lo[q] = lam[q];
+    }
+    for (int q = 0; q < dim; ++q) {
+        // GiiInv is the diagonal of 1/G_ii stored as a dense block (condensed_assembler.cpp:308-312)
+        double g = (q == 0 ? k.ginv[0] : 0.0) * r[0];
+        for (int j = 1; j < dim; ++j) g = g + (q == j ? k.ginv[j] : 0.0) * r[j];
+        ln[q] = ((relax * g) * alpha) + lo[q];
+    }
+    ln[0] = std::min(ln[0], 0.0);
+    if (dim == 3) {
+        const double tn = std::sqrt(ln[1] * ln[1] + ln[2] * ln[2]);
+        if (tn > 0.0) {
+            const double sc = std::min(1.0, (-k.mu * ln[0]) / tn);
+            ln[1] = ln[1] * sc;
+            ln[2] = ln[2] * sc;
+        }
+    }
+    for (int q = 0; q < dim; ++q) d[q] = ln[q] - lo[q];
+    if (k.a >= 0) cond_scatter(k.Ja, dim, d, &minv[6 * (size_t)k.a], &u[6 * (size_t)k.a]);
+    cond_scatter(k.Jb, dim, d, &minv[6 * (size_t)k.b], &u[6 * (size_t)k.b]);
+    for (int q = 0; q < dim; ++q) lam[q] = ln[q];
+}
+
+struct CondResult {
+    int iters = 0;
+    bool diverged = false;
+    double err = 0;
+};
+
+// residualNorm (condensed_solver.cpp:500-506): sqrt(1/nV) ||(u_cur - u_prev) / q||, q = tol_rel
+// max(|u_free - u_prev|, |u_free - u_cur|) + tol_abs, the sum in the fixed chunked order
+double cond_residual(const std::vector<double>& uf, const std::vector<double>& up, const std::vector<double>& uc,
+                     double tol_rel, double tol_abs) {
+    const int nv = (int)uf.size();
+    const double s = chunk_sum(nv, [&](int j) {
+        const double diff = uc[j] - up[j];
+        const double v0 = uf[j] - up[j], v1 = uf[j] - uc[j];
+        const double q = std::max(std::fabs(v0), std::fabs(v1)) * tol_rel + tol_abs;
+        const double t = diff / q;
+        return t * t;
+    });
+    return 1.0 / std::sqrt((double)nv) * std::sqrt(s);
+}
+
+// The solve: u_free (CondensedAssembler::ufree, condensed_assembler.cpp:348-356), rhs (:367-462),
+// the warm start with the normal sign inverted (warmstart.hpp:26-39), the initial u_corr, the
+// coloring, then colored sweeps until the residual is below 1 (or diverges). x receives
+// u = u_free - u_corr; lam_mem the impulses as stored for the next step (normal sign inverted back).
+CondResult condensed_colored(const Engine& E, const std::vector<Contact>& C, double dt, std::vector<double>& x,
+                             std::vector<double>& lam_mem) {
+    const int N = E.N, nv = 6 * N;
+    const bool implicit_gyro = E.cfg.moreau_implicit_gyroscopy != 0;
+    std::vector<double> uf(nv);
+    for (int i = 0; i < N; ++i) {
+        const double* w = &E.w[3 * (size_t)i];
+        const double Iw[3] = {E.inertia[i] * w[0], E.inertia[i] * w[1], E.inertia[i] * w[2]};
+        double cgy[3];
+        cross3(w, Iw, cgy);
+        for (int k = 0; k < 6; ++k) {
+            const size_t j = 6 * (size_t)i + k;
+            const double vn = k < 3 ? E.v[3 * (size_t)i + k] : w[k - 3];
+            const double fext = k < 3 ? E.mass[i] * E.cfg.sim_gravity[k] : 0.0;
+            double u = vn + E.minv[j] * (dt * fext);
+            if (!implicit_gyro) u = u + E.minv[j] * (dt * (k < 3 ? 0.0 : -cgy[k - 3]));
+            uf[j] = u;
+        }
+    }
+    CondResult res;
+    if (C.empty()) {  // no constraint rows: the free velocity (condensed_solver.cpp:453)
+        x = uf;
+        lam_mem.clear();
+        return res;
+    }
+    std::vector<CondBlock> B(C.size());
+    for (size_t ci = 0; ci < C.size(); ++ci) {
+        const Contact& c = C[ci];
+        CondBlock& k = B[ci];
+        k.ci = (int)ci;
+        k.dim = c.frictional ? 3 : 1;
+        k.a = c.ba;
+        k.b = c.bb;
+        k.mu = c.mu;
+        const double* dirs[3] = {c.n, c.t1, c.t2};
+        for (int q = 0; q < k.dim; ++q)
+            for (int j = 0; j < 3; ++j) {
+                k.Ja[6 * q + j] = -dirs[q][j];
+                k.Ja[6 * q + 3 + j] = -c.cA[3 * q + j];
+                k.Jb[6 * q + j] = dirs[q][j];
+                k.Jb[6 * q + 3 + j] = c.cB[3 * q + j];
+            }
+        for (int q = 0; q < k.dim; ++q) {
+            // G_ii = Ja diag(M^-1) Ja^T + Jb diag(M^-1) Jb^T, its diagonal (condensed_assembler.cpp:244-256)
+            double ga = 0.0;
+            if (k.a >= 0) {
+                ga = (k.Ja[6 * q] * E.minv[6 * (size_t)k.a]) * k.Ja[6 * q];
+                for (int j = 1; j < 6; ++j) ga = ga + (k.Ja[6 * q + j] * E.minv[6 * (size_t)k.a + j]) * k.Ja[6 * q + j];
+            }
+            double gb = (k.Jb[6 * q] * E.minv[6 * (size_t)k.b]) * k.Jb[6 * q];
+            for (int j = 1; j < 6; ++j) gb = gb + (k.Jb[6 * q + j] * E.minv[6 * (size_t)k.b + j]) * k.Jb[6 * q + j];
+            const double G = (0.0 + ga) + gb;
+            k.ginv[q] = G > 0 ? 1.0 / G : 0.0;
+            double ut = 0.0;
+            if (k.a >= 0) ut = ut + cond_row(&k.Ja[6 * q], &uf[6 * (size_t)k.a]);
+            ut = ut + cond_row(&k.Jb[6 * q], &uf[6 * (size_t)k.b]);
+            k.rhs[q] = ut + c.cb[q];
+        }
+    }
+    // impulses (normal <= 0 inside) and the initial u_corr = sum_blocks M^-1 J^T lambda
+    std::vector<double> lam(3 * C.size(), 0.0), u(nv, 0.0);
+    for (size_t ci = 0; ci < C.size(); ++ci) {
+        const CondBlock& k = B[ci];
+        double* l = &lam[3 * ci];
+        if (E.cfg.pj_warmstart) {
+            l[0] = -C[ci].lam0[0];
+            if (k.dim == 3) {
+                l[1] = C[ci].lam0[1];
+                l[2] = C[ci].lam0[2];
+            }
+        }
+        if (k.a >= 0) cond_scatter(k.Ja, k.dim, l, &E.minv[6 * (size_t)k.a], &u[6 * (size_t)k.a]);
+        cond_scatter(k.Jb, k.dim, l, &E.minv[6 * (size_t)k.b], &u[6 * (size_t)k.b]);
+    }
+    int ncol = 0;
+    const std::vector<int> color = color_blocks(B, N, &ncol);
+    std::vector<std::vector<int>> classes(ncol);
+    for (size_t i = 0; i < B.size(); ++i) classes[color[i]].push_back((int)i);
+    const double relax = E.cfg.pj_relaxation, alpha = E.cfg.pj_alpha;
+    std::vector<double> uprev = u;
+    for (int it = 0; it < E.cfg.pj_max_iterations; ++it) {
+        for (const auto& cls : classes)
+            for (int bi : cls) cond_block_update(B[bi], relax, alpha, E.minv.data(), &lam[3 * (size_t)bi], u.data());
+        res.iters = it + 1;
+        res.err = cond_residual(uf, uprev, u, E.cfg.pj_tol_rel, E.cfg.pj_tol_abs);
+        if (!std::isfinite(res.err)) {
+            res.diverged = true;  // checkResidual throws "Condensed solver diverged" (:507-513)
+            break;
+        }
+        if (res.err < 1.0) break;
+        uprev = u;
+    }
+    x.assign(nv, 0.0);
+    for (int j = 0; j < nv; ++j) x[j] = uf[j] - u[j];
+    lam_mem.assign(3 * C.size(), 0.0);
+    for (size_t ci = 0; ci < C.size(); ++ci) {
+        lam_mem[3 * ci] = -lam[3 * ci];
+        if (B[ci].dim == 3) {
+            lam_mem[3 * ci + 1] = lam[3 * ci + 1];
+            lam_mem[3 * ci + 2] = lam[3 * ci + 2];
+        }
+    }
+    return res;
+}
+
 // MoreauIntegrator::step (src/physics/integration/moreau.cpp:6-13)
 void step_once(Engine& E) {
     const int N = E.N, S = E.S, nv = 6 * N;
@@ -1135,7 +1372,28 @@ void step_once(Engine& E) {
     }
     E.trace.clear();
     SolveResult sr;
-    if (C.empty()) {
+    std::vector<double> cond_mem;
+    if (E.cfg.solver_type == 1) {
+        // solver.type=condensed (colored sweeps); its stats residual is the complementarity
+        // residual of the result with the impulses in the projected Jacobi convention
+        CondResult cr = condensed_colored(E, C, dt, x, cond_mem);
+        sr.iters = cr.iters;
+        sr.res_last = cr.err;
+        if (cr.diverged) E.status = 4;
+        for (size_t ci = 0; ci < C.size(); ++ci) {
+            const int r0 = W.row_base[ci];
+            lam[r0] = cond_mem[3 * ci];
+            if (C[ci].frictional) {
+                lam[r0 + 1] = -cond_mem[3 * ci + 1];
+                lam[r0 + 2] = -cond_mem[3 * ci + 2];
+            }
+        }
+        if (!C.empty()) {
+            std::vector<double> dl(W.nrows), ac(nv);
+            SweepOut fin = pj_sweep(P, x.data(), lam.data(), dl.data(), ac.data(), E.Mdiag.data(), omp_all, false);
+            sr.res_final = rel_residual(fin);
+        }
+    } else if (C.empty()) {
 #pragma omp parallel for schedule(static) if (omp_all)
         for (int j = 0; j < nv; ++j) x[j] = rhs[j] / E.Mdiag[j];
     } else {
@@ -1153,7 +1411,7 @@ void step_once(Engine& E) {
         for (int k = 0; k < 3; ++k) E.prev_point[3 * ci + k] = C[ci].point[k];
         const int r0 = W.row_base[ci];
         const int nr = C[ci].frictional ? 3 : 1;
-        for (int k = 0; k < nr; ++k) E.prev_lambda[3 * ci + k] = lam[r0 + k];
+        for (int k = 0; k < nr; ++k) E.prev_lambda[3 * ci + k] = E.cfg.solver_type == 1 ? cond_mem[3 * ci + k] : lam[r0 + k];
     }
     E.last = C;
     E.last_lambda = E.prev_lambda;
@@ -1234,8 +1492,9 @@ void or_destroy(void* h) { delete (Engine*)h; }
 
 int or_step(void* h, int32_t nsteps) {
     Engine* E = (Engine*)h;
-    for (int s = 0; s < nsteps; ++s) step_once(*E);
-    return 0;
+    E->status = 0;
+    for (int s = 0; s < nsteps && !E->status; ++s) step_once(*E);
+    return E->status;
 }
 
 void or_get_state(void* h, double* pos, double* quat, double* vel, double* omega) {

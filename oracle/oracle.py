@@ -74,6 +74,11 @@ class OrConfig(C.Structure):
         ("pj_anderson_m", C.c_int32),
         ("pj_rdiag_true_delassus", C.c_int32),
         ("moreau_implicit_gyroscopy", C.c_int32),
+        ("solver_type", C.c_int32),
+        ("condensed_sweep_mode", C.c_int32),
+        ("pj_relaxation", C.c_double),
+        ("pad0", C.c_int32),
+        ("status", C.c_int32),
     ]
 
 
@@ -115,6 +120,7 @@ def lib():
             L.or_create.restype = C.c_void_p
             L.or_create.argtypes = [C.POINTER(OrConfig), C.POINTER(OrScene)]
             L.or_destroy.argtypes = [C.c_void_p]
+            L.or_step.restype = C.c_int
             L.or_step.argtypes = [C.c_void_p, C.c_int32]
             L.or_get_state.argtypes = [C.c_void_p, _P, _P, _P, _P]
             L.or_get_stats.argtypes = [C.c_void_p, C.POINTER(OrStats)]
@@ -182,6 +188,10 @@ def config_from(cfg: dict, omp_mode: int = 0, num_threads: int = 0) -> OrConfig:
     c.pj_anderson_m = int(cfg.get("pj.anderson_m", 2))
     c.pj_rdiag_true_delassus = int(bool(cfg.get("pj.rdiag_true_delassus", False)))
     c.moreau_implicit_gyroscopy = int(bool(cfg.get("moreau.implicit_gyroscopy", False)))
+    c.solver_type = {"projected_jacobi": 0, "condensed": 1}[str(cfg.get("solver.type", "projected_jacobi"))]
+    c.condensed_sweep_mode = {"gauss_seidel": 0, "jacobi": 1, "colored": 2, "chaotic": 3}[
+        str(cfg.get("condensed.sweep_mode", "gauss_seidel"))]
+    c.pj_relaxation = float(cfg.get("pj.relaxation", 1.0))
     c.omp_mode = omp_mode
     c.num_threads = num_threads
     return c
@@ -217,7 +227,9 @@ class Oracle:
             self.h = None
 
     def step(self, n: int = 1):
-        self.L.or_step(self.h, int(n))
+        st = self.L.or_step(self.h, int(n))
+        if st:
+            raise RuntimeError(f"oracle step failed with status {st} (a solve diverged)")
 
     def state(self):
         N = self.N

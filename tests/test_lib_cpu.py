@@ -87,9 +87,22 @@ def test_config_file_parsing(cdxlib, tmp_path):
 
 
 def test_config_rejects_other_solvers(cdxlib):
-    from cardillocxx_gb300 import CdxError, Config
+    from cardillocxx_gb300 import CdxError, Config, PhysicsEngine
     with pytest.raises(CdxError):
         Config().set("solver.type", "pgs")
+    c = Config({"solver.type": "condensed"})
+    assert c.get("solver_type") == 1 and c.get("condensed_sweep_mode") == 0  # gauss_seidel by default
+    assert Config({"condensed.sweep_mode": "colored"}).get("condensed_sweep_mode") == 2
+    assert Config({"condensed.sweep_mode": "nonsense"}).get("condensed_sweep_mode") == 0
+    # the GPU runs the condensed solver's colored sweeps in the plain FP64 method: other sweep modes,
+    # the split form and its accelerated loops are refused before any device call
+    for bad in ({"solver.type": "condensed"},
+                {"solver.type": "condensed", "condensed.sweep_mode": "jacobi"},
+                {"solver.type": "condensed", "condensed.sweep_mode": "colored", "gpu.precision": "split"},
+                {"solver.type": "condensed", "condensed.sweep_mode": "colored", "pj.nesterov": True}):
+        with pytest.raises(CdxError) as e:
+            PhysicsEngine(bad)
+        assert e.value.status == 6
 
 
 def test_generator_deterministic_and_non_overlapping(cdxlib):
