@@ -311,6 +311,7 @@ def at_residual_leg(a, scene, cfg, flush):
     """ms/step at complementarity residual <= 1e-6: the input stepped --warm-steps times by the split
     form (the warm start of a settled pile), then that state and contact memory loaded into each
     form, each solving every step until the residual is at most 1e-6 (cap --residual-cap sweeps)."""
+    import numpy as np
     from cardillocxx_gb300 import PhysicsEngine
     tol = 1e-6
     t0 = time.time()
@@ -346,6 +347,23 @@ def at_residual_leg(a, scene, cfg, flush):
                      "contact_iters_per_s": sum(c * i for c, i in zip(con, it)) / tot_s}
         log(f"at residual 1e-6, {name}: {out[name]['ms_per_step']:.2f} ms/step, {out[name]['sweeps_per_step']:.0f} "
             f"sweeps, residual <= {out[name]['residual_max']:.2e}")
+    # the condensed solver's colored Gauss-Seidel sweeps (plain FP64, solver.type=condensed) on the
+    # same state, with its own stop rule (the velocity-increment residual, here at tolerances 1e-6)
+    # and alpha = relaxation = 1; the memory's tangential impulses enter in its own sign convention
+    cmem = dict(mem)
+    cmem["lambda"] = mem["lambda"] * np.array([1.0, -1.0, -1.0])
+    ccfg = dict(cfg, **{"gpu.precision": "fp64", "solver.type": "condensed", "condensed.sweep_mode": "colored",
+                        "pj.alpha": 1.0, "pj.relaxation": 1.0, "pj.tol_abs": 1e-6, "pj.tol_rel": 1e-6,
+                        "pj.max_iterations": a.residual_cap, "gpu.check_every": 10})
+    e = PhysicsEngine(ccfg).load_scene(s2).set_contacts(cmem)
+    ms, it, con, res, _ = time_engine(e, min(a.residual_steps, 5), min(a.residual_warmup, 5), flush)
+    e.close()
+    out["condensed_colored_fp64"] = {"ms_per_step": sum(ms) / len(ms), "sweeps_per_step": sum(it) / len(it),
+                                     "residual_max": max(res), "steps": len(ms),
+                                     "stop": "velocity-increment residual <= 1 at pj.tol_abs = pj.tol_rel = 1e-6",
+                                     "alpha": 1.0, "relaxation": 1.0}
+    log(f"condensed colored (fp64): {out['condensed_colored_fp64']['ms_per_step']:.2f} ms/step, "
+        f"{out['condensed_colored_fp64']['sweeps_per_step']:.0f} sweeps, residual <= {max(res):.2e}")
     if out["split"]["residual_max"] <= tol and out["fp64"]["residual_max"] <= tol:
         out["speedup_at_equal_residual"] = out["fp64"]["ms_per_step"] / out["split"]["ms_per_step"]
     else:
