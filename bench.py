@@ -79,6 +79,8 @@ def parse():
     p.add_argument("--residual-warmup", type=int, default=20, help="at_residual leg: untimed steps per GPU form")
     p.add_argument("--residual-cap", type=int, default=20000, help="at_residual leg: sweep cap a step")
     p.add_argument("--no-residual-leg", action="store_true")
+    p.add_argument("--residual-forms", default="split,fp64,split_nesterov,condensed",
+                   help="at_residual leg: the forms to run (comma-separated)")
     p.add_argument("--no-workloads", action="store_true", help="skip the batched, drum and rollout workloads")
     p.add_argument("--adjoint", action="store_true",
                    help="time only the differentiable rollout (forward with checkpoints, then the adjoint) of "
@@ -334,6 +336,8 @@ def at_residual_leg(a, scene, cfg, flush):
              "split_nesterov": {"gpu.precision": "split", "gpu.check_every": 1, "gpu.residual_tol": split_tol,
                                 "pj.nesterov": True, "pj.tol_abs": 1e-100, "pj.tol_rel": 0.0}}
     out["split_stop_tol"] = split_tol
+    chosen = set(a.residual_forms.split(","))
+    forms = {k: v for k, v in forms.items() if k in chosen}
     for name, over in forms.items():
         e = PhysicsEngine(dict(cfg, **dict(rule, **over))).load_scene(s2).set_contacts(mem)
         n = a.residual_steps
@@ -350,26 +354,30 @@ def at_residual_leg(a, scene, cfg, flush):
     # the condensed solver's colored Gauss-Seidel sweeps (plain FP64, solver.type=condensed) on the
     # same state, with its own stop rule (the velocity-increment residual, here at tolerances 1e-6)
     # and alpha = relaxation = 1; the memory's tangential impulses enter in its own sign convention
-    cmem = dict(mem)
-    cmem["lambda"] = mem["lambda"] * np.array([1.0, -1.0, -1.0])
-    ccfg = dict(cfg, **{"gpu.precision": "fp64", "solver.type": "condensed", "condensed.sweep_mode": "colored",
-                        "pj.alpha": 1.0, "pj.relaxation": 1.0, "pj.tol_abs": 1e-6, "pj.tol_rel": 1e-6,
-                        "pj.max_iterations": a.residual_cap, "gpu.check_every": 10})
-    e = PhysicsEngine(ccfg).load_scene(s2).set_contacts(cmem)
-    ms, it, con, res, _ = time_engine(e, min(a.residual_steps, 5), min(a.residual_warmup, 5), flush)
-    e.close()
-    out["condensed_colored_fp64"] = {"ms_per_step": sum(ms) / len(ms), "sweeps_per_step": sum(it) / len(it),
-                                     "residual_max": max(res), "steps": len(ms),
-                                     "stop": "velocity-increment residual <= 1 at pj.tol_abs = pj.tol_rel = 1e-6",
-                                     "alpha": 1.0, "relaxation": 1.0}
-    log(f"condensed colored (fp64): {out['condensed_colored_fp64']['ms_per_step']:.2f} ms/step, "
-        f"{out['condensed_colored_fp64']['sweeps_per_step']:.0f} sweeps, residual <= {max(res):.2e}")
-    if out["split"]["residual_max"] <= tol and out["fp64"]["residual_max"] <= tol:
+    if "condensed" in chosen:
+        cmem = dict(mem)
+        cmem["lambda"] = mem["lambda"] * np.array([1.0, -1.0, -1.0])
+        ccfg = dict(cfg, **{"gpu.precision": "fp64", "solver.type": "condensed", "condensed.sweep_mode": "colored",
+                            "pj.alpha": 1.0, "pj.relaxation": 1.0, "pj.tol_abs": 1e-6, "pj.tol_rel": 1e-6,
+                            "pj.max_iterations": a.residual_cap, "gpu.check_every": 10})
+        e = PhysicsEngine(ccfg).load_scene(s2).set_contacts(cmem)
+        ms, it, con, res, _ = time_engine(e, min(a.residual_steps, 5), min(a.residual_warmup, 5), flush)
+        e.close()
+        out["condensed_colored_fp64"] = {"ms_per_step": sum(ms) / len(ms), "sweeps_per_step": sum(it) / len(it),
+                                         "residual_max": max(res), "steps": len(ms),
+                                         "stop": "velocity-increment residual <= 1 at pj.tol_abs = pj.tol_rel = 1e-6",
+                                         "alpha": 1.0, "relaxation": 1.0}
+        log(f"condensed colored (fp64): {out['condensed_colored_fp64']['ms_per_step']:.2f} ms/step, "
+            f"{out['condensed_colored_fp64']['sweeps_per_step']:.0f} sweeps, residual <= {max(res):.2e}")
+    if "split" not in out or "fp64" not in out:
+        out["speedup_at_equal_residual"] = None
+    elif out["split"]["residual_max"] <= tol and out["fp64"]["residual_max"] <= tol:
         out["speedup_at_equal_residual"] = out["fp64"]["ms_per_step"] / out["split"]["ms_per_step"]
     else:
         out["speedup_at_equal_residual"] = None
         out["note"] = "a form reached the sweep cap above the residual tolerance; its residual is stated"
-    out["contact_iters_ratio"] = out["split"]["contact_iters_per_s"] / out["fp64"]["contact_iters_per_s"]
+    if "split" in out and "fp64" in out:
+        out["contact_iters_ratio"] = out["split"]["contact_iters_per_s"] / out["fp64"]["contact_iters_per_s"]
     return out, s2, mem
 
 
@@ -617,12 +625,12 @@ def run_cdx(a):
     if a.scene == "pile_200k" and not a.no_residual_leg and rank == 0:
         at_res, s2, mem2 = at_residual_leg(a, scene, cfg, flush)
         s2m = (s2, mem2)
-        if a.precision == "split":
+        if a.precision == "split" and {"split", "fp64"} <= set(a.residual_forms.split(",")):
             serr = split_error(s2, mem2, cfg)
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu:
         cpu = cpu_baseline(scene, cfg, a.cpu_seconds, steps=a.cpu_steps)
-        if s2m is not None:
+        if s2m is not None and "split" in at_res:
             cpu_res = cpu_at_residual(s2m[0], s2m[1], cfg, a)
             at_res["cpu"] = cpu_res
             # one CPU step against the GPU forms' averages: compare the rates of contact-iterations
