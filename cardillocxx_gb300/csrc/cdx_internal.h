@@ -183,6 +183,21 @@ struct CondBufs {
     int32_t* cend = nullptr;
 };
 
+// projected Gauss-Seidel (k_fp64_pgs.cu): the order of the blocks and the per-body chains that
+// make a sweep sequential
+struct PgsBufs {
+    int64_t cap = 0;
+    int32_t* pred = nullptr;      // 2*cap: previous block of body A / body B in row order (-1: none)
+    int32_t* done = nullptr;      // cap: the last sweep a block finished (-1 before the first)
+    uint32_t* by_rank = nullptr;  // cap: contact of each rank in row order
+    unsigned* bar = nullptr;      // grid barrier counter
+    int32_t* err = nullptr;       // a wait ran out (1 barrier, 2 predecessor)
+    int32_t* stop = nullptr;      // the stop decision of the last sweep
+    int32_t* lev = nullptr;       // cap: level of each block (longest chain of predecessors)
+    int32_t* rflag = nullptr;     // 3: change flags of the level rounds
+    int32_t* maxlev = nullptr;    // the largest level
+};
+
 struct Incidence {
     int64_t cap = 0;
     uint32_t* key_in = nullptr;
@@ -228,6 +243,19 @@ void launch_cond_copy(int n, const double* src, double* dst, const DevScalars* d
 // the projected Jacobi convention (for the complementarity residual)
 void launch_cond_final(const Scene& sc, Contacts& C, int gen, int nc, const CondBufs& B, double* x, int pj_convention,
                        cudaStream_t s);
+// projected Gauss-Seidel (k_fp64_pgs.cu): rhs, Dinv, the warm start and u_corr (B.uf from
+// launch_cond_setup's free velocity), the per-body chains; then the whole solve in one cooperative
+// launch (returns the launch's cudaError_t)
+void launch_pgs_setup(const Scene& sc, Contacts& C, int gen, int nc, int warmstart, CondBufs& B, const Incidence& inc,
+                      PgsBufs& P, cudaStream_t s);
+// levels of the blocks and the sort keys (level) and values (contact) in row order
+int launch_pgs_levels(const PgsBufs& P, int nc, uint32_t* keys, uint32_t* vals, unsigned long long wait_ns,
+                      cudaStream_t s);
+// order: the contacts sorted by level
+int launch_pgs_solve(const Scene& sc, const Contacts& C, int nc, const CondBufs& B, const PgsBufs& P,
+                     const uint32_t* order, double relax, double alpha, double tol_rel, double tol_abs, int max_iter,
+                     DevScalars* ds, unsigned long long wait_ns, cudaStream_t s);
+void launch_cond_ufree(const Scene& sc, double dt, const double* g, int implicit_gyro, CondBufs& B, cudaStream_t s);
 // nonfinite (optional): set to 1 when a body's state after the drift is not finite
 void launch_drift64(const Scene& sc, double h, int compute_R, cudaStream_t s, int32_t* nonfinite = nullptr);
 void launch_static_flags64(const Scene& sc, double margin, int32_t* flags, cudaStream_t s);

@@ -133,6 +133,7 @@ int cdx_config_set(cdx_config* c, const char* key_c, const char* val_c) {
         const std::string v = lower(val);
         if (v == "projected_jacobi" || v == "projectedjacobi" || v == "pj" || v == "gpu_pj") c->solver_type = 0;
         else if (v == "condensed" || v == "condensed_solver") c->solver_type = 1;
+        else if (v == "projected_gauss_seidel" || v == "projectedgaussseidel" || v == "pgs") c->solver_type = 2;
         else return CDX_ERR_UNSUPPORTED;  // other solvers are not on this path
     } else if (key == "condensed.sweep_mode") {
         const std::string v = lower(val);

@@ -97,10 +97,13 @@ int Engine::init(const cdx_config& c) {
 //    its cooperative solve; Chebyshev and Anderson (selected when Nesterov is off, as in
 //    projected_jacobi.cpp:470-491) run in the plain FP64 method only;
 //  - solver.type=condensed runs in the plain FP64 method with condensed.sweep_mode=colored (its
-//    other sweep modes, and its Nesterov and Chebyshev loops, are not built).
+//    other sweep modes, and its Nesterov and Chebyshev loops, are not built);
+//  - solver.type=projected_gauss_seidel runs its plain loop in the plain FP64 method (its Nesterov
+//    loop is not built).
 int Engine::check_solver_config(const cdx_config& c) {
-    if (c.solver_type != 0 && c.solver_type != 1)
-        return fail(CDX_ERR_UNSUPPORTED, "only solver.type=projected_jacobi and condensed are on this path");
+    if (c.solver_type < 0 || c.solver_type > 2)
+        return fail(CDX_ERR_UNSUPPORTED,
+                    "only solver.type=projected_jacobi, projected_gauss_seidel and condensed are on this path");
     if (c.gpu_precision == CDX_PRECISION_SPLIT && !c.pj_nesterov && (c.pj_chebyshev || c.pj_anderson))
         return fail(CDX_ERR_UNSUPPORTED, "pj.chebyshev and pj.anderson run in the plain FP64 method only "
                                          "(gpu.precision=fp64); the split form runs pj.nesterov and the standard loop");
@@ -111,6 +114,13 @@ int Engine::check_solver_config(const cdx_config& c) {
             return fail(CDX_ERR_UNSUPPORTED, "solver.type=condensed runs with condensed.sweep_mode=colored on the GPU");
         if (c.pj_nesterov || c.pj_chebyshev)
             return fail(CDX_ERR_UNSUPPORTED, "solver.type=condensed runs its standard loop (no pj.nesterov or pj.chebyshev)");
+    }
+    if (c.solver_type == 2) {
+        if (c.gpu_precision != CDX_PRECISION_FP64)
+            return fail(CDX_ERR_UNSUPPORTED,
+                        "solver.type=projected_gauss_seidel runs in the plain FP64 method (gpu.precision=fp64)");
+        if (c.pj_nesterov)
+            return fail(CDX_ERR_UNSUPPORTED, "solver.type=projected_gauss_seidel runs its plain loop (no pj.nesterov)");
     }
     return CDX_OK;
 }
@@ -760,7 +770,7 @@ int Engine::step64() {
     if (timing) cudaEventRecord(ev[1], stream);
     if ((st = setup64())) return st;
     if (timing) cudaEventRecord(ev[2], stream);
-    if ((st = (cfg.solver_type == 1 ? solve_condensed() : solve64()))) return st;
+    if ((st = (cfg.solver_type == 1 ? solve_condensed() : cfg.solver_type == 2 ? solve_pgs() : solve64()))) return st;
     if (timing) cudaEventRecord(ev[3], stream);
     launch_writeback64(sc, x, stream);
     launch_drift64(sc, th * dt, 0, stream, &ds->nonfinite);
@@ -789,8 +799,9 @@ int Engine::step64() {
     // the step itself completed and the context stays usable (cdx_set_state can repair the state)
     if (hs->nonfinite) return fail(CDX_ERR_NONFINITE, "the state after the step is not finite (NaN or infinity)");
     if (cond_diverged)
-        return fail(CDX_ERR_NONFINITE, "condensed solver diverged: the velocity-increment residual is not finite "
-                                       "(pj.tol_abs and pj.tol_rel must not both be 0)");
+        return fail(CDX_ERR_NONFINITE, std::string(cfg.solver_type == 2 ? "projected Gauss-Seidel" : "condensed solver") +
+                                           " diverged: the velocity-increment residual is not finite "
+                                           "(pj.tol_abs and pj.tol_rel must not both be 0)");
     return CDX_OK;
 }
 

@@ -123,6 +123,11 @@ struct Engine {
     int cond_diverged = 0;
     int ensure_cond();
     int solve_condensed();
+    // projected Gauss-Seidel (plain FP64 method; engine_pgs.cpp)
+    cdx::PgsBufs pgs;
+    int last_levels = 0;  // levels of the last projected Gauss-Seidel step (its longest chain of blocks)
+    int ensure_pgs();
+    int solve_pgs();
     void split_config_changed();
     int load_scene(const cdx_scene& s);
     int ensure_tmp(int64_t n);

@@ -54,7 +54,8 @@ __device__ __forceinline__ double minv_of(const Scene& sc, int i, int k) {
     return k < 3 ? sc.bf(BF_MINVL)[i] : sc.bf(BF_MINVA)[i];
 }
 
-// u_free = v_n + M^-1 (dt f_ext) [+ M^-1 (dt f_gyro)] (CondensedAssembler::ufree, condensed_assembler.cpp:348-356)
+// u_free = v_n + M^-1 (dt f_ext) [+ M^-1 (dt f_gyro)] (CondensedAssembler::ufree, condensed_assembler.cpp:348-356;
+// PgsAssembler::ufree, pgs_assembler.cpp:96-103, is the same)
 __global__ void k_cond_ufree(Scene sc, double dt, double g0, double g1, double g2, int implicit_gyro, double* uf) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= sc.N) return;
@@ -321,6 +322,9 @@ void launch_cond_setup(const Scene& sc, Contacts& C, int gen, int nc, double dt,
     if (sc.N > 0) k_cond_ufree<<<nblk(sc.N), NT, 0, s>>>(sc, dt, g[0], g[1], g[2], implicit_gyro, B.uf);
     if (nc > 0) k_cond_setup<<<nblk(nc), NT, 0, s>>>(sc, C, gen, nc, B.uf, warmstart, B, inc);
     if (sc.N > 0) k_cond_ucorr_init<<<nblk(sc.N), NT, 0, s>>>(sc, C, B, inc, B.u);
+}
+void launch_cond_ufree(const Scene& sc, double dt, const double* g, int implicit_gyro, CondBufs& B, cudaStream_t s) {
+    if (sc.N > 0) k_cond_ufree<<<nblk(sc.N), NT, 0, s>>>(sc, dt, g[0], g[1], g[2], implicit_gyro, B.uf);
 }
 void launch_cond_color_round(const Contacts& C, int nc, const CondBufs& B, const Incidence& inc,
                              const int32_t* col_in, int32_t* col_out, int32_t* uncolored, int32_t* too_many,

@@ -61,7 +61,8 @@ typedef struct cdx_config {
     double pj_alpha;                  /* pj.alpha */
     double pj_relaxation;             /* pj.relaxation (accepted, unused by PJ as in the reference) */
     int32_t solver_type;              /* solver.type: 0 projected_jacobi, 1 condensed (plain FP64 method,
-                                         condensed.sweep_mode=colored) */
+                                         condensed.sweep_mode=colored), 2 projected_gauss_seidel (plain
+                                         FP64 method, plain loop) */
     double collision_security_margin; /* collision.security_margin */
     double collision_match_max_dist;  /* collision.match_max_dist */
     int32_t collision_broadphase;     /* collision.broadphase: 0 uniform_grid (any reference value maps here) */

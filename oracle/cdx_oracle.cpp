@@ -1294,6 +1294,146 @@ CondResult condensed_colored(const Engine& E, const std::vector<Contact>& C, dou
     return res;
 }
 
+// ---- projected Gauss-Seidel, src/physics/solver/projected_gauss_seidel.cpp ----
+// ProjectedGaussSeidelSolver::solve (projected_gauss_seidel.cpp:56-264) with the plain loop, for
+// contact rows only (no springs or dampers). The blocks are the contacts in W's row order
+// (frictionless contacts first, then frictional ones, each in contact order); a sweep visits them
+// in that order (pgs_sweep, :158-182). Inside, the normal impulse is <= 0 (project, :11-27) and the
+// velocity is u = u_free - u_corr with u_corr = M^-1 W^T lambda.
+//   u_free = v + M^-1 (h f_ext) [+ M^-1 (h f_gyro)]        PgsAssembler::ufree (pgs_assembler.cpp:96-103)
+//   rhs    = W u_free + b (+ e . (W v + b) with restitution)  PgsAssembler::rhs (:71-80)
+//   Dinv   = 1 / sum_nz w^2 M^-1_col per row                   PgsAssembler::DinvDiag (:219-294)
+// Sums run in W's column order, from zero, as Eigen's row-major sparse kernels do; u_corr gets its
+// terms column by column (W row order), as Eigen's column-major M^-1 W^T kernels do.
+CondResult pgs_solve(const Engine& E, const std::vector<Contact>& C, const Rows& W, double dt, std::vector<double>& x,
+                     std::vector<double>& lam_mem) {
+    const int N = E.N, nv = 6 * N, nr = W.nrows;
+    const bool implicit_gyro = E.cfg.moreau_implicit_gyroscopy != 0;
+    std::vector<double> uf(nv), vn(nv);
+    for (int i = 0; i < N; ++i) {
+        const double* w = &E.w[3 * (size_t)i];
+        const double Iw[3] = {E.inertia[i] * w[0], E.inertia[i] * w[1], E.inertia[i] * w[2]};
+        double cgy[3];
+        cross3(w, Iw, cgy);
+        for (int k = 0; k < 6; ++k) {
+            const size_t j = 6 * (size_t)i + k;
+            const double v = k < 3 ? E.v[3 * (size_t)i + k] : w[k - 3];
+            const double fext = k < 3 ? E.mass[i] * E.cfg.sim_gravity[k] : 0.0;
+            double u = v + E.minv[j] * (dt * fext);
+            if (!implicit_gyro) u = u + E.minv[j] * (dt * (k < 3 ? 0.0 : -cgy[k - 3]));
+            uf[j] = u;
+            vn[j] = v;
+        }
+    }
+    CondResult res;
+    if (nr == 0) {  // numLambda == 0: the free velocity (projected_gauss_seidel.cpp:79)
+        x = uf;
+        lam_mem.clear();
+        return res;
+    }
+    auto row_dot = [&](int r, const double* u) {
+        double t = 0.0;
+        for (int k = W.ptr[r]; k < W.ptr[r + 1]; ++k) t = t + W.val[k] * u[W.col[k]];
+        return t;
+    };
+    bool restitution = false;
+    for (int r = 0; r < nr; ++r) restitution = restitution || W.e[r] != 0.0;
+    std::vector<double> rhs(nr), dinv(nr);
+    for (int r = 0; r < nr; ++r) {
+        double b = W.cb[r];
+        if (restitution) b = b + W.e[r] * (row_dot(r, vn.data()) + W.cb[r]);
+        rhs[r] = row_dot(r, uf.data()) + b;
+        double d = 0.0;
+        for (int k = W.ptr[r]; k < W.ptr[r + 1]; ++k) d = d + (W.val[k] * W.val[k]) * E.minv[W.col[k]];
+        // frictionless rows guard a zero diagonal (:284-287); frictional ones take cwiseInverse (:289-292)
+        dinv[r] = r < W.nfl ? (d > 0 ? 1.0 / d : 0.0) : 1.0 / d;
+    }
+    // warm start with the normal sign inverted (:103-109), then u_corr = M^-1 W^T lambda (:117)
+    std::vector<double> lam(nr, 0.0), u(nv, 0.0);
+    if (E.cfg.pj_warmstart)
+        for (size_t ci = 0; ci < C.size(); ++ci) {
+            const int r0 = W.row_base[ci];
+            lam[r0] = -C[ci].lam0[0];
+            if (C[ci].frictional) {
+                lam[r0 + 1] = C[ci].lam0[1];
+                lam[r0 + 2] = C[ci].lam0[2];
+            }
+        }
+    auto scatter_row = [&](int r, double d) {
+        for (int k = W.ptr[r]; k < W.ptr[r + 1]; ++k) {
+            const int j = W.col[k];
+            u[j] = u[j] + (E.minv[j] * W.val[k]) * d;
+        }
+    };
+    for (int r = 0; r < nr; ++r) scatter_row(r, lam[r]);
+    const double relax = E.cfg.pj_relaxation, alpha = E.cfg.pj_alpha;
+    // blocks: one row per frictionless contact, then three per frictional contact
+    auto block_update = [&](int r0, int dim) {
+        double rs[3], dl[3];
+        for (int q = 0; q < dim; ++q) {
+            double o = rhs[r0 + q];
+            o = o - row_dot(r0 + q, u.data());
+            o = o - 0.0 * lam[r0 + q];  // C is zero on contact rows
+            rs[q] = o;
+        }
+        for (int q = 0; q < dim; ++q) {
+            // the block of Dinv is diagonal, stored dense (BlockDiagonal::addBlockDiag)
+            double g = (q == 0 ? dinv[r0] : 0.0) * rs[0];
+            for (int j = 1; j < dim; ++j) g = g + (q == j ? dinv[r0 + j] : 0.0) * rs[j];
+            dl[q] = (g * relax) * alpha;
+            lam[r0 + q] = lam[r0 + q] + dl[q];
+        }
+        // project (:11-27): the corrections enter dlambda
+        const double n0 = lam[r0];
+        lam[r0] = std::min(n0, 0.0);
+        dl[0] = dl[0] + (lam[r0] - n0);
+        if (dim == 3) {
+            const double t1 = lam[r0 + 1], t2 = lam[r0 + 2];
+            const double tn = std::sqrt(t1 * t1 + t2 * t2);
+            if (tn > 0.0) {
+                const double s = std::min(1.0, -(W.mu[r0] * lam[r0]) / tn);
+                const double p1 = s * t1, p2 = s * t2;
+                dl[1] = dl[1] + (p1 - t1);
+                dl[2] = dl[2] + (p2 - t2);
+                lam[r0 + 1] = p1;
+                lam[r0 + 2] = p2;
+            }
+        }
+        for (int q = 0; q < dim; ++q) scatter_row(r0 + q, dl[q]);
+    };
+    std::vector<double> uprev = u;
+    for (int it = 0; it < E.cfg.pj_max_iterations; ++it) {
+        for (int r = 0; r < nr;) {
+            const int dim = r < W.nfl ? 1 : 3;
+            block_update(r, dim);
+            r += dim;
+        }
+        res.iters = it + 1;
+        // check_residual (:142-151): the velocity-increment residual of u_corr, the sum in the
+        // fixed chunked order; a non-finite value throws "Projected Gauss-Seidel diverged"
+        res.err = cond_residual(uf, uprev, u, E.cfg.pj_tol_rel, E.cfg.pj_tol_abs);
+        if (!std::isfinite(res.err)) {
+            res.diverged = true;
+            break;
+        }
+        if (res.err < 1.0) break;
+        uprev = u;
+    }
+    x.assign(nv, 0.0);
+    for (int j = 0; j < nv; ++j) x[j] = uf[j] - u[j];
+    // storeImpulse with the normal sign inverted (:257-259)
+    lam_mem.assign(3 * C.size(), 0.0);
+    for (size_t ci = 0; ci < C.size(); ++ci) {
+        const int r0 = W.row_base[ci];
+        lam_mem[3 * ci] = -lam[r0];
+        if (C[ci].frictional) {
+            lam_mem[3 * ci + 1] = lam[r0 + 1];
+            lam_mem[3 * ci + 2] = lam[r0 + 2];
+        }
+    }
+    return res;
+}
+
 // MoreauIntegrator::step (src/physics/integration/moreau.cpp:6-13)
 void step_once(Engine& E) {
     const int N = E.N, S = E.S, nv = 6 * N;
@@ -1373,10 +1513,11 @@ void step_once(Engine& E) {
     E.trace.clear();
     SolveResult sr;
     std::vector<double> cond_mem;
-    if (E.cfg.solver_type == 1) {
-        // solver.type=condensed (colored sweeps); its stats residual is the complementarity
-        // residual of the result with the impulses in the projected Jacobi convention
-        CondResult cr = condensed_colored(E, C, dt, x, cond_mem);
+    if (E.cfg.solver_type == 1 || E.cfg.solver_type == 2) {
+        // solver.type=condensed (colored sweeps) or projected_gauss_seidel; the stats residual is
+        // the complementarity residual of the result with the impulses in the projected Jacobi
+        // convention
+        CondResult cr = E.cfg.solver_type == 1 ? condensed_colored(E, C, dt, x, cond_mem) : pgs_solve(E, C, W, dt, x, cond_mem);
         sr.iters = cr.iters;
         sr.res_last = cr.err;
         if (cr.diverged) E.status = 4;
@@ -1411,7 +1552,7 @@ void step_once(Engine& E) {
         for (int k = 0; k < 3; ++k) E.prev_point[3 * ci + k] = C[ci].point[k];
         const int r0 = W.row_base[ci];
         const int nr = C[ci].frictional ? 3 : 1;
-        for (int k = 0; k < nr; ++k) E.prev_lambda[3 * ci + k] = E.cfg.solver_type == 1 ? cond_mem[3 * ci + k] : lam[r0 + k];
+        for (int k = 0; k < nr; ++k) E.prev_lambda[3 * ci + k] = E.cfg.solver_type != 0 ? cond_mem[3 * ci + k] : lam[r0 + k];
     }
     E.last = C;
     E.last_lambda = E.prev_lambda;

@@ -188,7 +188,8 @@ def config_from(cfg: dict, omp_mode: int = 0, num_threads: int = 0) -> OrConfig:
     c.pj_anderson_m = int(cfg.get("pj.anderson_m", 2))
     c.pj_rdiag_true_delassus = int(bool(cfg.get("pj.rdiag_true_delassus", False)))
     c.moreau_implicit_gyroscopy = int(bool(cfg.get("moreau.implicit_gyroscopy", False)))
-    c.solver_type = {"projected_jacobi": 0, "condensed": 1}[str(cfg.get("solver.type", "projected_jacobi"))]
+    c.solver_type = {"projected_jacobi": 0, "condensed": 1, "projected_gauss_seidel": 2, "pgs": 2}[
+        str(cfg.get("solver.type", "projected_jacobi"))]
     c.condensed_sweep_mode = {"gauss_seidel": 0, "jacobi": 1, "colored": 2, "chaotic": 3}[
         str(cfg.get("condensed.sweep_mode", "gauss_seidel"))]
     c.pj_relaxation = float(cfg.get("pj.relaxation", 1.0))

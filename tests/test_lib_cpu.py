@@ -89,7 +89,9 @@ def test_config_file_parsing(cdxlib, tmp_path):
 def test_config_rejects_other_solvers(cdxlib):
     from cardillocxx_gb300 import CdxError, Config, PhysicsEngine
     with pytest.raises(CdxError):
-        Config().set("solver.type", "pgs")
+        Config().set("solver.type", "clarabel")
+    for name in ("pgs", "projected_gauss_seidel", "ProjectedGaussSeidel"):
+        assert Config({"solver.type": name}).get("solver_type") == 2
     c = Config({"solver.type": "condensed"})
     assert c.get("solver_type") == 1 and c.get("condensed_sweep_mode") == 0  # gauss_seidel by default
     assert Config({"condensed.sweep_mode": "colored"}).get("condensed_sweep_mode") == 2
@@ -99,7 +101,10 @@ def test_config_rejects_other_solvers(cdxlib):
     for bad in ({"solver.type": "condensed"},
                 {"solver.type": "condensed", "condensed.sweep_mode": "jacobi"},
                 {"solver.type": "condensed", "condensed.sweep_mode": "colored", "gpu.precision": "split"},
-                {"solver.type": "condensed", "condensed.sweep_mode": "colored", "pj.nesterov": True}):
+                {"solver.type": "condensed", "condensed.sweep_mode": "colored", "pj.nesterov": True},
+                # projected Gauss-Seidel: its plain loop in the plain FP64 method
+                {"solver.type": "pgs", "gpu.precision": "split"},
+                {"solver.type": "pgs", "gpu.precision": "fp64", "pj.nesterov": True}):
         with pytest.raises(CdxError) as e:
             PhysicsEngine(bad)
         assert e.value.status == 6

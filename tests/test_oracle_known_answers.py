@@ -280,3 +280,74 @@ def test_implicit_gyroscopy_drops_the_gyroscopic_force(oracle_mod):
     o_exp = oracle_mod.Oracle(s, cfg())
     o_exp.step(20)
     np.testing.assert_allclose(o_exp.state()["omega"][0], [3.0, -7.0, 11.0], rtol=1e-12)
+
+
+# ---- projected Gauss-Seidel (projected_gauss_seidel.cpp:56-264) ----
+PGS = {"solver.type": "pgs", "pj.alpha": 1.0, "pj.relaxation": 1.0, "pj.tol_abs": 1e-12, "pj.tol_rel": 1e-12,
+       "pj.max_iterations": 10000}
+
+
+def test_pgs_one_sweep_is_sequential(oracle_mod):
+    # two equal spheres stacked on the ground (touching within 1e-6 m), at rest, frictionless: one
+    # sweep visits the ground
+    # contact first (it stops the lower sphere, lambda_0 = -m g h inside the solver), then the
+    # sphere-sphere contact, which sees the lower sphere's corrected velocity and shares it
+    # (lambda_1 = -m g h / 2): both spheres leave the sweep at -g h / 2. A Jacobi sweep would leave
+    # the upper sphere at -g h.
+    r = 0.05
+    s = make_scene([{"pos": (0.0, 0.0, r), "radius": r, "mu": 0.0},
+                    {"pos": (0.0, 0.0, 3 * r - 1e-6), "radius": r, "mu": 0.0}], [dict(GROUND, mu=0.0)])
+    m = s["mass"][0]
+    o = oracle_mod.Oracle(s, cfg(**dict(PGS, **{"pj.max_iterations": 1, "pj.warmstart": False,
+                                                "pj.tol_abs": 1.0, "pj.tol_rel": 1.0})))
+    o.step(1)
+    c = o.contacts()
+    assert c["id_a"].tolist() == [0, 1] and c["id_b"].tolist() == [1, 2]
+    np.testing.assert_allclose(c["lambda"][:, 0], [m * G * H, m * G * H / 2], rtol=1e-12)
+    np.testing.assert_allclose(o.state()["vel"][:, 2], [-G * H / 2, -G * H / 2], rtol=1e-12)
+    assert o.stats()["iterations"] == 1
+
+
+def test_pgs_resting_contact_and_sliding_friction(oracle_mod):
+    r, mu, v0 = 0.05, 0.3, 1.0
+    s = make_scene([{"pos": (0.0, 0.0, r), "radius": r, "vel": (v0, 0, 0), "mu": mu}], [dict(GROUND, mu=mu)])
+    m = s["mass"][0]
+    o = oracle_mod.Oracle(s, cfg(**PGS))
+    o.step(1)
+    c = o.contacts()
+    # stored convention: the normal impulse non-negative; it carries the weight
+    np.testing.assert_allclose(c["lambda"][0, 0], m * G * H, rtol=1e-9)
+    assert abs(o.state()["vel"][0, 2]) < 1e-10
+    o.step(9)
+    # sliding: v decreases by mu g per unit time, the spin grows by the friction torque
+    np.testing.assert_allclose(o.state()["vel"][0, 0], v0 - mu * G * 10 * H, rtol=1e-8)
+    np.testing.assert_allclose(o.state()["omega"][0, 1], 10 * H * 5 * mu * G / (2 * r), rtol=1e-8)
+    o.step(190)
+    # rolling from t = 2 v0 / (7 mu g): v = 5 v0 / 7
+    np.testing.assert_allclose(o.state()["vel"][0, 0], 5 * v0 / 7, rtol=1e-8)
+
+
+def test_pgs_converges_to_the_projected_jacobi_solution(oracle_mod):
+    from cardillocxx_gb300 import scenes
+    s = scenes.generate("pile_1k", scale=0.1)
+    base = scenes.config_for("pile_1k")
+    o = oracle_mod.Oracle(s, base)
+    o.step(200)
+    st = o.state()
+    sc = dict(s)
+    for k in st:
+        sc[k] = st[k].copy()
+    tight = {"pj.tol_abs": 1e-10, "pj.tol_rel": 1e-10, "pj.max_iterations": 100000, "pj.warmstart": False}
+    pj = oracle_mod.Oracle(sc, dict(base, **tight))
+    pj.step(1)
+    gs = oracle_mod.Oracle(sc, dict(base, **tight, **{"solver.type": "pgs", "pj.alpha": 1.0, "pj.relaxation": 1.0}))
+    gs.step(1)
+    assert gs.stats()["num_contacts"] > 20
+    vs = np.abs(st["vel"]).max() + G * 1e-3
+    assert np.abs(pj.state()["vel"] - gs.state()["vel"]).max() <= 1e-6 * vs
+    # Gauss-Seidel with alpha 1 takes fewer sweeps than Jacobi with alpha 0.5
+    assert gs.stats()["iterations"] < pj.stats()["iterations"]
+    # without a tolerance the velocity-increment residual divides by zero: the reference throws
+    # "Projected Gauss-Seidel diverged" (projected_gauss_seidel.cpp:144-147)
+    with pytest.raises(RuntimeError):
+        oracle_mod.Oracle(sc, dict(base, **{"solver.type": "pgs"})).step(1)
