@@ -471,12 +471,41 @@ def other_workloads(flush):
             rec[prec] = {"ms_per_step": sum(ms) / len(ms), "sweeps": it[-1], "residual": res[-1], "steps": n,
                          "contacts": con[-1], "shape": names[v] if prec == "split" and 0 <= v < len(names) else None}
         rec["fp64_over_split"] = rec["fp64"]["ms_per_step"] / rec["split"]["ms_per_step"]
+        if name == "batch_4096":
+            rec["at_residual"] = scenes_at_residual(s2, mem, cfg, flush)
         rec["seconds"] = time.time() - t0
         out[name] = rec
         log(f"{name}: split {rec['split']['ms_per_step']:.2f} ms/step, fp64 {rec['fp64']['ms_per_step']:.1f} ms/step")
     t0 = time.time()
     out["diff_256x256"] = rollout("diff_256x256", 1.0, 200, 1, 1)
     out["diff_256x256"]["seconds"] = time.time() - t0
+    return out
+
+
+def scenes_at_residual(s2, mem, cfg, flush, tol=1e-6, cap=2000, steps=5, warmup=8):
+    """The batched scenes solved per scene to the residual tolerance: pj.alpha everywhere against
+    the autotuner's per-scene alpha (gpu.tune_alpha). The untimed first steps hold the shape
+    autotuner's trial steps and the alpha tuner's trial solves."""
+    import numpy as np
+    from cardillocxx_gb300 import PhysicsEngine
+    ns = int(s2["num_scenes"])
+    out = {"residual_tol": tol, "sweep_cap": cap}
+    for name, over in (("alpha_fixed", {}), ("alpha_tuned", {"gpu.tune_alpha": True})):
+        e = PhysicsEngine(dict(cfg, **{"gpu.precision": "split", "gpu.residual_tol": tol, "pj.max_iterations": cap},
+                               **over)).load_scene(s2).set_contacts(mem)
+        ms, it, con, res, _ = time_engine(e, steps, warmup, flush)
+        info = e.scene_solve(ns)
+        sw = info["sweeps"]
+        out[name] = {"ms_per_step": sum(ms) / len(ms), "residual_max": max(res), "max_sweeps": int(sw.max()),
+                     "mean_scene_sweeps": float(sw.mean()), "scenes_at_cap": int((sw >= cap).sum()),
+                     "steps": steps, "warmup_steps": warmup}
+        if name == "alpha_tuned":
+            a = info["alpha"]
+            out[name]["alpha_counts"] = {f"{v:g}": int((np.abs(a - v) < 1e-6).sum()) for v in np.unique(a)}
+        e.close()
+        log(f"batch_4096 at residual {tol:g}, {name}: {out[name]['ms_per_step']:.2f} ms/step, mean scene sweeps "
+            f"{out[name]['mean_scene_sweeps']:.1f}, at cap {out[name]['scenes_at_cap']}")
+    out["tuned_speedup"] = out["alpha_fixed"]["ms_per_step"] / out["alpha_tuned"]["ms_per_step"]
     return out
 
 

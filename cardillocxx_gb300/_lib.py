@@ -72,10 +72,10 @@ class CdxConfig(C.Structure):
         ("output_filename_prefix", C.c_char * 128),
         ("gpu_coop_smem_contacts", C.c_int32),
         ("gpu_coop_blocks", C.c_int32),
-        ("gpu_pad0", C.c_int32),
+        ("gpu_tune_alpha", C.c_int32),
         ("gpu_coop_wait_ns", C.c_int64),
         ("condensed_sweep_mode", C.c_int32),
-        ("pad1", C.c_int32),
+        ("gpu_tune_alpha_every", C.c_int32),
     ]
 
 
@@ -115,6 +115,7 @@ class CdxStats(C.Structure):
         ("redone_steps", C.c_int32),
         ("graph_steps", C.c_int64),
         ("sweep_variant", C.c_int32),
+        ("levels", C.c_int32),
     ]
 
 
@@ -158,6 +159,7 @@ SIGNATURES = [
     ("cdx_get_contacts", C.c_int, [C.c_void_p, _PI, _PI, _P, _P, _P, _PI]),
     ("cdx_set_contacts", C.c_int, [C.c_void_p, C.c_int32, _PI, _PI, _P, _P]),
     ("cdx_set_config", C.c_int, [C.c_void_p, C.POINTER(CdxConfig)]),
+    ("cdx_get_scene_solve", C.c_int, [C.c_void_p, C.POINTER(C.c_float), _PI, C.c_int32]),
     ("cdx_track", C.c_int, [C.c_void_p, C.c_int32, C.c_char_p]),
     ("cdx_output_flush", C.c_int, [C.c_void_p]),
     ("cdx_set_trace", C.c_int, [C.c_void_p, C.c_int32]),

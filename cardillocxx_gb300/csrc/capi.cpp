@@ -86,6 +86,11 @@ int cdx_set_contacts(cdx_ctx* ctx, int32_t count, const int32_t* id_a, const int
     }
 }
 
+int cdx_get_scene_solve(cdx_ctx* ctx, float* alpha, int32_t* sweeps, int32_t n) {
+    if (!ctx || n < 0) return CDX_ERR_ARG;
+    return ctx->eng.scene_solve_info(alpha, sweeps, n);
+}
+
 int cdx_track(cdx_ctx* ctx, int32_t body, const char* name) {
     if (!ctx) return CDX_ERR_ARG;
     try {

@@ -82,6 +82,8 @@ int cdx_config_default(cdx_config* c) {
     c->pj_relaxation = 1.0;
     c->solver_type = 0;
     c->condensed_sweep_mode = 0;  // condensed.sweep_mode = gauss_seidel (config.hpp:118)
+    c->gpu_tune_alpha = 0;
+    c->gpu_tune_alpha_every = 500;
     c->collision_security_margin = 0.0;
     c->collision_match_max_dist = 0.02;
     c->collision_broadphase = 0;
@@ -202,6 +204,10 @@ int cdx_config_set(cdx_config* c, const char* key_c, const char* val_c) {
         if (as_int(val, &i)) c->gpu_coop_blocks = std::max(0, i);
     } else if (key == "gpu.coop_wait_ns") {
         if (as_double(val, &d) && d >= 0 && d < 9e18) c->gpu_coop_wait_ns = (int64_t)d;
+    } else if (key == "gpu.tune_alpha") {
+        c->gpu_tune_alpha = as_bool(val);
+    } else if (key == "gpu.tune_alpha_every") {
+        if (as_int(val, &i) && i >= 1) c->gpu_tune_alpha_every = i;
     } else if (key == "gpu.sync_counts") {
         c->gpu_sync_counts = as_bool(val);
     } else if (key_is(key, "pj.nesterov")) {

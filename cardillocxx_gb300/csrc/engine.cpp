@@ -1073,6 +1073,7 @@ void Engine::fill_stats(cdx_stats* s) {
     s->redone_steps = split_redos();
     s->graph_steps = split_graph_steps();
     s->sweep_variant = split_sweep_variant();
+    s->levels = last_levels;
 }
 
 double Engine::solve_bytes_per_iter() const {

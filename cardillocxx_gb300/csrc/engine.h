@@ -129,6 +129,7 @@ struct Engine {
     int ensure_pgs();
     int solve_pgs();
     void split_config_changed();
+    int scene_solve_info(float* alpha, int32_t* sweeps, int32_t n);
     int load_scene(const cdx_scene& s);
     int ensure_tmp(int64_t n);
     int ensure_contacts(int64_t need);

@@ -46,6 +46,16 @@ struct SplitState {
     int64_t scene_tuned_at = 0;      // contact count when the scenes shapes were last timed
     double scene_ms[16] = {0};
     int scene_timing = -1;           // shape timed in the current step
+    // the scenes' alpha autotuner (gpu.tune_alpha): each scene's alpha, the best trial per scene,
+    // each scene's sweeps and residual in the last solve, and the warm start kept for the trials
+    float* scene_alpha = nullptr;
+    float4* tune_best = nullptr;
+    int4* scene_out = nullptr;
+    int scene_bufs_n = 0;
+    float4* lam_save = nullptr;
+    int64_t lam_save_cap = 0;
+    int64_t alpha_tuned_step = -1;
+    int alpha_tunings = 0;
     // steps that find their contact totals on the device: a snapshot of the state they change, so
     // a step whose contacts outgrow the buffers or the plan can be undone and redone
     double* snap = nullptr;   // 13 N: position, quaternion, velocity, omega (body field order)
@@ -115,6 +125,88 @@ void Engine::destroy_split() {
     if (split->h_ss) cudaFreeHost(split->h_ss);
     delete split;
     split = nullptr;
+}
+
+// per-scene buffers of the alpha autotuner; a new scene count starts from the configured alpha
+static int split_alpha_bufs(Engine& E) {
+    SplitState* S = E.split;
+    const int ns = std::max(E.sc.nscenes, 1);
+    if (S->scene_bufs_n != ns) {
+        int st;
+        if ((st = salloc(E, (void**)&S->scene_alpha, sizeof(float) * ns, "scene alpha"))) return st;
+        if ((st = salloc(E, (void**)&S->tune_best, sizeof(float4) * ns, "scene alpha"))) return st;
+        if ((st = salloc(E, (void**)&S->scene_out, sizeof(int4) * ns, "scene alpha"))) return st;
+        S->scene_bufs_n = ns;
+        launch_s_tune_alpha(0, ns, (float)E.cfg.pj_alpha, nullptr, S->tune_best, nullptr, E.stream);
+        launch_s_tune_alpha(2, ns, 0.f, nullptr, S->tune_best, S->scene_alpha, E.stream);
+        S->alpha_tuned_step = -1;
+    }
+    if (S->lam_save_cap < S->sb.cap) {
+        int st;
+        if ((st = salloc(E, (void**)&S->lam_save, sizeof(float4) * std::max<int64_t>(S->sb.cap, 1), "scene alpha")))
+            return st;
+        S->lam_save_cap = S->sb.cap;
+    }
+    return CDX_OK;
+}
+
+// The scenes' alpha autotuner: trial solves of this step, from its warm start, with each candidate
+// alpha; per scene the candidate that reaches gpu.residual_tol in the fewest sweeps (or, without a
+// tolerance or when none reaches it, the lowest residual at the cap) is kept. Every alpha > 0 has
+// the same fixed points (lambda = Pi(lambda - alpha D^-1 gamma) holds for all of them at a
+// complementarity solution), so alpha changes how fast a scene converges, not what it converges to.
+// The trial residuals are rescaled to the configured alpha, which the stop rule and the FP64
+// residual keep using.
+static int split_tune_alpha(Engine& E, int gen, int scene_v, int maxit, const int32_t* spos, const int32_t* sflags,
+                            const int32_t* poff, int cblocks) {
+    SplitState* S = E.split;
+    SplitBuf& sb = S->sb;
+    const int ns = std::max(E.sc.nscenes, 1);
+    const int nc = S->nc;
+    const float a0 = (float)E.cfg.pj_alpha;
+    static const float cand[] = {0.2f, 0.3f, 0.4f, 0.5f, 0.6f, 0.7f, 0.85f, 1.0f};
+    cudaMemcpyAsync(S->lam_save, sb.lam[gen], sizeof(float4) * (size_t)nc, cudaMemcpyDeviceToDevice, E.stream);
+    launch_s_tune_alpha(0, ns, a0, nullptr, S->tune_best, nullptr, E.stream);
+    auto trial = [&](float a, int ref) -> int {
+        cudaMemcpyAsync(sb.lam[gen], S->lam_save, sizeof(float4) * (size_t)nc, cudaMemcpyDeviceToDevice, E.stream);
+        launch_s_reset(sb, E.stream);
+        launch_s_acc_init(sb, E.stream);
+        launch_s_apply_warm(sb, gen, cblocks, E.stream);
+        int st = launch_s_solve_scenes(E.sc, sb, gen, a, scene_v, maxit, (float)E.cfg.gpu_residual_tol, spos, sflags,
+                                       poff, S->scene_order, S->scene_nbmax, E.stream, nullptr, a0, S->scene_out);
+        if (st) return E.cuda_check((cudaError_t)st, "alpha trial solve");
+        launch_s_tune_alpha(ref ? 3 : 1, ns, a, S->scene_out, S->tune_best, nullptr, E.stream);
+        E.launches += 5;
+        return CDX_OK;
+    };
+    int st;
+    if ((st = trial(a0, 1))) return st;
+    for (float a : cand)
+        if (a != a0 && (st = trial(a, 0))) return st;
+    // back to the step's own start
+    cudaMemcpyAsync(sb.lam[gen], S->lam_save, sizeof(float4) * (size_t)nc, cudaMemcpyDeviceToDevice, E.stream);
+    launch_s_reset(sb, E.stream);
+    launch_s_acc_init(sb, E.stream);
+    launch_s_apply_warm(sb, gen, cblocks, E.stream);
+    launch_s_tune_alpha(2, ns, 0.f, nullptr, S->tune_best, S->scene_alpha, E.stream);
+    E.launches += 4;
+    S->alpha_tuned_step = E.steps;
+    ++S->alpha_tunings;
+    return E.cuda_check(cudaGetLastError(), "alpha tuning");
+}
+
+// the scenes' alpha and last sweeps (gpu.tune_alpha), for inspection
+int Engine::scene_solve_info(float* alpha, int32_t* sweeps, int32_t n) {
+    if (!split || !split->scene_alpha) return fail(CDX_ERR_STATE, "no per-scene solve has run");
+    const int ns = std::min(n, split->scene_bufs_n);
+    std::vector<int4> out(ns);
+    if (alpha) cudaMemcpyAsync(alpha, split->scene_alpha, sizeof(float) * ns, cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(out.data(), split->scene_out, sizeof(int4) * ns, cudaMemcpyDeviceToHost, stream);
+    int st = cuda_check(cudaStreamSynchronize(stream), "scene solve info");
+    if (st) return st;
+    if (sweeps)
+        for (int i = 0; i < ns; ++i) sweeps[i] = out[i].x;
+    return CDX_OK;
 }
 
 static int split_contacts(Engine& E, int64_t need) {
@@ -364,8 +456,13 @@ int Engine::step_split() {
         S->scene_tried = 0;
     }
     const bool scene_tuning = scene_fit && pinned < 0 && S->scene_best == -1 && cfg.gpu_autotune;
+    // the scenes' alpha is tuned on the first step of the scenes kernel and then every
+    // gpu.tune_alpha_every steps (trial solves need the true contact count: a synchronous step)
+    const bool scenes_chosen = pinned >= 0 ? split_variant_is_scenes(pinned) : (cfg.gpu_autotune ? S->scene_best >= 0 : true);
+    const bool alpha_due = scene_fit && scenes_chosen && cfg.gpu_tune_alpha &&
+                           (S->alpha_tuned_step < 0 || steps - S->alpha_tuned_step >= cfg.gpu_tune_alpha_every);
     const bool async = !cfg.gpu_sync_counts && S->prev_count > 0 && sb.cap > 0 && !S->force_sync && !scene_tuning &&
-                       !tune_due(S->prev_count);
+                       !tune_due(S->prev_count) && !alpha_due;
     S->force_sync = false;
     if (async) {
         // the warm-start layout of the last step is read on the device
@@ -390,7 +487,8 @@ int Engine::step_split() {
         }
     }
     const long long gkey[8] = {(long long)sb.cap, (long long)S->variant, scenes0 ? 1 : 0, S->gplan.cpb, S->gplan.bpb,
-                               S->gplan.vf, S->gplan.smem, (long long)cfg.pj_warmstart};
+                               S->gplan.vf, S->gplan.smem,
+                               (long long)cfg.pj_warmstart | ((long long)(cfg.gpu_tune_alpha != 0) << 1)};
     bool capturing = false;
     int64_t launches0 = launches;
     int64_t n_static = 0;
@@ -531,9 +629,19 @@ int Engine::step_split() {
         cudaEventRecord(S->tev[0], stream);
     }
     if (scenes) {
+        const float* salpha = nullptr;
+        if ((st = split_alpha_bufs(*this))) return st;
+        if (cfg.gpu_tune_alpha) {
+            if (alpha_due && !capturing && !async) {
+                if ((st = split_tune_alpha(*this, gen, scene_v, maxit, nflag > 0 ? spos : nullptr,
+                                           nflag > 0 ? sflags : nullptr, poff, cblocks)))
+                    return st;
+            }
+            salpha = S->scene_alpha;
+        }
         st = launch_s_solve_scenes(sc, sb, gen, (float)cfg.pj_alpha, scene_v, maxit, (float)cfg.gpu_residual_tol,
                                    nflag > 0 ? spos : nullptr, nflag > 0 ? sflags : nullptr, poff, S->scene_order,
-                                   S->scene_nbmax, stream);
+                                   S->scene_nbmax, stream, salpha, (float)cfg.pj_alpha, S->scene_out);
         if ((st = cuda_check((cudaError_t)st, "scenes solve"))) return st;
         S->last_variant = scene_v;
         ++launches;

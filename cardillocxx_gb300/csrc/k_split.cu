@@ -1399,18 +1399,24 @@ __global__ void __launch_bounds__(NTH, 1) k_s_solve_coop_loop(SplitBuf sb, int g
 // The final velocities go to accumulator 0; the largest per-scene sweep count and residual go to
 // the step's scalars.
 // 1024 / NT blocks an SM at least: 64 registers a thread, 32 warps an SM
+// scene_alpha (optional): each scene's alpha; the in-sweep residual is then rescaled to alpha_ref
+// (the residual's R is alpha / D, and near the fixed point it scales with alpha) for the stop rule
+// and the statistics. scene_out (optional): each scene's sweeps and rescaled residual.
 template <int NT, int CSM>
 __global__ void __launch_bounds__(NT, 1024 / NT) k_s_solve_scenes(Scene sc, SplitBuf sb, int gen, float alpha, int max_iter,
                                                        float tol, const int32_t* spos, const int32_t* sflags,
-                                                       const int32_t* poff, const int32_t* order, int L, int ccap) {
+                                                       const int32_t* poff, const int32_t* order, int L, int ccap,
+                                                       const float* scene_alpha, float alpha_ref, int4* scene_out) {
     extern __shared__ float4 sm4[];
     // a device-counted step whose contacts overflowed the buffers wrote only the slots below the
     // capacity, while the scene ranges below count them all: nothing runs, the host redoes the step
     if (*(volatile const int32_t*)&sb.ss->cap_err) return;
-    __shared__ float s_r;
+    __shared__ float s_r, s_l;
     const int s = order[blockIdx.x];
     const int b0 = sc.scene_body_start[s], nb = sc.scene_body_start[s + 1] - b0;
     const int tid = threadIdx.x;
+    const float a_s = scene_alpha ? scene_alpha[s] : alpha;
+    const float rscale = alpha_ref / a_s;
     const int64_t nflag = (int64_t)sc.N * L;
     int n_static = 0;
     if (nflag > 0) n_static = spos[nflag - 1] + sflags[nflag - 1];
@@ -1472,7 +1478,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_s_solve_scenes(Scene sc, Spli
                     va = make_float4(0.f, 0.f, 0.f, 0.f);
                     wa = va;
                 }
-                pj_contact(r0, r1, l, va, wa, vb, wb, &sb.bias[c], alpha, o);
+                pj_contact(r0, r1, l, va, wa, vb, wb, &sb.bias[c], a_s, o);
                 if (local)
                     ls[k] = o.lam;
                 else
@@ -1488,12 +1494,16 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_s_solve_scenes(Scene sc, Spli
         }
         // the barriers below also order this sweep's reductions before the next sweep's gathers
         block_max2(maxd2, maxl);
-        if (tid == 0) s_r = sweep_residual(maxd2, maxl);
+        if (tid == 0) {
+            s_r = sweep_residual(maxd2, maxl) * rscale;
+            s_l = maxl;
+        }
         __syncthreads();
         r = s_r;
         ++it;
         if (it >= max_iter || (tol > 0.f && r <= tol) || !(r == r)) break;
     }
+    if (scene_out && tid == 0) scene_out[s] = make_int4(it, __float_as_int(r), __float_as_int(s_l), 0);
     // the final velocities to accumulator 0, where the final FP64 pass reads them
     if (it % 3 != 0) {
         const float4* Gf = sb.acc[it % 3];
@@ -1511,6 +1521,47 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_s_solve_scenes(Scene sc, Spli
         atomicMax(reinterpret_cast<unsigned*>(&sb.ss->res_last), __float_as_uint(r == r ? r : 0.f));
         atomicAdd(&sb.ss->iters_sum, (unsigned long long)it);
     }
+}
+
+// the accumulators back to the free velocities (as k_s_prep leaves them), before the warm start
+__global__ void k_s_acc_init(SplitBuf sb) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sb.N) return;
+    const float4 v = sb.vel4[2 * i], w = sb.vel4[2 * i + 1];
+    for (int k = 0; k < 3; ++k) {
+        sb.acc[k][2 * i] = v;
+        sb.acc[k][2 * i + 1] = w;
+    }
+}
+
+// the scenes' alpha autotuner: best (sweeps, residual, alpha) per scene over the trial solves
+__global__ void k_s_tune_init(int ns, float alpha, float4* best) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < ns) best[s] = make_float4(__int_as_float(0x7fffffff), INFINITY, alpha, 0.f);
+}
+// The first trial (the configured alpha) is the reference. Another trial is kept when its residual
+// is finite, its impulses stay at the reference's scale (the residual is relative to max |lambda|,
+// so impulses that grow without bound can look converged), and it needs fewer sweeps (with a
+// tolerance) or, at equal sweeps, ends lower.
+__global__ void k_s_tune_pick(int ns, float cand, const int4* out, float4* best, int is_ref) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= ns) return;
+    const int it = out[s].x;
+    const float r = __int_as_float(out[s].y);
+    const float lm = __int_as_float(out[s].z);
+    if (is_ref) {
+        best[s] = make_float4(__int_as_float(it), r, cand, lm);
+        return;
+    }
+    if (!(r == r) || isinf(r) || !(lm == lm) || isinf(lm)) return;
+    const float4 b = best[s];
+    if (!(lm <= 1.25f * b.w && b.w <= 1.25f * lm)) return;
+    const int bit = __float_as_int(b.x);
+    if (it < bit || (it == bit && r < b.y)) best[s] = make_float4(__int_as_float(it), r, cand, b.w);
+}
+__global__ void k_s_tune_commit(int ns, const float4* best, float* scene_alpha) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < ns) scene_alpha[s] = best[s].z;
 }
 
 __global__ void k_s_totals(SplitBuf sb, const int32_t* spos, const int32_t* sflags, int64_t nflag,
@@ -1868,7 +1919,7 @@ static CoopLoopVariant g_coop_loop[2][2] = {
 // Batched scenes (one block per scene): threads per block and contacts per thread per pass.
 struct ScenesVariant {
     void (*kernel)(Scene, SplitBuf, int, float, int, float, const int32_t*, const int32_t*, const int32_t*,
-                   const int32_t*, int, int);
+                   const int32_t*, int, int, const float*, float, int4*);
     int nth, csm;
     int smem_set;  // dynamic shared memory the kernel has been opted in to
 };
@@ -1908,9 +1959,20 @@ const char* split_variant_name(int v) {
     return names[v];
 }
 
+void launch_s_tune_alpha(int op, int ns, float alpha, const int4* out, float4* best, float* scene_alpha,
+                         cudaStream_t s) {
+    if (ns <= 0) return;
+    if (op == 0) k_s_tune_init<<<nblk(ns), NT, 0, s>>>(ns, alpha, best);
+    if (op == 1 || op == 3) k_s_tune_pick<<<nblk(ns), NT, 0, s>>>(ns, alpha, out, best, op == 3);
+    if (op == 2) k_s_tune_commit<<<nblk(ns), NT, 0, s>>>(ns, best, scene_alpha);
+}
+void launch_s_acc_init(const SplitBuf& sb, cudaStream_t s) {
+    if (sb.N > 0) k_s_acc_init<<<nblk(sb.N), NT, 0, s>>>(sb);
+}
+
 int launch_s_solve_scenes(const Scene& sc, const SplitBuf& sb, int gen, float alpha, int v, int max_iter, float tol,
                           const int32_t* spos, const int32_t* sflags, const int32_t* poff, const int32_t* order,
-                          int nbmax, cudaStream_t s) {
+                          int nbmax, cudaStream_t s, const float* scene_alpha, float alpha_ref, int4* scene_out) {
     if (!split_variant_is_scenes(v) || sc.nscenes <= 0) return (int)cudaErrorInvalidValue;
     ScenesVariant& cv = g_scenes[v - N_STREAM - N_COOP];
     // shared memory (contact-resident shapes): 48 B for each of up to 3 contacts a body (a settled
@@ -1925,7 +1987,8 @@ int launch_s_solve_scenes(const Scene& sc, const SplitBuf& sb, int gen, float al
         cv.smem_set = smem;
     }
     cv.kernel<<<sc.nscenes, cv.nth, smem, s>>>(sc, sb, gen, alpha, max_iter, tol, spos, sflags, poff, order,
-                                              sc.max_statics, ccap);
+                                              sc.max_statics, ccap, scene_alpha, alpha_ref > 0.f ? alpha_ref : alpha,
+                                              scene_out);
     return (int)cudaGetLastError();
 }
 

@@ -136,9 +136,19 @@ int split_first_coop_variant();
 int split_num_scenes_variants();
 // batched scenes: the whole solve of every scene, one block per scene (order = scene ids by
 // decreasing size; nbmax = bodies of the largest scene). Returns a cudaError_t.
+// scene_alpha (optional): per-scene alpha, with the residual rescaled to alpha_ref; scene_out
+// (optional): per-scene sweeps and residual
 int launch_s_solve_scenes(const Scene& sc, const SplitBuf& sb, int gen, float alpha, int v, int max_iter, float tol,
                           const int32_t* spos, const int32_t* sflags, const int32_t* poff, const int32_t* order,
-                          int nbmax, cudaStream_t s);
+                          int nbmax, cudaStream_t s, const float* scene_alpha = nullptr, float alpha_ref = 0.f,
+                          int4* scene_out = nullptr);
+// the scenes' alpha autotuner: op 0 resets the best (alpha = the configured one), 3 records the
+// reference trial (the configured alpha), 1 keeps trial `alpha` where it beats the best, 2 writes
+// the best alphas
+void launch_s_tune_alpha(int op, int ns, float alpha, const int4* out, float4* best, float* scene_alpha,
+                         cudaStream_t s);
+// the accumulators back to the free velocities (before a warm start is applied again)
+void launch_s_acc_init(const SplitBuf& sb, cudaStream_t s);
 // cooperative whole-solve partition (grid = one block per SM, contact and body ranges per block)
 struct CoopPlan {
     int grid = 0, nth = 0, cpb = 0, bpb = 0, vf = 0, smem = 0;

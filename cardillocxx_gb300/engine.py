@@ -182,6 +182,13 @@ class PhysicsEngine:
         self._check(self.L.cdx_set_contacts(self.h, n, ip(ia), ip(ib), dp(pt), dp(lam)))
         return self
 
+    def scene_solve(self, nscenes: int) -> dict:
+        """Batched scenes (per-scene solve): each scene's alpha and its sweeps in its last solve."""
+        a = np.empty(nscenes, np.float32)
+        it = np.empty(nscenes, np.int32)
+        self._check(self.L.cdx_get_scene_solve(self.h, a.ctypes.data_as(C.POINTER(C.c_float)), ip(it), nscenes))
+        return {"alpha": a, "sweeps": it}
+
     def track(self, body: int, name: str):
         """Write sphere `body` to <output.folder>/<output.filename_prefix>_tracked.csv every step."""
         self._check(self.L.cdx_track(self.h, int(body), str(name).encode()))

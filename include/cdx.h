@@ -96,13 +96,16 @@ typedef struct cdx_config {
                                                cooperative solve keeps in shared memory (0 = all that fit) */
     int32_t gpu_coop_blocks;                /* gpu.coop_blocks: blocks of the cooperative solve (0 = one per SM;
                                                more than that is capped) */
-    int32_t gpu_pad0;
+    int32_t gpu_tune_alpha;                 /* gpu.tune_alpha: batched scenes (split form): the autotuner also picks
+                                               each scene's pj.alpha from a candidate set by trial solves of the
+                                               same step (fewest sweeps to gpu.residual_tol, else the lowest
+                                               residual at the sweep cap); off keeps pj.alpha everywhere */
     int64_t gpu_coop_wait_ns;               /* gpu.coop_wait_ns: longest wait of a block of the cooperative solve
                                                at a grid barrier before the step fails with CDX_ERR_TIMEOUT
                                                (0 = 0.2 s) */
     int32_t condensed_sweep_mode;           /* condensed.sweep_mode: 0 gauss_seidel (default), 1 jacobi,
                                                2 colored (the one run on the GPU), 3 chaotic */
-    int32_t pad1;
+    int32_t gpu_tune_alpha_every;           /* gpu.tune_alpha_every: steps between two tunings of the scenes' alpha */
 } cdx_config;
 
 /* Scene: dynamic spheres plus static shapes (halfspaces, drums). Bodies of one scene are
@@ -155,6 +158,8 @@ typedef struct cdx_stats {
     int64_t graph_steps;       /* split form: steps replayed whole from a captured CUDA graph */
     int32_t sweep_variant;     /* split form: the shape cdx_time_sweeps times (the whole-problem solver,
                                   also when a batched-scenes shape ran the step) */
+    int32_t levels;            /* projected Gauss-Seidel: levels of the last step's sweep (its longest
+                                  chain of dependent blocks) */
 } cdx_stats;
 
 typedef struct cdx_ctx cdx_ctx;
@@ -192,6 +197,11 @@ int cdx_get_contacts(cdx_ctx* ctx, int32_t* id_a, int32_t* id_b, double* point, 
  * cdx_get_contacts returns this memory with zero normals. */
 int cdx_set_contacts(cdx_ctx* ctx, int32_t count, const int32_t* id_a, const int32_t* id_b, const double* point,
                      const double* lambda);
+/* Batched scenes (split form, per-scene solve): each scene's pj.alpha (as gpu.tune_alpha chose it;
+ * pj.alpha without it) and the sweeps each scene took in its last solve (either pointer may be
+ * NULL; n scenes at most). No reference counterpart: the reference runs one alpha for every
+ * contact. CDX_ERR_STATE before a per-scene solve has run. */
+int cdx_get_scene_solve(cdx_ctx* ctx, float* alpha, int32_t* sweeps, int32_t n);
 /* track a sphere in <output.folder>/<output.filename_prefix>_tracked.csv, one row every step
  * (World::track, world.cpp:38-45; CsvWriter::writeTrackedState, csv_writer.hpp:43-52) */
 int cdx_track(cdx_ctx* ctx, int32_t body, const char* name);
