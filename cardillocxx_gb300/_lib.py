@@ -160,6 +160,8 @@ SIGNATURES = [
     ("cdx_set_contacts", C.c_int, [C.c_void_p, C.c_int32, _PI, _PI, _P, _P]),
     ("cdx_set_config", C.c_int, [C.c_void_p, C.POINTER(CdxConfig)]),
     ("cdx_get_scene_solve", C.c_int, [C.c_void_p, C.POINTER(C.c_float), _PI, C.c_int32]),
+    ("cdx_set_static_motion", C.c_int, [C.c_void_p, C.c_int32, _PI, _P, _P, _P, _P]),
+    ("cdx_get_static_state", C.c_int, [C.c_void_p, _P, _P, _P, _P]),
     ("cdx_track", C.c_int, [C.c_void_p, C.c_int32, C.c_char_p]),
     ("cdx_output_flush", C.c_int, [C.c_void_p]),
     ("cdx_set_trace", C.c_int, [C.c_void_p, C.c_int32]),

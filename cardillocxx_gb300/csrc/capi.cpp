@@ -86,6 +86,21 @@ int cdx_set_contacts(cdx_ctx* ctx, int32_t count, const int32_t* id_a, const int
     }
 }
 
+int cdx_set_static_motion(cdx_ctx* ctx, int32_t count, const int32_t* statics, const double* pos,
+                          const double* quat, const double* vel, const double* omega) {
+    if (!ctx) return CDX_ERR_ARG;
+    try {
+        return ctx->eng.set_static_motion(count, statics, pos, quat, vel, omega);
+    } catch (const std::exception& e) {
+        return ctx->eng.fail(CDX_ERR_ARG, e.what());
+    }
+}
+
+int cdx_get_static_state(cdx_ctx* ctx, double* pos, double* quat, double* vel, double* omega) {
+    if (!ctx) return CDX_ERR_ARG;
+    return ctx->eng.get_static_state(pos, quat, vel, omega);
+}
+
 int cdx_get_scene_solve(cdx_ctx* ctx, float* alpha, int32_t* sweeps, int32_t n) {
     if (!ctx || n < 0) return CDX_ERR_ARG;
     return ctx->eng.scene_solve_info(alpha, sweeps, n);

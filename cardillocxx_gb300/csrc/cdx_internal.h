@@ -258,6 +258,9 @@ int launch_pgs_solve(const Scene& sc, const Contacts& C, int nc, const CondBufs&
 void launch_cond_ufree(const Scene& sc, double dt, const double* g, int implicit_gyro, CondBufs& B, cudaStream_t s);
 // nonfinite (optional): set to 1 when a body's state after the drift is not finite
 void launch_drift64(const Scene& sc, double h, int compute_R, cudaStream_t s, int32_t* nonfinite = nullptr);
+// prescribed static motion for the coming step (13 doubles a static: position, quaternion,
+// velocity, angular velocity; flags 1/2/4/8 say which apply), after the first drift
+void launch_static_motion64(const Scene& sc, const double* mot, const int32_t* flag, cudaStream_t s);
 void launch_static_flags64(const Scene& sc, double margin, int32_t* flags, cudaStream_t s);
 // FP32 copy of the positions (relative to the grid origin) and radii: the pair kernels' conservative
 // pre-test, so that only pairs near contact reach the FP64 test

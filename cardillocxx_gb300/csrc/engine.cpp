@@ -306,6 +306,12 @@ int Engine::load_scene(const cdx_scene& s) {
         if ((st = cuda_check(cudaMemcpy(sc.static_kind, kind.data(), sizeof(int32_t) * S, cudaMemcpyHostToDevice), "upload"))) return st;
         if ((st = cuda_check(cudaMemcpy(sc.static_scene, ssc.data(), sizeof(int32_t) * S, cudaMemcpyHostToDevice), "upload"))) return st;
     }
+    if ((st = dalloc((void**)&smot, sizeof(double) * 13 * std::max(1, S), "static motion"))) return st;
+    if ((st = dalloc((void**)&smflag, sizeof(int32_t) * std::max(1, S), "static motion"))) return st;
+    if ((st = cuda_check(cudaMemset(smflag, 0, sizeof(int32_t) * std::max(1, S)), "static motion"))) return st;
+    h_smot.assign(13 * (size_t)S, 0.0);
+    h_smflag.assign((size_t)S, 0);
+    smotion_pending = false;
     if ((st = cuda_check(cudaMemcpy(sc.scene_body_start, bstart.data(), sizeof(int32_t) * (nsc + 1), cudaMemcpyHostToDevice), "upload"))) return st;
     if ((st = cuda_check(cudaMemcpy(sc.scene_static_start, sstart.data(), sizeof(int32_t) * (nsc + 1), cudaMemcpyHostToDevice), "upload"))) return st;
     h_scene_body_start = bstart;
@@ -766,6 +772,11 @@ int Engine::step64() {
     launch_rhs64(sc, dt, cfg.sim_gravity, rhs, stream, cfg.moreau_implicit_gyroscopy);
     launch_drift64(sc, (1.0 - th) * dt, 1, stream);
     launches += 2;
+    if (smotion_pending) {
+        // Trajectory::update runs here, inside updateStateDependentTerms (dynamics_assembler.cpp:515-522)
+        launch_static_motion64(sc, smot, smflag, stream);
+        ++launches;
+    }
     if ((st = collide64())) return st;
     if (timing) cudaEventRecord(ev[1], stream);
     if ((st = setup64())) return st;
@@ -817,6 +828,12 @@ int Engine::step(int nsteps) {
     for (int k = 0; k < nsteps; ++k) {
         st = (cfg.gpu_precision == CDX_PRECISION_SPLIT) ? step_split() : step64();
         if (st) return st;
+        if (smotion_pending) {
+            // a prescribed motion holds for one step
+            cudaMemsetAsync(smflag, 0, sizeof(int32_t) * (size_t)std::max(1, sc.S), stream);
+            std::fill(h_smflag.begin(), h_smflag.end(), 0);
+            smotion_pending = false;
+        }
         if (out) {
             out_time += cfg.sim_dt;
             if (out->due(steps) && (st = output_frame())) return st;
@@ -906,6 +923,66 @@ static void* device_view(const void* p) {
         return nullptr;
     }
     return (at.type == cudaMemoryTypeHost && at.devicePointer) ? at.devicePointer : nullptr;
+}
+
+// Trajectory::update (trajectory.cpp:69-120) evaluates the statics' position and velocity callbacks
+// on the host; their results enter here for the coming step and are applied where the reference
+// applies them, after the first drift and before contact detection. A halfspace's plane stays as
+// built (CollisionCoal::applyTransforms gives halfspaces no transform, collision_coal.cpp:386-391):
+// its motion enters the contacts through its velocity.
+int Engine::set_static_motion(int32_t count, const int32_t* idx, const double* pos, const double* quat,
+                              const double* vel, const double* omega) {
+    if (!loaded) return fail(CDX_ERR_STATE, "no scene loaded");
+    if (count < 0 || (count > 0 && !idx)) return fail(CDX_ERR_ARG, "static indices missing");
+    const int f = (pos ? 1 : 0) | (quat ? 2 : 0) | (vel ? 4 : 0) | (omega ? 8 : 0);
+    for (int32_t c = 0; c < count; ++c) {
+        const int s = idx[c];
+        if (s < 0 || s >= sc.S) return fail(CDX_ERR_ARG, "static index out of range");
+        double* m = &h_smot[13 * (size_t)s];
+        for (int k = 0; k < 3; ++k) {
+            if (pos) m[k] = pos[3 * (size_t)c + k];
+            if (vel) m[7 + k] = vel[3 * (size_t)c + k];
+            if (omega) m[10 + k] = omega[3 * (size_t)c + k];
+        }
+        if (quat)
+            for (int k = 0; k < 4; ++k) m[3 + k] = quat[4 * (size_t)c + k];
+        for (int k = 0; k < 13; ++k)
+            if (!std::isfinite(m[k]) && (f & (k < 3 ? 1 : k < 7 ? 2 : k < 10 ? 4 : 8)))
+                return fail(CDX_ERR_ARG, "static motion must be finite");
+        h_smflag[s] |= f;
+    }
+    if (count == 0 || sc.S == 0) return CDX_OK;
+    int st;
+    if ((st = cuda_check(cudaMemcpyAsync(smot, h_smot.data(), sizeof(double) * h_smot.size(), cudaMemcpyHostToDevice,
+                                         stream), "static motion")))
+        return st;
+    if ((st = cuda_check(cudaMemcpyAsync(smflag, h_smflag.data(), sizeof(int32_t) * h_smflag.size(),
+                                         cudaMemcpyHostToDevice, stream), "static motion")))
+        return st;
+    smotion_pending = true;
+    return cuda_check(cudaStreamSynchronize(stream), "static motion");
+}
+
+int Engine::get_static_state(double* pos, double* quat, double* vel, double* omega) {
+    if (!loaded) return fail(CDX_ERR_STATE, "no scene loaded");
+    const size_t S = (size_t)sc.S;
+    if (S == 0) return CDX_OK;
+    std::vector<double> St((size_t)SF_COUNT * S);
+    int st;
+    if ((st = cuda_check(cudaMemcpyAsync(St.data(), sc.St, sizeof(double) * St.size(), cudaMemcpyDeviceToHost, stream),
+                         "download statics")))
+        return st;
+    if ((st = cuda_check(cudaStreamSynchronize(stream), "download statics"))) return st;
+    for (size_t s = 0; s < S; ++s) {
+        for (int k = 0; k < 3; ++k) {
+            if (pos) pos[3 * s + k] = St[(SF_PX + k) * S + s];
+            if (vel) vel[3 * s + k] = St[(SF_VX + k) * S + s];
+            if (omega) omega[3 * s + k] = St[(SF_WX + k) * S + s];
+        }
+        if (quat)
+            for (int k = 0; k < 4; ++k) quat[4 * s + k] = St[(SF_QX + k) * S + s];
+    }
+    return CDX_OK;
 }
 
 int Engine::get_state(double* pos, double* quat, double* vel, double* omega) {

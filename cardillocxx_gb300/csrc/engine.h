@@ -130,6 +130,16 @@ struct Engine {
     int solve_pgs();
     void split_config_changed();
     int scene_solve_info(float* alpha, int32_t* sweeps, int32_t n);
+    // prescribed static motion for the coming step (Trajectory::update); device record and flags,
+    // and their host copy until a step consumes them
+    double* smot = nullptr;
+    int32_t* smflag = nullptr;
+    std::vector<double> h_smot;
+    std::vector<int32_t> h_smflag;
+    bool smotion_pending = false;
+    int set_static_motion(int32_t count, const int32_t* idx, const double* pos, const double* quat,
+                          const double* vel, const double* omega);
+    int get_static_state(double* pos, double* quat, double* vel, double* omega);
     int load_scene(const cdx_scene& s);
     int ensure_tmp(int64_t n);
     int ensure_contacts(int64_t need);

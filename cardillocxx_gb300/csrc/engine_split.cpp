@@ -539,7 +539,8 @@ int Engine::step_split() {
     }
 
     if (timing) cudaEventRecord(ev[0], stream);
-    launch_s_prep(sc, sb, dt, cfg.sim_gravity, (1.0 - th) * dt, stream, cfg.moreau_implicit_gyroscopy);
+    launch_s_prep(sc, sb, dt, cfg.sim_gravity, (1.0 - th) * dt, stream, cfg.moreau_implicit_gyroscopy,
+                  sc.S > 0 ? smot : nullptr, sc.S > 0 ? smflag : nullptr);
     launch_cell_keys(sc, grid, cell_key_in, cell_val_in, stream, 1);
     if ((st = cuda_check(sort_pairs(tmp, tmp_bytes, cell_key_in, cell_key_out, cell_val_in, cell_val_out, N,
                                     grid.key_bits, stream), "sort cells"))) return st;

@@ -248,6 +248,43 @@ __global__ void k_drift64(Scene sc, double h, int compute_R, int32_t* nonfinite)
     }
 }
 
+// Prescribed static motion (Trajectory::update, trajectory.cpp:69-120, run by
+// DynamicsAssembler::updateStateDependentTerms after the first drift): per static a record
+// (position 3, quaternion 4, velocity 3, angular velocity 3) and flags (1 position, 2 orientation,
+// 4 velocity, 8 angular velocity) set by the host for the coming step. The rotation matrix follows
+// a new orientation.
+__device__ __forceinline__ void apply_static_motion(const double* m, int f, double* x, double* q, double* v,
+                                                    double* w) {
+    if (f & 1)
+        for (int k = 0; k < 3; ++k) x[k] = m[k];
+    if (f & 2)
+        for (int k = 0; k < 4; ++k) q[k] = m[3 + k];
+    if (f & 4)
+        for (int k = 0; k < 3; ++k) v[k] = m[7 + k];
+    if (f & 8)
+        for (int k = 0; k < 3; ++k) w[k] = m[10 + k];
+}
+__global__ void k_static_motion64(Scene sc, const double* mot, const int32_t* flag) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= sc.S) return;
+    const int f = flag[s];
+    if (!f) return;
+    double x[3] = {sc.sf(SF_PX)[s], sc.sf(SF_PY)[s], sc.sf(SF_PZ)[s]};
+    double q[4] = {sc.sf(SF_QX)[s], sc.sf(SF_QY)[s], sc.sf(SF_QZ)[s], sc.sf(SF_QW)[s]};
+    double v[3] = {sc.sf(SF_VX)[s], sc.sf(SF_VY)[s], sc.sf(SF_VZ)[s]};
+    double w[3] = {sc.sf(SF_WX)[s], sc.sf(SF_WY)[s], sc.sf(SF_WZ)[s]};
+    apply_static_motion(mot + 13 * (size_t)s, f, x, q, v, w);
+    for (int k = 0; k < 3; ++k) {
+        sc.sf(SF_PX + k)[s] = x[k];
+        sc.sf(SF_VX + k)[s] = v[k];
+        sc.sf(SF_WX + k)[s] = w[k];
+    }
+    for (int k = 0; k < 4; ++k) sc.sf(SF_QX + k)[s] = q[k];
+    double R[9];
+    rotmat(q, R);
+    for (int k = 0; k < 9; ++k) sc.sf(SF_R0 + k)[s] = R[k];
+}
+
 // flags laid out per scene as [static slot l][sphere within scene], so an exclusive scan yields
 // positions in (static id, sphere id) order
 __global__ void k_static_flags64(Scene sc, double margin, int32_t* flags) {
@@ -1370,6 +1407,9 @@ void launch_rhs64(const Scene& sc, double dt, const double* g, double* rhs, cuda
 void launch_drift64(const Scene& sc, double h, int compute_R, cudaStream_t s, int32_t* nonfinite) {
     if (sc.N + sc.S == 0) return;
     k_drift64<<<nblk(sc.N + sc.S), NT, 0, s>>>(sc, h, compute_R, nonfinite);
+}
+void launch_static_motion64(const Scene& sc, const double* mot, const int32_t* flag, cudaStream_t s) {
+    if (sc.S > 0 && mot && flag) k_static_motion64<<<nblk(sc.S), NT, 0, s>>>(sc, mot, flag);
 }
 void launch_static_flags64(const Scene& sc, double margin, int32_t* flags, cudaStream_t s) {
     if (sc.N == 0) return;

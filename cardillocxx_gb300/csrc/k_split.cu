@@ -114,7 +114,7 @@ __device__ __forceinline__ void drift_fast(double* x, double* q, const double* v
 
 // ------------------------------------------------------------------ per-body preparation (FP64)
 __global__ void k_s_prep(Scene sc, SplitBuf sb, double dt, double g0, double g1, double g2, double h1,
-                         int implicit_gyro) {
+                         int implicit_gyro, const double* smot, const int32_t* smflag) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < sc.N) {
         const int N = sc.N;
@@ -169,9 +169,26 @@ __global__ void k_s_prep(Scene sc, SplitBuf sb, double dt, double g0, double g1,
         const int s = i - sc.N;
         double x[3] = {sc.sf(SF_PX)[s], sc.sf(SF_PY)[s], sc.sf(SF_PZ)[s]};
         double q[4] = {sc.sf(SF_QX)[s], sc.sf(SF_QY)[s], sc.sf(SF_QZ)[s], sc.sf(SF_QW)[s]};
-        const double v[3] = {sc.sf(SF_VX)[s], sc.sf(SF_VY)[s], sc.sf(SF_VZ)[s]};
-        const double w[3] = {sc.sf(SF_WX)[s], sc.sf(SF_WY)[s], sc.sf(SF_WZ)[s]};
+        double v[3] = {sc.sf(SF_VX)[s], sc.sf(SF_VY)[s], sc.sf(SF_VZ)[s]};
+        double w[3] = {sc.sf(SF_WX)[s], sc.sf(SF_WY)[s], sc.sf(SF_WZ)[s]};
         drift_fast(x, q, v, w, h1);
+        // prescribed motion (Trajectory::update, after the first drift): pose and twist as given
+        const int f = smflag ? smflag[s] : 0;
+        if (f) {
+            const double* m = smot + 13 * (size_t)s;
+            if (f & 1)
+                for (int k = 0; k < 3; ++k) x[k] = m[k];
+            if (f & 2)
+                for (int k = 0; k < 4; ++k) q[k] = m[3 + k];
+            if (f & 4)
+                for (int k = 0; k < 3; ++k) v[k] = m[7 + k];
+            if (f & 8)
+                for (int k = 0; k < 3; ++k) w[k] = m[10 + k];
+            for (int k = 0; k < 3; ++k) {
+                sc.sf(SF_VX + k)[s] = v[k];
+                sc.sf(SF_WX + k)[s] = w[k];
+            }
+        }
         sc.sf(SF_PX)[s] = x[0]; sc.sf(SF_PY)[s] = x[1]; sc.sf(SF_PZ)[s] = x[2];
         sc.sf(SF_QX)[s] = q[0]; sc.sf(SF_QY)[s] = q[1]; sc.sf(SF_QZ)[s] = q[2]; sc.sf(SF_QW)[s] = q[3];
         double R[9];
@@ -2104,9 +2121,9 @@ int launch_s_solve_coop_loop(const SplitBuf& sb, int gen, float alpha, int v, co
 }
 
 void launch_s_prep(const Scene& sc, const SplitBuf& sb, double dt, const double* g, double h1, cudaStream_t s,
-                   int implicit_gyro) {
+                   int implicit_gyro, const double* smot, const int32_t* smflag) {
     if (sc.N + sc.S == 0) return;
-    k_s_prep<<<nblk(sc.N + sc.S), NT, 0, s>>>(sc, sb, dt, g[0], g[1], g[2], h1, implicit_gyro);
+    k_s_prep<<<nblk(sc.N + sc.S), NT, 0, s>>>(sc, sb, dt, g[0], g[1], g[2], h1, implicit_gyro, smot, smflag);
 }
 void launch_s_static_flags(const Scene& sc, const SplitBuf& sb, float margin, int32_t* flags, cudaStream_t s) {
     if (sc.N == 0) return;

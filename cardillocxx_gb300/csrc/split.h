@@ -170,8 +170,9 @@ int launch_s_solve_coop(const SplitBuf& sb, int gen, float alpha, int v, const C
 int launch_s_solve_coop_loop(const SplitBuf& sb, int gen, float alpha, int v, const CoopPlan& p, int max_iter,
                              float tol, int max_sweeps, int check_every, int loop, const CoopLoopArgs& la,
                              unsigned long long wait_ns, cudaStream_t s);
+// smot/smflag (optional): prescribed static motion applied after the statics' first drift
 void launch_s_prep(const Scene& sc, const SplitBuf& sb, double dt, const double* g, double h1, cudaStream_t s,
-                   int implicit_gyro = 0);
+                   int implicit_gyro = 0, const double* smot = nullptr, const int32_t* smflag = nullptr);
 void launch_s_static_flags(const Scene& sc, const SplitBuf& sb, float margin, int32_t* flags, cudaStream_t s);
 // cell_body / cell_key: the bodies and their cell keys sorted by cell
 void launch_s_pair_count(const Scene& sc, const Grid& g, const SplitBuf& sb, const uint32_t* cell_body,

@@ -130,6 +130,7 @@ class PhysicsEngine:
         s, keep = scene_struct(scene)
         self._check(self.L.cdx_load_scene(self.h, C.byref(s)))
         self.N = s.num_bodies
+        self._nstatics = s.num_statics
         return self
 
     def step(self, n: int = 1):
@@ -181,6 +182,28 @@ class PhysicsEngine:
         assert ib.shape[0] == n and pt.shape[0] == n and lam.shape[0] == n
         self._check(self.L.cdx_set_contacts(self.h, n, ip(ia), ip(ib), dp(pt), dp(lam)))
         return self
+
+    def set_static_motion(self, statics, pos=None, quat=None, vel=None, omega=None):
+        """Prescribed pose/twist of the listed statics for the next step (what Trajectory::update
+        sets from a static's callbacks); None leaves that part as it is."""
+        idx = np.ascontiguousarray(np.atleast_1d(statics), np.int32)
+        n = idx.shape[0]
+
+        def arr(a, w):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, np.float64).reshape(n, w)
+            return a
+        p, q, v, w = arr(pos, 3), arr(quat, 4), arr(vel, 3), arr(omega, 3)
+        self._check(self.L.cdx_set_static_motion(self.h, n, ip(idx), *[None if a is None else dp(a) for a in (p, q, v, w)]))
+        return self
+
+    def static_state(self) -> dict:
+        s = self._nstatics
+        out = {"pos": np.empty((s, 3)), "quat": np.empty((s, 4)), "vel": np.empty((s, 3)), "omega": np.empty((s, 3))}
+        self._check(self.L.cdx_get_static_state(self.h, dp(out["pos"]), dp(out["quat"]), dp(out["vel"]),
+                                                dp(out["omega"])))
+        return out
 
     def scene_solve(self, nscenes: int) -> dict:
         """Batched scenes (per-scene solve): each scene's alpha and its sweeps in its last solve."""

@@ -197,6 +197,19 @@ int cdx_get_contacts(cdx_ctx* ctx, int32_t* id_a, int32_t* id_b, double* point, 
  * cdx_get_contacts returns this memory with zero normals. */
 int cdx_set_contacts(cdx_ctx* ctx, int32_t count, const int32_t* id_a, const int32_t* id_b, const double* point,
                      const double* lambda);
+/* Prescribed motion of statics for the next step: what Trajectory::update (trajectory.cpp:69-120)
+ * sets from a static's position and velocity callbacks, which run on the host. For each listed
+ * static the given pose (position, unit quaternion x,y,z,w) and twist (world-frame velocity,
+ * body-frame angular velocity) replace its own after the first drift and before contact detection,
+ * where updateStateDependentTerms runs the trajectories (dynamics_assembler.cpp:515-522); the
+ * second drift then moves it by the new twist, and the twist stays until changed. Any of pos, quat,
+ * vel, omega may be NULL (left as they are). As in the reference a halfspace's plane stays where
+ * it was built (CollisionCoal::applyTransforms, collision_coal.cpp:386-391): its motion reaches the
+ * contacts through its velocity. Calls before one step accumulate; the step consumes them. */
+int cdx_set_static_motion(cdx_ctx* ctx, int32_t count, const int32_t* statics, const double* pos,
+                          const double* quat, const double* vel, const double* omega);
+/* the statics' current pose and twist (arrays of 3S / 4S / 3S / 3S, any may be NULL) */
+int cdx_get_static_state(cdx_ctx* ctx, double* pos, double* quat, double* vel, double* omega);
 /* Batched scenes (split form, per-scene solve): each scene's pj.alpha (as gpu.tune_alpha chose it;
  * pj.alpha without it) and the sweeps each scene took in its last solve (either pointer may be
  * NULL; n scenes at most). No reference counterpart: the reference runs one alpha for every

@@ -142,6 +142,9 @@ struct Engine {
     or_stats stats{};
     double rmax = 0;
     int status = 0;  // 4 once a condensed solve diverged
+    // prescribed static motion of the coming step (Trajectory::update): 13 values a static and flags
+    std::vector<double> smot;
+    std::vector<int32_t> smflag;
 };
 
 // Sphere mass matrix, src/physics/assembly/dynamics_assembler.cpp:41-62 (rebuildMass_) with
@@ -1470,6 +1473,23 @@ void step_once(Engine& E) {
 #pragma omp parallel for schedule(static) if (omp_all)
     for (int i = 0; i < N; ++i) rotmat(&E.q[4 * (size_t)i], &E.R[9 * (size_t)i]);
     for (int s = 0; s < S; ++s) rotmat(&E.sq[4 * s], &E.sR[9 * s]);
+    // updateStateDependentTerms begins with DerivedEntitySync::updateEntities, which runs
+    // Trajectory::update (dynamics_assembler.cpp:515-522, trajectory.cpp:69-120): the statics'
+    // prescribed pose and twist, evaluated by the caller, replace their own
+    for (int s = 0; s < S; ++s) {
+        const int f = E.smflag.empty() ? 0 : E.smflag[s];
+        if (!f) continue;
+        const double* m = &E.smot[13 * (size_t)s];
+        for (int k = 0; k < 3; ++k) {
+            if (f & 1) E.spos[3 * s + k] = m[k];
+            if (f & 4) E.sv[3 * s + k] = m[7 + k];
+            if (f & 8) E.sw[3 * s + k] = m[10 + k];
+        }
+        if (f & 2)
+            for (int k = 0; k < 4; ++k) E.sq[4 * s + k] = m[3 + k];
+        rotmat(&E.sq[4 * s], &E.sR[9 * s]);
+        E.smflag[s] = 0;
+    }
 
     // updateStateDependentTerms: collision + W
     std::vector<Contact> C;
@@ -1630,6 +1650,42 @@ void* or_create(const or_config* cfg, const or_scene* sc) {
 }
 
 void or_destroy(void* h) { delete (Engine*)h; }
+
+void or_set_static_motion(void* h, int32_t count, const int32_t* statics, const double* pos, const double* quat,
+                          const double* vel, const double* omega) {
+    Engine& E = *(Engine*)h;
+    if (E.smflag.size() != (size_t)E.S) {
+        E.smflag.assign(E.S, 0);
+        E.smot.assign(13 * (size_t)E.S, 0.0);
+    }
+    const int f = (pos ? 1 : 0) | (quat ? 2 : 0) | (vel ? 4 : 0) | (omega ? 8 : 0);
+    for (int32_t c = 0; c < count; ++c) {
+        const int s = statics[c];
+        if (s < 0 || s >= E.S) continue;
+        double* m = &E.smot[13 * (size_t)s];
+        for (int k = 0; k < 3; ++k) {
+            if (pos) m[k] = pos[3 * (size_t)c + k];
+            if (vel) m[7 + k] = vel[3 * (size_t)c + k];
+            if (omega) m[10 + k] = omega[3 * (size_t)c + k];
+        }
+        if (quat)
+            for (int k = 0; k < 4; ++k) m[3 + k] = quat[4 * (size_t)c + k];
+        E.smflag[s] |= f;
+    }
+}
+
+void or_get_static_state(void* h, double* pos, double* quat, double* vel, double* omega) {
+    const Engine& E = *(const Engine*)h;
+    for (int s = 0; s < E.S; ++s) {
+        for (int k = 0; k < 3; ++k) {
+            if (pos) pos[3 * s + k] = E.spos[3 * s + k];
+            if (vel) vel[3 * s + k] = E.sv[3 * s + k];
+            if (omega) omega[3 * s + k] = E.sw[3 * s + k];
+        }
+        if (quat)
+            for (int k = 0; k < 4; ++k) quat[4 * s + k] = E.sq[4 * s + k];
+    }
+}
 
 int or_step(void* h, int32_t nsteps) {
     Engine* E = (Engine*)h;

@@ -92,6 +92,10 @@ typedef struct or_stats {
 
 void* or_create(const or_config* cfg, const or_scene* scene);
 void or_destroy(void* h);
+/* prescribed static motion for the next step (Trajectory::update); NULL arrays leave that part */
+void or_set_static_motion(void* h, int32_t count, const int32_t* statics, const double* pos, const double* quat,
+                          const double* vel, const double* omega);
+void or_get_static_state(void* h, double* pos, double* quat, double* vel, double* omega);
 int or_step(void* h, int32_t nsteps);
 void or_get_state(void* h, double* pos, double* quat, double* vel, double* omega);
 void or_get_stats(void* h, or_stats* out);

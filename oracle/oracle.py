@@ -128,6 +128,8 @@ def lib():
             L.or_get_contacts.argtypes = [C.c_void_p, _PI, _PI, _P, _P, _P]
             L.or_set_trace.argtypes = [C.c_void_p, C.c_int32]
             L.or_set_contacts.argtypes = [C.c_void_p, C.c_int32, _PI, _PI, _P, _P]
+            L.or_set_static_motion.argtypes = [C.c_void_p, C.c_int32, _PI, _P, _P, _P, _P]
+            L.or_get_static_state.argtypes = [C.c_void_p, _P, _P, _P, _P]
             L.or_get_trace.restype = C.c_int32
             L.or_get_trace.argtypes = [C.c_void_p, _P, C.c_int64]
             L.or_pj_solve_csr.restype = C.c_int32
@@ -258,6 +260,22 @@ class Oracle:
         lam = np.ascontiguousarray(contacts["lambda"], np.float64).reshape(-1, 3)
         self.L.or_set_contacts(self.h, int(ia.shape[0]), _ip(ia), _ip(ib), _dp(pt), _dp(lam))
         return self
+
+    def set_static_motion(self, statics, pos=None, quat=None, vel=None, omega=None):
+        """Prescribed pose/twist of the listed statics for the next step (Trajectory::update)."""
+        idx = np.ascontiguousarray(np.atleast_1d(statics), np.int32)
+        n = idx.shape[0]
+        arrs = [None if a is None else np.ascontiguousarray(a, np.float64).reshape(n, w)
+                for a, w in ((pos, 3), (quat, 4), (vel, 3), (omega, 3))]
+        self._motion = arrs
+        self.L.or_set_static_motion(self.h, n, _ip(idx), *[None if a is None else _dp(a) for a in arrs])
+        return self
+
+    def static_state(self):
+        S = int(self._keep["static_kind"].shape[0])
+        out = {"pos": np.empty((S, 3)), "quat": np.empty((S, 4)), "vel": np.empty((S, 3)), "omega": np.empty((S, 3))}
+        self.L.or_get_static_state(self.h, _dp(out["pos"]), _dp(out["quat"]), _dp(out["vel"]), _dp(out["omega"]))
+        return out
 
     def set_trace(self, on: bool = True):
         self.L.or_set_trace(self.h, int(on))

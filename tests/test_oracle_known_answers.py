@@ -351,3 +351,34 @@ def test_pgs_converges_to_the_projected_jacobi_solution(oracle_mod):
     # "Projected Gauss-Seidel diverged" (projected_gauss_seidel.cpp:144-147)
     with pytest.raises(RuntimeError):
         oracle_mod.Oracle(sc, dict(base, **{"solver.type": "pgs"})).step(1)
+
+
+# ---- prescribed static motion (Trajectory::update, trajectory.cpp:69-120) ----
+def test_prescribed_wall_velocity_moves_resting_sphere(oracle_mod):
+    # the ground's twist set for one step: its velocity enters the contact (its plane stays where it
+    # was built, collision_coal.cpp:386-391); a resting sphere leaves the step at the wall's normal
+    # velocity, and a tangential wall velocity drags it by kinetic friction, mu g h a step
+    r, mu = 0.05, 0.3
+    s = make_scene([{"pos": (0.0, 0.0, r), "radius": r, "mu": mu}], [dict(GROUND, mu=mu)])
+    o = oracle_mod.Oracle(s, cfg())
+    o.set_static_motion([0], vel=[(0.0, 0.0, 0.1)])
+    o.step(1)
+    np.testing.assert_allclose(o.state()["vel"][0, 2], 0.1, rtol=1e-9)
+    st = o.static_state()
+    np.testing.assert_allclose(st["vel"][0], [0.0, 0.0, 0.1])
+    np.testing.assert_allclose(st["pos"][0], [0.0, 0.0, 0.5 * H * 0.1], rtol=1e-12)
+    c = oracle_mod.Oracle(s, cfg())
+    c.set_static_motion([0], vel=[(1.0, 0.0, 0.0)])
+    c.step(1)
+    np.testing.assert_allclose(c.state()["vel"][0, 0], mu * G * H, rtol=1e-9)
+    # a prescribed pose: the drum moved down by 1 mm leaves a sphere that rested on its wall free
+    R = 0.3
+    d = make_scene([{"pos": (0.0, 0.0, -R + r), "radius": r}],
+                   [{"kind": "drum", "pos": (0, 0, 0), "dir": (0, 1, 0), "radius": R, "mu": 0.3}])
+    od = oracle_mod.Oracle(d, cfg())
+    od.step(1)
+    assert od.stats()["num_contacts"] == 1
+    od.set_static_motion([0], pos=[(0.0, 0.0, -1e-3)], quat=[(0.0, 0.0, 0.0, 1.0)])
+    od.step(1)
+    assert od.stats()["num_contacts"] == 0
+    np.testing.assert_allclose(od.static_state()["pos"][0], [0.0, 0.0, -1e-3])
