@@ -26,6 +26,7 @@
 #include "physics/integration/integration_base.hpp"
 #include "physics/solver/solver_base.hpp"
 #include "physics/solver/warmstart.hpp"
+#include "physics/synchronization/trajectory.hpp"
 #include "physics/world.hpp"
 
 namespace cardillo::solver {
@@ -110,6 +111,11 @@ namespace cardillo::integration {
 //    state back into C_Position3, C_Orientation (setValue keeps the rotation in sync),
 //    C_LinearVelocity3 and C_AngularVelocity3 (body frame). The warm-start memory stays in the
 //    context across steps.
+//  - Halfspaces driven by a trajectory (C_StaticTrajectory): each step runs Trajectory::update
+//    (trajectory.cpp:69-120; the reference runs it inside updateStateDependentTerms, after the first
+//    drift, and what it computes does not depend on that drift) and hands the poses and twists it
+//    set to cdx_set_static_motion, which applies them at the same point of the step; afterwards
+//    their pose and twist come back from the context (cdx_get_static_state).
 //  - Other dynamic shapes (boxes, meshes, capsules, cones, cylinders), dynamic planes, point
 //    masses without C_RB_Sphere, constraints and soft bodies are not on this path: step() throws
 //    std::runtime_error, as the reference's own components throw on what they cannot handle.
@@ -144,8 +150,10 @@ class GpuMoreauIntegrator : public IntegrationBase {
             m_quat[4 * i + 3] = q.w();
         }
         check(cdx_set_state(m_ctx, m_pos.data(), m_quat.data(), m_vel.data(), m_omega.data()));
+        if (!m_traj.empty()) upload_trajectories(dt);
         check(cdx_step(m_ctx, 1));
         check(cdx_get_state(m_ctx, m_pos.data(), m_quat.data(), m_vel.data(), m_omega.data()));
+        if (!m_traj.empty()) download_trajectories();
         for (size_t i = 0; i < n; ++i) {
             const entt::entity e = m_spheres[i];
             auto& x = reg.get<C_Position3>(e).value;
@@ -162,6 +170,55 @@ class GpuMoreauIntegrator : public IntegrationBase {
     }
 
    private:
+    // the poses (where a position callback exists) and twists Trajectory::update set, for this step
+    void upload_trajectories(real_t dt) {
+        physics::Trajectory::update(m_world, dt);
+        auto& reg = m_world.ecs();
+        std::vector<int32_t> with_pose, twist_only;
+        std::vector<double> pos, quat, vel, omega, vel2, omega2;
+        for (size_t t = 0; t < m_traj.size(); ++t) {
+            const entt::entity e = m_traj[t];
+            const auto& traj = reg.get<C_StaticTrajectory>(e);
+            const auto& v = reg.get<C_LinearVelocity3>(e).value;
+            const bool has_w = reg.all_of<C_AngularVelocity3>(e);
+            const bool posed = traj.positionFunc.has_value();
+            (posed ? with_pose : twist_only).push_back(m_traj_index[t]);
+            auto& vv = posed ? vel : vel2;
+            auto& ww = posed ? omega : omega2;
+            for (int k = 0; k < 3; ++k) {
+                vv.push_back(v[k]);
+                ww.push_back(has_w ? reg.get<C_AngularVelocity3>(e).value[k] : 0.0);
+            }
+            if (posed) {
+                const auto& x = reg.get<C_Position3>(e).value;
+                const auto& q = reg.get<C_Orientation>(e).value;
+                for (int k = 0; k < 3; ++k) pos.push_back(x[k]);
+                quat.insert(quat.end(), {q.x(), q.y(), q.z(), q.w()});
+            }
+        }
+        if (!with_pose.empty())
+            check(cdx_set_static_motion(m_ctx, (int32_t)with_pose.size(), with_pose.data(), pos.data(), quat.data(),
+                                        vel.data(), omega.data()));
+        if (!twist_only.empty())
+            check(cdx_set_static_motion(m_ctx, (int32_t)twist_only.size(), twist_only.data(), nullptr, nullptr,
+                                        vel2.data(), omega2.data()));
+    }
+
+    // the trajectory statics' pose after the step's second drift, back into the ECS
+    void download_trajectories() {
+        auto& reg = m_world.ecs();
+        const size_t ns = m_nstatics;
+        std::vector<double> pos(3 * ns), quat(4 * ns);
+        check(cdx_get_static_state(m_ctx, pos.data(), quat.data(), nullptr, nullptr));
+        for (size_t t = 0; t < m_traj.size(); ++t) {
+            const entt::entity e = m_traj[t];
+            const size_t s = (size_t)m_traj_index[t];
+            auto& x = reg.get<C_Position3>(e).value;
+            for (int k = 0; k < 3; ++k) x[k] = pos[3 * s + k];
+            reg.get<C_Orientation>(e).setValue(Quaternion4r(quat[4 * s + 3], quat[4 * s + 0], quat[4 * s + 1], quat[4 * s + 2]));
+        }
+    }
+
     void check(int st) const {
         if (st != CDX_OK)
             throw std::runtime_error(std::string("GpuMoreauIntegrator: ") + (m_ctx ? cdx_last_error(m_ctx) : "cdx"));
@@ -217,6 +274,14 @@ class GpuMoreauIntegrator : public IntegrationBase {
         }
         const size_t n = m_spheres.size(), ns = planes.size();
         (void)dynamic;
+        m_traj.clear();
+        m_traj_index.clear();
+        m_nstatics = ns;
+        for (size_t s = 0; s < ns; ++s)
+            if (reg.all_of<C_StaticTrajectory>(planes[s])) {
+                m_traj.push_back(planes[s]);
+                m_traj_index.push_back((int32_t)s);
+            }
         std::vector<double> rad(n), mass(n), inertia(n), mu(n), rn(n), rt(n);
         m_pos.assign(3 * n, 0.0);
         m_quat.assign(4 * n, 0.0);
@@ -297,6 +362,9 @@ class GpuMoreauIntegrator : public IntegrationBase {
     real_t m_dt = 0;
     std::vector<entt::entity> m_spheres;
     std::vector<double> m_pos, m_quat, m_vel, m_omega;
+    std::vector<entt::entity> m_traj;    // statics driven by a trajectory
+    std::vector<int32_t> m_traj_index;   // their index among the context's statics
+    size_t m_nstatics = 0;
 };
 
 }  // namespace cardillo::integration

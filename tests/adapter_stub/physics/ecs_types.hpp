@@ -1,10 +1,13 @@
 // Stand-ins for the ECS pieces the integrator adapter uses: the component types of ecs_types.hpp
-// (C_Position3 ... C_InertiaDiag, lines 15-166), the Eigen types they hold (fixed-size vector,
+// (C_Position3 ... C_InertiaDiag and C_StaticTrajectory, lines 15-166), the Eigen types they hold (fixed-size vector,
 // quaternion with x()/y()/z()/w() and the (w, x, y, z) constructor, 3x3 rotation), and the EnTT
 // registry calls (view, get, all_of). Enough to compile the adapter syntax-only.
 #pragma once
 #include <cmath>
 #include <cstdint>
+#include <functional>
+#include <optional>
+#include <utility>
 #include <vector>
 
 #include "solver/solver_base.hpp"
@@ -76,4 +79,13 @@ struct C_Restitution {
     real_t tangential;
 };
 struct C_InertiaDiag { Vector3r I; };
+using TrajectoryPose = std::pair<Vector3r, Quaternion4r>;
+using TrajectoryTwist = std::pair<Vector3r, Vector3r>;
+struct C_StaticTrajectory {
+    std::optional<std::function<TrajectoryPose(real_t)>> positionFunc;
+    std::optional<std::function<TrajectoryTwist(real_t)>> velocityFunc;
+    real_t elapsed{(real_t)0};
+    bool initialized{false};
+    std::optional<TrajectoryPose> previousPosition;
+};
 }  // namespace cardillo
