@@ -92,6 +92,7 @@ class CdxScene(C.Structure):
         ("static_mu", _P), ("static_rest_n", _P), ("static_rest_t", _P),
         ("static_scene", _PI),
         ("num_scenes", C.c_int32),
+        ("static_half_length", _P),
     ]
 
 

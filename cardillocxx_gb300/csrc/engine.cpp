@@ -178,9 +178,14 @@ int Engine::load_scene(const cdx_scene& s) {
         if (!(s.radius[i] > 0) || !(s.mass[i] > 0) || !(s.inertia[i] > 0))
             return fail(CDX_ERR_ARG, "bodies need positive radius, mass and inertia");
     }
-    for (int i = 0; i < S; ++i)
-        if (s.static_kind[i] != CDX_STATIC_HALFSPACE && s.static_kind[i] != CDX_STATIC_DRUM)
+    for (int i = 0; i < S; ++i) {
+        const int k = s.static_kind[i];
+        if (k != CDX_STATIC_HALFSPACE && k != CDX_STATIC_DRUM && k != CDX_STATIC_CYLINDER)
             return fail(CDX_ERR_ARG, "unknown static kind");
+        if (k == CDX_STATIC_CYLINDER &&
+            (!s.static_radius || !s.static_half_length || !(s.static_radius[i] > 0) || !(s.static_half_length[i] > 0)))
+            return fail(CDX_ERR_ARG, "a cylinder needs a positive radius and half length");
+    }
 
     // host staging: body fields (field-major)
     std::vector<double> B((size_t)BF_COUNT * N, 0.0);
@@ -226,6 +231,7 @@ int Engine::load_scene(const cdx_scene& s) {
         const double* p = &s.static_pos[3 * (size_t)i];
         sf(SF_D, i) = (un[0] * p[0] + un[1] * p[1]) + un[2] * p[2];
         sf(SF_RAD, i) = s.static_radius ? s.static_radius[i] : 0.0;
+        sf(SF_HL, i) = s.static_half_length ? s.static_half_length[i] : 0.0;
         sf(SF_MU, i) = s.static_mu[i];
         sf(SF_RN, i) = s.static_rest_n[i];
         sf(SF_RT, i) = s.static_rest_t[i];
@@ -359,6 +365,8 @@ int Engine::load_scene(const cdx_scene& s) {
         oscene.smu.assign(s.static_mu, s.static_mu + S);
         oscene.srad.assign(S, 0.0);
         if (s.static_radius) oscene.srad.assign(s.static_radius, s.static_radius + S);
+        oscene.shl.assign(S, 0.0);
+        if (s.static_half_length) oscene.shl.assign(s.static_half_length, s.static_half_length + S);
     }
     if (out) {
         out->flush();

@@ -43,7 +43,75 @@ struct Geom {
     double p1[3], p2[3], nraw[3], xa[3];
 };
 
-// coal::Halfspace {x : n.x <= d} (shape 1) against a sphere (shape 2), or the inner wall of a drum.
+// Sphere against a solid cylinder (coal::Cylinder, collision_coal.cpp:307-310): the exact nearest
+// points in closed form. In the cylinder's frame (axial coordinate ax, radial part perp of length
+// rho): outside, the nearest point is on the side (|ax| <= h), a cap (rho <= R) or a rim; inside,
+// on the nearer of the side and the cap (the side on a tie). The normal points from the cylinder
+// to the sphere.
+__device__ __forceinline__ bool cylinder_geom(const double* xa, const double* u, double R, double h,
+                                              const double* xb, double rb, double margin, Geom& g) {
+    double rel[3], perp[3];
+    for (int k = 0; k < 3; ++k) rel[k] = xb[k] - xa[k];
+    const double ax = dot3(rel, u);
+    for (int k = 0; k < 3; ++k) perp[k] = rel[k] - ax * u[k];
+    const double rho = norm3(perp);
+    const double sg = ax < 0.0 ? -1.0 : 1.0;
+    const double aax = fabs(ax);
+    double e[3];
+    if (rho > 0.0) {
+        for (int k = 0; k < 3; ++k) e[k] = perp[k] / rho;
+    } else {
+        double t2[3];
+        tangent_frame(u, e, t2);
+    }
+    const bool out_side = rho > R, out_cap = aax > h;
+    int region;
+    double sd;
+    if (!out_side && !out_cap) {
+        const double dside = R - rho, dcap = h - aax;
+        region = dside <= dcap ? 0 : 1;
+        sd = region == 0 ? -dside : -dcap;
+    } else if (!out_cap) {
+        region = 0;
+        sd = rho - R;
+    } else if (!out_side) {
+        region = 1;
+        sd = aax - h;
+    } else {
+        region = 2;
+        sd = 0.0;
+    }
+    double q[3], n[3];
+    if (region == 0) {
+        for (int k = 0; k < 3; ++k) {
+            q[k] = (xa[k] + ax * u[k]) + R * e[k];
+            n[k] = e[k];
+        }
+    } else if (region == 1) {
+        for (int k = 0; k < 3; ++k) {
+            q[k] = (xa[k] + (sg * h) * u[k]) + perp[k];
+            n[k] = sg * u[k];
+        }
+    } else {
+        double d[3];
+        for (int k = 0; k < 3; ++k) {
+            q[k] = (xa[k] + (sg * h) * u[k]) + R * e[k];
+            d[k] = xb[k] - q[k];
+        }
+        sd = norm3(d);
+        for (int k = 0; k < 3; ++k) n[k] = d[k] / sd;
+    }
+    if (!((sd - rb) <= margin)) return false;
+    for (int k = 0; k < 3; ++k) {
+        g.p1[k] = q[k];
+        g.p2[k] = xb[k] - rb * n[k];
+        g.nraw[k] = n[k];
+    }
+    return true;
+}
+
+// coal::Halfspace {x : n.x <= d} (shape 1) against a sphere (shape 2), a solid cylinder, or the
+// inner wall of a drum.
 __device__ __forceinline__ bool static_geom(const Scene& sc, int s, const double* xb, double rb, double margin,
                                             Geom& g) {
     const double u[3] = {sc.sf(SF_DX)[s], sc.sf(SF_DY)[s], sc.sf(SF_DZ)[s]};
@@ -62,6 +130,7 @@ __device__ __forceinline__ bool static_geom(const Scene& sc, int s, const double
         }
         return true;
     }
+    if (sc.static_kind[s] == 2) return cylinder_geom(g.xa, u, sc.sf(SF_RAD)[s], sc.sf(SF_HL)[s], xb, rb, margin, g);
     const double R = sc.sf(SF_RAD)[s];
     double rel[3];
 #pragma unroll

@@ -201,7 +201,9 @@ __global__ void k_s_prep(Scene sc, SplitBuf sb, double dt, double g0, double g1,
         const double u[3] = {sc.sf(SF_DX)[s], sc.sf(SF_DY)[s], sc.sf(SF_DZ)[s]};
         const double pl[3] = {x[0] - o[0], x[1] - o[1], x[2] - o[2]};
         const double dl = u[0] * pl[0] + u[1] * pl[1] + u[2] * pl[2];
-        sb.st_dir[s] = make_float4((float)u[0], (float)u[1], (float)u[2], (float)dl);
+        // .w: the halfspace offset n . x, or a cylinder's half length
+        sb.st_dir[s] = make_float4((float)u[0], (float)u[1], (float)u[2],
+                                   sc.static_kind[s] == 2 ? (float)sc.sf(SF_HL)[s] : (float)dl);
         sb.st_pt[s] = make_float4((float)pl[0], (float)pl[1], (float)pl[2], (float)sc.sf(SF_RAD)[s]);
         sb.st_v[s] = make_float4((float)v[0], (float)v[1], (float)v[2], (float)sc.static_kind[s]);
         sb.st_w[s] = make_float4((float)ww[0], (float)ww[1], (float)ww[2], (float)sc.sf(SF_MU)[s]);
@@ -232,6 +234,46 @@ __device__ __forceinline__ bool static_test32(const SplitBuf& sb, int s, float3 
     const float ax = dot(rel, u);
     const float3 perp = rel - ax * u;
     const float rho = sqrtf(dot(perp, perp));
+    if (sb.st_v[s].w == 2.f) {
+        // solid cylinder: the nearest point of the side, a cap or a rim (the FP64 method's
+        // cylinder_geom in FP32); n from the cylinder to the sphere, sd the centre's signed distance
+        const float R = pp.w, h = dd.w, sg = ax < 0.f ? -1.f : 1.f, aax = fabsf(ax);
+        float3 e;
+        if (rho > 0.f) {
+            e = __frcp_rn(rho) * perp;
+        } else {
+            float3 t2;
+            frame32(u, e, t2);
+        }
+        const bool out_side = rho > R, out_cap = aax > h;
+        float sd;
+        float3 n;
+        if (!out_side && !out_cap) {
+            const float dside = R - rho, dcap = h - aax;
+            if (dside <= dcap) {
+                n = e;
+                sd = -dside;
+            } else {
+                n = sg * u;
+                sd = -dcap;
+            }
+        } else if (!out_cap) {
+            n = e;
+            sd = rho - R;
+        } else if (!out_side) {
+            n = sg * u;
+            sd = aax - h;
+        } else {
+            const float3 d = rel - ((sg * h) * u + R * e);
+            sd = sqrtf(dot(d, d));
+            n = __frcp_rn(sd) * d;
+        }
+        if (!((sd - r) <= margin)) return false;
+        g.n = n;
+        g.rhoB = -0.5f * (sd + r);
+        g.sep = sd;
+        return true;
+    }
     if (!(((pp.w - rho) - r) <= margin)) return false;
     g.n = rho > 0.f ? (-__frcp_rn(rho)) * perp : make_float3(0.f, 0.f, 1.f);
     g.rhoB = -0.5f * ((pp.w - rho) + r);
@@ -1627,6 +1669,7 @@ __global__ void k_s_reset(SplitBuf sb) {
 
 // ------------------------------------------------------------------ FP64 finalisation
 // FP64 contact geometry recomputed from FP64 positions (the same formulas as the plain method)
+__device__ __forceinline__ void frame64(const double* n, double* t1, double* t2);
 __device__ __forceinline__ void geom64(const Scene& sc, int a, int b, double* n, double& rhoA, double& rhoB) {
     const double xb[3] = {sc.bf(BF_PX)[b], sc.bf(BF_PY)[b], sc.bf(BF_PZ)[b]};
     const double rb = sc.bf(BF_RAD)[b];
@@ -1659,6 +1702,38 @@ __device__ __forceinline__ void geom64(const Scene& sc, int a, int b, double* n,
     const double ax = rel[0] * u[0] + rel[1] * u[1] + rel[2] * u[2];
     const double perp[3] = {rel[0] - ax * u[0], rel[1] - ax * u[1], rel[2] - ax * u[2]};
     const double rho2 = perp[0] * perp[0] + perp[1] * perp[1] + perp[2] * perp[2];
+    if (sc.static_kind[s] == 2) {
+        // solid cylinder: side, cap or rim, as in the narrow phase
+        const double R = sc.sf(SF_RAD)[s], h = sc.sf(SF_HL)[s];
+        const double sg = ax < 0.0 ? -1.0 : 1.0, aax = fabs(ax);
+        const double rho = rho2 > 0.0 ? rho2 * rsqrt_nr(rho2) : 0.0;
+        double e[3] = {0.0, 0.0, 0.0};
+        if (rho2 > 0.0) {
+            const double inv = rsqrt_nr(rho2);
+            for (int k = 0; k < 3; ++k) e[k] = perp[k] * inv;
+        } else {
+            double t2[3];
+            frame64(u, e, t2);
+        }
+        const bool out_side = rho > R, out_cap = aax > h;
+        double sd;
+        if ((!out_side && !out_cap && (R - rho) <= (h - aax)) || (out_side && !out_cap)) {
+            for (int k = 0; k < 3; ++k) n[k] = e[k];
+            sd = rho - R;
+        } else if (!out_side) {
+            for (int k = 0; k < 3; ++k) n[k] = sg * u[k];
+            sd = aax - h;
+        } else {
+            double d[3];
+            for (int k = 0; k < 3; ++k) d[k] = rel[k] - ((sg * h) * u[k] + R * e[k]);
+            const double dd2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+            const double inv = rsqrt_nr(dd2);
+            sd = dd2 * inv;
+            for (int k = 0; k < 3; ++k) n[k] = d[k] * inv;
+        }
+        rhoB = -0.5 * (sd + rb);
+        return;
+    }
     double rho = 0.0;
     if (rho2 > 0.0) {
         const double inv = rsqrt_nr(rho2);

@@ -292,7 +292,11 @@ void Output::frame(OutputFrame f) {
                     vel.insert(vel.end(), {0.f, 0.f, 0.f});
                     ids.push_back(s);
                 };
-                if (sc.skind[s] == CDX_STATIC_DRUM) {
+                if (sc.skind[s] == CDX_STATIC_CYLINDER) {
+                    lo = -sc.shl[s];
+                    hi = sc.shl[s];
+                }
+                if (sc.skind[s] == CDX_STATIC_DRUM || sc.skind[s] == CDX_STATIC_CYLINDER) {
                     const int seg = 64;
                     const double R = sc.srad[s];
                     for (int j = 0; j < seg; ++j) {
@@ -414,10 +418,17 @@ void Output::frame(OutputFrame f) {
                         if (dl > 0) for (int k = 0; k < 3; ++k) d[k] /= dl;
                         const double r[3] = {xb[0] - p[0], xb[1] - p[1], xb[2] - p[2]};
                         const double ax = dot3(r, d);
-                        if (sc.skind[a] == CDX_STATIC_DRUM)
+                        if (sc.skind[a] == CDX_STATIC_DRUM) {
                             depth = std::sqrt(std::max(0.0, dot3(r, r) - ax * ax)) + rb - sc.srad[a];
-                        else
+                        } else if (sc.skind[a] == CDX_STATIC_CYLINDER) {
+                            // distance of the centre to the solid cylinder (outside; inside counts 0)
+                            const double rho = std::sqrt(std::max(0.0, dot3(r, r) - ax * ax));
+                            const double dr = std::max(0.0, rho - sc.srad[a]);
+                            const double dz = std::max(0.0, std::fabs(ax) - sc.shl[a]);
+                            depth = rb - std::sqrt(dr * dr + dz * dz);
+                        } else {
                             depth = rb - ax;
+                        }
                         mu = combine_mu(combine_, sc.smu[a], sc.mu[b]);
                     } else {
                         const int ai = a - S;

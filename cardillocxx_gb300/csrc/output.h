@@ -23,7 +23,7 @@ struct OutputScene {
     int N = 0, S = 0;
     std::vector<double> radius, mu;
     std::vector<int32_t> skind;
-    std::vector<double> spos, sdir, srad, smu;
+    std::vector<double> spos, sdir, srad, smu, shl;  // shl: cylinder half lengths
     std::vector<double> pos0;  // initial sphere centres (extent of the static meshes)
 };
 

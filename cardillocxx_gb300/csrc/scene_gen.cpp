@@ -296,6 +296,7 @@ int cdx_gen_view(const cdx_gen_scene* g, cdx_scene* v) {
     v->static_rest_t = g->static_rest_t.data();
     v->static_scene = g->static_scene.data();
     v->num_scenes = g->num_scenes;
+    v->static_half_length = nullptr;  // the generated scenes hold no cylinder
     return CDX_OK;
 }
 

@@ -83,6 +83,8 @@ def scene_struct(scene: dict) -> tuple[CdxScene, dict]:
         setattr(s, name, dp(keep[name]))
     s.static_scene = ip(keep.get("static_scene"))
     s.num_scenes = int(keep.get("num_scenes", 1))
+    if "static_half_length" in keep:
+        s.static_half_length = dp(keep["static_half_length"])
     return s, keep
 
 

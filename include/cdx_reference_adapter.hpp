@@ -111,6 +111,8 @@ namespace cardillo::integration {
 //    state back into C_Position3, C_Orientation (setValue keeps the rotation in sync),
 //    C_LinearVelocity3 and C_AngularVelocity3 (body frame). The warm-start memory stays in the
 //    context across steps.
+//  - Static solid cylinders are the entities with C_RB_Cylinder and no C_PhysicsObject: their axis
+//    is the pose's local z (coal::Cylinder's), radius and half length from the component.
 //  - Halfspaces driven by a trajectory (C_StaticTrajectory): each step runs Trajectory::update
 //    (trajectory.cpp:69-120; the reference runs it inside updateStateDependentTerms, after the first
 //    drift, and what it computes does not depend on that drift) and hands the poses and twists it
@@ -272,6 +274,9 @@ class GpuMoreauIntegrator : public IntegrationBase {
                 throw std::runtime_error("GpuMoreauIntegrator: dynamic planes are not on the GPU path");
             planes.push_back(e);
         }
+        const size_t nplanes = planes.size();
+        for (auto e : reg.view<C_RB_Cylinder>())
+            if (!reg.all_of<C_PhysicsObject>(e)) planes.push_back(e);  // dynamic cylinders threw above
         const size_t n = m_spheres.size(), ns = planes.size();
         (void)dynamic;
         m_traj.clear();
@@ -299,14 +304,25 @@ class GpuMoreauIntegrator : public IntegrationBase {
         }
         std::vector<int32_t> kind(ns, CDX_STATIC_HALFSPACE);
         std::vector<double> spos(3 * ns), squat(4 * ns), svel(3 * ns, 0.0), somega(3 * ns, 0.0), sdir(3 * ns),
-            srad(ns, 0.0), smu(ns), srn(ns), srt(ns);
+            srad(ns, 0.0), smu(ns), srn(ns), srt(ns), shl(ns, 0.0);
         for (size_t s = 0; s < ns; ++s) {
             const entt::entity e = planes[s];
             const auto& x = reg.get<C_Position3>(e).value;
             const auto& o = reg.get<C_Orientation>(e);
-            // the halfspace normal in the world frame (CollisionCoal builds it from C_RB_Plane's
-            // normal and the entity pose, collision_coal.cpp:290-296)
-            const Vector3r nw = o.rotation * reg.get<C_RB_Plane>(e).normal.normalized();
+            Vector3r nw;
+            if (s < nplanes) {
+                // the halfspace normal in the world frame (CollisionCoal builds it from C_RB_Plane's
+                // normal and the entity pose, collision_coal.cpp:290-296)
+                nw = o.rotation * reg.get<C_RB_Plane>(e).normal.normalized();
+            } else {
+                // coal::Cylinder(radius, 2 halfLength) lies along its local z (collision_coal.cpp:307-310)
+                Vector3r ez;
+                ez[2] = 1.0;
+                nw = o.rotation * ez;
+                kind[s] = CDX_STATIC_CYLINDER;
+                srad[s] = reg.get<C_RB_Cylinder>(e).radius;
+                shl[s] = reg.get<C_RB_Cylinder>(e).halfLength;
+            }
             for (int k = 0; k < 3; ++k) {
                 spos[3 * s + k] = x[k];
                 sdir[3 * s + k] = nw[k];
@@ -352,6 +368,7 @@ class GpuMoreauIntegrator : public IntegrationBase {
         sc.static_rest_n = srn.data();
         sc.static_rest_t = srt.data();
         sc.num_scenes = 1;
+        sc.static_half_length = shl.data();
         check(cdx_load_scene(m_ctx, &sc));
         m_dt = dt;
         m_world.m_structure_dirty = false;

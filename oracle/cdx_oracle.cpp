@@ -130,7 +130,7 @@ struct Engine {
     std::vector<int32_t> scene;
     std::vector<double> minv, Mdiag;  // per DOF (6 per body)
     std::vector<int32_t> skind, sscene;
-    std::vector<double> spos, sq, sv, sw, sdir, srad, sd, smu, srn, srt, sR;
+    std::vector<double> spos, sq, sv, sw, sdir, srad, sd, smu, srn, srt, sR, shl;
     // warm-start memory of the previous step (canonical order, sorted by key)
     std::vector<uint64_t> prev_keys;
     std::vector<double> prev_point, prev_lambda;
@@ -162,6 +162,74 @@ void build_mass(Engine& E) {
     }
 }
 
+// Sphere (centre xb, radius rb) against a solid cylinder (centre xa, unit axis u, radius R, half
+// length h); coal answers this pair with the exact nearest points (GJK on the two convex shapes),
+// restated here in closed form. In the cylinder's frame (axial coordinate ax, radial part perp of
+// length rho): outside, the nearest point is on the side (|ax| <= h), a cap (rho <= R) or a rim;
+// inside, on the nearer of the side and the cap (the side on a tie). The normal points from the
+// cylinder to the sphere; sd is the centre's signed distance to the surface along it.
+bool cylinder_geom(const double* xa, const double* u, double R, double h, const double* xb, double rb, double margin,
+                   double* p1, double* p2, double* nraw) {
+    double rel[3], perp[3];
+    for (int k = 0; k < 3; ++k) rel[k] = xb[k] - xa[k];
+    const double ax = dot3(rel, u);
+    for (int k = 0; k < 3; ++k) perp[k] = rel[k] - ax * u[k];
+    const double rho = norm3(perp);
+    const double sg = ax < 0.0 ? -1.0 : 1.0;
+    const double aax = std::fabs(ax);
+    double e[3];
+    if (rho > 0.0) {
+        for (int k = 0; k < 3; ++k) e[k] = perp[k] / rho;
+    } else {
+        double t2[3];
+        tangent_frame(u, e, t2);  // on the axis any radial direction is nearest
+    }
+    const bool out_side = rho > R, out_cap = aax > h;
+    int region;  // 0 side, 1 cap, 2 rim
+    double sd;
+    if (!out_side && !out_cap) {
+        const double dside = R - rho, dcap = h - aax;
+        region = dside <= dcap ? 0 : 1;
+        sd = region == 0 ? -dside : -dcap;
+    } else if (!out_cap) {
+        region = 0;
+        sd = rho - R;
+    } else if (!out_side) {
+        region = 1;
+        sd = aax - h;
+    } else {
+        region = 2;
+        sd = 0.0;
+    }
+    double q[3], n[3];
+    if (region == 0) {
+        for (int k = 0; k < 3; ++k) {
+            q[k] = (xa[k] + ax * u[k]) + R * e[k];
+            n[k] = e[k];
+        }
+    } else if (region == 1) {
+        for (int k = 0; k < 3; ++k) {
+            q[k] = (xa[k] + (sg * h) * u[k]) + perp[k];
+            n[k] = sg * u[k];
+        }
+    } else {
+        double d[3];
+        for (int k = 0; k < 3; ++k) {
+            q[k] = (xa[k] + (sg * h) * u[k]) + R * e[k];
+            d[k] = xb[k] - q[k];
+        }
+        sd = norm3(d);
+        for (int k = 0; k < 3; ++k) n[k] = d[k] / sd;
+    }
+    if (!((sd - rb) <= margin)) return false;
+    for (int k = 0; k < 3; ++k) {
+        p1[k] = q[k];
+        p2[k] = xb[k] - rb * n[k];
+        nraw[k] = n[k];
+    }
+    return true;
+}
+
 // Narrow phase for one (static, sphere) or (sphere, sphere) pair plus makeContact
 // (src/collision/collision_coal.cpp:112-163). Returns false when the shapes are apart
 // (distance > collision.security_margin, coal's ShapeShapeCollider rule).
@@ -184,6 +252,10 @@ bool make_contact(const Engine& E, int a_static, int a_body, int b_body, Contact
                 p2[k] = xb[k] - rb * u[k];
                 nraw[k] = u[k];
             }
+        } else if (E.skind[s] == 2) {
+            // solid cylinder (C_RB_Cylinder, coal::Cylinder(radius, 2 halfLength) along the axis;
+            // collision_coal.cpp:307-310): the nearest point of the side, a cap or a rim
+            if (!cylinder_geom(xa, &E.sdir[3 * s], E.srad[s], E.shl[s], xb, rb, margin, p1, p2, nraw)) return false;
         } else {
             // hollow drum wall (new primitive; the reference has no counterpart)
             double rel[3];
@@ -1636,6 +1708,8 @@ void* or_create(const or_config* cfg, const or_scene* sc) {
     }
     E->srad.assign(S, 0.0);
     if (sc->static_radius) E->srad.assign(sc->static_radius, sc->static_radius + S);
+    E->shl.assign(S, 0.0);
+    if (sc->static_half_length) E->shl.assign(sc->static_half_length, sc->static_half_length + S);
     E->smu.assign(sc->static_mu, sc->static_mu + S);
     E->srn.assign(sc->static_rest_n, sc->static_rest_n + S);
     E->srt.assign(sc->static_rest_t, sc->static_rest_t + S);

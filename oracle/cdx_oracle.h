@@ -68,7 +68,7 @@ typedef struct or_scene {
     const double* rest_t;  /* [N] */
     const int32_t* body_scene; /* [N] or NULL */
     int32_t num_statics;
-    const int32_t* static_kind; /* 0 halfspace, 1 hollow drum */
+    const int32_t* static_kind; /* 0 halfspace, 1 hollow drum, 2 solid cylinder */
     const double* static_pos;   /* [3S] */
     const double* static_quat;  /* [4S] */
     const double* static_vel;   /* [3S] world */
@@ -80,6 +80,7 @@ typedef struct or_scene {
     const double* static_rest_t;
     const int32_t* static_scene; /* [S] or NULL */
     int32_t num_scenes;
+    const double* static_half_length; /* [S] cylinder half length, or NULL */
 } or_scene;
 
 typedef struct or_stats {

@@ -99,6 +99,7 @@ class OrScene(C.Structure):
         ("static_mu", _P), ("static_rest_n", _P), ("static_rest_t", _P),
         ("static_scene", _PI),
         ("num_scenes", C.c_int32),
+        ("static_half_length", _P),
     ]
 
 
@@ -219,6 +220,8 @@ class Oracle:
             setattr(sc, name, _dp(s[name]))
         sc.static_scene = _ip(s.get("static_scene"))
         sc.num_scenes = int(s.get("num_scenes", 1))
+        if "static_half_length" in s:
+            sc.static_half_length = _dp(s["static_half_length"])
         self.cfg = config_from(cfg, omp_mode, num_threads)
         self.h = self.L.or_create(C.byref(self.cfg), C.byref(sc))
         self.N = sc.num_bodies

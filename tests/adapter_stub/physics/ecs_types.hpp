@@ -79,6 +79,10 @@ struct C_Restitution {
     real_t tangential;
 };
 struct C_InertiaDiag { Vector3r I; };
+struct C_RB_Cylinder {
+    real_t radius;
+    real_t halfLength;
+};
 using TrajectoryPose = std::pair<Vector3r, Quaternion4r>;
 using TrajectoryTwist = std::pair<Vector3r, Vector3r>;
 struct C_StaticTrajectory {

@@ -382,3 +382,44 @@ def test_prescribed_wall_velocity_moves_resting_sphere(oracle_mod):
     od.step(1)
     assert od.stats()["num_contacts"] == 0
     np.testing.assert_allclose(od.static_state()["pos"][0], [0.0, 0.0, -1e-3])
+
+
+# ---- solid cylinder (C_RB_Cylinder, coal::Cylinder; collision_coal.cpp:307-310) ----
+def cyl(**kw):
+    c = {"kind": "cylinder", "pos": (0.0, 0.0, 0.0), "dir": (0.0, 0.0, 1.0), "radius": 0.2, "half_length": 0.1,
+         "mu": 0.3}
+    c.update(kw)
+    return c
+
+
+@pytest.mark.parametrize("centre, normal", [
+    ((0.05, -0.03, 0.15), (0.0, 0.0, 1.0)),                                 # on the top cap
+    ((0.25, 0.0, 0.02), (1.0, 0.0, 0.0)),                                   # against the side
+    ((0.2 + 0.03, 0.0, 0.1 + 0.04), (0.6, 0.0, 0.8)),                       # on the rim: centre 0.05 from it
+    ((0.17, 0.0, 0.0), (1.0, 0.0, 0.0)),                                    # centre inside, nearer the side
+    ((0.0, 0.0, -0.09), (0.0, 0.0, -1.0)),                                  # centre inside, nearer the bottom cap
+])
+def test_cylinder_contact_geometry(oracle_mod, centre, normal):
+    # zero gravity, at rest: one contact whose normal points from the cylinder to the sphere and
+    # whose point is the midpoint of the two surfaces' nearest points
+    r = 0.05
+    s = make_scene([{"pos": centre, "radius": r}], [cyl()])
+    o = oracle_mod.Oracle(s, cfg(**{"sim.gravity": (0.0, 0.0, 0.0)}))
+    o.step(1)
+    c = o.contacts()
+    assert c["id_a"].tolist() == [0] and c["id_b"].tolist() == [1]
+    np.testing.assert_allclose(c["normal"][0], normal, atol=1e-12)
+
+
+def test_sphere_rests_on_cylinder_cap_and_side(oracle_mod):
+    r = 0.05
+    # touching within 1e-9 m (0.1 + 0.05 rounds above 0.15)
+    for body, c in (({"pos": (0.02, 0.0, 0.1 + r - 1e-9)}, cyl()),
+                    ({"pos": (0.0, 0.0, 0.2 + r - 1e-9)}, cyl(dir=(1.0, 0.0, 0.0)))):
+        s = make_scene([dict(body, radius=r)], [c])
+        m = s["mass"][0]
+        o = oracle_mod.Oracle(s, cfg())
+        o.step(1)
+        lam = o.contacts()["lambda"][0]
+        np.testing.assert_allclose(lam[0], m * G * H, rtol=1e-10)
+        assert abs(o.state()["vel"][0, 2]) < 1e-12
