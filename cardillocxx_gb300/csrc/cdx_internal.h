@@ -174,6 +174,7 @@ struct CondBufs {
     double* u = nullptr;
     double* up = nullptr;
     double* part = nullptr;
+    double* dl = nullptr;      // 3 x cap: the Jacobi sweep's impulse increments
     int32_t* flags = nullptr;  // [0] diverged, [1] uncolored after a round, [2] more colors than the limit
     double* err = nullptr;     // the last residual (err) evaluated
     uint32_t* kin = nullptr;   // sort by color: keys (colors) and values (contacts), in and out
@@ -253,9 +254,17 @@ void launch_pgs_setup(const Scene& sc, Contacts& C, int gen, int nc, int warmsta
 int launch_pgs_levels(const PgsBufs& P, int nc, uint32_t* keys, uint32_t* vals, unsigned long long wait_ns,
                       cudaStream_t s);
 // order: the contacts sorted by level
+// condensed: run the condensed solver's block update (its sequential gauss_seidel sweep mode)
 int launch_pgs_solve(const Scene& sc, const Contacts& C, int nc, const CondBufs& B, const PgsBufs& P,
                      const uint32_t* order, double relax, double alpha, double tol_rel, double tol_abs, int max_iter,
-                     DevScalars* ds, unsigned long long wait_ns, cudaStream_t s);
+                     DevScalars* ds, unsigned long long wait_ns, cudaStream_t s, int condensed = 0);
+// the per-body chains of blocks (predecessors) and the blocks in sweep order: W's row order, or
+// contact order (contact_order = 1, the condensed solver's)
+void launch_pgs_links(const Scene& sc, const Contacts& C, int nc, const Incidence& inc, PgsBufs& P,
+                      int contact_order, cudaStream_t s);
+// condensed solver, Jacobi sweep (both passes)
+void launch_cond_jacobi(const Scene& sc, const Contacts& C, int nc, const CondBufs& B, const Incidence& inc,
+                        double relax, double alpha, double* u, const DevScalars* ds, cudaStream_t s);
 void launch_cond_ufree(const Scene& sc, double dt, const double* g, int implicit_gyro, CondBufs& B, cudaStream_t s);
 // nonfinite (optional): set to 1 when a body's state after the drift is not finite
 void launch_drift64(const Scene& sc, double h, int compute_R, cudaStream_t s, int32_t* nonfinite = nullptr);

@@ -96,8 +96,8 @@ int Engine::init(const cdx_config& c) {
 //  - the split form runs the reference's Nesterov loop and the standard loop's tolerance exit in
 //    its cooperative solve; Chebyshev and Anderson (selected when Nesterov is off, as in
 //    projected_jacobi.cpp:470-491) run in the plain FP64 method only;
-//  - solver.type=condensed runs in the plain FP64 method with condensed.sweep_mode=colored (its
-//    other sweep modes, and its Nesterov and Chebyshev loops, are not built);
+//  - solver.type=condensed runs in the plain FP64 method with condensed.sweep_mode gauss_seidel,
+//    jacobi or colored (chaotic, and its Nesterov and Chebyshev loops, are not built);
 //  - solver.type=projected_gauss_seidel runs its plain loop in the plain FP64 method (its Nesterov
 //    loop is not built).
 int Engine::check_solver_config(const cdx_config& c) {
@@ -110,8 +110,9 @@ int Engine::check_solver_config(const cdx_config& c) {
     if (c.solver_type == 1) {
         if (c.gpu_precision != CDX_PRECISION_FP64)
             return fail(CDX_ERR_UNSUPPORTED, "solver.type=condensed runs in the plain FP64 method (gpu.precision=fp64)");
-        if (c.condensed_sweep_mode != 2)
-            return fail(CDX_ERR_UNSUPPORTED, "solver.type=condensed runs with condensed.sweep_mode=colored on the GPU");
+        if (c.condensed_sweep_mode < 0 || c.condensed_sweep_mode > 2)
+            return fail(CDX_ERR_UNSUPPORTED, "condensed.sweep_mode=chaotic is not on the GPU path (its result depends "
+                                             "on the order of unsynchronised updates)");
         if (c.pj_nesterov || c.pj_chebyshev)
             return fail(CDX_ERR_UNSUPPORTED, "solver.type=condensed runs its standard loop (no pj.nesterov or pj.chebyshev)");
     }

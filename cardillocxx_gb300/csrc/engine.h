@@ -123,6 +123,8 @@ struct Engine {
     int cond_diverged = 0;
     int ensure_cond();
     int solve_condensed();
+    int solve_condensed_gs();
+    int finish_condensed();
     // projected Gauss-Seidel (plain FP64 method; engine_pgs.cpp)
     cdx::PgsBufs pgs;
     int last_levels = 0;  // levels of the last projected Gauss-Seidel step (its longest chain of blocks)

@@ -22,7 +22,7 @@ int Engine::ensure_cond() {
     const int N = std::max(sc.N, 1);
     if (B.cap == cap && B.N == N) return CDX_OK;
     void* old[] = {B.ginv, B.rhs, B.lam, B.deg, B.col, B.col2, B.uf, B.u, B.up, B.part, B.flags, B.err,
-                   B.kin, B.vin, B.kout, B.vout, B.cstart, B.cend};
+                   B.kin, B.vin, B.kout, B.vout, B.cstart, B.cend, B.dl};
     for (void* p : old)
         if (p) dfree(p);
     B = CondBufs{};
@@ -30,6 +30,7 @@ int Engine::ensure_cond() {
     if ((st = dalloc((void**)&B.ginv, sizeof(double) * 3 * cap, "condensed"))) return st;
     if ((st = dalloc((void**)&B.rhs, sizeof(double) * 3 * cap, "condensed"))) return st;
     if ((st = dalloc((void**)&B.lam, sizeof(double) * 3 * cap, "condensed"))) return st;
+    if ((st = dalloc((void**)&B.dl, sizeof(double) * 3 * cap, "condensed"))) return st;
     if ((st = dalloc((void**)&B.deg, sizeof(int32_t) * cap, "condensed"))) return st;
     if ((st = dalloc((void**)&B.col, sizeof(int32_t) * cap, "condensed"))) return st;
     if ((st = dalloc((void**)&B.col2, sizeof(int32_t) * cap, "condensed"))) return st;
@@ -69,6 +70,26 @@ int Engine::solve_condensed() {
         launch_cond_final(sc, C, gen, nc, B, x, -1, stream);
         ++launches;
         return CDX_OK;
+    }
+    if (cfg.condensed_sweep_mode == 0) return solve_condensed_gs();
+    if (cfg.condensed_sweep_mode == 1) {
+        // Jacobi sweeps (jacobiSweep, condensed_solver.cpp:268-317): both passes, then the stop test
+        const int nv6 = 6 * N;
+        launch_cond_copy(nv6, B.u, B.up, ds, stream);
+        const int maxit = std::max(1, cfg.pj_max_iterations);
+        const int every = std::max(1, cfg.gpu_check_every);
+        for (int it = 0; it < maxit; ++it) {
+            launch_cond_jacobi(sc, C, nc, B, inc, cfg.pj_relaxation, cfg.pj_alpha, B.u, ds, stream);
+            launch_cond_check(N, B, cfg.pj_tol_rel, cfg.pj_tol_abs, it, ds, stream);
+            launch_cond_copy(nv6, B.u, B.up, ds, stream);
+            launches += 5;
+            if ((it + 1) % every == 0 && it + 1 < maxit) {
+                cudaMemcpyAsync(&hs->done, &ds->done, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+                if ((st = cuda_check(cudaStreamSynchronize(stream), "condensed poll"))) return st;
+                if (hs->done) break;
+            }
+        }
+        return finish_condensed();
     }
     // coloring: rounds until every block is colored
     int32_t* col_in = B.col;
@@ -125,15 +146,60 @@ int Engine::solve_condensed() {
             if (hs->done) break;
         }
     }
-    // the result, the complementarity residual on the applied impulses, the stored impulses
+    return finish_condensed();
+}
+
+// the result, the complementarity residual on the applied impulses, the stored impulses
+int Engine::finish_condensed() {
+    CondBufs& B = cond;
     launch_cond_final(sc, C, gen, nc, B, x, -1, stream);
     launch_cond_final(sc, C, gen, nc, B, x, 1, stream);
     launch_sweep_contact64(sc, C, gen, nc, x, ds, 1, stream);
     launch_final_residual(ds, stream);
     launch_cond_final(sc, C, gen, nc, B, x, 0, stream);
     launches += 5;
+    int32_t hflags[4] = {0, 0, 0, 0};
     cudaMemcpyAsync(hflags, B.flags, sizeof(hflags), cudaMemcpyDeviceToHost, stream);
+    int st;
     if ((st = cuda_check(cudaStreamSynchronize(stream), "condensed solve"))) return st;
     cond_diverged = hflags[0];
     return CDX_OK;
+}
+
+// condensed.sweep_mode=gauss_seidel (gaussSeidelSweep, condensed_solver.cpp:166-182): blocks in
+// contact order, each seeing the u_corr of every earlier block; run by the projected Gauss-Seidel
+// machinery (levels of the per-body chains, then the ordered sweep in one cooperative launch)
+int Engine::solve_condensed_gs() {
+    CondBufs& B = cond;
+    int st;
+    if ((st = ensure_pgs())) return st;
+    launch_pgs_links(sc, C, nc, inc, pgs, 1, stream);
+    launch_cond_copy(6 * sc.N, B.u, B.up, ds, stream);
+    launches += 2;
+    const unsigned long long wait_ns = cfg.gpu_coop_wait_ns > 0 ? (unsigned long long)cfg.gpu_coop_wait_ns : 0ull;
+    if ((st = cuda_check((cudaError_t)launch_pgs_levels(pgs, nc, B.kin, B.vin, wait_ns, stream), "levels launch")))
+        return st;
+    ++launches;
+    int32_t hl[2] = {0, 0};
+    cudaMemcpyAsync(&hl[0], pgs.maxlev, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(&hl[1], pgs.err, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+    if ((st = cuda_check(cudaStreamSynchronize(stream), "condensed levels"))) return st;
+    if (hl[1]) return fail(CDX_ERR_TIMEOUT, "condensed levels: a grid barrier wait ran out (gpu.coop_wait_ns)");
+    last_levels = hl[0] + 1;
+    int bits = 1;
+    while (bits < 32 && (hl[0] >> bits) != 0) ++bits;
+    if ((st = cuda_check(sort_pairs(tmp, tmp_bytes, B.kin, B.kout, B.vin, B.vout, nc, bits, stream), "sort levels")))
+        return st;
+    launches += 4;
+    if ((st = cuda_check((cudaError_t)launch_pgs_solve(sc, C, nc, B, pgs, B.vout, cfg.pj_relaxation, cfg.pj_alpha,
+                                                       cfg.pj_tol_rel, cfg.pj_tol_abs, cfg.pj_max_iterations, ds,
+                                                       wait_ns, stream, 1),
+                         "condensed sweep launch")))
+        return st;
+    ++launches;
+    int32_t herr = 0;
+    cudaMemcpyAsync(&herr, pgs.err, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+    if ((st = cuda_check(cudaStreamSynchronize(stream), "condensed sweeps"))) return st;
+    if (herr) return fail(CDX_ERR_TIMEOUT, "condensed sweeps: a wait ran out (gpu.coop_wait_ns)");
+    return finish_condensed();
 }

@@ -54,6 +54,12 @@ __device__ __forceinline__ double minv_of(const Scene& sc, int i, int k) {
     return k < 3 ? sc.bf(BF_MINVL)[i] : sc.bf(BF_MINVA)[i];
 }
 
+}  // namespace
+}  // namespace cdx
+#include "cond_block.cuh"
+namespace cdx {
+namespace {
+
 // u_free = v_n + M^-1 (dt f_ext) [+ M^-1 (dt f_gyro)] (CondensedAssembler::ufree, condensed_assembler.cpp:348-356;
 // PgsAssembler::ufree, pgs_assembler.cpp:96-103, is the same)
 __global__ void k_cond_ufree(Scene sc, double dt, double g0, double g1, double g2, int implicit_gyro, double* uf) {
@@ -193,50 +199,50 @@ __global__ void k_cond_sweep_color(Scene sc, Contacts C, CondBufs B, const uint3
     if (*(volatile const int32_t*)&ds->done) return;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
-    const int c = (int)blocks[t];
+    double d[3];
+    cond_block<false, true>(sc, C, B, (int)blocks[t], relax, alpha, u, d);
+}
+
+// Jacobi sweep, pass 1 (jacobiSweep, condensed_solver.cpp:285-296): every block against the
+// previous sweep's u_corr (untouched in this pass); the increments go to dl
+__global__ void k_cond_jacobi_blocks(Scene sc, Contacts C, CondBufs B, int nc, double relax, double alpha,
+                                     const double* u, const DevScalars* ds) {
+    if (*(volatile const int32_t*)&ds->done) return;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    double d[3] = {0.0, 0.0, 0.0};
+    cond_block<false, false>(sc, C, B, c, relax, alpha, const_cast<double*>(u), d);
+    const int64_t cap = C.cap;
+    for (int q = 0; q < 3; ++q) B.dl[q * cap + c] = d[q];
+}
+
+// pass 2 (:302-316): each body gathers J^T dl from its blocks in block order, u += M^-1 acc
+__global__ void k_cond_jacobi_bodies(Scene sc, Contacts C, CondBufs B, Incidence inc, double* u,
+                                     const DevScalars* ds) {
+    if (*(volatile const int32_t*)&ds->done) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sc.N) return;
+    if (inc.end[i] <= inc.start[i]) return;
     const int N = sc.N;
     const int64_t cap = C.cap;
-    const int a = C.a[c], b = C.b[c];
-    const int dim = (C.flags[c] & CF_FRICTIONAL) ? 3 : 1;
-    double Ja[3][6], Jb[3][6], r[3], lo[3], ln[3], dl[3];
-    for (int q = 0; q < dim; ++q) {
-        jac_row(C, c, q, false, Ja[q]);
-        jac_row(C, c, q, true, Jb[q]);
-        double o = B.rhs[q * cap + c];
-        if (a >= 0) o = o - row_dot(Ja[q], u, N, a);
-        o = o - row_dot(Jb[q], u, N, b);
-        lo[q] = B.lam[q * cap + c];
-        o = o - 0.0 * lo[q];  // contact rows carry no compliance
-        r[q] = o;
-    }
-    for (int q = 0; q < dim; ++q) {
-        // GiiInv is diagonal but stored dense: the zero entries multiply the other residuals
-        double g = (q == 0 ? B.ginv[c] : 0.0) * r[0];
-        for (int j = 1; j < dim; ++j) g = g + (q == j ? B.ginv[j * cap + c] : 0.0) * r[j];
-        ln[q] = ((relax * g) * alpha) + lo[q];
-    }
-    ln[0] = smin(ln[0], 0.0);
-    if (dim == 3) {
-        const double tn = sqrt(ln[1] * ln[1] + ln[2] * ln[2]);
-        if (tn > 0.0) {
-            const double s = smin(1.0, (-C.mu[c] * ln[0]) / tn);
-            ln[1] = ln[1] * s;
-            ln[2] = ln[2] * s;
-        }
-    }
-    for (int q = 0; q < dim; ++q) dl[q] = ln[q] - lo[q];
-    for (int side = 0; side < 2; ++side) {
-        const int body = side == 0 ? a : b;
-        if (body < 0) continue;
-        double (*J)[6] = side == 0 ? Ja : Jb;
+    double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int p = inc.start[i]; p < inc.end[i]; ++p) {
+        const uint32_t code = inc.val_out[p];
+        const int c = (int)(code >> 1);
+        const bool sideB = (code & 1u) != 0;
+        const int dim = (C.flags[c] & CF_FRICTIONAL) ? 3 : 1;
+        double J[3][6];
+        for (int q = 0; q < dim; ++q) jac_row(C, c, q, sideB, J[q]);
         for (int k = 0; k < 6; ++k) {
-            double tk = J[0][k] * dl[0];
-            for (int q = 1; q < dim; ++q) tk = tk + J[q][k] * dl[q];
-            const size_t j = (size_t)k * N + body;
-            u[j] = u[j] + minv_of(sc, body, k) * tk;
+            double t = J[0][k] * B.dl[c];
+            for (int q = 1; q < dim; ++q) t = t + J[q][k] * B.dl[q * cap + c];
+            acc[k] = acc[k] + t;
         }
     }
-    for (int q = 0; q < dim; ++q) B.lam[q * cap + c] = ln[q];
+    for (int k = 0; k < 6; ++k) {
+        const size_t j = (size_t)k * N + i;
+        u[j] = u[j] + minv_of(sc, i, k) * acc[k];
+    }
 }
 
 // residualNorm (condensed_solver.cpp:500-506) over the stacked velocity vector (entry 6 i + k),
@@ -330,6 +336,11 @@ void launch_cond_color_round(const Contacts& C, int nc, const CondBufs& B, const
                              const int32_t* col_in, int32_t* col_out, int32_t* uncolored, int32_t* too_many,
                              cudaStream_t s) {
     if (nc > 0) k_cond_color_round<<<nblk(nc), NT, 0, s>>>(C, nc, B, inc, col_in, col_out, uncolored, too_many);
+}
+void launch_cond_jacobi(const Scene& sc, const Contacts& C, int nc, const CondBufs& B, const Incidence& inc,
+                        double relax, double alpha, double* u, const DevScalars* ds, cudaStream_t s) {
+    if (nc > 0) k_cond_jacobi_blocks<<<nblk(nc, 128), 128, 0, s>>>(sc, C, B, nc, relax, alpha, u, ds);
+    if (sc.N > 0) k_cond_jacobi_bodies<<<nblk(sc.N, 128), 128, 0, s>>>(sc, C, B, inc, u, ds);
 }
 void launch_cond_sweep_color(const Scene& sc, const Contacts& C, const CondBufs& B, const uint32_t* blocks, int n,
                              double relax, double alpha, double* u, const DevScalars* ds, cudaStream_t s) {

@@ -40,7 +40,7 @@ __device__ __forceinline__ double minv_of(const Scene& sc, int i, int k) {
 }
 
 // W row q of contact c on one side: sign * [d_q (world), c_q (body-frame lever product)]
-__device__ __forceinline__ void wside(const Contacts& C, int c, int q, bool sideB, double* J) {
+__device__ __forceinline__ void jac_row(const Contacts& C, int c, int q, bool sideB, double* J) {
     const int64_t cap = C.cap;
     const double* cc = sideB ? C.cB : C.cA;
 #pragma unroll
@@ -58,6 +58,12 @@ template <bool LD>
 __device__ __forceinline__ double uget(const double* u, size_t j) {
     return LD ? __ldcg(u + j) : u[j];
 }
+
+}  // namespace
+}  // namespace cdx
+#include "cond_block.cuh"
+namespace cdx {
+namespace {
 
 // sum over row q's nonzeros in W's column order (the lower body index first), from zero, as
 // Eigen's row-major sparse product sums a row
@@ -89,8 +95,8 @@ __global__ void k_pgs_setup(Scene sc, Contacts C, int gen, int nc, const double*
     const int dim = fr ? 3 : 1;
     for (int q = 0; q < dim; ++q) {
         double J[2][6];
-        wside(C, c, q, false, J[0]);
-        wside(C, c, q, true, J[1]);
+        jac_row(C, c, q, false, J[0]);
+        jac_row(C, c, q, true, J[1]);
         const double cb = C.cb[q * cap + c];
         const double e = q == 0 ? C.eN[c] : C.eT[c];
         // the reference adds e . v_prev to every row once some row has restitution; on a row with
@@ -143,7 +149,7 @@ __global__ void k_pgs_ucorr_init(Scene sc, Contacts C, CondBufs B, Incidence inc
         const int dim = (C.flags[c] & CF_FRICTIONAL) ? 3 : 1;
         for (int q = 0; q < dim; ++q) {
             double J[6];
-            wside(C, c, q, sideB, J);
+            jac_row(C, c, q, sideB, J);
             const double l = B.lam[q * cap + c];
             for (int k = 0; k < 6; ++k) acc[k] = acc[k] + (minv_of(sc, i, k) * J[k]) * l;
         }
@@ -153,9 +159,9 @@ __global__ void k_pgs_ucorr_init(Scene sc, Contacts C, CondBufs B, Incidence inc
 
 // predecessors: per contact and side, the previous block of that body in row order (or -1); the
 // blocks by rank
-__global__ void k_pgs_links(int N, Contacts C, int nc, Incidence inc, PgsBufs P) {
+__global__ void k_pgs_links(int N, Contacts C, int nc, Incidence inc, PgsBufs P, int contact_order) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < nc) P.by_rank[C.rank[t]] = (uint32_t)t;
+    if (t < nc) P.by_rank[contact_order ? t : C.rank[t]] = (uint32_t)t;
     if (t >= N) return;
     int prev = -1;
     for (int p = inc.start[t]; p < inc.end[t]; ++p) {
@@ -273,8 +279,8 @@ __device__ __forceinline__ void pgs_block(const Scene& sc, const Contacts& C, co
     const int dim = (C.flags[c] & CF_FRICTIONAL) ? 3 : 1;
     double J[3][2][6], rs[3], dl[3], lam[3];
     for (int q = 0; q < dim; ++q) {
-        wside(C, c, q, false, J[q][0]);
-        wside(C, c, q, true, J[q][1]);
+        jac_row(C, c, q, false, J[q][0]);
+        jac_row(C, c, q, true, J[q][1]);
         lam[q] = __ldcg(&B.lam[q * cap + c]);
         double o = B.rhs[q * cap + c];
         o = o - wdot<true>(J[q], a, b, u, N);
@@ -319,6 +325,7 @@ __device__ __forceinline__ void pgs_block(const Scene& sc, const Contacts& C, co
 
 // The solve: sweeps until the velocity-increment residual is below 1 (or not finite: the solve
 // diverged, check_residual :142-151) or max_iter sweeps.
+template <int COND>
 __global__ void __launch_bounds__(NT) k_pgs_solve(Scene sc, Contacts C, CondBufs B, PgsBufs P, const uint32_t* order,
                                                   int nc, double relax,
                                                   double alpha, double tol_rel, double tol_abs, int max_iter,
@@ -336,7 +343,13 @@ __global__ void __launch_bounds__(NT) k_pgs_solve(Scene sc, Contacts C, CondBufs
             ok = wait_done(P.done, P.pred[c], it, P.err, wait_ns) &&
                  wait_done(P.done, P.pred[P.cap + c], it, P.err, wait_ns);
             if (!ok) break;
-            pgs_block(sc, C, B, c, relax, alpha, B.u);
+            if (COND) {
+                // the condensed solver's sequential sweep (gaussSeidelSweep, condensed_solver.cpp:166-182)
+                double d[3];
+                cond_block<true, true>(sc, C, B, c, relax, alpha, B.u, d);
+            } else {
+                pgs_block(sc, C, B, c, relax, alpha, B.u);
+            }
             st_release_s32(P.done + c, it);
         }
         if (!grid_sync(P.bar, ++epoch, P.err, wait_ns)) return;
@@ -386,10 +399,14 @@ void launch_pgs_setup(const Scene& sc, Contacts& C, int gen, int nc, int warmsta
                       PgsBufs& P, cudaStream_t s) {
     if (nc > 0) k_pgs_setup<<<nblk(nc), NT, 0, s>>>(sc, C, gen, nc, B.uf, warmstart, B);
     if (sc.N > 0) k_pgs_ucorr_init<<<nblk(sc.N), NT, 0, s>>>(sc, C, B, inc, B.u);
+    launch_pgs_links(sc, C, nc, inc, P, 0, s);
+}
+void launch_pgs_links(const Scene& sc, const Contacts& C, int nc, const Incidence& inc, PgsBufs& P,
+                      int contact_order, cudaStream_t s) {
     cudaMemsetAsync(P.pred, 0xff, sizeof(int32_t) * 2 * (size_t)P.cap, s);
     cudaMemsetAsync(P.done, 0xff, sizeof(int32_t) * (size_t)P.cap, s);
     const int n = std::max(nc, sc.N);
-    if (n > 0) k_pgs_links<<<nblk(n), NT, 0, s>>>(sc.N, C, nc, inc, P);
+    if (n > 0) k_pgs_links<<<nblk(n), NT, 0, s>>>(sc.N, C, nc, inc, P, contact_order);
 }
 
 // grid of a cooperative launch: every block resident (at most two an SM)
@@ -422,7 +439,7 @@ int launch_pgs_levels(const PgsBufs& P, int nc, uint32_t* keys, uint32_t* vals, 
 
 int launch_pgs_solve(const Scene& sc, const Contacts& C, int nc, const CondBufs& B, const PgsBufs& P,
                      const uint32_t* order, double relax, double alpha, double tol_rel, double tol_abs, int max_iter,
-                     DevScalars* ds, unsigned long long wait_ns, cudaStream_t s) {
+                     DevScalars* ds, unsigned long long wait_ns, cudaStream_t s, int condensed) {
     cudaMemsetAsync(P.bar, 0, sizeof(unsigned), s);
     cudaMemsetAsync(P.err, 0, sizeof(int32_t), s);
     cudaMemsetAsync(P.stop, 0, sizeof(int32_t), s);
@@ -435,9 +452,10 @@ int launch_pgs_solve(const Scene& sc, const Contacts& C, int nc, const CondBufs&
     double rl = relax, al = alpha, tr = tol_rel, ta = tol_abs;
     unsigned long long wn = wait_ns > 0 ? wait_ns : PGS_WAIT_NS;
     void* args[] = {&a0, &a1, &a2, &a3, &o, &n, &rl, &al, &tr, &ta, &mi, &ds, &wn};
-    static int grid = 0;
-    if (grid == 0) grid = coop_grid(k_pgs_solve);
-    return (int)cudaLaunchCooperativeKernel((const void*)k_pgs_solve, dim3(grid), dim3(NT), args, 0, s);
+    static int grid[2] = {0, 0};
+    const void* k = condensed ? (const void*)k_pgs_solve<1> : (const void*)k_pgs_solve<0>;
+    if (grid[condensed ? 1 : 0] == 0) grid[condensed ? 1 : 0] = condensed ? coop_grid(k_pgs_solve<1>) : coop_grid(k_pgs_solve<0>);
+    return (int)cudaLaunchCooperativeKernel(k, dim3(grid[condensed ? 1 : 0]), dim3(NT), args, 0, s);
 }
 
 }  // namespace cdx

@@ -62,9 +62,9 @@ typedef struct cdx_config {
     double pj_tol_rel;                /* pj.tol_rel */
     double pj_alpha;                  /* pj.alpha */
     double pj_relaxation;             /* pj.relaxation (accepted, unused by PJ as in the reference) */
-    int32_t solver_type;              /* solver.type: 0 projected_jacobi, 1 condensed (plain FP64 method,
-                                         condensed.sweep_mode=colored), 2 projected_gauss_seidel (plain
-                                         FP64 method, plain loop) */
+    int32_t solver_type;              /* solver.type: 0 projected_jacobi, 1 condensed (plain FP64 method;
+                                         sweep modes gauss_seidel, jacobi, colored), 2 projected_gauss_seidel
+                                         (plain FP64 method, plain loop) */
     double collision_security_margin; /* collision.security_margin */
     double collision_match_max_dist;  /* collision.match_max_dist */
     int32_t collision_broadphase;     /* collision.broadphase: 0 uniform_grid (any reference value maps here) */
@@ -106,7 +106,7 @@ typedef struct cdx_config {
                                                at a grid barrier before the step fails with CDX_ERR_TIMEOUT
                                                (0 = 0.2 s) */
     int32_t condensed_sweep_mode;           /* condensed.sweep_mode: 0 gauss_seidel (default), 1 jacobi,
-                                               2 colored (the one run on the GPU), 3 chaotic */
+                                               2 colored (these three run on the GPU), 3 chaotic */
     int32_t gpu_tune_alpha_every;           /* gpu.tune_alpha_every: steps between two tunings of the scenes' alpha */
 } cdx_config;
 

@@ -1133,8 +1133,9 @@ SolveResult solve_dispatch(PJ& P, const or_config& cfg, double* rhs, const doubl
                     tr);
 }
 
-// ---- the condensed solver's colored sweep, src/physics/solver/condensed_solver.cpp ----
-// CondensedSolver::solve (condensed_solver.cpp:443-760) with condensed.sweep_mode=colored, the
+// ---- the condensed solver's sweeps, src/physics/solver/condensed_solver.cpp ----
+// CondensedSolver::solve (condensed_solver.cpp:443-760) with condensed.sweep_mode gauss_seidel,
+// jacobi or colored, the
 // projection local solve, natural ordering, no true_schur / auto_alpha, and the standard loop, for
 // sphere contacts. One block per contact in contact order (condensed_assembler.cpp:203-262); its
 // rows are the contact's W rows split by side: Ja = -[d_r, r_A x d_r] on body A (when dynamic),
@@ -1207,9 +1208,10 @@ inline double cond_row(const double* Jr, const double* u) {
 
 // One block of the colored sweep: coloredSweep's body (condensed_solver.cpp:205-226) with
 // blockResidual (:62-69), computeBlockUpdate (:139-158) and projectBlock (:41-52).
-void cond_block_update(const CondBlock& k, double relax, double alpha, const double* minv, double* lam, double* u) {
+// the block's new impulses against u (lam is overwritten; d receives new - old)
+void cond_block_lambda(const CondBlock& k, double relax, double alpha, const double* u, double* lam, double* d) {
     const int dim = k.dim;
-    double r[3], lo[3], ln[3], d[3];
+    double r[3], lo[3], ln[3];
     for (int q = 0; q < dim; ++q) {
         double o = k.rhs[q];
         if (k.a >= 0) o = o - cond_row(&k.Ja[6 * q], &u[6 * (size_t)k.a]);
@@ -1234,9 +1236,13 @@ void cond_block_update(const CondBlock& k, double relax, double alpha, const dou
         }
     }
     for (int q = 0; q < dim; ++q) d[q] = ln[q] - lo[q];
-    if (k.a >= 0) cond_scatter(k.Ja, dim, d, &minv[6 * (size_t)k.a], &u[6 * (size_t)k.a]);
-    cond_scatter(k.Jb, dim, d, &minv[6 * (size_t)k.b], &u[6 * (size_t)k.b]);
     for (int q = 0; q < dim; ++q) lam[q] = ln[q];
+}
+void cond_block_update(const CondBlock& k, double relax, double alpha, const double* minv, double* lam, double* u) {
+    double d[3];
+    cond_block_lambda(k, relax, alpha, u, lam, d);
+    if (k.a >= 0) cond_scatter(k.Ja, k.dim, d, &minv[6 * (size_t)k.a], &u[6 * (size_t)k.a]);
+    cond_scatter(k.Jb, k.dim, d, &minv[6 * (size_t)k.b], &u[6 * (size_t)k.b]);
 }
 
 struct CondResult {
@@ -1338,15 +1344,56 @@ CondResult condensed_colored(const Engine& E, const std::vector<Contact>& C, dou
         if (k.a >= 0) cond_scatter(k.Ja, k.dim, l, &E.minv[6 * (size_t)k.a], &u[6 * (size_t)k.a]);
         cond_scatter(k.Jb, k.dim, l, &E.minv[6 * (size_t)k.b], &u[6 * (size_t)k.b]);
     }
-    int ncol = 0;
-    const std::vector<int> color = color_blocks(B, N, &ncol);
-    std::vector<std::vector<int>> classes(ncol);
-    for (size_t i = 0; i < B.size(); ++i) classes[color[i]].push_back((int)i);
+    // the sweep mode: 0 gauss_seidel (gaussSeidelSweep, :166-182: blocks in order, u_corr updated
+    // after each), 1 jacobi (jacobiSweep, :268-317: every block against the previous sweep's
+    // u_corr, then each body gathers its blocks' increments in block order), 2 colored
+    const int mode = E.cfg.condensed_sweep_mode;
+    std::vector<std::vector<int>> classes;
+    if (mode == 2) {
+        int ncol = 0;
+        const std::vector<int> color = color_blocks(B, N, &ncol);
+        classes.resize(ncol);
+        for (size_t i = 0; i < B.size(); ++i) classes[color[i]].push_back((int)i);
+    } else {
+        classes.resize(1);
+        for (size_t i = 0; i < B.size(); ++i) classes[0].push_back((int)i);
+    }
+    std::vector<std::vector<std::pair<int, int>>> blocks_of(mode == 1 ? N : 0);  // (block, side) in block order
+    if (mode == 1)
+        for (size_t i = 0; i < B.size(); ++i) {
+            if (B[i].a >= 0) blocks_of[B[i].a].push_back({(int)i, 0});
+            blocks_of[B[i].b].push_back({(int)i, 1});
+        }
+    std::vector<double> dl(mode == 1 ? 3 * B.size() : 0), uread;
     const double relax = E.cfg.pj_relaxation, alpha = E.cfg.pj_alpha;
     std::vector<double> uprev = u;
     for (int it = 0; it < E.cfg.pj_max_iterations; ++it) {
-        for (const auto& cls : classes)
-            for (int bi : cls) cond_block_update(B[bi], relax, alpha, E.minv.data(), &lam[3 * (size_t)bi], u.data());
+        if (mode == 1) {
+            uread = u;
+            for (size_t bi = 0; bi < B.size(); ++bi) {
+                dl[3 * bi + 1] = dl[3 * bi + 2] = 0.0;
+                cond_block_lambda(B[bi], relax, alpha, uread.data(), &lam[3 * bi], &dl[3 * bi]);
+            }
+            for (int b = 0; b < N; ++b) {
+                if (blocks_of[b].empty()) continue;
+                double acc[6] = {0, 0, 0, 0, 0, 0};
+                for (const auto& bs : blocks_of[b]) {
+                    const CondBlock& k = B[bs.first];
+                    const double* J = bs.second ? k.Jb : k.Ja;
+                    const double* d = &dl[3 * (size_t)bs.first];
+                    for (int c = 0; c < 6; ++c) {
+                        double t = J[c] * d[0];
+                        for (int q = 1; q < k.dim; ++q) t = t + J[6 * q + c] * d[q];
+                        acc[c] = acc[c] + t;
+                    }
+                }
+                for (int c = 0; c < 6; ++c)
+                    u[6 * (size_t)b + c] = uread[6 * (size_t)b + c] + E.minv[6 * (size_t)b + c] * acc[c];
+            }
+        } else {
+            for (const auto& cls : classes)
+                for (int bi : cls) cond_block_update(B[bi], relax, alpha, E.minv.data(), &lam[3 * (size_t)bi], u.data());
+        }
         res.iters = it + 1;
         res.err = cond_residual(uf, uprev, u, E.cfg.pj_tol_rel, E.cfg.pj_tol_abs);
         if (!std::isfinite(res.err)) {

@@ -48,7 +48,7 @@ typedef struct or_config {
     int32_t pj_rdiag_true_delassus;      /* pj.rdiag_true_delassus */
     int32_t moreau_implicit_gyroscopy;   /* moreau.implicit_gyroscopy */
     int32_t solver_type;                 /* solver.type: 0 projected_jacobi, 1 condensed, 2 projected_gauss_seidel */
-    int32_t condensed_sweep_mode;        /* condensed.sweep_mode: 2 colored (the one restated here) */
+    int32_t condensed_sweep_mode;        /* condensed.sweep_mode: 0 gauss_seidel, 1 jacobi, 2 colored (3 chaotic is not restated) */
     double pj_relaxation;                /* pj.relaxation (condensed and PGS multiply it with pj.alpha) */
     int32_t pad0;
     int32_t status;                      /* out: 0, or 4 when a solve diverged (non-finite residual) */

@@ -1,8 +1,9 @@
-"""The condensed solver's colored sweeps (solver.type=condensed, condensed.sweep_mode=colored) in the
-plain FP64 method, against the oracle's restatement of CondensedSolver::solve
-(condensed_solver.cpp:443-760): the same coloring (the GPU's Jones-Plassmann rounds give the greedy
-Welsh-Powell colors), the same per-block updates in the same color order, the same stop test; the
-results are compared bit for bit. The converged solution also agrees with projected Jacobi's."""
+"""The condensed solver (solver.type=condensed) in the plain FP64 method, against the oracle's restatement
+of CondensedSolver::solve (condensed_solver.cpp:443-760), for its three deterministic sweep modes:
+colored (the GPU's Jones-Plassmann rounds give the greedy Welsh-Powell colors), gauss_seidel (the
+sequential order, run through the per-body chains of blocks) and jacobi (two passes). The same
+per-block updates in the same order and the same stop test: the results are compared bit for bit.
+The converged solution also agrees with projected Jacobi's."""
 import numpy as np
 import pytest
 
@@ -112,3 +113,27 @@ def test_condensed_agrees_with_projected_jacobi_at_convergence():
     t_cd, t_pj = cd["lambda"][:, 1:], pj["lambda"][:, 1:]
     if np.abs(t_pj).max() > 0:
         assert np.sum(t_cd * t_pj) < 0
+
+
+@pytest.mark.parametrize("mode", ["gauss_seidel", "jacobi"])
+def test_condensed_sequential_and_jacobi_modes_bit_identical(oracle_mod, mode):
+    s = scenes.generate("pile_1k", scale=0.3)
+    cfg = scenes.config_for("pile_1k", **dict(COND, **{"condensed.sweep_mode": mode}))
+    eng, _ = run_pair(oracle_mod, s, cfg, 150, every=50)
+    st = eng.stats()
+    assert st["num_contacts"] > 50 and 1 < st["iterations"] < 5000
+    # a frictionless subset, relaxation and alpha below 1, implicit gyroscopy
+    s2 = scenes.generate("pile_1k", scale=0.08)
+    s2["mu"][::3] = 0.0
+    c2 = scenes.config_for("pile_1k", **dict(COND, **{"condensed.sweep_mode": mode, "pj.relaxation": 0.8,
+                                                      "pj.alpha": 0.9, "moreau.implicit_gyroscopy": True}))
+    run_pair(oracle_mod, s2, c2, 40, every=20)
+
+
+def test_condensed_default_mode_is_sequential_gauss_seidel():
+    # condensed.sweep_mode defaults to gauss_seidel (config.hpp:118), which now runs as is
+    s = scenes.generate("pile_1k", scale=0.05)
+    e = PhysicsEngine(scenes.config_for("pile_1k", **{"solver.type": "condensed", "pj.tol_abs": 1e-6,
+                                                      "pj.tol_rel": 1e-6})).load_scene(s)
+    e.step(300)
+    assert np.isfinite(e.state()["vel"]).all() and e.stats()["num_contacts"] > 0 and e.stats()["levels"] >= 1

@@ -96,10 +96,10 @@ def test_config_rejects_other_solvers(cdxlib):
     assert c.get("solver_type") == 1 and c.get("condensed_sweep_mode") == 0  # gauss_seidel by default
     assert Config({"condensed.sweep_mode": "colored"}).get("condensed_sweep_mode") == 2
     assert Config({"condensed.sweep_mode": "nonsense"}).get("condensed_sweep_mode") == 0
-    # the GPU runs the condensed solver's colored sweeps in the plain FP64 method: other sweep modes,
-    # the split form and its accelerated loops are refused before any device call
-    for bad in ({"solver.type": "condensed"},
-                {"solver.type": "condensed", "condensed.sweep_mode": "jacobi"},
+    # the GPU runs the condensed solver's gauss_seidel, jacobi and colored sweeps in the plain FP64
+    # method: the chaotic mode, the split form and its accelerated loops are refused before any
+    # device call
+    for bad in ({"solver.type": "condensed", "condensed.sweep_mode": "chaotic"},
                 {"solver.type": "condensed", "condensed.sweep_mode": "colored", "gpu.precision": "split"},
                 {"solver.type": "condensed", "condensed.sweep_mode": "colored", "pj.nesterov": True},
                 # projected Gauss-Seidel: its plain loop in the plain FP64 method
