@@ -185,10 +185,10 @@ def with_state(scene, state):
     return s
 
 
-def settle_gpu(scene, cfg, steps: int, precision="split"):
+def settle_gpu(scene, cfg, steps: int, precision="split", extra=None):
     """Steps a generated scene with the GPU engine (input synthesis for scenes without a file)."""
     from cardillocxx_gb300 import PhysicsEngine
-    e = PhysicsEngine(dict(cfg, **{"gpu.precision": precision})).load_scene(scene)
+    e = PhysicsEngine(dict(cfg, **{"gpu.precision": precision}, **(extra or {}))).load_scene(scene)
     t = time.time()
     done = 0
     while done < steps:
@@ -574,7 +574,13 @@ def run_cdx(a):
         input_name = f"generated, settled {settle} steps by the split form on the GPU"
         desc = f"seeded {a.scene} (scale {a.scale}) {input_name}"
         if settle > 0:
-            state, mem = settle_gpu(scene, cfg, settle, "split")
+            # a pinned shape runs the settle too (a profiler then counts its launches exactly)
+            pin = None
+            if a.sweep_variant is not None:
+                names = PhysicsEngine.split_variants()
+                pin = {"gpu.sweep_variant": names.index(a.sweep_variant) if a.sweep_variant in names
+                       else int(a.sweep_variant)}
+            state, mem = settle_gpu(scene, cfg, settle, "split", pin)
             scene = with_state(scene, state)
     N = scene["pos"].shape[0]
     shared = shared_config(a, scene, cfg, input_name)
