@@ -312,6 +312,7 @@ static int init_split(Engine& E) {
     for (int k = 0; k < SPLIT_NACC; ++k)
         if ((st = salloc(E, (void**)&b.acc[k], sizeof(float4) * 2 * n1, "split bodies"))) return st;
     if ((st = salloc(E, (void**)&b.vn4, sizeof(float4) * 2 * n1, "split bodies"))) return st;
+    if ((st = salloc(E, (void**)&b.mat4, sizeof(float4) * n1, "split bodies"))) return st;
     if ((st = salloc(E, (void**)&b.vfree, sizeof(double) * 6 * n1, "split bodies"))) return st;
     if ((st = salloc(E, (void**)&b.acc64, sizeof(double) * 6 * n1, "split bodies"))) return st;
     if ((st = salloc(E, (void**)&b.origin, sizeof(double) * 3 * nsc, "split scenes"))) return st;
@@ -350,6 +351,14 @@ static int init_split(Engine& E) {
     }
     for (int i = 0; i < N && !b.has_restitution; ++i)
         if (B[(size_t)BF_RN * N + i] > 0 || B[(size_t)BF_RT * N + i] > 0) b.has_restitution = 1;
+    if (N) {
+        std::vector<float4> mat(N);
+        for (int i = 0; i < N; ++i)
+            mat[i] = make_float4((float)B[(size_t)BF_MU * N + i], (float)B[(size_t)BF_RN * N + i],
+                                 (float)B[(size_t)BF_RT * N + i], 0.f);
+        if ((st = E.cuda_check(cudaMemcpy(b.mat4, mat.data(), sizeof(float4) * N, cudaMemcpyHostToDevice), "materials")))
+            return st;
+    }
     if (Ss > 0) {
         std::vector<double> St((size_t)SF_COUNT * Ss);
         if ((st = E.cuda_check(cudaMemcpy(St.data(), E.sc.St, sizeof(double) * St.size(), cudaMemcpyDeviceToHost), "statics"))) return st;
@@ -439,7 +448,7 @@ int Engine::step_split() {
         for (int v = 0; v < split_num_variants(); ++v) {
             CoopPlan probe;
             if (split_variant_is_coop(v))
-                sweeps += coop_plan(*this, v, n, &probe) ? 8 : 0;
+                sweeps += coop_plan(*this, v, n, &probe) ? 12 : 0;
             else if (!split_variant_is_scenes(v))
                 sweeps += 2;
         }
@@ -649,12 +658,12 @@ int Engine::step_split() {
         solved = true;
     }
     const int nv = split_num_variants();
-    // sweeps the autotuner spends: two per streaming shape, eight per feasible cooperative one
+    // sweeps the autotuner spends: two per streaming shape, twelve per feasible cooperative one
     int tune_sweeps = 0;
     for (int v = 0; v < nv; ++v) {
         CoopPlan probe;
         if (split_variant_is_coop(v))
-            tune_sweeps += (S->nc > 0 && coop_plan(*this, v, S->nc, &probe)) ? 8 : 0;
+            tune_sweeps += (S->nc > 0 && coop_plan(*this, v, S->nc, &probe)) ? 12 : 0;
         else if (!split_variant_is_scenes(v))
             tune_sweeps += 2;
     }
@@ -673,12 +682,14 @@ int Engine::step_split() {
             double t = 0;
             if (split_variant_is_scenes(v)) continue;
             if (split_variant_is_coop(v)) {
-                // two launches of 2 and 6 sweeps: their difference is the cost of a sweep, the rest
-                // (loading and storing the contacts) is paid once per solve of maxit sweeps
+                // two launches of 2 and 10 sweeps: their difference is the cost of a sweep, the rest
+                // (loading and storing the contacts) is paid once per solve of maxit sweeps (the
+                // shapes differ by a few percent a sweep: 8 sweeps of difference keep that above
+                // the noise of one measurement)
                 CoopPlan plan;
                 if (!coop_plan(*this, v, S->nc, &plan)) continue;
                 float ms[2] = {0.f, 0.f};
-                const int ks[2] = {2, 6};
+                const int ks[2] = {2, 10};
                 for (int r = 0; r < 2; ++r) {
                     cudaEventRecord(S->tev[0], stream);
                     st = launch_coop(*this, sb, gen, v, plan, maxit, (float)cfg.gpu_residual_tol, ks[r], stream);

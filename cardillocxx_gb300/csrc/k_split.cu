@@ -327,7 +327,8 @@ __device__ __forceinline__ void finish_contact32(const Scene& sc, SplitBuf& sb, 
         vna = f3(sb.vn4[2 * a]);
         wna = f3(sb.vn4[2 * a + 1]);
     }
-    float mu = combine_mu32(P.combine, mu_a, (float)sc.bf(BF_MU)[b]);
+    const float4 mb = sb.mat4[b];
+    float mu = combine_mu32(P.combine, mu_a, mb.x);
     if (!P.friction_enable || !(mu > 0.f)) mu = 0.f;
     float3 t1, t2;
     frame32(n, t1, t2);
@@ -340,8 +341,8 @@ __device__ __forceinline__ void finish_contact32(const Scene& sc, SplitBuf& sb, 
         cb[1] = -dot(t1, vw);
         cb[2] = -dot(t2, vw);
     }
-    const float eN = fminf(fmaxf(0.f, rn_a), fmaxf(0.f, (float)sc.bf(BF_RN)[b]));
-    const float eT = fminf(fmaxf(0.f, rt_a), fmaxf(0.f, (float)sc.bf(BF_RT)[b]));
+    const float eN = fminf(fmaxf(0.f, rn_a), fmaxf(0.f, mb.y));
+    const float eT = fminf(fmaxf(0.f, rt_a), fmaxf(0.f, mb.z));
     float4 bias = make_float4(cb[0], cb[1], cb[2], 0.f);
     if (eN > 0.f || eT > 0.f) {
         const float3 dv = f3(sb.vn4[2 * b]) - vna;
@@ -488,8 +489,8 @@ __global__ void k_s_pairs(Scene sc, Grid gr, SplitBuf sb, const uint32_t* cell_b
         plo = pns + P.prev_poff[i];
         phi = pns + P.prev_poff[i + 1];
     }
-    const float mu_a = (float)sc.bf(BF_MU)[i];
-    const float rn_a = (float)sc.bf(BF_RN)[i], rt_a = (float)sc.bf(BF_RT)[i];
+    const float4 ma = sb.mat4[i];
+    const float mu_a = ma.x, rn_a = ma.y, rt_a = ma.z;
     for (int k = 0; k < cnt; ++k) {
         const int j = list[k];
         const float4 pj = sb.pos4[j];
@@ -853,7 +854,7 @@ __device__ __forceinline__ unsigned long long global_ns() {
 // a block can run one barrier ahead of a slow reader, never two. The wait is bounded: after
 // COOP_WAIT_NS, or once another block has given up, the block sets *err and returns false.
 constexpr unsigned long long COOP_WAIT_NS = 200000000ull;  // 0.2 s
-constexpr int COOP_MAX_GRID = 256;                         // records a lane reads: COOP_MAX_GRID / 32
+constexpr int COOP_MAX_GRID = 320;                         // records a lane reads: COOP_MAX_GRID / 32
 // Arrival half: publish the block's maxima and add one to the counter (after every thread's
 // writes of the sweep, through __syncthreads and a release reduction).
 __device__ __forceinline__ void grid_arrive(unsigned* ctr, float2* recs, unsigned epoch, bool reduce, float maxd,
@@ -867,8 +868,8 @@ __device__ __forceinline__ void grid_arrive(unsigned* ctr, float2* recs, unsigne
 }
 // Waiting half: thread 0 waits (bounded, acquire loads) for every block's arrival, then warp 0
 // reduces the records.
-__device__ __forceinline__ bool grid_wait_max(unsigned* ctr, float2* recs, unsigned epoch, int32_t* err, bool reduce,
-                                              float& maxd, float& maxl, unsigned long long wait_ns) {
+__device__ __forceinline__ bool grid_wait_max(unsigned* ctr, float2* recs, unsigned epoch, unsigned base, int32_t* err,
+                                              bool reduce, float& maxd, float& maxl, unsigned long long wait_ns) {
     __shared__ float s_md, s_ml;
     __shared__ int s_ok;
     float2* bank = recs + (size_t)(epoch & 1u) * SPLIT_MAX_PARTS;
@@ -876,7 +877,7 @@ __device__ __forceinline__ bool grid_wait_max(unsigned* ctr, float2* recs, unsig
         const unsigned FULL = 0xffffffffu;
         int ok = 1;
         if (threadIdx.x == 0) {
-            const unsigned target = epoch * gridDim.x;
+            const unsigned target = base + epoch * gridDim.x;
             const unsigned long long t0 = global_ns();
             while ((int)(ld_acquire(ctr) - target) < 0) {
                 if (ld_acquire(reinterpret_cast<const unsigned*>(err)) != 0u || global_ns() - t0 > wait_ns) {
@@ -934,8 +935,10 @@ __device__ __forceinline__ bool grid_wait_max(unsigned* ctr, float2* recs, unsig
 // HYB: a block's range may hold more contacts than its shared memory (cpb); the first cpb stay in
 // shared memory and the rest are read from memory every sweep (records through the read-only
 // path, impulses through L2), so problems of any size run as one launch.
-template <int NTH, int UNROLL, int AGG, int HYB>
-__global__ void __launch_bounds__(NTH, 1) k_s_solve_coop(SplitBuf sb, int gen, float alpha, int max_iter, float tol,
+// MINB > 1: that many blocks an SM (more threads an SM at fewer registers a thread, so a settled
+// pile's ~3,100 contacts an SM take three passes instead of four)
+template <int NTH, int UNROLL, int AGG, int HYB, int MINB = 1>
+__global__ void __launch_bounds__(NTH, MINB) k_s_solve_coop(SplitBuf sb, int gen, float alpha, int max_iter, float tol,
                                                          int cpb, int bpb, int vf_smem, int max_sweeps,
                                                          int check_every, unsigned long long wait_ns) {
     extern __shared__ float4 smem[];
@@ -947,6 +950,9 @@ __global__ void __launch_bounds__(NTH, 1) k_s_solve_coop(SplitBuf sb, int gen, f
     float4* s_vf = smem + 3 * cpb;  // free velocities of the block's bodies
     const int it0 = *(volatile int32_t*)&ss->iters;
     unsigned epoch = *(volatile unsigned*)&ss->bar_base;
+    // arrivals so far this step: the launches before this one may have had other grid sizes (the
+    // autotuner's trials), so the counter's target is counted from them (modulo 2^32)
+    const unsigned bbase = *(volatile unsigned*)&ss->bar_arr - epoch * gridDim.x;
     const int nc = *sb.nc_dev, N = sb.N, tid = threadIdx.x;
     if (!HYB && (int64_t)nc > (int64_t)cpb * gridDim.x) {
         // planned from an estimate of the contact count that fell short: every block returns (no
@@ -1040,7 +1046,7 @@ __global__ void __launch_bounds__(NTH, 1) k_s_solve_coop(SplitBuf sb, int gen, f
             const float4 w0 = vf_smem ? s_vf[2 * i + 1] : ldg4(&sb.vel4[2 * (bb + i) + 1]);
             stcg_body(&Aclr[2 * (bb + i)], v0, w0);
         }
-        if (!grid_wait_max(&ss->bar, sb.recs, epoch, &ss->err, check, maxd2, maxl, wait_ns)) return;
+        if (!grid_wait_max(&ss->bar, sb.recs, epoch, bbase, &ss->err, check, maxd2, maxl, wait_ns)) return;
         ++it;
         if (check) {
             r = sweep_residual(maxd2, maxl);
@@ -1057,6 +1063,7 @@ __global__ void __launch_bounds__(NTH, 1) k_s_solve_coop(SplitBuf sb, int gen, f
         ss->res_last = r;
         ss->done = stop;
         ss->bar_base = epoch;
+        ss->bar_arr = bbase + epoch * gridDim.x;
     }
 }
 
@@ -1094,8 +1101,8 @@ __device__ __forceinline__ void grid_arrive_sum(unsigned* ctr, double2* sums, un
     __syncthreads();
     if (threadIdx.x == 0) asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(ctr) : "memory");
 }
-__device__ __forceinline__ bool grid_wait_sum(unsigned* ctr, double2* sums, unsigned epoch, int32_t* err, double& a,
-                                              double& b, unsigned long long wait_ns) {
+__device__ __forceinline__ bool grid_wait_sum(unsigned* ctr, double2* sums, unsigned epoch, unsigned base, int32_t* err,
+                                              double& a, double& b, unsigned long long wait_ns) {
     __shared__ double s_a, s_b;
     __shared__ int s_ok;
     double2* bank = sums + (size_t)(epoch & 1u) * SPLIT_MAX_PARTS;
@@ -1103,7 +1110,7 @@ __device__ __forceinline__ bool grid_wait_sum(unsigned* ctr, double2* sums, unsi
         const unsigned FULL = 0xffffffffu;
         int ok = 1;
         if (threadIdx.x == 0) {
-            const unsigned target = epoch * gridDim.x;
+            const unsigned target = base + epoch * gridDim.x;
             const unsigned long long t0 = global_ns();
             while ((int)(ld_acquire(ctr) - target) < 0) {
                 if (ld_acquire(reinterpret_cast<const unsigned*>(err)) != 0u || global_ns() - t0 > wait_ns) {
@@ -1213,6 +1220,9 @@ __global__ void __launch_bounds__(NTH, 1) k_s_solve_coop_loop(SplitBuf sb, int g
     float4* s_vf = smem + (NES ? 4 : 3) * cpb;    // free velocities of the block's bodies
     const int it0 = *(volatile int32_t*)&ss->iters;
     unsigned epoch = *(volatile unsigned*)&ss->bar_base;
+    // arrivals so far this step: the launches before this one may have had other grid sizes (the
+    // autotuner's trials), so the counter's target is counted from them (modulo 2^32)
+    const unsigned bbase = *(volatile unsigned*)&ss->bar_arr - epoch * gridDim.x;
     const int nc = *sb.nc_dev, N = sb.N, tid = threadIdx.x;
     if (!HYB && (int64_t)nc > (int64_t)cpb * gridDim.x) {
         if (blockIdx.x == 0 && tid == 0) ss->err = 4;
@@ -1315,7 +1325,7 @@ __global__ void __launch_bounds__(NTH, 1) k_s_solve_coop_loop(SplitBuf sb, int g
                 stcg_body(&Clr[2 * (bb + i)], v0, w0);
             }
         }
-        if (!grid_wait_max(&ss->bar, sb.recs, epoch, &ss->err, check, maxd2, maxl, wait_ns)) return;
+        if (!grid_wait_max(&ss->bar, sb.recs, epoch, bbase, &ss->err, check, maxd2, maxl, wait_ns)) return;
         if (velchk) {
             // the velocity-increment residual between the new velocities and those the sweep read
             // (and Nesterov's restart dot product), over the block's own bodies, then over the grid
@@ -1334,7 +1344,7 @@ __global__ void __launch_bounds__(NTH, 1) k_s_solve_coop_loop(SplitBuf sb, int g
             }
             block_sum2d(e, d);
             grid_arrive_sum(&ss->bar, sb.sums, ++epoch, e, d);
-            if (!grid_wait_sum(&ss->bar, sb.sums, epoch, &ss->err, e, d, wait_ns)) return;
+            if (!grid_wait_sum(&ss->bar, sb.sums, epoch, bbase, &ss->err, e, d, wait_ns)) return;
             if (tid == 0) {
                 L.verr = (1.0 / sqrt((double)la.nv)) * sqrt(e);
                 L.dot = d;
@@ -1418,7 +1428,7 @@ __global__ void __launch_bounds__(NTH, 1) k_s_solve_coop_loop(SplitBuf sb, int g
                 L.ixk = t;
             }
             float u0, u1;
-            if (!grid_wait_max(&ss->bar, sb.recs, epoch, &ss->err, false, u0, u1, wait_ns)) return;
+            if (!grid_wait_max(&ss->bar, sb.recs, epoch, bbase, &ss->err, false, u0, u1, wait_ns)) return;
         }
     }
     for (int i = tid; i < ncs; i += NTH) {
@@ -1430,6 +1440,7 @@ __global__ void __launch_bounds__(NTH, 1) k_s_solve_coop_loop(SplitBuf sb, int g
         ss->res_last = r;
         ss->done = stop;
         ss->bar_base = epoch;
+        ss->bar_arr = bbase + epoch * gridDim.x;
         ss->vel_err = L.verr;
         if (NES) {
             ss->final_acc = L.ix1;
@@ -1654,6 +1665,7 @@ __global__ void k_s_reset(SplitBuf sb) {
     ss->err = 0;
     ss->bar = 0u;
     ss->bar_base = 0u;
+    ss->bar_arr = 0u;
     ss->final_acc = -1;
     ss->iters_sum = 0ull;
     ss->nonfinite = 0;
@@ -1788,6 +1800,7 @@ __global__ void k_s_residual(Scene sc, SplitBuf sb, int gen, double alpha, int f
     const int nc = *sb.nc_dev;
     const int N = sc.N;
     double maxd = 0.0, maxl = 0.0;
+    float maxlf = 0.f;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
         const float4 r0 = sb.rec0[c], r1 = sb.rec1[c];
         const int2 ab = make_int2(__float_as_int(r1.z), __float_as_int(r1.w));
@@ -1838,9 +1851,12 @@ __global__ void k_s_residual(Scene sc, SplitBuf sb, int gen, double alpha, int f
                 cb[1] = -(t1[0] * vw[0] + t1[1] * vw[1] + t1[2] * vw[2]);
                 cb[2] = -(t2[0] * vw[0] + t2[1] * vw[1] + t2[2] * vw[2]);
             }
-            eN = fmin(fmax(0.0, sc.sf(SF_RN)[s]), fmax(0.0, sc.bf(BF_RN)[ab.y]));
-            eT = fmin(fmax(0.0, sc.sf(SF_RT)[s]), fmax(0.0, sc.bf(BF_RT)[ab.y]));
-        } else {
+            if (sb.has_restitution) {
+                eN = fmin(fmax(0.0, sc.sf(SF_RN)[s]), fmax(0.0, sc.bf(BF_RN)[ab.y]));
+                eT = fmin(fmax(0.0, sc.sf(SF_RT)[s]), fmax(0.0, sc.bf(BF_RT)[ab.y]));
+            }
+        } else if (sb.has_restitution) {
+            // (a scene without restitution skips these FP64 min/max: the FP64 pipe bounds this kernel)
             eN = fmin(fmax(0.0, sc.bf(BF_RN)[ab.x]), fmax(0.0, sc.bf(BF_RN)[ab.y]));
             eT = fmin(fmax(0.0, sc.bf(BF_RT)[ab.x]), fmax(0.0, sc.bf(BF_RT)[ab.y]));
         }
@@ -1892,8 +1908,10 @@ __global__ void k_s_residual(Scene sc, SplitBuf sb, int gen, double alpha, int f
         }
         const double d0 = ln - lo[0], d1 = lt1 - lo[1], d2 = lt2 - lo[2];
         maxd = fmax(maxd, d0 * d0 + d1 * d1 + d2 * d2);  // squared; the root is taken once at the end
-        maxl = fmax(maxl, fmax(fabs(lo[0]), fmax(fabs(lo[1]), fabs(lo[2]))));
+        // max |lambda| of FP32 impulses: exact in FP32, converted once
+        maxlf = fmaxf(maxlf, fmaxf(fabsf(l.x), fmaxf(fabsf(l.y), fabsf(l.z))));
     }
+    maxl = (double)maxlf;
     (void)friction_enable;
     (void)combine;
     block_max2(maxd, maxl);
@@ -1990,11 +2008,16 @@ struct CoopVariant {
     int nth, unroll, agg, hyb;
     int per_sm;    // resident blocks per SM with the full shared-memory budget (0 = not queried)
     int smem_max;  // dynamic shared memory budget of one block
+    int minb;      // blocks an SM the shape is built for (its shared memory is split between them)
 };
 static CoopVariant g_coop[] = {
-    {k_s_solve_coop<1024, 1, 2, 0>, 1024, 1, 2, 0, 0, 0},
-    {k_s_solve_coop<512, 2, 2, 0>, 512, 2, 2, 0, 0, 0},
-    {k_s_solve_coop<1024, 1, 2, 1>, 1024, 1, 2, 1, 0, 0},
+    {k_s_solve_coop<1024, 1, 2, 0>, 1024, 1, 2, 0, 0, 0, 1},
+    {k_s_solve_coop<512, 2, 2, 0>, 512, 2, 2, 0, 0, 0, 1},
+    {k_s_solve_coop<1024, 1, 2, 1>, 1024, 1, 2, 1, 0, 0, 1},
+    // two blocks an SM of 576 threads at 56 registers: 1,152 threads an SM instead of 1,024, so the
+    // settled 200k pile's 3,133 contacts an SM take three passes instead of four (9.9 against 10.4 us
+    // a sweep)
+    {k_s_solve_coop<576, 1, 2, 0, 2>, 576, 1, 2, 0, 0, 0, 2},
 };
 constexpr int N_COOP = sizeof(g_coop) / sizeof(g_coop[0]);
 // The same shapes under the reference's loop controls (1024 threads, one contact per thread and
@@ -2041,8 +2064,11 @@ const char* split_variant_name(int v) {
             snprintf(names[v], sizeof(names[v]), "sweep-u%d-t%d-b%d-g%d", cv.unroll, cv.nth, cv.minb, cv.agg);
         } else if (v < N_STREAM + N_COOP) {
             const CoopVariant& cv = g_coop[v - N_STREAM];
-            snprintf(names[v], sizeof(names[v]), cv.hyb ? "coop-hyb-t%d-u%d-g%d" : "coop-t%d-u%d-g%d", cv.nth,
-                     cv.unroll, cv.agg);
+            if (cv.minb > 1)
+                snprintf(names[v], sizeof(names[v]), "coop-t%d-u%d-g%d-b%d", cv.nth, cv.unroll, cv.agg, cv.minb);
+            else
+                snprintf(names[v], sizeof(names[v]), cv.hyb ? "coop-hyb-t%d-u%d-g%d" : "coop-t%d-u%d-g%d", cv.nth,
+                         cv.unroll, cv.agg);
         } else {
             const ScenesVariant& cv = g_scenes[v - N_STREAM - N_COOP];
             snprintf(names[v], sizeof(names[v]), "scenes-t%d-c%d", cv.nth, cv.csm);
@@ -2104,14 +2130,18 @@ int split_contact_blocks(int vi, int64_t n, int sms) {
 // velocities (32 B a body) are kept there too when they also fit.
 // the shared-memory budget and residency of a cooperative kernel, queried once
 template <class K>
-static bool coop_setup(K kernel, int nth, int* per_sm, int* smem_max) {
+static bool coop_setup(K kernel, int nth, int* per_sm, int* smem_max, int minb = 1) {
     if (*per_sm == 0) {
-        int dev = 0, optin = 0;
+        int dev = 0, optin = 0, per_sm_smem = 0, reserved = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        cudaDeviceGetAttribute(&per_sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+        cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
         cudaFuncAttributes fa;
         if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess) return false;
         *smem_max = optin - (int)fa.sharedSizeBytes;
+        // several blocks an SM share its shared memory
+        if (minb > 1) *smem_max = std::min(*smem_max, per_sm_smem / minb - reserved - (int)fa.sharedSizeBytes);
         if (*smem_max <= 0 ||
             cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, *smem_max) != cudaSuccess)
             return false;
@@ -2134,7 +2164,7 @@ bool split_coop_plan(int v, int64_t nc, int64_t nbodies, int sms, CoopPlan* p, i
         per_sm = lv.per_sm;
         smem_max = lv.smem_max;
     } else {
-        if (!coop_setup(cv.kernel, cv.nth, &cv.per_sm, &cv.smem_max)) return false;
+        if (!coop_setup(cv.kernel, cv.nth, &cv.per_sm, &cv.smem_max, cv.minb)) return false;
         per_sm = cv.per_sm;
         smem_max = cv.smem_max;
     }

@@ -12,7 +12,7 @@ struct SplitScalars {
     int32_t done;
     int32_t iters;
     unsigned int blocks_done;  // completion counter of the body pass (last block runs the check)
-    int32_t pad1;
+    unsigned int bar_arr;      // cooperative solve: arrivals at the grid barrier counter so far this step
     unsigned int maxd;  // bits of max ||dlambda_c|| (FP32, non-negative)
     unsigned int maxl;  // bits of max |lambda|
     float res_last;
@@ -99,6 +99,8 @@ struct SplitBuf {
     // (read in sweep k - 1, next added into in sweep k + 2) to the free velocities
     float4* acc[SPLIT_NACC] = {nullptr, nullptr, nullptr, nullptr};
     float4* vn4 = nullptr;    // 2N: pre-solve velocities (v, omega_world)
+    float4* mat4 = nullptr;   // N: (mu, normal restitution, tangential restitution, 0) in FP32, constant per
+                              // body (the narrow phase reads them without FP64 conversions)
     double* vfree = nullptr;  // 6N FP64 free velocities (world frame)
     double* acc64 = nullptr;  // 6N FP64 W^T lambda, then final velocities
     double* origin = nullptr; // 3 per scene
