@@ -189,14 +189,15 @@ struct CondBufs {
 // make a sweep sequential
 struct PgsBufs {
     int64_t cap = 0;
-    int32_t* pred = nullptr;      // 2*cap: previous block of body A / body B in row order (-1: none)
-    int32_t* done = nullptr;      // cap: the last sweep a block finished (-1 before the first)
-    uint32_t* by_rank = nullptr;  // cap: contact of each rank in row order
+    int32_t* pred = nullptr;      // 2*cap: previous block of body A / body B in sweep order (-1: none)
+    int32_t* succ = nullptr;      // 2*cap: next block of body A / body B in sweep order (-1: none)
+    int32_t* lstart = nullptr;    // cap: first position of each level in the level order
+    int32_t* lend = nullptr;      // cap: one past its last
     unsigned* bar = nullptr;      // grid barrier counter
     int32_t* err = nullptr;       // a wait ran out (1 barrier, 2 predecessor)
     int32_t* stop = nullptr;      // the stop decision of the last sweep
-    int32_t* lev = nullptr;       // cap: level of each block (longest chain of predecessors)
-    int32_t* rflag = nullptr;     // 3: change flags of the level rounds
+    int32_t* lev = nullptr;       // cap: the level pass's count of unfinished predecessors a block
+    int32_t* rflag = nullptr;     // 3: [0] blocks placed by the level pass
     int32_t* maxlev = nullptr;    // the largest level
 };
 
@@ -250,18 +251,17 @@ void launch_cond_final(const Scene& sc, Contacts& C, int gen, int nc, const Cond
 // launch (returns the launch's cudaError_t)
 void launch_pgs_setup(const Scene& sc, Contacts& C, int gen, int nc, int warmstart, CondBufs& B, const Incidence& inc,
                       PgsBufs& P, cudaStream_t s);
-// levels of the blocks and the sort keys (level) and values (contact) in row order
-int launch_pgs_levels(const PgsBufs& P, int nc, uint32_t* keys, uint32_t* vals, unsigned long long wait_ns,
-                      cudaStream_t s);
-// order: the contacts sorted by level
+// levels of the blocks: the blocks level by level into `order`, each level's range in P.lstart /
+// P.lend, the largest level in P.maxlev
+int launch_pgs_levels(const PgsBufs& P, int nc, uint32_t* order, unsigned long long wait_ns, cudaStream_t s);
+// order: the contacts sorted by level; nlev levels, their ranges in P.lstart / P.lend
 // condensed: run the condensed solver's block update (its sequential gauss_seidel sweep mode)
-int launch_pgs_solve(const Scene& sc, const Contacts& C, int nc, const CondBufs& B, const PgsBufs& P,
+int launch_pgs_solve(const Scene& sc, const Contacts& C, int nlev, const CondBufs& B, const PgsBufs& P,
                      const uint32_t* order, double relax, double alpha, double tol_rel, double tol_abs, int max_iter,
                      DevScalars* ds, unsigned long long wait_ns, cudaStream_t s, int condensed = 0);
-// the per-body chains of blocks (predecessors) and the blocks in sweep order: W's row order, or
-// contact order (contact_order = 1, the condensed solver's)
-void launch_pgs_links(const Scene& sc, const Contacts& C, int nc, const Incidence& inc, PgsBufs& P,
-                      int contact_order, cudaStream_t s);
+// the per-body chains of blocks (predecessors and successors) from incidence lists in sweep order
+// (W's row order for projected Gauss-Seidel, contact order for the condensed solver)
+void launch_pgs_links(const Scene& sc, int nc, const Incidence& inc, PgsBufs& P, cudaStream_t s);
 // condensed solver, Jacobi sweep (both passes)
 void launch_cond_jacobi(const Scene& sc, const Contacts& C, int nc, const CondBufs& B, const Incidence& inc,
                         double relax, double alpha, double* u, const DevScalars* ds, cudaStream_t s);

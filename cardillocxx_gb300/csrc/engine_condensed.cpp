@@ -37,7 +37,9 @@ int Engine::ensure_cond() {
     if ((st = dalloc((void**)&B.uf, sizeof(double) * 6 * N, "condensed"))) return st;
     if ((st = dalloc((void**)&B.u, sizeof(double) * 6 * N, "condensed"))) return st;
     if ((st = dalloc((void**)&B.up, sizeof(double) * 6 * N, "condensed"))) return st;
-    if ((st = dalloc((void**)&B.part, sizeof(double) * std::max(cond_chunks(N), 1), "condensed"))) return st;
+    // the chunk sums, then the group sums of the fixed three-level order
+    if ((st = dalloc((void**)&B.part, sizeof(double) * (cond_chunks(N) + cond_chunks(N) / 64 + 2), "condensed")))
+        return st;
     if ((st = dalloc((void**)&B.flags, sizeof(int32_t) * 4, "condensed"))) return st;
     if ((st = dalloc((void**)&B.err, sizeof(double), "condensed"))) return st;
     uint32_t** u32[] = {&B.kin, &B.vin, &B.kout, &B.vout};
@@ -173,25 +175,21 @@ int Engine::solve_condensed_gs() {
     CondBufs& B = cond;
     int st;
     if ((st = ensure_pgs())) return st;
-    launch_pgs_links(sc, C, nc, inc, pgs, 1, stream);
+    launch_pgs_links(sc, nc, inc, pgs, stream);
     launch_cond_copy(6 * sc.N, B.u, B.up, ds, stream);
     launches += 2;
     const unsigned long long wait_ns = cfg.gpu_coop_wait_ns > 0 ? (unsigned long long)cfg.gpu_coop_wait_ns : 0ull;
-    if ((st = cuda_check((cudaError_t)launch_pgs_levels(pgs, nc, B.kin, B.vin, wait_ns, stream), "levels launch")))
+    if ((st = cuda_check((cudaError_t)launch_pgs_levels(pgs, nc, B.vout, wait_ns, stream), "levels launch")))
         return st;
     ++launches;
     int32_t hl[2] = {0, 0};
     cudaMemcpyAsync(&hl[0], pgs.maxlev, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
     cudaMemcpyAsync(&hl[1], pgs.err, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
     if ((st = cuda_check(cudaStreamSynchronize(stream), "condensed levels"))) return st;
+    if (hl[1] == 3) return fail(CDX_ERR_STATE, "condensed levels: the block chains made no progress");
     if (hl[1]) return fail(CDX_ERR_TIMEOUT, "condensed levels: a grid barrier wait ran out (gpu.coop_wait_ns)");
     last_levels = hl[0] + 1;
-    int bits = 1;
-    while (bits < 32 && (hl[0] >> bits) != 0) ++bits;
-    if ((st = cuda_check(sort_pairs(tmp, tmp_bytes, B.kin, B.kout, B.vin, B.vout, nc, bits, stream), "sort levels")))
-        return st;
-    launches += 4;
-    if ((st = cuda_check((cudaError_t)launch_pgs_solve(sc, C, nc, B, pgs, B.vout, cfg.pj_relaxation, cfg.pj_alpha,
+    if ((st = cuda_check((cudaError_t)launch_pgs_solve(sc, C, last_levels, B, pgs, B.vout, cfg.pj_relaxation, cfg.pj_alpha,
                                                        cfg.pj_tol_rel, cfg.pj_tol_abs, cfg.pj_max_iterations, ds,
                                                        wait_ns, stream, 1),
                          "condensed sweep launch")))

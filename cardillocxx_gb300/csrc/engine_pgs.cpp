@@ -16,14 +16,15 @@ int Engine::ensure_pgs() {
     PgsBufs& P = pgs;
     const int64_t cap = std::max<int64_t>(C.cap, 1);
     if (P.cap == cap) return CDX_OK;
-    void* old[] = {P.pred, P.done, P.by_rank, P.bar, P.err, P.stop, P.lev, P.rflag, P.maxlev};
+    void* old[] = {P.pred, P.succ, P.lstart, P.lend, P.bar, P.err, P.stop, P.lev, P.rflag, P.maxlev};
     for (void* p : old)
         if (p) dfree(p);
     P = PgsBufs{};
     int st;
     if ((st = dalloc((void**)&P.pred, sizeof(int32_t) * 2 * cap, "pgs"))) return st;
-    if ((st = dalloc((void**)&P.done, sizeof(int32_t) * cap, "pgs"))) return st;
-    if ((st = dalloc((void**)&P.by_rank, sizeof(uint32_t) * cap, "pgs"))) return st;
+    if ((st = dalloc((void**)&P.succ, sizeof(int32_t) * 2 * cap, "pgs"))) return st;
+    if ((st = dalloc((void**)&P.lstart, sizeof(int32_t) * cap, "pgs"))) return st;
+    if ((st = dalloc((void**)&P.lend, sizeof(int32_t) * cap, "pgs"))) return st;
     if ((st = dalloc((void**)&P.bar, sizeof(unsigned), "pgs"))) return st;
     if ((st = dalloc((void**)&P.err, sizeof(int32_t), "pgs"))) return st;
     if ((st = dalloc((void**)&P.stop, sizeof(int32_t), "pgs"))) return st;
@@ -57,22 +58,18 @@ int Engine::solve_pgs() {
     launch_cond_copy(6 * sc.N, B.u, B.up, ds, stream);
     launches += 4;
     const unsigned long long wait_ns = cfg.gpu_coop_wait_ns > 0 ? (unsigned long long)cfg.gpu_coop_wait_ns : 0ull;
-    // the blocks' levels, then the blocks sorted by level (row order within a level)
-    if ((st = cuda_check((cudaError_t)launch_pgs_levels(pgs, nc, B.kin, B.vin, wait_ns, stream), "pgs levels launch")))
+    // the blocks' levels: the blocks level by level, each level's range
+    if ((st = cuda_check((cudaError_t)launch_pgs_levels(pgs, nc, B.vout, wait_ns, stream), "pgs levels launch")))
         return st;
     ++launches;
     int32_t hl[2] = {0, 0};
     cudaMemcpyAsync(&hl[0], pgs.maxlev, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
     cudaMemcpyAsync(&hl[1], pgs.err, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
     if ((st = cuda_check(cudaStreamSynchronize(stream), "pgs levels"))) return st;
+    if (hl[1] == 3) return fail(CDX_ERR_STATE, "pgs levels: the block chains made no progress");
     if (hl[1]) return fail(CDX_ERR_TIMEOUT, "pgs levels: a grid barrier wait ran out (gpu.coop_wait_ns)");
     last_levels = hl[0] + 1;
-    int bits = 1;
-    while (bits < 32 && (hl[0] >> bits) != 0) ++bits;
-    if ((st = cuda_check(sort_pairs(tmp, tmp_bytes, B.kin, B.kout, B.vin, B.vout, nc, bits, stream), "sort levels")))
-        return st;
-    launches += 4;
-    if ((st = cuda_check((cudaError_t)launch_pgs_solve(sc, C, nc, B, pgs, B.vout, cfg.pj_relaxation, cfg.pj_alpha,
+    if ((st = cuda_check((cudaError_t)launch_pgs_solve(sc, C, last_levels, B, pgs, B.vout, cfg.pj_relaxation, cfg.pj_alpha,
                                                        cfg.pj_tol_rel, cfg.pj_tol_abs, cfg.pj_max_iterations, ds,
                                                        wait_ns, stream),
                          "pgs solve launch")))

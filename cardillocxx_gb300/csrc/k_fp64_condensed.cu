@@ -268,12 +268,29 @@ __global__ void k_cond_res_partials(int N, const double* uf, const double* up, c
 }
 
 // the stop test after sweep `iter`: err = sqrt(1/nV) sqrt(sum); not finite: the solve diverged
-// (checkResidual throws, :507-513); err < 1: converged
+// (checkResidual throws, :507-513); err < 1: converged. The chunk sums are added in groups of
+// RED_GROUP (a thread a group), then the group sums in order (one block).
+constexpr int RED_GROUP = 64;  // the fixed three-level order (shared with the oracle)
 __global__ void k_cond_check(int N, const double* part, int nch, int iter, DevScalars* ds, int32_t* diverged,
                              double* err_out) {
-    if (ds->done) return;
+    if (*(volatile const int32_t*)&ds->done) return;
+    __shared__ double gs[128];
+    const int ngroups = (nch + RED_GROUP - 1) / RED_GROUP;
     double tot = 0.0;
-    for (int k = 0; k < nch; ++k) tot = tot + part[k];
+    for (int g0 = 0; g0 < ngroups; g0 += 128) {
+        const int g = g0 + (int)threadIdx.x;
+        if (g < ngroups) {
+            double s = 0.0;
+            const int c1 = min(nch, (g + 1) * RED_GROUP);
+            for (int c = g * RED_GROUP; c < c1; ++c) s = s + part[c];
+            gs[threadIdx.x] = s;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0)
+            for (int k = 0; k < 128 && g0 + k < ngroups; ++k) tot = tot + gs[k];
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
     const double err = 1.0 / sqrt((double)(6 * N)) * sqrt(tot);
     ds->iters = iter + 1;
     ds->res_last = err;
@@ -351,7 +368,7 @@ void launch_cond_check(int N, const CondBufs& B, double tol_rel, double tol_abs,
                        cudaStream_t s) {
     const int nch = cond_chunks(N);
     if (nch > 0) k_cond_res_partials<<<nblk(nch, 128), 128, 0, s>>>(N, B.uf, B.up, B.u, tol_rel, tol_abs, B.part, ds);
-    k_cond_check<<<1, 1, 0, s>>>(N, B.part, nch, iter, ds, B.flags, B.err);
+    k_cond_check<<<1, 128, 0, s>>>(N, B.part, nch, iter, ds, B.flags, B.err);
 }
 void launch_cond_copy(int n, const double* src, double* dst, const DevScalars* ds, cudaStream_t s) {
     if (n > 0) k_cond_copy<<<nblk(n), NT, 0, s>>>(n, src, dst, ds);

@@ -8,17 +8,15 @@
 // velocity correction u_corr of its two bodies, so a sweep is sequential along every body's list of
 // blocks and free across bodies.
 //  - Levels: a block's level is one more than the larger level of its predecessors (the previous
-//    block of each of its bodies in row order); blocks of one level share no body. They are
-//    computed per step by relaxation rounds in one cooperative launch (as many rounds as the
-//    longest chain), and the blocks are sorted by level (stable: row order within a level).
-//  - The sweeps run as one cooperative launch: position p of the level order goes to thread
-//    p mod T, which runs its blocks in increasing position; before a block runs in sweep s, its
-//    predecessors must have finished sweep s (a per-block counter done[] released after the
-//    block's writes, acquired before the reads; bounded waits). The lowest unfinished position
-//    always has its predecessors (lower levels) and its thread's earlier blocks finished, so a
-//    sweep always advances, and a warp's lanes (one level) become ready together.
-//  - After a sweep: a grid barrier, the velocity-increment residual (fixed chunked order, as the
-//    oracle sums it) and the stop decision.
+//    block of each of its bodies in sweep order); blocks of one level share no body. They are
+//    computed per step by frontiers over the chains in one cooperative launch (a grid barrier a
+//    level), which writes the blocks level by level.
+//  - The sweeps run as one cooperative launch, one level at a time: a level's blocks are spread
+//    over all threads, then a grid barrier (release/acquire, bounded wait) lets the next level
+//    read what they wrote. (Per-block ready flags instead of the barrier measured slower: tens of
+//    thousands of waiting threads polling L2 starve the ones that compute.)
+//  - After a sweep: a grid barrier, the velocity-increment residual (the fixed three-level order
+//    the oracle sums in) and the stop decision.
 // Every block therefore sees exactly the u_corr of the sequential sweep, and the result is the
 // sequential sweep's, bit for bit.
 #include <cstdint>
@@ -31,7 +29,8 @@ namespace {
 
 constexpr int NT = 256;
 inline int nblk(int64_t n, int nt = NT) { return (int)((n + nt - 1) / nt); }
-constexpr int RED_CHUNK = 256;  // the fixed chunked order of the residual sum (shared with the oracle)
+constexpr int RED_CHUNK = 256;  // the fixed three-level order of the residual sum (shared with the oracle)
+constexpr int RED_GROUP = 64;
 constexpr unsigned long long PGS_WAIT_NS = 500000000ull;  // 0.5 s: a wait that long means a fault
 using f64::smin;
 
@@ -157,18 +156,20 @@ __global__ void k_pgs_ucorr_init(Scene sc, Contacts C, CondBufs B, Incidence inc
     for (int k = 0; k < 6; ++k) u[(size_t)k * N + i] = acc[k];
 }
 
-// predecessors: per contact and side, the previous block of that body in row order (or -1); the
-// blocks by rank
-__global__ void k_pgs_links(int N, Contacts C, int nc, Incidence inc, PgsBufs P, int contact_order) {
+// predecessors and successors: per contact and side, the previous and the next block of that body
+// in sweep order (or -1); the incidence lists are in sweep order
+__global__ void k_pgs_links(int N, Incidence inc, PgsBufs P) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < nc) P.by_rank[contact_order ? t : C.rank[t]] = (uint32_t)t;
     if (t >= N) return;
     int prev = -1;
+    uint32_t prev_code = 0;
     for (int p = inc.start[t]; p < inc.end[t]; ++p) {
         const uint32_t code = inc.val_out[p];
         const int c = (int)(code >> 1);
         P.pred[(size_t)(code & 1u) * P.cap + c] = prev;
+        if (prev >= 0) P.succ[(size_t)(prev_code & 1u) * P.cap + prev] = c;
         prev = c;
+        prev_code = code;
     }
 }
 
@@ -176,9 +177,6 @@ __device__ __forceinline__ int ld_acquire_s32(const int32_t* p) {
     int v;
     asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
-}
-__device__ __forceinline__ void st_release_s32(int32_t* p, int v) {
-    asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
     unsigned v;
@@ -215,57 +213,52 @@ __device__ __forceinline__ bool grid_sync(unsigned* ctr, unsigned epoch, int32_t
     return s_ok != 0;
 }
 
-// waits (bounded) until block p has finished sweep s; false on a timeout or another wait's failure
-__device__ __forceinline__ bool wait_done(const int32_t* done, int p, int s, int32_t* err, unsigned long long wait_ns) {
-    if (p < 0 || ld_acquire_s32(done + p) >= s) return true;
-    const unsigned long long t0 = global_ns();
-    while (ld_acquire_s32(done + p) < s) {
-        if (ld_acquire_s32(err) != 0 || global_ns() - t0 > wait_ns) {
-            atomicExch(err, 2);
-            return false;
-        }
-        __nanosleep(20);
-    }
-    return true;
-}
 
-// Levels by relaxation rounds: lev = 1 + max(lev of the predecessors), from 0, until a round
-// changes nothing (at most the longest chain + 1 rounds). Round r's change flag lives in slot r % 3;
-// slot (r + 1) % 3 is cleared during round r, after every block has read it (round r - 2's flag,
-// read before round r - 1's barrier). Then the largest level, and the sort keys (level, contact).
-__global__ void __launch_bounds__(NT) k_pgs_levels(PgsBufs P, int nc, uint32_t* keys, uint32_t* vals,
-                                                   unsigned long long wait_ns) {
+// Levels by frontiers (Kahn's order over the per-body chains): a block's count of unfinished
+// predecessors starts at how many it has; level 0 is the blocks with none; each level's blocks then
+// count down their successors, and those reaching zero form the next level. A block joins a level
+// when its last predecessor is done, so its level is one more than its predecessors' largest: the
+// longest chain ending at it. The blocks are written level by level into `order` (the order
+// within a level varies from run to run and does not matter: a level's blocks share no body); each
+// level's range goes to P.lstart / P.lend, the number of levels to P.maxlev + 1. One grid barrier a
+// level; no sort.
+__global__ void __launch_bounds__(NT) k_pgs_levels(PgsBufs P, int nc, uint32_t* order, unsigned long long wait_ns) {
     const int T = gridDim.x * blockDim.x;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    int32_t* cnt = P.rflag;  // blocks placed so far
     unsigned epoch = 0;
-    for (int round = 0; round <= nc; ++round) {
-        if (t == 0) __stcg(P.rflag + (round + 1) % 3, 0);
-        int changed = 0;
-        for (int r = t; r < nc; r += T) {
-            const int c = (int)P.by_rank[r];
-            const int pa = P.pred[c], pb = P.pred[P.cap + c];
-            const int la = pa >= 0 ? __ldcg(P.lev + pa) : -1;
-            const int lb = pb >= 0 ? __ldcg(P.lev + pb) : -1;
-            const int nl = max(la, lb) + 1;
-            if (nl > __ldcg(P.lev + c)) {
-                __stcg(P.lev + c, nl);
-                changed = 1;
+    for (int c = t; c < nc; c += T) P.lev[c] = (P.pred[c] >= 0 ? 1 : 0) + (P.pred[P.cap + c] >= 0 ? 1 : 0);
+    if (!grid_sync(P.bar, ++epoch, P.err, wait_ns)) return;
+    for (int c = t; c < nc; c += T)
+        if (__ldcg(P.lev + c) == 0) __stcg(order + atomicAdd(cnt, 1), (uint32_t)c);
+    if (!grid_sync(P.bar, ++epoch, P.err, wait_ns)) return;
+    int b0 = 0, b1 = __ldcg(cnt), L = 0;
+    if (t == 0) {
+        P.lstart[0] = 0;
+        P.lend[0] = b1;
+    }
+    while (b1 < nc) {
+        for (int r = b0 + t; r < b1; r += T) {
+            const int c = (int)__ldcg(order + r);
+            for (int side = 0; side < 2; ++side) {
+                const int sc_ = P.succ[(size_t)side * P.cap + c];
+                if (sc_ >= 0 && atomicSub(P.lev + sc_, 1) == 1) __stcg(order + atomicAdd(cnt, 1), (uint32_t)sc_);
             }
         }
-        if (__syncthreads_or(changed) && threadIdx.x == 0) atomicExch(P.rflag + round % 3, 1);
         if (!grid_sync(P.bar, ++epoch, P.err, wait_ns)) return;
-        if (__ldcg(P.rflag + round % 3) == 0) break;
+        b0 = b1;
+        b1 = __ldcg(cnt);
+        if (b1 == b0) {  // no progress: the chains are not in sweep order (cannot happen)
+            if (t == 0) atomicExch(P.err, 3);
+            return;
+        }
+        ++L;
+        if (t == 0) {
+            P.lstart[L] = b0;
+            P.lend[L] = b1;
+        }
     }
-    int m = 0;
-    for (int r = t; r < nc; r += T) {
-        const int c = (int)P.by_rank[r];
-        const int l = __ldcg(P.lev + c);
-        keys[r] = (uint32_t)l;
-        vals[r] = (uint32_t)c;
-        m = max(m, l);
-    }
-    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0) atomicMax(P.maxlev, m);
+    if (t == 0) *P.maxlev = L;
 }
 
 // One block of pgs_sweep (:158-182): res = rhs - W_b u_corr (- C lambda, zero on contact rows),
@@ -327,9 +320,9 @@ __device__ __forceinline__ void pgs_block(const Scene& sc, const Contacts& C, co
 // diverged, check_residual :142-151) or max_iter sweeps.
 template <int COND>
 __global__ void __launch_bounds__(NT) k_pgs_solve(Scene sc, Contacts C, CondBufs B, PgsBufs P, const uint32_t* order,
-                                                  int nc, double relax,
-                                                  double alpha, double tol_rel, double tol_abs, int max_iter,
-                                                  DevScalars* ds, unsigned long long wait_ns) {
+                                                  int nlev, double relax, double alpha, double tol_rel,
+                                                  double tol_abs, int max_iter, DevScalars* ds,
+                                                  unsigned long long wait_ns) {
     const int T = gridDim.x * blockDim.x;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int N = sc.N, nv = 6 * N;
@@ -337,22 +330,21 @@ __global__ void __launch_bounds__(NT) k_pgs_solve(Scene sc, Contacts C, CondBufs
     __shared__ int s_stop;
     unsigned epoch = 0;
     for (int it = 0; it < max_iter; ++it) {
-        bool ok = true;
-        for (int r = t; r < nc && ok; r += T) {
-            const int c = (int)order[r];
-            ok = wait_done(P.done, P.pred[c], it, P.err, wait_ns) &&
-                 wait_done(P.done, P.pred[P.cap + c], it, P.err, wait_ns);
-            if (!ok) break;
-            if (COND) {
-                // the condensed solver's sequential sweep (gaussSeidelSweep, condensed_solver.cpp:166-182)
-                double d[3];
-                cond_block<true, true>(sc, C, B, c, relax, alpha, B.u, d);
-            } else {
-                pgs_block(sc, C, B, c, relax, alpha, B.u);
+        // one level at a time: its blocks share no body, and every earlier level is done
+        for (int L = 0; L < nlev; ++L) {
+            const int r1 = P.lend[L];
+            for (int r = P.lstart[L] + t; r < r1; r += T) {
+                const int c = (int)order[r];
+                if (COND) {
+                    // the condensed solver's sequential sweep (gaussSeidelSweep, condensed_solver.cpp:166-182)
+                    double d[3];
+                    cond_block<true, true>(sc, C, B, c, relax, alpha, B.u, d);
+                } else {
+                    pgs_block(sc, C, B, c, relax, alpha, B.u);
+                }
             }
-            st_release_s32(P.done + c, it);
+            if (!grid_sync(P.bar, ++epoch, P.err, wait_ns)) return;
         }
-        if (!grid_sync(P.bar, ++epoch, P.err, wait_ns)) return;
         // the residual's chunk sums; up takes u for the next sweep's test
         for (int ch = t; ch < nch; ch += T) {
             const int j0 = ch * RED_CHUNK, j1 = min(nv, j0 + RED_CHUNK);
@@ -370,9 +362,19 @@ __global__ void __launch_bounds__(NT) k_pgs_solve(Scene sc, Contacts C, CondBufs
             __stcg(B.part + ch, s);
         }
         if (!grid_sync(P.bar, ++epoch, P.err, wait_ns)) return;
+        // the chunk sums in groups of RED_GROUP (a thread a group), then the group sums in order:
+        // the fixed three-level order the oracle sums in
+        const int ngroups = (nch + RED_GROUP - 1) / RED_GROUP;
+        for (int g = t; g < ngroups; g += T) {
+            double gsum = 0.0;
+            const int c1 = min(nch, (g + 1) * RED_GROUP);
+            for (int c = g * RED_GROUP; c < c1; ++c) gsum = gsum + __ldcg(B.part + c);
+            __stcg(B.part + nch + g, gsum);
+        }
+        if (!grid_sync(P.bar, ++epoch, P.err, wait_ns)) return;
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             double tot = 0.0;
-            for (int k = 0; k < nch; ++k) tot = tot + __ldcg(B.part + k);
+            for (int k = 0; k < ngroups; ++k) tot = tot + __ldcg(B.part + nch + k);
             const double err = 1.0 / sqrt((double)nv) * sqrt(tot);
             ds->iters = it + 1;
             ds->res_last = err;
@@ -399,14 +401,13 @@ void launch_pgs_setup(const Scene& sc, Contacts& C, int gen, int nc, int warmsta
                       PgsBufs& P, cudaStream_t s) {
     if (nc > 0) k_pgs_setup<<<nblk(nc), NT, 0, s>>>(sc, C, gen, nc, B.uf, warmstart, B);
     if (sc.N > 0) k_pgs_ucorr_init<<<nblk(sc.N), NT, 0, s>>>(sc, C, B, inc, B.u);
-    launch_pgs_links(sc, C, nc, inc, P, 0, s);
+    launch_pgs_links(sc, nc, inc, P, s);
 }
-void launch_pgs_links(const Scene& sc, const Contacts& C, int nc, const Incidence& inc, PgsBufs& P,
-                      int contact_order, cudaStream_t s) {
+void launch_pgs_links(const Scene& sc, int nc, const Incidence& inc, PgsBufs& P, cudaStream_t s) {
     cudaMemsetAsync(P.pred, 0xff, sizeof(int32_t) * 2 * (size_t)P.cap, s);
-    cudaMemsetAsync(P.done, 0xff, sizeof(int32_t) * (size_t)P.cap, s);
-    const int n = std::max(nc, sc.N);
-    if (n > 0) k_pgs_links<<<nblk(n), NT, 0, s>>>(sc.N, C, nc, inc, P, contact_order);
+    cudaMemsetAsync(P.succ, 0xff, sizeof(int32_t) * 2 * (size_t)P.cap, s);
+    (void)nc;
+    if (sc.N > 0) k_pgs_links<<<nblk(sc.N), NT, 0, s>>>(sc.N, inc, P);
 }
 
 // grid of a cooperative launch: every block resident (at most two an SM)
@@ -419,25 +420,22 @@ static int coop_grid(K kernel) {
     return sms * std::max(1, std::min(per, 2));
 }
 
-int launch_pgs_levels(const PgsBufs& P, int nc, uint32_t* keys, uint32_t* vals, unsigned long long wait_ns,
-                      cudaStream_t s) {
+int launch_pgs_levels(const PgsBufs& P, int nc, uint32_t* order, unsigned long long wait_ns, cudaStream_t s) {
     cudaMemsetAsync(P.bar, 0, sizeof(unsigned), s);
     cudaMemsetAsync(P.err, 0, sizeof(int32_t), s);
     cudaMemsetAsync(P.rflag, 0, sizeof(int32_t) * 3, s);
     cudaMemsetAsync(P.maxlev, 0, sizeof(int32_t), s);
-    cudaMemsetAsync(P.lev, 0, sizeof(int32_t) * (size_t)P.cap, s);
     PgsBufs a0 = P;
     int n = nc;
-    uint32_t* k = keys;
-    uint32_t* v = vals;
+    uint32_t* o = order;
     unsigned long long wn = wait_ns > 0 ? wait_ns : PGS_WAIT_NS;
-    void* args[] = {&a0, &n, &k, &v, &wn};
+    void* args[] = {&a0, &n, &o, &wn};
     static int grid = 0;
     if (grid == 0) grid = coop_grid(k_pgs_levels);
     return (int)cudaLaunchCooperativeKernel((const void*)k_pgs_levels, dim3(grid), dim3(NT), args, 0, s);
 }
 
-int launch_pgs_solve(const Scene& sc, const Contacts& C, int nc, const CondBufs& B, const PgsBufs& P,
+int launch_pgs_solve(const Scene& sc, const Contacts& C, int nlev, const CondBufs& B, const PgsBufs& P,
                      const uint32_t* order, double relax, double alpha, double tol_rel, double tol_abs, int max_iter,
                      DevScalars* ds, unsigned long long wait_ns, cudaStream_t s, int condensed) {
     cudaMemsetAsync(P.bar, 0, sizeof(unsigned), s);
@@ -448,10 +446,10 @@ int launch_pgs_solve(const Scene& sc, const Contacts& C, int nc, const CondBufs&
     CondBufs a2 = B;
     PgsBufs a3 = P;
     const uint32_t* o = order;
-    int n = nc, mi = max_iter;
+    int nl = nlev, mi = max_iter;
     double rl = relax, al = alpha, tr = tol_rel, ta = tol_abs;
     unsigned long long wn = wait_ns > 0 ? wait_ns : PGS_WAIT_NS;
-    void* args[] = {&a0, &a1, &a2, &a3, &o, &n, &rl, &al, &tr, &ta, &mi, &ds, &wn};
+    void* args[] = {&a0, &a1, &a2, &a3, &o, &nl, &rl, &al, &tr, &ta, &mi, &ds, &wn};
     static int grid[2] = {0, 0};
     const void* k = condensed ? (const void*)k_pgs_solve<1> : (const void*)k_pgs_solve<0>;
     if (grid[condensed ? 1 : 0] == 0) grid[condensed ? 1 : 0] = condensed ? coop_grid(k_pgs_solve<1>) : coop_grid(k_pgs_solve<0>);
