@@ -22,8 +22,9 @@ and print its digest; neither synthesises its input with the other's code.
                 buffers and read back every step
   roofline      the dominant kernel (the split form's projected Jacobi solve) per sweep
   at_residual   every form solved to complementarity residual <= 1e-6 on the warm-started pile
-                (the input stepped --warm-steps times with the split form; state and contact
-                memory loaded into each form): ms/step, sweeps, residual, and the speed-up of the
+                (the input stepped --warm-steps times with the plain FP64 method, so the state is
+                the same on every run; state and contact memory loaded into each form): ms/step,
+                sweeps, residual, and the speed-up of the
                 split form over the plain FP64 method at equal residual
   split_error   the split form against the plain FP64 method on one step from the warm-started
                 pile, both solved to residual 1e-6
@@ -74,7 +75,7 @@ def parse():
     p.add_argument("--sweep-variant", default=None,
                    help="pin the split-form solver shape (index or name; default: autotuned)")
     p.add_argument("--warm-steps", type=int, default=3000,
-                   help="at_residual leg: split-form steps that rebuild the warm start on the input")
+                   help="at_residual leg: plain FP64 steps that rebuild the warm start on the input")
     p.add_argument("--residual-steps", type=int, default=10, help="at_residual leg: timed steps per GPU form")
     p.add_argument("--residual-warmup", type=int, default=20, help="at_residual leg: untimed steps per GPU form")
     p.add_argument("--residual-cap", type=int, default=20000, help="at_residual leg: sweep cap a step")
@@ -310,18 +311,22 @@ def split_error(scene, mem, cfg):
 
 
 def at_residual_leg(a, scene, cfg, flush):
-    """ms/step at complementarity residual <= 1e-6: the input stepped --warm-steps times by the split
-    form (the warm start of a settled pile), then that state and contact memory loaded into each
-    form, each solving every step until the residual is at most 1e-6 (cap --residual-cap sweeps)."""
+    """ms/step at complementarity residual <= 1e-6: the input stepped --warm-steps times by the plain
+    FP64 method (the warm start of a settled pile; that method is bit-reproducible, so every run
+    starts the forms from the same state, where warm steps by the split form gave states whose
+    sweeps to 1e-6 varied severalfold from run to run), then that state and contact memory loaded
+    into each form, each solving every step until the residual is at most 1e-6 (cap --residual-cap
+    sweeps)."""
     import numpy as np
-    from cardillocxx_gb300 import PhysicsEngine
+    from cardillocxx_gb300 import PhysicsEngine, scenes
     tol = 1e-6
     t0 = time.time()
-    state, mem = settle_gpu(scene, cfg, a.warm_steps, "split")
+    state, mem = settle_gpu(scene, cfg, a.warm_steps, "fp64")
     warm_s = time.time() - t0
     s2 = with_state(scene, state)
     rule = {"gpu.residual_tol": tol, "pj.max_iterations": a.residual_cap}
-    out = {"residual_tol": tol, "sweep_cap": a.residual_cap, "warm_steps": a.warm_steps,
+    out = {"residual_tol": tol, "sweep_cap": a.residual_cap, "warm_steps": a.warm_steps, "warm_form": "fp64",
+           "warm_state_digest": scenes.state_digest(state),
            "form_warmup_steps": a.residual_warmup,
            "warm_seconds": warm_s, "contacts": int(mem["id_a"].shape[0]),
            "stop_test": "every sweep (the plain FP64 method's host polls every 10 sweeps; the device stops at the "

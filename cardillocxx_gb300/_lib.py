@@ -93,6 +93,7 @@ class CdxScene(C.Structure):
         ("static_scene", _PI),
         ("num_scenes", C.c_int32),
         ("static_half_length", _P),
+        ("static_half_extents", _P),
     ]
 
 

@@ -38,7 +38,9 @@ enum StaticField {
     SF_DX, SF_DY, SF_DZ,
     SF_D, SF_RAD, SF_MU, SF_RN, SF_RT,
     SF_R0, SF_R1, SF_R2, SF_R3, SF_R4, SF_R5, SF_R6, SF_R7, SF_R8,
-    SF_HL,  // cylinder half length
+    SF_HL,                  // cylinder half length
+    SF_AX, SF_AY, SF_AZ,    // cylinder axis in the static's own frame (world axis = R a)
+    SF_EX, SF_EY, SF_EZ,    // box half extents along the static's own axes
     SF_COUNT
 };
 

@@ -20,6 +20,21 @@ using namespace cdx;
 
 namespace cdx {
 
+namespace {
+// The rotation of a unit quaternion (x, y, z, w), row-major, in the arithmetic of the kernels'
+// rotmat; the static geometry turns body-frame directions with it.
+void host_rotmat(const double* q, double* R) {
+    const double x = q[0], y = q[1], z = q[2], w = q[3];
+    const double tx = 2.0 * x, ty = 2.0 * y, tz = 2.0 * z;
+    const double twx = tx * w, twy = ty * w, twz = tz * w;
+    const double txx = tx * x, txy = ty * x, txz = tz * x;
+    const double tyy = ty * y, tyz = tz * y, tzz = tz * z;
+    R[0] = 1.0 - (tyy + tzz); R[1] = txy - twz;         R[2] = txz + twy;
+    R[3] = txy + twz;         R[4] = 1.0 - (txx + tzz); R[5] = tyz - twx;
+    R[6] = txz - twy;         R[7] = tyz + twx;         R[8] = 1.0 - (txx + tyy);
+}
+}  // namespace
+
 const char* status_name(int st) {
     switch (st) {
         case CDX_OK: return "ok";
@@ -181,11 +196,17 @@ int Engine::load_scene(const cdx_scene& s) {
     }
     for (int i = 0; i < S; ++i) {
         const int k = s.static_kind[i];
-        if (k != CDX_STATIC_HALFSPACE && k != CDX_STATIC_DRUM && k != CDX_STATIC_CYLINDER)
+        if (k != CDX_STATIC_HALFSPACE && k != CDX_STATIC_DRUM && k != CDX_STATIC_CYLINDER && k != CDX_STATIC_BOX)
             return fail(CDX_ERR_ARG, "unknown static kind");
         if (k == CDX_STATIC_CYLINDER &&
             (!s.static_radius || !s.static_half_length || !(s.static_radius[i] > 0) || !(s.static_half_length[i] > 0)))
             return fail(CDX_ERR_ARG, "a cylinder needs a positive radius and half length");
+        if (k == CDX_STATIC_BOX) {
+            if (!s.static_half_extents) return fail(CDX_ERR_ARG, "a box needs its half extents");
+            for (int c = 0; c < 3; ++c)
+                if (!(s.static_half_extents[3 * (size_t)i + c] > 0) || !std::isfinite(s.static_half_extents[3 * (size_t)i + c]))
+                    return fail(CDX_ERR_ARG, "a box needs positive, finite half extents");
+        }
     }
 
     // host staging: body fields (field-major)
@@ -233,6 +254,12 @@ int Engine::load_scene(const cdx_scene& s) {
         sf(SF_D, i) = (un[0] * p[0] + un[1] * p[1]) + un[2] * p[2];
         sf(SF_RAD, i) = s.static_radius ? s.static_radius[i] : 0.0;
         sf(SF_HL, i) = s.static_half_length ? s.static_half_length[i] : 0.0;
+        // a cylinder's axis in its own frame, R(q0)^T u, so that the axis turns with the static
+        double R0[9];
+        host_rotmat(&s.static_quat[4 * (size_t)i], R0);
+        for (int k = 0; k < 3; ++k) sf(SF_AX + k, i) = (R0[0 + k] * un[0] + R0[3 + k] * un[1]) + R0[6 + k] * un[2];
+        for (int k = 0; k < 3; ++k)
+            sf(SF_EX + k, i) = (s.static_kind[i] == CDX_STATIC_BOX) ? s.static_half_extents[3 * (size_t)i + k] : 0.0;
         sf(SF_MU, i) = s.static_mu[i];
         sf(SF_RN, i) = s.static_rest_n[i];
         sf(SF_RT, i) = s.static_rest_t[i];
@@ -368,6 +395,9 @@ int Engine::load_scene(const cdx_scene& s) {
         if (s.static_radius) oscene.srad.assign(s.static_radius, s.static_radius + S);
         oscene.shl.assign(S, 0.0);
         if (s.static_half_length) oscene.shl.assign(s.static_half_length, s.static_half_length + S);
+        oscene.squat.assign(s.static_quat, s.static_quat + 4 * (size_t)S);
+        oscene.she.assign(3 * (size_t)S, 0.0);
+        if (s.static_half_extents) oscene.she.assign(s.static_half_extents, s.static_half_extents + 3 * (size_t)S);
     }
     if (out) {
         out->flush();

@@ -320,6 +320,7 @@ static int init_split(Engine& E) {
     float4** f4[] = {&b.st_dir, &b.st_pt, &b.st_v, &b.st_w};
     for (auto p : f4)
         if ((st = salloc(E, (void**)p, sizeof(float4) * s1, "split statics"))) return st;
+    if ((st = salloc(E, (void**)&b.st_box, sizeof(float4) * 3 * s1, "split statics"))) return st;
     if ((st = salloc(E, (void**)&b.nc_dev, sizeof(int32_t), "split"))) return st;
     if ((st = salloc(E, (void**)&b.ss, sizeof(SplitScalars), "split"))) return st;
     if ((st = salloc(E, (void**)&b.part, sizeof(float2) * SPLIT_MAX_PARTS, "split"))) return st;
@@ -639,7 +640,7 @@ int Engine::step_split() {
         cudaEventRecord(S->tev[0], stream);
     }
     if (scenes) {
-        const float* salpha = nullptr;
+        float* salpha = nullptr;
         if ((st = split_alpha_bufs(*this))) return st;
         if (cfg.gpu_tune_alpha) {
             if (alpha_due && !capturing && !async) {

@@ -34,6 +34,11 @@ __device__ __forceinline__ void matTvec(const double* R, const double* v, double
 #pragma unroll
     for (int i = 0; i < 3; ++i) o[i] = (R[0 + i] * v[0] + R[3 + i] * v[1]) + R[6 + i] * v[2];
 }
+// R v (a body-frame vector in world coordinates)
+__device__ __forceinline__ void matvec(const double* R, const double* v, double* o) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) o[i] = (R[3 * i] * v[0] + R[3 * i + 1] * v[1]) + R[3 * i + 2] * v[2];
+}
 
 // alignQuaternionTo with Eigen's normalize()
 __device__ __forceinline__ void align_quat(double* q, const double* qref) {

@@ -110,14 +110,80 @@ __device__ __forceinline__ bool cylinder_geom(const double* xa, const double* u,
     return true;
 }
 
-// coal::Halfspace {x : n.x <= d} (shape 1) against a sphere (shape 2), a solid cylinder, or the
-// inner wall of a drum.
+// Sphere against a solid box (coal::Box, collision_coal.cpp:288-290): the exact nearest points in
+// closed form. In the box's frame (R's columns are its axes, e its half extents) the centre is at
+// c = R^T (xb - xa). Outside (some |c_k| > e_k) the nearest point is c clamped to the box (a face,
+// edge or corner) and the normal is the direction from it to the centre; inside, it is on the face
+// nearest the centre (the lowest axis on a tie), whose outward normal is the contact normal. The
+// normal points from the box to the sphere.
+__device__ __forceinline__ bool box_geom(const double* xa, const double* R, const double* e, const double* xb,
+                                         double rb, double margin, Geom& g) {
+    double rel[3], c[3], ql[3], nl[3];
+    for (int k = 0; k < 3; ++k) rel[k] = xb[k] - xa[k];
+    matTvec(R, rel, c);
+    const bool out = fabs(c[0]) > e[0] || fabs(c[1]) > e[1] || fabs(c[2]) > e[2];
+    double sd;
+    if (!out) {
+        int f = 0;
+        double best = e[0] - fabs(c[0]);
+        for (int k = 1; k < 3; ++k) {
+            const double dk = e[k] - fabs(c[k]);
+            if (dk < best) {
+                best = dk;
+                f = k;
+            }
+        }
+        const double sg = c[f] < 0.0 ? -1.0 : 1.0;
+        for (int k = 0; k < 3; ++k) {
+            ql[k] = c[k];
+            nl[k] = 0.0;
+        }
+        ql[f] = sg * e[f];
+        nl[f] = sg;
+        sd = -best;
+    } else {
+        double d[3];
+        for (int k = 0; k < 3; ++k) {
+            ql[k] = c[k] < -e[k] ? -e[k] : (c[k] > e[k] ? e[k] : c[k]);
+            d[k] = c[k] - ql[k];
+        }
+        sd = norm3(d);
+        for (int k = 0; k < 3; ++k) nl[k] = d[k] / sd;
+    }
+    if (!((sd - rb) <= margin)) return false;
+    double n[3], q[3];
+    matvec(R, nl, n);
+    matvec(R, ql, q);
+    for (int k = 0; k < 3; ++k) {
+        g.p1[k] = xa[k] + q[k];
+        g.p2[k] = xb[k] - rb * n[k];
+        g.nraw[k] = n[k];
+    }
+    return true;
+}
+
+// coal::Halfspace {x : n.x <= d} (shape 1) against a sphere (shape 2), a solid cylinder, a solid
+// box, or the inner wall of a drum.
 __device__ __forceinline__ bool static_geom(const Scene& sc, int s, const double* xb, double rb, double margin,
                                             Geom& g) {
     const double u[3] = {sc.sf(SF_DX)[s], sc.sf(SF_DY)[s], sc.sf(SF_DZ)[s]};
     g.xa[0] = sc.sf(SF_PX)[s];
     g.xa[1] = sc.sf(SF_PY)[s];
     g.xa[2] = sc.sf(SF_PZ)[s];
+    const int kind = sc.static_kind[s];
+    if (kind >= 2) {
+        double R[9];
+        for (int k = 0; k < 9; ++k) R[k] = sc.sf(SF_R0 + k)[s];
+        if (kind == 3) {
+            const double e[3] = {sc.sf(SF_EX)[s], sc.sf(SF_EY)[s], sc.sf(SF_EZ)[s]};
+            return box_geom(g.xa, R, e, xb, rb, margin, g);
+        }
+        // the cylinder's axis turns with the static: R times its axis in the static's frame
+        const double a[3] = {sc.sf(SF_AX)[s], sc.sf(SF_AY)[s], sc.sf(SF_AZ)[s]};
+        double ua[3];
+        matvec(R, a, ua);
+        return cylinder_geom(g.xa, ua, sc.sf(SF_RAD)[s], sc.sf(SF_HL)[s], xb, rb, margin, g);
+    }
     if (sc.static_kind[s] == 0) {
         const double sdist = dot3(u, xb) - sc.sf(SF_D)[s];
         const double dist = sdist - rb;
@@ -130,7 +196,6 @@ __device__ __forceinline__ bool static_geom(const Scene& sc, int s, const double
         }
         return true;
     }
-    if (sc.static_kind[s] == 2) return cylinder_geom(g.xa, u, sc.sf(SF_RAD)[s], sc.sf(SF_HL)[s], xb, rb, margin, g);
     const double R = sc.sf(SF_RAD)[s];
     double rel[3];
 #pragma unroll

@@ -26,7 +26,7 @@ namespace {
 
 constexpr int NT = 256;
 inline int nblk(int64_t n, int nt = NT) { return (int)((n + nt - 1) / nt); }
-constexpr int RED_CHUNK = 256;  // the fixed chunked order of the reductions (shared with the oracle)
+constexpr int RED_CHUNK = 256;  // chunk size of the fixed three-level reduction order (shared with the oracle)
 using f64::cross3;
 using f64::smin;
 

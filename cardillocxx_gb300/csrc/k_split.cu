@@ -198,12 +198,22 @@ __global__ void k_s_prep(Scene sc, SplitBuf sb, double dt, double g0, double g1,
         for (int k = 0; k < 3; ++k) ww[k] = R[3 * k] * w[0] + R[3 * k + 1] * w[1] + R[3 * k + 2] * w[2];
         const int scn = sc.static_scene[s];
         const double* o = &sb.origin[3 * scn];
-        const double u[3] = {sc.sf(SF_DX)[s], sc.sf(SF_DY)[s], sc.sf(SF_DZ)[s]};
+        const int kind = sc.static_kind[s];
+        double u[3] = {sc.sf(SF_DX)[s], sc.sf(SF_DY)[s], sc.sf(SF_DZ)[s]};
+        if (kind == 2) {
+            // a cylinder's axis turns with the static
+            const double a[3] = {sc.sf(SF_AX)[s], sc.sf(SF_AY)[s], sc.sf(SF_AZ)[s]};
+            for (int k = 0; k < 3; ++k) u[k] = (R[3 * k] * a[0] + R[3 * k + 1] * a[1]) + R[3 * k + 2] * a[2];
+        } else if (kind == 3) {
+            // a box's axes are the columns of R
+            for (int k = 0; k < 3; ++k)
+                sb.st_box[3 * s + k] = make_float4((float)R[k], (float)R[3 + k], (float)R[6 + k], (float)sc.sf(SF_EX + k)[s]);
+        }
         const double pl[3] = {x[0] - o[0], x[1] - o[1], x[2] - o[2]};
         const double dl = u[0] * pl[0] + u[1] * pl[1] + u[2] * pl[2];
         // .w: the halfspace offset n . x, or a cylinder's half length
         sb.st_dir[s] = make_float4((float)u[0], (float)u[1], (float)u[2],
-                                   sc.static_kind[s] == 2 ? (float)sc.sf(SF_HL)[s] : (float)dl);
+                                   kind == 2 ? (float)sc.sf(SF_HL)[s] : (float)dl);
         sb.st_pt[s] = make_float4((float)pl[0], (float)pl[1], (float)pl[2], (float)sc.sf(SF_RAD)[s]);
         sb.st_v[s] = make_float4((float)v[0], (float)v[1], (float)v[2], (float)sc.static_kind[s]);
         sb.st_w[s] = make_float4((float)ww[0], (float)ww[1], (float)ww[2], (float)sc.sf(SF_MU)[s]);
@@ -231,6 +241,38 @@ __device__ __forceinline__ bool static_test32(const SplitBuf& sb, int s, float3 
     }
     const float4 pp = sb.st_pt[s];
     const float3 rel = x - f3(pp);
+    if (sb.st_v[s].w == 3.f) {
+        // solid box: the FP64 method's box_geom in FP32 (centre in the box frame, clamped outside,
+        // nearest face inside); n from the box to the sphere, sd the centre's signed distance
+        const float4 b0 = sb.st_box[3 * s], b1 = sb.st_box[3 * s + 1], b2 = sb.st_box[3 * s + 2];
+        const float c[3] = {dot(f3(b0), rel), dot(f3(b1), rel), dot(f3(b2), rel)};
+        const float e[3] = {b0.w, b1.w, b2.w};
+        float d[3];
+        float sd;
+        if (!(fabsf(c[0]) > e[0] || fabsf(c[1]) > e[1] || fabsf(c[2]) > e[2])) {
+            int f = 0;
+            float best = e[0] - fabsf(c[0]);
+            for (int k = 1; k < 3; ++k) {
+                const float dk = e[k] - fabsf(c[k]);
+                if (dk < best) {
+                    best = dk;
+                    f = k;
+                }
+            }
+            for (int k = 0; k < 3; ++k) d[k] = k == f ? (c[k] < 0.f ? -1.f : 1.f) : 0.f;
+            sd = -best;
+        } else {
+            for (int k = 0; k < 3; ++k) d[k] = c[k] - fminf(fmaxf(c[k], -e[k]), e[k]);
+            sd = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+            const float inv = __frcp_rn(sd);
+            for (int k = 0; k < 3; ++k) d[k] *= inv;
+        }
+        if (!((sd - r) <= margin)) return false;
+        g.n = d[0] * f3(b0) + d[1] * f3(b1) + d[2] * f3(b2);
+        g.rhoB = -0.5f * (sd + r);
+        g.sep = sd;
+        return true;
+    }
     const float ax = dot(rel, u);
     const float3 perp = rel - ax * u;
     const float rho = sqrtf(dot(perp, perp));
@@ -1476,7 +1518,7 @@ template <int NT, int CSM>
 __global__ void __launch_bounds__(NT, 1024 / NT) k_s_solve_scenes(Scene sc, SplitBuf sb, int gen, float alpha, int max_iter,
                                                        float tol, const int32_t* spos, const int32_t* sflags,
                                                        const int32_t* poff, const int32_t* order, int L, int ccap,
-                                                       const float* scene_alpha, float alpha_ref, int4* scene_out) {
+                                                       float* scene_alpha, float alpha_ref, int4* scene_out) {
     extern __shared__ float4 sm4[];
     // a device-counted step whose contacts overflowed the buffers wrote only the slots below the
     // capacity, while the scene ranges below count them all: nothing runs, the host redoes the step
@@ -1485,8 +1527,16 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_s_solve_scenes(Scene sc, Spli
     const int s = order[blockIdx.x];
     const int b0 = sc.scene_body_start[s], nb = sc.scene_body_start[s + 1] - b0;
     const int tid = threadIdx.x;
-    const float a_s = scene_alpha ? scene_alpha[s] : alpha;
-    const float rscale = alpha_ref / a_s;
+    float a_s = scene_alpha ? scene_alpha[s] : alpha;
+    float rscale = alpha_ref / a_s;
+    // A tuned alpha above the configured one can lose stability when the scene's contacts change
+    // after the tuning (projected Jacobi converges for alpha < 2 / the largest eigenvalue of
+    // D^-1/2 W D^-1/2, and new contacts raise it). Divergence grows the impulses geometrically
+    // while their relative change stays level, so the stop rule does not see it: once the largest
+    // impulse exceeds 64 times its largest over the first 8 sweeps, the scene restarts from zero
+    // impulses at the configured alpha, which it keeps from then on.
+    bool guard = scene_alpha != nullptr && a_s > alpha_ref;  // block-uniform
+    float lm_ref = 0.f;
     const int64_t nflag = (int64_t)sc.N * L;
     int n_static = 0;
     if (nflag > 0) n_static = spos[nflag - 1] + sflags[nflag - 1];
@@ -1571,6 +1621,32 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_s_solve_scenes(Scene sc, Spli
         __syncthreads();
         r = s_r;
         ++it;
+        if (guard) {
+            const float lmax = s_l;
+            if (it <= 8) {
+                lm_ref = fmaxf(lm_ref, lmax);
+            } else if (!(r == r) || !(lmax <= 64.f * lm_ref)) {
+                guard = false;
+                a_s = alpha_ref;
+                rscale = 1.f;
+                if (tid == 0) scene_alpha[s] = alpha_ref;
+                for (int k = tid; k < nc; k += NT) {
+                    if (local)
+                        ls[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    else
+                        lamp[k < ns ? cs0 + k : cp0 + (k - ns)] = make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+                // the next sweep gathers accumulator it % 3: back to the free velocities
+                float4* Gx = sb.acc[it % 3];
+                for (int i = tid; i < nb; i += NT) {
+                    const float4 v0 = ldg4(&sb.vel4[2 * (b0 + i)]), w0 = ldg4(&sb.vel4[2 * (b0 + i) + 1]);
+                    stcg_body(&Gx[2 * (b0 + i)], v0, w0);
+                }
+                __syncthreads();
+                if (it >= max_iter) break;
+                continue;
+            }
+        }
         if (it >= max_iter || (tol > 0.f && r <= tol) || !(r == r)) break;
     }
     if (scene_out && tid == 0) scene_out[s] = make_int4(it, __float_as_int(r), __float_as_int(s_l), 0);
@@ -1701,9 +1777,47 @@ __device__ __forceinline__ void geom64(const Scene& sc, int a, int b, double* n,
         return;
     }
     const int s = -a - 1;
-    const double u[3] = {sc.sf(SF_DX)[s], sc.sf(SF_DY)[s], sc.sf(SF_DZ)[s]};
+    double u[3] = {sc.sf(SF_DX)[s], sc.sf(SF_DY)[s], sc.sf(SF_DZ)[s]};
     rhoA = 0.0;
-    if (sc.static_kind[s] == 0) {
+    const int kind = sc.static_kind[s];
+    if (kind >= 2) {
+        double R[9];
+        for (int k = 0; k < 9; ++k) R[k] = sc.sf(SF_R0 + k)[s];
+        const double p[3] = {sc.sf(SF_PX)[s], sc.sf(SF_PY)[s], sc.sf(SF_PZ)[s]};
+        if (kind == 3) {
+            // solid box, as in the narrow phase
+            const double rel[3] = {xb[0] - p[0], xb[1] - p[1], xb[2] - p[2]};
+            double c[3], d[3];
+            for (int k = 0; k < 3; ++k) c[k] = (R[k] * rel[0] + R[3 + k] * rel[1]) + R[6 + k] * rel[2];
+            const double e[3] = {sc.sf(SF_EX)[s], sc.sf(SF_EY)[s], sc.sf(SF_EZ)[s]};
+            double sd;
+            if (!(fabs(c[0]) > e[0] || fabs(c[1]) > e[1] || fabs(c[2]) > e[2])) {
+                int f = 0;
+                double best = e[0] - fabs(c[0]);
+                for (int k = 1; k < 3; ++k) {
+                    const double dk = e[k] - fabs(c[k]);
+                    if (dk < best) {
+                        best = dk;
+                        f = k;
+                    }
+                }
+                for (int k = 0; k < 3; ++k) d[k] = k == f ? (c[k] < 0.0 ? -1.0 : 1.0) : 0.0;
+                sd = -best;
+            } else {
+                for (int k = 0; k < 3; ++k) d[k] = c[k] - fmin(fmax(c[k], -e[k]), e[k]);
+                const double dd2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+                const double inv = rsqrt_nr(dd2);
+                sd = dd2 * inv;
+                for (int k = 0; k < 3; ++k) d[k] *= inv;
+            }
+            for (int k = 0; k < 3; ++k) n[k] = (R[3 * k] * d[0] + R[3 * k + 1] * d[1]) + R[3 * k + 2] * d[2];
+            rhoB = -0.5 * (sd + rb);
+            return;
+        }
+        const double a3[3] = {sc.sf(SF_AX)[s], sc.sf(SF_AY)[s], sc.sf(SF_AZ)[s]};
+        for (int k = 0; k < 3; ++k) u[k] = (R[3 * k] * a3[0] + R[3 * k + 1] * a3[1]) + R[3 * k + 2] * a3[2];
+    }
+    if (kind == 0) {
         const double sd = (u[0] * xb[0] + u[1] * xb[1] + u[2] * xb[2]) - sc.sf(SF_D)[s];
         n[0] = u[0]; n[1] = u[1]; n[2] = u[2];
         rhoB = -0.5 * (sd + rb);
@@ -2034,7 +2148,7 @@ static CoopLoopVariant g_coop_loop[2][2] = {
 // Batched scenes (one block per scene): threads per block and contacts per thread per pass.
 struct ScenesVariant {
     void (*kernel)(Scene, SplitBuf, int, float, int, float, const int32_t*, const int32_t*, const int32_t*,
-                   const int32_t*, int, int, const float*, float, int4*);
+                   const int32_t*, int, int, float*, float, int4*);
     int nth, csm;
     int smem_set;  // dynamic shared memory the kernel has been opted in to
 };
@@ -2090,7 +2204,7 @@ void launch_s_acc_init(const SplitBuf& sb, cudaStream_t s) {
 
 int launch_s_solve_scenes(const Scene& sc, const SplitBuf& sb, int gen, float alpha, int v, int max_iter, float tol,
                           const int32_t* spos, const int32_t* sflags, const int32_t* poff, const int32_t* order,
-                          int nbmax, cudaStream_t s, const float* scene_alpha, float alpha_ref, int4* scene_out) {
+                          int nbmax, cudaStream_t s, float* scene_alpha, float alpha_ref, int4* scene_out) {
     if (!split_variant_is_scenes(v) || sc.nscenes <= 0) return (int)cudaErrorInvalidValue;
     ScenesVariant& cv = g_scenes[v - N_STREAM - N_COOP];
     // shared memory (contact-resident shapes): 48 B for each of up to 3 contacts a body (a settled

@@ -258,8 +258,8 @@ void Output::frame(OutputFrame f) {
         };
         char num[32];
         std::snprintf(num, sizeof(num), "_%04lld.vtp", (long long)f.step);
-        // static shapes: a square patch per halfspace, a cylinder wall per drum, sized to the
-        // initial extent of the spheres
+        // static shapes: a square patch per halfspace sized to the initial extent of the spheres, a
+        // cylinder wall per drum or cylinder, a box's faces; all at their pose at load
         if (write_static) {
             std::vector<float> pts;
             std::vector<float> vel;
@@ -296,7 +296,24 @@ void Output::frame(OutputFrame f) {
                     lo = -sc.shl[s];
                     hi = sc.shl[s];
                 }
-                if (sc.skind[s] == CDX_STATIC_DRUM || sc.skind[s] == CDX_STATIC_CYLINDER) {
+                if (sc.skind[s] == CDX_STATIC_BOX) {
+                    // the box's eight corners and twelve triangles, in its orientation at load
+                    double R[9];
+                    quat_to_R(&sc.squat[4 * s], R);
+                    const double* e = &sc.she[3 * s];
+                    for (int j = 0; j < 8; ++j) {
+                        const double l[3] = {(j & 1) ? e[0] : -e[0], (j & 2) ? e[1] : -e[1], (j & 4) ? e[2] : -e[2]};
+                        double x[3];
+                        for (int k = 0; k < 3; ++k) x[k] = p[k] + ((R[3 * k] * l[0] + R[3 * k + 1] * l[1]) + R[3 * k + 2] * l[2]);
+                        add_pt(x);
+                    }
+                    static const int quads[6][4] = {{0, 2, 6, 4}, {1, 5, 7, 3}, {0, 4, 5, 1},
+                                                    {2, 3, 7, 6}, {0, 1, 3, 2}, {4, 6, 7, 5}};
+                    for (auto& qd : quads) {
+                        add_tri(base + qd[0], base + qd[1], base + qd[2]);
+                        add_tri(base + qd[0], base + qd[2], base + qd[3]);
+                    }
+                } else if (sc.skind[s] == CDX_STATIC_DRUM || sc.skind[s] == CDX_STATIC_CYLINDER) {
                     const int seg = 64;
                     const double R = sc.srad[s];
                     for (int j = 0; j < seg; ++j) {
@@ -426,6 +443,17 @@ void Output::frame(OutputFrame f) {
                             const double dr = std::max(0.0, rho - sc.srad[a]);
                             const double dz = std::max(0.0, std::fabs(ax) - sc.shl[a]);
                             depth = rb - std::sqrt(dr * dr + dz * dz);
+                        } else if (sc.skind[a] == CDX_STATIC_BOX) {
+                            // distance of the centre to the solid box (outside; inside counts 0)
+                            double R[9];
+                            quat_to_R(&sc.squat[4 * a], R);
+                            double o2 = 0.0;
+                            for (int k = 0; k < 3; ++k) {
+                                const double c = (R[k] * r[0] + R[3 + k] * r[1]) + R[6 + k] * r[2];
+                                const double o = std::max(0.0, std::fabs(c) - sc.she[3 * a + k]);
+                                o2 += o * o;
+                            }
+                            depth = rb - std::sqrt(o2);
                         } else {
                             depth = rb - ax;
                         }

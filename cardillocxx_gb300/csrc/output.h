@@ -24,6 +24,7 @@ struct OutputScene {
     std::vector<double> radius, mu;
     std::vector<int32_t> skind;
     std::vector<double> spos, sdir, srad, smu, shl;  // shl: cylinder half lengths
+    std::vector<double> squat, she;                  // orientations (x, y, z, w); box half extents
     std::vector<double> pos0;  // initial sphere centres (extent of the static meshes)
 };
 

@@ -106,6 +106,7 @@ struct SplitBuf {
     double* origin = nullptr; // 3 per scene
     float4* st_dir = nullptr; // S: (normal/axis, plane offset in scene coordinates)
     float4* st_pt = nullptr;  // S: (anchor in scene coordinates, drum radius)
+    float4* st_box = nullptr; // 3S: a box's axes in world (columns of its rotation), .w its half extents
     float4* st_v = nullptr;   // S: (wall velocity, kind)
     float4* st_w = nullptr;   // S: (wall angular velocity world, mu)
     float4* rec0 = nullptr;
@@ -142,7 +143,7 @@ int split_num_scenes_variants();
 // (optional): per-scene sweeps and residual
 int launch_s_solve_scenes(const Scene& sc, const SplitBuf& sb, int gen, float alpha, int v, int max_iter, float tol,
                           const int32_t* spos, const int32_t* sflags, const int32_t* poff, const int32_t* order,
-                          int nbmax, cudaStream_t s, const float* scene_alpha = nullptr, float alpha_ref = 0.f,
+                          int nbmax, cudaStream_t s, float* scene_alpha = nullptr, float alpha_ref = 0.f,
                           int4* scene_out = nullptr);
 // the scenes' alpha autotuner: op 0 resets the best (alpha = the configured one), 3 records the
 // reference trial (the configured alpha), 1 keeps trial `alpha` where it beats the best, 2 writes

@@ -85,6 +85,8 @@ def scene_struct(scene: dict) -> tuple[CdxScene, dict]:
     s.num_scenes = int(keep.get("num_scenes", 1))
     if "static_half_length" in keep:
         s.static_half_length = dp(keep["static_half_length"])
+    if "static_half_extents" in keep:
+        s.static_half_extents = dp(keep["static_half_extents"])
     return s, keep
 
 

@@ -167,7 +167,8 @@ def state_digest(state: dict) -> str:
 
 def make_scene(bodies: list[dict], statics: list[dict], scene_ids=None, static_scene_ids=None) -> dict:
     """Hand-built scene from per-body dicts (pos, radius, density|mass, vel, omega, quat, mu, rest_n)
-    and statics (kind 'halfspace'|'drum'|'cylinder', pos, dir, radius, half_length, vel, omega, mu)."""
+    and statics (kind 'halfspace'|'drum'|'cylinder'|'box', pos, dir, radius, half_length, half_extents,
+    quat, vel, omega, mu). A box's axes are the columns of its quaternion's rotation; it needs no dir."""
     N, S = len(bodies), len(statics)
     out = {k: np.zeros((N, d)) for k, d in (("pos", 3), ("quat", 4), ("vel", 3), ("omega", 3))}
     for k in ("radius", "mass", "inertia", "mu", "rest_n", "rest_t"):
@@ -189,22 +190,24 @@ def make_scene(bodies: list[dict], statics: list[dict], scene_ids=None, static_s
         out["rest_n"][i] = b.get("rest_n", 0.0)
         out["rest_t"][i] = b.get("rest_t", 0.0)
     out["body_scene"] = np.asarray(scene_ids if scene_ids is not None else np.zeros(N), np.int32)
-    kinds = {"halfspace": 0, "drum": 1, "cylinder": 2}
+    kinds = {"halfspace": 0, "drum": 1, "cylinder": 2, "box": 3}
     out["static_kind"] = np.array([kinds[s.get("kind", "halfspace")] for s in statics], np.int32)
-    for k, d in (("static_pos", 3), ("static_vel", 3), ("static_omega", 3), ("static_dir", 3)):
+    for k, d in (("static_pos", 3), ("static_vel", 3), ("static_omega", 3), ("static_dir", 3),
+                 ("static_half_extents", 3)):
         out[k] = np.zeros((S, d))
     out["static_quat"] = np.tile(np.array([0.0, 0.0, 0.0, 1.0]), (S, 1)) if S else np.zeros((0, 4))
     for k in ("static_radius", "static_mu", "static_rest_n", "static_rest_t", "static_half_length"):
         out[k] = np.zeros(S)
     for i, s in enumerate(statics):
         out["static_pos"][i] = s["pos"]
-        out["static_dir"][i] = s["dir"]
+        out["static_dir"][i] = s.get("dir", (0, 0, 1))
         out["static_vel"][i] = s.get("vel", (0, 0, 0))
         out["static_omega"][i] = s.get("omega", (0, 0, 0))
         if "quat" in s:
             out["static_quat"][i] = s["quat"]
         out["static_radius"][i] = s.get("radius", 0.0)
         out["static_half_length"][i] = s.get("half_length", 0.0)
+        out["static_half_extents"][i] = s.get("half_extents", (0.0, 0.0, 0.0))
         out["static_mu"][i] = s.get("mu", 0.3)
         out["static_rest_n"][i] = s.get("rest_n", 0.0)
         out["static_rest_t"][i] = s.get("rest_t", 0.0)

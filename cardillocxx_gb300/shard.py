@@ -15,7 +15,8 @@ from __future__ import annotations
 import numpy as np
 
 SCENE_KEYS_STATIC = ("static_kind", "static_pos", "static_quat", "static_vel", "static_omega", "static_dir",
-                     "static_radius", "static_mu", "static_rest_n", "static_rest_t")
+                     "static_radius", "static_mu", "static_rest_n", "static_rest_t", "static_half_length",
+                     "static_half_extents")
 
 
 def partition_scenes(body_counts, world: int) -> list[np.ndarray]:

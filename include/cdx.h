@@ -40,6 +40,8 @@ extern "C" {
 #define CDX_STATIC_DRUM 1 /* hollow cylinder: spheres touch its inner wall */
 #define CDX_STATIC_CYLINDER 2 /* solid finite cylinder (the reference's C_RB_Cylinder, coal::Cylinder):
                                  spheres touch its side, its caps or their rims */
+#define CDX_STATIC_BOX 3      /* solid box (the reference's static C_RB_Cube, coal::Box): spheres touch its
+                                 faces, edges or corners */
 
 /* Engine configuration. Field names follow the reference's config keys
  * (src/config/config.hpp:12-237, parsed by ConfigReader::fromFile, src/config/config.cpp:22-420).
@@ -110,7 +112,7 @@ typedef struct cdx_config {
     int32_t gpu_tune_alpha_every;           /* gpu.tune_alpha_every: steps between two tunings of the scenes' alpha */
 } cdx_config;
 
-/* Scene: dynamic spheres plus static shapes (halfspaces, drums, cylinders). Bodies of one scene are
+/* Scene: dynamic spheres plus static shapes (halfspaces, drums, cylinders, boxes). Bodies of one scene are
  * contiguous; body_scene/static_scene may be NULL for a single scene. */
 typedef struct cdx_scene {
     int32_t num_bodies;
@@ -127,11 +129,12 @@ typedef struct cdx_scene {
     const int32_t* body_scene; /* [N] nondecreasing, or NULL */
     int32_t num_statics;
     const int32_t* static_kind; /* CDX_STATIC_* */
-    const double* static_pos;   /* [3S] halfspace point / drum axis point / cylinder centre */
+    const double* static_pos;   /* [3S] halfspace point / drum axis point / cylinder or box centre */
     const double* static_quat;  /* [4S] */
     const double* static_vel;   /* [3S] world-frame velocity (enters the contact bias) */
     const double* static_omega; /* [3S] body-frame angular velocity (moving walls) */
-    const double* static_dir;   /* [3S] halfspace normal / drum or cylinder axis, world frame */
+    const double* static_dir;   /* [3S] halfspace normal / drum or cylinder axis, world frame at load (a
+                                   cylinder's axis then turns with its orientation; ignored for boxes) */
     const double* static_radius;/* [S] drum or cylinder radius (ignored for halfspaces) */
     const double* static_mu;
     const double* static_rest_n;
@@ -140,6 +143,9 @@ typedef struct cdx_scene {
     int32_t num_scenes;
     const double* static_half_length; /* [S] cylinder half length along its axis (C_RB_Cylinder::halfLength;
                                          ignored for other kinds; may be NULL when there is no cylinder) */
+    const double* static_half_extents; /* [3S] box half extents along the box's own axes, which are the
+                                          columns of static_quat's rotation (C_RB_Cube::halfExtents; ignored
+                                          for other kinds; may be NULL when there is no box) */
 } cdx_scene;
 
 typedef struct cdx_stats {

@@ -113,12 +113,17 @@ namespace cardillo::integration {
 //    context across steps.
 //  - Static solid cylinders are the entities with C_RB_Cylinder and no C_PhysicsObject: their axis
 //    is the pose's local z (coal::Cylinder's), radius and half length from the component.
-//  - Halfspaces driven by a trajectory (C_StaticTrajectory): each step runs Trajectory::update
+//  - Static boxes are the entities with C_RB_Cube and no C_PhysicsObject (the walls and the
+//    trajectory-driven floor of the stacked_spheres scene): half extents from the component, the
+//    box posed as coal poses it (makeTfFromEcs, collision_coal.cpp:43-64: orientation q * cube.q,
+//    centre x + (q * cube.q) * cube.center). A box with a local offset (cube.center or cube.q not
+//    the identity) that moves is not on this path (step() throws).
+//  - Statics driven by a trajectory (C_StaticTrajectory): each step runs Trajectory::update
 //    (trajectory.cpp:69-120; the reference runs it inside updateStateDependentTerms, after the first
 //    drift, and what it computes does not depend on that drift) and hands the poses and twists it
 //    set to cdx_set_static_motion, which applies them at the same point of the step; afterwards
 //    their pose and twist come back from the context (cdx_get_static_state).
-//  - Other dynamic shapes (boxes, meshes, capsules, cones, cylinders), dynamic planes, point
+//  - Dynamic shapes other than spheres (boxes, meshes, capsules, cones, cylinders), dynamic planes, point
 //    masses without C_RB_Sphere, constraints and soft bodies are not on this path: step() throws
 //    std::runtime_error, as the reference's own components throw on what they cannot handle.
 //  - precision: CDX_PRECISION_FP64 (bit-identical to the reference restatement) or
@@ -277,6 +282,8 @@ class GpuMoreauIntegrator : public IntegrationBase {
         const size_t nplanes = planes.size();
         for (auto e : reg.view<C_RB_Cylinder>())
             if (!reg.all_of<C_PhysicsObject>(e)) planes.push_back(e);  // dynamic cylinders threw above
+        for (auto e : reg.view<C_RB_Cube>())
+            if (!reg.all_of<C_PhysicsObject>(e)) planes.push_back(e);  // dynamic boxes threw above
         const size_t n = m_spheres.size(), ns = planes.size();
         (void)dynamic;
         m_traj.clear();
@@ -304,13 +311,30 @@ class GpuMoreauIntegrator : public IntegrationBase {
         }
         std::vector<int32_t> kind(ns, CDX_STATIC_HALFSPACE);
         std::vector<double> spos(3 * ns), squat(4 * ns), svel(3 * ns, 0.0), somega(3 * ns, 0.0), sdir(3 * ns),
-            srad(ns, 0.0), smu(ns), srn(ns), srt(ns), shl(ns, 0.0);
+            srad(ns, 0.0), smu(ns), srn(ns), srt(ns), shl(ns, 0.0), she(3 * ns, 0.0);
         for (size_t s = 0; s < ns; ++s) {
             const entt::entity e = planes[s];
-            const auto& x = reg.get<C_Position3>(e).value;
+            Vector3r x = reg.get<C_Position3>(e).value;
             const auto& o = reg.get<C_Orientation>(e);
+            Quaternion4r q = o.value;
             Vector3r nw;
-            if (s < nplanes) {
+            if (reg.all_of<C_RB_Cube>(e)) {
+                const auto& cb = reg.get<C_RB_Cube>(e);
+                const bool offset = cb.center.squaredNorm() > 0 || cb.q.vec().squaredNorm() > 0;
+                if (offset) {
+                    const bool moves = reg.all_of<C_StaticTrajectory>(e) ||
+                                       (reg.all_of<C_LinearVelocity3>(e) && reg.get<C_LinearVelocity3>(e).value.squaredNorm() > 0) ||
+                                       (reg.all_of<C_AngularVelocity3>(e) && reg.get<C_AngularVelocity3>(e).value.squaredNorm() > 0);
+                    if (moves)
+                        throw std::runtime_error("GpuMoreauIntegrator: a moving box with a local offset is not on the GPU path");
+                    q = q * cb.q;
+                    q.normalize();
+                    x = x + q * cb.center;
+                }
+                kind[s] = CDX_STATIC_BOX;
+                for (int k = 0; k < 3; ++k) she[3 * s + k] = cb.halfExtents[k];
+                nw = Vector3r::Zero();
+            } else if (s < nplanes) {
                 // the halfspace normal in the world frame (CollisionCoal builds it from C_RB_Plane's
                 // normal and the entity pose, collision_coal.cpp:290-296)
                 nw = o.rotation * reg.get<C_RB_Plane>(e).normal.normalized();
@@ -327,10 +351,10 @@ class GpuMoreauIntegrator : public IntegrationBase {
                 spos[3 * s + k] = x[k];
                 sdir[3 * s + k] = nw[k];
             }
-            squat[4 * s + 0] = o.value.x();
-            squat[4 * s + 1] = o.value.y();
-            squat[4 * s + 2] = o.value.z();
-            squat[4 * s + 3] = o.value.w();
+            squat[4 * s + 0] = q.x();
+            squat[4 * s + 1] = q.y();
+            squat[4 * s + 2] = q.z();
+            squat[4 * s + 3] = q.w();
             if (reg.all_of<C_LinearVelocity3>(e))
                 for (int k = 0; k < 3; ++k) svel[3 * s + k] = reg.get<C_LinearVelocity3>(e).value[k];
             if (reg.all_of<C_AngularVelocity3>(e))
@@ -369,6 +393,7 @@ class GpuMoreauIntegrator : public IntegrationBase {
         sc.static_rest_t = srt.data();
         sc.num_scenes = 1;
         sc.static_half_length = shl.data();
+        sc.static_half_extents = she.data();
         check(cdx_load_scene(m_ctx, &sc));
         m_dt = dt;
         m_world.m_structure_dirty = false;

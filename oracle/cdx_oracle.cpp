@@ -52,6 +52,10 @@ inline void rotmat(const double* q, double* R) {
 inline void matTvec(const double* R, const double* v, double* o) {
     for (int i = 0; i < 3; ++i) o[i] = (R[0 + i] * v[0] + R[3 + i] * v[1]) + R[6 + i] * v[2];
 }
+// R v (bodyToInertialVector, src/rigid_body/transformations.hpp:38-40)
+inline void matvec(const double* R, const double* v, double* o) {
+    for (int i = 0; i < 3; ++i) o[i] = (R[3 * i] * v[0] + R[3 * i + 1] * v[1]) + R[3 * i + 2] * v[2];
+}
 
 // src/misc/math_helper.hpp:11-17 (alignQuaternionTo) with Eigen's normalize()
 inline void align_quat(double* q, const double* qref) {
@@ -130,7 +134,7 @@ struct Engine {
     std::vector<int32_t> scene;
     std::vector<double> minv, Mdiag;  // per DOF (6 per body)
     std::vector<int32_t> skind, sscene;
-    std::vector<double> spos, sq, sv, sw, sdir, srad, sd, smu, srn, srt, sR, shl;
+    std::vector<double> spos, sq, sv, sw, sdir, srad, sd, smu, srn, srt, sR, shl, sax, she;
     // warm-start memory of the previous step (canonical order, sorted by key)
     std::vector<uint64_t> prev_keys;
     std::vector<double> prev_point, prev_lambda;
@@ -230,6 +234,58 @@ bool cylinder_geom(const double* xa, const double* u, double R, double h, const 
     return true;
 }
 
+// Sphere against a solid box (C_RB_Cube, coal::Box of full sides 2 halfExtents,
+// collision_coal.cpp:288-290), the exact nearest points in closed form. With the box's axes the
+// columns of R and c = R^T (xb - xa) the centre in its frame: outside (some |c_k| > e_k) the
+// nearest point is c clamped to the box and the normal runs from it to the centre; inside, the
+// nearest face (the lowest axis on a tie) gives the point and its outward normal. Normal from the
+// box to the sphere; coal's GJK/EPA reports the same points up to its own tolerance.
+bool box_geom(const double* xa, const double* R, const double* e, const double* xb, double rb, double margin,
+              double* p1, double* p2, double* nraw) {
+    double rel[3], c[3], ql[3], nl[3];
+    for (int k = 0; k < 3; ++k) rel[k] = xb[k] - xa[k];
+    matTvec(R, rel, c);
+    const bool out = std::fabs(c[0]) > e[0] || std::fabs(c[1]) > e[1] || std::fabs(c[2]) > e[2];
+    double sd;
+    if (!out) {
+        int f = 0;
+        double best = e[0] - std::fabs(c[0]);
+        for (int k = 1; k < 3; ++k) {
+            const double dk = e[k] - std::fabs(c[k]);
+            if (dk < best) {
+                best = dk;
+                f = k;
+            }
+        }
+        const double sg = c[f] < 0.0 ? -1.0 : 1.0;
+        for (int k = 0; k < 3; ++k) {
+            ql[k] = c[k];
+            nl[k] = 0.0;
+        }
+        ql[f] = sg * e[f];
+        nl[f] = sg;
+        sd = -best;
+    } else {
+        double d[3];
+        for (int k = 0; k < 3; ++k) {
+            ql[k] = c[k] < -e[k] ? -e[k] : (c[k] > e[k] ? e[k] : c[k]);
+            d[k] = c[k] - ql[k];
+        }
+        sd = norm3(d);
+        for (int k = 0; k < 3; ++k) nl[k] = d[k] / sd;
+    }
+    if (!((sd - rb) <= margin)) return false;
+    double n[3], q[3];
+    matvec(R, nl, n);
+    matvec(R, ql, q);
+    for (int k = 0; k < 3; ++k) {
+        p1[k] = xa[k] + q[k];
+        p2[k] = xb[k] - rb * n[k];
+        nraw[k] = n[k];
+    }
+    return true;
+}
+
 // Narrow phase for one (static, sphere) or (sphere, sphere) pair plus makeContact
 // (src/collision/collision_coal.cpp:112-163). Returns false when the shapes are apart
 // (distance > collision.security_margin, coal's ShapeShapeCollider rule).
@@ -254,8 +310,15 @@ bool make_contact(const Engine& E, int a_static, int a_body, int b_body, Contact
             }
         } else if (E.skind[s] == 2) {
             // solid cylinder (C_RB_Cylinder, coal::Cylinder(radius, 2 halfLength) along the axis;
-            // collision_coal.cpp:307-310): the nearest point of the side, a cap or a rim
-            if (!cylinder_geom(xa, &E.sdir[3 * s], E.srad[s], E.shl[s], xb, rb, margin, p1, p2, nraw)) return false;
+            // collision_coal.cpp:307-310): the nearest point of the side, a cap or a rim. Its axis
+            // turns with the static (coal places the shape with the object's transform each step,
+            // collision_coal.cpp:380-401): R times the axis in the static's frame.
+            double ua[3];
+            matvec(&E.sR[9 * s], &E.sax[3 * s], ua);
+            if (!cylinder_geom(xa, ua, E.srad[s], E.shl[s], xb, rb, margin, p1, p2, nraw)) return false;
+        } else if (E.skind[s] == 3) {
+            // solid box (C_RB_Cube), posed by the static's rotation
+            if (!box_geom(xa, &E.sR[9 * s], &E.she[3 * s], xb, rb, margin, p1, p2, nraw)) return false;
         } else {
             // hollow drum wall (new primitive; the reference has no counterpart)
             double rel[3];
@@ -1554,8 +1617,8 @@ CondResult pgs_solve(const Engine& E, const std::vector<Contact>& C, const Rows&
             r += dim;
         }
         res.iters = it + 1;
-        // check_residual (:142-151): the velocity-increment residual of u_corr, the sum in the
-        // fixed chunked order; a non-finite value throws "Projected Gauss-Seidel diverged"
+        // check_residual (:142-151): the velocity-increment residual of u_corr, summed in the
+        // fixed three-level order; a non-finite value throws "Projected Gauss-Seidel diverged"
         res.err = cond_residual(uf, uprev, u, E.cfg.pj_tol_rel, E.cfg.pj_tol_abs);
         if (!std::isfinite(res.err)) {
             res.diverged = true;
@@ -1780,6 +1843,15 @@ void* or_create(const or_config* cfg, const or_scene* sc) {
     if (sc->static_radius) E->srad.assign(sc->static_radius, sc->static_radius + S);
     E->shl.assign(S, 0.0);
     if (sc->static_half_length) E->shl.assign(sc->static_half_length, sc->static_half_length + S);
+    E->she.assign(3 * S, 0.0);
+    if (sc->static_half_extents) E->she.assign(sc->static_half_extents, sc->static_half_extents + 3 * S);
+    // a cylinder's axis in the static's own frame, R(q0)^T u
+    E->sax.assign(3 * S, 0.0);
+    for (size_t s = 0; s < S; ++s) {
+        double R0[9];
+        rotmat(&E->sq[4 * s], R0);
+        matTvec(R0, &E->sdir[3 * s], &E->sax[3 * s]);
+    }
     E->smu.assign(sc->static_mu, sc->static_mu + S);
     E->srn.assign(sc->static_rest_n, sc->static_rest_n + S);
     E->srt.assign(sc->static_rest_t, sc->static_rest_t + S);

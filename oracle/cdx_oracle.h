@@ -1,6 +1,6 @@
 /*
  * Oracle for the contact hot path: a CPU, FP64 restatement of CardilloCxx's Moreau midpoint step
- * for sphere scenes (grid broad phase, sphere-sphere / sphere-halfspace / sphere-drum narrow phase,
+ * for sphere scenes (grid broad phase, sphere-sphere / -halfspace / -drum / -cylinder / -box narrow phase,
  * projected Jacobi over disk-shaped Coulomb cones, velocity and quaternion update).
  *
  * TEST INFRASTRUCTURE ONLY. Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg
@@ -68,7 +68,7 @@ typedef struct or_scene {
     const double* rest_t;  /* [N] */
     const int32_t* body_scene; /* [N] or NULL */
     int32_t num_statics;
-    const int32_t* static_kind; /* 0 halfspace, 1 hollow drum, 2 solid cylinder */
+    const int32_t* static_kind; /* 0 halfspace, 1 hollow drum, 2 solid cylinder, 3 solid box */
     const double* static_pos;   /* [3S] */
     const double* static_quat;  /* [4S] */
     const double* static_vel;   /* [3S] world */
@@ -81,6 +81,7 @@ typedef struct or_scene {
     const int32_t* static_scene; /* [S] or NULL */
     int32_t num_scenes;
     const double* static_half_length; /* [S] cylinder half length, or NULL */
+    const double* static_half_extents; /* [3S] box half extents, or NULL */
 } or_scene;
 
 typedef struct or_stats {

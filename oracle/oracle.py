@@ -100,6 +100,7 @@ class OrScene(C.Structure):
         ("static_scene", _PI),
         ("num_scenes", C.c_int32),
         ("static_half_length", _P),
+        ("static_half_extents", _P),
     ]
 
 
@@ -222,6 +223,8 @@ class Oracle:
         sc.num_scenes = int(s.get("num_scenes", 1))
         if "static_half_length" in s:
             sc.static_half_length = _dp(s["static_half_length"])
+        if "static_half_extents" in s:
+            sc.static_half_extents = _dp(s["static_half_extents"])
         self.cfg = config_from(cfg, omp_mode, num_threads)
         self.h = self.L.or_create(C.byref(self.cfg), C.byref(sc))
         self.N = sc.num_bodies

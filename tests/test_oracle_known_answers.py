@@ -423,3 +423,112 @@ def test_sphere_rests_on_cylinder_cap_and_side(oracle_mod):
         lam = o.contacts()["lambda"][0]
         np.testing.assert_allclose(lam[0], m * G * H, rtol=1e-10)
         assert abs(o.state()["vel"][0, 2]) < 1e-12
+
+
+# ---- solid box (C_RB_Cube, coal::Box; collision_coal.cpp:288-290) ----
+def box(**kw):
+    b = {"kind": "box", "pos": (0.0, 0.0, 0.0), "half_extents": (0.3, 0.2, 0.1), "mu": 0.3}
+    b.update(kw)
+    return b
+
+
+def _rotz(deg):
+    a = math.radians(deg) / 2
+    return (0.0, 0.0, math.sin(a), math.cos(a))
+
+
+@pytest.mark.parametrize("centre, normal", [
+    ((0.1, -0.05, 0.14), (0.0, 0.0, 1.0)),                                  # on the top face
+    ((0.33, 0.05, 0.0), (1.0, 0.0, 0.0)),                                   # against the +x face
+    ((-0.1, -0.24, 0.02), (0.0, -1.0, 0.0)),                                # against the -y face
+    ((0.3 + 0.03, 0.0, 0.1 + 0.04), (0.6, 0.0, 0.8)),                       # on an edge: centre 0.05 from it
+    ((0.3 + 0.02, 0.2 + 0.02, 0.1 + 0.01), (2 / 3, 2 / 3, 1 / 3)),          # on a corner: centre 0.03 from it
+    ((0.28, 0.0, 0.0), (1.0, 0.0, 0.0)),                                    # centre inside, nearest +x
+    ((0.0, 0.0, -0.09), (0.0, 0.0, -1.0)),                                  # centre inside, nearest -z
+])
+@pytest.mark.parametrize("turn", [0.0, 30.0])
+def test_box_contact_geometry(oracle_mod, centre, normal, turn):
+    # zero gravity, at rest: one contact whose normal points from the box to the sphere, in the box's
+    # own axes (the box turned about z by `turn` degrees, the sphere with it)
+    r = 0.05
+    q = _rotz(turn)
+    c, s_ = math.cos(math.radians(turn)), math.sin(math.radians(turn))
+    rot = np.array([[c, -s_, 0.0], [s_, c, 0.0], [0.0, 0.0, 1.0]])
+    x = rot @ np.array(centre)
+    sc = make_scene([{"pos": tuple(x), "radius": r}], [box(quat=q)])
+    o = oracle_mod.Oracle(sc, cfg(**{"sim.gravity": (0.0, 0.0, 0.0)}))
+    o.step(1)
+    k = o.contacts()
+    assert k["id_a"].tolist() == [0] and k["id_b"].tolist() == [1]
+    np.testing.assert_allclose(k["normal"][0], rot @ np.array(normal), atol=1e-12)
+    # the point is the midpoint of the box's nearest point and the sphere's deepest point
+    n = rot @ np.array(normal)
+    loc = np.array(centre)
+    e = np.array([0.3, 0.2, 0.1])
+    if np.all(np.abs(loc) <= e):
+        f = int(np.argmin(e - np.abs(loc)))
+        qb = loc.copy()
+        qb[f] = math.copysign(e[f], loc[f])
+    else:
+        qb = np.clip(loc, -e, e)
+    np.testing.assert_allclose(k["point"][0], 0.5 * ((rot @ qb) + (x - r * n)), atol=1e-12)
+
+
+def test_box_far_sphere_has_no_contact(oracle_mod):
+    sc = make_scene([{"pos": (0.3 + 0.04, 0.2 + 0.04, 0.0), "radius": 0.05}], [box()])
+    o = oracle_mod.Oracle(sc, cfg(**{"sim.gravity": (0.0, 0.0, 0.0)}))
+    o.step(1)
+    # 0.04 * sqrt(2) = 0.0566 > 0.05 from the edge: apart
+    assert o.stats()["num_contacts"] == 0
+
+
+def test_sphere_rests_on_box_and_slides_on_it(oracle_mod):
+    r = 0.05
+    # resting on the top face of a box turned about z: the impulse carries the weight
+    s = make_scene([{"pos": (0.05, 0.02, 0.1 + r - 1e-9), "radius": r}], [box(quat=_rotz(40.0))])
+    m = s["mass"][0]
+    o = oracle_mod.Oracle(s, cfg())
+    o.step(1)
+    np.testing.assert_allclose(o.contacts()["lambda"][0][0], m * G * H, rtol=1e-10)
+    assert abs(o.state()["vel"][0, 2]) < 1e-12
+    # sliding along the top face: Coulomb friction takes mu g h a step off the speed
+    mu = 0.3
+    s = make_scene([{"pos": (0.0, 0.0, 0.1 + r - 1e-9), "radius": r, "vel": (1.0, 0.0, 0.0), "mu": mu}],
+                   [box(mu=mu, half_extents=(3.0, 3.0, 0.1))])
+    o = oracle_mod.Oracle(s, cfg())
+    o.step(1)
+    v = o.state()["vel"][0, 0]
+    assert 1.0 - mu * G * H - 1e-9 < v < 1.0
+
+
+def test_box_moves_with_its_prescribed_pose(oracle_mod):
+    # a box turned by a prescribed orientation carries its faces with it: a sphere above the +x end
+    # of a long thin box touches it only once the box is tilted up at that end
+    r = 0.05
+    sc = make_scene([{"pos": (0.9, 0.0, 0.1 + r + 0.05), "radius": r}],
+                    [box(half_extents=(1.0, 0.2, 0.1))])
+    o = oracle_mod.Oracle(sc, cfg(**{"sim.gravity": (0.0, 0.0, 0.0)}))
+    o.step(1)
+    assert o.stats()["num_contacts"] == 0
+    a = math.radians(4.0) / 2  # about -y: the +x end rises by 0.9 * sin(4 deg) = 0.063
+    o.set_static_motion([0], quat=[(0.0, -math.sin(a), 0.0, math.cos(a))])
+    o.step(1)
+    assert o.stats()["num_contacts"] == 1
+    c = o.contacts()
+    np.testing.assert_allclose(c["normal"][0], [-math.sin(2 * a), 0.0, math.cos(2 * a)], atol=1e-12)
+
+
+def test_cylinder_axis_turns_with_the_static(oracle_mod):
+    # coal poses the cylinder with the static's transform every step: a prescribed quarter turn about
+    # z swings a cylinder lying along x onto y, under a sphere that it did not reach before
+    r = 0.05
+    sc = make_scene([{"pos": (0.0, 0.32, 0.0), "radius": r}],
+                    [cyl(dir=(1.0, 0.0, 0.0), radius=0.1, half_length=0.3)])
+    o = oracle_mod.Oracle(sc, cfg(**{"sim.gravity": (0.0, 0.0, 0.0)}))
+    o.step(1)
+    assert o.stats()["num_contacts"] == 0
+    a = math.pi / 4
+    o.set_static_motion([0], quat=[(0.0, 0.0, math.sin(a), math.cos(a))])
+    o.step(1)
+    assert o.stats()["num_contacts"] == 1
+    np.testing.assert_allclose(o.contacts()["normal"][0], [0.0, 1.0, 0.0], atol=1e-12)

@@ -25,6 +25,27 @@ def test_partition_balances_sphere_counts():
     assert [list(p) for p in partition_scenes([5, 1, 4, 2], 2)] == [[0, 1], [2, 3]]
 
 
+def test_shard_keeps_every_per_static_array():
+    # cylinders and boxes carry per-static arrays beyond the halfspace's (half length, half extents):
+    # a shard takes its scenes' rows of every one of them
+    from cardillocxx_gb300.scenes import make_scene
+    from cardillocxx_gb300.shard import shard_scene
+    bodies = [{"pos": (0.0, 0.0, 0.5 + 0.2 * i), "radius": 0.05} for i in range(6)]
+    statics = [{"kind": "halfspace", "pos": (0, 0, 0), "dir": (0, 0, 1)},
+               {"kind": "cylinder", "pos": (0, 0, 0.2), "dir": (1, 0, 0), "radius": 0.1, "half_length": 0.3},
+               {"kind": "box", "pos": (0, 0, 0.1), "half_extents": (0.3, 0.2, 0.1)},
+               {"kind": "box", "pos": (0, 0, 0.1), "half_extents": (0.5, 0.6, 0.7)}]
+    s = make_scene(bodies, statics, scene_ids=[0, 0, 1, 1, 2, 2], static_scene_ids=[0, 1, 1, 2])
+    out, bsel = shard_scene(s, [1, 2])
+    assert out["static_kind"].tolist() == [2, 3, 3]
+    assert out["static_half_length"].tolist() == [0.3, 0.0, 0.0]
+    assert out["static_half_extents"].tolist() == [[0.0, 0.0, 0.0], [0.3, 0.2, 0.1], [0.5, 0.6, 0.7]]
+    assert out["static_scene"].tolist() == [0, 0, 1] and out["body_scene"].tolist() == [0, 0, 1, 1]
+    for k, v in out.items():
+        if k.startswith("static_") and isinstance(v, np.ndarray):
+            assert v.shape[0] == 3, k
+
+
 def _free_port():
     with socket.socket() as s:
         s.bind(("127.0.0.1", 0))
