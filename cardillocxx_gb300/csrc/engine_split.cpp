@@ -289,6 +289,15 @@ static int launch_coop(const Engine& E, const SplitBuf& sb, int gen, int v, cons
     la.check_vel = (c.pj_tol_abs == 0.0 && c.pj_tol_rel == 0.0) ? 0 : 1;
     la.restart_limit = c.pj_nesterov_restart_limit;
     la.nv = 6 * E.sc.N;
+    auto fits32 = [](double t) { return t >= 1e-12 && t <= 1e12; };
+    if (c.pj_tol_rel == 0.0 && c.pj_tol_abs > 0.0)
+        la.res_mode = 1;
+    else if (c.pj_tol_abs == 0.0 && c.pj_tol_rel > 0.0)
+        la.res_mode = 2;
+    else if (fits32(c.pj_tol_abs) && fits32(c.pj_tol_rel))
+        la.res_mode = 3;
+    else
+        la.res_mode = 0;
     return launch_s_solve_coop_loop(sb, gen, (float)c.pj_alpha, v, plan, max_iter, tol, max_sweeps, c.gpu_check_every,
                                     loop, la, wait_ns, s);
 }

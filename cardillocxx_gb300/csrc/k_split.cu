@@ -1204,6 +1204,31 @@ __device__ __forceinline__ double velres_body(float4 xv, float4 xw, float4 pv, f
     }
     return s;
 }
+// The same terms on the FP32 pipe (GB300's FP64 divisions made the residual cost more than the
+// sweep): mode 1 sums (x - xp)^2, mode 2 ((x - xp) / max(|x|, |xp|))^2 (the tolerance divides the
+// sum once, in FP64, so any tolerance stays exact), mode 3 the full term with both tolerances in
+// FP32's comfortable range. A body's few terms are summed in FP32, the bodies in FP64.
+__device__ __forceinline__ float velres_body32(float4 xv, float4 xw, float4 pv, float4 pw, int mode, float tr,
+                                               float ta) {
+    const float x[6] = {xv.x, xv.y, xv.z, xw.x, xw.y, xw.z};
+    const float p[6] = {pv.x, pv.y, pv.z, pw.x, pw.y, pw.z};
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        const float dx = x[k] - p[k];
+        float d = dx;
+        if (mode == 2)
+            d = dx / fmaxf(fabsf(x[k]), fabsf(p[k]));
+        else if (mode == 3)
+            d = dx / (fmaxf(fabsf(x[k]), fabsf(p[k])) * tr + ta);
+        s += d * d;
+    }
+    return s;
+}
+__device__ __forceinline__ float nes_dot_body32(float4 yv, float4 yw, float4 v1, float4 w1, float4 v0, float4 w0) {
+    return ((yv.x - v1.x) * (v1.x - v0.x) + (yv.y - v1.y) * (v1.y - v0.y) + (yv.z - v1.z) * (v1.z - v0.z)) +
+           ((yw.x - w1.x) * (w1.x - w0.x) + (yw.y - w1.y) * (w1.y - w0.y) + (yw.z - w1.z) * (w1.z - w0.z));
+}
 // (y - x1) . (x1 - x0) over one body's six velocities (nesterov_loop's restart test), in FP64
 __device__ __forceinline__ double nes_dot_body(float4 yv, float4 yw, float4 v1, float4 w1, float4 v0, float4 w0) {
     return ((double)yv.x - v1.x) * ((double)v1.x - v0.x) + ((double)yv.y - v1.y) * ((double)v1.y - v0.y) +
@@ -1373,22 +1398,30 @@ __global__ void __launch_bounds__(NTH, 1) k_s_solve_coop_loop(SplitBuf sb, int g
             // (and Nesterov's restart dot product), over the block's own bodies, then over the grid
             double e = 0.0, d = 0.0;
             const float4* XK = sb.acc[L.ixk];
+            const int rm = la.res_mode;
+            const float tr32 = (float)la.tol_rel, ta32 = (float)la.tol_abs;
             for (int i = tid; i < nbb; i += NTH) {
                 float4 v1, w1, v0, w0;
                 ldcg_body(&Add[2 * (bb + i)], v1, w1);
                 ldcg_body(&G[2 * (bb + i)], v0, w0);
-                e += velres_body(v1, w1, v0, w0, la.tol_rel, la.tol_abs);
+                if (rm)
+                    e += (double)velres_body32(v1, w1, v0, w0, rm, tr32, ta32);
+                else
+                    e += velres_body(v1, w1, v0, w0, la.tol_rel, la.tol_abs);
                 if (NES) {
                     float4 vk, wk;
                     ldcg_body(&XK[2 * (bb + i)], vk, wk);
-                    d += nes_dot_body(v0, w0, v1, w1, vk, wk);
+                    d += rm ? (double)nes_dot_body32(v0, w0, v1, w1, vk, wk) : nes_dot_body(v0, w0, v1, w1, vk, wk);
                 }
             }
             block_sum2d(e, d);
             grid_arrive_sum(&ss->bar, sb.sums, ++epoch, e, d);
             if (!grid_wait_sum(&ss->bar, sb.sums, epoch, bbase, &ss->err, e, d, wait_ns)) return;
             if (tid == 0) {
-                L.verr = (1.0 / sqrt((double)la.nv)) * sqrt(e);
+                double verr = (1.0 / sqrt((double)la.nv)) * sqrt(e);
+                if (rm == 1) verr /= la.tol_abs;
+                if (rm == 2) verr /= la.tol_rel;
+                L.verr = verr;
                 L.dot = d;
             }
             __syncthreads();

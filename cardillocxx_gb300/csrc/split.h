@@ -58,7 +58,10 @@ struct CoopLoopArgs {
     int check_vel;             // standard loop: the exit is on (the tolerances are not both 0)
     int restart_limit;         // pj.nesterov_restart_limit
     int nv;                    // velocities (6 per body)
-    int pad;
+    // how the velocity-increment residual is summed: 0 in FP64 term by term; 1 (pj.tol_rel = 0) the
+    // squared increments in FP32, divided by tol_abs once; 2 (pj.tol_abs = 0) the squared relative
+    // increments in FP32, divided by tol_rel once; 3 (both in [1e-12, 1e12]) term by term in FP32
+    int res_mode;
 };
 
 struct SplitParams {
