@@ -138,7 +138,7 @@ static int split_alpha_bufs(Engine& E) {
         if ((st = salloc(E, (void**)&S->scene_out, sizeof(int4) * ns, "scene alpha"))) return st;
         S->scene_bufs_n = ns;
         launch_s_tune_alpha(0, ns, (float)E.cfg.pj_alpha, nullptr, S->tune_best, nullptr, E.stream);
-        launch_s_tune_alpha(2, ns, 0.f, nullptr, S->tune_best, S->scene_alpha, E.stream);
+        launch_s_tune_alpha(2, ns, (float)E.cfg.pj_alpha, nullptr, S->tune_best, S->scene_alpha, E.stream);
         S->alpha_tuned_step = -1;
     }
     if (S->lam_save_cap < S->sb.cap) {
@@ -146,6 +146,8 @@ static int split_alpha_bufs(Engine& E) {
         if ((st = salloc(E, (void**)&S->lam_save, sizeof(float4) * std::max<int64_t>(S->sb.cap, 1), "scene alpha")))
             return st;
         S->lam_save_cap = S->sb.cap;
+        S->sb.lam_warm = S->lam_save;
+        destroy_graphs(S);  // a captured step holds the old address
     }
     return CDX_OK;
 }
@@ -188,7 +190,7 @@ static int split_tune_alpha(Engine& E, int gen, int scene_v, int maxit, const in
     launch_s_reset(sb, E.stream);
     launch_s_acc_init(sb, E.stream);
     launch_s_apply_warm(sb, gen, cblocks, E.stream);
-    launch_s_tune_alpha(2, ns, 0.f, nullptr, S->tune_best, S->scene_alpha, E.stream);
+    launch_s_tune_alpha(2, ns, a0, nullptr, S->tune_best, S->scene_alpha, E.stream);
     E.launches += 4;
     S->alpha_tuned_step = E.steps;
     ++S->alpha_tunings;

@@ -1565,11 +1565,13 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_s_solve_scenes(Scene sc, Spli
     // A tuned alpha above the configured one can lose stability when the scene's contacts change
     // after the tuning (projected Jacobi converges for alpha < 2 / the largest eigenvalue of
     // D^-1/2 W D^-1/2, and new contacts raise it). Divergence grows the impulses geometrically
-    // while their relative change stays level, so the stop rule does not see it: once the largest
-    // impulse exceeds 64 times its largest over the first 8 sweeps, the scene restarts from zero
-    // impulses at the configured alpha, which it keeps from then on.
-    bool guard = scene_alpha != nullptr && a_s > alpha_ref;  // block-uniform
-    float lm_ref = 0.f;
+    // while their relative change stays level, so the stop rule does not see it; near the bound the
+    // projections can also hold the impulses in a bounded oscillation. Once the largest impulse
+    // exceeds 16 times its largest over the first 8 sweeps, or the residual has not halved from
+    // sweep 32 to sweep 256, the scene starts over from its warm start (kept aside at the start)
+    // at the configured alpha, which it keeps from then on.
+    bool guard = scene_alpha != nullptr && a_s > alpha_ref && sb.lam_warm != nullptr;  // block-uniform
+    float lm_ref = 0.f, r32 = 0.f;
     const int64_t nflag = (int64_t)sc.N * L;
     int n_static = 0;
     if (nflag > 0) n_static = spos[nflag - 1] + sflags[nflag - 1];
@@ -1593,6 +1595,11 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_s_solve_scenes(Scene sc, Spli
             q0s[k] = ldg4(&sb.rec0[c]);
             q1s[k] = ldg4(&sb.rec1[c]);
             ls[k] = lamp[c];
+        }
+    if (guard)
+        for (int k = tid; k < nc; k += NT) {
+            const int c = k < ns ? cs0 + k : cp0 + (k - ns);
+            sb.lam_warm[c] = lamp[c];
         }
     __syncthreads();
     int it = 0;
@@ -1656,24 +1663,39 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_s_solve_scenes(Scene sc, Spli
         ++it;
         if (guard) {
             const float lmax = s_l;
+            if (it == 32) r32 = r;
             if (it <= 8) {
                 lm_ref = fmaxf(lm_ref, lmax);
-            } else if (!(r == r) || !(lmax <= 64.f * lm_ref)) {
+            } else if (!(r == r) || !(lmax <= 16.f * lm_ref) || (it == 256 && !(r <= 0.5f * r32))) {
                 guard = false;
                 a_s = alpha_ref;
                 rscale = 1.f;
                 if (tid == 0) scene_alpha[s] = alpha_ref;
-                for (int k = tid; k < nc; k += NT) {
-                    if (local)
-                        ls[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-                    else
-                        lamp[k < ns ? cs0 + k : cp0 + (k - ns)] = make_float4(0.f, 0.f, 0.f, 0.f);
-                }
-                // the next sweep gathers accumulator it % 3: back to the free velocities
+                // the next sweep gathers accumulator it % 3: the free velocities plus M^-1 W^T of
+                // the warm start, as the step's warm start left them
                 float4* Gx = sb.acc[it % 3];
                 for (int i = tid; i < nb; i += NT) {
                     const float4 v0 = ldg4(&sb.vel4[2 * (b0 + i)]), w0 = ldg4(&sb.vel4[2 * (b0 + i) + 1]);
                     stcg_body(&Gx[2 * (b0 + i)], v0, w0);
+                }
+                __syncthreads();
+                for (int k = tid; k < nc; k += NT) {
+                    const int c = k < ns ? cs0 + k : cp0 + (k - ns);
+                    const float4 l = sb.lam_warm[c];
+                    if (local)
+                        ls[k] = l;
+                    else
+                        lamp[c] = l;
+                    if (l.x == 0.f && l.y == 0.f && l.z == 0.f) continue;
+                    const float4 r0 = local ? q0s[k] : ldg4(&sb.rec0[c]);
+                    const float4 r1 = local ? q1s[k] : ldg4(&sb.rec1[c]);
+                    const int a = __float_as_int(r1.z), b = __float_as_int(r1.w);
+                    const float3 n = f3(r0);
+                    float3 t1, t2;
+                    frame32(n, t1, t2);
+                    const float imb = sb.vel4[2 * b].w, iib = sb.vel4[2 * b + 1].w;
+                    const float ima = a >= 0 ? sb.vel4[2 * a].w : 0.f, iia = a >= 0 ? sb.vel4[2 * a + 1].w : 0.f;
+                    scatter(Gx, a, b, n, t1, t2, r1.x, r1.y, l.x, l.y, l.z, imb, iib, ima, iia);
                 }
                 __syncthreads();
                 if (it >= max_iter) break;
@@ -1738,9 +1760,14 @@ __global__ void k_s_tune_pick(int ns, float cand, const int4* out, float4* best,
     const int bit = __float_as_int(b.x);
     if (it < bit || (it == bit && r < b.y)) best[s] = make_float4(__int_as_float(it), r, cand, b.w);
 }
-__global__ void k_s_tune_commit(int ns, const float4* best, float* scene_alpha) {
+// A pick above the configured alpha is kept with a 15 % margin below it: the trial shows the pick
+// stable on this step's contacts, and the next steps' contacts can lower the bound it sits under.
+__global__ void k_s_tune_commit(int ns, const float4* best, float* scene_alpha, float alpha_ref) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s < ns) scene_alpha[s] = best[s].z;
+    if (s < ns) {
+        const float a = best[s].z;
+        scene_alpha[s] = a > alpha_ref ? fmaxf(alpha_ref, 0.85f * a) : a;
+    }
 }
 
 __global__ void k_s_totals(SplitBuf sb, const int32_t* spos, const int32_t* sflags, int64_t nflag,
@@ -2229,7 +2256,7 @@ void launch_s_tune_alpha(int op, int ns, float alpha, const int4* out, float4* b
     if (ns <= 0) return;
     if (op == 0) k_s_tune_init<<<nblk(ns), NT, 0, s>>>(ns, alpha, best);
     if (op == 1 || op == 3) k_s_tune_pick<<<nblk(ns), NT, 0, s>>>(ns, alpha, out, best, op == 3);
-    if (op == 2) k_s_tune_commit<<<nblk(ns), NT, 0, s>>>(ns, best, scene_alpha);
+    if (op == 2) k_s_tune_commit<<<nblk(ns), NT, 0, s>>>(ns, best, scene_alpha, alpha);
 }
 void launch_s_acc_init(const SplitBuf& sb, cudaStream_t s) {
     if (sb.N > 0) k_s_acc_init<<<nblk(sb.N), NT, 0, s>>>(sb);

@@ -124,6 +124,7 @@ struct SplitBuf {
     float2* recs = nullptr;   // cooperative solve: 2 banks x per-block (max ||dlambda||, max |lambda|)
     double2* sums = nullptr;  // cooperative solve: 2 banks x per-block sums (velocity-increment residual, dot)
     float4* lamk = nullptr;   // Nesterov: the previous iterate's impulses (contacts outside shared memory)
+    float4* lam_warm = nullptr;  // per-scene solve with tuned alpha: each guarded scene's starting impulses
     int has_restitution = 0;  // pre-solve velocities are only needed for restitution terms
 };
 

@@ -382,7 +382,9 @@ def test_batched_scenes_alpha_autotuner(gpu):
         # every scene stopped on the tolerance, not at the cap
         assert it.max() < 400 and e.stats()["residual_last"] <= 1e-4 * 1.0001
     a = tuned.scene_solve(ns)["alpha"]
-    cand = {0.2, 0.3, 0.4, 0.5, 0.6, 0.7, 0.85, 1.0, float(base["pj.alpha"])}
+    a0 = float(base["pj.alpha"])
+    # a pick above pj.alpha is kept with a 15 % margin below it
+    cand = {c if c <= a0 else max(a0, 0.85 * c) for c in (0.2, 0.3, 0.4, 0.5, 0.6, 0.7, 0.85, 1.0, a0)}
     assert all(any(abs(x - c) < 1e-6 for c in cand) for x in a), a
     assert np.allclose(plain.scene_solve(ns)["alpha"], base["pj.alpha"])
     # the tuner keeps pj.alpha where no candidate beats it; the FP32 reductions' order varies, so
