@@ -332,7 +332,7 @@ def at_residual_leg(a, scene, cfg, flush):
     warm_s = time.time() - t0
     s2 = with_state(scene, state)
     rule = {"gpu.residual_tol": tol, "pj.max_iterations": a.residual_cap}
-    split_tol = 0.9 * tol
+    split_tol = 0.98 * tol
     out = {"residual_tol": tol, "sweep_cap": a.residual_cap, "warm_steps": a.warm_steps,
            "warm_form": "fp64, the pile's configuration (100 sweeps or residual 1e-6)",
            "warm_state_digest": scenes.state_digest(state),
@@ -341,8 +341,8 @@ def at_residual_leg(a, scene, cfg, flush):
            "stop_test": "every 10 sweeps in every form (gpu.check_every = 10: the plain FP64 method's host polls "
                         "the residual every 10 sweeps, the split form's device tests it every 10 sweeps)"}
     # The split form stops on its FP32 in-sweep residual; the FP64 residual of its result is
-    # evaluated afterwards on FP64 geometry and runs a few percent above, so the split forms stop at
-    # 0.9e-6 for their FP64 residual to stay within 1e-6. Nesterov runs with a velocity tolerance
+    # evaluated afterwards on FP64 geometry and ran up to 0.1 % above it, so the split forms stop at
+    # 0.98e-6 for their FP64 residual to stay within 1e-6. Nesterov runs with a velocity tolerance
     # too small to end the loop, so the residual ends it.
     forms = {"split": {"gpu.precision": "split", "gpu.check_every": 10, "gpu.residual_tol": split_tol},
              "fp64": {"gpu.precision": "fp64", "gpu.check_every": 10},

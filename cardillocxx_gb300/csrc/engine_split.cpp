@@ -429,6 +429,7 @@ int Engine::step_split() {
     SplitParams P;
     P.alpha = (float)cfg.pj_alpha;
     P.margin = (float)cfg.collision_security_margin;
+    P.margin64 = cfg.collision_security_margin;
     P.match2 = (float)(cfg.collision_match_max_dist * cfg.collision_match_max_dist);
     P.combine = cfg.friction_combine;
     P.friction_enable = cfg.friction_enable;
@@ -571,7 +572,7 @@ int Engine::step_split() {
     launches += 8;
     const int64_t nflag = (int64_t)N * sc.max_statics;
     if (nflag > 0) {
-        launch_s_static_flags(sc, sb, P.margin, sflags, stream);
+        launch_s_static_flags(sc, sb, P.margin, P.margin64, sflags, stream);
         if ((st = cuda_check(exclusive_scan(tmp, tmp_bytes, sflags, spos, nflag, stream), "scan"))) return st;
         launches += 3;
     }

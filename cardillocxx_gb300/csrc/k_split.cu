@@ -323,7 +323,39 @@ __device__ __forceinline__ bool static_test32(const SplitBuf& sb, int s, float3 
     return true;
 }
 
-__global__ void k_s_static_flags(Scene sc, SplitBuf sb, float margin, int32_t* flags) {
+// Contact membership near the threshold. The FP32 distance of a pair or of a sphere and a static
+// is off the FP64 one by the rounding of the FP32 coordinates (relative to the scene origin): at
+// most a few 1e-7 of the coordinates' magnitude. A settled pile rests on contacts whose gaps are
+// that small, so FP32 alone admitted and dropped hundreds of them from step to step (each new one
+// starting from a zero impulse, each lost one unloading its spheres), and a warm-started step
+// that the FP64 method solved in 26 sweeps took the split form about 2,000. So the FP32 test only
+// settles the pairs farther than a band of 5e-7 (1 + the largest coordinate) from the threshold;
+// inside the band the FP64 distance, on the FP64 positions, decides.
+__device__ __forceinline__ void geom64(const Scene& sc, int a, int b, double* n, double& rhoA, double& rhoB);
+__device__ __forceinline__ float band32(float3 x, float3 y) {
+    const float m = fmaxf(fmaxf(fmaxf(fabsf(x.x), fabsf(x.y)), fabsf(x.z)), fmaxf(fmaxf(fabsf(y.x), fabsf(y.y)), fabsf(y.z)));
+    return 5e-7f * (1.f + m);
+}
+// the FP64 distance of a pair (a >= 0) or of static -a-1 and sphere b, against the margin
+__device__ __forceinline__ bool member64(const Scene& sc, int a, int b, double margin) {
+    double n[3], rA, rB;
+    geom64(sc, a, b, n, rA, rB);
+    // rhoB = -(gap + r_b) / 2 for statics and (r_a - r_b - |d|) / 2 for pairs: -2 rhoB - 2 r_b is the gap
+    return (-2.0 * rB - 2.0 * sc.bf(BF_RAD)[b]) <= margin;
+}
+__device__ __forceinline__ bool static_member(const Scene& sc, const SplitBuf& sb, int st, int i, float4 p, float margin,
+                                              double margin64) {
+    CGeom32 g;
+    const float4 pp = sb.st_pt[st], dd = sb.st_dir[st];
+    float ext = fabsf(pp.w) + fabsf(dd.w);
+    if (sb.st_v[st].w == 3.f) ext += fmaxf(fmaxf(sb.st_box[3 * st].w, sb.st_box[3 * st + 1].w), sb.st_box[3 * st + 2].w);
+    const float band = band32(f3(p), f3(pp)) + 5e-7f * ext;
+    if (!static_test32(sb, st, f3(p), p.w, margin + band, g)) return false;
+    if (static_test32(sb, st, f3(p), p.w, margin - band, g)) return true;
+    return member64(sc, -st - 1, i, margin64);
+}
+
+__global__ void k_s_static_flags(Scene sc, SplitBuf sb, float margin, double margin64, int32_t* flags) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= sc.N) return;
     const int s = sc.body_scene[i];
@@ -333,10 +365,7 @@ __global__ void k_s_static_flags(Scene sc, SplitBuf sb, float margin, int32_t* f
     const int L = sc.max_statics;
     for (int l = 0; l < L; ++l) {
         int f = 0;
-        if (l < nst) {
-            CGeom32 g;
-            f = static_test32(sb, st0 + l, f3(p), p.w, margin, g) ? 1 : 0;
-        }
+        if (l < nst) f = static_member(sc, sb, st0 + l, i, p, margin, margin64) ? 1 : 0;
         flags[(size_t)b0 * L + (size_t)l * ns_b + (i - b0)] = f;
     }
 }
@@ -424,7 +453,7 @@ __global__ void k_s_static_write(Scene sc, SplitBuf sb, const int32_t* flags, co
         if (!flags[slot]) continue;
         const int st = st0 + l;
         CGeom32 g;
-        static_test32(sb, st, f3(p), p.w, P.margin, g);
+        static_test32(sb, st, f3(p), p.w, INFINITY, g);  // the flag decided membership; this fills the geometry
         const float3 pt = f3(p) + g.rhoB * g.n;
         const float3 wv = f3(sb.st_v[st]), ww = f3(sb.st_w[st]), wp = f3(sb.st_pt[st]);
         const bool moving = (wv.x != 0.f || wv.y != 0.f || wv.z != 0.f || ww.x != 0.f || ww.y != 0.f || ww.z != 0.f);
@@ -497,9 +526,14 @@ __global__ void k_s_pairs(Scene sc, Grid gr, SplitBuf sb, const uint32_t* cell_b
                 if (j <= i) continue;
                 const float4 pj = sb.pos4[j];
                 const float dx = pj.x - pi.x, dy2 = pj.y - pi.y, dz2 = pj.z - pi.z;
+                const float d2 = dx * dx + dy2 * dy2 + dz2 * dz2;
                 const float lim = pi.w + pj.w + P.margin;
-                if (dx * dx + dy2 * dy2 + dz2 * dz2 > lim * lim) continue;
+                const float band = band32(f3(pi), f3(pj));
+                const float hi = lim + band;
+                if (d2 > hi * hi) continue;
                 if (sc.body_scene[j] != si) continue;
+                const float lo = lim - band;
+                if (!(lo > 0.f && d2 <= lo * lo) && !member64(sc, i, j, P.margin64)) continue;
                 if (WRITE) {
                     if (cnt < MAX_PAIR) list[cnt] = j;
                 } else if (cnt < SPLIT_PLIST) {
@@ -2404,9 +2438,10 @@ void launch_s_prep(const Scene& sc, const SplitBuf& sb, double dt, const double*
     if (sc.N + sc.S == 0) return;
     k_s_prep<<<nblk(sc.N + sc.S), NT, 0, s>>>(sc, sb, dt, g[0], g[1], g[2], h1, implicit_gyro, smot, smflag);
 }
-void launch_s_static_flags(const Scene& sc, const SplitBuf& sb, float margin, int32_t* flags, cudaStream_t s) {
+void launch_s_static_flags(const Scene& sc, const SplitBuf& sb, float margin, double margin64, int32_t* flags,
+                           cudaStream_t s) {
     if (sc.N == 0) return;
-    k_s_static_flags<<<nblk(sc.N), NT, 0, s>>>(sc, sb, margin, flags);
+    k_s_static_flags<<<nblk(sc.N), NT, 0, s>>>(sc, sb, margin, margin64, flags);
 }
 void launch_s_pair_count(const Scene& sc, const Grid& g, const SplitBuf& sb, const uint32_t* cell_body,
                          const uint32_t* cell_key, const int32_t* cell_start, const int32_t* cell_end, int32_t* counts,

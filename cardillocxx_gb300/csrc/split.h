@@ -67,6 +67,7 @@ struct CoopLoopArgs {
 struct SplitParams {
     float alpha;
     float margin;
+    double margin64;  // collision.security_margin in FP64: membership decided near the threshold
     float match2;
     int combine;
     int friction_enable;
@@ -180,7 +181,8 @@ int launch_s_solve_coop_loop(const SplitBuf& sb, int gen, float alpha, int v, co
 // smot/smflag (optional): prescribed static motion applied after the statics' first drift
 void launch_s_prep(const Scene& sc, const SplitBuf& sb, double dt, const double* g, double h1, cudaStream_t s,
                    int implicit_gyro = 0, const double* smot = nullptr, const int32_t* smflag = nullptr);
-void launch_s_static_flags(const Scene& sc, const SplitBuf& sb, float margin, int32_t* flags, cudaStream_t s);
+void launch_s_static_flags(const Scene& sc, const SplitBuf& sb, float margin, double margin64, int32_t* flags,
+                           cudaStream_t s);
 // cell_body / cell_key: the bodies and their cell keys sorted by cell
 void launch_s_pair_count(const Scene& sc, const Grid& g, const SplitBuf& sb, const uint32_t* cell_body,
                          const uint32_t* cell_key, const int32_t* cell_start, const int32_t* cell_end, int32_t* counts,

@@ -393,3 +393,24 @@ def test_batched_scenes_alpha_autotuner(gpu):
     vscale = np.abs(st["vel"]).max() + 9.81e-3
     assert np.isfinite(tuned.state()["vel"]).all()
     assert np.abs(tuned.state()["vel"] - plain.state()["vel"]).max() <= 1e-2 * vscale
+
+
+def test_split_contact_set_equals_fp64_on_the_settled_pile(gpu):
+    # the FP32 narrow phase leaves the pairs within a few 1e-7 of the threshold to the FP64
+    # distance: from the settled 200k pile at rest (its resting contacts have gaps of that size)
+    # the split form finds exactly the FP64 method's contacts
+    import os
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "pile_200k_settled.npz")
+    s = scenes.settled_pile(path)
+    cfg = scenes.config_for("pile_200k")
+    out = {}
+    for prec in ("fp64", "split"):
+        e = PhysicsEngine(dict(cfg, **{"gpu.precision": prec})).load_scene(s)
+        e.step(1)
+        out[prec] = e.contacts()
+        e.close()
+    a, b = out["fp64"], out["split"]
+    ka = a["id_a"].astype(np.int64) << 32 | a["id_b"].astype(np.int64)
+    kb = b["id_a"].astype(np.int64) << 32 | b["id_b"].astype(np.int64)
+    assert ka.size > 400_000
+    assert np.array_equal(np.sort(ka), np.sort(kb))
