@@ -163,6 +163,7 @@ __global__ void k_s_prep(Scene sc, SplitBuf sb, double dt, double g0, double g1,
         sb.acc[2][2 * i + 1] = sb.vel4[2 * i + 1];
         const int s = sc.body_scene[i];
         const double* o = &sb.origin[3 * s];
+        sb.pos64[i] = make_double4(x[0], x[1], x[2], sc.bf(BF_RAD)[i]);
         sb.pos4[i] = make_float4((float)(x[0] - o[0]), (float)(x[1] - o[1]), (float)(x[2] - o[2]),
                                  (float)sc.bf(BF_RAD)[i]);
     } else if (i < sc.N + sc.S) {
@@ -329,19 +330,30 @@ __device__ __forceinline__ bool static_test32(const SplitBuf& sb, int s, float3 
 // that small, so FP32 alone admitted and dropped hundreds of them from step to step (each new one
 // starting from a zero impulse, each lost one unloading its spheres), and a warm-started step
 // that the FP64 method solved in 26 sweeps took the split form about 2,000. So the FP32 test only
-// settles the pairs farther than a band of 5e-7 (1 + the largest coordinate) from the threshold;
+// settles the pairs farther than a band of 3e-7 (1 + the largest coordinate + the radii and
+// extents) from the threshold (the rounding is at most 2.1e-7 of the largest coordinate, plus the
+// FP32 arithmetic's few 1e-7 of the lengths compared);
 // inside the band the FP64 distance, on the FP64 positions, decides.
 __device__ __forceinline__ void geom64(const Scene& sc, int a, int b, double* n, double& rhoA, double& rhoB);
 __device__ __forceinline__ float band32(float3 x, float3 y) {
     const float m = fmaxf(fmaxf(fmaxf(fabsf(x.x), fabsf(x.y)), fabsf(x.z)), fmaxf(fmaxf(fabsf(y.x), fabsf(y.y)), fabsf(y.z)));
-    return 5e-7f * (1.f + m);
+    return 3e-7f * (1.f + m);
 }
-// the FP64 distance of a pair (a >= 0) or of static -a-1 and sphere b, against the margin
-__device__ __forceinline__ bool member64(const Scene& sc, int a, int b, double margin) {
+// the FP64 distance of static -a-1 and sphere b against the margin (out of line: taken by few
+// spheres, it would otherwise hold its FP64 registers across the whole static loop)
+__device__ __noinline__ bool member64(const Scene& sc, int a, int b, double margin) {
     double n[3], rA, rB;
     geom64(sc, a, b, n, rA, rB);
-    // rhoB = -(gap + r_b) / 2 for statics and (r_a - r_b - |d|) / 2 for pairs: -2 rhoB - 2 r_b is the gap
+    // rhoB = -(gap + r_b) / 2 for statics: -2 rhoB - 2 r_b is the gap
     return (-2.0 * rB - 2.0 * sc.bf(BF_RAD)[b]) <= margin;
+}
+// a pair's FP64 test as squared lengths, |d|^2 <= (r_a + r_b + margin)^2: no square root on the
+// FP64 pipe (the FP64 method's (|d| - r_a) - r_b <= margin, up to its last bit)
+__device__ __forceinline__ bool pair_member64(const SplitBuf& sb, int a, int b, double margin) {
+    const double4 pa = sb.pos64[a], pb = sb.pos64[b];
+    const double dx = pb.x - pa.x, dy = pb.y - pa.y, dz = pb.z - pa.z;
+    const double L = (pa.w + pb.w) + margin;
+    return L >= 0.0 && dx * dx + dy * dy + dz * dz <= L * L;
 }
 __device__ __forceinline__ bool static_member(const Scene& sc, const SplitBuf& sb, int st, int i, float4 p, float margin,
                                               double margin64) {
@@ -349,13 +361,17 @@ __device__ __forceinline__ bool static_member(const Scene& sc, const SplitBuf& s
     const float4 pp = sb.st_pt[st], dd = sb.st_dir[st];
     float ext = fabsf(pp.w) + fabsf(dd.w);
     if (sb.st_v[st].w == 3.f) ext += fmaxf(fmaxf(sb.st_box[3 * st].w, sb.st_box[3 * st + 1].w), sb.st_box[3 * st + 2].w);
-    const float band = band32(f3(p), f3(pp)) + 5e-7f * ext;
+    const float band = band32(f3(p), f3(pp)) + 3e-7f * (ext + p.w);
     if (!static_test32(sb, st, f3(p), p.w, margin + band, g)) return false;
-    if (static_test32(sb, st, f3(p), p.w, margin - band, g)) return true;
+    // the FP32 gap: sep is the signed distance of the centre (the radial one for a drum's wall)
+    const float gap = sb.st_v[st].w == 1.f ? (pp.w - g.sep) - p.w : g.sep - p.w;
+    if (gap <= margin - band) return true;
     return member64(sc, -st - 1, i, margin64);
 }
 
-__global__ void k_s_static_flags(Scene sc, SplitBuf sb, float margin, double margin64, int32_t* flags) {
+// (at most 42 registers, as the pair kernels: one wave of 1,316 spheres an SM)
+__global__ void __launch_bounds__(256, 6) k_s_static_flags(Scene sc, SplitBuf sb, float margin, double margin64,
+                                                            int32_t* flags) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= sc.N) return;
     const int s = sc.body_scene[i];
@@ -468,8 +484,11 @@ __global__ void k_s_static_write(Scene sc, SplitBuf sb, const int32_t* flags, co
     }
 }
 
+// Six blocks of 256 an SM (at most 42 registers a thread): the 200k pile's 1,316 spheres an SM
+// then run in one wave; the FP64 test near the threshold had pushed the count pass to 54
+// registers and two waves (+70 us a step).
 template <bool WRITE>
-__global__ void k_s_pairs(Scene sc, Grid gr, SplitBuf sb, const uint32_t* cell_body, const uint32_t* cell_key,
+__global__ void __launch_bounds__(256, 6) k_s_pairs(Scene sc, Grid gr, SplitBuf sb, const uint32_t* cell_body, const uint32_t* cell_key,
                           const int32_t* cell_start, const int32_t* cell_end, int32_t* counts, const int32_t* offsets,
                           int32_t base, int gen, SplitParams P, DevScalars* ds) {
     // threads take the bodies in cell order, so a warp walks neighbouring cells (shared cache
@@ -528,12 +547,12 @@ __global__ void k_s_pairs(Scene sc, Grid gr, SplitBuf sb, const uint32_t* cell_b
                 const float dx = pj.x - pi.x, dy2 = pj.y - pi.y, dz2 = pj.z - pi.z;
                 const float d2 = dx * dx + dy2 * dy2 + dz2 * dz2;
                 const float lim = pi.w + pj.w + P.margin;
-                const float band = band32(f3(pi), f3(pj));
+                const float band = band32(f3(pi), f3(pj)) + 3e-7f * lim;
                 const float hi = lim + band;
                 if (d2 > hi * hi) continue;
                 if (sc.body_scene[j] != si) continue;
                 const float lo = lim - band;
-                if (!(lo > 0.f && d2 <= lo * lo) && !member64(sc, i, j, P.margin64)) continue;
+                if (!(lo > 0.f && d2 <= lo * lo) && !pair_member64(sb, i, j, P.margin64)) continue;
                 if (WRITE) {
                     if (cnt < MAX_PAIR) list[cnt] = j;
                 } else if (cnt < SPLIT_PLIST) {
