@@ -319,6 +319,7 @@ static int init_split(Engine& E) {
     const size_t n1 = std::max(1, N);
     if ((st = salloc(E, (void**)&b.pos4, sizeof(float4) * n1, "split bodies"))) return st;
     if ((st = salloc(E, (void**)&b.pos64, sizeof(double4) * n1, "split bodies"))) return st;
+    if ((st = salloc(E, (void**)&b.pos4lo, sizeof(float4) * n1, "split bodies"))) return st;
     if ((st = salloc(E, (void**)&b.plist, sizeof(int32_t) * SPLIT_PLIST * n1, "split bodies"))) return st;
     if ((st = salloc(E, (void**)&b.vel4, sizeof(float4) * 2 * n1, "split bodies"))) return st;
     for (int k = 0; k < SPLIT_NACC; ++k)

@@ -163,9 +163,13 @@ __global__ void k_s_prep(Scene sc, SplitBuf sb, double dt, double g0, double g1,
         sb.acc[2][2 * i + 1] = sb.vel4[2 * i + 1];
         const int s = sc.body_scene[i];
         const double* o = &sb.origin[3 * s];
-        sb.pos64[i] = make_double4(x[0], x[1], x[2], sc.bf(BF_RAD)[i]);
-        sb.pos4[i] = make_float4((float)(x[0] - o[0]), (float)(x[1] - o[1]), (float)(x[2] - o[2]),
-                                 (float)sc.bf(BF_RAD)[i]);
+        const double rad = sc.bf(BF_RAD)[i];
+        const double xr[3] = {x[0] - o[0], x[1] - o[1], x[2] - o[2]};
+        const float4 hi = make_float4((float)xr[0], (float)xr[1], (float)xr[2], (float)rad);
+        sb.pos64[i] = make_double4(x[0], x[1], x[2], rad);
+        sb.pos4[i] = hi;
+        sb.pos4lo[i] = make_float4((float)(xr[0] - (double)hi.x), (float)(xr[1] - (double)hi.y),
+                                   (float)(xr[2] - (double)hi.z), (float)(rad - (double)hi.w));
     } else if (i < sc.N + sc.S) {
         const int s = i - sc.N;
         double x[3] = {sc.sf(SF_PX)[s], sc.sf(SF_PY)[s], sc.sf(SF_PZ)[s]};
@@ -552,7 +556,19 @@ __global__ void __launch_bounds__(256, 6) k_s_pairs(Scene sc, Grid gr, SplitBuf 
                 if (d2 > hi * hi) continue;
                 if (sc.body_scene[j] != si) continue;
                 const float lo = lim - band;
-                if (!(lo > 0.f && d2 <= lo * lo) && !pair_member64(sb, i, j, P.margin64)) continue;
+                if (!(lo > 0.f && d2 <= lo * lo)) {
+                    // the band: coordinates and radii with what FP32 rounded off added back (the hi
+                    // differences of nearby values are exact or off by half an ulp of |d|), which
+                    // narrows the band to a few 1e-8 of the lengths compared; inside that, FP64
+                    const float4 li = sb.pos4lo[i], lj = sb.pos4lo[j];
+                    const float ex = (pj.x - pi.x) + (lj.x - li.x), ey = (pj.y - pi.y) + (lj.y - li.y);
+                    const float ez = (pj.z - pi.z) + (lj.z - li.z);
+                    const float e2 = ex * ex + ey * ey + ez * ez;
+                    const float L = (pi.w + pj.w) + ((li.w + lj.w) + P.margin);
+                    const float fb = 5e-8f + 3e-7f * L;
+                    if (e2 > (L + fb) * (L + fb)) continue;
+                    if (!(L - fb > 0.f && e2 <= (L - fb) * (L - fb)) && !pair_member64(sb, i, j, P.margin64)) continue;
+                }
                 if (WRITE) {
                     if (cnt < MAX_PAIR) list[cnt] = j;
                 } else if (cnt < SPLIT_PLIST) {

@@ -96,6 +96,7 @@ struct SplitBuf {
     int64_t cap = 0;
     float4* pos4 = nullptr;   // N: position relative to the scene origin, radius
     double4* pos64 = nullptr; // N: FP64 position and radius in one 32-byte record (the narrow phase's FP64 test)
+    float4* pos4lo = nullptr; // N: what pos4 rounded off (position relative to the scene origin, radius)
     // SPLIT_PLIST per body: the partners the narrow phase's count pass found (when they fit), so
     // the write pass does not walk the neighbour cells again
     int32_t* plist = nullptr;
