@@ -336,8 +336,10 @@ __device__ __forceinline__ bool static_test32(const SplitBuf& sb, int s, float3 
 // that the FP64 method solved in 26 sweeps took the split form about 2,000. So the FP32 test only
 // settles the pairs farther than a band of 3e-7 (1 + the largest coordinate + the radii and
 // extents) from the threshold (the rounding is at most 2.1e-7 of the largest coordinate, plus the
-// FP32 arithmetic's few 1e-7 of the lengths compared);
-// inside the band the FP64 distance, on the FP64 positions, decides.
+// FP32 arithmetic's few 1e-7 of the lengths compared); inside the band a pair is tested again in
+// FP32 with the rounded-off low parts of its coordinates and radii added back (a band of a few
+// 1e-8), and only inside that does the FP64 distance, on the FP64 positions, decide. A sphere and
+// a static go from the first band straight to FP64.
 __device__ __forceinline__ void geom64(const Scene& sc, int a, int b, double* n, double& rhoA, double& rhoB);
 __device__ __forceinline__ float band32(float3 x, float3 y) {
     const float m = fmaxf(fmaxf(fmaxf(fabsf(x.x), fabsf(x.y)), fabsf(x.z)), fmaxf(fmaxf(fabsf(y.x), fabsf(y.y)), fabsf(y.z)));
