@@ -2263,6 +2263,8 @@ static CoopVariant g_coop[] = {
     // settled 200k pile's 3,133 contacts an SM take three passes instead of four (9.9 against 10.4 us
     // a sweep)
     {k_s_solve_coop<576, 1, 2, 0, 2>, 576, 1, 2, 0, 0, 0, 2},
+    // (reductions without the warp run sums, AGG 1, measured 13.2 against 9.9 us a sweep at 1,024
+    // threads: the L2 serialises reductions to one address, so the run sums pay for themselves)
 };
 constexpr int N_COOP = sizeof(g_coop) / sizeof(g_coop[0]);
 // The same shapes under the reference's loop controls (1024 threads, one contact per thread and
