@@ -2264,7 +2264,10 @@ static CoopVariant g_coop[] = {
     // a sweep)
     {k_s_solve_coop<576, 1, 2, 0, 2>, 576, 1, 2, 0, 0, 0, 2},
     // (reductions without the warp run sums, AGG 1, measured 13.2 against 9.9 us a sweep at 1,024
-    // threads: the L2 serialises reductions to one address, so the run sums pay for themselves)
+    // threads: the L2 serialises reductions to one address, so the run sums pay for themselves;
+    // body B's shares summed over the lanes that share B anywhere in the warp (__match_any_sync),
+    // which saves about 7 of a warp's 32 reductions on the settled pile, measured 11.4 us: the
+    // grouping's shuffles cost more than the reductions they save)
 };
 constexpr int N_COOP = sizeof(g_coop) / sizeof(g_coop[0]);
 // The same shapes under the reference's loop controls (1024 threads, one contact per thread and
