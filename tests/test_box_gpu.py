@@ -182,3 +182,20 @@ def test_stacked_spheres_scene_split_form():
     assert np.isfinite(p32).all() and np.abs(p32[:, :2]).max() < TUBE_W / 2
     assert abs(p64[:, 2].mean() - p32[:, 2].mean()) < 2e-2
     np.testing.assert_allclose(e32.static_state()["quat"], e64.static_state()["quat"], atol=1e-12)
+
+
+def test_box_without_positive_extents_is_refused():
+    from cardillocxx_gb300 import CdxError
+    cfg = scenes.config_for("pile_1k")
+    for ext in ((0.0, 0.2, 0.1), (0.3, -0.2, 0.1), (0.3, float("nan"), 0.1)):
+        s = make_scene([{"pos": (0.0, 0.0, 0.5), "radius": 0.05}],
+                       [{"kind": "box", "pos": (0, 0, 0), "half_extents": ext}])
+        with pytest.raises(CdxError) as e:
+            PhysicsEngine(cfg).load_scene(s)
+        assert e.value.status == 1, ext
+    s = make_scene([{"pos": (0.0, 0.0, 0.5), "radius": 0.05}],
+                   [{"kind": "box", "pos": (0, 0, 0), "half_extents": (0.3, 0.2, 0.1)}])
+    del s["static_half_extents"]
+    with pytest.raises(CdxError) as e:
+        PhysicsEngine(cfg).load_scene(s)
+    assert e.value.status == 1
