@@ -37,6 +37,7 @@ struct SplitState {
     int graph_variant = -1;
     int64_t tuned_at = 0;    // contact count at the last tuning
     int tune_runs = 0;
+    int tune_cut = 0;        // tunings in a row that the solve's convergence cut short
     cudaEvent_t tev[2] = {nullptr, nullptr};
     // batched scenes: one block per scene
     int32_t* scene_order = nullptr;  // scene ids by decreasing body count (device)
@@ -459,15 +460,18 @@ int Engine::step_split() {
         if (!(n > 0 && !loopk && cfg.gpu_autotune && pinned < 0 && n >= 4096 &&
               (double)n >= 1.5 * (double)S->tuned_at))
             return false;
+        // the same count as the tuner's below
+        const int k = maxit >= 1000 ? 40 : 12;
         int sweeps = 0;
         for (int v = 0; v < split_num_variants(); ++v) {
             CoopPlan probe;
             if (split_variant_is_coop(v))
-                sweeps += coop_plan(*this, v, n, &probe) ? 12 : 0;
+                sweeps += coop_plan(*this, v, n, &probe) ? k : 0;
             else if (!split_variant_is_scenes(v))
                 sweeps += 2;
         }
-        return maxit > 2 * sweeps;
+        const int expect = S->last_iters > 0 ? S->last_iters : maxit;
+        return maxit > 2 * sweeps && expect > 2 * sweeps;
     };
     // the per-scene kernel (one block a scene) is a candidate for batches and for a single scene
     // small enough that one block can carry it
@@ -673,17 +677,24 @@ int Engine::step_split() {
         solved = true;
     }
     const int nv = split_num_variants();
-    // sweeps the autotuner spends: two per streaming shape, twelve per feasible cooperative one
+    // sweeps the autotuner spends: two per streaming shape, and per feasible cooperative one a
+    // launch of k0 and one of k1 sweeps (their difference times a sweep); a solve of a thousand
+    // sweeps or more times 32 sweeps of difference instead of 8, where the shapes' per-sweep costs
+    // (a few percent apart) decide its time and 8 sweeps measured them within the noise
+    const int coop_k0 = maxit >= 1000 ? 4 : 2, coop_k1 = maxit >= 1000 ? 36 : 10;
     int tune_sweeps = 0;
     for (int v = 0; v < nv; ++v) {
         CoopPlan probe;
         if (split_variant_is_coop(v))
-            tune_sweeps += (S->nc > 0 && coop_plan(*this, v, S->nc, &probe)) ? 12 : 0;
+            tune_sweeps += (S->nc > 0 && coop_plan(*this, v, S->nc, &probe)) ? coop_k0 + coop_k1 : 0;
         else if (!split_variant_is_scenes(v))
             tune_sweeps += 2;
     }
+    // the trials are the step's first sweeps: a solve expected to end sooner (the previous step's
+    // sweeps, or the cap on a first step) waits for a step that needs enough of them
+    const int expect = S->last_iters > 0 ? S->last_iters : maxit;
     if (!async && !scenes && !loopk && S->nc > 0 && cfg.gpu_autotune && cfg.gpu_sweep_variant < 0 && S->nc >= 4096 &&
-        (double)S->nc >= 1.5 * (double)S->tuned_at && maxit > 2 * tune_sweeps) {
+        (double)S->nc >= 1.5 * (double)S->tuned_at && maxit > 2 * tune_sweeps && expect > 2 * tune_sweeps) {
         // autotune: the first sweeps of this step run with every shape; each is a full sweep of
         // the same math, so the step's result does not depend on which shape ran them
         if (!S->tev[0]) {
@@ -704,7 +715,7 @@ int Engine::step_split() {
                 CoopPlan plan;
                 if (!coop_plan(*this, v, S->nc, &plan)) continue;
                 float ms[2] = {0.f, 0.f};
-                const int ks[2] = {2, 10};
+                const int ks[2] = {coop_k0, coop_k1};
                 for (int r = 0; r < 2; ++r) {
                     cudaEventRecord(S->tev[0], stream);
                     st = launch_coop(*this, sb, gen, v, plan, maxit, (float)cfg.gpu_residual_tol, ks[r], stream);
@@ -731,18 +742,32 @@ int Engine::step_split() {
                 }
                 launches += 2;
             }
+            cudaMemcpyAsync(&S->h_ss->done, &sb.ss->done, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+            if ((st = cuda_check(cudaStreamSynchronize(stream), "autotune"))) return st;
+            solved = S->h_ss->done != 0;
+            // a trial during which the solve met its stop rule ran fewer sweeps than it timed: it
+            // does not count, and the shapes after it were not timed
+            if (solved) break;
             if (t < best_t) {
                 best_t = t;
                 best = v;
             }
-            cudaMemcpyAsync(&S->h_ss->done, &sb.ss->done, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
-            if ((st = cuda_check(cudaStreamSynchronize(stream), "autotune"))) return st;
-            solved = S->h_ss->done != 0;
         }
-        S->variant = best;
-        S->last_variant = best;
-        S->tuned_at = S->nc;
-        ++S->tune_runs;
+        // the solve ended inside the trials (a warm-started step needing few sweeps): keep the
+        // current shape, time them all again on a later step that needs enough sweeps, and after
+        // four such cuts stop trying at this contact count
+        bool all = true;
+        if (solved) {
+            all = ++S->tune_cut >= 4;
+        } else {
+            S->variant = best;
+            S->last_variant = best;
+        }
+        if (all) {
+            S->tuned_at = S->nc;
+            S->tune_cut = 0;
+            ++S->tune_runs;
+        }
     }
     CoopPlan plan;
     const int64_t plan_nc = async ? (int64_t)S->nc + S->nc / 16 + 64 : (int64_t)S->nc;
