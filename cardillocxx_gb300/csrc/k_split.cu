@@ -2295,6 +2295,8 @@ static ScenesVariant g_scenes[] = {
     {k_s_solve_scenes<128, 0>, 128, 0, 0},
     {k_s_solve_scenes<256, 0>, 256, 0, 0},
     {k_s_solve_scenes<256, 1>, 256, 1, 0},
+    // (512 threads a scene: 43.4 against 38.3 ms a step on 4,096 settled scenes at residual 1e-6,
+    // where the largest scenes' sweeps set the step: fewer blocks fit an SM)
 };
 constexpr int N_SCENES = sizeof(g_scenes) / sizeof(g_scenes[0]);
 
