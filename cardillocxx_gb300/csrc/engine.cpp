@@ -274,7 +274,8 @@ int Engine::load_scene(const cdx_scene& s) {
         }
     if (N == 0)
         for (int k = 0; k < 3; ++k) { lo[k] = 0; hi[k] = 1; }
-    const double cell = 2.0 * rmax * 1.0001 + 1e-9;
+    // (a scene without bodies gets a grid of a few cells: nothing is ever sorted into it)
+    const double cell = N > 0 ? 2.0 * rmax * 1.0001 + 1e-9 : 1.0;
     for (int k = 0; k < 3; ++k) {
         const double pad = 0.05 * (hi[k] - lo[k]) + 2 * cell;
         lo[k] -= pad;
@@ -287,13 +288,19 @@ int Engine::load_scene(const cdx_scene& s) {
         g.dim[k] = (int)std::min<double>(std::ceil((hi[k] - lo[k]) / cell) + 1, 1 << 20);
         ncells *= g.dim[k];
     }
-    // keep the dense cell table modest: coarsen cells if needed (still >= 2 rmax, so exact)
+    // keep the dense cell table modest: coarsen cells if needed (still >= 2 rmax, so exact); the
+    // count is formed in double, as a fine grid over a wide box overflows 64-bit integers
     double cs = cell;
-    while (ncells > (int64_t)64 << 20) {
+    double nd = (double)g.dim[0] * (double)g.dim[1] * (double)g.dim[2];
+    while (nd > (double)((int64_t)64 << 20)) {
         cs *= 1.25;
+        nd = 1.0;
+        for (int k = 0; k < 3; ++k) nd *= std::ceil((hi[k] - lo[k]) / cs) + 1.0;
+    }
+    if (cs != cell) {
         ncells = 1;
         for (int k = 0; k < 3; ++k) {
-            g.dim[k] = (int)std::ceil((hi[k] - lo[k]) / cs) + 1;
+            g.dim[k] = (int)(std::ceil((hi[k] - lo[k]) / cs) + 1.0);
             ncells *= g.dim[k];
         }
     }
