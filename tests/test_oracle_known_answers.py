@@ -532,3 +532,17 @@ def test_cylinder_axis_turns_with_the_static(oracle_mod):
     o.step(1)
     assert o.stats()["num_contacts"] == 1
     np.testing.assert_allclose(o.contacts()["normal"][0], [0.0, 1.0, 0.0], atol=1e-12)
+
+
+def test_scene_without_bodies_and_a_lone_sphere(oracle_mod):
+    # nothing to collide: no contacts, no sweeps
+    o = oracle_mod.Oracle(make_scene([], [{"kind": "halfspace", "pos": (0, 0, 0), "dir": (0, 0, 1)}]), cfg())
+    o.step(3)
+    st = o.stats()
+    assert st["num_contacts"] == 0 and st["iterations"] == 0
+    # a sphere with no statics falls freely: after n midpoint steps from rest x = x0 - g h^2 n^2 / 2
+    o = oracle_mod.Oracle(make_scene([{"pos": (0.0, 0.0, 1.0), "radius": 0.1}], []), cfg())
+    n = 7
+    o.step(n)
+    np.testing.assert_allclose(o.state()["pos"][0, 2], 1.0 - G * H * H * n * n / 2, rtol=0, atol=1e-14)
+    np.testing.assert_allclose(o.state()["vel"][0, 2], -G * H * n, rtol=1e-12)
